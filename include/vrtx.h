@@ -1,0 +1,380 @@
+/*
+ * vrtx.h -- C ABI of libvrtx, a GB300-native (sm_103a) implementation of the
+ * VisRTX ANARI device's hot path: BVH traversal over triangles, spheres and
+ * instances, and emission-absorption ray marching through structured-regular
+ * volumes with a 1D transfer function.
+ *
+ * Every entry point is plain C: opaque handles, plain pointers and sizes. No
+ * C++ or torch type crosses this boundary and no exception escapes it; errors
+ * are reported through the status callback given to vrtxNewDevice (the ANARI
+ * convention) and, where a call returns a value, through that value.
+ *
+ * Each declaration names the reference interface it replaces as
+ * file:line within the VisRTX project (devices/rtx/...). Object subtypes,
+ * parameter names, frame channel names and their defaults are the
+ * reference's; data type codes are this library's own (VRTX_*), named after
+ * the ANARI data types they stand for.
+ */
+#ifndef VRTX_H
+#define VRTX_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(_WIN32)
+#define VRTX_API __declspec(dllexport)
+#else
+#define VRTX_API __attribute__((visibility("default")))
+#endif
+
+/* ------------------------------------------------------------------------ */
+/* Handles                                                                  */
+/* ------------------------------------------------------------------------ */
+
+typedef struct VRTXDevice_st *VRTXDevice;
+typedef struct VRTXObject_st *VRTXObject;
+typedef VRTXObject VRTXArray;
+typedef VRTXObject VRTXFrame;
+
+/* ------------------------------------------------------------------------ */
+/* Data types (ANARIDataType stand-ins)                                     */
+/* ------------------------------------------------------------------------ */
+
+typedef enum VRTXDataType {
+  VRTX_UNKNOWN = 0,
+  VRTX_STRING = 1,
+  VRTX_VOID_POINTER = 2,
+  VRTX_BOOL = 3,
+  VRTX_FUNCTION_POINTER = 4, /* frameCompletionCallback */
+  VRTX_MEMORY_DELETER = 5,
+
+  VRTX_OBJECT = 100,
+  VRTX_ARRAY1D = 101,
+  VRTX_ARRAY2D = 102,
+  VRTX_ARRAY3D = 103,
+  VRTX_CAMERA = 104,
+  VRTX_FRAME = 105,
+  VRTX_GEOMETRY = 106,
+  VRTX_GROUP = 107,
+  VRTX_INSTANCE = 108,
+  VRTX_LIGHT = 109,
+  VRTX_MATERIAL = 110,
+  VRTX_RENDERER = 111,
+  VRTX_SURFACE = 112,
+  VRTX_SAMPLER = 113,
+  VRTX_SPATIAL_FIELD = 114,
+  VRTX_VOLUME = 115,
+  VRTX_WORLD = 116,
+
+  VRTX_INT32 = 200,
+  VRTX_INT32_VEC2 = 201,
+  VRTX_UINT32 = 210,
+  VRTX_UINT32_VEC2 = 211,
+  VRTX_UINT32_VEC3 = 212,
+  VRTX_UINT32_VEC4 = 213,
+  VRTX_UINT64 = 214,
+  VRTX_FIXED8 = 220,
+  VRTX_UFIXED8 = 221,
+  VRTX_FIXED16 = 222,
+  VRTX_UFIXED16 = 223,
+  VRTX_FLOAT16 = 230,
+  VRTX_BFLOAT16 = 231,
+  VRTX_FLOAT32 = 240,
+  VRTX_FLOAT32_VEC2 = 241,
+  VRTX_FLOAT32_VEC3 = 242,
+  VRTX_FLOAT32_VEC4 = 243,
+  VRTX_FLOAT32_BOX1 = 244,
+  VRTX_FLOAT32_BOX2 = 245,
+  VRTX_FLOAT32_BOX3 = 246,
+  VRTX_FLOAT32_MAT3x4 = 247, /* ANARI_FLOAT32_MAT4x3: 4 columns of vec3 */
+  VRTX_FLOAT32_MAT4 = 248,
+  VRTX_FLOAT64 = 250,
+  VRTX_FLOAT64_BOX1 = 251,
+  VRTX_UFIXED8_VEC4 = 260,
+  VRTX_UFIXED8_RGBA_SRGB = 261,
+  VRTX_DATA_TYPE = 270 /* a parameter whose value is a VRTXDataType */
+} VRTXDataType;
+
+typedef enum VRTXStatusSeverity {
+  VRTX_SEVERITY_FATAL_ERROR = 0,
+  VRTX_SEVERITY_ERROR = 1,
+  VRTX_SEVERITY_WARNING = 2,
+  VRTX_SEVERITY_PERFORMANCE_WARNING = 3,
+  VRTX_SEVERITY_INFO = 4,
+  VRTX_SEVERITY_DEBUG = 5
+} VRTXStatusSeverity;
+
+typedef enum VRTXWaitMask {
+  VRTX_NO_WAIT = 0,
+  VRTX_WAIT = 1
+} VRTXWaitMask;
+
+/* ANARIStatusCallback: same argument order as the ANARI status callback. */
+typedef void (*VRTXStatusCallback)(const void *userPtr,
+    VRTXDevice device,
+    VRTXObject source,
+    int sourceType,
+    int severity,
+    int code,
+    const char *message);
+
+/* ANARIMemoryDeleter */
+typedef void (*VRTXMemoryDeleter)(const void *userPtr, const void *appMemory);
+
+/* ANARIFrameCompletionCallback */
+typedef void (*VRTXFrameCompletionCallback)(
+    const void *userPtr, VRTXDevice device, VRTXFrame frame);
+
+/* ------------------------------------------------------------------------ */
+/* Library / device                                                         */
+/* ------------------------------------------------------------------------ */
+
+/* Replaces makeVisRTXDevice (VisRTXLibrary.cpp:76-80,
+ * include/anari/ext/visrtx/visrtx.h:49-51). CUDA is initialised lazily on
+ * the first object creation, as VisRTXDevice::initDevice does
+ * (VisRTXDevice.cpp:435-458). Returns NULL only when out of host memory. */
+VRTX_API VRTXDevice vrtxNewDevice(
+    VRTXStatusCallback statusCallback, const void *statusCallbackUserData);
+
+/* Device parameters ("cudaDevice", "statusCallback"); replaces
+ * VisRTXDevice::deviceSetParameter / deviceCommitParameters
+ * (VisRTXDevice.cpp:460-471). */
+VRTX_API void vrtxDeviceSetParameter(
+    VRTXDevice d, const char *name, int type, const void *mem);
+VRTX_API void vrtxDeviceCommitParameters(VRTXDevice d);
+
+/* Releases the device and every object it still owns. */
+VRTX_API void vrtxDeviceRelease(VRTXDevice d);
+
+/* Device properties ("version", "visrtx", "extension"); replaces
+ * VisRTXDevice::deviceGetProperty (VisRTXDevice.cpp:520-552). Returns 1 when
+ * the property was written. */
+VRTX_API int vrtxDeviceGetProperty(VRTXDevice d,
+    const char *name,
+    int type,
+    void *mem,
+    uint64_t size,
+    uint32_t waitMask);
+
+/* 1 when the build has a usable CUDA device, 0 otherwise (after init). */
+VRTX_API int vrtxDeviceIsValid(VRTXDevice d);
+
+/* ------------------------------------------------------------------------ */
+/* Arrays                                                                   */
+/* ------------------------------------------------------------------------ */
+
+/* Replace VisRTXDevice::newArray1D/2D/3D (VisRTXDevice.cpp:131-188) with the
+ * ownership rules of Array.cpp:69-119: appMemory != NULL and deleter == NULL
+ * -> shared; appMemory != NULL and deleter != NULL -> captured;
+ * appMemory == NULL -> managed (fill through vrtxMapArray). appMemory may be
+ * CUDA device memory (NV_ARRAY_CUDA, detected as Array.cpp:38-65 does). */
+VRTX_API VRTXArray vrtxNewArray1D(VRTXDevice d,
+    const void *appMemory,
+    VRTXMemoryDeleter deleter,
+    const void *userData,
+    int elementType,
+    uint64_t numItems1);
+VRTX_API VRTXArray vrtxNewArray2D(VRTXDevice d,
+    const void *appMemory,
+    VRTXMemoryDeleter deleter,
+    const void *userData,
+    int elementType,
+    uint64_t numItems1,
+    uint64_t numItems2);
+VRTX_API VRTXArray vrtxNewArray3D(VRTXDevice d,
+    const void *appMemory,
+    VRTXMemoryDeleter deleter,
+    const void *userData,
+    int elementType,
+    uint64_t numItems1,
+    uint64_t numItems2,
+    uint64_t numItems3);
+
+/* Replace VisRTXDevice::mapArray / unmapArray (VisRTXDevice.cpp:190-200). */
+VRTX_API void *vrtxMapArray(VRTXDevice d, VRTXArray a);
+VRTX_API void vrtxUnmapArray(VRTXDevice d, VRTXArray a);
+
+/* ------------------------------------------------------------------------ */
+/* Object creation (VisRTXDevice.cpp:202-292)                               */
+/* ------------------------------------------------------------------------ */
+
+VRTX_API VRTXObject vrtxNewCamera(VRTXDevice d, const char *subtype);
+VRTX_API VRTXObject vrtxNewGeometry(VRTXDevice d, const char *subtype);
+VRTX_API VRTXObject vrtxNewLight(VRTXDevice d, const char *subtype);
+VRTX_API VRTXObject vrtxNewMaterial(VRTXDevice d, const char *subtype);
+VRTX_API VRTXObject vrtxNewRenderer(VRTXDevice d, const char *subtype);
+VRTX_API VRTXObject vrtxNewSampler(VRTXDevice d, const char *subtype);
+VRTX_API VRTXObject vrtxNewSpatialField(VRTXDevice d, const char *subtype);
+VRTX_API VRTXObject vrtxNewVolume(VRTXDevice d, const char *subtype);
+VRTX_API VRTXObject vrtxNewSurface(VRTXDevice d);
+VRTX_API VRTXObject vrtxNewGroup(VRTXDevice d);
+VRTX_API VRTXObject vrtxNewInstance(VRTXDevice d, const char *subtype);
+VRTX_API VRTXObject vrtxNewWorld(VRTXDevice d);
+VRTX_API VRTXFrame vrtxNewFrame(VRTXDevice d);
+
+/* ------------------------------------------------------------------------ */
+/* Parameters, commit, reference counting (helium::BaseDevice semantics)     */
+/* ------------------------------------------------------------------------ */
+
+/* mem points at the value; for object-typed parameters it points at the
+ * VRTXObject handle, for VRTX_STRING it is the C string itself. */
+VRTX_API void vrtxSetParameter(VRTXDevice d,
+    VRTXObject o,
+    const char *name,
+    int type,
+    const void *mem);
+VRTX_API void vrtxUnsetParameter(VRTXDevice d, VRTXObject o, const char *name);
+VRTX_API void vrtxUnsetAllParameters(VRTXDevice d, VRTXObject o);
+VRTX_API void vrtxCommitParameters(VRTXDevice d, VRTXObject o);
+VRTX_API void vrtxRelease(VRTXDevice d, VRTXObject o);
+VRTX_API void vrtxRetain(VRTXDevice d, VRTXObject o);
+
+/* Object properties: World/Group "bounds" (World.cpp:100-118,
+ * Group.cpp:65-86), Frame "duration"/"numSamples"/"nextFrameReset"
+ * (Frame.cu:163-193), "valid" on any object. Returns 1 when written. */
+VRTX_API int vrtxGetProperty(VRTXDevice d,
+    VRTXObject o,
+    const char *name,
+    int type,
+    void *mem,
+    uint64_t size,
+    uint32_t waitMask);
+
+/* ------------------------------------------------------------------------ */
+/* Frame operations                                                         */
+/* ------------------------------------------------------------------------ */
+
+/* Replaces VisRTXDevice::renderFrame -> Frame::renderFrame
+ * (VisRTXDevice.cpp:360-366, frame/Frame.cu:195-310). Asynchronous on the
+ * device's CUDA stream. */
+VRTX_API void vrtxRenderFrame(VRTXDevice d, VRTXFrame f);
+
+/* Replaces Frame::frameReady (Frame.cu:425-432): 1 when the last render has
+ * finished; with VRTX_WAIT it blocks until then. */
+VRTX_API int vrtxFrameReady(VRTXDevice d, VRTXFrame f, uint32_t waitMask);
+
+/* Replaces Frame::discardFrame (no-op in the reference). */
+VRTX_API void vrtxDiscardFrame(VRTXDevice d, VRTXFrame f);
+
+/* Replaces Frame::map (Frame.cu:312-423). Channels: "channel.color",
+ * "channel.depth", "channel.primitiveId", "channel.objectId",
+ * "channel.instanceId", "channel.albedo", "channel.normal" (host copies) and
+ * the same names with a "CUDA" suffix (device pointers owned by the frame,
+ * valid until the next render or frame change). Unknown or disabled channels
+ * return NULL with width = height = 0 and pixelType = VRTX_UNKNOWN. */
+VRTX_API const void *vrtxMapFrame(VRTXDevice d,
+    VRTXFrame f,
+    const char *channel,
+    uint32_t *width,
+    uint32_t *height,
+    int *pixelType);
+VRTX_API void vrtxUnmapFrame(VRTXDevice d, VRTXFrame f, const char *channel);
+
+/* ------------------------------------------------------------------------ */
+/* Introspection used by tests, the benchmark and the roofline accounting.   */
+/* These have no ANARI counterpart; they expose what the reference keeps     */
+/* inside OptiX (BVH layout, traversal statistics).                          */
+/* ------------------------------------------------------------------------ */
+
+/* Copies the world's acceleration structures for the last render to host
+ * memory so a CPU traversal can count node visits on the same BVH. kind: 0 =
+ * TLAS nodes, 1 = BLAS nodes (all BLASes, concatenated), 2 = BLAS triangle
+ * records, 3 = instance records, 4 = sphere records, 5 = BLAS table. Returns
+ * the number of bytes (call with dst = NULL to query). */
+VRTX_API uint64_t vrtxDebugCopyAccel(
+    VRTXDevice d, VRTXObject world, int kind, void *dst, uint64_t capacity);
+
+/* Milliseconds spent in the last BVH / macrocell-grid build of a world
+ * (host wall clock around the device build, synchronised). */
+VRTX_API float vrtxWorldBuildMilliseconds(VRTXDevice d, VRTXObject world);
+
+/* Device milliseconds of the last frame's integrator kernel alone (CUDA
+ * events on the device stream), and the number of kernels the last
+ * renderFrame launched. */
+VRTX_API float vrtxFrameKernelMilliseconds(VRTXDevice d, VRTXFrame f);
+VRTX_API int vrtxFrameKernelLaunches(VRTXDevice d, VRTXFrame f);
+
+/* The CUDA stream (cudaStream_t) the device renders on. */
+VRTX_API void *vrtxDeviceStream(VRTXDevice d);
+
+/* ------------------------------------------------------------------------ */
+/* Differentiable volume marcher. No reference counterpart: VisRTX has no    */
+/* gradient path; this is the emission-absorption model of its scivis        */
+/* marcher (devices/rtx/gpu/volumeIntegration.h:64-103) made differentiable. */
+/*                                                                          */
+/* Model, per pixel ray in voxel space (voxel i's centre at coordinate i,   */
+/* box [0, dims-1]): samples at t_k = t_in + (k + 0.5) * step inside the box; */
+/* s_k = trilinear(density, p_k); x = clamp((s-lo)/(hi-lo), 0, 1)*(N-1);     */
+/* (rgb, A) = lerp(tf[floor x], tf[floor x + 1]); alpha = min(A * scale,    */
+/* 0.999); sigma_k = (step/unit) * log(1 - alpha) (<= 0); log T_{k+1} =      */
+/* log T_k + sigma_k (Kahan-compensated); pixel = sum T_k (1 - e^sigma_k)   */
+/* rgb_k + T_end * background. Marching stops once T < 1e-3.                */
+/*                                                                          */
+/* All pointers are CUDA device pointers; work is queued on `stream` (a     */
+/* cudaStream_t, NULL = legacy default stream). One launch covers every    */
+/* view: views are cut into tiles that persistent blocks pull from a queue. */
+/* ------------------------------------------------------------------------ */
+
+typedef struct VRTXDMVolume {
+  const void *density;   /* dims[0] fastest; fp32, fp16 or bf16 */
+  int densityType;       /* VRTX_FLOAT32, VRTX_FLOAT16 or VRTX_BFLOAT16 */
+  int dims[3];
+  const float *tf;       /* tfSize x RGBA, fp32 */
+  int tfSize;            /* 2..256 */
+  float opacityScale;    /* multiplies TF alpha */
+  float step;            /* sample spacing, voxels */
+  float unitDistance;    /* voxels */
+  float valueLo, valueHi;/* density range mapped onto the TF */
+  float *gradDensity;    /* fp32, same dims; backward only, may be NULL */
+  float *gradTf;         /* fp32, tfSize x 4; backward only, may be NULL */
+  float *gradOpacityScale; /* one fp32; backward only, may be NULL */
+} VRTXDMVolume;
+
+typedef struct VRTXDMView {
+  int volume;            /* index into the volume array */
+  int width, height;
+  float eye[3];          /* camera position, voxel space */
+  float d00[3], du[3], dv[3]; /* ray dir = normalize(d00 + (x+.5) du + (y+.5) dv) */
+  float background[3];
+  int64_t pixelOffset;   /* first pixel of this view in image/state */
+} VRTXDMView;
+
+/* Forward. image: 3 floats per pixel. state: 2 floats per pixel (final
+ * log-transmittance, and the sample count stored as an int32 bit pattern);
+ * the backward pass reads it. tileW x tileH pixels per work item
+ * (tileW * tileH a multiple of 32, at most 1024). Returns 0, or a negative
+ * code after reporting the error through the device's status callback. */
+VRTX_API int vrtxDMForward(VRTXDevice d,
+    const VRTXDMVolume *volumes,
+    int numVolumes,
+    const VRTXDMView *views,
+    int numViews,
+    float *image,
+    float *state,
+    int tileW,
+    int tileH,
+    void *stream);
+
+/* Backward: reverse-order march from each pixel's stored end state;
+ * accumulates (adds) into the gradient buffers named in volumes[]. */
+VRTX_API int vrtxDMBackward(VRTXDevice d,
+    const VRTXDMVolume *volumes,
+    int numVolumes,
+    const VRTXDMView *views,
+    int numViews,
+    const float *image,
+    const float *state,
+    const float *gradImage,
+    int tileW,
+    int tileH,
+    void *stream);
+
+#ifdef __cplusplus
+} /* extern "C" */
+#endif
+
+#endif /* VRTX_H */

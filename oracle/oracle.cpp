@@ -1,0 +1,1936 @@
+// CPU oracle for the VisRTX hot path -- TEST INFRASTRUCTURE ONLY (see
+// oracle.h). Plain C++17, built with -ffp-contract=off so x86 and Arm hosts
+// produce the same bits. Each function names the reference code it
+// restates (paths within the VisRTX project).
+#include "oracle.h"
+
+#include <algorithm>
+#include <atomic>
+#include <cfloat>
+#include <cmath>
+#include <cstring>
+#include <thread>
+#include <vector>
+
+namespace {
+
+// ---------------------------------------------------------------------------
+// small vector math (float; the reference computes in fp32 via glm)
+// ---------------------------------------------------------------------------
+
+struct V3
+{
+  float x, y, z;
+};
+inline V3 v3(float x, float y, float z)
+{
+  return V3{x, y, z};
+}
+inline V3 operator+(V3 a, V3 b)
+{
+  return {a.x + b.x, a.y + b.y, a.z + b.z};
+}
+inline V3 operator-(V3 a, V3 b)
+{
+  return {a.x - b.x, a.y - b.y, a.z - b.z};
+}
+inline V3 operator-(V3 a)
+{
+  return {-a.x, -a.y, -a.z};
+}
+inline V3 operator*(V3 a, float s)
+{
+  return {a.x * s, a.y * s, a.z * s};
+}
+inline V3 operator*(float s, V3 a)
+{
+  return {a.x * s, a.y * s, a.z * s};
+}
+inline V3 operator*(V3 a, V3 b)
+{
+  return {a.x * b.x, a.y * b.y, a.z * b.z};
+}
+inline V3 operator/(V3 a, float s)
+{
+  return {a.x / s, a.y / s, a.z / s};
+}
+inline float dot(V3 a, V3 b)
+{
+  return a.x * b.x + a.y * b.y + a.z * b.z;
+}
+inline V3 cross(V3 a, V3 b)
+{
+  return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+inline V3 normalize(V3 v)
+{
+  const float inv = 1.f / std::sqrt(dot(v, v));
+  return v * inv;
+}
+inline float comp(V3 v, int i)
+{
+  return i == 0 ? v.x : (i == 1 ? v.y : v.z);
+}
+inline V3 ld3(const float *p, size_t i)
+{
+  return {p[3 * i], p[3 * i + 1], p[3 * i + 2]};
+}
+inline float cmax(V3 v)
+{
+  return std::max(v.x, std::max(v.y, v.z));
+}
+inline V3 vabs(V3 v)
+{
+  return {std::fabs(v.x), std::fabs(v.y), std::fabs(v.z)};
+}
+
+struct X34
+{
+  float m[12];
+};
+inline V3 xPoint(const X34 &t, V3 p)
+{
+  const float *m = t.m;
+  return {m[0] * p.x + m[1] * p.y + m[2] * p.z + m[3],
+      m[4] * p.x + m[5] * p.y + m[6] * p.z + m[7],
+      m[8] * p.x + m[9] * p.y + m[10] * p.z + m[11]};
+}
+inline V3 xVec(const X34 &t, V3 p)
+{
+  const float *m = t.m;
+  return {m[0] * p.x + m[1] * p.y + m[2] * p.z,
+      m[4] * p.x + m[5] * p.y + m[6] * p.z,
+      m[8] * p.x + m[9] * p.y + m[10] * p.z};
+}
+inline V3 xNormalT(const X34 &w2o, V3 n)
+{
+  const float *m = w2o.m;
+  return {m[0] * n.x + m[4] * n.y + m[8] * n.z,
+      m[1] * n.x + m[5] * n.y + m[9] * n.z,
+      m[2] * n.x + m[6] * n.y + m[10] * n.z};
+}
+
+// Affine inverse in double, rounded to float.
+X34 invert(const float *m)
+{
+  const double a = m[0], b = m[1], c = m[2], d = m[4], e = m[5], f = m[6],
+               g = m[8], h = m[9], k = m[10];
+  const double A = e * k - f * h, B = -(d * k - f * g), C = d * h - e * g;
+  double det = a * A + b * B + c * C;
+  if (det == 0.0)
+    det = 1e-30;
+  const double inv[3][3] = {{A / det, -(b * k - c * h) / det, (b * f - c * e) / det},
+      {B / det, (a * k - c * g) / det, -(a * f - c * d) / det},
+      {C / det, -(a * h - b * g) / det, (a * e - b * d) / det}};
+  const double t[3] = {m[3], m[7], m[11]};
+  X34 o;
+  for (int r = 0; r < 3; r++) {
+    for (int cc = 0; cc < 3; cc++)
+      o.m[r * 4 + cc] = (float)inv[r][cc];
+    o.m[r * 4 + 3] =
+        (float)(-(inv[r][0] * t[0] + inv[r][1] * t[1] + inv[r][2] * t[2]));
+  }
+  return o;
+}
+
+// ---------------------------------------------------------------------------
+// Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11) and the curand-style
+// stream the reference draws from (gpu/createScreenSample.h:58,
+// cameraCreateRay.h:76, volumeIntegration.h:83,120, gpu_util.h:199).
+// ---------------------------------------------------------------------------
+
+const uint32_t PH_M0 = 0xD2511F53u, PH_M1 = 0xCD9E8D57u;
+const uint32_t PH_W0 = 0x9E3779B9u, PH_W1 = 0xBB67AE85u;
+
+void philox(const uint32_t in[4], const uint32_t key[2], uint32_t out[4])
+{
+  uint32_t c0 = in[0], c1 = in[1], c2 = in[2], c3 = in[3];
+  uint32_t k0 = key[0], k1 = key[1];
+  for (int r = 0; r < 10; r++) {
+    if (r > 0) {
+      k0 += PH_W0;
+      k1 += PH_W1;
+    }
+    const uint64_t p0 = (uint64_t)PH_M0 * c0;
+    const uint64_t p1 = (uint64_t)PH_M1 * c2;
+    const uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0;
+    const uint32_t hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
+    c0 = hi1 ^ c1 ^ k0;
+    c1 = lo1;
+    c2 = hi0 ^ c3 ^ k1;
+    c3 = lo0;
+  }
+  out[0] = c0;
+  out[1] = c1;
+  out[2] = c2;
+  out[3] = c3;
+}
+
+// Stream state: a 128-bit counter (word 0 least significant), the 64-bit
+// seed as key, the current 4-word block and the next word's index in it.
+// init(seed, subsequence, offset): the subsequence selects the counter's
+// upper 64 bits, the offset skips `offset` words of the stream.
+struct Stream
+{
+  uint32_t ctr[4];
+  uint32_t key[2];
+  uint32_t blk[4];
+  int idx;
+
+  void add(uint64_t n)
+  {
+    uint64_t lo = (uint64_t)ctr[0] | ((uint64_t)ctr[1] << 32);
+    const uint64_t nlo = lo + n;
+    const uint64_t carry = nlo < lo ? 1 : 0;
+    ctr[0] = (uint32_t)nlo;
+    ctr[1] = (uint32_t)(nlo >> 32);
+    uint64_t hi = (uint64_t)ctr[2] | ((uint64_t)ctr[3] << 32);
+    hi += carry;
+    ctr[2] = (uint32_t)hi;
+    ctr[3] = (uint32_t)(hi >> 32);
+  }
+  void addHi(uint64_t n)
+  {
+    uint64_t hi = (uint64_t)ctr[2] | ((uint64_t)ctr[3] << 32);
+    hi += n;
+    ctr[2] = (uint32_t)hi;
+    ctr[3] = (uint32_t)(hi >> 32);
+  }
+  void init(uint64_t seed, uint64_t subsequence, uint64_t offset)
+  {
+    ctr[0] = ctr[1] = ctr[2] = ctr[3] = 0;
+    key[0] = (uint32_t)seed;
+    key[1] = (uint32_t)(seed >> 32);
+    idx = 0;
+    addHi(subsequence);
+    idx += (int)(offset & 3);
+    add(offset >> 2);
+    philox(ctr, key, blk);
+  }
+  uint32_t next()
+  {
+    const uint32_t r = blk[idx++];
+    if (idx == 4) {
+      add(1);
+      philox(ctr, key, blk);
+      idx = 0;
+    }
+    return r;
+  }
+  void next4(uint32_t r[4])
+  {
+    uint32_t cur[4];
+    std::memcpy(cur, blk, sizeof(cur));
+    add(1);
+    philox(ctr, key, blk);
+    for (int i = 0; i < 4; i++) {
+      const int j = idx + i;
+      r[i] = j < 4 ? cur[j] : blk[j - 4];
+    }
+  }
+};
+
+// (x + 1/2) * 2^-32, evaluated as the float expression x * 2^-32 + 2^-33
+inline float u01(uint32_t x)
+{
+  const float inv = 2.3283064365386963e-10f;
+  return (float)x * inv + inv * 0.5f;
+}
+
+inline float uniform(Stream &s)
+{
+  return u01(s.next());
+}
+inline void uniform4(Stream &s, float r[4])
+{
+  uint32_t v[4];
+  s.next4(v);
+  for (int i = 0; i < 4; i++)
+    r[i] = u01(v[i]);
+}
+
+// ---------------------------------------------------------------------------
+// texture filtering (parity mode): weights with 8 fractional bits
+// ---------------------------------------------------------------------------
+
+inline float quantW(float a, int round)
+{
+  return round ? std::nearbyint(a * 256.f) * (1.f / 256.f)
+               : std::floor(a * 256.f) * (1.f / 256.f);
+}
+
+inline void axisTap(float coord, int n, int round, int &i0, int &i1, float &w)
+{
+  const float x = coord * (float)n - 0.5f;
+  const float fl = std::floor(x);
+  w = quantW(x - fl, round);
+  const int i = (int)fl;
+  i0 = std::min(std::max(i, 0), n - 1);
+  i1 = std::min(std::max(i + 1, 0), n - 1);
+}
+
+float tex3dLinear(const float *v, const int d[3], float cx, float cy, float cz, int round)
+{
+  int x0, x1, y0, y1, z0, z1;
+  float a, b, c;
+  axisTap(cx, d[0], round, x0, x1, a);
+  axisTap(cy, d[1], round, y0, y1, b);
+  axisTap(cz, d[2], round, z0, z1, c);
+  auto at = [&](int x, int y, int z) {
+    return v[((size_t)z * d[1] + y) * d[0] + x];
+  };
+  const float c00 = (1.f - a) * at(x0, y0, z0) + a * at(x1, y0, z0);
+  const float c10 = (1.f - a) * at(x0, y1, z0) + a * at(x1, y1, z0);
+  const float c01 = (1.f - a) * at(x0, y0, z1) + a * at(x1, y0, z1);
+  const float c11 = (1.f - a) * at(x0, y1, z1) + a * at(x1, y1, z1);
+  const float c0 = (1.f - b) * c00 + b * c10;
+  const float c1 = (1.f - b) * c01 + b * c11;
+  return (1.f - c) * c0 + c * c1;
+}
+
+float tex3dPoint(const float *v, const int d[3], float cx, float cy, float cz)
+{
+  auto idx = [](float c, int n) {
+    return std::min(std::max((int)std::floor(c * (float)n), 0), n - 1);
+  };
+  return v[((size_t)idx(cz, d[2]) * d[1] + idx(cy, d[1])) * d[0] + idx(cx, d[0])];
+}
+
+// exact (FP64) trilinear at the same texel convention
+double tex3dExact(const float *v, const int d[3], double cx, double cy, double cz)
+{
+  int i0[3], i1[3];
+  double w[3];
+  const double c[3] = {cx, cy, cz};
+  for (int k = 0; k < 3; k++) {
+    const double x = c[k] * d[k] - 0.5;
+    const double fl = std::floor(x);
+    w[k] = x - fl;
+    i0[k] = std::min(std::max((int)fl, 0), d[k] - 1);
+    i1[k] = std::min(std::max((int)fl + 1, 0), d[k] - 1);
+  }
+  double s = 0.0;
+  for (int q = 0; q < 8; q++) {
+    const int ix = (q & 1) ? i1[0] : i0[0], iy = (q & 2) ? i1[1] : i0[1],
+              iz = (q & 4) ? i1[2] : i0[2];
+    const double ww = ((q & 1) ? w[0] : 1 - w[0]) * ((q & 2) ? w[1] : 1 - w[1])
+        * ((q & 4) ? w[2] : 1 - w[2]);
+    s += ww * v[((size_t)iz * d[1] + iy) * d[0] + ix];
+  }
+  return s;
+}
+
+void tex1dLinear(const float *t, int n, int comps, float coord, int round, float *out)
+{
+  int i0, i1;
+  float a;
+  axisTap(coord, n, round, i0, i1, a);
+  for (int c = 0; c < comps; c++)
+    out[c] = (1.f - a) * t[i0 * comps + c] + a * t[i1 * comps + c];
+}
+
+void tex1dExact(const float *t, int n, double coord, double *out)
+{
+  const double x = coord * n - 0.5;
+  const double fl = std::floor(x);
+  const double a = x - fl;
+  const int i0 = std::min(std::max((int)fl, 0), n - 1);
+  const int i1 = std::min(std::max((int)fl + 1, 0), n - 1);
+  for (int c = 0; c < 4; c++)
+    out[c] = (1 - a) * t[i0 * 4 + c] + a * t[i1 * 4 + c];
+}
+
+// ---------------------------------------------------------------------------
+// oracle BVH: binned SAH binary tree per instance, object space
+// ---------------------------------------------------------------------------
+
+struct Box
+{
+  V3 lo{FLT_MAX, FLT_MAX, FLT_MAX}, hi{-FLT_MAX, -FLT_MAX, -FLT_MAX};
+  void ext(V3 p)
+  {
+    lo = {std::min(lo.x, p.x), std::min(lo.y, p.y), std::min(lo.z, p.z)};
+    hi = {std::max(hi.x, p.x), std::max(hi.y, p.y), std::max(hi.z, p.z)};
+  }
+  void ext(const Box &b)
+  {
+    ext(b.lo);
+    ext(b.hi);
+  }
+  float area() const
+  {
+    const V3 d = hi - lo;
+    if (d.x < 0)
+      return 0.f;
+    return 2.f * (d.x * d.y + d.y * d.z + d.z * d.x);
+  }
+};
+
+struct Prim
+{
+  int surface; // index into scene surfaces
+  uint32_t prim;
+};
+
+struct BNode
+{
+  Box box;
+  int left; // internal: child index; leaf: first prim
+  int count; // 0 = internal
+};
+
+struct InstBVH
+{
+  std::vector<BNode> nodes;
+  std::vector<Prim> prims;
+};
+
+struct SceneCtx
+{
+  const OrcScene *sc;
+  std::vector<InstBVH> unique; // one per distinct surface range
+  std::vector<const InstBVH *> bvh; // per instance
+  std::vector<X34> w2o, o2w;
+  std::vector<Box> worldBox;
+  bool allOpaque = true;
+};
+
+void triVerts(const OrcSurface &s, uint32_t p, V3 &a, V3 &b, V3 &c)
+{
+  uint32_t i0, i1, i2;
+  if (s.indices) {
+    i0 = s.indices[3 * p];
+    i1 = s.indices[3 * p + 1];
+    i2 = s.indices[3 * p + 2];
+  } else {
+    i0 = 3 * p;
+    i1 = i0 + 1;
+    i2 = i0 + 2;
+  }
+  a = ld3(s.vertices, i0);
+  b = ld3(s.vertices, i1);
+  c = ld3(s.vertices, i2);
+}
+
+void sphereOf(const OrcSurface &s, uint32_t p, V3 &c, float &r)
+{
+  const uint32_t i = s.indices ? s.indices[p] : p;
+  c = ld3(s.vertices, i);
+  r = s.radii ? s.radii[i] : s.radius;
+}
+
+Box primBox(const OrcScene *sc, const Prim &pr)
+{
+  const OrcSurface &s = sc->surfaces[pr.surface];
+  Box b;
+  if (s.type == 0) {
+    V3 a, bb, c;
+    triVerts(s, pr.prim, a, bb, c);
+    b.ext(a);
+    b.ext(bb);
+    b.ext(c);
+  } else {
+    V3 c;
+    float r;
+    sphereOf(s, pr.prim, c, r);
+    b.ext(c - v3(r, r, r));
+    b.ext(c + v3(r, r, r));
+  }
+  return b;
+}
+
+void buildBVH(const OrcScene *sc, InstBVH &b)
+{
+  const int n = (int)b.prims.size();
+  if (n == 0)
+    return;
+  std::vector<Box> boxes(n);
+  std::vector<V3> cent(n);
+  for (int i = 0; i < n; i++) {
+    boxes[i] = primBox(sc, b.prims[i]);
+    cent[i] = (boxes[i].lo + boxes[i].hi) * 0.5f;
+  }
+  std::vector<int> idx(n);
+  for (int i = 0; i < n; i++)
+    idx[i] = i;
+  struct Task
+  {
+    int node, begin, end;
+  };
+  b.nodes.reserve(2 * n);
+  b.nodes.push_back(BNode{});
+  std::vector<Task> st{{0, 0, n}};
+  const int NB = 16;
+  while (!st.empty()) {
+    Task t = st.back();
+    st.pop_back();
+    Box bb, cb;
+    for (int i = t.begin; i < t.end; i++) {
+      bb.ext(boxes[idx[i]]);
+      cb.ext(cent[idx[i]]);
+    }
+    BNode &nd = b.nodes[t.node];
+    nd.box = bb;
+    const int cnt = t.end - t.begin;
+    if (cnt <= 4) {
+      nd.left = t.begin;
+      nd.count = cnt;
+      continue;
+    }
+    int bestAxis = -1, bestBin = -1;
+    float bestCost = FLT_MAX;
+    for (int ax = 0; ax < 3; ax++) {
+      const float lo = comp(cb.lo, ax), hi = comp(cb.hi, ax);
+      if (!(hi > lo))
+        continue;
+      Box bins[NB];
+      int counts[NB] = {0};
+      const float sc2 = NB / (hi - lo);
+      for (int i = t.begin; i < t.end; i++) {
+        int k = (int)((comp(cent[idx[i]], ax) - lo) * sc2);
+        k = std::min(std::max(k, 0), NB - 1);
+        bins[k].ext(boxes[idx[i]]);
+        counts[k]++;
+      }
+      float la[NB], ra[NB];
+      int lc[NB], rc[NB];
+      Box acc;
+      int c = 0;
+      for (int k = 0; k < NB; k++) {
+        acc.ext(bins[k]);
+        c += counts[k];
+        la[k] = acc.area();
+        lc[k] = c;
+      }
+      acc = Box();
+      c = 0;
+      for (int k = NB - 1; k >= 0; k--) {
+        acc.ext(bins[k]);
+        c += counts[k];
+        ra[k] = acc.area();
+        rc[k] = c;
+      }
+      for (int k = 0; k < NB - 1; k++) {
+        if (lc[k] == 0 || rc[k + 1] == 0)
+          continue;
+        const float cost = la[k] * lc[k] + ra[k + 1] * rc[k + 1];
+        if (cost < bestCost) {
+          bestCost = cost;
+          bestAxis = ax;
+          bestBin = k;
+        }
+      }
+    }
+    int mid;
+    if (bestAxis < 0) {
+      mid = (t.begin + t.end) / 2;
+    } else {
+      const float lo = comp(cb.lo, bestAxis), hi = comp(cb.hi, bestAxis);
+      const float sc2 = NB / (hi - lo);
+      auto it = std::partition(idx.begin() + t.begin, idx.begin() + t.end, [&](int i) {
+        int k = (int)((comp(cent[i], bestAxis) - lo) * sc2);
+        k = std::min(std::max(k, 0), NB - 1);
+        return k <= bestBin;
+      });
+      mid = (int)(it - idx.begin());
+      if (mid == t.begin || mid == t.end)
+        mid = (t.begin + t.end) / 2;
+    }
+    const int l = (int)b.nodes.size();
+    b.nodes.push_back(BNode{});
+    b.nodes.push_back(BNode{});
+    b.nodes[t.node].left = l;
+    b.nodes[t.node].count = 0;
+    st.push_back({l + 1, mid, t.end});
+    st.push_back({l, t.begin, mid});
+  }
+  std::vector<Prim> sorted(n);
+  for (int i = 0; i < n; i++)
+    sorted[i] = b.prims[idx[i]];
+  b.prims.swap(sorted);
+}
+
+// ---------------------------------------------------------------------------
+// ray/primitive tests
+// ---------------------------------------------------------------------------
+
+struct RayPre
+{
+  V3 o, d, inv;
+  int kx, ky, kz;
+  float Sx, Sy, Sz;
+};
+
+RayPre prep(V3 o, V3 d)
+{
+  RayPre r;
+  r.o = o;
+  r.d = d;
+  r.inv = v3(1.f / d.x, 1.f / d.y, 1.f / d.z);
+  const float ax = std::fabs(d.x), ay = std::fabs(d.y), az = std::fabs(d.z);
+  int kz = 0;
+  if (ay > ax)
+    kz = 1;
+  if (az > std::max(ax, ay))
+    kz = 2;
+  int kx = (kz + 1) % 3, ky = (kx + 1) % 3;
+  if (comp(d, kz) < 0.f)
+    std::swap(kx, ky);
+  r.kx = kx;
+  r.ky = ky;
+  r.kz = kz;
+  r.Sx = comp(d, kx) / comp(d, kz);
+  r.Sy = comp(d, ky) / comp(d, kz);
+  r.Sz = 1.f / comp(d, kz);
+  return r;
+}
+
+// Watertight ray/triangle intersection (Woop, Benthin, Wald, JCGT 2013),
+// standing in for OptiX's built-in triangle test. u, v are the weights of
+// v1 and v2 (OptiX barycentrics, populateHit.h:144-148); front face when the
+// vertices wind counter-clockwise seen from the ray origin.
+bool hitTriangle(const RayPre &r, V3 a, V3 b, V3 c, float tmin, float tmax,
+    float &t, float &u, float &v, bool &front)
+{
+  const V3 A = a - r.o, B = b - r.o, C = c - r.o;
+  const float Ax = comp(A, r.kx) - r.Sx * comp(A, r.kz);
+  const float Ay = comp(A, r.ky) - r.Sy * comp(A, r.kz);
+  const float Bx = comp(B, r.kx) - r.Sx * comp(B, r.kz);
+  const float By = comp(B, r.ky) - r.Sy * comp(B, r.kz);
+  const float Cx = comp(C, r.kx) - r.Sx * comp(C, r.kz);
+  const float Cy = comp(C, r.ky) - r.Sy * comp(C, r.kz);
+  float U = Cx * By - Cy * Bx;
+  float V = Ax * Cy - Ay * Cx;
+  float W = Bx * Ay - By * Ax;
+  if (U == 0.f || V == 0.f || W == 0.f) {
+    U = (float)((double)Cx * By - (double)Cy * Bx);
+    V = (float)((double)Ax * Cy - (double)Ay * Cx);
+    W = (float)((double)Bx * Ay - (double)By * Ax);
+  }
+  if ((U < 0.f || V < 0.f || W < 0.f) && (U > 0.f || V > 0.f || W > 0.f))
+    return false;
+  const float det = U + V + W;
+  if (det == 0.f)
+    return false;
+  const float T = U * (r.Sz * comp(A, r.kz)) + V * (r.Sz * comp(B, r.kz))
+      + W * (r.Sz * comp(C, r.kz));
+  const float rcp = 1.f / det;
+  const float tt = T * rcp;
+  if (!(tt >= tmin && tt < tmax))
+    return false;
+  t = tt;
+  u = V * rcp;
+  v = W * rcp;
+  front = dot(r.d, cross(b - a, c - a)) < 0.f;
+  return true;
+}
+
+// intersectSphere (scene/Intersectors_ptx.cu:74-99): object space, non-unit
+// direction, near root only; OptiX drops t outside the ray interval.
+bool hitSphere(const RayPre &r, V3 center, float radius, float tmin, float tmax, float &t)
+{
+  const V3 d = r.d;
+  const float rd2 = 1.f / dot(d, d);
+  const V3 CO = center - r.o;
+  const float projCO = dot(CO, d) * rd2;
+  const V3 perp = CO - projCO * d;
+  const float l2 = dot(perp, perp);
+  const float r2 = radius * radius;
+  if (l2 > r2)
+    return false;
+  const float td = std::sqrt((r2 - l2) * rd2);
+  const float tt = projCO - td;
+  if (!(tt >= tmin && tt < tmax))
+    return false;
+  t = tt;
+  return true;
+}
+
+bool hitBox(const Box &b, const RayPre &r, float tmin, float tmax)
+{
+  float t0 = tmin, t1 = tmax;
+  for (int a = 0; a < 3; a++) {
+    const float inv = comp(r.inv, a), o = comp(r.o, a);
+    float tn = (comp(b.lo, a) - o) * inv, tf = (comp(b.hi, a) - o) * inv;
+    if (tn > tf)
+      std::swap(tn, tf);
+    if (!(tn <= tf))
+      continue; // NaN from 0 * inf on a degenerate axis: keep
+    t0 = std::max(t0, tn);
+    t1 = std::min(t1, tf * 1.0000004f);
+  }
+  return t0 <= t1;
+}
+
+struct HitRec
+{
+  float t, u, v;
+  int inst;
+  int surface;
+  uint32_t prim;
+  bool front;
+};
+
+float surfOpacity(const OrcSurface &s)
+{
+  if (s.alphaMode == 0)
+    return 1.f;
+  if (s.alphaMode == 1)
+    return s.opacity;
+  return s.opacity < s.cutoff ? 0.f : 1.f;
+}
+
+// MODE 0 closest hit (cull per flags); MODE 1 any-hit opacity accumulation
+// (DirectLight_ptx.cu:233-256, AmbientOcclusion_ptx.cu:53-69).
+template <int MODE>
+bool trace(const SceneCtx &S, V3 org, V3 dir, float tmin, float tmax, bool cullRay,
+    bool geomCull, HitRec &hit, float &opacity)
+{
+  bool found = false;
+  opacity = 0.f;
+  const RayPre wr = prep(org, dir);
+  for (int ii = 0; ii < S.sc->numInstances; ii++) {
+    if (!hitBox(S.worldBox[ii], wr, tmin, tmax))
+      continue;
+    const InstBVH &B = *S.bvh[ii];
+    if (B.nodes.empty())
+      continue;
+    const RayPre r = prep(xPoint(S.w2o[ii], org), xVec(S.w2o[ii], dir));
+    int stack[128];
+    int sp = 0;
+    stack[sp++] = 0;
+    while (sp) {
+      const BNode &n = B.nodes[stack[--sp]];
+      if (!hitBox(n.box, r, tmin, tmax))
+        continue;
+      if (n.count == 0) {
+        stack[sp++] = n.left + 1;
+        stack[sp++] = n.left;
+        continue;
+      }
+      for (int k = 0; k < n.count; k++) {
+        const Prim &p = B.prims[n.left + k];
+        const OrcSurface &s = S.sc->surfaces[p.surface];
+        float t, u = 0.f, v = 0.f;
+        bool front = false, ok;
+        if (s.type == 0) {
+          V3 a, b, c;
+          triVerts(s, p.prim, a, b, c);
+          ok = hitTriangle(r, a, b, c, tmin, tmax, t, u, v, front);
+          if (ok && MODE == 0 && !front && (cullRay || (geomCull && s.cullBackfaces)))
+            ok = false;
+        } else {
+          V3 c;
+          float rad;
+          sphereOf(s, p.prim, c, rad);
+          ok = hitSphere(r, c, rad, tmin, tmax, t);
+        }
+        if (!ok)
+          continue;
+        if (MODE == 0) {
+          tmax = t;
+          hit = HitRec{t, u, v, ii, p.surface, p.prim, front};
+          found = true;
+        } else {
+          opacity += surfOpacity(s) * (1.f - opacity);
+          if (opacity >= 0.99f)
+            return true;
+        }
+      }
+    }
+  }
+  return found;
+}
+
+// ---------------------------------------------------------------------------
+// integrators
+// ---------------------------------------------------------------------------
+
+struct Ray
+{
+  V3 org, dir;
+  float tmin, tmax;
+};
+
+struct CamPre
+{
+  int type;
+  float region[4];
+  V3 pos, dir, d00, du, dv, p00, pdu, pdv;
+  float aperture, aspect;
+};
+
+// Camera::readBaseParameters + Perspective/Orthographic::commitParameters
+// (camera/Camera.cpp:68-76, Perspective.cpp:40-72, Orthographic.cpp:38-52)
+CamPre camSetup(const OrcCamera &c)
+{
+  CamPre p{};
+  p.type = c.type;
+  for (int i = 0; i < 4; i++)
+    p.region[i] = c.imageRegion[i];
+  p.pos = ld3(c.position, 0);
+  p.dir = normalize(ld3(c.direction, 0));
+  const V3 up = normalize(ld3(c.up, 0));
+  if (c.type == 1) {
+    const float sx = c.height * c.aspect, sy = c.height;
+    p.pdu = normalize(cross(p.dir, up)) * sx;
+    p.pdv = normalize(cross(p.pdu, p.dir)) * sy;
+    p.p00 = p.pos - 0.5f * p.pdu - 0.5f * p.pdv;
+  } else {
+    const float ipy = 2.f * std::tan(0.5f * c.fovy);
+    const float ipx = ipy * c.aspect;
+    V3 du = normalize(cross(p.dir, up)) * ipx;
+    V3 dv = normalize(cross(du, p.dir)) * ipy;
+    V3 d00 = p.dir - .5f * du - .5f * dv;
+    const float ap = c.apertureRadius / (ipx * c.focusDistance);
+    if (ap > 0.f) {
+      du = du * c.focusDistance;
+      dv = dv * c.focusDistance;
+      d00 = d00 * c.focusDistance;
+    }
+    p.du = du;
+    p.dv = dv;
+    p.d00 = d00;
+    p.aperture = ap;
+    p.aspect = c.aspect;
+  }
+  return p;
+}
+
+inline float mixf(float a, float b, float t)
+{
+  return a * (1.f - t) + b * t;
+}
+
+// makePrimaryRay + cameraCreateRay (gpu/cameraCreateRay.h:38-81)
+Ray primaryRay(const CamPre &c, Stream &rs, int px, int py, float invW, float invH,
+    bool centerPixel)
+{
+  float r[4];
+  uniform4(rs, r);
+  const float sx0 = (centerPixel ? (float)px : (float)px + r[0]) * invW;
+  const float sy0 = (centerPixel ? (float)py : (float)py + r[1]) * invH;
+  const float sx = mixf(c.region[0], c.region[2], sx0);
+  const float sy = mixf(c.region[1], c.region[3], sy0);
+  Ray ray;
+  ray.tmin = 0.f;
+  ray.tmax = FLT_MAX;
+  if (c.type == 0) {
+    ray.org = c.pos;
+    V3 d = c.d00 + sx * c.du + sy * c.dv;
+    if (c.aperture > 0.f) {
+      const float rr = std::sqrt(r[2]) * c.aperture;
+      const float phi = 2.f * (float)M_PI * r[3];
+      const V3 lp = (rr * std::cos(phi)) * c.du + ((rr * std::sin(phi)) * c.aspect) * c.dv;
+      ray.org = ray.org + lp;
+      d = d - lp;
+    }
+    ray.dir = normalize(d);
+  } else {
+    ray.dir = c.dir;
+    ray.org = c.p00 + sx * c.pdu + sy * c.pdv;
+  }
+  return ray;
+}
+
+struct SHit
+{
+  float t;
+  V3 P, Ng, Ns;
+  float eps;
+  uint32_t primId, objId, instId;
+  int surface;
+};
+
+// epsilonFrom (gpu/gpu_util.h:245-250)
+float epsilonFrom(V3 P, V3 d, float t)
+{
+  return std::max(cmax(vabs(P)), cmax(vabs(d)) * t) * 0x1.fp-21f;
+}
+
+// populateSurfaceHit + computeTangentSpace (gpu/populateHit.h:200-368);
+// primitive ids per computeGeometryPrimId (gpu_util.h:309-315)
+SHit populate(const SceneCtx &S, const Ray &ray, const HitRec &h)
+{
+  const OrcSurface &s = S.sc->surfaces[h.surface];
+  const OrcInstance &in = S.sc->instances[h.inst];
+  SHit sh;
+  sh.t = h.t;
+  sh.P = ray.org + h.t * ray.dir;
+  sh.eps = epsilonFrom(sh.P, ray.dir, h.t);
+  sh.surface = h.surface;
+  sh.primId = s.primIds ? s.primIds[h.prim] : h.prim;
+  sh.objId = s.id;
+  sh.instId = in.userId;
+  V3 Ng, Ns;
+  if (s.type == 0) {
+    V3 a, b, c;
+    triVerts(s, h.prim, a, b, c);
+    Ng = normalize(cross(b - a, c - a));
+    if (!h.front)
+      Ng = -Ng;
+    if (s.normals) {
+      uint32_t i0, i1, i2;
+      if (s.indices) {
+        i0 = s.indices[3 * h.prim];
+        i1 = s.indices[3 * h.prim + 1];
+        i2 = s.indices[3 * h.prim + 2];
+      } else {
+        i0 = 3 * h.prim;
+        i1 = i0 + 1;
+        i2 = i0 + 2;
+      }
+      const float b0 = 1.f - h.u - h.v;
+      Ns = b0 * ld3(s.normals, i0) + h.u * ld3(s.normals, i1) + h.v * ld3(s.normals, i2);
+    } else
+      Ns = Ng;
+    Ns = normalize(Ns);
+    if (dot(Ng, Ns) < 0.f)
+      Ns = -Ns;
+  } else {
+    V3 c;
+    float r;
+    sphereOf(s, h.prim, c, r);
+    const V3 lo = xPoint(S.w2o[h.inst], ray.org);
+    const V3 ld = xVec(S.w2o[h.inst], ray.dir);
+    Ng = Ns = (lo + h.t * ld) - c;
+  }
+  sh.Ng = normalize(xNormalT(S.w2o[h.inst], Ng));
+  sh.Ns = normalize(xNormalT(S.w2o[h.inst], Ns));
+  return sh;
+}
+
+// randomDir(rs, normal) (gpu/gpu_util.h:190-208)
+V3 randomDir(Stream &rs, V3 n)
+{
+  float r[4];
+  uniform4(rs, r);
+  const V3 d = normalize(v3(2.f * r[0] - 1.f, 2.f * r[1] - 1.f, 2.f * r[2] - 1.f));
+  return dot(d, n) > 0.f ? d : -d;
+}
+
+struct Ctx
+{
+  const SceneCtx *S;
+  const OrcRenderer *R;
+  int volMode;
+  int texRound;
+  uint64_t rays = 0;
+};
+
+float surfaceAttenuation(Ctx &C, V3 o, V3 d, float tmin, float tmax)
+{
+  HitRec h;
+  float op;
+  C.rays++;
+  trace<1>(*C.S, o, d, tmin, tmax, false, false, h, op);
+  return op;
+}
+
+// computeAO (gpu/computeAO.h:38-60)
+float computeAO(Ctx &C, Stream &rs, const SHit &hit, float dist, int n)
+{
+  float weights = 0.f, hits = 0.f;
+  const V3 org = hit.P + (hit.eps * hit.Ng);
+  for (int i = 0; i < n; i++) {
+    const V3 dir = randomDir(rs, hit.Ns);
+    const float w = std::max(0.f, dot(dir, hit.Ns));
+    weights += w;
+    if (w != 0.f)
+      hits += w * surfaceAttenuation(C, org, dir, 0.f, dist);
+  }
+  return weights > 0.f ? 1.f - hits / weights : 0.f;
+}
+
+// --- volumes (gpu/volumeIntegration.h, sampleSpatialField.h) ----------------
+
+struct VolHit
+{
+  int entry;
+  V3 lo, ld;
+  float t0, t1;
+};
+
+bool volumeSlab(const OrcVolume &v, const X34 &w2o, V3 o, V3 d, float tmin, float tmax,
+    VolHit &h)
+{
+  const V3 lo = xPoint(w2o, o), ld = xVec(w2o, d);
+  const V3 inv = v3(1.f / ld.x, 1.f / ld.y, 1.f / ld.z);
+  const V3 blo = ld3(v.origin, 0);
+  const V3 bhi = blo
+      + v3((float)(v.dims[0] - 1) * v.spacing[0],
+          (float)(v.dims[1] - 1) * v.spacing[1],
+          (float)(v.dims[2] - 1) * v.spacing[2]);
+  const V3 mins = (blo - lo) * inv, maxs = (bhi - lo) * inv;
+  const V3 nr = v3(std::min(mins.x, maxs.x), std::min(mins.y, maxs.y), std::min(mins.z, maxs.z));
+  const V3 fr = v3(std::max(mins.x, maxs.x), std::max(mins.y, maxs.y), std::max(mins.z, maxs.z));
+  float t0 = cmax(nr), t1 = std::min(fr.x, std::min(fr.y, fr.z));
+  if (!(t0 < t1))
+    return false;
+  t0 = std::max(tmin, std::min(t0, tmax));
+  t1 = std::max(tmin, std::min(t1, tmax));
+  h.lo = lo;
+  h.ld = ld;
+  h.t0 = t0;
+  h.t1 = t1;
+  return true;
+}
+
+struct VolCtx
+{
+  std::vector<X34> w2o;
+};
+
+float sampleFieldParity(const OrcVolume &v, V3 p, int round)
+{
+  const V3 sp = ld3(v.spacing, 0);
+  const V3 inv = v3(1.f / (sp.x * (float)v.dims[0]), 1.f / (sp.y * (float)v.dims[1]),
+      1.f / (sp.z * (float)v.dims[2]));
+  const V3 c = ((p - ld3(v.origin, 0)) + 0.5f * sp) * inv;
+  return v.filterLinear ? tex3dLinear(v.field, v.dims, c.x, c.y, c.z, round)
+                        : tex3dPoint(v.field, v.dims, c.x, c.y, c.z);
+}
+
+void classifyParity(const OrcVolume &v, float s, int round, float out[4])
+{
+  if (!v.tf) {
+    out[0] = v.uniformColor[0];
+    out[1] = v.uniformColor[1];
+    out[2] = v.uniformColor[2];
+    out[3] = v.uniformOpacity;
+    return;
+  }
+  const float lo = v.valueRange[0], hi = v.valueRange[1];
+  const float cs = std::max(lo, std::min(s, hi));
+  const float coord = (cs - lo) * (1.f / (hi - lo));
+  tex1dLinear(v.tf, 256, 4, coord, round, out);
+}
+
+float volStep(const OrcVolume &v)
+{
+  return std::min(v.spacing[0] / 2.f, std::min(v.spacing[1] / 2.f, v.spacing[2] / 2.f));
+}
+
+// rayMarchVolume + _rayMarchVolume (volumeIntegration.h:64-126), in fp32
+// with emulated texture filtering (parity mode) or in FP64 with exact
+// filtering (clean mode).
+float rayMarchVolume(Ctx &C, const OrcVolume &v, const VolHit &h, Stream &rs, V3 *color,
+    float &opacity, float invSamplingRate)
+{
+  float lower = h.t0;
+  const float upper = h.t1;
+  const float depth = lower;
+  const float st0 = volStep(v);
+  const float u0 = uniform(rs);
+  lower += st0 * u0;
+  const float stepSize = st0 * invSamplingRate;
+  const float exponent = stepSize * (1.f / v.unitDistance);
+  const float u1 = uniform(rs);
+  lower += stepSize * u1;
+  if (C.volMode == 0) {
+    float T = 1.f;
+    while (opacity < 0.99f && upper - lower >= 0.f) {
+      const V3 p = h.lo + h.ld * lower;
+      const float s = sampleFieldParity(v, p, C.texRound);
+      if (!std::isnan(s)) {
+        float co[4];
+        classifyParity(v, s, C.texRound, co);
+        const float stT = std::pow(1.f - co[3], exponent);
+        const float a = T * (1.f - stT);
+        if (color)
+          *color = *color + a * v3(co[0], co[1], co[2]);
+        opacity += a;
+        T *= stT;
+      }
+      lower += stepSize;
+    }
+    return depth;
+  }
+  // clean FP64 mode: same jitter draws and sample lattice, exact arithmetic
+  double lo = (double)h.t0 + (double)st0 * u0;
+  const double step = (double)st0 * invSamplingRate;
+  lo += step * u1;
+  const double ex = step / v.unitDistance;
+  double T = 1.0, op = opacity;
+  double col[3] = {0, 0, 0};
+  const double sx = v.spacing[0], sy = v.spacing[1], sz = v.spacing[2];
+  for (long k = 0; op < 0.99 && (double)upper - lo >= 0.0; k++) {
+    const double px = (double)h.lo.x + (double)h.ld.x * lo;
+    const double py = (double)h.lo.y + (double)h.ld.y * lo;
+    const double pz = (double)h.lo.z + (double)h.ld.z * lo;
+    const double cx = ((px - v.origin[0]) + 0.5 * sx) / (sx * v.dims[0]);
+    const double cy = ((py - v.origin[1]) + 0.5 * sy) / (sy * v.dims[1]);
+    const double cz = ((pz - v.origin[2]) + 0.5 * sz) / (sz * v.dims[2]);
+    const double s = v.filterLinear
+        ? tex3dExact(v.field, v.dims, cx, cy, cz)
+        : (double)tex3dPoint(v.field, v.dims, (float)cx, (float)cy, (float)cz);
+    if (!std::isnan(s)) {
+      double co[4];
+      if (v.tf) {
+        const double l = v.valueRange[0], hh = v.valueRange[1];
+        const double cs = std::max(l, std::min(s, hh));
+        tex1dExact(v.tf, 256, (cs - l) / (hh - l), co);
+      } else {
+        co[0] = v.uniformColor[0];
+        co[1] = v.uniformColor[1];
+        co[2] = v.uniformColor[2];
+        co[3] = v.uniformOpacity;
+      }
+      const double stT = std::pow(1.0 - co[3], ex);
+      const double a = T * (1.0 - stT);
+      for (int c = 0; c < 3; c++)
+        col[c] += a * co[c];
+      op += a;
+      T *= stT;
+    }
+    lo = (double)h.t0 + (double)st0 * u0 + step * u1 + step * (double)(k + 1);
+  }
+  opacity = (float)op;
+  if (color)
+    *color = *color + v3((float)col[0], (float)col[1], (float)col[2]);
+  return depth;
+}
+
+bool intersectVolumes(const Ctx &C, const VolCtx &VC, V3 o, V3 d, float tmin, float tmax,
+    int skip, VolHit &best)
+{
+  bool found = false;
+  for (int i = 0; i < C.S->sc->numVolumes; i++) {
+    if (i == skip)
+      continue;
+    VolHit h;
+    if (volumeSlab(C.S->sc->volumes[i], VC.w2o[i], o, d, tmin, tmax, h)) {
+      if (!found || h.t0 < best.t0) {
+        best = h;
+        best.entry = i;
+        found = true;
+      }
+    }
+  }
+  return found;
+}
+
+// rayMarchAllVolumes (volumeIntegration.h:318-350)
+float rayMarchAllVolumes(Ctx &C, const VolCtx &VC, Stream &rs, V3 o, V3 d, float tmin,
+    float tfar, float invRate, V3 &color, float &opacity, uint32_t &objID,
+    uint32_t &instID)
+{
+  float depth = tfar;
+  if (C.S->sc->numVolumes == 0)
+    return depth;
+  bool first = true;
+  int last = -1;
+  do {
+    VolHit h;
+    if (!intersectVolumes(C, VC, o, d, tmin, tfar, last, h))
+      break;
+    const OrcVolume &v = C.S->sc->volumes[h.entry];
+    if (first) {
+      objID = v.id;
+      instID = v.instId;
+      first = false;
+    }
+    depth = std::min(depth, h.t0);
+    h.t1 = std::min(tfar, h.t1);
+    rayMarchVolume(C, v, h, rs, &color, opacity, invRate);
+    tmin = h.t1 + 1e-3f;
+    last = h.entry;
+  } while (opacity < 0.99f);
+  return depth;
+}
+
+float volumeAttenuation(Ctx &C, const VolCtx &VC, Stream &rs, V3 o, V3 d, float tmin,
+    float tmax, float invRate)
+{
+  float a = 0.f;
+  for (int i = 0; i < C.S->sc->numVolumes; i++) {
+    VolHit h;
+    if (!volumeSlab(C.S->sc->volumes[i], VC.w2o[i], o, d, tmin, tmax, h))
+      continue;
+    h.entry = i;
+    rayMarchVolume(C, C.S->sc->volumes[i], h, rs, nullptr, a, invRate);
+    if (a >= 0.99f)
+      break;
+  }
+  return a;
+}
+
+float matteOpacity(const OrcSurface &s)
+{
+  return surfOpacity(s);
+}
+
+// shadeSurface (renderer/DirectLight_ptx.cu:73-224), matte material
+// (shaders/MatteShader_ptx.cu:38-80), directional/point lights
+// (gpu/sampleLight.h:60-90)
+void shadeDL(Ctx &C, const VolCtx &VC, Stream &rs, const Ray &ray, const SHit &hit,
+    float out[4])
+{
+  const OrcRenderer &R = *C.R;
+  const OrcSurface &s = C.S->sc->surfaces[hit.surface];
+  const V3 shadePoint = hit.P + (hit.eps * hit.Ns);
+  const float aoFactor = R.ambientSamples > 0
+      ? computeAO(C, rs, hit, R.occlusionDistance, R.ambientSamples)
+      : 1.f;
+  V3 contrib = v3(0, 0, 0);
+  const V3 base = ld3(s.color, 0);
+  const float opacity = matteOpacity(s);
+  if (R.ambientRadiance > 0.f)
+    contrib = ld3(R.ambientColor, 0) * R.ambientRadiance * base;
+  for (int l = 0; l < C.S->sc->numLights; l++) {
+    const OrcLight &L = C.S->sc->lights[l];
+    V3 ldir, rad;
+    float dist;
+    if (L.type == 0) {
+      ldir = -normalize(ld3(L.direction, 0));
+      dist = INFINITY;
+      rad = ld3(L.radiance, 0);
+    } else {
+      const V3 dd = ld3(L.position, 0) - hit.P;
+      dist = std::sqrt(dot(dd, dd));
+      ldir = dd / dist;
+      rad = ld3(L.radiance, 0) * (1.f / (dist * dist));
+    }
+    const float so = 1.f - surfaceAttenuation(C, shadePoint, ldir, 0.f, dist);
+    const float vo = 1.f
+        - volumeAttenuation(C, VC, rs, shadePoint, ldir, 0.f, dist,
+            1.f / std::min(std::max(R.volumeSamplingRate, 1e-3f), 10.f));
+    const float att = so * vo;
+    const float NdotL = std::max(0.f, dot(hit.Ns, ldir));
+    const V3 tl = base * (float)M_1_PI * NdotL * rad / 1.f;
+    if (std::isnan(tl.x) || std::isnan(tl.y) || std::isnan(tl.z))
+      continue;
+    contrib = contrib + tl * att;
+  }
+  contrib = contrib * aoFactor;
+  out[0] = contrib.x;
+  out[1] = contrib.y;
+  out[2] = contrib.z;
+  out[3] = opacity;
+}
+
+struct Sample
+{
+  V3 color;
+  float opacity;
+  float depth;
+  uint32_t prim, obj, inst;
+};
+
+// default/directLight, raycast and ao raygen bodies
+// (DirectLight_ptx.cu:294-418, Raycast_ptx.cu:60-179,
+// AmbientOcclusion_ptx.cu:86-220)
+Sample integrate(Ctx &C, const VolCtx &VC, const CamPre &cam, Stream &rs, int px, int py,
+    float invW, float invH)
+{
+  const OrcRenderer &R = *C.R;
+  const int rt = R.type;
+  const float invRate = 1.f / std::min(std::max(R.volumeSamplingRate, 1e-3f), 10.f);
+  Ray ray = primaryRay(cam, rs, px, py, invW, invH, rt == 1);
+  const float tmax = ray.tmax;
+  V3 outC = v3(0, 0, 0);
+  float outO = 0.f, depth = 1e30f;
+  uint32_t prim = ~0u, obj = ~0u, inst = ~0u;
+  bool first = true;
+  while (outO < 0.99f) {
+    ray.tmax = tmax;
+    HitRec h;
+    float unused;
+    C.rays++;
+    const bool found = trace<0>(*C.S, ray.org, ray.dir, ray.tmin, ray.tmax,
+        R.cullTriangleBackfaces != 0, true, h, unused);
+    V3 color = v3(0, 0, 0);
+    float opacity = 0.f;
+    if (found) {
+      const SHit sh = populate(*C.S, ray, h);
+      uint32_t vo = ~0u, vi = ~0u;
+      const float vDepth = rayMarchAllVolumes(
+          C, VC, rs, ray.org, ray.dir, ray.tmin, sh.t, invRate, color, opacity, vo, vi);
+      if (first) {
+        if (vDepth < sh.t) {
+          depth = vDepth;
+          prim = 0;
+          obj = vo;
+          inst = vi;
+        } else {
+          depth = sh.t;
+          prim = sh.primId;
+          obj = sh.objId;
+          inst = sh.instId;
+        }
+        first = false;
+      }
+      const OrcSurface &s = C.S->sc->surfaces[sh.surface];
+      if (rt == 0) {
+        float sr[4];
+        shadeDL(C, VC, rs, ray, sh, sr);
+        const V3 srgb = v3(sr[0], sr[1], sr[2]);
+        if (std::isnan(sr[0]) || std::isnan(sr[1]) || std::isnan(sr[2])) {
+          color = v3(0, 0, 0);
+          opacity = 0.f;
+        } else {
+          color = srgb;
+          opacity = sr[3];
+        }
+        color = color + srgb * (1.f - opacity);
+        opacity += sr[3] * (1.f - opacity);
+      } else if (rt == 1) {
+        const V3 lighting = std::fabs(dot(ray.dir, sh.Ns)) * ld3(R.ambientColor, 0);
+        color = color + (ld3(s.color, 0) * lighting) * (1.f - opacity);
+        opacity += matteOpacity(s) * (1.f - opacity);
+      } else {
+        const float ao = R.ambientSamples > 0
+            ? computeAO(C, rs, sh, R.occlusionDistance, R.ambientSamples)
+            : 1.f;
+        const V3 lighting = ao * R.ambientRadiance * ld3(R.ambientColor, 0);
+        color = color + (ld3(s.color, 0) * lighting) * (1.f - opacity);
+        opacity += matteOpacity(s) * (1.f - opacity);
+      }
+      color = color * opacity;
+      outC = outC + color * (1.f - outO);
+      outO += opacity * (1.f - outO);
+      ray.tmin = sh.t + sh.eps;
+    } else {
+      uint32_t vo = ~0u, vi = ~0u;
+      const float vd = rayMarchAllVolumes(
+          C, VC, rs, ray.org, ray.dir, ray.tmin, ray.tmax, invRate, color, opacity, vo, vi);
+      if (first) {
+        depth = std::min(depth, vd);
+        prim = 0;
+        obj = vo;
+        inst = vi;
+      }
+      color = color * opacity;
+      color = color + v3(R.background[0], R.background[1], R.background[2]) * (1.f - opacity);
+      opacity += R.background[3] * (1.f - opacity);
+      outC = outC + color * (1.f - outO);
+      outO += opacity * (1.f - outO);
+      break;
+    }
+  }
+  return Sample{outC, outO, depth, prim, obj, inst};
+}
+
+// --- output (gpu/gpu_util.h:321-443) ---------------------------------------
+
+inline void tonemap(float v[4])
+{
+  const float d = 1.f + std::max(0.f, std::max(v[0], std::max(v[1], v[2])));
+  v[0] /= d;
+  v[1] /= d;
+  v[2] /= d;
+}
+
+inline float srgb(float c)
+{
+  const float x = std::min(std::max(c, 0.f), 1.f);
+  return x < 0.0031308f ? x * 12.92f : std::pow(x, 0.41666f) * 1.055f - 0.055f;
+}
+
+inline uint32_t pack8(float r, float g, float b, float a)
+{
+  auto q = [](float v) {
+    return (uint32_t)std::round(std::min(std::max(v, 0.f), 1.f) * 255.f);
+  };
+  return q(r) | (q(g) << 8) | (q(b) << 16) | (q(a) << 24);
+}
+
+void writeColor(const OrcFrame &F, const float acc[4], size_t idx, int offs)
+{
+  const float n = (float)(F.frameID + offs + 1);
+  float c[4] = {acc[0] / n, acc[1] / n, acc[2] / n, acc[3] / n};
+  const float d = std::max(1e-12f, 1.f - std::max(c[0], std::max(c[1], c[2])));
+  c[0] /= d;
+  c[1] /= d;
+  c[2] /= d;
+  if (F.colorFormat == 0)
+    ((uint32_t *)F.color)[idx] = pack8(srgb(c[0]), srgb(c[1]), srgb(c[2]), c[3]);
+  else if (F.colorFormat == 1)
+    ((uint32_t *)F.color)[idx] = pack8(c[0], c[1], c[2], c[3]);
+  else
+    std::memcpy((float *)F.color + 4 * idx, c, 16);
+}
+
+// computeOrthonormalBasis (gpu_util.h:210-222) applied to s
+V3 onb(V3 n, V3 s)
+{
+  const float sign = n.z >= 0.f ? 1.f : -1.f;
+  const float a = -1.f / (sign + n.z);
+  const float b = n.x * n.y * a;
+  const V3 u = v3(1.f + sign * n.x * n.x * a, sign * b, -sign * n.x);
+  const V3 v = v3(b, sign + n.y * n.y * a, -n.y);
+  return u * s.x + v * s.y + n * s.z;
+}
+
+// diffuse path tracer raygen (renderer/DiffusePathTracer_ptx.cu:82-215),
+// surfaces only; the path state persists across the pixel's samples as in
+// the reference
+struct PathState
+{
+  int depth;
+  V3 Lw;
+};
+
+Sample integrateDPT(Ctx &C, const CamPre &cam, Stream &rs, int px, int py, float invW,
+    float invH, PathState &pd)
+{
+  const OrcRenderer &R = *C.R;
+  Ray ray = primaryRay(cam, rs, px, py, invW, invH, false);
+  const V3 bg = v3(R.background[0], R.background[1], R.background[2]);
+  Sample out{bg, 1.f, ray.tmax, ~0u, ~0u, ~0u};
+  while (true) {
+    HitRec h;
+    float unused;
+    C.rays++;
+    const bool found = trace<0>(*C.S, ray.org, ray.dir, ray.tmin, ray.tmax,
+        R.cullTriangleBackfaces != 0, false, h, unused);
+    if (!found)
+      break;
+    const SHit sh = populate(*C.S, ray, h);
+    if (pd.depth++ >= R.maxDepth) {
+      pd.Lw = v3(0, 0, 0);
+      break;
+    }
+    const V3 pos = sh.P + (sh.eps * sh.Ng);
+    pd.Lw = pd.Lw * ld3(C.S->sc->surfaces[sh.surface].color, 0);
+    const float P = cmax(pd.Lw);
+    if (P < .2f) {
+      if (uniform(rs) > P) {
+        pd.Lw = v3(0, 0, 0);
+        break;
+      }
+      pd.Lw = pd.Lw / P;
+    }
+    const V3 sd = randomDir(rs, sh.Ns);
+    pd.Lw = pd.Lw * std::max(0.f, dot(sd, sh.Ng));
+    ray.org = pos;
+    ray.dir = sd;
+    ray.tmin = 0.f;
+    ray.tmax = R.occlusionDistance;
+  }
+  const V3 Ld = v3(R.ambientRadiance, R.ambientRadiance, R.ambientRadiance);
+  out.color = pd.depth ? pd.Lw * Ld : bg;
+  return out;
+}
+
+} // namespace
+
+// ===========================================================================
+// C API
+// ===========================================================================
+
+extern "C" {
+
+void orc_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4])
+{
+  philox(ctr, key, out);
+}
+
+void orc_philox_stream(
+    uint64_t seed, uint64_t subsequence, uint64_t offset, int kind, int n, void *out)
+{
+  Stream s;
+  s.init(seed, subsequence, offset);
+  if (kind == 0) {
+    for (int i = 0; i < n; i++)
+      ((uint32_t *)out)[i] = s.next();
+  } else if (kind == 1) {
+    for (int i = 0; i < n; i++)
+      ((float *)out)[i] = uniform(s);
+  } else {
+    for (int i = 0; i + 3 < n; i += 4)
+      uniform4(s, (float *)out + i);
+  }
+}
+
+void orc_tex1d(const float *table, int n, int comps, float coord, int round, float *out)
+{
+  tex1dLinear(table, n, comps, coord, round, out);
+}
+
+float orc_tex3d(const float *vox, const int dims[3], const float coord[3], int round)
+{
+  return tex3dLinear(vox, dims, coord[0], coord[1], coord[2], round);
+}
+
+// TransferFunction1D::discritizeTFData (TransferFunction1D.cpp:101-150) with
+// generateLinearPositions / getInterpolatedValue (colorMapHelpers.h:43-73)
+void orc_discretize_tf(const float *color, int nc, int cc, const float *opacity, int no,
+    float lo, float hi, float uniformOpacity, float *out)
+{
+  auto positions = [&](int n) {
+    std::vector<float> p(n);
+    p.front() = 0.f;
+    p.back() = 1.f;
+    const float w = 1.f / (float)(n - 1);
+    for (int i = 1; i + 1 < n; i++)
+      p[i] = p[i - 1] + w;
+    for (auto &v : p)
+      v = v * (hi - lo) + lo;
+    return p;
+  };
+  auto pos01 = [](float v, float a, float b) {
+    v = std::max(a, std::min(v, b));
+    return (v - a) * (1.f / (b - a));
+  };
+  auto interp = [&](const float *vals, int comps, const std::vector<float> &ps, float p,
+                    float *o) {
+    for (size_t i = 0; i + 1 < ps.size(); i++) {
+      const float a = pos01(ps[i], lo, hi), b = pos01(ps[i + 1], lo, hi);
+      if (p >= a && p <= b) {
+        const float t = pos01(p, a, b);
+        for (int c = 0; c < comps; c++)
+          o[c] = vals[i * comps + c] * (1.f - t) + vals[(i + 1) * comps + c] * t;
+        return;
+      }
+    }
+    const size_t k = p <= pos01(ps[0], lo, hi) ? 0 : ps.size() - 1;
+    for (int c = 0; c < comps; c++)
+      o[c] = vals[k * comps + c];
+  };
+  std::vector<float> cp, op;
+  if (color && nc >= 2)
+    cp = positions(nc);
+  if (opacity && no >= 2)
+    op = positions(no);
+  for (int i = 0; i < 256; i++) {
+    const float p = (float)i / 255.f;
+    float c[4] = {1.f, 1.f, 1.f, 1.f};
+    if (!cp.empty()) {
+      float v[4] = {0, 0, 0, 1};
+      interp(color, cc, cp, p, v);
+      c[0] = v[0];
+      c[1] = v[1];
+      c[2] = v[2];
+      c[3] = cc == 4 ? v[3] : 1.f;
+    }
+    float o = uniformOpacity;
+    if (!op.empty())
+      interp(opacity, 1, op, p, &o);
+    out[4 * i + 0] = c[0];
+    out[4 * i + 1] = c[1];
+    out[4 * i + 2] = c[2];
+    out[4 * i + 3] = c[3] * o;
+  }
+}
+
+struct OrcPrepared
+{
+  SceneCtx S;
+  VolCtx VC;
+};
+
+void *orc_prepare(const OrcScene *scene)
+{
+  auto *P = new OrcPrepared();
+  SceneCtx &S = P->S;
+  S.sc = scene;
+  const int ni = scene->numInstances;
+  S.bvh.resize(ni);
+  S.w2o.resize(ni);
+  S.o2w.resize(ni);
+  S.worldBox.resize(ni);
+  // instances that share a surface range share one BVH build
+  std::vector<int> which(ni, -1);
+  std::vector<std::pair<int, int>> ranges;
+  for (int i = 0; i < ni; i++) {
+    const OrcInstance &in = scene->instances[i];
+    std::memcpy(S.o2w[i].m, in.xfm, sizeof(in.xfm));
+    S.w2o[i] = invert(in.xfm);
+    const std::pair<int, int> r{in.firstSurface, in.numSurfaces};
+    for (size_t j = 0; j < ranges.size(); j++)
+      if (ranges[j] == r)
+        which[i] = (int)j;
+    if (which[i] < 0) {
+      which[i] = (int)ranges.size();
+      ranges.push_back(r);
+    }
+  }
+  S.unique.resize(ranges.size());
+  for (size_t j = 0; j < ranges.size(); j++) {
+    InstBVH &b = S.unique[j];
+    for (int k = 0; k < ranges[j].second; k++) {
+      const int si = ranges[j].first + k;
+      for (uint32_t p = 0; p < scene->surfaces[si].numPrims; p++)
+        b.prims.push_back(Prim{si, p});
+    }
+    buildBVH(scene, b);
+  }
+  for (int i = 0; i < ni; i++) {
+    S.bvh[i] = &S.unique[which[i]];
+    Box wb;
+    if (!S.bvh[i]->nodes.empty()) {
+      const Box &ob = S.bvh[i]->nodes[0].box;
+      for (int c = 0; c < 8; c++)
+        wb.ext(xPoint(S.o2w[i],
+            v3((c & 1) ? ob.hi.x : ob.lo.x,
+                (c & 2) ? ob.hi.y : ob.lo.y,
+                (c & 4) ? ob.hi.z : ob.lo.z)));
+    }
+    S.worldBox[i] = wb;
+  }
+  for (int i = 0; i < scene->numVolumes; i++)
+    P->VC.w2o.push_back(invert(scene->volumes[i].xfm));
+  return P;
+}
+
+void orc_release(void *prepared)
+{
+  delete (OrcPrepared *)prepared;
+}
+
+int orc_render(const OrcScene *scene, const OrcCamera *camera, const OrcRenderer *renderer,
+    OrcFrame *frame, int volumeMode, int texRound, int threads)
+{
+  void *p = orc_prepare(scene);
+  const int rc =
+      orc_render_prepared(p, camera, renderer, frame, volumeMode, texRound, threads);
+  orc_release(p);
+  return rc;
+}
+
+int orc_render_prepared(void *prepared, const OrcCamera *camera, const OrcRenderer *renderer,
+    OrcFrame *frame, int volumeMode, int texRound, int threads)
+{
+  const SceneCtx &S = ((OrcPrepared *)prepared)->S;
+  const VolCtx &VC = ((OrcPrepared *)prepared)->VC;
+  const CamPre cam = camSetup(*camera);
+  OrcFrame &F = *frame;
+  const int W = F.width, H = F.height;
+  const float invW = 1.f / (float)W, invH = 1.f / (float)H;
+  const int rb = std::max(0, F.rowBegin), re = std::min(H, F.rowEnd);
+  const int tilesX = (W + 15) / 16, tilesY = (re - rb + 15) / 16;
+  std::atomic<int> next{0};
+  std::atomic<uint64_t> rays{0};
+  auto worker = [&]() {
+    Ctx C{&S, renderer, volumeMode, texRound, 0};
+    while (true) {
+      const int t = next.fetch_add(1);
+      if (t >= tilesX * tilesY)
+        break;
+      const int tx = t % tilesX, ty = t / tilesX;
+      for (int y = rb + ty * 16; y < std::min(re, rb + ty * 16 + 16); y++)
+        for (int x = tx * 16; x < std::min(W, tx * 16 + 16); x++) {
+          Stream rs;
+          rs.init((uint64_t)(y * W + x), 0, (uint64_t)F.frameID * 512ull);
+          const size_t idx = (size_t)y * W + x;
+          float acc[4] = {F.accum[4 * idx], F.accum[4 * idx + 1], F.accum[4 * idx + 2],
+              F.accum[4 * idx + 3]};
+          float cur = F.depth ? F.depth[idx] : 0.f;
+          const int iters = renderer->type == 1 ? 1 : std::max(renderer->pixelSamples, 1);
+          PathState pd{0, v3(1, 1, 1)};
+          for (int i = 0; i < iters; i++) {
+            const Sample s = renderer->type == 3
+                ? integrateDPT(C, cam, rs, x, y, invW, invH, pd)
+                : integrate(C, VC, cam, rs, x, y, invW, invH);
+            float v[4] = {s.color.x, s.color.y, s.color.z, s.opacity};
+            tonemap(v);
+            for (int c = 0; c < 4; c++)
+              acc[c] += v[c];
+            if (!F.depth || s.depth < cur) {
+              cur = s.depth;
+              if (F.depth)
+                F.depth[idx] = cur;
+              if (F.primId)
+                F.primId[idx] = s.prim;
+              if (F.objId)
+                F.objId[idx] = s.obj;
+              if (F.instId)
+                F.instId[idx] = s.inst;
+            }
+          }
+          std::memcpy(F.accum + 4 * idx, acc, 16);
+          writeColor(F, acc, idx, iters - 1);
+        }
+    }
+    rays += C.rays;
+  };
+  int nt = threads > 0 ? threads : (int)std::thread::hardware_concurrency();
+  nt = std::max(1, nt);
+  std::vector<std::thread> pool;
+  for (int i = 0; i < nt; i++)
+    pool.emplace_back(worker);
+  for (auto &t : pool)
+    t.join();
+  F.raysTraced = rays.load();
+  return 0;
+}
+
+// ---------------------------------------------------------------------------
+// BVH8 visit counter over libvrtx's node layout (80-byte nodes, 48-byte
+// triangle records); closest-hit order as in the GPU traversal.
+// ---------------------------------------------------------------------------
+
+void orc_bvh8_count(const void *nodesV, const void *trisV, const float *rays, int numRays,
+    uint64_t *nodeVisits, uint64_t *primTests, float *tHit)
+{
+  const uint8_t *nodes = (const uint8_t *)nodesV;
+  const float *tris = (const float *)trisV;
+  uint64_t nv = 0, pt = 0;
+  for (int ri = 0; ri < numRays; ri++) {
+    const V3 o = v3(rays[7 * ri], rays[7 * ri + 1], rays[7 * ri + 2]);
+    const V3 d = v3(rays[7 * ri + 3], rays[7 * ri + 4], rays[7 * ri + 5]);
+    float tmax = rays[7 * ri + 6];
+    const RayPre r = prep(o, d);
+    const uint32_t oct = (d.x < 0 ? 1u : 0u) | (d.y < 0 ? 2u : 0u) | (d.z < 0 ? 4u : 0u);
+    struct G
+    {
+      uint32_t base, bits;
+    };
+    std::vector<G> stack;
+    G cur{0, 0x80000000u}, tri{0, 0};
+    while (true) {
+      if (tri.bits) {
+        while (tri.bits) {
+          const int b = __builtin_ctz(tri.bits);
+          tri.bits &= tri.bits - 1;
+          const float *t = tris + 12 * (size_t)(tri.base + b);
+          float th, u, v;
+          bool fr;
+          pt++;
+          if (hitTriangle(r, v3(t[0], t[1], t[2]), v3(t[4], t[5], t[6]),
+                  v3(t[8], t[9], t[10]), 0.f, tmax, th, u, v, fr))
+            tmax = th;
+        }
+        continue;
+      }
+      if (cur.bits & 0xff000000u) {
+        const uint32_t bit = __builtin_ctz(cur.bits >> 24);
+        cur.bits &= ~(1u << (24 + bit));
+        const uint32_t slot = bit ^ oct;
+        const uint32_t idx = cur.base + __builtin_popcount(cur.bits & 0xffu & ((1u << slot) - 1u));
+        if (cur.bits & 0xff000000u)
+          stack.push_back(cur);
+        nv++;
+        const uint8_t *n = nodes + 80 * (size_t)idx;
+        float p[3];
+        std::memcpy(p, n, 12);
+        const uint8_t ex = n[12], ey = n[13], ez = n[14], imask = n[15];
+        uint32_t childBase, primBase;
+        std::memcpy(&childBase, n + 16, 4);
+        std::memcpy(&primBase, n + 20, 4);
+        const uint8_t *meta = n + 24;
+        const uint8_t *q = n + 32; // qlox, qloy, qloz, qhix, qhiy, qhiz
+        auto sc = [](uint8_t e) {
+          uint32_t b = (uint32_t)e << 23;
+          float f;
+          std::memcpy(&f, &b, 4);
+          return f;
+        };
+        const float s[3] = {sc(ex), sc(ey), sc(ez)};
+        uint32_t hits = 0;
+        for (int c = 0; c < 8; c++) {
+          if (!meta[c])
+            continue;
+          Box bb;
+          bb.lo = v3(p[0] + q[c] * s[0], p[1] + q[8 + c] * s[1], p[2] + q[16 + c] * s[2]);
+          bb.hi = v3(p[0] + q[24 + c] * s[0], p[1] + q[32 + c] * s[1], p[2] + q[40 + c] * s[2]);
+          if (!hitBox(bb, r, 0.f, tmax))
+            continue;
+          if (imask & (1u << c))
+            hits |= 1u << (24 + (c ^ oct));
+          else
+            hits |= (uint32_t)(meta[c] >> 5) << (meta[c] & 31);
+        }
+        cur = G{childBase, (hits & 0xff000000u) | imask};
+        tri = G{primBase, hits & 0x00ffffffu};
+        continue;
+      }
+      if (stack.empty())
+        break;
+      cur = stack.back();
+      stack.pop_back();
+    }
+    if (tHit)
+      tHit[ri] = tmax;
+  }
+  *nodeVisits = nv;
+  *primTests = pt;
+}
+
+// ---------------------------------------------------------------------------
+// differentiable marcher, FP64 (model stated next to vrtxDMForward)
+// ---------------------------------------------------------------------------
+
+void orc_dm(const OrcDMVolume *vol, const OrcDMView *view, double *image,
+    const double *gradImage, double *gradDensity, double *gradTf, double *gradScale,
+    int threads)
+{
+  const OrcDMVolume &v = *vol;
+  const OrcDMView &w = *view;
+  const int N = v.tfSize;
+  const double ratio = v.step / v.unitDistance;
+  const double logStop = std::log(1e-3);
+  const int nt = std::max(1, threads > 0 ? threads : (int)std::thread::hardware_concurrency());
+  std::vector<std::vector<double>> gD(gradDensity ? nt : 0), gT(gradTf ? nt : 0);
+  std::vector<double> gS(nt, 0.0);
+  const size_t nvox = (size_t)v.dims[0] * v.dims[1] * v.dims[2];
+  std::atomic<int> nextRow{0};
+  auto work = [&](int tid) {
+    if (gradDensity)
+      gD[tid].assign(nvox, 0.0);
+    if (gradTf)
+      gT[tid].assign((size_t)N * 4, 0.0);
+    struct S
+    {
+      double s;
+      int ix[3], st[3];
+      double f[3];
+      double c[4];
+      int i0;
+      double fr;
+      double dxds;
+    };
+    std::vector<S> samples;
+    while (true) {
+      const int py = nextRow.fetch_add(1);
+      if (py >= w.height)
+        break;
+      for (int px = 0; px < w.width; px++) {
+        double d[3];
+        for (int k = 0; k < 3; k++)
+          d[k] = w.d00[k] + (px + 0.5) * w.du[k] + (py + 0.5) * w.dv[k];
+        const double dl = std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+        for (int k = 0; k < 3; k++)
+          d[k] /= dl;
+        double t0 = 0.0, t1 = 1e300;
+        for (int k = 0; k < 3; k++) {
+          const double inv = 1.0 / d[k];
+          double a = (0.0 - w.eye[k]) * inv, b = ((v.dims[k] - 1) - w.eye[k]) * inv;
+          if (a > b)
+            std::swap(a, b);
+          t0 = std::max(t0, a);
+          t1 = std::min(t1, b);
+        }
+        samples.clear();
+        double logT = 0.0;
+        double C[3] = {0, 0, 0};
+        if (t0 < t1) {
+          for (int k = 0;; k++) {
+            const double t = t0 + (k + 0.5) * v.step;
+            if (t > t1)
+              break;
+            S sm;
+            size_t base = 0;
+            for (int a = 0; a < 3; a++) {
+              const int n = v.dims[a];
+              const double p = w.eye[a] + t * d[a];
+              if (n < 2) {
+                sm.ix[a] = 0;
+                sm.st[a] = 0;
+                sm.f[a] = 0;
+                continue;
+              }
+              const double c = std::min(std::max(p, 0.0), (double)(n - 1));
+              sm.ix[a] = std::min((int)std::floor(c), n - 2);
+              sm.st[a] = 1;
+              sm.f[a] = c - sm.ix[a];
+            }
+            (void)base;
+            double s = 0.0;
+            for (int q = 0; q < 8; q++) {
+              const int x = sm.ix[0] + ((q & 1) ? sm.st[0] : 0);
+              const int y = sm.ix[1] + ((q & 2) ? sm.st[1] : 0);
+              const int z = sm.ix[2] + ((q & 4) ? sm.st[2] : 0);
+              const double ww = ((q & 1) ? sm.f[0] : 1 - sm.f[0])
+                  * ((q & 2) ? sm.f[1] : 1 - sm.f[1]) * ((q & 4) ? sm.f[2] : 1 - sm.f[2]);
+              s += ww * v.density[((size_t)z * v.dims[1] + y) * v.dims[0] + x];
+            }
+            sm.s = s;
+            const double range = v.valueHi - v.valueLo;
+            double u = (s - v.valueLo) / range;
+            sm.dxds = (u > 0 && u < 1) ? (N - 1) / range : 0.0;
+            u = std::min(std::max(u, 0.0), 1.0);
+            const double x = u * (N - 1);
+            sm.i0 = std::min((int)std::floor(x), N - 2);
+            sm.fr = x - sm.i0;
+            for (int c = 0; c < 4; c++)
+              sm.c[c] = v.tf[4 * sm.i0 + c] + sm.fr * (v.tf[4 * (sm.i0 + 1) + c] - v.tf[4 * sm.i0 + c]);
+            const double alpha = std::min(sm.c[3] * v.opacityScale, 0.999);
+            const double sigma = ratio * std::log1p(-alpha);
+            const double T = std::exp(logT);
+            const double a = -std::expm1(sigma);
+            for (int c = 0; c < 3; c++)
+              C[c] += T * a * sm.c[c];
+            logT += sigma;
+            samples.push_back(sm);
+            if (logT < logStop)
+              break;
+          }
+        }
+        const double Tend = std::exp(logT);
+        const size_t pix = (size_t)py * w.width + px;
+        for (int c = 0; c < 3; c++)
+          image[3 * pix + c] = C[c] + Tend * w.background[c];
+        if (!gradImage)
+          continue;
+        const double g[3] = {gradImage[3 * pix], gradImage[3 * pix + 1], gradImage[3 * pix + 2]};
+        double Snext[3] = {Tend * w.background[0], Tend * w.background[1], Tend * w.background[2]};
+        double lt = logT;
+        double Tnext = Tend;
+        for (int k = (int)samples.size() - 1; k >= 0; k--) {
+          const S &sm = samples[k];
+          const double araw = sm.c[3] * v.opacityScale;
+          const double alpha = std::min(araw, 0.999);
+          const double sigma = ratio * std::log1p(-alpha);
+          lt -= sigma;
+          const double Tk = std::exp(lt);
+          const double a = -std::expm1(sigma);
+          const double wk = Tk * a;
+          double dSigma = 0.0;
+          for (int c = 0; c < 3; c++)
+            dSigma += g[c] * (Snext[c] - Tnext * sm.c[c]);
+          for (int c = 0; c < 3; c++)
+            Snext[c] += wk * sm.c[c];
+          Tnext = Tk;
+          const double dAlpha = araw < 0.999 ? dSigma * (-ratio / (1.0 - alpha)) : 0.0;
+          const double dA = dAlpha * v.opacityScale;
+          gS[tid] += dAlpha * sm.c[3];
+          const double dc[3] = {wk * g[0], wk * g[1], wk * g[2]};
+          if (gradTf) {
+            double *e0 = gT[tid].data() + 4 * sm.i0;
+            for (int c = 0; c < 3; c++) {
+              e0[c] += (1 - sm.fr) * dc[c];
+              e0[4 + c] += sm.fr * dc[c];
+            }
+            e0[3] += (1 - sm.fr) * dA;
+            e0[7] += sm.fr * dA;
+          }
+          if (gradDensity && sm.dxds != 0.0) {
+            const double *ea = v.tf + 4 * sm.i0, *eb = v.tf + 4 * (sm.i0 + 1);
+            const double dval = dc[0] * (eb[0] - ea[0]) + dc[1] * (eb[1] - ea[1])
+                + dc[2] * (eb[2] - ea[2]) + dA * (eb[3] - ea[3]);
+            const double ds = dval * sm.dxds;
+            for (int q = 0; q < 8; q++) {
+              const int x = sm.ix[0] + ((q & 1) ? sm.st[0] : 0);
+              const int y = sm.ix[1] + ((q & 2) ? sm.st[1] : 0);
+              const int z = sm.ix[2] + ((q & 4) ? sm.st[2] : 0);
+              const double ww = ((q & 1) ? sm.f[0] : 1 - sm.f[0])
+                  * ((q & 2) ? sm.f[1] : 1 - sm.f[1]) * ((q & 4) ? sm.f[2] : 1 - sm.f[2]);
+              gD[tid][((size_t)z * v.dims[1] + y) * v.dims[0] + x] += ww * ds;
+            }
+          }
+        }
+      }
+    }
+  };
+  std::vector<std::thread> pool;
+  for (int i = 0; i < nt; i++)
+    pool.emplace_back(work, i);
+  for (auto &t : pool)
+    t.join();
+  if (gradImage) {
+    for (int i = 0; i < nt; i++) {
+      if (gradDensity)
+        for (size_t k = 0; k < nvox; k++)
+          gradDensity[k] += gD[i][k];
+      if (gradTf)
+        for (int k = 0; k < 4 * N; k++)
+          gradTf[k] += gT[i][k];
+      if (gradScale)
+        *gradScale += gS[i];
+    }
+  }
+}
+
+} // extern "C"

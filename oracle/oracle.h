@@ -1,0 +1,226 @@
+/*
+ * oracle.h -- CPU oracle for the VisRTX hot path. TEST INFRASTRUCTURE ONLY:
+ * tests, the smoke check and bench.py's CPU-baseline/reference legs call it
+ * as the checker; libvrtx never links or calls it.
+ *
+ * It restates, on the CPU, the reference's algorithms for ray generation,
+ * ray/primitive intersection, the default/raycast/ao/dpt integrators, the
+ * scivis volume marcher and the frame output path (citations per function
+ * in oracle.cpp), plus an FP64 marcher and FP64 adjoint for the
+ * differentiable marcher of this library.
+ *
+ * Parity status: the reference cannot be built here (OptiX and the
+ * ANARI-SDK are absent) and ships no golden images or known-answer tests,
+ * so the end-to-end algorithm is "parity unpinned". The third-party
+ * arithmetic at its boundary is pinned separately: Philox4x32-10 against the
+ * SC'11 paper's algorithm and against curand outputs captured on the GPU,
+ * and the texture-filter emulation against tex1D/tex3D outputs captured on
+ * the GPU (tests/golden/).
+ */
+#ifndef VRTX_ORACLE_H
+#define VRTX_ORACLE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* --- RNG ----------------------------------------------------------------- */
+
+/* Philox4x32-10 block function (Salmon et al., SC'11). */
+void orc_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
+
+/* curand-style Philox stream: init(seed, subsequence, offset), then n
+ * draws. kind 0: curand() raw u32; 1: curand_uniform; 2: curand_uniform4
+ * (n must be a multiple of 4). out is uint32 or float accordingly. */
+void orc_philox_stream(uint64_t seed,
+    uint64_t subsequence,
+    uint64_t offset,
+    int kind,
+    int n,
+    void *out);
+
+/* --- texture filter emulation (parity mode) ------------------------------ */
+
+/* Linear-filtered, clamped, normalised-coordinate fetch from a 1D table of
+ * `comps`-component floats, with weights quantised to 8 fractional bits
+ * (CUDA Programming Guide, "Linear Filtering"). round: 0 = truncate,
+ * 1 = round to nearest. */
+void orc_tex1d(const float *table, int n, int comps, float coord, int round,
+    float *out);
+float orc_tex3d(const float *vox, const int dims[3], const float coord[3], int round);
+
+/* --- scene ---------------------------------------------------------------- */
+
+typedef struct OrcSurface {
+  int type; /* 0 triangle, 1 sphere */
+  const float *vertices; /* vec3 */
+  const uint32_t *indices; /* uvec3 per triangle or u32 per sphere; NULL */
+  uint32_t numPrims;
+  const float *normals; /* vertex.normal (vec3) or NULL */
+  const uint32_t *primIds; /* primitive.id or NULL */
+  const float *radii; /* sphere per-vertex radius or NULL */
+  float radius;
+  int cullBackfaces;
+  uint32_t id; /* Surface id */
+  float color[3];
+  float opacity;
+  int alphaMode; /* 0 opaque, 1 blend, 2 mask */
+  float cutoff;
+} OrcSurface;
+
+typedef struct OrcInstance {
+  float xfm[12]; /* 3 rows x 4 */
+  uint32_t userId;
+  int firstSurface;
+  int numSurfaces;
+} OrcInstance;
+
+typedef struct OrcLight {
+  int type; /* 0 directional, 1 point */
+  float direction[3]; /* world-space direction of travel */
+  float position[3];
+  float radiance[3];
+} OrcLight;
+
+typedef struct OrcVolume {
+  const float *field; /* dims[0] fastest */
+  int dims[3];
+  float origin[3], spacing[3];
+  int filterLinear;
+  const float *tf; /* 256 x RGBA, NULL = uniform */
+  float valueRange[2];
+  float unitDistance;
+  float uniformColor[3];
+  float uniformOpacity;
+  uint32_t id;
+  uint32_t instId;
+  float xfm[12];
+} OrcVolume;
+
+typedef struct OrcScene {
+  const OrcSurface *surfaces;
+  int numSurfaces;
+  const OrcInstance *instances;
+  int numInstances;
+  const OrcLight *lights;
+  int numLights;
+  const OrcVolume *volumes;
+  int numVolumes;
+} OrcScene;
+
+typedef struct OrcCamera {
+  int type; /* 0 perspective, 1 orthographic */
+  float position[3], direction[3], up[3];
+  float fovy, aspect, height;
+  float imageRegion[4];
+  float apertureRadius, focusDistance;
+} OrcCamera;
+
+typedef struct OrcRenderer {
+  int type; /* 0 default/directLight, 1 raycast, 2 ao, 3 dpt */
+  float background[4];
+  float ambientColor[3];
+  float ambientRadiance;
+  float occlusionDistance;
+  int cullTriangleBackfaces;
+  float volumeSamplingRate;
+  int pixelSamples;
+  int ambientSamples;
+  int maxDepth;
+} OrcRenderer;
+
+typedef struct OrcFrame {
+  int width, height;
+  int frameID; /* sample index base (RNG offset = frameID * 512) */
+  int colorFormat; /* 0 sRGB rgba8, 1 linear rgba8, 2 float4 */
+  int rowBegin, rowEnd; /* rows to render */
+  /* outputs (full-frame buffers; only rows in range are written) */
+  float *accum; /* float4, in/out */
+  void *color; /* u32 or float4 */
+  float *depth; /* in/out (cleared to FLT_MAX by the caller) */
+  uint32_t *primId, *objId, *instId;
+  /* statistics: rays traced (primary + secondary) */
+  uint64_t raysTraced;
+} OrcFrame;
+
+/* Renders rows [rowBegin, rowEnd). volumeMode 0: parity (texture
+ * emulation, float32 like the reference), 1: clean FP64 volumes.
+ * threads <= 0 uses all hardware threads. Returns 0 on success. */
+/* Builds the oracle's acceleration structures for `scene` once (the scene
+ * arrays must stay alive); render with orc_render_prepared, free with
+ * orc_release. */
+void *orc_prepare(const OrcScene *scene);
+void orc_release(void *prepared);
+int orc_render_prepared(void *prepared,
+    const OrcCamera *camera,
+    const OrcRenderer *renderer,
+    OrcFrame *frame,
+    int volumeMode,
+    int texRound,
+    int threads);
+
+int orc_render(const OrcScene *scene,
+    const OrcCamera *camera,
+    const OrcRenderer *renderer,
+    OrcFrame *frame,
+    int volumeMode,
+    int texRound,
+    int threads);
+
+/* TF discretisation of the reference (TransferFunction1D.cpp:101-150):
+ * color (nc x 3 or 4 floats), opacity (no floats) -> 256 x RGBA. */
+void orc_discretize_tf(const float *color,
+    int nc,
+    int colorComps,
+    const float *opacity,
+    int no,
+    float valueLo,
+    float valueHi,
+    float uniformOpacity,
+    float *out256x4);
+
+/* Counts node visits and primitive tests of a closest-hit traversal over a
+ * libvrtx BVH8 (one BLAS: nodes + triangle records, as copied by
+ * vrtxDebugCopyAccel) for the given rays (org/dir/tmax, 7 floats each). */
+void orc_bvh8_count(const void *nodes,
+    const void *triRecords,
+    const float *rays,
+    int numRays,
+    uint64_t *nodeVisits,
+    uint64_t *primTests,
+    float *tHit);
+
+/* --- differentiable marcher, FP64 ----------------------------------------- */
+
+typedef struct OrcDMVolume {
+  const double *density;
+  int dims[3];
+  const double *tf; /* tfSize x 4 */
+  int tfSize;
+  double opacityScale, step, unitDistance, valueLo, valueHi;
+} OrcDMVolume;
+
+typedef struct OrcDMView {
+  int width, height;
+  double eye[3], d00[3], du[3], dv[3], background[3];
+} OrcDMView;
+
+/* Forward image (3 doubles per pixel); when gradImage != NULL, also the
+ * adjoint: gradDensity (dims), gradTf (tfSize x 4), gradScale (1),
+ * accumulated. */
+void orc_dm(const OrcDMVolume *vol,
+    const OrcDMView *view,
+    double *image,
+    const double *gradImage,
+    double *gradDensity,
+    double *gradTf,
+    double *gradScale,
+    int threads);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

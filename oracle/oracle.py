@@ -1,0 +1,357 @@
+"""Python binding of the CPU oracle (oracle.h). TEST INFRASTRUCTURE ONLY:
+used by tests/, __graft_entry__.smoke() and bench.py's CPU-baseline and
+reference legs as the checker, never by the product path.
+
+render(spec) renders a visrtx_gb300.scenes.SceneSpec with the oracle's
+restatement of the reference integrators; dm(...) runs the FP64
+differentiable-marcher forward/adjoint.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+_lib = None
+
+
+def load() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        from . import build as _b  # noqa: F401  (package-relative when imported as oracle.oracle)
+        path = _b.build()
+        _lib = C.CDLL(path)
+        _lib.orc_render.restype = C.c_int
+        _lib.orc_tex3d.restype = C.c_float
+    return _lib
+
+
+class OrcSurface(C.Structure):
+    _fields_ = [("type", C.c_int), ("vertices", C.c_void_p), ("indices", C.c_void_p),
+                ("numPrims", C.c_uint32), ("normals", C.c_void_p), ("primIds", C.c_void_p),
+                ("radii", C.c_void_p), ("radius", C.c_float), ("cullBackfaces", C.c_int),
+                ("id", C.c_uint32), ("color", C.c_float * 3), ("opacity", C.c_float),
+                ("alphaMode", C.c_int), ("cutoff", C.c_float)]
+
+
+class OrcInstance(C.Structure):
+    _fields_ = [("xfm", C.c_float * 12), ("userId", C.c_uint32), ("firstSurface", C.c_int),
+                ("numSurfaces", C.c_int)]
+
+
+class OrcLight(C.Structure):
+    _fields_ = [("type", C.c_int), ("direction", C.c_float * 3), ("position", C.c_float * 3),
+                ("radiance", C.c_float * 3)]
+
+
+class OrcVolume(C.Structure):
+    _fields_ = [("field", C.c_void_p), ("dims", C.c_int * 3), ("origin", C.c_float * 3),
+                ("spacing", C.c_float * 3), ("filterLinear", C.c_int), ("tf", C.c_void_p),
+                ("valueRange", C.c_float * 2), ("unitDistance", C.c_float),
+                ("uniformColor", C.c_float * 3), ("uniformOpacity", C.c_float),
+                ("id", C.c_uint32), ("instId", C.c_uint32), ("xfm", C.c_float * 12)]
+
+
+class OrcScene(C.Structure):
+    _fields_ = [("surfaces", C.c_void_p), ("numSurfaces", C.c_int), ("instances", C.c_void_p),
+                ("numInstances", C.c_int), ("lights", C.c_void_p), ("numLights", C.c_int),
+                ("volumes", C.c_void_p), ("numVolumes", C.c_int)]
+
+
+class OrcCamera(C.Structure):
+    _fields_ = [("type", C.c_int), ("position", C.c_float * 3), ("direction", C.c_float * 3),
+                ("up", C.c_float * 3), ("fovy", C.c_float), ("aspect", C.c_float),
+                ("height", C.c_float), ("imageRegion", C.c_float * 4),
+                ("apertureRadius", C.c_float), ("focusDistance", C.c_float)]
+
+
+class OrcRenderer(C.Structure):
+    _fields_ = [("type", C.c_int), ("background", C.c_float * 4), ("ambientColor", C.c_float * 3),
+                ("ambientRadiance", C.c_float), ("occlusionDistance", C.c_float),
+                ("cullTriangleBackfaces", C.c_int), ("volumeSamplingRate", C.c_float),
+                ("pixelSamples", C.c_int), ("ambientSamples", C.c_int), ("maxDepth", C.c_int)]
+
+
+class OrcFrame(C.Structure):
+    _fields_ = [("width", C.c_int), ("height", C.c_int), ("frameID", C.c_int),
+                ("colorFormat", C.c_int), ("rowBegin", C.c_int), ("rowEnd", C.c_int),
+                ("accum", C.c_void_p), ("color", C.c_void_p), ("depth", C.c_void_p),
+                ("primId", C.c_void_p), ("objId", C.c_void_p), ("instId", C.c_void_p),
+                ("raysTraced", C.c_uint64)]
+
+
+class OrcDMVolume(C.Structure):
+    _fields_ = [("density", C.c_void_p), ("dims", C.c_int * 3), ("tf", C.c_void_p),
+                ("tfSize", C.c_int), ("opacityScale", C.c_double), ("step", C.c_double),
+                ("unitDistance", C.c_double), ("valueLo", C.c_double), ("valueHi", C.c_double)]
+
+
+class OrcDMView(C.Structure):
+    _fields_ = [("width", C.c_int), ("height", C.c_int), ("eye", C.c_double * 3),
+                ("d00", C.c_double * 3), ("du", C.c_double * 3), ("dv", C.c_double * 3),
+                ("background", C.c_double * 3)]
+
+
+_RENDERERS = {"default": 0, "directLight": 0, "raycast": 1, "ao": 2, "dpt": 3,
+              "diffuse_pathtracer": 3}
+_ALPHA = {"opaque": 0, "blend": 1, "mask": 2}
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def _rows(m4):
+    m = np.asarray(m4, np.float32)
+    return (C.c_float * 12)(*[float(m[r, c]) for r in range(3) for c in range(4)])
+
+
+def discretize_tf(color, opacity, value_range=(0.0, 1.0), uniform_opacity=1.0) -> np.ndarray:
+    lib = load()
+    out = np.zeros((256, 4), np.float32)
+    c = None if color is None else np.ascontiguousarray(color, np.float32)
+    o = None if opacity is None else np.ascontiguousarray(opacity, np.float32)
+    lib.orc_discretize_tf(_ptr(c), C.c_int(0 if c is None else len(c)),
+                          C.c_int(0 if c is None else c.shape[1]), _ptr(o),
+                          C.c_int(0 if o is None else len(o)), C.c_float(value_range[0]),
+                          C.c_float(value_range[1]), C.c_float(uniform_opacity), _ptr(out))
+    return out
+
+
+def render(spec, frame_id: int = 0, rows: tuple[int, int] | None = None, volume_mode: int = 0,
+           tex_round: int = 1, threads: int = 0, accum=None, depth=None):
+    """Renders `spec` on the CPU. Returns a dict of numpy outputs (color as
+    packed sRGB uint32, depth, primitiveId, objectId, instanceId, accum)
+    plus 'rays' (rays traced)."""
+    sc = OracleScene(spec)
+    try:
+        return sc.render(frame_id, rows, volume_mode, tex_round, threads, accum, depth)
+    finally:
+        sc.release()
+
+
+class OracleScene:
+    """The oracle's acceleration structures for one spec, built once."""
+
+    def __init__(self, spec):
+        self.spec = spec
+        self.lib = load()
+        self._keep, self._scene = _scene_structs(spec)
+        self.lib.orc_prepare.restype = C.c_void_p
+        self.handle = C.c_void_p(self.lib.orc_prepare(C.byref(self._scene)))
+
+    def release(self):
+        if self.handle:
+            self.lib.orc_release(self.handle)
+            self.handle = None
+
+    def render(self, frame_id=0, rows=None, volume_mode=0, tex_round=1, threads=0, accum=None,
+               depth=None, spec=None):
+        return _render_prepared(self.lib, self.handle, spec or self.spec, frame_id, rows,
+                                volume_mode, tex_round, threads, accum, depth)
+
+
+def _scene_structs(spec):
+    keep = []
+    surfs = (OrcSurface * max(1, len(spec.surfaces)))()
+    for i, s in enumerate(spec.surfaces):
+        o = surfs[i]
+        o.type = 0 if s.type == "triangle" else 1
+        v = np.ascontiguousarray(s.vertices, np.float32)
+        keep.append(v)
+        o.vertices = _ptr(v)
+        if s.indices is not None:
+            ix = np.ascontiguousarray(s.indices, np.uint32)
+            keep.append(ix)
+            o.indices = _ptr(ix)
+        o.numPrims = s.num_prims
+        for name, arr, dt in (("normals", s.normals, np.float32), ("primIds", s.prim_ids, np.uint32),
+                              ("radii", s.radii, np.float32)):
+            if arr is not None:
+                a = np.ascontiguousarray(arr, dt)
+                keep.append(a)
+                setattr(o, name, _ptr(a))
+        o.radius = s.radius
+        o.cullBackfaces = int(bool(s.cull))
+        o.id = s.id & 0xFFFFFFFF
+        o.color = (C.c_float * 3)(*map(float, s.color))
+        o.opacity = s.opacity
+        o.alphaMode = _ALPHA[s.alpha_mode]
+        o.cutoff = s.cutoff
+    insts = []
+    for ins in spec.instances:
+        if not ins.surfaces:
+            continue
+        first = min(ins.surfaces)
+        assert sorted(ins.surfaces) == list(range(first, first + len(ins.surfaces)))
+        oi = OrcInstance()
+        oi.xfm = _rows(np.eye(4) if ins.zero else ins.xfm)
+        oi.userId = (spec.world_id if ins.zero else ins.id) & 0xFFFFFFFF
+        oi.firstSurface = first
+        oi.numSurfaces = len(ins.surfaces)
+        insts.append(oi)
+    inst_arr = (OrcInstance * max(1, len(insts)))(*insts)
+    lights = (OrcLight * max(1, len(spec.lights)))()
+    for i, l in enumerate(spec.lights):
+        lights[i].type = 0 if l.type == "directional" else 1
+        lights[i].direction = (C.c_float * 3)(*map(float, l.direction))
+        lights[i].position = (C.c_float * 3)(*map(float, l.position))
+        rad = [float(np.float32(c) * np.float32(l.irradiance)) for c in l.color]
+        lights[i].radiance = (C.c_float * 3)(*rad)
+    vols = (OrcVolume * max(1, len(spec.volumes)))()
+    for i, v in enumerate(spec.volumes):
+        f = np.ascontiguousarray(v.field, np.float32)
+        keep.append(f)
+        o = vols[i]
+        o.field = _ptr(f)
+        o.dims = (C.c_int * 3)(f.shape[2], f.shape[1], f.shape[0])
+        o.origin = (C.c_float * 3)(*map(float, v.origin))
+        o.spacing = (C.c_float * 3)(*map(float, v.spacing))
+        o.filterLinear = int(v.filter != "nearest")
+        if v.color is not None or v.opacity is not None:
+            tf = discretize_tf(v.color, v.opacity, v.value_range,
+                               v.uniform_opacity)
+            keep.append(tf)
+            o.tf = _ptr(tf)
+        o.valueRange = (C.c_float * 2)(*map(float, v.value_range))
+        o.unitDistance = v.unit_distance
+        o.uniformColor = (C.c_float * 3)(*map(float, v.uniform_color))
+        o.uniformOpacity = v.uniform_opacity
+        o.id = v.id & 0xFFFFFFFF
+        o.instId = spec.world_id & 0xFFFFFFFF
+        o.xfm = _rows(np.eye(4))
+    scene = OrcScene(C.cast(surfs, C.c_void_p), len(spec.surfaces), C.cast(inst_arr, C.c_void_p),
+                     len(insts), C.cast(lights, C.c_void_p), len(spec.lights),
+                     C.cast(vols, C.c_void_p), len(spec.volumes))
+    keep += [surfs, inst_arr, lights, vols]
+    return keep, scene
+
+
+def _render_prepared(lib, handle, spec, frame_id, rows, volume_mode, tex_round, threads, accum,
+                     depth):
+    c = spec.camera
+    cam = OrcCamera()
+    cam.type = 0 if c.type == "perspective" else 1
+    cam.position = (C.c_float * 3)(*map(float, c.position))
+    cam.direction = (C.c_float * 3)(*map(float, c.direction))
+    cam.up = (C.c_float * 3)(*map(float, c.up))
+    cam.fovy = c.fovy
+    cam.aspect = c.aspect
+    cam.height = c.height
+    cam.imageRegion = (C.c_float * 4)(*map(float, c.region))
+    cam.apertureRadius = c.aperture
+    cam.focusDistance = c.focus
+    r = spec.renderer
+    ren = OrcRenderer()
+    ren.type = _RENDERERS[r.subtype]
+    ren.background = (C.c_float * 4)(*map(float, r.background))
+    ren.ambientColor = (C.c_float * 3)(*map(float, r.ambient_color))
+    ren.ambientRadiance = r.resolved_ambient()
+    ren.occlusionDistance = r.ao_distance
+    ren.cullTriangleBackfaces = int(bool(r.cull))
+    ren.volumeSamplingRate = r.volume_sampling_rate
+    ren.pixelSamples = r.pixel_samples
+    ren.ambientSamples = r.ambient_samples if ren.type in (0, 2) else 0
+    ren.maxDepth = r.max_depth
+    W, H = spec.width, spec.height
+    out = {
+        "accum": np.zeros((H, W, 4), np.float32) if accum is None else accum,
+        "color": np.zeros((H, W), np.uint32),
+        "depth": np.full((H, W), np.finfo(np.float32).max, np.float32) if depth is None else depth,
+        "primitiveId": np.zeros((H, W), np.uint32),
+        "objectId": np.zeros((H, W), np.uint32),
+        "instanceId": np.zeros((H, W), np.uint32),
+    }
+    fr = OrcFrame()
+    fr.width, fr.height, fr.frameID, fr.colorFormat = W, H, frame_id, 0
+    fr.rowBegin, fr.rowEnd = (0, H) if rows is None else rows
+    fr.accum = _ptr(out["accum"])
+    fr.color = _ptr(out["color"])
+    fr.depth = _ptr(out["depth"])
+    fr.primId = _ptr(out["primitiveId"])
+    fr.objId = _ptr(out["objectId"])
+    fr.instId = _ptr(out["instanceId"])
+    rc = lib.orc_render_prepared(handle, C.byref(cam), C.byref(ren), C.byref(fr),
+                                 C.c_int(volume_mode), C.c_int(tex_round), C.c_int(threads))
+    assert rc == 0
+    out["rays"] = int(fr.raysTraced)
+    return out
+
+
+def philox_stream(seed: int, subsequence: int, offset: int, kind: int, n: int) -> np.ndarray:
+    lib = load()
+    out = np.zeros(n, np.uint32 if kind == 0 else np.float32)
+    lib.orc_philox_stream(C.c_uint64(seed), C.c_uint64(subsequence), C.c_uint64(offset),
+                          C.c_int(kind), C.c_int(n), _ptr(out))
+    return out
+
+
+def philox_block(ctr, key) -> np.ndarray:
+    lib = load()
+    c = np.asarray(ctr, np.uint32)
+    k = np.asarray(key, np.uint32)
+    out = np.zeros(4, np.uint32)
+    lib.orc_philox4x32_10(_ptr(c), _ptr(k), _ptr(out))
+    return out
+
+
+def tex1d(table: np.ndarray, coord: float, round_mode: int = 1) -> np.ndarray:
+    lib = load()
+    t = np.ascontiguousarray(table, np.float32)
+    comps = t.shape[1] if t.ndim == 2 else 1
+    out = np.zeros(comps, np.float32)
+    lib.orc_tex1d(_ptr(t), C.c_int(len(t)), C.c_int(comps), C.c_float(coord), C.c_int(round_mode),
+                  _ptr(out))
+    return out
+
+
+def tex3d(vox: np.ndarray, coord, round_mode: int = 1) -> float:
+    lib = load()
+    v = np.ascontiguousarray(vox, np.float32)
+    dims = np.array([v.shape[2], v.shape[1], v.shape[0]], np.int32)
+    c = np.asarray(coord, np.float32)
+    return float(lib.orc_tex3d(_ptr(v), _ptr(dims), _ptr(c), C.c_int(round_mode)))
+
+
+def bvh8_count(nodes: bytes, tris: bytes, rays: np.ndarray):
+    lib = load()
+    nb = np.frombuffer(nodes, np.uint8)
+    tb = np.frombuffer(tris, np.uint8)
+    r = np.ascontiguousarray(rays, np.float32)
+    nv, pt = C.c_uint64(), C.c_uint64()
+    th = np.zeros(len(r), np.float32)
+    lib.orc_bvh8_count(_ptr(nb), _ptr(tb), _ptr(r), C.c_int(len(r)), C.byref(nv), C.byref(pt),
+                       _ptr(th))
+    return int(nv.value), int(pt.value), th
+
+
+def dm(density: np.ndarray, tf: np.ndarray, view: dict, opacity_scale: float, step: float,
+       unit: float = 1.0, value_range=(0.0, 1.0), grad_image: np.ndarray | None = None,
+       threads: int = 0):
+    """FP64 forward (and adjoint when grad_image is given) of the
+    differentiable marcher for one view. density: (nz, ny, nx); view:
+    width, height, eye, d00, du, dv, background (voxel space)."""
+    lib = load()
+    d = np.ascontiguousarray(density, np.float64)
+    t = np.ascontiguousarray(tf, np.float64)
+    ov = OrcDMVolume(_ptr(d), (C.c_int * 3)(d.shape[2], d.shape[1], d.shape[0]), _ptr(t), len(t),
+                     opacity_scale, step, unit, value_range[0], value_range[1])
+    vw = OrcDMView()
+    vw.width, vw.height = view["width"], view["height"]
+    for k in ("eye", "d00", "du", "dv", "background"):
+        setattr(vw, k, (C.c_double * 3)(*map(float, view[k])))
+    img = np.zeros((view["height"], view["width"], 3), np.float64)
+    gD = gT = gS = None
+    if grad_image is not None:
+        g = np.ascontiguousarray(grad_image, np.float64)
+        gD = np.zeros_like(d)
+        gT = np.zeros_like(t)
+        gS = np.zeros(1, np.float64)
+        lib.orc_dm(C.byref(ov), C.byref(vw), _ptr(img), _ptr(g), _ptr(gD), _ptr(gT), _ptr(gS),
+                   C.c_int(threads))
+        return img, gD, gT, float(gS[0])
+    lib.orc_dm(C.byref(ov), C.byref(vw), _ptr(img), None, None, None, None, C.c_int(threads))
+    return img

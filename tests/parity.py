@@ -1,0 +1,73 @@
+"""Comparison helpers for GPU-vs-oracle parity tests.
+
+Tolerances follow the stated bar: primitiveId/objectId/instanceId
+bit-exact except for at most `id_frac` of pixels (grazing or tied hits),
+depth within 1e-5 relative, colour within `color_tol`/255 per channel.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from visrtx_gb300 import anari, scenes
+
+ID_FRAC = 1e-4
+DEPTH_REL = 1e-5
+
+
+def render_gpu(dev, spec: scenes.SceneSpec, frames: int = 1):
+    frame, world, keep = scenes.build_on_device(dev, spec)
+    for _ in range(frames):
+        frame.render()
+    frame.wait()
+    out = {ch: frame.map("channel." + ch)
+           for ch in ("color", "depth", "primitiveId", "objectId", "instanceId")}
+    out["frame"] = frame
+    out["world"] = world
+    out["keep"] = keep
+    return out
+
+
+def render_oracle(spec: scenes.SceneSpec, frames: int = 1, **kw):
+    from oracle import oracle as O
+
+    accum = None
+    depth = None
+    out = None
+    for f in range(frames):
+        out = O.render(spec, frame_id=f * max(1, spec.renderer.pixel_samples)
+                       if spec.renderer.subtype != "raycast" else f,
+                       accum=accum, depth=depth, **kw)
+        accum, depth = out["accum"], out["depth"]
+    return out
+
+
+def compare(gpu, ref, id_frac=ID_FRAC, depth_rel=DEPTH_REL, color_tol=1, allow_ids=0):
+    """Returns a report dict; raises AssertionError with details on failure."""
+    n = gpu["primitiveId"].size
+    idm = np.zeros(gpu["primitiveId"].shape, bool)
+    for ch in ("primitiveId", "objectId", "instanceId"):
+        idm |= gpu[ch] != ref[ch]
+    frac = idm.sum() / n
+    same = ~idm
+    hit = same & (ref["depth"] < 1e29)
+    drel = np.abs(gpu["depth"][hit].astype(np.float64) - ref["depth"][hit]) / np.maximum(
+        np.abs(ref["depth"][hit]), 1e-12)
+    bg_ok = np.all(gpu["depth"][same & (ref["depth"] >= 1e29)] == ref["depth"][same & (ref["depth"] >= 1e29)])
+    cg = anari.rgba8(gpu["color"]).astype(np.int32)
+    cr = anari.rgba8(ref["color"]).astype(np.int32)
+    cdiff = np.abs(cg - cr)[same]
+    rep = {
+        "pixels": n,
+        "id_mismatch": int(idm.sum()),
+        "id_frac": float(frac),
+        "depth_rel_max": float(drel.max()) if drel.size else 0.0,
+        "depth_rel_q999": float(np.quantile(drel, 0.999)) if drel.size else 0.0,
+        "color_max": int(cdiff.max()) if cdiff.size else 0,
+        "color_mean": float(cdiff.mean()) if cdiff.size else 0.0,
+        "color_frac_over": float((cdiff > color_tol).any(axis=-1).mean()) if cdiff.size else 0.0,
+    }
+    ok = (idm.sum() <= max(allow_ids, int(id_frac * n))
+          and rep["depth_rel_q999"] <= depth_rel and bg_ok
+          and rep["color_frac_over"] <= max(id_frac, allow_ids / n))
+    assert ok, f"parity failure: {rep}"
+    return rep

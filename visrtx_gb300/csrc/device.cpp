@@ -1,0 +1,2438 @@
+// libvrtx host side: object model, world build and the C ABI (include/vrtx.h).
+//
+// Mirrors the VisRTX device's object layer (devices/rtx/VisRTXDevice.cpp,
+// array/, camera/, frame/Frame.cu, renderer/Renderer.cpp, scene/) for the
+// hot path: same subtypes, parameter names, defaults and error behaviour
+// (status callback, null handles, skipped renders), with OptiX replaced by
+// the kernels of bvh.cu / scene.cu / render.cu.
+#include <algorithm>
+#include <array>
+#include <chrono>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <set>
+
+#include "objects.h"
+
+namespace vrtx {
+
+static std::atomic<uint64_t> g_stamp{1};
+uint64_t newStamp()
+{
+  return g_stamp.fetch_add(1) + 1;
+}
+
+size_t sizeOfType(int t)
+{
+  switch (t) {
+  case VRTX_BOOL:
+    return 4;
+  case VRTX_INT32:
+  case VRTX_UINT32:
+  case VRTX_FLOAT32:
+  case VRTX_DATA_TYPE:
+    return 4;
+  case VRTX_INT32_VEC2:
+  case VRTX_UINT32_VEC2:
+  case VRTX_FLOAT32_VEC2:
+  case VRTX_FLOAT32_BOX1:
+    return 8;
+  case VRTX_UINT32_VEC3:
+  case VRTX_FLOAT32_VEC3:
+    return 12;
+  case VRTX_UINT32_VEC4:
+  case VRTX_FLOAT32_VEC4:
+  case VRTX_FLOAT32_BOX2:
+    return 16;
+  case VRTX_FLOAT32_BOX3:
+    return 24;
+  case VRTX_FLOAT32_MAT3x4:
+    return 48;
+  case VRTX_FLOAT32_MAT4:
+    return 64;
+  case VRTX_FLOAT64:
+    return 8;
+  case VRTX_FLOAT64_BOX1:
+    return 16;
+  case VRTX_FIXED8:
+  case VRTX_UFIXED8:
+    return 1;
+  case VRTX_FIXED16:
+  case VRTX_UFIXED16:
+  case VRTX_FLOAT16:
+  case VRTX_BFLOAT16:
+    return 2;
+  case VRTX_UFIXED8_VEC4:
+  case VRTX_UFIXED8_RGBA_SRGB:
+    return 4;
+  case VRTX_VOID_POINTER:
+  case VRTX_FUNCTION_POINTER:
+  case VRTX_MEMORY_DELETER:
+    return sizeof(void *);
+  default:
+    if (isObjectType(t))
+      return sizeof(void *);
+    return 0;
+  }
+}
+
+bool isObjectType(int t)
+{
+  return t >= VRTX_OBJECT && t <= VRTX_WORLD;
+}
+
+const char *typeName(int t)
+{
+  switch (t) {
+  case VRTX_CAMERA:
+    return "ANARICamera";
+  case VRTX_FRAME:
+    return "ANARIFrame";
+  case VRTX_GEOMETRY:
+    return "ANARIGeometry";
+  case VRTX_GROUP:
+    return "ANARIGroup";
+  case VRTX_INSTANCE:
+    return "ANARIInstance";
+  case VRTX_LIGHT:
+    return "ANARILight";
+  case VRTX_MATERIAL:
+    return "ANARIMaterial";
+  case VRTX_RENDERER:
+    return "ANARIRenderer";
+  case VRTX_SURFACE:
+    return "ANARISurface";
+  case VRTX_SPATIAL_FIELD:
+    return "ANARISpatialField";
+  case VRTX_VOLUME:
+    return "ANARIVolume";
+  case VRTX_WORLD:
+    return "ANARIWorld";
+  case VRTX_ARRAY1D:
+  case VRTX_ARRAY2D:
+  case VRTX_ARRAY3D:
+    return "ANARIArray";
+  default:
+    return "ANARIObject";
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Device
+// ---------------------------------------------------------------------------
+
+void Device::report(const Object *src, int severity, const char *msg)
+{
+  if (cb)
+    cb(cbPtr,
+        reinterpret_cast<VRTXDevice>(this),
+        reinterpret_cast<VRTXObject>(const_cast<Object *>(src)),
+        src ? src->type : 0,
+        severity,
+        0,
+        msg);
+}
+
+// Lazy CUDA init (VisRTXDevice::initDevice, VisRTXDevice.cpp:435-458).
+bool Device::init()
+{
+  std::lock_guard<std::recursive_mutex> lock(mutex);
+  if (initTried)
+    return initOk;
+  initTried = true;
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+    cudaGetLastError();
+    report(nullptr,
+        VRTX_SEVERITY_FATAL_ERROR,
+        "no CUDA device found: libvrtx has no CPU path");
+    return false;
+  }
+  if (cudaDevice < 0 || cudaDevice >= n) {
+    report(nullptr, VRTX_SEVERITY_FATAL_ERROR, "invalid 'cudaDevice'");
+    return false;
+  }
+  if (cudaSetDevice(cudaDevice) != cudaSuccess
+      || cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking)
+          != cudaSuccess) {
+    report(nullptr, VRTX_SEVERITY_FATAL_ERROR, "CUDA initialisation failed");
+    return false;
+  }
+  cudaDeviceGetAttribute(&numSMs, cudaDevAttrMultiProcessorCount, cudaDevice);
+  // keep freed stream-ordered memory in the pool between frames
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, cudaDevice) == cudaSuccess) {
+    uint64_t thresh = ~0ull;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thresh);
+  }
+  initOk = true;
+  return true;
+}
+
+// ---------------------------------------------------------------------------
+// Object
+// ---------------------------------------------------------------------------
+
+Object::Object(Device *d, int t, const std::string &st)
+    : dev(d), type(t), subtype(st)
+{}
+
+Object::~Object()
+{
+  for (auto &p : pending)
+    if (p.second.obj)
+      releaseObj(p.second.obj);
+  for (auto &p : params)
+    if (p.second.obj)
+      releaseObj(p.second.obj);
+}
+
+void retainObj(Object *o)
+{
+  if (o)
+    o->refs++;
+}
+
+void releaseObj(Object *o)
+{
+  if (o && --o->refs == 0) {
+    Device *d = o->dev;
+    {
+      std::lock_guard<std::recursive_mutex> lock(d->mutex);
+      auto it = std::find(d->live.begin(), d->live.end(), o);
+      if (it != d->live.end())
+        d->live.erase(it);
+    }
+    delete o;
+  }
+}
+
+void Object::report(int severity, const char *fmt, ...) const
+{
+  char buf[1024];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  dev->report(this, severity, buf);
+}
+
+void Object::setParam(const std::string &name, int t, const void *mem)
+{
+  Param p;
+  p.type = t;
+  if (isObjectType(t)) {
+    Object *o = mem ? *reinterpret_cast<Object *const *>(mem) : nullptr;
+    retainObj(o);
+    p.obj = o;
+  } else if (t == VRTX_STRING) {
+    p.str = mem ? (const char *)mem : "";
+  } else {
+    const size_t sz = sizeOfType(t);
+    if (sz == 0 || !mem) {
+      report(VRTX_SEVERITY_WARNING,
+          "ignoring parameter '%s' of unsupported type %d",
+          name.c_str(),
+          t);
+      return;
+    }
+    p.bytes.resize(sz);
+    std::memcpy(p.bytes.data(), mem, sz);
+  }
+  auto it = pending.find(name);
+  if (it != pending.end() && it->second.obj)
+    releaseObj(it->second.obj);
+  pending[name] = std::move(p);
+}
+
+void Object::unsetParam(const std::string &name)
+{
+  auto it = pending.find(name);
+  if (it == pending.end())
+    return;
+  if (it->second.obj)
+    releaseObj(it->second.obj);
+  pending.erase(it);
+}
+
+void Object::unsetAll()
+{
+  for (auto &p : pending)
+    if (p.second.obj)
+      releaseObj(p.second.obj);
+  pending.clear();
+}
+
+void Object::commitParams()
+{
+  for (auto &p : params)
+    if (p.second.obj)
+      releaseObj(p.second.obj);
+  params = pending;
+  for (auto &p : params)
+    if (p.second.obj)
+      retainObj(p.second.obj);
+  commitStamp = newStamp();
+  commit();
+  dev->markChanged();
+}
+
+bool Object::has(const std::string &name, int t) const
+{
+  auto it = params.find(name);
+  return it != params.end() && it->second.type == t;
+}
+
+Object *Object::getObject(const std::string &name, int t) const
+{
+  auto it = params.find(name);
+  if (it == params.end() || !it->second.obj)
+    return nullptr;
+  Object *o = it->second.obj;
+  if (t == VRTX_OBJECT || o->type == t)
+    return o;
+  if ((t == VRTX_ARRAY1D || t == VRTX_ARRAY2D || t == VRTX_ARRAY3D)
+      && o->type == t)
+    return o;
+  return nullptr;
+}
+
+std::string Object::getString(const std::string &name, const std::string &def) const
+{
+  auto it = params.find(name);
+  if (it == params.end() || it->second.type != VRTX_STRING)
+    return def;
+  return it->second.str;
+}
+
+bool Object::getProperty(
+    const std::string &name, int t, void *mem, uint64_t size, uint32_t)
+{
+  if (name == "valid" && t == VRTX_BOOL && size >= 4) {
+    int32_t v = isValid() ? 1 : 0;
+    std::memcpy(mem, &v, 4);
+    return true;
+  }
+  return false;
+}
+
+// ---------------------------------------------------------------------------
+// Array (array/Array.cpp:38-297)
+// ---------------------------------------------------------------------------
+
+Array::Array(Device *d,
+    int dims,
+    const void *mem,
+    VRTXMemoryDeleter del,
+    const void *delPtr,
+    int et,
+    uint64_t n1,
+    uint64_t n2,
+    uint64_t n3)
+    : Object(d,
+          dims == 1 ? VRTX_ARRAY1D : (dims == 2 ? VRTX_ARRAY2D : VRTX_ARRAY3D)),
+      elemType(et),
+      n{n1, n2, n3},
+      appMem(mem),
+      deleter(del),
+      deleterPtr(delPtr)
+{
+  if (!appMem)
+    owned.resize(bytes());
+  else if (d->initOk) {
+    // NV_ARRAY_CUDA: application device pointers are used in place
+    cudaPointerAttributes attr{};
+    if (cudaPointerGetAttributes(&attr, appMem) == cudaSuccess
+        && (attr.type == cudaMemoryTypeDevice
+            || attr.type == cudaMemoryTypeManaged))
+      appIsDevice = true;
+    cudaGetLastError();
+  }
+  dataStamp = newStamp();
+  refreshHandles();
+}
+
+Array::~Array()
+{
+  for (auto *h : handles)
+    releaseObj(h);
+  if (dptr && devBytes)
+    cudaFree(dptr);
+  if (deleter && appMem)
+    deleter(deleterPtr, appMem);
+}
+
+const void *Array::hostData() const
+{
+  if (appIsDevice)
+    return nullptr;
+  return appMem ? appMem : owned.data();
+}
+
+const void *Array::deviceData()
+{
+  if (appIsDevice)
+    return appMem;
+  if (!Object::dev->initOk)
+    return nullptr;
+  const size_t b = bytes();
+  if (b == 0)
+    return nullptr;
+  if (devStamp >= dataStamp && dptr)
+    return dptr;
+  if (devBytes < b) {
+    if (dptr)
+      cudaFree(dptr);
+    dptr = nullptr;
+    devBytes = 0;
+    if (cudaMalloc(&dptr, b) != cudaSuccess) {
+      report(VRTX_SEVERITY_ERROR, "device allocation of %zu bytes failed", b);
+      cudaGetLastError();
+      return nullptr;
+    }
+    devBytes = b;
+  }
+  cudaMemcpyAsync(
+      dptr, hostData(), b, cudaMemcpyHostToDevice, Object::dev->stream);
+  devStamp = dataStamp;
+  return dptr;
+}
+
+void *Array::map()
+{
+  if (appIsDevice)
+    return const_cast<void *>(appMem);
+  return const_cast<void *>(hostData());
+}
+
+void Array::unmap()
+{
+  dataStamp = newStamp();
+  refreshHandles();
+  Object::dev->markChanged();
+}
+
+void Array::privatize()
+{
+  if (!appMem || deleter || appIsDevice)
+    return;
+  owned.assign((const uint8_t *)appMem, (const uint8_t *)appMem + bytes());
+  appMem = nullptr;
+}
+
+void Array::refreshHandles()
+{
+  for (auto *h : handles)
+    releaseObj(h);
+  handles.clear();
+  if (!isObjectType(elemType) || appIsDevice)
+    return;
+  const Object *const *p = reinterpret_cast<const Object *const *>(hostData());
+  if (!p)
+    return;
+  for (uint64_t i = 0; i < count(); i++) {
+    Object *o = const_cast<Object *>(p[i]);
+    retainObj(o);
+    handles.push_back(o);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Camera (camera/Camera.cpp:68-76, Perspective.cpp:40-72,
+// Orthographic.cpp:38-52)
+// ---------------------------------------------------------------------------
+
+void Camera::commit()
+{
+  float region[4] = {0.f, 0.f, 1.f, 1.f};
+  if (has("imageRegion", VRTX_FLOAT32_BOX2))
+    std::memcpy(region, params["imageRegion"].bytes.data(), 16);
+  for (int i = 0; i < 4; i++)
+    gpu.region[i] = region[i];
+  gpu.pos = get<f3>("position", VRTX_FLOAT32_VEC3, f3{0.f, 0.f, 0.f});
+  gpu.dir = normalize(get<f3>("direction", VRTX_FLOAT32_VEC3, f3{0.f, 0.f, 1.f}));
+  const f3 up = normalize(get<f3>("up", VRTX_FLOAT32_VEC3, f3{0.f, 1.f, 0.f}));
+  const float aspect = get<float>("aspect", VRTX_FLOAT32, 1.f);
+  if (subtype == "orthographic") {
+    gpu.type = CAMERA_ORTHOGRAPHIC;
+    const float height = get<float>("height", VRTX_FLOAT32, 1.f);
+    const float sx = height * aspect, sy = height;
+    gpu.posDu = normalize(cross(gpu.dir, up)) * sx;
+    gpu.posDv = normalize(cross(gpu.posDu, gpu.dir)) * sy;
+    gpu.pos00 = gpu.pos - 0.5f * gpu.posDu - 0.5f * gpu.posDv;
+  } else {
+    if (subtype != "perspective")
+      report(VRTX_SEVERITY_WARNING,
+          "unknown camera subtype '%s', using perspective",
+          subtype.c_str());
+    gpu.type = CAMERA_PERSPECTIVE;
+    const float fovy =
+        get<float>("fovy", VRTX_FLOAT32, 60.f * float(M_PI) / 180.f);
+    const float ipy = 2.f * tanf(0.5f * fovy);
+    const float ipx = ipy * aspect;
+    f3 du = normalize(cross(gpu.dir, up)) * ipx;
+    f3 dv = normalize(cross(du, gpu.dir)) * ipy;
+    f3 d00 = gpu.dir - .5f * du - .5f * dv;
+    const float focusDistance = get<float>("focusDistance", VRTX_FLOAT32, 1.f);
+    const float apertureRadius =
+        get<float>("apertureRadius", VRTX_FLOAT32, 0.f) / (ipx * focusDistance);
+    if (apertureRadius > 0.f) {
+      du *= focusDistance;
+      dv *= focusDistance;
+      d00 *= focusDistance;
+    }
+    gpu.dirDu = du;
+    gpu.dirDv = dv;
+    gpu.dir00 = d00;
+    gpu.scaledAperture = apertureRadius;
+    gpu.aspect = aspect;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Geometry (scene/surface/geometry/Triangle.cpp:42-175, Sphere.cu:40-115)
+// ---------------------------------------------------------------------------
+
+static Array *arrayParam(Object *o, const char *name, int elemType)
+{
+  auto *a = static_cast<Array *>(o->getObject(name, VRTX_ARRAY1D));
+  if (!a)
+    return nullptr;
+  if (a->elemType != elemType) {
+    o->report(VRTX_SEVERITY_WARNING,
+        "'%s' array has element type %d, expected %d; ignored",
+        name,
+        a->elemType,
+        elemType);
+    return nullptr;
+  }
+  return a;
+}
+
+void Geometry::commit()
+{
+  vertex = arrayParam(this, "vertex.position", VRTX_FLOAT32_VEC3);
+  if (subtype == "sphere") {
+    index = arrayParam(this, "primitive.index", VRTX_UINT32);
+    radius = arrayParam(this, "vertex.radius", VRTX_FLOAT32);
+    globalRadius = get<float>("radius", VRTX_FLOAT32, 0.01f);
+    normal = normalFV = nullptr;
+    numPrims = index ? (uint32_t)index->count()
+                     : (vertex ? (uint32_t)vertex->count() : 0);
+  } else {
+    if (subtype != "triangle")
+      report(VRTX_SEVERITY_WARNING,
+          "geometry subtype '%s' is not supported by this device",
+          subtype.c_str());
+    index = arrayParam(this, "primitive.index", VRTX_UINT32_VEC3);
+    normal = arrayParam(this, "vertex.normal", VRTX_FLOAT32_VEC3);
+    normalFV = arrayParam(this, "faceVarying.normal", VRTX_FLOAT32_VEC3);
+    radius = nullptr;
+    cull = get<int32_t>("cullBackfaces", VRTX_BOOL, 0) != 0;
+    numPrims = index ? (uint32_t)index->count()
+                     : (vertex ? (uint32_t)(vertex->count() / 3) : 0);
+  }
+  primId = arrayParam(this, "primitive.id", VRTX_UINT32);
+  if (!vertex)
+    report(VRTX_SEVERITY_WARNING,
+        "missing required parameter 'vertex.position' on %s geometry",
+        subtype.c_str());
+}
+
+bool Geometry::isValid() const
+{
+  return vertex != nullptr && (subtype == "triangle" || subtype == "sphere");
+}
+
+uint64_t Geometry::deepStamp() const
+{
+  uint64_t s = commitStamp;
+  for (const Array *a : {vertex, index, normal, normalFV, primId, radius})
+    if (a)
+      s = std::max(s, a->deepStamp());
+  return s;
+}
+
+GeometryGPU Geometry::gpuData()
+{
+  GeometryGPU g{};
+  g.type = (uint32_t)geomClass();
+  g.numPrims = numPrims;
+  g.vertices = vertex ? (const f3 *)vertex->deviceData() : nullptr;
+  g.indices = index ? (const uint32_t *)index->deviceData() : nullptr;
+  g.normals = normal ? (const f3 *)normal->deviceData() : nullptr;
+  g.normalsFV = normalFV ? (const f3 *)normalFV->deviceData() : nullptr;
+  g.primIds = primId ? (const uint32_t *)primId->deviceData() : nullptr;
+  g.radii = radius ? (const float *)radius->deviceData() : nullptr;
+  g.radius = globalRadius;
+  g.cullBackfaces = cull ? 1u : 0u;
+  return g;
+}
+
+// ---------------------------------------------------------------------------
+// Material (Matte.cpp:39-53) and Light (Directional.cpp:38-55, Light.cpp)
+// ---------------------------------------------------------------------------
+
+void Material::commit()
+{
+  if (subtype != "matte")
+    report(VRTX_SEVERITY_WARNING,
+        "material subtype '%s' is evaluated as matte",
+        subtype.c_str());
+  float c[4] = {0.8f, 0.8f, 0.8f, 1.f};
+  if (has("color", VRTX_FLOAT32_VEC4))
+    std::memcpy(c, params["color"].bytes.data(), 16);
+  else if (has("color", VRTX_FLOAT32_VEC3))
+    std::memcpy(c, params["color"].bytes.data(), 12);
+  gpu.color = f3{c[0], c[1], c[2]};
+  gpu.opacity = c[3] * get<float>("opacity", VRTX_FLOAT32, 1.f);
+  gpu.cutoff = get<float>("alphaCutoff", VRTX_FLOAT32, 0.5f);
+  const std::string mode = getString("alphaMode", "opaque");
+  gpu.alphaMode = mode == "blend" ? ALPHA_BLEND
+                                  : (mode == "mask" ? ALPHA_MASK : ALPHA_OPAQUE);
+}
+
+void Light::commit()
+{
+  const f3 color = get<f3>("color", VRTX_FLOAT32_VEC3, f3{1.f, 1.f, 1.f});
+  if (subtype == "point") {
+    gpu.type = LIGHT_POINT;
+    gpu.position = get<f3>("position", VRTX_FLOAT32_VEC3, f3{0.f, 0.f, 0.f});
+    gpu.radiance = color * std::max(0.f, get<float>("intensity", VRTX_FLOAT32, 1.f));
+  } else {
+    if (subtype != "directional")
+      report(VRTX_SEVERITY_WARNING,
+          "light subtype '%s' is not supported; using directional",
+          subtype.c_str());
+    gpu.type = LIGHT_DIRECTIONAL;
+    const f3 d =
+        normalize(get<f3>("direction", VRTX_FLOAT32_VEC3, f3{0.f, 0.f, -1.f}));
+    const float irr = std::min(std::max(get<float>("irradiance", VRTX_FLOAT32, 1.f), 0.f),
+        3.402823466e+38f);
+    gpu.dirToLight = -d; // transformed per instance at world build
+    gpu.radiance = color * irr;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Surface (Surface.cpp:41-118)
+// ---------------------------------------------------------------------------
+
+void Surface::commit()
+{
+  id = get<uint32_t>("id", VRTX_UINT32, ~0u);
+  geometry = static_cast<Geometry *>(getObject("geometry", VRTX_GEOMETRY));
+  material = static_cast<Material *>(getObject("material", VRTX_MATERIAL));
+  if (!material)
+    report(VRTX_SEVERITY_WARNING, "missing 'material' on ANARISurface");
+  if (!geometry)
+    report(VRTX_SEVERITY_WARNING, "missing 'geometry' on ANARISurface");
+}
+
+bool Surface::isValid() const
+{
+  return geometry && material && geometry->isValid();
+}
+
+uint64_t Surface::deepStamp() const
+{
+  uint64_t s = commitStamp;
+  if (geometry)
+    s = std::max(s, geometry->deepStamp());
+  if (material)
+    s = std::max(s, material->commitStamp);
+  return s;
+}
+
+// ---------------------------------------------------------------------------
+// Group / Instance
+// ---------------------------------------------------------------------------
+
+static Array *objectArrayParam(Object *o, const char *name)
+{
+  auto *a = static_cast<Array *>(o->getObject(name, VRTX_ARRAY1D));
+  if (a && !isObjectType(a->elemType))
+    return nullptr;
+  return a;
+}
+
+void Group::commit()
+{
+  surfaces = objectArrayParam(this, "surface");
+  volumes = objectArrayParam(this, "volume");
+  lights = objectArrayParam(this, "light");
+}
+
+template <typename T>
+static std::vector<T *> validOf(Array *a, int type)
+{
+  std::vector<T *> out;
+  if (!a)
+    return out;
+  for (Object *o : a->handles)
+    if (o && o->type == type && o->isValid())
+      out.push_back(static_cast<T *>(o));
+  return out;
+}
+
+std::vector<Surface *> Group::validSurfaces() const
+{
+  return validOf<Surface>(surfaces, VRTX_SURFACE);
+}
+std::vector<Volume *> Group::validVolumes() const
+{
+  return validOf<Volume>(volumes, VRTX_VOLUME);
+}
+std::vector<Light *> Group::validLights() const
+{
+  return validOf<Light>(lights, VRTX_LIGHT);
+}
+
+uint64_t Group::deepStamp() const
+{
+  uint64_t s = commitStamp;
+  for (Array *a : {surfaces, volumes, lights}) {
+    if (!a)
+      continue;
+    s = std::max(s, a->deepStamp());
+    for (Object *o : a->handles)
+      if (o)
+        s = std::max(s, o->deepStamp());
+  }
+  return s;
+}
+
+bool Group::getProperty(
+    const std::string &name, int t, void *mem, uint64_t size, uint32_t mask)
+{
+  return Object::getProperty(name, t, mem, size, mask);
+}
+
+void Instance::commit()
+{
+  group = static_cast<Group *>(getObject("group", VRTX_GROUP));
+  xfmArray = static_cast<Array *>(getObject("transform", VRTX_ARRAY1D));
+  if (xfmArray && xfmArray->elemType != VRTX_FLOAT32_MAT4) {
+    report(VRTX_SEVERITY_WARNING,
+        "'transform' array elements need to be FLOAT32_MAT4");
+    xfmArray = nullptr;
+  }
+  idArray = static_cast<Array *>(getObject("id", VRTX_ARRAY1D));
+  if (idArray && idArray->elemType != VRTX_UINT32) {
+    report(VRTX_SEVERITY_WARNING, "'id' array elements need to be UINT32");
+    idArray = nullptr;
+  }
+  id = get<uint32_t>("id", VRTX_UINT32, ~0u);
+  const float identity[12] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0};
+  std::memcpy(xfm, identity, sizeof(xfm));
+  if (has("transform", VRTX_FLOAT32_MAT4)) {
+    const float *m = reinterpret_cast<const float *>(params["transform"].bytes.data());
+    for (int r = 0; r < 3; r++)
+      for (int c = 0; c < 4; c++)
+        xfm[r * 4 + c] = m[c * 4 + r];
+  } else if (has("transform", VRTX_FLOAT32_MAT3x4)) {
+    const float *m = reinterpret_cast<const float *>(params["transform"].bytes.data());
+    for (int r = 0; r < 3; r++)
+      for (int c = 0; c < 4; c++)
+        xfm[r * 4 + c] = m[c * 3 + r];
+  }
+  if (!group)
+    report(VRTX_SEVERITY_WARNING, "missing 'group' on ANARIInstance");
+}
+
+uint64_t Instance::deepStamp() const
+{
+  uint64_t s = commitStamp;
+  if (group)
+    s = std::max(s, group->deepStamp());
+  if (xfmArray)
+    s = std::max(s, xfmArray->deepStamp());
+  if (idArray)
+    s = std::max(s, idArray->deepStamp());
+  return s;
+}
+
+size_t Instance::numTransforms() const
+{
+  return xfmArray ? (size_t)xfmArray->count() : 1;
+}
+
+void Instance::transform(size_t i, float out[12]) const
+{
+  if (xfmArray) {
+    const float *m =
+        reinterpret_cast<const float *>(xfmArray->hostData()) + 16 * i;
+    for (int r = 0; r < 3; r++)
+      for (int c = 0; c < 4; c++)
+        out[r * 4 + c] = m[c * 4 + r];
+  } else
+    std::memcpy(out, xfm, sizeof(xfm));
+}
+
+uint32_t Instance::userID(size_t i) const
+{
+  if (xfmArray && idArray && i < idArray->count())
+    return reinterpret_cast<const uint32_t *>(idArray->hostData())[i];
+  return id;
+}
+
+static void invertAffine(const float m[12], xfm34 &out)
+{
+  const double a = m[0], b = m[1], c = m[2], d = m[4], e = m[5], f = m[6],
+               g = m[8], h = m[9], k = m[10];
+  const double A = e * k - f * h, B = -(d * k - f * g), C = d * h - e * g;
+  double det = a * A + b * B + c * C;
+  if (det == 0.0)
+    det = 1e-30;
+  const double inv[3][3] = {{A / det, -(b * k - c * h) / det, (b * f - c * e) / det},
+      {B / det, (a * k - c * g) / det, -(a * f - c * d) / det},
+      {C / det, -(a * h - b * g) / det, (a * e - b * d) / det}};
+  const double t[3] = {m[3], m[7], m[11]};
+  for (int r = 0; r < 3; r++) {
+    for (int cc = 0; cc < 3; cc++)
+      out.r[r][cc] = (float)inv[r][cc];
+    out.r[r][3] =
+        (float)(-(inv[r][0] * t[0] + inv[r][1] * t[1] + inv[r][2] * t[2]));
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Spatial field (StructuredRegularField.cpp:64-192)
+// ---------------------------------------------------------------------------
+
+SpatialField::~SpatialField()
+{
+  cleanup();
+}
+
+void SpatialField::cleanup()
+{
+  if (tex)
+    cudaDestroyTextureObject(tex);
+  if (pointTex)
+    cudaDestroyTextureObject(pointTex);
+  if (cuArray)
+    cudaFreeArray(cuArray);
+  if (ranges)
+    cudaFree(ranges);
+  tex = pointTex = 0;
+  cuArray = nullptr;
+  ranges = nullptr;
+  builtStamp = 0;
+}
+
+void SpatialField::commit()
+{
+  if (subtype != "structuredRegular")
+    report(VRTX_SEVERITY_WARNING,
+        "spatial field subtype '%s' is not supported",
+        subtype.c_str());
+  origin = get<f3>("origin", VRTX_FLOAT32_VEC3, f3{0.f, 0.f, 0.f});
+  spacing = get<f3>("spacing", VRTX_FLOAT32_VEC3, f3{1.f, 1.f, 1.f});
+  filter = getString("filter", "linear");
+  data = static_cast<Array *>(getObject("data", VRTX_ARRAY3D));
+  if (!data)
+    report(VRTX_SEVERITY_WARNING,
+        "missing required parameter 'data' on structuredRegular spatial field");
+  builtStamp = 0;
+}
+
+static bool validFieldType(int t)
+{
+  return t == VRTX_FIXED8 || t == VRTX_UFIXED8 || t == VRTX_FIXED16
+      || t == VRTX_UFIXED16 || t == VRTX_FLOAT32;
+}
+
+bool SpatialField::isValid() const
+{
+  return data && validFieldType(data->elemType);
+}
+
+uint64_t SpatialField::deepStamp() const
+{
+  return std::max(commitStamp, data ? data->deepStamp() : 0);
+}
+
+box3 SpatialField::bounds() const
+{
+  if (!isValid())
+    return box3{{0.f, 0.f, 0.f}, {1.f, 1.f, 1.f}};
+  return box3{origin,
+      origin
+          + f3{(float(data->n[0]) - 1.f) * spacing.x,
+              (float(data->n[1]) - 1.f) * spacing.y,
+              (float(data->n[2]) - 1.f) * spacing.z}};
+}
+
+float SpatialField::stepSize() const
+{
+  return std::min(spacing.x / 2.f, std::min(spacing.y / 2.f, spacing.z / 2.f));
+}
+
+bool SpatialField::ensureBuilt()
+{
+  if (!isValid())
+    return false;
+  const uint64_t want = deepStamp();
+  if (builtStamp >= want && tex)
+    return true;
+  cleanup();
+  cudaStream_t s = Object::dev->stream;
+  const int et = data->elemType;
+  dims[0] = (int)data->n[0];
+  dims[1] = (int)data->n[1];
+  dims[2] = (int)data->n[2];
+  const int bits = (int)sizeOfType(et) * 8;
+  const cudaChannelFormatKind kind = et == VRTX_FLOAT32
+      ? cudaChannelFormatKindFloat
+      : ((et == VRTX_UFIXED8 || et == VRTX_UFIXED16)
+              ? cudaChannelFormatKindUnsigned
+              : cudaChannelFormatKindSigned);
+  cudaChannelFormatDesc desc = cudaCreateChannelDesc(bits, 0, 0, 0, kind);
+  if (cudaMalloc3DArray(&cuArray, &desc, make_cudaExtent(dims[0], dims[1], dims[2]))
+      != cudaSuccess) {
+    cudaGetLastError();
+    report(VRTX_SEVERITY_ERROR, "cudaMalloc3DArray failed for field data");
+    cuArray = nullptr;
+    return false;
+  }
+  cudaMemcpy3DParms cp{};
+  const void *src = data->deviceData();
+  cp.srcPtr = make_cudaPitchedPtr(const_cast<void *>(src),
+      dims[0] * sizeOfType(et),
+      dims[0],
+      dims[1]);
+  cp.dstArray = cuArray;
+  cp.extent = make_cudaExtent(dims[0], dims[1], dims[2]);
+  cp.kind = cudaMemcpyDeviceToDevice;
+  cudaMemcpy3DAsync(&cp, s);
+  cudaResourceDesc rd{};
+  rd.resType = cudaResourceTypeArray;
+  rd.res.array.array = cuArray;
+  cudaTextureDesc td{};
+  td.addressMode[0] = td.addressMode[1] = td.addressMode[2] = cudaAddressModeClamp;
+  td.filterMode = filter == "nearest" ? cudaFilterModePoint : cudaFilterModeLinear;
+  td.readMode = et == VRTX_FLOAT32 ? cudaReadModeElementType
+                                   : cudaReadModeNormalizedFloat;
+  td.normalizedCoords = 1;
+  cudaCreateTextureObject(&tex, &rd, &td, nullptr);
+  cudaTextureDesc tp = td;
+  tp.filterMode = cudaFilterModePoint;
+  tp.normalizedCoords = 0;
+  cudaCreateTextureObject(&pointTex, &rd, &tp, nullptr);
+  mcDims[0] = (dims[0] + 15) / 16;
+  mcDims[1] = (dims[1] + 15) / 16;
+  mcDims[2] = (dims[2] + 15) / 16;
+  const size_t cells = (size_t)mcDims[0] * mcDims[1] * mcDims[2];
+  if (cudaMalloc(&ranges, 2 * cells * sizeof(float)) != cudaSuccess) {
+    cudaGetLastError();
+    ranges = nullptr;
+    return false;
+  }
+  launchMacrocellRanges(pointTex, dims, mcDims, ranges, s);
+  builtStamp = want;
+  return cudaGetLastError() == cudaSuccess;
+}
+
+// ---------------------------------------------------------------------------
+// Volume: transferFunction1D / scivis (scene/volume/TransferFunction1D.cpp,
+// utility/colorMapHelpers.h)
+// ---------------------------------------------------------------------------
+
+Volume::~Volume()
+{
+  cleanup();
+}
+
+void Volume::cleanup()
+{
+  if (tfTex)
+    cudaDestroyTextureObject(tfTex);
+  if (tfArray)
+    cudaFreeArray(tfArray);
+  if (tfDev)
+    cudaFree(tfDev);
+  if (majorants)
+    cudaFree(majorants);
+  tfTex = 0;
+  tfArray = nullptr;
+  tfDev = nullptr;
+  majorants = nullptr;
+  builtStamp = 0;
+}
+
+void Volume::commit()
+{
+  if (subtype != "transferFunction1D" && subtype != "scivis")
+    report(VRTX_SEVERITY_WARNING,
+        "volume subtype '%s' is not supported",
+        subtype.c_str());
+  id = get<uint32_t>("id", VRTX_UINT32, ~0u);
+  field = static_cast<SpatialField *>(getObject("value", VRTX_SPATIAL_FIELD));
+  color = static_cast<Array *>(getObject("color", VRTX_ARRAY1D));
+  opacity = static_cast<Array *>(getObject("opacity", VRTX_ARRAY1D));
+  float uc[4] = {1.f, 1.f, 1.f, 1.f};
+  if (has("color", VRTX_FLOAT32_VEC3))
+    std::memcpy(uc, params["color"].bytes.data(), 12);
+  if (has("color", VRTX_FLOAT32_VEC4))
+    std::memcpy(uc, params["color"].bytes.data(), 16);
+  uniformColor = f3{uc[0], uc[1], uc[2]};
+  uniformColorW = uc[3];
+  uniformOpacity = get<float>("opacity", VRTX_FLOAT32, 1.f) * uc[3];
+  unitDistance = get<float>("unitDistance", VRTX_FLOAT32, 1.f);
+  if (has("valueRange", VRTX_FLOAT32_VEC2) || has("valueRange", VRTX_FLOAT32_BOX1)) {
+    const auto &b = params.count("valueRange") ? params["valueRange"].bytes
+                                               : std::vector<uint8_t>();
+    std::memcpy(valueRange, b.data(), 8);
+  }
+  if (has("valueRange", VRTX_FLOAT64_BOX1)) {
+    double d[2];
+    std::memcpy(d, params["valueRange"].bytes.data(), 16);
+    valueRange[0] = float(d[0]);
+    valueRange[1] = float(d[1]);
+  }
+  if (!field)
+    report(VRTX_SEVERITY_WARNING,
+        "missing parameter 'value' on transferFunction1D ANARIVolume");
+  builtStamp = 0;
+}
+
+bool Volume::isValid() const
+{
+  return field && field->isValid();
+}
+
+uint64_t Volume::deepStamp() const
+{
+  uint64_t s = commitStamp;
+  if (field)
+    s = std::max(s, field->deepStamp());
+  if (color)
+    s = std::max(s, color->deepStamp());
+  if (opacity)
+    s = std::max(s, opacity->deepStamp());
+  return s;
+}
+
+// position(v, r) (gpu_math.h): clamp, then (v - lo) * (1 / size)
+static float positionIn(float v, float lo, float hi)
+{
+  v = std::max(lo, std::min(v, hi));
+  return (v - lo) * (1.f / (hi - lo));
+}
+
+// generateLinearPositions (colorMapHelpers.h:43-61)
+static std::vector<float> linearPositions(size_t n, float lo, float hi)
+{
+  std::vector<float> p(n);
+  p.front() = 0.f;
+  p.back() = 1.f;
+  const float w = 1.f / float(n - 1);
+  for (size_t i = 1; i + 1 < n; i++)
+    p[i] = p[i - 1] + w;
+  for (auto &v : p)
+    v = v * (hi - lo) + lo;
+  return p;
+}
+
+// getInterpolatedValue (colorMapHelpers.h:63-73) on nc-component values
+static void interpolated(const float *values,
+    int nc,
+    const std::vector<float> &pos,
+    float lo,
+    float hi,
+    float p,
+    float *out)
+{
+  for (size_t i = 0; i + 1 < pos.size(); i++) {
+    const float a = positionIn(pos[i], lo, hi);
+    const float b = positionIn(pos[i + 1], lo, hi);
+    if (p >= a && p <= b) {
+      const float t = positionIn(p, a, b);
+      for (int c = 0; c < nc; c++)
+        out[c] = values[i * nc + c] * (1.f - t) + values[(i + 1) * nc + c] * t;
+      return;
+    }
+  }
+  const size_t k = p <= positionIn(pos[0], lo, hi) ? 0 : pos.size() - 1;
+  for (int c = 0; c < nc; c++)
+    out[c] = values[k * nc + c];
+}
+
+// discritizeTFData (TransferFunction1D.cpp:101-150): 256 entries,
+// entry = (rgb, c.w * o)
+void Volume::discretize()
+{
+  const int N = 256;
+  tf.assign(N * 4, 0.f);
+  const float lo = valueRange[0], hi = valueRange[1];
+  std::vector<float> cpos, opos;
+  const float *cvals = nullptr;
+  int cnc = 0;
+  if (color && color->count() >= 2
+      && (color->elemType == VRTX_FLOAT32_VEC3
+          || color->elemType == VRTX_FLOAT32_VEC4)) {
+    cpos = linearPositions(color->count(), lo, hi);
+    cvals = reinterpret_cast<const float *>(color->hostData());
+    cnc = color->elemType == VRTX_FLOAT32_VEC3 ? 3 : 4;
+  } else if (color)
+    report(VRTX_SEVERITY_WARNING, "unusable tf1D color array type set");
+  const float *ovals = nullptr;
+  if (opacity && opacity->count() >= 2 && opacity->elemType == VRTX_FLOAT32) {
+    opos = linearPositions(opacity->count(), lo, hi);
+    ovals = reinterpret_cast<const float *>(opacity->hostData());
+  }
+  for (int i = 0; i < N; i++) {
+    const float p = float(i) / float(N - 1);
+    float c[4] = {uniformColor.x, uniformColor.y, uniformColor.z, uniformColorW};
+    if (cvals) {
+      float v[4] = {0.f, 0.f, 0.f, 1.f};
+      interpolated(cvals, cnc, cpos, lo, hi, p, v);
+      c[0] = v[0];
+      c[1] = v[1];
+      c[2] = v[2];
+      c[3] = cnc == 4 ? v[3] : 1.f;
+    }
+    float o = uniformOpacity;
+    if (ovals)
+      interpolated(ovals, 1, opos, lo, hi, p, &o);
+    tf[4 * i + 0] = c[0];
+    tf[4 * i + 1] = c[1];
+    tf[4 * i + 2] = c[2];
+    tf[4 * i + 3] = c[3] * o;
+  }
+}
+
+bool Volume::ensureBuilt()
+{
+  if (!isValid() || !field->ensureBuilt())
+    return false;
+  const uint64_t want = deepStamp();
+  if (builtStamp >= want && majorants)
+    return true;
+  cleanup();
+  cudaStream_t s = Object::dev->stream;
+  const bool hasTF = color != nullptr || opacity != nullptr;
+  if (hasTF) {
+    discretize();
+    cudaChannelFormatDesc desc =
+        cudaCreateChannelDesc(32, 32, 32, 32, cudaChannelFormatKindFloat);
+    if (cudaMallocArray(&tfArray, &desc, 256) != cudaSuccess) {
+      cudaGetLastError();
+      tfArray = nullptr;
+      return false;
+    }
+    cudaMemcpy2DToArrayAsync(tfArray,
+        0,
+        0,
+        tf.data(),
+        256 * sizeof(float4),
+        256 * sizeof(float4),
+        1,
+        cudaMemcpyHostToDevice,
+        s);
+    cudaResourceDesc rd{};
+    rd.resType = cudaResourceTypeArray;
+    rd.res.array.array = tfArray;
+    cudaTextureDesc td{};
+    td.addressMode[0] = cudaAddressModeClamp;
+    td.filterMode = cudaFilterModeLinear;
+    td.readMode = cudaReadModeElementType;
+    td.normalizedCoords = 1;
+    cudaCreateTextureObject(&tfTex, &rd, &td, nullptr);
+    cudaMalloc(&tfDev, 256 * sizeof(float4));
+    cudaMemcpyAsync(
+        tfDev, tf.data(), 256 * sizeof(float4), cudaMemcpyHostToDevice, s);
+  }
+  const size_t cells =
+      (size_t)field->mcDims[0] * field->mcDims[1] * field->mcDims[2];
+  if (cudaMalloc(&majorants, cells * sizeof(float)) != cudaSuccess) {
+    cudaGetLastError();
+    majorants = nullptr;
+    return false;
+  }
+  launchMacrocellMajorants(field->ranges,
+      field->mcDims,
+      tfDev,
+      256,
+      valueRange[0],
+      valueRange[1],
+      uniformOpacity,
+      majorants,
+      s);
+  builtStamp = want;
+  return cudaGetLastError() == cudaSuccess;
+}
+
+// ---------------------------------------------------------------------------
+// World (scene/World.cpp:100-442, Group.cpp:189-266, optix_visrtx.cpp)
+// ---------------------------------------------------------------------------
+
+World::~World()
+{
+  freeBuilt();
+  if (zeroInstance)
+    releaseObj(zeroInstance);
+  if (zeroGroup)
+    releaseObj(zeroGroup);
+}
+
+void World::commit()
+{
+  instances = objectArrayParam(this, "instance");
+  zeroSurfaces = objectArrayParam(this, "surface");
+  zeroVolumes = objectArrayParam(this, "volume");
+  zeroLights = objectArrayParam(this, "light");
+  id = get<uint32_t>("id", VRTX_UINT32, ~0u);
+  if (!zeroGroup) {
+    zeroGroup = new Group(Object::dev, VRTX_GROUP);
+    zeroInstance = new Instance(Object::dev, VRTX_INSTANCE, "transform");
+  }
+  zeroGroup->surfaces = zeroSurfaces;
+  zeroGroup->volumes = zeroVolumes;
+  zeroGroup->lights = zeroLights;
+  zeroGroup->commitStamp = commitStamp;
+  zeroInstance->group = zeroGroup;
+  zeroInstance->id = id;
+  const float identity[12] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0};
+  std::memcpy(zeroInstance->xfm, identity, sizeof(identity));
+  zeroInstance->commitStamp = commitStamp;
+  builtStamp = 0;
+}
+
+std::vector<Instance *> World::instanceList() const
+{
+  std::vector<Instance *> out;
+  if (instances)
+    for (Object *o : instances->handles)
+      if (o && o->type == VRTX_INSTANCE && o->isValid())
+        out.push_back(static_cast<Instance *>(o));
+  if (zeroGroup && (zeroSurfaces || zeroVolumes || zeroLights))
+    out.push_back(zeroInstance);
+  return out;
+}
+
+uint64_t World::deepStamp() const
+{
+  uint64_t s = commitStamp;
+  if (instances) {
+    s = std::max(s, instances->deepStamp());
+    for (Object *o : instances->handles)
+      if (o)
+        s = std::max(s, o->deepStamp());
+  }
+  if (zeroGroup)
+    s = std::max(s, zeroGroup->deepStamp());
+  return s;
+}
+
+void World::freeBuilt()
+{
+  cudaStream_t s = Object::dev->stream;
+  for (auto &b : blases) {
+    freeBVH8(b.bvh, s);
+    if (b.records)
+      cudaFreeAsync(b.records, s);
+  }
+  blases.clear();
+  freeBVH8(tlas, s);
+  for (void *p : allocations)
+    cudaFreeAsync(p, s);
+  allocations.clear();
+  gpu = WorldGPU{};
+  builtStamp = 0;
+}
+
+template <typename T>
+static T *uploadVec(World *w, const std::vector<T> &v, cudaStream_t s)
+{
+  if (v.empty())
+    return nullptr;
+  T *p = nullptr;
+  if (cudaMallocAsync((void **)&p, sizeof(T) * v.size(), s) != cudaSuccess)
+    return nullptr;
+  cudaMemcpyAsync(p, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice, s);
+  w->allocations.push_back(p);
+  return p;
+}
+
+static box3 xfmBox(const float m[12], const box3 &b)
+{
+  box3 o = emptyBox();
+  for (int i = 0; i < 8; i++) {
+    const f3 p{(i & 1) ? b.hi.x : b.lo.x,
+        (i & 2) ? b.hi.y : b.lo.y,
+        (i & 4) ? b.hi.z : b.lo.z};
+    const f3 q{m[0] * p.x + m[1] * p.y + m[2] * p.z + m[3],
+        m[4] * p.x + m[5] * p.y + m[6] * p.z + m[7],
+        m[8] * p.x + m[9] * p.y + m[10] * p.z + m[11]};
+    extend(o, q);
+  }
+  return o;
+}
+
+bool World::rebuild()
+{
+  const auto t0 = std::chrono::steady_clock::now();
+  cudaStream_t s = Object::dev->stream;
+  freeBuilt();
+  const auto insts = instanceList();
+
+  std::vector<Surface *> surfaces;
+  std::map<Surface *, uint32_t> surfIdx;
+  std::vector<Geometry *> geoms;
+  std::map<Geometry *, uint32_t> geomIdx;
+  std::vector<Material *> mats;
+  std::map<Material *, uint32_t> matIdx;
+  std::vector<Group *> groups;
+  std::map<Group *, std::vector<Surface *>> groupSurfaces;
+  for (Instance *inst : insts) {
+    Group *g = inst->group;
+    if (groupSurfaces.count(g))
+      continue;
+    groups.push_back(g);
+    auto ss = g->validSurfaces();
+    groupSurfaces[g] = ss;
+    for (Surface *sf : ss) {
+      if (surfIdx.count(sf))
+        continue;
+      surfIdx[sf] = (uint32_t)surfaces.size();
+      surfaces.push_back(sf);
+      if (!geomIdx.count(sf->geometry)) {
+        geomIdx[sf->geometry] = (uint32_t)geoms.size();
+        geoms.push_back(sf->geometry);
+      }
+      if (!matIdx.count(sf->material)) {
+        matIdx[sf->material] = (uint32_t)mats.size();
+        mats.push_back(sf->material);
+      }
+    }
+  }
+
+  std::vector<GeometryGPU> hGeoms;
+  for (Geometry *g : geoms)
+    hGeoms.push_back(g->gpuData());
+  std::vector<MaterialGPU> hMats;
+  bool allOpaque = true;
+  for (Material *m : mats) {
+    hMats.push_back(m->gpu);
+    if (m->gpu.alphaMode != ALPHA_OPAQUE)
+      allOpaque = false;
+  }
+  std::vector<SurfaceGPU> hSurfs;
+  for (Surface *sf : surfaces)
+    hSurfs.push_back(SurfaceGPU{
+        geomIdx[sf->geometry], matIdx[sf->material], sf->id, 0u});
+  GeometryGPU *dGeoms = uploadVec(this, hGeoms, s);
+  MaterialGPU *dMats = uploadVec(this, hMats, s);
+  SurfaceGPU *dSurfs = uploadVec(this, hSurfs, s);
+
+  // BLAS per (group, primitive class)
+  std::map<Group *, std::array<int, 2>> groupBlas;
+  std::vector<BLASDesc> hBlas;
+  for (Group *g : groups) {
+    std::array<int, 2> ids{-1, -1};
+    for (int cls = 0; cls < GEOM_NUM_TYPES; cls++) {
+      uint32_t n = 0;
+      for (Surface *sf : groupSurfaces[g])
+        if (sf->geometry->geomClass() == cls)
+          n += sf->geometry->numPrims;
+      if (n == 0)
+        continue;
+      uint2 *refs = nullptr;
+      box3 *boxes = nullptr;
+      cudaMallocAsync((void **)&refs, sizeof(uint2) * n, s);
+      cudaMallocAsync((void **)&boxes, sizeof(box3) * n, s);
+      uint32_t off = 0;
+      for (Surface *sf : groupSurfaces[g]) {
+        if (sf->geometry->geomClass() != cls)
+          continue;
+        launchFillRefs(surfIdx[sf], sf->geometry->numPrims, refs + off, s);
+        off += sf->geometry->numPrims;
+      }
+      if (cls == GEOM_TRIANGLE)
+        launchTriangleBoxes(dGeoms, refs, dSurfs, n, boxes, s);
+      else
+        launchSphereBoxes(dGeoms, refs, dSurfs, n, boxes, s);
+      BLASBuild b;
+      b.type = (uint32_t)cls;
+      b.numPrims = n;
+      cudaError_t err = buildBVH8(boxes, n, s, b.bvh);
+      if (err == cudaSuccess) {
+        const size_t recBytes =
+            cls == GEOM_TRIANGLE ? sizeof(TriRecord) : sizeof(SphereRecord);
+        cudaMallocAsync(&b.records, recBytes * b.bvh.numPrims, s);
+        if (cls == GEOM_TRIANGLE)
+          launchGatherTriangles(dGeoms,
+              refs,
+              dSurfs,
+              b.bvh.primOrder,
+              b.bvh.numPrims,
+              (TriRecord *)b.records,
+              s);
+        else
+          launchGatherSpheres(dGeoms,
+              refs,
+              dSurfs,
+              b.bvh.primOrder,
+              b.bvh.numPrims,
+              (SphereRecord *)b.records,
+              s);
+      }
+      cudaFreeAsync(refs, s);
+      cudaFreeAsync(boxes, s);
+      if (err != cudaSuccess) {
+        report(VRTX_SEVERITY_ERROR,
+            "BVH build failed: %s",
+            cudaGetErrorString(err));
+        cudaGetLastError();
+        continue;
+      }
+      ids[cls] = (int)hBlas.size();
+      BLASDesc d{};
+      d.nodes = b.bvh.nodes;
+      d.prims = b.records;
+      d.type = b.type;
+      d.numPrims = b.bvh.numPrims;
+      d.bounds = b.bvh.bounds;
+      hBlas.push_back(d);
+      blases.push_back(b);
+    }
+    groupBlas[g] = ids;
+  }
+  BLASDesc *dBlas = uploadVec(this, hBlas, s);
+
+  // top level: one record per (instance, transform, class)
+  std::vector<InstanceRecord> recs;
+  std::vector<box3> recBoxes;
+  std::vector<LightGPU> lights;
+  std::vector<VolumeGPU> vols;
+  worldBounds = emptyBox();
+  for (Instance *inst : insts) {
+    Group *g = inst->group;
+    const auto ids = groupBlas[g];
+    const auto gl = g->validLights();
+    const auto gv = g->validVolumes();
+    for (size_t t = 0; t < inst->numTransforms(); t++) {
+      float m[12];
+      inst->transform(t, m);
+      InstanceRecord r{};
+      invertAffine(m, r.worldToObject);
+      for (int i = 0; i < 12; i++)
+        r.objectToWorld.r[i / 4][i % 4] = m[i];
+      r.userId = inst->userID(t);
+      for (int cls = 0; cls < GEOM_NUM_TYPES; cls++) {
+        if (ids[cls] < 0)
+          continue;
+        r.blas = (uint32_t)ids[cls];
+        recs.push_back(r);
+        const box3 wb = xfmBox(m, hBlas[ids[cls]].bounds);
+        recBoxes.push_back(wb);
+        extend(worldBounds, wb);
+      }
+      for (Light *l : gl) {
+        LightGPU lg = l->gpu;
+        if (lg.type == LIGHT_DIRECTIONAL)
+          lg.dirToLight = f3{m[0] * l->gpu.dirToLight.x + m[1] * l->gpu.dirToLight.y
+                  + m[2] * l->gpu.dirToLight.z,
+              m[4] * l->gpu.dirToLight.x + m[5] * l->gpu.dirToLight.y
+                  + m[6] * l->gpu.dirToLight.z,
+              m[8] * l->gpu.dirToLight.x + m[9] * l->gpu.dirToLight.y
+                  + m[10] * l->gpu.dirToLight.z};
+        else
+          lg.position = f3{m[0] * lg.position.x + m[1] * lg.position.y
+                  + m[2] * lg.position.z + m[3],
+              m[4] * lg.position.x + m[5] * lg.position.y + m[6] * lg.position.z
+                  + m[7],
+              m[8] * lg.position.x + m[9] * lg.position.y + m[10] * lg.position.z
+                  + m[11]};
+        lights.push_back(lg);
+      }
+      for (Volume *v : gv) {
+        if (!v->ensureBuilt())
+          continue;
+        SpatialField *f = v->field;
+        VolumeGPU vg{};
+        vg.field = f->tex;
+        vg.tf = v->tfTex;
+        vg.hasTF = v->tfTex ? 1u : 0u;
+        vg.origin = f->origin;
+        vg.spacing = f->spacing;
+        vg.invSpacing = f3{1.f / (f->spacing.x * float(f->dims[0])),
+            1.f / (f->spacing.y * float(f->dims[1])),
+            1.f / (f->spacing.z * float(f->dims[2]))};
+        vg.bounds = f->bounds();
+        vg.stepSize = f->stepSize();
+        vg.oneOverUnitDistance = 1.f / v->unitDistance;
+        vg.valueLo = v->valueRange[0];
+        vg.valueHi = v->valueRange[1];
+        vg.uniformColor = v->uniformColor;
+        vg.uniformOpacity = v->uniformOpacity;
+        vg.id = v->id;
+        vg.instId = inst->userID(t);
+        vg.worldToObject = r.worldToObject;
+        vg.majorants = v->majorants;
+        for (int k = 0; k < 3; k++) {
+          vg.mcDims[k] = f->mcDims[k];
+          vg.dims[k] = f->dims[k];
+        }
+        vols.push_back(vg);
+        extend(worldBounds, xfmBox(m, vg.bounds));
+      }
+    }
+  }
+
+  // TLAS over instance records
+  InstanceRecord *dRecs = nullptr;
+  if (!recs.empty()) {
+    box3 *dBoxes = nullptr;
+    cudaMallocAsync((void **)&dBoxes, sizeof(box3) * recBoxes.size(), s);
+    cudaMemcpyAsync(dBoxes,
+        recBoxes.data(),
+        sizeof(box3) * recBoxes.size(),
+        cudaMemcpyHostToDevice,
+        s);
+    cudaError_t err = buildBVH8(dBoxes, (uint32_t)recBoxes.size(), s, tlas, 1);
+    cudaFreeAsync(dBoxes, s);
+    if (err != cudaSuccess) {
+      report(VRTX_SEVERITY_ERROR, "TLAS build failed: %s", cudaGetErrorString(err));
+      return false;
+    }
+    std::vector<uint32_t> order(tlas.numPrims);
+    cudaMemcpyAsync(order.data(),
+        tlas.primOrder,
+        sizeof(uint32_t) * order.size(),
+        cudaMemcpyDeviceToHost,
+        s);
+    cudaStreamSynchronize(s);
+    std::vector<InstanceRecord> sorted(order.size());
+    for (size_t i = 0; i < order.size(); i++)
+      sorted[i] = recs[order[i]];
+    dRecs = uploadVec(this, sorted, s);
+  }
+
+  gpu.tlasNodes = tlas.nodes;
+  gpu.instances = dRecs;
+  gpu.numInstances = (uint32_t)recs.size();
+  gpu.blas = dBlas;
+  gpu.surfaces = dSurfs;
+  gpu.geometries = dGeoms;
+  gpu.materials = dMats;
+  gpu.lights = uploadVec(this, lights, s);
+  gpu.numLights = (uint32_t)lights.size();
+  gpu.volumes = uploadVec(this, vols, s);
+  gpu.numVolumes = (uint32_t)vols.size();
+  gpu.allOpaque = allOpaque ? 1u : 0u;
+  const cudaError_t err = cudaStreamSynchronize(s);
+  builtStamp = deepStamp();
+  buildMs = std::chrono::duration<float, std::milli>(
+      std::chrono::steady_clock::now() - t0)
+                .count();
+  if (err != cudaSuccess) {
+    report(VRTX_SEVERITY_ERROR, "world build failed: %s", cudaGetErrorString(err));
+    return false;
+  }
+  return true;
+}
+
+bool World::getProperty(
+    const std::string &name, int t, void *mem, uint64_t size, uint32_t mask)
+{
+  if (name == "bounds" && t == VRTX_FLOAT32_BOX3 && size >= 24) {
+    if (Object::dev->initOk && (builtStamp == 0 || deepStamp() > builtStamp))
+      rebuild();
+    std::memcpy(mem, &worldBounds, 24);
+    return true;
+  }
+  return Object::getProperty(name, t, mem, size, mask);
+}
+
+// ---------------------------------------------------------------------------
+// Renderer (renderer/Renderer.cpp:152-207, DirectLight.cpp, AmbientOcclusion
+// .cpp, Raycast.cpp, DiffusePathTracer.cpp)
+// ---------------------------------------------------------------------------
+
+void Renderer::commit()
+{
+  RendererGPU &r = gpu;
+  float defaultAmbient = 0.f;
+  if (subtype == "raycast")
+    r.type = RENDERER_RAYCAST;
+  else if (subtype == "ao") {
+    r.type = RENDERER_AO;
+    defaultAmbient = 1.f;
+  } else if (subtype == "dpt" || subtype == "diffuse_pathtracer") {
+    r.type = RENDERER_DPT;
+    defaultAmbient = 1.f;
+  } else {
+    if (subtype != "default" && subtype != "directLight")
+      report(VRTX_SEVERITY_WARNING,
+          "unknown renderer subtype '%s', using 'default'",
+          subtype.c_str());
+    r.type = RENDERER_DIRECT_LIGHT;
+  }
+  float bg[4] = {0.f, 0.f, 0.f, 1.f};
+  if (has("background", VRTX_FLOAT32_VEC4))
+    std::memcpy(bg, params["background"].bytes.data(), 16);
+  r.background = make_float4(bg[0], bg[1], bg[2], bg[3]);
+  spp = get<int32_t>("pixelSamples", VRTX_INT32, 1);
+  r.maxRayDepth = get<int32_t>("maxRayDepth", VRTX_INT32, 5);
+  r.ambientColor = get<f3>("ambientColor", VRTX_FLOAT32_VEC3, f3{1.f, 1.f, 1.f});
+  r.ambientIntensity = get<float>("ambientRadiance", VRTX_FLOAT32, defaultAmbient);
+  r.occlusionDistance = get<float>("ambientOcclusionDistance", VRTX_FLOAT32, 1e20f);
+  checkerboard = get<int32_t>("checkerboarding", VRTX_BOOL, 0) != 0;
+  sampleLimit = get<int32_t>("sampleLimit", VRTX_INT32, 128);
+  r.cullTriangleBF = get<int32_t>("cullTriangleBackfaces", VRTX_BOOL, 0) != 0;
+  const float vsr = std::min(
+      std::max(get<float>("volumeSamplingRate", VRTX_FLOAT32, 0.125f), 1e-3f),
+      10.f);
+  r.invVolumeSamplingRate = 1.f / vsr;
+  if (checkerboard)
+    spp = 1;
+  r.aoSamples = 0;
+  if (r.type == RENDERER_DIRECT_LIGHT || r.type == RENDERER_AO)
+    r.aoSamples = std::min(std::max(get<int32_t>("ambientSamples", VRTX_INT32, 1), 0), 256);
+  r.lightFalloff =
+      std::min(std::max(get<float>("lightFalloff", VRTX_FLOAT32, 1.f), 0.f), 1.f);
+  r.maxDepth = std::min(std::max(get<int32_t>("maxDepth", VRTX_INT32, 5), 1), 256);
+  if (r.type == RENDERER_RAYCAST)
+    sampleLimit = 1; // single-shot renderer (Raycast.cpp:46-51)
+  r.numIterations = std::max(spp, 1);
+}
+
+bool Renderer::isValid() const
+{
+  return true;
+}
+
+// ---------------------------------------------------------------------------
+// Frame (frame/Frame.cu)
+// ---------------------------------------------------------------------------
+
+Frame::~Frame()
+{
+  if (Object::dev->initOk) {
+    wait();
+    freeBuffers();
+    for (cudaEvent_t e : {evStart, evEnd, evKStart, evKEnd})
+      if (e)
+        cudaEventDestroy(e);
+    if (workCounter)
+      cudaFree(workCounter);
+    if (errorFlag)
+      cudaFree(errorFlag);
+    if (stats)
+      cudaFree(stats);
+  }
+}
+
+void Frame::freeBuffers()
+{
+  for (void *&b : buffers) {
+    if (b)
+      cudaFree(b);
+    b = nullptr;
+  }
+  fb = FramebufferGPU{};
+}
+
+void Frame::commit()
+{
+  renderer = static_cast<Renderer *>(getObject("renderer", VRTX_RENDERER));
+  camera = static_cast<Camera *>(getObject("camera", VRTX_CAMERA));
+  world = static_cast<World *>(getObject("world", VRTX_WORLD));
+  callback = get<VRTXFrameCompletionCallback>(
+      "frameCompletionCallback", VRTX_FUNCTION_POINTER, nullptr);
+  callbackPtr =
+      get<const void *>("frameCompletionCallbackUserData", VRTX_VOID_POINTER, nullptr);
+  colorType =
+      get<int32_t>("channel.color", VRTX_DATA_TYPE, VRTX_UFIXED8_RGBA_SRGB);
+  uint32_t sz[2] = {10, 10};
+  if (has("size", VRTX_UINT32_VEC2))
+    std::memcpy(sz, params["size"].bytes.data(), 8);
+  depthType = get<int32_t>("channel.depth", VRTX_DATA_TYPE, VRTX_UNKNOWN);
+  primType = get<int32_t>("channel.primitiveId", VRTX_DATA_TYPE, VRTX_UNKNOWN);
+  objType = get<int32_t>("channel.objectId", VRTX_DATA_TYPE, VRTX_UNKNOWN);
+  instType = get<int32_t>("channel.instanceId", VRTX_DATA_TYPE, VRTX_UNKNOWN);
+  albedoType = get<int32_t>("channel.albedo", VRTX_DATA_TYPE, VRTX_UNKNOWN);
+  normalType = get<int32_t>("channel.normal", VRTX_DATA_TYPE, VRTX_UNKNOWN);
+  size[0] = sz[0];
+  size[1] = sz[1];
+  // frame buffers (Frame::finalize, Frame.cu:96-161)
+  if (!Object::dev->initOk)
+    return;
+  wait();
+  freeBuffers();
+  const size_t n = (size_t)size[0] * size[1];
+  const bool useFloat = colorType == VRTX_FLOAT32_VEC4;
+  fb.format = useFloat
+      ? FORMAT_FLOAT
+      : (colorType == VRTX_UFIXED8_RGBA_SRGB ? FORMAT_SRGB : FORMAT_UINT);
+  fb.w = size[0];
+  fb.h = size[1];
+  fb.invW = 1.f / float(size[0]);
+  fb.invH = 1.f / float(size[1]);
+  const bool cPrim = primType == VRTX_UINT32, cObj = objType == VRTX_UINT32,
+             cInst = instType == VRTX_UINT32;
+  const bool cDepth = depthType == VRTX_FLOAT32 || cPrim || cObj || cInst;
+  if (cDepth)
+    depthType = VRTX_FLOAT32;
+  auto alloc = [&](int slot, size_t bytes) -> void * {
+    if (!bytes)
+      return nullptr;
+    if (cudaMalloc(&buffers[slot], bytes) != cudaSuccess) {
+      cudaGetLastError();
+      report(VRTX_SEVERITY_ERROR, "frame buffer allocation failed");
+      buffers[slot] = nullptr;
+    }
+    return buffers[slot];
+  };
+  fb.accum = (float4 *)alloc(0, n * sizeof(float4));
+  if (useFloat)
+    fb.outColorF = (float4 *)alloc(1, n * sizeof(float4));
+  else
+    fb.outColorU = (uint32_t *)alloc(1, n * sizeof(uint32_t));
+  fb.depth = cDepth ? (float *)alloc(2, n * 4) : nullptr;
+  fb.primID = cPrim ? (uint32_t *)alloc(3, n * 4) : nullptr;
+  fb.objID = cObj ? (uint32_t *)alloc(4, n * 4) : nullptr;
+  fb.instID = cInst ? (uint32_t *)alloc(5, n * 4) : nullptr;
+  fb.albedo = albedoType == VRTX_FLOAT32_VEC3 ? (f3 *)alloc(6, n * 12) : nullptr;
+  fb.normal = normalType == VRTX_FLOAT32_VEC3 ? (f3 *)alloc(7, n * 12) : nullptr;
+  if (!workCounter)
+    cudaMalloc(&workCounter, 16);
+  if (!errorFlag) {
+    cudaMalloc(&errorFlag, 16);
+    cudaMemset(errorFlag, 0, 16);
+  }
+  if (!stats) {
+    cudaMalloc(&stats, 8 * sizeof(unsigned long long));
+    cudaMemset(stats, 0, 8 * sizeof(unsigned long long));
+  }
+  countTraversal = get<int32_t>("vrtx.countTraversal", VRTX_BOOL, 0) != 0;
+  for (cudaEvent_t *e : {&evStart, &evEnd, &evKStart, &evKEnd})
+    if (!*e)
+      cudaEventCreate(e);
+  nextFrameReset = true;
+  rendered = false;
+}
+
+bool Frame::isValid() const
+{
+  return renderer && camera && world && renderer->isValid();
+}
+
+void Frame::wait()
+{
+  if (rendered && evEnd)
+    cudaEventSynchronize(evEnd);
+}
+
+bool Frame::ready()
+{
+  if (!rendered || !evEnd)
+    return true;
+  return cudaEventQuery(evEnd) == cudaSuccess;
+}
+
+void Frame::render()
+{
+  Device *d = Object::dev;
+  wait();
+  launches = 0;
+  if (!d->initOk) {
+    report(VRTX_SEVERITY_ERROR, "skipping render: no CUDA device");
+    return;
+  }
+  if (!isValid() || !fb.accum) {
+    const char *why = !renderer ? "missing ANARIRenderer"
+        : !camera                ? "missing ANARICamera"
+        : !world                 ? "missing ANARIWorld"
+                                 : "invalid frame buffers";
+    report(VRTX_SEVERITY_ERROR,
+        "skipping render of incomplete or invalid frame object -- issue: %s",
+        why);
+    return;
+  }
+  cudaStream_t s = d->stream;
+  if (world->builtStamp == 0 || world->deepStamp() > world->builtStamp) {
+    if (!world->rebuild())
+      return;
+    d->markChanged();
+  }
+  // checkAccumulationReset (Frame.cu:574-588)
+  const uint64_t change = d->lastChange.load();
+  if (change > lastSeenStamp) {
+    lastSeenStamp = change;
+    nextFrameReset = true;
+  }
+  if (!nextFrameReset && renderer->sampleLimit > 0
+      && fb.frameID >= renderer->sampleLimit)
+    return;
+  cudaEventRecord(evStart, s);
+  // newFrame (Frame.cu:590-660)
+  if (nextFrameReset) {
+    fb.frameID = 0;
+    fb.checkerboardID = renderer->checkerboard ? 0 : -1;
+    nextFrameReset = false;
+    launchClearFrame(fb, s);
+    launches++;
+  } else {
+    if (renderer->checkerboard)
+      fb.frameID += int(fb.checkerboardID == 3);
+    else
+      fb.frameID += renderer->spp;
+    fb.checkerboardID = renderer->checkerboard ? ((fb.checkerboardID + 1) & 0x3) : -1;
+  }
+  FrameParams P{};
+  P.world = world->gpu;
+  P.camera = camera->gpu;
+  P.renderer = renderer->gpu;
+  P.fb = fb;
+  P.workCounter = workCounter;
+  P.errorFlag = errorFlag;
+  P.launchW = renderer->checkerboard ? (fb.w + 1) / 2 : fb.w;
+  P.launchH = renderer->checkerboard ? (fb.h + 1) / 2 : fb.h;
+  P.numTilesX = (P.launchW + 7) / 8;
+  P.numTilesY = (P.launchH + 3) / 4;
+  P.stats = stats;
+  cudaMemsetAsync(workCounter, 0, 4, s);
+  cudaMemsetAsync(stats, 0, 8 * sizeof(unsigned long long), s);
+  const int blocks =
+      d->numSMs * renderOccupancyBlocks(P.renderer.type, countTraversal);
+  cudaEventRecord(evKStart, s);
+  cudaError_t err = launchRender(P, blocks, countTraversal, s);
+  cudaEventRecord(evKEnd, s);
+  launches++;
+  if (err != cudaSuccess)
+    report(VRTX_SEVERITY_ERROR, "render launch failed: %s", cudaGetErrorString(err));
+  if (callback) {
+    cudaLaunchHostFunc(
+        s,
+        [](void *p) {
+          auto *f = (Frame *)p;
+          f->callback(f->callbackPtr,
+              reinterpret_cast<VRTXDevice>(f->Object::dev),
+              reinterpret_cast<VRTXFrame>(f));
+        },
+        this);
+  }
+  cudaEventRecord(evEnd, s);
+  rendered = true;
+}
+
+const void *Frame::map(
+    const std::string &channel, uint32_t *w, uint32_t *h, int *pixelType)
+{
+  wait();
+  int t = VRTX_UNKNOWN;
+  const void *ret = nullptr;
+  const size_t n = (size_t)fb.w * fb.h;
+  const bool cuda = channel.size() > 4
+      && channel.compare(channel.size() - 4, 4, "CUDA") == 0;
+  const std::string base = cuda ? channel.substr(0, channel.size() - 4) : channel;
+  void *src = nullptr;
+  size_t bytes = 0;
+  std::vector<uint8_t> *host = nullptr;
+  if (base == "channel.color" && fb.accum) {
+    t = colorType;
+    src = fb.format == FORMAT_FLOAT ? (void *)fb.outColorF : (void *)fb.outColorU;
+    bytes = n * (fb.format == FORMAT_FLOAT ? 16 : 4);
+    host = &hostColor;
+  } else if (base == "channel.depth" && fb.depth) {
+    t = VRTX_FLOAT32;
+    src = fb.depth;
+    bytes = n * 4;
+    host = &hostDepth;
+  } else if (base == "channel.primitiveId" && fb.primID) {
+    t = VRTX_UINT32;
+    src = fb.primID;
+    bytes = n * 4;
+    host = &hostPrim;
+  } else if (base == "channel.objectId" && fb.objID) {
+    t = VRTX_UINT32;
+    src = fb.objID;
+    bytes = n * 4;
+    host = &hostObj;
+  } else if (base == "channel.instanceId" && fb.instID) {
+    t = VRTX_UINT32;
+    src = fb.instID;
+    bytes = n * 4;
+    host = &hostInst;
+  } else if (base == "channel.albedo" && fb.albedo) {
+    t = VRTX_FLOAT32_VEC3;
+    src = fb.albedo;
+    bytes = n * 12;
+    host = &hostAlbedo;
+  } else if (base == "channel.normal" && fb.normal) {
+    t = VRTX_FLOAT32_VEC3;
+    src = fb.normal;
+    bytes = n * 12;
+    host = &hostNormal;
+  }
+  if (t == VRTX_UNKNOWN || !src) {
+    *w = *h = 0;
+    *pixelType = VRTX_UNKNOWN;
+    return nullptr;
+  }
+  if (cuda)
+    ret = src;
+  else {
+    host->resize(bytes);
+    cudaMemcpy(host->data(), src, bytes, cudaMemcpyDeviceToHost);
+    ret = host->data();
+  }
+  *w = fb.w;
+  *h = fb.h;
+  *pixelType = t;
+  return ret;
+}
+
+bool Frame::getProperty(
+    const std::string &name, int t, void *mem, uint64_t size, uint32_t mask)
+{
+  if (name == "duration" && t == VRTX_FLOAT32 && size >= 4) {
+    if (mask & VRTX_WAIT)
+      wait();
+    float ms = 0.f;
+    if (rendered)
+      cudaEventElapsedTime(&ms, evStart, evEnd);
+    const float sec = ms / 1000.f;
+    std::memcpy(mem, &sec, 4);
+    return true;
+  }
+  if (name == "numSamples" && t == VRTX_INT32 && size >= 4) {
+    if (mask & VRTX_WAIT)
+      wait();
+    int32_t v = fb.frameID;
+    std::memcpy(mem, &v, 4);
+    return true;
+  }
+  // libvrtx extension (no reference counterpart): traversal counters of the
+  // last render: rays traced, and with "vrtx.countTraversal" set also BVH8
+  // nodes visited, triangle tests, sphere tests, BLAS entries; then the
+  // traversal error flags (bit 0: stack overflow).
+  if (name == "vrtx.stats" && t == VRTX_UINT64 && size >= 48 && stats) {
+    wait();
+    unsigned long long v[6] = {};
+    cudaMemcpy(v, stats, 5 * sizeof(unsigned long long), cudaMemcpyDeviceToHost);
+    uint32_t flags = 0;
+    cudaMemcpy(&flags, errorFlag, 4, cudaMemcpyDeviceToHost);
+    v[5] = flags;
+    std::memcpy(mem, v, sizeof(v));
+    return true;
+  }
+  if (name == "nextFrameReset" && t == VRTX_BOOL && size >= 4) {
+    if (mask & VRTX_WAIT)
+      wait();
+    const bool reset = nextFrameReset || Object::dev->lastChange.load() > lastSeenStamp;
+    int32_t v = reset ? 1 : 0;
+    std::memcpy(mem, &v, 4);
+    return true;
+  }
+  return Object::getProperty(name, t, mem, size, mask);
+}
+
+} // namespace vrtx
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+
+using namespace vrtx;
+
+#define VRTX_GUARD_BEGIN try {
+#define VRTX_GUARD_END(dev, ret)                                               \
+  }                                                                            \
+  catch (const std::exception &e)                                              \
+  {                                                                            \
+    if (dev)                                                                   \
+      reinterpret_cast<Device *>(dev)->report(                                 \
+          nullptr, VRTX_SEVERITY_FATAL_ERROR, e.what());                       \
+    return ret;                                                                \
+  }                                                                            \
+  catch (...)                                                                  \
+  {                                                                            \
+    return ret;                                                                \
+  }
+
+static Device *D(VRTXDevice d)
+{
+  return reinterpret_cast<Device *>(d);
+}
+static Object *O(VRTXObject o)
+{
+  return reinterpret_cast<Object *>(o);
+}
+
+template <typename T>
+static VRTXObject newObj(VRTXDevice d, int type, const char *subtype)
+{
+  Device *dev = D(d);
+  if (!dev)
+    return nullptr;
+  std::lock_guard<std::recursive_mutex> lock(dev->mutex);
+  if (!dev->init())
+    return nullptr; // factory calls return null when init failed
+  Object *o = new T(dev, type, subtype ? subtype : "");
+  dev->live.push_back(o);
+  return reinterpret_cast<VRTXObject>(o);
+}
+
+extern "C" {
+
+VRTX_API VRTXDevice vrtxNewDevice(VRTXStatusCallback cb, const void *ptr)
+{
+  try {
+    Device *d = new Device();
+    d->cb = cb;
+    d->cbPtr = ptr;
+    return reinterpret_cast<VRTXDevice>(d);
+  } catch (...) {
+    return nullptr;
+  }
+}
+
+VRTX_API void vrtxDeviceSetParameter(
+    VRTXDevice d, const char *name, int type, const void *mem)
+{
+  if (!d || !name)
+    return;
+  std::string n(name);
+  if (n == "cudaDevice" && type == VRTX_INT32 && mem)
+    D(d)->cudaDevice = *(const int32_t *)mem;
+  else if (n == "statusCallback" && mem)
+    D(d)->cb = *(const VRTXStatusCallback *)mem;
+  else if (n == "statusCallbackUserData")
+    D(d)->cbPtr = mem ? *(const void *const *)mem : nullptr;
+}
+
+VRTX_API void vrtxDeviceCommitParameters(VRTXDevice) {}
+
+VRTX_API void vrtxDeviceRelease(VRTXDevice d)
+{
+  if (!d)
+    return;
+  Device *dev = D(d);
+  if (dev->initOk)
+    cudaStreamSynchronize(dev->stream);
+  // objects still alive are released in reverse creation order
+  while (!dev->live.empty()) {
+    Object *o = dev->live.back();
+    dev->live.pop_back();
+    o->refs = 1 << 20; // detach from app references
+    for (auto &p : o->params)
+      p.second.obj = nullptr;
+    for (auto &p : o->pending)
+      p.second.obj = nullptr;
+    if (o->type == VRTX_ARRAY1D || o->type == VRTX_ARRAY2D
+        || o->type == VRTX_ARRAY3D)
+      static_cast<Array *>(o)->handles.clear();
+    if (o->type == VRTX_WORLD) {
+      auto *w = static_cast<World *>(o);
+      w->zeroGroup = nullptr;
+      w->zeroInstance = nullptr;
+    }
+    delete o;
+  }
+  if (dev->initOk)
+    cudaStreamDestroy(dev->stream);
+  delete dev;
+}
+
+VRTX_API int vrtxDeviceGetProperty(VRTXDevice d,
+    const char *name,
+    int type,
+    void *mem,
+    uint64_t size,
+    uint32_t)
+{
+  if (!d || !name || !mem)
+    return 0;
+  std::string n(name);
+  if (n == "version" && type == VRTX_INT32 && size >= 4) {
+    int32_t v = 13; // VisRTX 0.13.0 device surface
+    std::memcpy(mem, &v, 4);
+    return 1;
+  }
+  if (n == "visrtx" && type == VRTX_BOOL && size >= 4) {
+    int32_t v = 1;
+    std::memcpy(mem, &v, 4);
+    return 1;
+  }
+  if (n == "numSMs" && type == VRTX_INT32 && size >= 4) {
+    D(d)->init();
+    int32_t v = D(d)->numSMs;
+    std::memcpy(mem, &v, 4);
+    return 1;
+  }
+  return 0;
+}
+
+VRTX_API int vrtxDeviceIsValid(VRTXDevice d)
+{
+  return d && D(d)->init() ? 1 : 0;
+}
+
+static VRTXArray newArray(VRTXDevice d,
+    int dims,
+    const void *mem,
+    VRTXMemoryDeleter del,
+    const void *ud,
+    int et,
+    uint64_t n1,
+    uint64_t n2,
+    uint64_t n3)
+{
+  Device *dev = D(d);
+  if (!dev)
+    return nullptr;
+  VRTX_GUARD_BEGIN
+  std::lock_guard<std::recursive_mutex> lock(dev->mutex);
+  if (!dev->init())
+    return nullptr;
+  if (sizeOfType(et) == 0 && !isObjectType(et)) {
+    dev->report(nullptr, VRTX_SEVERITY_ERROR, "array element type not supported");
+    return nullptr;
+  }
+  auto *a = new Array(dev, dims, mem, del, ud, et, n1, n2, n3);
+  dev->live.push_back(a);
+  dev->markChanged();
+  return reinterpret_cast<VRTXArray>(a);
+  VRTX_GUARD_END(d, nullptr)
+}
+
+VRTX_API VRTXArray vrtxNewArray1D(VRTXDevice d,
+    const void *mem,
+    VRTXMemoryDeleter del,
+    const void *ud,
+    int et,
+    uint64_t n1)
+{
+  return newArray(d, 1, mem, del, ud, et, n1, 1, 1);
+}
+
+VRTX_API VRTXArray vrtxNewArray2D(VRTXDevice d,
+    const void *mem,
+    VRTXMemoryDeleter del,
+    const void *ud,
+    int et,
+    uint64_t n1,
+    uint64_t n2)
+{
+  return newArray(d, 2, mem, del, ud, et, n1, n2, 1);
+}
+
+VRTX_API VRTXArray vrtxNewArray3D(VRTXDevice d,
+    const void *mem,
+    VRTXMemoryDeleter del,
+    const void *ud,
+    int et,
+    uint64_t n1,
+    uint64_t n2,
+    uint64_t n3)
+{
+  return newArray(d, 3, mem, del, ud, et, n1, n2, n3);
+}
+
+VRTX_API void *vrtxMapArray(VRTXDevice d, VRTXArray a)
+{
+  if (!d || !a)
+    return nullptr;
+  return static_cast<Array *>(O(a))->map();
+}
+
+VRTX_API void vrtxUnmapArray(VRTXDevice d, VRTXArray a)
+{
+  if (!d || !a)
+    return;
+  std::lock_guard<std::recursive_mutex> lock(D(d)->mutex);
+  static_cast<Array *>(O(a))->unmap();
+}
+
+VRTX_API VRTXObject vrtxNewCamera(VRTXDevice d, const char *st)
+{
+  return newObj<Camera>(d, VRTX_CAMERA, st);
+}
+VRTX_API VRTXObject vrtxNewGeometry(VRTXDevice d, const char *st)
+{
+  return newObj<Geometry>(d, VRTX_GEOMETRY, st);
+}
+VRTX_API VRTXObject vrtxNewLight(VRTXDevice d, const char *st)
+{
+  return newObj<Light>(d, VRTX_LIGHT, st);
+}
+VRTX_API VRTXObject vrtxNewMaterial(VRTXDevice d, const char *st)
+{
+  return newObj<Material>(d, VRTX_MATERIAL, st);
+}
+VRTX_API VRTXObject vrtxNewRenderer(VRTXDevice d, const char *st)
+{
+  VRTXObject o = newObj<Renderer>(d, VRTX_RENDERER, st);
+  if (o) // renderers are usable with defaults before any commit
+    static_cast<Renderer *>(O(o))->commit();
+  return o;
+}
+VRTX_API VRTXObject vrtxNewSampler(VRTXDevice d, const char *st)
+{
+  return newObj<Object>(d, VRTX_SAMPLER, st);
+}
+VRTX_API VRTXObject vrtxNewSpatialField(VRTXDevice d, const char *st)
+{
+  return newObj<SpatialField>(d, VRTX_SPATIAL_FIELD, st);
+}
+VRTX_API VRTXObject vrtxNewVolume(VRTXDevice d, const char *st)
+{
+  return newObj<Volume>(d, VRTX_VOLUME, st);
+}
+VRTX_API VRTXObject vrtxNewSurface(VRTXDevice d)
+{
+  return newObj<Surface>(d, VRTX_SURFACE, "");
+}
+VRTX_API VRTXObject vrtxNewGroup(VRTXDevice d)
+{
+  return newObj<Group>(d, VRTX_GROUP, "");
+}
+VRTX_API VRTXObject vrtxNewInstance(VRTXDevice d, const char *st)
+{
+  VRTXObject o = newObj<Instance>(d, VRTX_INSTANCE, st ? st : "transform");
+  if (o)
+    static_cast<Instance *>(O(o))->commit();
+  return o;
+}
+VRTX_API VRTXObject vrtxNewWorld(VRTXDevice d)
+{
+  VRTXObject o = newObj<World>(d, VRTX_WORLD, "");
+  if (o)
+    static_cast<World *>(O(o))->commit();
+  return o;
+}
+VRTX_API VRTXFrame vrtxNewFrame(VRTXDevice d)
+{
+  return newObj<Frame>(d, VRTX_FRAME, "");
+}
+
+VRTX_API void vrtxSetParameter(
+    VRTXDevice d, VRTXObject o, const char *name, int type, const void *mem)
+{
+  if (!d || !o || !name)
+    return;
+  VRTX_GUARD_BEGIN
+  std::lock_guard<std::recursive_mutex> lock(D(d)->mutex);
+  O(o)->setParam(name, type, mem);
+  VRTX_GUARD_END(d, )
+}
+
+VRTX_API void vrtxUnsetParameter(VRTXDevice d, VRTXObject o, const char *name)
+{
+  if (!d || !o || !name)
+    return;
+  std::lock_guard<std::recursive_mutex> lock(D(d)->mutex);
+  O(o)->unsetParam(name);
+}
+
+VRTX_API void vrtxUnsetAllParameters(VRTXDevice d, VRTXObject o)
+{
+  if (!d || !o)
+    return;
+  std::lock_guard<std::recursive_mutex> lock(D(d)->mutex);
+  O(o)->unsetAll();
+}
+
+VRTX_API void vrtxCommitParameters(VRTXDevice d, VRTXObject o)
+{
+  if (!d || !o)
+    return;
+  VRTX_GUARD_BEGIN
+  std::lock_guard<std::recursive_mutex> lock(D(d)->mutex);
+  O(o)->commitParams();
+  VRTX_GUARD_END(d, )
+}
+
+VRTX_API void vrtxRelease(VRTXDevice d, VRTXObject o)
+{
+  if (!d || !o)
+    return;
+  std::lock_guard<std::recursive_mutex> lock(D(d)->mutex);
+  Object *obj = O(o);
+  if (--obj->publicRefs <= 0 && obj->refs > 1
+      && (obj->type == VRTX_ARRAY1D || obj->type == VRTX_ARRAY2D
+          || obj->type == VRTX_ARRAY3D))
+    static_cast<Array *>(obj)->privatize();
+  releaseObj(obj);
+}
+
+VRTX_API void vrtxRetain(VRTXDevice d, VRTXObject o)
+{
+  if (!d || !o)
+    return;
+  O(o)->publicRefs++;
+  retainObj(O(o));
+}
+
+VRTX_API int vrtxGetProperty(VRTXDevice d,
+    VRTXObject o,
+    const char *name,
+    int type,
+    void *mem,
+    uint64_t size,
+    uint32_t mask)
+{
+  if (!d || !o || !name || !mem)
+    return 0;
+  VRTX_GUARD_BEGIN
+  std::lock_guard<std::recursive_mutex> lock(D(d)->mutex);
+  return O(o)->getProperty(name, type, mem, size, mask) ? 1 : 0;
+  VRTX_GUARD_END(d, 0)
+}
+
+VRTX_API void vrtxRenderFrame(VRTXDevice d, VRTXFrame f)
+{
+  if (!d || !f)
+    return;
+  VRTX_GUARD_BEGIN
+  std::lock_guard<std::recursive_mutex> lock(D(d)->mutex);
+  Object *o = O(f);
+  if (o->type != VRTX_FRAME)
+    return;
+  static_cast<Frame *>(o)->render();
+  VRTX_GUARD_END(d, )
+}
+
+VRTX_API int vrtxFrameReady(VRTXDevice d, VRTXFrame f, uint32_t waitMask)
+{
+  if (!d || !f)
+    return 1;
+  auto *fr = static_cast<Frame *>(O(f));
+  if (waitMask & VRTX_WAIT) {
+    fr->wait();
+    return 1;
+  }
+  return fr->ready() ? 1 : 0;
+}
+
+VRTX_API void vrtxDiscardFrame(VRTXDevice, VRTXFrame) {}
+
+VRTX_API const void *vrtxMapFrame(VRTXDevice d,
+    VRTXFrame f,
+    const char *channel,
+    uint32_t *width,
+    uint32_t *height,
+    int *pixelType)
+{
+  uint32_t w0, h0;
+  int t0;
+  if (!width)
+    width = &w0;
+  if (!height)
+    height = &h0;
+  if (!pixelType)
+    pixelType = &t0;
+  *width = *height = 0;
+  *pixelType = VRTX_UNKNOWN;
+  if (!d || !f || !channel)
+    return nullptr;
+  VRTX_GUARD_BEGIN
+  std::lock_guard<std::recursive_mutex> lock(D(d)->mutex);
+  return static_cast<Frame *>(O(f))->map(channel, width, height, pixelType);
+  VRTX_GUARD_END(d, nullptr)
+}
+
+VRTX_API void vrtxUnmapFrame(VRTXDevice, VRTXFrame, const char *) {}
+
+VRTX_API uint64_t vrtxDebugCopyAccel(
+    VRTXDevice d, VRTXObject world, int kind, void *dst, uint64_t capacity)
+{
+  if (!d || !world || O(world)->type != VRTX_WORLD)
+    return 0;
+  std::lock_guard<std::recursive_mutex> lock(D(d)->mutex);
+  auto *w = static_cast<World *>(O(world));
+  cudaStream_t s = D(d)->stream;
+  cudaStreamSynchronize(s);
+  std::vector<std::pair<const void *, size_t>> parts;
+  if (kind == 0 && w->tlas.nodes)
+    parts.push_back({w->tlas.nodes, w->tlas.numNodes * sizeof(BVH8Node)});
+  else if (kind == 1)
+    for (auto &b : w->blases)
+      parts.push_back({b.bvh.nodes, b.bvh.numNodes * sizeof(BVH8Node)});
+  else if (kind == 2)
+    for (auto &b : w->blases) {
+      if (b.type == GEOM_TRIANGLE)
+        parts.push_back({b.records, b.bvh.numPrims * sizeof(TriRecord)});
+    }
+  else if (kind == 3 && w->gpu.instances)
+    parts.push_back({w->gpu.instances, w->gpu.numInstances * sizeof(InstanceRecord)});
+  else if (kind == 4)
+    for (auto &b : w->blases) {
+      if (b.type == GEOM_SPHERE)
+        parts.push_back({b.records, b.bvh.numPrims * sizeof(SphereRecord)});
+    }
+  else if (kind == 5) {
+    // host-side table: per BLAS {type, numNodes, numPrims, pad}
+    uint64_t total = w->blases.size() * 16;
+    if (dst && capacity >= total)
+      for (size_t i = 0; i < w->blases.size(); i++) {
+        uint32_t row[4] = {w->blases[i].type,
+            w->blases[i].bvh.numNodes,
+            w->blases[i].bvh.numPrims,
+            0};
+        std::memcpy((uint8_t *)dst + 16 * i, row, 16);
+      }
+    return total;
+  }
+  uint64_t total = 0;
+  for (auto &p : parts)
+    total += p.second;
+  if (!dst)
+    return total;
+  if (capacity < total)
+    return 0;
+  uint64_t off = 0;
+  for (auto &p : parts) {
+    cudaMemcpy((uint8_t *)dst + off, p.first, p.second, cudaMemcpyDeviceToHost);
+    off += p.second;
+  }
+  return total;
+}
+
+VRTX_API float vrtxWorldBuildMilliseconds(VRTXDevice d, VRTXObject world)
+{
+  if (!d || !world || O(world)->type != VRTX_WORLD)
+    return 0.f;
+  return static_cast<World *>(O(world))->buildMs;
+}
+
+VRTX_API float vrtxFrameKernelMilliseconds(VRTXDevice d, VRTXFrame f)
+{
+  if (!d || !f)
+    return 0.f;
+  auto *fr = static_cast<Frame *>(O(f));
+  if (!fr->rendered)
+    return 0.f;
+  fr->wait();
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, fr->evKStart, fr->evKEnd);
+  return ms;
+}
+
+VRTX_API int vrtxFrameKernelLaunches(VRTXDevice d, VRTXFrame f)
+{
+  if (!d || !f)
+    return 0;
+  return static_cast<Frame *>(O(f))->launches;
+}
+
+void vrtxInternalReport(VRTXDevice d, int severity, const char *msg)
+{
+  if (d)
+    D(d)->report(nullptr, severity, msg);
+}
+
+VRTX_API void *vrtxDeviceStream(VRTXDevice d)
+{
+  if (!d || !D(d)->init())
+    return nullptr;
+  return D(d)->stream;
+}
+
+} // extern "C"

@@ -1,0 +1,606 @@
+// Differentiable emission-absorption marcher (forward + adjoint), batched
+// over many views of many volumes in one persistent launch.
+//
+// The model is the one stated in include/vrtx.h next to vrtxDMForward. Its
+// classification and compositing are the reference scivis marcher's
+// (devices/rtx/gpu/volumeIntegration.h:46-103: TF lookup, alpha ->
+// 1 - (1 - alpha)^(step/unit), front-to-back accumulation), written in the
+// log-transmittance form so that
+//   * the forward sums sigma_k = (step/unit) * log(1 - alpha_k) with Kahan
+//     compensation (long rays keep T accurate), and
+//   * the adjoint walks the same samples in reverse from the stored end
+//     state (log T_end, sample count), recovering log T_k = log T_{k+1} -
+//     sigma_k without storing any per-sample state, and building the suffix
+//     radiance S_k = S_{k+1} + T_k a_k c_k from S_K = T_end * background, so
+//     dL/dsigma_k = g . (S_{k+1} - T_{k+1} c_k) needs no division.
+// Density is read as fp32, fp16 or bf16 and interpolated in fp32; TF
+// gradients are accumulated per tile in shared memory; density gradients go
+// to fp32 global memory with atomics.
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+
+#include <vector>
+
+#include "../../include/vrtx.h"
+#include "vmath.h"
+
+namespace vrtx {
+namespace {
+
+constexpr float kAlphaMax = 0.999f;
+constexpr float kLogTStop = -6.90775527898f; // log(1e-3)
+constexpr int kMaxSamples = 1 << 20; // per ray (the host also bounds step)
+
+struct DMVol
+{
+  const void *density;
+  int type;
+  int dims[3];
+  const float4 *tf;
+  int tfSize;
+  float scale, step, ratio, lo, hi;
+  float *gD;
+  float *gTF;
+  float *gS;
+};
+
+struct DMViewG
+{
+  int vol, w, h, tilesX;
+  f3 eye, d00, du, dv, bg;
+  long long pixOff;
+  unsigned tileStart;
+};
+
+template <typename T>
+__device__ __forceinline__ float ld(const T *p, size_t i);
+template <>
+__device__ __forceinline__ float ld<float>(const float *p, size_t i)
+{
+  return __ldg(p + i);
+}
+template <>
+__device__ __forceinline__ float ld<__half>(const __half *p, size_t i)
+{
+  return __half2float(__ldg(p + i));
+}
+template <>
+__device__ __forceinline__ float ld<__nv_bfloat16>(const __nv_bfloat16 *p, size_t i)
+{
+  return __bfloat162float(__ldg(p + i));
+}
+
+struct Tri
+{
+  size_t base;
+  int sx, sy, sz; // index strides to the +1 neighbour (0 on a 1-voxel axis)
+  float fx, fy, fz;
+};
+
+__device__ __forceinline__ void axis(float p, int n, int &i0, int &step, float &f)
+{
+  if (n < 2) {
+    i0 = 0;
+    step = 0;
+    f = 0.f;
+    return;
+  }
+  const float c = fminf(fmaxf(p, 0.f), float(n - 1));
+  i0 = min((int)floorf(c), n - 2);
+  step = 1;
+  f = c - float(i0);
+}
+
+__device__ __forceinline__ Tri triSetup(const DMVol &v, f3 p)
+{
+  int ix, iy, iz, sx, sy, sz;
+  Tri t;
+  axis(p.x, v.dims[0], ix, sx, t.fx);
+  axis(p.y, v.dims[1], iy, sy, t.fy);
+  axis(p.z, v.dims[2], iz, sz, t.fz);
+  const size_t X = v.dims[0], XY = (size_t)v.dims[0] * v.dims[1];
+  t.base = (size_t)iz * XY + (size_t)iy * X + ix;
+  t.sx = sx;
+  t.sy = sy * v.dims[0];
+  t.sz = (int)(sz * XY);
+  return t;
+}
+
+template <typename T>
+__device__ __forceinline__ float trilinear(const DMVol &v, const Tri &t)
+{
+  const T *D = reinterpret_cast<const T *>(v.density);
+  const size_t b = t.base;
+  const float c000 = ld(D, b), c100 = ld(D, b + t.sx);
+  const float c010 = ld(D, b + t.sy), c110 = ld(D, b + t.sy + t.sx);
+  const float c001 = ld(D, b + t.sz), c101 = ld(D, b + t.sz + t.sx);
+  const float c011 = ld(D, b + t.sz + t.sy), c111 = ld(D, b + t.sz + t.sy + t.sx);
+  const float c00 = c000 + t.fx * (c100 - c000);
+  const float c10 = c010 + t.fx * (c110 - c010);
+  const float c01 = c001 + t.fx * (c101 - c001);
+  const float c11 = c011 + t.fx * (c111 - c011);
+  const float c0 = c00 + t.fy * (c10 - c00);
+  const float c1 = c01 + t.fy * (c11 - c01);
+  return c0 + t.fz * (c1 - c0);
+}
+
+struct Classified
+{
+  float4 c; // rgb + raw TF alpha
+  int i0;
+  float f;
+  float dxds; // d(x)/d(s), 0 where the value range clamps
+};
+
+__device__ __forceinline__ Classified classify(const DMVol &v, float s)
+{
+  Classified r;
+  const float range = v.hi - v.lo;
+  float u = (s - v.lo) / range;
+  r.dxds = (u > 0.f && u < 1.f) ? float(v.tfSize - 1) / range : 0.f;
+  u = fminf(fmaxf(u, 0.f), 1.f);
+  const float x = u * float(v.tfSize - 1);
+  r.i0 = min((int)floorf(x), v.tfSize - 2);
+  r.f = x - float(r.i0);
+  const float4 a = __ldg(v.tf + r.i0), b = __ldg(v.tf + r.i0 + 1);
+  r.c = make_float4(a.x + r.f * (b.x - a.x),
+      a.y + r.f * (b.y - a.y),
+      a.z + r.f * (b.z - a.z),
+      a.w + r.f * (b.w - a.w));
+  return r;
+}
+
+__device__ __forceinline__ bool rayBox(
+    f3 o, f3 d, const int dims[3], float &t0, float &t1)
+{
+  const f3 inv = mk3(1.f / d.x, 1.f / d.y, 1.f / d.z);
+  const f3 hi = mk3(float(dims[0] - 1), float(dims[1] - 1), float(dims[2] - 1));
+  const f3 a = (mk3(0.f, 0.f, 0.f) - o) * inv;
+  const f3 b = (hi - o) * inv;
+  t0 = fmaxf(compMax(fmin3(a, b)), 0.f);
+  t1 = compMin(fmax3(a, b));
+  return t0 < t1;
+}
+
+__device__ __forceinline__ int findView(const DMViewG *views, int n, unsigned item)
+{
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (views[mid].tileStart <= item)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  return lo;
+}
+
+__device__ __forceinline__ f3 viewRay(const DMViewG &vw, int px, int py)
+{
+  return normalize(vw.d00 + (float(px) + 0.5f) * vw.du + (float(py) + 0.5f) * vw.dv);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_dmForward(const DMVol *vols,
+    const DMViewG *views,
+    int numViews,
+    unsigned numItems,
+    unsigned *counter,
+    int tileW,
+    int tileH,
+    float *image,
+    float *state)
+{
+  __shared__ unsigned item;
+  while (true) {
+    __syncthreads();
+    if (threadIdx.x == 0)
+      item = atomicAdd(counter, 1u);
+    __syncthreads();
+    const unsigned it = item;
+    if (it >= numItems)
+      break;
+    const DMViewG vw = views[findView(views, numViews, it)];
+    const unsigned tile = it - vw.tileStart;
+    const int px = (int)(tile % vw.tilesX) * tileW + (int)threadIdx.x % tileW;
+    const int py = (int)(tile / vw.tilesX) * tileH + (int)threadIdx.x / tileW;
+    if (px >= vw.w || py >= vw.h)
+      continue;
+    const DMVol v = vols[vw.vol];
+    const f3 d = viewRay(vw, px, py);
+    float t0, t1;
+    f3 C = mk3(0.f, 0.f, 0.f);
+    float logT = 0.f, comp = 0.f;
+    int k = 0;
+    if (rayBox(vw.eye, d, v.dims, t0, t1)) {
+      while (k < kMaxSamples) {
+        const float t = t0 + (float(k) + 0.5f) * v.step;
+        if (t > t1)
+          break;
+        const f3 p = vw.eye + t * d;
+        const float s = trilinear<T>(v, triSetup(v, p));
+        const Classified cl = classify(v, s);
+        const float alpha = fminf(cl.c.w * v.scale, kAlphaMax);
+        const float sigma = v.ratio * log1pf(-alpha);
+        const float T0 = __expf(logT);
+        const float a = -expm1f(sigma);
+        C += (T0 * a) * mk3(cl.c.x, cl.c.y, cl.c.z);
+        // Kahan: logT += sigma
+        const float y = sigma - comp;
+        const float nt = logT + y;
+        comp = (nt - logT) - y;
+        logT = nt;
+        k++;
+        if (logT < kLogTStop)
+          break;
+      }
+    }
+    const float Tend = __expf(logT);
+    const size_t pix = (size_t)vw.pixOff + (size_t)py * vw.w + px;
+    image[3 * pix + 0] = C.x + Tend * vw.bg.x;
+    image[3 * pix + 1] = C.y + Tend * vw.bg.y;
+    image[3 * pix + 2] = C.z + Tend * vw.bg.z;
+    state[2 * pix + 0] = logT;
+    state[2 * pix + 1] = __int_as_float(k);
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_dmBackward(const DMVol *vols,
+    const DMViewG *views,
+    int numViews,
+    unsigned numItems,
+    unsigned *counter,
+    int tileW,
+    int tileH,
+    const float *state,
+    const float *gradImage)
+{
+  extern __shared__ float sTF[]; // tfSize x 4 per tile
+  __shared__ unsigned item;
+  __shared__ float sScale[8];
+  while (true) {
+    __syncthreads();
+    if (threadIdx.x == 0)
+      item = atomicAdd(counter, 1u);
+    __syncthreads();
+    const unsigned it = item;
+    if (it >= numItems)
+      break;
+    const DMViewG vw = views[findView(views, numViews, it)];
+    const DMVol v = vols[vw.vol];
+    for (int i = threadIdx.x; i < v.tfSize * 4; i += blockDim.x)
+      sTF[i] = 0.f;
+    __syncthreads();
+    const unsigned tile = it - vw.tileStart;
+    const int px = (int)(tile % vw.tilesX) * tileW + (int)threadIdx.x % tileW;
+    const int py = (int)(tile / vw.tilesX) * tileH + (int)threadIdx.x / tileW;
+    float gScale = 0.f;
+    if (px < vw.w && py < vw.h) {
+      const size_t pix = (size_t)vw.pixOff + (size_t)py * vw.w + px;
+      const int K = __float_as_int(state[2 * pix + 1]);
+      float logT = state[2 * pix + 0];
+      const f3 g = mk3(gradImage[3 * pix], gradImage[3 * pix + 1], gradImage[3 * pix + 2]);
+      const f3 d = viewRay(vw, px, py);
+      float t0 = 0.f, t1 = 0.f;
+      if (K > 0 && rayBox(vw.eye, d, v.dims, t0, t1)) {
+        float Tnext = __expf(logT);
+        f3 S = Tnext * vw.bg;
+        float comp = 0.f;
+        for (int k = K - 1; k >= 0; k--) {
+          const float t = t0 + (float(k) + 0.5f) * v.step;
+          const f3 p = vw.eye + t * d;
+          const Tri tr = triSetup(v, p);
+          const float s = trilinear<T>(v, tr);
+          const Classified cl = classify(v, s);
+          const float araw = cl.c.w * v.scale;
+          const float alpha = fminf(araw, kAlphaMax);
+          const float sigma = v.ratio * log1pf(-alpha);
+          // Kahan: logT -= sigma
+          const float y = -sigma - comp;
+          const float nt = logT + y;
+          comp = (nt - logT) - y;
+          logT = nt;
+          const float Tk = __expf(logT);
+          const float a = -expm1f(sigma);
+          const float w = Tk * a;
+          const f3 c = mk3(cl.c.x, cl.c.y, cl.c.z);
+          const f3 dc = w * g;
+          const float dSigma = dot(g, S - Tnext * c);
+          S += w * c;
+          Tnext = Tk;
+          const float dAlpha =
+              araw < kAlphaMax ? dSigma * (-v.ratio / (1.f - alpha)) : 0.f;
+          const float dA = dAlpha * v.scale;
+          gScale += dAlpha * cl.c.w;
+          if (v.gTF) {
+            const float f0 = 1.f - cl.f, f1 = cl.f;
+            float *e0 = sTF + 4 * cl.i0;
+            atomicAdd(e0 + 0, f0 * dc.x);
+            atomicAdd(e0 + 1, f0 * dc.y);
+            atomicAdd(e0 + 2, f0 * dc.z);
+            atomicAdd(e0 + 3, f0 * dA);
+            atomicAdd(e0 + 4, f1 * dc.x);
+            atomicAdd(e0 + 5, f1 * dc.y);
+            atomicAdd(e0 + 6, f1 * dc.z);
+            atomicAdd(e0 + 7, f1 * dA);
+          }
+          if (v.gD && cl.dxds != 0.f) {
+            const float4 ea = __ldg(v.tf + cl.i0), eb = __ldg(v.tf + cl.i0 + 1);
+            const float dval = dc.x * (eb.x - ea.x) + dc.y * (eb.y - ea.y)
+                + dc.z * (eb.z - ea.z) + dA * (eb.w - ea.w);
+            const float ds = dval * cl.dxds;
+            if (ds != 0.f) {
+              const float gx0 = 1.f - tr.fx, gy0 = 1.f - tr.fy, gz0 = 1.f - tr.fz;
+              float *G = v.gD + tr.base;
+              atomicAdd(G, ds * gx0 * gy0 * gz0);
+              atomicAdd(G + tr.sx, ds * tr.fx * gy0 * gz0);
+              atomicAdd(G + tr.sy, ds * gx0 * tr.fy * gz0);
+              atomicAdd(G + tr.sy + tr.sx, ds * tr.fx * tr.fy * gz0);
+              atomicAdd(G + tr.sz, ds * gx0 * gy0 * tr.fz);
+              atomicAdd(G + tr.sz + tr.sx, ds * tr.fx * gy0 * tr.fz);
+              atomicAdd(G + tr.sz + tr.sy, ds * gx0 * tr.fy * tr.fz);
+              atomicAdd(G + tr.sz + tr.sy + tr.sx, ds * tr.fx * tr.fy * tr.fz);
+            }
+          }
+        }
+      }
+    }
+    // opacity-scale gradient: block reduction, one atomic per tile
+    for (int o = 16; o > 0; o >>= 1)
+      gScale += __shfl_xor_sync(0xffffffffu, gScale, o);
+    if ((threadIdx.x & 31) == 0)
+      sScale[threadIdx.x >> 5] = gScale;
+    __syncthreads();
+    if (threadIdx.x == 0 && v.gS) {
+      float sum = 0.f;
+      for (int i = 0; i < (int)(blockDim.x >> 5); i++)
+        sum += sScale[i];
+      atomicAdd(v.gS, sum);
+    }
+    if (v.gTF)
+      for (int i = threadIdx.x; i < v.tfSize * 4; i += blockDim.x)
+        if (sTF[i] != 0.f)
+          atomicAdd(v.gTF + i, sTF[i]);
+  }
+}
+
+struct Prepared
+{
+  DMVol *dVols = nullptr;
+  DMViewG *dViews = nullptr;
+  unsigned *counter = nullptr;
+  unsigned numItems = 0;
+  int type = 0;
+  int maxTf = 0;
+};
+
+int prepare(VRTXDevice dev,
+    const VRTXDMVolume *volumes,
+    int numVolumes,
+    const VRTXDMView *views,
+    int numViews,
+    int tileW,
+    int tileH,
+    cudaStream_t s,
+    Prepared &P,
+    const char **err)
+{
+  (void)dev;
+  if (!volumes || numVolumes <= 0 || !views || numViews <= 0) {
+    *err = "no volumes or no views";
+    return -1;
+  }
+  if (tileW <= 0 || tileH <= 0 || (tileW * tileH) % 32 != 0 || tileW * tileH > 256) {
+    *err = "tileW * tileH must be a positive multiple of 32, at most 256";
+    return -2;
+  }
+  std::vector<DMVol> hv(numVolumes);
+  for (int i = 0; i < numVolumes; i++) {
+    const VRTXDMVolume &v = volumes[i];
+    if (!v.density || !v.tf || v.tfSize < 2 || v.tfSize > 256 || v.dims[0] < 1
+        || v.dims[1] < 1 || v.dims[2] < 1 || !(v.step >= 1e-3f)
+        || !(v.unitDistance > 0.f) || !(v.valueHi != v.valueLo)) {
+      *err = "invalid volume description";
+      return -3;
+    }
+    if (v.densityType != VRTX_FLOAT32 && v.densityType != VRTX_FLOAT16
+        && v.densityType != VRTX_BFLOAT16) {
+      *err = "density must be FLOAT32, FLOAT16 or BFLOAT16";
+      return -4;
+    }
+    if (i == 0)
+      P.type = v.densityType;
+    else if (v.densityType != P.type) {
+      *err = "all volumes of one launch must share the density type";
+      return -5;
+    }
+    P.maxTf = v.tfSize > P.maxTf ? v.tfSize : P.maxTf;
+    DMVol &o = hv[i];
+    o.density = v.density;
+    o.type = v.densityType;
+    for (int k = 0; k < 3; k++)
+      o.dims[k] = v.dims[k];
+    o.tf = reinterpret_cast<const float4 *>(v.tf);
+    o.tfSize = v.tfSize;
+    o.scale = v.opacityScale;
+    o.step = v.step;
+    o.ratio = v.step / v.unitDistance;
+    o.lo = v.valueLo;
+    o.hi = v.valueHi;
+    o.gD = v.gradDensity;
+    o.gTF = v.gradTf;
+    o.gS = v.gradOpacityScale;
+  }
+  std::vector<DMViewG> hw(numViews);
+  unsigned items = 0;
+  for (int i = 0; i < numViews; i++) {
+    const VRTXDMView &w = views[i];
+    if (w.volume < 0 || w.volume >= numVolumes || w.width <= 0 || w.height <= 0
+        || w.pixelOffset < 0) {
+      *err = "invalid view description";
+      return -6;
+    }
+    DMViewG &o = hw[i];
+    o.vol = w.volume;
+    o.w = w.width;
+    o.h = w.height;
+    o.tilesX = (w.width + tileW - 1) / tileW;
+    const int tilesY = (w.height + tileH - 1) / tileH;
+    o.eye = mk3(w.eye[0], w.eye[1], w.eye[2]);
+    o.d00 = mk3(w.d00[0], w.d00[1], w.d00[2]);
+    o.du = mk3(w.du[0], w.du[1], w.du[2]);
+    o.dv = mk3(w.dv[0], w.dv[1], w.dv[2]);
+    o.bg = mk3(w.background[0], w.background[1], w.background[2]);
+    o.pixOff = w.pixelOffset;
+    o.tileStart = items;
+    items += (unsigned)(o.tilesX * tilesY);
+  }
+  P.numItems = items;
+  // one stream-ordered block: [counter | volumes | views]
+  const size_t offV = 256, offW = offV + ((sizeof(DMVol) * numVolumes + 255) / 256) * 256;
+  const size_t bytes = offW + sizeof(DMViewG) * numViews;
+  uint8_t *blk = nullptr;
+  if (cudaMallocAsync((void **)&blk, bytes, s) != cudaSuccess) {
+    cudaGetLastError();
+    *err = "device allocation failed";
+    return -7;
+  }
+  P.counter = reinterpret_cast<unsigned *>(blk);
+  P.dVols = reinterpret_cast<DMVol *>(blk + offV);
+  P.dViews = reinterpret_cast<DMViewG *>(blk + offW);
+  cudaMemsetAsync(blk, 0, 256, s);
+  cudaMemcpyAsync(P.dVols, hv.data(), sizeof(DMVol) * numVolumes, cudaMemcpyHostToDevice, s);
+  cudaMemcpyAsync(P.dViews, hw.data(), sizeof(DMViewG) * numViews, cudaMemcpyHostToDevice, s);
+  return 0;
+}
+
+int gridFor(const void *kernel, int threads, size_t smem)
+{
+  int dev = 0, sms = 0, per = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, threads, smem);
+  return sms * (per > 0 ? per : 1);
+}
+
+void reportErr(VRTXDevice d, const char *msg);
+
+} // namespace
+
+} // namespace vrtx
+
+// status reporting lives in device.cpp
+extern "C" void vrtxInternalReport(VRTXDevice d, int severity, const char *msg);
+
+namespace vrtx {
+namespace {
+void reportErr(VRTXDevice d, const char *msg)
+{
+  vrtxInternalReport(d, VRTX_SEVERITY_ERROR, msg);
+}
+} // namespace
+} // namespace vrtx
+
+using namespace vrtx;
+
+extern "C" {
+
+VRTX_API int vrtxDMForward(VRTXDevice d,
+    const VRTXDMVolume *volumes,
+    int numVolumes,
+    const VRTXDMView *views,
+    int numViews,
+    float *image,
+    float *state,
+    int tileW,
+    int tileH,
+    void *stream)
+{
+  cudaStream_t s = (cudaStream_t)stream;
+  Prepared P;
+  const char *err = nullptr;
+  if (!image || !state) {
+    reportErr(d, "vrtxDMForward: image and state are required");
+    return -1;
+  }
+  int rc = prepare(d, volumes, numVolumes, views, numViews, tileW, tileH, s, P, &err);
+  if (rc) {
+    reportErr(d, err);
+    return rc;
+  }
+  const int threads = tileW * tileH;
+  switch (P.type) {
+  case VRTX_FLOAT16:
+    k_dmForward<__half><<<gridFor((const void *)k_dmForward<__half>, threads, 0), threads, 0, s>>>(
+        P.dVols, P.dViews, numViews, P.numItems, P.counter, tileW, tileH, image, state);
+    break;
+  case VRTX_BFLOAT16:
+    k_dmForward<__nv_bfloat16><<<gridFor((const void *)k_dmForward<__nv_bfloat16>, threads, 0), threads, 0, s>>>(
+        P.dVols, P.dViews, numViews, P.numItems, P.counter, tileW, tileH, image, state);
+    break;
+  default:
+    k_dmForward<float><<<gridFor((const void *)k_dmForward<float>, threads, 0), threads, 0, s>>>(
+        P.dVols, P.dViews, numViews, P.numItems, P.counter, tileW, tileH, image, state);
+    break;
+  }
+  const cudaError_t e = cudaGetLastError();
+  cudaFreeAsync(P.counter, s);
+  if (e != cudaSuccess) {
+    reportErr(d, cudaGetErrorString(e));
+    return -8;
+  }
+  return 0;
+}
+
+VRTX_API int vrtxDMBackward(VRTXDevice d,
+    const VRTXDMVolume *volumes,
+    int numVolumes,
+    const VRTXDMView *views,
+    int numViews,
+    const float *image,
+    const float *state,
+    const float *gradImage,
+    int tileW,
+    int tileH,
+    void *stream)
+{
+  (void)image;
+  cudaStream_t s = (cudaStream_t)stream;
+  Prepared P;
+  const char *err = nullptr;
+  if (!state || !gradImage) {
+    reportErr(d, "vrtxDMBackward: state and gradImage are required");
+    return -1;
+  }
+  int rc = prepare(d, volumes, numVolumes, views, numViews, tileW, tileH, s, P, &err);
+  if (rc) {
+    reportErr(d, err);
+    return rc;
+  }
+  const int threads = tileW * tileH;
+  const size_t smem = sizeof(float) * 4 * P.maxTf;
+  switch (P.type) {
+  case VRTX_FLOAT16:
+    k_dmBackward<__half><<<gridFor((const void *)k_dmBackward<__half>, threads, smem), threads, smem, s>>>(
+        P.dVols, P.dViews, numViews, P.numItems, P.counter, tileW, tileH, state, gradImage);
+    break;
+  case VRTX_BFLOAT16:
+    k_dmBackward<__nv_bfloat16><<<gridFor((const void *)k_dmBackward<__nv_bfloat16>, threads, smem), threads, smem, s>>>(
+        P.dVols, P.dViews, numViews, P.numItems, P.counter, tileW, tileH, state, gradImage);
+    break;
+  default:
+    k_dmBackward<float><<<gridFor((const void *)k_dmBackward<float>, threads, smem), threads, smem, s>>>(
+        P.dVols, P.dViews, numViews, P.numItems, P.counter, tileW, tileH, state, gradImage);
+    break;
+  }
+  const cudaError_t e = cudaGetLastError();
+  cudaFreeAsync(P.counter, s);
+  if (e != cudaSuccess) {
+    reportErr(d, cudaGetErrorString(e));
+    return -8;
+  }
+  return 0;
+}
+
+} // extern "C"

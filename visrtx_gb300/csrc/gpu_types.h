@@ -1,0 +1,266 @@
+// Device-side data layout of libvrtx: scene registries, acceleration
+// structures, camera, renderer and framebuffer parameters.
+//
+// The fields follow the reference's GPU structs where they carry the same
+// meaning (devices/rtx/gpu/gpu_objects.h: GeometryGPUData, SurfaceGPUData,
+// CameraGPUData, RendererGPUData, FramebufferGPUData), re-laid out for this
+// kernel design: no OptiX handles, explicit BVH8 nodes and primitive records.
+#pragma once
+
+#include "vmath.h"
+
+namespace vrtx {
+
+// ---------------------------------------------------------------------------
+// Scene registries
+// ---------------------------------------------------------------------------
+
+enum GeomType : uint32_t
+{
+  GEOM_TRIANGLE = 0,
+  GEOM_SPHERE = 1,
+  GEOM_NUM_TYPES = 2
+};
+
+struct GeometryGPU
+{
+  uint32_t type;
+  uint32_t numPrims;
+  const f3 *vertices; // triangle: vertex.position; sphere: vertex.position
+  const uint32_t *indices; // triangle: uvec3 per prim or NULL (soup);
+                           // sphere: primitive.index or NULL
+  const f3 *normals; // triangle vertex.normal or NULL
+  const f3 *normalsFV; // triangle faceVarying.normal or NULL
+  const uint32_t *primIds; // primitive.id or NULL
+  const float *radii; // sphere vertex.radius or NULL
+  float radius; // sphere uniform radius (default 0.01, Sphere.cu:52)
+  uint32_t cullBackfaces; // VISRTX_TRIANGLE_BACK_FACE_CULLING extension
+};
+
+enum AlphaMode : int
+{
+  ALPHA_OPAQUE = 0,
+  ALPHA_BLEND = 1,
+  ALPHA_MASK = 2
+};
+
+struct MaterialGPU
+{
+  f3 color; // matte "color" (default 0.8 grey, Matte.cpp:44)
+  float opacity; // color.w * opacity, before the alpha mode
+  int alphaMode;
+  float cutoff;
+  int pad[2];
+};
+
+struct SurfaceGPU
+{
+  uint32_t geometry;
+  uint32_t material;
+  uint32_t id; // Surface "id" (default ~0u, Surface.cpp:44)
+  uint32_t pad;
+};
+
+enum LightType : int
+{
+  LIGHT_DIRECTIONAL = 0,
+  LIGHT_POINT = 1
+};
+
+struct LightGPU
+{
+  int type;
+  f3 dirToLight; // directional: xfmVec(xfm, -direction) (sampleLight.h:60-70)
+  f3 radiance; // color * irradiance (or intensity for point)
+  f3 position; // point light
+};
+
+// ---------------------------------------------------------------------------
+// Compressed 8-wide BVH (one 80-byte node = five 16-byte loads)
+// ---------------------------------------------------------------------------
+//
+// Child boxes are quantised to 8 bits per plane relative to the node origin p
+// with a per-axis power-of-two scale 2^e (e stored as a biased float
+// exponent). Quantisation rounds outward, so every decoded child box
+// contains the exact one. meta[i] == 0 marks an empty slot; an internal
+// child has meta = 0b001'xxxxx with xxxxx = 24 + slot; a leaf child has meta
+// = (unary prim count) << 5 | (offset of its first prim from primBase).
+// Internal children are stored contiguously from childBase in slot order
+// (imask bit i set <=> slot i is internal).
+struct alignas(16) BVH8Node
+{
+  float px, py, pz;
+  uint8_t ex, ey, ez, imask;
+  uint32_t childBase;
+  uint32_t primBase;
+  uint8_t meta[8];
+  uint8_t qlox[8], qloy[8], qloz[8];
+  uint8_t qhix[8], qhiy[8], qhiz[8];
+};
+static_assert(sizeof(BVH8Node) == 80, "BVH8Node must be 80 bytes");
+
+// Triangle leaf record: the three vertices, gathered in leaf order.
+struct alignas(16) TriRecord
+{
+  float4 v0; // .w = primID (bit pattern) within its geometry
+  float4 v1; // .w = global surface index (bit pattern)
+  float4 v2; // .w unused
+};
+
+struct alignas(16) SphereRecord
+{
+  float4 cr; // center, radius
+  uint32_t primID; // OptiX-style primitive index within the geometry
+  uint32_t surface; // global surface index
+  uint32_t pad[2];
+};
+
+// One bottom-level structure: a group's triangles or a group's spheres.
+struct BLASDesc
+{
+  const BVH8Node *nodes;
+  const void *prims; // TriRecord* or SphereRecord*
+  uint32_t type; // GeomType
+  uint32_t numPrims;
+  box3 bounds;
+};
+
+// One top-level leaf: (instance, transform index, primitive class).
+struct alignas(16) InstanceRecord
+{
+  xfm34 worldToObject;
+  xfm34 objectToWorld;
+  uint32_t blas; // index into the BLAS table
+  uint32_t userId; // Instance "id" / id array entry (Instance.cpp:115-118)
+  uint32_t pad[2];
+};
+
+// ---------------------------------------------------------------------------
+// Volumes
+// ---------------------------------------------------------------------------
+
+struct VolumeGPU
+{
+  cudaTextureObject_t field; // 3D texture, normalised coords, clamp
+  cudaTextureObject_t tf; // 1D float4 texture, linear, clamp (0 = uniform)
+  f3 origin;
+  f3 spacing;
+  f3 invSpacing; // 1 / (spacing * dims) (StructuredRegularField.cpp:188-189)
+  box3 bounds; // [origin, origin + (dims - 1) * spacing]
+  float stepSize; // min(spacing) / 2
+  float oneOverUnitDistance;
+  float valueLo, valueHi; // TF valueRange
+  f3 uniformColor;
+  float uniformOpacity;
+  uint32_t id; // Volume "id"
+  uint32_t instId; // instance user id
+  uint32_t hasTF;
+  uint32_t pad0;
+  xfm34 worldToObject;
+  // conservative macrocell majorants (max TF opacity reachable in a cell)
+  const float *majorants;
+  int mcDims[3];
+  int dims[3]; // voxel dims
+};
+
+// ---------------------------------------------------------------------------
+// Camera / renderer / framebuffer
+// ---------------------------------------------------------------------------
+
+enum CameraType : int
+{
+  CAMERA_PERSPECTIVE = 0,
+  CAMERA_ORTHOGRAPHIC = 1
+};
+
+struct CameraGPU
+{
+  int type;
+  float region[4]; // imageRegion (lo.x, lo.y, hi.x, hi.y)
+  f3 pos;
+  f3 dir;
+  f3 dir00, dirDu, dirDv; // perspective (Perspective.cpp:51-58)
+  float scaledAperture, aspect;
+  f3 pos00, posDu, posDv; // orthographic (Orthographic.cpp:47-50)
+};
+
+enum RendererType : int
+{
+  RENDERER_DIRECT_LIGHT = 0, // "default", "directLight"
+  RENDERER_RAYCAST = 1,
+  RENDERER_AO = 2,
+  RENDERER_DPT = 3 // "dpt", "diffuse_pathtracer"
+};
+
+struct RendererGPU
+{
+  int type;
+  float4 background;
+  f3 ambientColor;
+  float ambientIntensity;
+  float occlusionDistance;
+  int cullTriangleBF;
+  float invVolumeSamplingRate;
+  int numIterations; // pixelSamples
+  int maxRayDepth;
+  int aoSamples;
+  int maxDepth; // dpt
+  float lightFalloff;
+};
+
+enum FrameFormat : int
+{
+  FORMAT_SRGB = 0,
+  FORMAT_UINT = 1,
+  FORMAT_FLOAT = 2
+};
+
+struct FramebufferGPU
+{
+  uint32_t w, h;
+  float invW, invH;
+  int frameID;
+  int checkerboardID;
+  int format;
+  float4 *accum;
+  uint32_t *outColorU;
+  float4 *outColorF;
+  float *depth;
+  uint32_t *primID;
+  uint32_t *objID;
+  uint32_t *instID;
+  f3 *albedo;
+  f3 *normal;
+};
+
+struct WorldGPU
+{
+  const BVH8Node *tlasNodes;
+  const InstanceRecord *instances;
+  uint32_t numInstances;
+  uint32_t numLights;
+  const BLASDesc *blas;
+  const SurfaceGPU *surfaces;
+  const GeometryGPU *geometries;
+  const MaterialGPU *materials;
+  const LightGPU *lights;
+  const VolumeGPU *volumes;
+  uint32_t numVolumes;
+  uint32_t allOpaque; // every material is opaque: any-hit = first hit
+};
+
+struct FrameParams
+{
+  WorldGPU world;
+  CameraGPU camera;
+  RendererGPU renderer;
+  FramebufferGPU fb;
+  uint32_t *workCounter; // persistent scheduling counter (zeroed per launch)
+  uint32_t *errorFlag; // bit 0: traversal stack overflow
+  unsigned long long *stats; // [0] rays, [1] nodes, [2] tri tests,
+                             // [3] sphere tests, [4] BLAS entries
+  uint32_t numTilesX, numTilesY;
+  uint32_t launchW, launchH; // checkerboarding halves these
+};
+
+} // namespace vrtx

@@ -1,0 +1,388 @@
+// Host object model of libvrtx: the ANARI objects of the VisRTX device
+// (devices/rtx/{array,camera,frame,renderer,scene}) reduced to what the hot
+// path reads, with helium's parameter/commit/refcount semantics.
+#pragma once
+
+#include <atomic>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/vrtx.h"
+#include "bvh.h"
+#include "render.h"
+
+namespace vrtx {
+
+struct Device;
+struct Object;
+
+uint64_t newStamp();
+size_t sizeOfType(int t);
+bool isObjectType(int t);
+const char *typeName(int t);
+
+struct Param
+{
+  int type = VRTX_UNKNOWN;
+  std::vector<uint8_t> bytes;
+  std::string str;
+  Object *obj = nullptr;
+};
+
+struct Object
+{
+  Device *dev;
+  int type;
+  std::string subtype;
+  std::atomic<int> refs{1}; // internal + public references
+  std::atomic<int> publicRefs{1}; // references held by the application
+  std::map<std::string, Param> pending;
+  std::map<std::string, Param> params; // committed
+  uint64_t commitStamp = 0;
+
+  Object(Device *d, int t, const std::string &st = "");
+  virtual ~Object();
+
+  void setParam(const std::string &name, int type, const void *mem);
+  void unsetParam(const std::string &name);
+  void unsetAll();
+  void commitParams();
+  virtual void commit() {}
+  virtual bool isValid() const
+  {
+    return true;
+  }
+  virtual bool getProperty(
+      const std::string &name, int type, void *mem, uint64_t size, uint32_t mask);
+  // newest stamp of this object and everything it references
+  virtual uint64_t deepStamp() const
+  {
+    return commitStamp;
+  }
+
+  bool has(const std::string &name, int type) const;
+  template <typename T>
+  T get(const std::string &name, int type, T def) const
+  {
+    auto it = params.find(name);
+    if (it == params.end() || it->second.type != type
+        || it->second.bytes.size() < sizeof(T))
+      return def;
+    T v;
+    std::memcpy(&v, it->second.bytes.data(), sizeof(T));
+    return v;
+  }
+  Object *getObject(const std::string &name, int type) const;
+  std::string getString(const std::string &name, const std::string &def) const;
+
+  void report(int severity, const char *fmt, ...) const;
+};
+
+void retainObj(Object *o);
+void releaseObj(Object *o);
+
+// ---------------------------------------------------------------------------
+
+struct Array : Object
+{
+  int elemType;
+  uint64_t n[3];
+  const void *appMem = nullptr;
+  VRTXMemoryDeleter deleter = nullptr;
+  const void *deleterPtr = nullptr;
+  std::vector<uint8_t> owned; // managed arrays / privatised copies
+  bool appIsDevice = false;
+  void *dptr = nullptr;
+  size_t devBytes = 0;
+  uint64_t dataStamp = 0;
+  uint64_t devStamp = 0;
+  std::vector<Object *> handles; // object arrays: retained elements
+
+  Array(Device *d,
+      int dims,
+      const void *mem,
+      VRTXMemoryDeleter del,
+      const void *delPtr,
+      int et,
+      uint64_t n1,
+      uint64_t n2,
+      uint64_t n3);
+  ~Array() override;
+  uint64_t count() const
+  {
+    return n[0] * n[1] * n[2];
+  }
+  size_t bytes() const
+  {
+    return count() * sizeOfType(elemType);
+  }
+  const void *hostData() const;
+  // device copy (uploads on first use after a data change)
+  const void *deviceData();
+  void *map();
+  void unmap();
+  void refreshHandles();
+  // shared app memory -> owned copy, once the app no longer holds the array
+  // (Array.cpp:164-182)
+  void privatize();
+  uint64_t deepStamp() const override
+  {
+    return dataStamp > commitStamp ? dataStamp : commitStamp;
+  }
+};
+
+struct Camera : Object
+{
+  CameraGPU gpu{};
+  using Object::Object;
+  void commit() override;
+};
+
+struct Geometry : Object
+{
+  using Object::Object;
+  Array *vertex = nullptr, *index = nullptr, *normal = nullptr,
+        *normalFV = nullptr, *primId = nullptr, *radius = nullptr;
+  float globalRadius = 0.01f;
+  bool cull = false;
+  uint32_t numPrims = 0;
+  void commit() override;
+  bool isValid() const override;
+  uint64_t deepStamp() const override;
+  int geomClass() const
+  {
+    return subtype == "sphere" ? GEOM_SPHERE : GEOM_TRIANGLE;
+  }
+  GeometryGPU gpuData();
+};
+
+struct Material : Object
+{
+  using Object::Object;
+  MaterialGPU gpu{};
+  void commit() override;
+};
+
+struct Light : Object
+{
+  using Object::Object;
+  LightGPU gpu{};
+  void commit() override;
+};
+
+struct Surface : Object
+{
+  using Object::Object;
+  Geometry *geometry = nullptr;
+  Material *material = nullptr;
+  uint32_t id = ~0u;
+  void commit() override;
+  bool isValid() const override;
+  uint64_t deepStamp() const override;
+};
+
+struct SpatialField : Object
+{
+  using Object::Object;
+  Array *data = nullptr;
+  f3 origin{0.f, 0.f, 0.f}, spacing{1.f, 1.f, 1.f};
+  std::string filter = "linear";
+  cudaArray_t cuArray = nullptr;
+  cudaTextureObject_t tex = 0, pointTex = 0;
+  int dims[3] = {0, 0, 0};
+  int mcDims[3] = {0, 0, 0};
+  float *ranges = nullptr; // 2 floats per macrocell
+  uint64_t builtStamp = 0;
+  ~SpatialField() override;
+  void commit() override;
+  bool isValid() const override;
+  uint64_t deepStamp() const override;
+  void cleanup();
+  bool ensureBuilt();
+  box3 bounds() const;
+  float stepSize() const;
+};
+
+struct Volume : Object
+{
+  using Object::Object;
+  SpatialField *field = nullptr;
+  Array *color = nullptr, *opacity = nullptr;
+  float valueRange[2] = {0.f, 1.f};
+  float unitDistance = 1.f;
+  f3 uniformColor{1.f, 1.f, 1.f};
+  float uniformColorW = 1.f;
+  float uniformOpacity = 1.f;
+  uint32_t id = ~0u;
+  std::vector<float> tf; // 256 x RGBA
+  cudaArray_t tfArray = nullptr;
+  cudaTextureObject_t tfTex = 0;
+  float4 *tfDev = nullptr;
+  float *majorants = nullptr;
+  uint64_t builtStamp = 0;
+  ~Volume() override;
+  void commit() override;
+  bool isValid() const override;
+  uint64_t deepStamp() const override;
+  void cleanup();
+  bool ensureBuilt();
+  void discretize();
+};
+
+struct Group : Object
+{
+  using Object::Object;
+  Array *surfaces = nullptr, *volumes = nullptr, *lights = nullptr;
+  void commit() override;
+  uint64_t deepStamp() const override;
+  std::vector<Surface *> validSurfaces() const;
+  std::vector<Volume *> validVolumes() const;
+  std::vector<Light *> validLights() const;
+  bool getProperty(const std::string &name,
+      int type,
+      void *mem,
+      uint64_t size,
+      uint32_t mask) override;
+};
+
+struct Instance : Object
+{
+  using Object::Object;
+  Group *group = nullptr;
+  Array *xfmArray = nullptr, *idArray = nullptr;
+  float xfm[12]; // 3 rows x 4
+  uint32_t id = ~0u;
+  void commit() override;
+  bool isValid() const override
+  {
+    return group != nullptr;
+  }
+  uint64_t deepStamp() const override;
+  size_t numTransforms() const;
+  void transform(size_t i, float out[12]) const;
+  uint32_t userID(size_t i) const;
+};
+
+struct BLASBuild
+{
+  BVH8Build bvh;
+  void *records = nullptr;
+  uint32_t type = 0;
+  uint32_t numPrims = 0;
+};
+
+struct World : Object
+{
+  using Object::Object;
+  Array *instances = nullptr;
+  Array *zeroSurfaces = nullptr, *zeroVolumes = nullptr, *zeroLights = nullptr;
+  uint32_t id = ~0u;
+  Group *zeroGroup = nullptr;
+  Instance *zeroInstance = nullptr;
+
+  // built state
+  uint64_t builtStamp = 0;
+  WorldGPU gpu{};
+  std::vector<BLASBuild> blases;
+  BVH8Build tlas;
+  std::vector<void *> allocations;
+  box3 worldBounds = emptyBox();
+  float buildMs = 0.f;
+
+  ~World() override;
+  void commit() override;
+  uint64_t deepStamp() const override;
+  bool rebuild();
+  void freeBuilt();
+  std::vector<Instance *> instanceList() const;
+  bool getProperty(const std::string &name,
+      int type,
+      void *mem,
+      uint64_t size,
+      uint32_t mask) override;
+};
+
+struct Renderer : Object
+{
+  using Object::Object;
+  RendererGPU gpu{};
+  int spp = 1;
+  int sampleLimit = 128;
+  bool checkerboard = false;
+  void commit() override;
+  bool isValid() const override;
+};
+
+struct Frame : Object
+{
+  using Object::Object;
+  Renderer *renderer = nullptr;
+  Camera *camera = nullptr;
+  World *world = nullptr;
+  uint32_t size[2] = {10, 10};
+  int colorType = VRTX_UFIXED8_RGBA_SRGB;
+  int depthType = VRTX_UNKNOWN, primType = VRTX_UNKNOWN,
+      objType = VRTX_UNKNOWN, instType = VRTX_UNKNOWN,
+      albedoType = VRTX_UNKNOWN, normalType = VRTX_UNKNOWN;
+  VRTXFrameCompletionCallback callback = nullptr;
+  const void *callbackPtr = nullptr;
+
+  FramebufferGPU fb{};
+  void *buffers[10] = {};
+  uint32_t *workCounter = nullptr;
+  uint32_t *errorFlag = nullptr;
+  unsigned long long *stats = nullptr; // see FrameParams::stats
+  bool countTraversal = false; // "vrtx.countTraversal": counting build
+  bool nextFrameReset = true;
+  uint64_t lastSeenStamp = 0;
+  cudaEvent_t evStart = nullptr, evEnd = nullptr, evKStart = nullptr,
+              evKEnd = nullptr;
+  bool rendered = false;
+  int launches = 0;
+  std::vector<uint8_t> hostColor, hostDepth, hostPrim, hostObj, hostInst,
+      hostAlbedo, hostNormal;
+
+  ~Frame() override;
+  void commit() override;
+  bool isValid() const override;
+  void freeBuffers();
+  void render();
+  void wait();
+  bool ready();
+  const void *map(const std::string &channel,
+      uint32_t *w,
+      uint32_t *h,
+      int *pixelType);
+  bool getProperty(const std::string &name,
+      int type,
+      void *mem,
+      uint64_t size,
+      uint32_t mask) override;
+};
+
+struct Device
+{
+  VRTXStatusCallback cb = nullptr;
+  const void *cbPtr = nullptr;
+  int cudaDevice = 0;
+  std::recursive_mutex mutex;
+  bool initTried = false;
+  bool initOk = false;
+  cudaStream_t stream = nullptr;
+  int numSMs = 0;
+  std::atomic<uint64_t> lastChange{0};
+  std::vector<Object *> live; // every object ever created and not destroyed
+
+  bool init();
+  void report(const Object *src, int severity, const char *msg);
+  void markChanged()
+  {
+    lastChange = newStamp();
+  }
+};
+
+} // namespace vrtx

@@ -1,0 +1,66 @@
+// Host-side declarations of the device kernels' launch wrappers.
+#pragma once
+
+#include "gpu_types.h"
+
+namespace vrtx {
+
+// integrator (render.cu)
+int renderOccupancyBlocks(int rendererType, bool stats);
+// stats: the counting build (node visits, primitive tests, BLAS entries)
+cudaError_t launchRender(
+    const FrameParams &P, int gridBlocks, bool stats, cudaStream_t s);
+cudaError_t launchClearFrame(const FramebufferGPU &fb, cudaStream_t s);
+
+// scene preparation (scene.cu)
+cudaError_t launchTriangleBoxes(const GeometryGPU *geoms,
+    const uint2 *refs, // (surface, prim) per BLAS primitive
+    const SurfaceGPU *surfaces,
+    uint32_t n,
+    box3 *boxes,
+    cudaStream_t s);
+cudaError_t launchSphereBoxes(const GeometryGPU *geoms,
+    const uint2 *refs,
+    const SurfaceGPU *surfaces,
+    uint32_t n,
+    box3 *boxes,
+    cudaStream_t s);
+cudaError_t launchGatherTriangles(const GeometryGPU *geoms,
+    const uint2 *refs,
+    const SurfaceGPU *surfaces,
+    const uint32_t *order,
+    uint32_t n,
+    TriRecord *out,
+    cudaStream_t s);
+cudaError_t launchGatherSpheres(const GeometryGPU *geoms,
+    const uint2 *refs,
+    const SurfaceGPU *surfaces,
+    const uint32_t *order,
+    uint32_t n,
+    SphereRecord *out,
+    cudaStream_t s);
+cudaError_t launchFillRefs(uint32_t surface, uint32_t count, uint2 *out,
+    cudaStream_t s);
+
+// Conservative macrocell majorants of a structured-regular field through a
+// TF table (scene.cu). Cells are 16^3 voxels from the origin; a cell's value
+// range covers every voxel the trilinear filter can touch for a sample inside
+// it (one voxel of apron on each side), and its majorant is the largest TF
+// alpha over all table entries that range can reach through linear filtering
+// (one entry of apron). ranges: scratch of 2 * numCells floats.
+cudaError_t launchMacrocellRanges(cudaTextureObject_t field,
+    const int dims[3],
+    const int mcDims[3],
+    float *ranges,
+    cudaStream_t s);
+cudaError_t launchMacrocellMajorants(const float *ranges,
+    const int mcDims[3],
+    const float4 *tf,
+    int tfSize,
+    float valueLo,
+    float valueHi,
+    float uniformOpacity,
+    float *majorants,
+    cudaStream_t s);
+
+} // namespace vrtx

@@ -1,0 +1,319 @@
+// Scene preparation kernels: primitive boxes, leaf-record gathers and the
+// conservative macrocell majorant grid.
+//
+// Replaces the reference's sphere AABB transform (scene/surface/geometry/
+// Sphere.cu:56-115) and its UniformGrid build (scene/volume/space_skipping/
+// UniformGrid.cu:44-150). The grid here is built differently on purpose:
+// the reference samples 8 texture taps per macrocell at world positions
+// treated as texture coordinates, which does not bound the voxels a sample
+// can see; skipping cells needs a bound that does, so every voxel of the
+// cell plus a one-voxel apron is read.
+#include "render.h"
+
+namespace vrtx {
+namespace {
+
+__device__ __forceinline__ void triIndices(
+    const GeometryGPU &g, uint32_t prim, uint32_t &i0, uint32_t &i1, uint32_t &i2)
+{
+  if (g.indices) {
+    i0 = g.indices[3 * prim];
+    i1 = g.indices[3 * prim + 1];
+    i2 = g.indices[3 * prim + 2];
+  } else {
+    i0 = 3 * prim;
+    i1 = i0 + 1;
+    i2 = i0 + 2;
+  }
+}
+
+__global__ void k_triBoxes(const GeometryGPU *geoms,
+    const uint2 *refs,
+    const SurfaceGPU *surfaces,
+    uint32_t n,
+    box3 *boxes)
+{
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n)
+    return;
+  const uint2 r = refs[i];
+  const GeometryGPU &g = geoms[surfaces[r.x].geometry];
+  uint32_t i0, i1, i2;
+  triIndices(g, r.y, i0, i1, i2);
+  box3 b = emptyBox();
+  extend(b, g.vertices[i0]);
+  extend(b, g.vertices[i1]);
+  extend(b, g.vertices[i2]);
+  boxes[i] = b;
+}
+
+__device__ __forceinline__ void sphereOf(
+    const GeometryGPU &g, uint32_t prim, f3 &c, float &r)
+{
+  const uint32_t idx = g.indices ? g.indices[prim] : prim;
+  c = g.vertices[idx];
+  r = g.radii ? g.radii[idx] : g.radius;
+}
+
+__global__ void k_sphereBoxes(const GeometryGPU *geoms,
+    const uint2 *refs,
+    const SurfaceGPU *surfaces,
+    uint32_t n,
+    box3 *boxes)
+{
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n)
+    return;
+  const uint2 r = refs[i];
+  const GeometryGPU &g = geoms[surfaces[r.x].geometry];
+  f3 c;
+  float rad;
+  sphereOf(g, r.y, c, rad);
+  const f3 e = mk3(rad, rad, rad);
+  boxes[i] = box3{c - e, c + e};
+}
+
+__global__ void k_gatherTris(const GeometryGPU *geoms,
+    const uint2 *refs,
+    const SurfaceGPU *surfaces,
+    const uint32_t *order,
+    uint32_t n,
+    TriRecord *out)
+{
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n)
+    return;
+  const uint2 r = refs[order[i]];
+  const GeometryGPU &g = geoms[surfaces[r.x].geometry];
+  uint32_t i0, i1, i2;
+  triIndices(g, r.y, i0, i1, i2);
+  const f3 a = g.vertices[i0], b = g.vertices[i1], c = g.vertices[i2];
+  TriRecord t;
+  t.v0 = make_float4(a.x, a.y, a.z, __uint_as_float(r.y));
+  t.v1 = make_float4(b.x, b.y, b.z, __uint_as_float(r.x));
+  t.v2 = make_float4(c.x, c.y, c.z, __uint_as_float(g.cullBackfaces ? 1u : 0u));
+  out[i] = t;
+}
+
+__global__ void k_gatherSpheres(const GeometryGPU *geoms,
+    const uint2 *refs,
+    const SurfaceGPU *surfaces,
+    const uint32_t *order,
+    uint32_t n,
+    SphereRecord *out)
+{
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n)
+    return;
+  const uint2 r = refs[order[i]];
+  const GeometryGPU &g = geoms[surfaces[r.x].geometry];
+  f3 c;
+  float rad;
+  sphereOf(g, r.y, c, rad);
+  SphereRecord s;
+  s.cr = make_float4(c.x, c.y, c.z, rad);
+  s.primID = r.y;
+  s.surface = r.x;
+  s.pad[0] = s.pad[1] = 0;
+  out[i] = s;
+}
+
+__global__ void k_fillRefs(uint32_t surface, uint32_t count, uint2 *out)
+{
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < count)
+    out[i] = make_uint2(surface, i);
+}
+
+// One block per macrocell: min/max over voxels [16c - 1, 16c + 17) per axis
+// (clamped), read with point sampling at unnormalised voxel centres.
+__global__ void __launch_bounds__(256) k_mcRanges(cudaTextureObject_t pointTex,
+    int dx,
+    int dy,
+    int dz,
+    int mx,
+    int my,
+    int mz,
+    float *ranges)
+{
+  const int cell = blockIdx.x;
+  const int cx = cell % mx, cy = (cell / mx) % my, cz = cell / (mx * my);
+  const int x0 = max(16 * cx - 1, 0), x1 = min(16 * cx + 17, dx - 1);
+  const int y0 = max(16 * cy - 1, 0), y1 = min(16 * cy + 17, dy - 1);
+  const int z0 = max(16 * cz - 1, 0), z1 = min(16 * cz + 17, dz - 1);
+  const int nx = x1 - x0 + 1, ny = y1 - y0 + 1, nz = z1 - z0 + 1;
+  const int total = nx * ny * nz;
+  float lo = 3.0e38f, hi = -3.0e38f;
+  for (int i = threadIdx.x; i < total; i += blockDim.x) {
+    const int x = x0 + i % nx, y = y0 + (i / nx) % ny, z = z0 + i / (nx * ny);
+    const float v = tex3D<float>(pointTex, x + 0.5f, y + 0.5f, z + 0.5f);
+    lo = fminf(lo, v);
+    hi = fmaxf(hi, v);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    lo = fminf(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+    hi = fmaxf(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+  }
+  __shared__ float slo[8], shi[8];
+  if ((threadIdx.x & 31) == 0) {
+    slo[threadIdx.x >> 5] = lo;
+    shi[threadIdx.x >> 5] = hi;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < (int)(blockDim.x >> 5); w++) {
+      lo = fminf(lo, slo[w]);
+      hi = fmaxf(hi, shi[w]);
+    }
+    ranges[2 * cell] = lo;
+    ranges[2 * cell + 1] = hi;
+  }
+}
+
+__device__ __forceinline__ float tfCoord(float s, float lo, float hi)
+{
+  const float cs = fmaxf(lo, fminf(s, hi));
+  return (cs - lo) * (1.f / (hi - lo));
+}
+
+__global__ void k_mcMajorants(const float *ranges,
+    int numCells,
+    const float4 *tf,
+    int tfSize,
+    float vlo,
+    float vhi,
+    float uniformOpacity,
+    float *majorants)
+{
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= numCells)
+    return;
+  const float lo = ranges[2 * c], hi = ranges[2 * c + 1];
+  if (!(lo <= hi)) { // empty or all-NaN cell
+    majorants[c] = 0.f;
+    return;
+  }
+  if (!tf) {
+    majorants[c] = uniformOpacity;
+    return;
+  }
+  int e0 = 0, e1 = tfSize - 1;
+  if (vhi != vlo) {
+    const float c0 = tfCoord(lo, vlo, vhi), c1 = tfCoord(hi, vlo, vhi);
+    const float a = fminf(c0, c1), b = fmaxf(c0, c1);
+    e0 = (int)floorf(a * tfSize - 0.5f) - 1;
+    e1 = (int)floorf(b * tfSize - 0.5f) + 2;
+    e0 = max(e0, 0);
+    e1 = min(e1, tfSize - 1);
+  }
+  float m = 0.f;
+  for (int e = e0; e <= e1; e++)
+    m = fmaxf(m, tf[e].w);
+  majorants[c] = m;
+}
+
+} // namespace
+
+cudaError_t launchTriangleBoxes(const GeometryGPU *geoms,
+    const uint2 *refs,
+    const SurfaceGPU *surfaces,
+    uint32_t n,
+    box3 *boxes,
+    cudaStream_t s)
+{
+  if (n)
+    k_triBoxes<<<(n + 255) / 256, 256, 0, s>>>(geoms, refs, surfaces, n, boxes);
+  return cudaGetLastError();
+}
+
+cudaError_t launchSphereBoxes(const GeometryGPU *geoms,
+    const uint2 *refs,
+    const SurfaceGPU *surfaces,
+    uint32_t n,
+    box3 *boxes,
+    cudaStream_t s)
+{
+  if (n)
+    k_sphereBoxes<<<(n + 255) / 256, 256, 0, s>>>(geoms, refs, surfaces, n, boxes);
+  return cudaGetLastError();
+}
+
+cudaError_t launchGatherTriangles(const GeometryGPU *geoms,
+    const uint2 *refs,
+    const SurfaceGPU *surfaces,
+    const uint32_t *order,
+    uint32_t n,
+    TriRecord *out,
+    cudaStream_t s)
+{
+  if (n)
+    k_gatherTris<<<(n + 255) / 256, 256, 0, s>>>(
+        geoms, refs, surfaces, order, n, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launchGatherSpheres(const GeometryGPU *geoms,
+    const uint2 *refs,
+    const SurfaceGPU *surfaces,
+    const uint32_t *order,
+    uint32_t n,
+    SphereRecord *out,
+    cudaStream_t s)
+{
+  if (n)
+    k_gatherSpheres<<<(n + 255) / 256, 256, 0, s>>>(
+        geoms, refs, surfaces, order, n, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launchFillRefs(
+    uint32_t surface, uint32_t count, uint2 *out, cudaStream_t s)
+{
+  if (count)
+    k_fillRefs<<<(count + 255) / 256, 256, 0, s>>>(surface, count, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launchMacrocellRanges(cudaTextureObject_t field,
+    const int dims[3],
+    const int mcDims[3],
+    float *ranges,
+    cudaStream_t s)
+{
+  const int cells = mcDims[0] * mcDims[1] * mcDims[2];
+  if (cells)
+    k_mcRanges<<<cells, 256, 0, s>>>(field,
+        dims[0],
+        dims[1],
+        dims[2],
+        mcDims[0],
+        mcDims[1],
+        mcDims[2],
+        ranges);
+  return cudaGetLastError();
+}
+
+cudaError_t launchMacrocellMajorants(const float *ranges,
+    const int mcDims[3],
+    const float4 *tf,
+    int tfSize,
+    float valueLo,
+    float valueHi,
+    float uniformOpacity,
+    float *majorants,
+    cudaStream_t s)
+{
+  const int cells = mcDims[0] * mcDims[1] * mcDims[2];
+  if (cells)
+    k_mcMajorants<<<(cells + 255) / 256, 256, 0, s>>>(ranges,
+        cells,
+        tf,
+        tfSize,
+        valueLo,
+        valueHi,
+        uniformOpacity,
+        majorants);
+  return cudaGetLastError();
+}
+
+} // namespace vrtx

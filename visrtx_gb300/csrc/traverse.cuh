@@ -1,0 +1,438 @@
+// Two-level BVH8 traversal (device code).
+//
+// Replaces optixTrace on the surface traversable (devices/rtx/gpu/
+// intersectRay.h:40-111) and the primitive programs it dispatches:
+//  * triangles: watertight ray/triangle test (Woop, Benthin, Wald, "Watertight
+//    Ray/Triangle Intersection", JCGT 2(1), 2013), standing in for OptiX's
+//    closed built-in test. Barycentrics follow OptiX: u weights v1, v if
+//    weights v2 (populateHit.h:144-148);
+//  * spheres: the reference's object-space test with the non-unit direction,
+//    reporting only the near root (scene/Intersectors_ptx.cu:74-99).
+//
+// One loop walks both levels: TLAS leaves are instance records; entering one
+// pushes a marker, transforms the ray to object space and continues in the
+// instance's BLAS; popping the marker restores the world ray. Node groups
+// are (base, hit bits) pairs: bits 24..31 hold internal-child hits ranked by
+// slot XOR ray octant (lowest = nearest), bits 0..7 the node's imask; a
+// primitive group holds leaf-primitive hits in bits 0..23.
+#pragma once
+
+#include "gpu_types.h"
+
+namespace vrtx {
+
+#ifndef VRTX_TRAVERSAL_STACK
+#define VRTX_TRAVERSAL_STACK 64
+#endif
+
+struct Hit
+{
+  float t;
+  float u, v;
+  uint32_t inst; // TLAS leaf (InstanceRecord) index
+  uint32_t rec; // primitive record index in the instance's BLAS
+  uint32_t front; // triangle front-face hit
+};
+
+struct TravRay
+{
+  f3 org, dir, invDir;
+  uint32_t oct;
+  int kx, ky, kz;
+  float Sx, Sy, Sz;
+};
+
+__device__ __forceinline__ float safeRcp(float d)
+{
+  return 1.f / (fabsf(d) > 1e-30f ? d : copysignf(1e-30f, d));
+}
+
+__device__ __forceinline__ void setupRay(TravRay &r, f3 o, f3 d)
+{
+  r.org = o;
+  r.dir = d;
+  r.invDir = mk3(safeRcp(d.x), safeRcp(d.y), safeRcp(d.z));
+  r.oct = (d.x < 0.f ? 1u : 0u) | (d.y < 0.f ? 2u : 0u) | (d.z < 0.f ? 4u : 0u);
+  const float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
+  int kz = 0;
+  if (ay > ax)
+    kz = 1;
+  if (az > fmaxf(ax, ay))
+    kz = 2;
+  int kx = kz + 1 == 3 ? 0 : kz + 1;
+  int ky = kx + 1 == 3 ? 0 : kx + 1;
+  const float dkz = get(d, kz);
+  if (dkz < 0.f) {
+    const int t = kx;
+    kx = ky;
+    ky = t;
+  }
+  r.kx = kx;
+  r.ky = ky;
+  r.kz = kz;
+  r.Sx = get(d, kx) / dkz;
+  r.Sy = get(d, ky) / dkz;
+  r.Sz = 1.f / dkz;
+}
+
+__device__ __forceinline__ uint32_t byteOf(uint2 w, int i)
+{
+  const uint32_t word = i < 4 ? w.x : w.y;
+  return (word >> ((i & 3) * 8)) & 0xffu;
+}
+
+// Tests the 8 child boxes of a node. Returns internal-child hits in bits
+// 24..31 (ranked) and leaf-primitive hits in bits 0..23.
+__device__ __forceinline__ uint32_t intersectNode(const BVH8Node *nodes,
+    uint32_t idx,
+    const TravRay &r,
+    float tmin,
+    float tmax,
+    uint32_t &childBase,
+    uint32_t &primBase,
+    uint32_t &imask)
+{
+  const float4 *p = reinterpret_cast<const float4 *>(nodes + idx);
+  const float4 n0 = __ldg(p + 0);
+  const float4 n1 = __ldg(p + 1);
+  const float4 n2 = __ldg(p + 2);
+  const float4 n3 = __ldg(p + 3);
+  const float4 n4 = __ldg(p + 4);
+  const uint32_t eb = __float_as_uint(n0.w);
+  const uint32_t ex = eb & 0xffu, ey = (eb >> 8) & 0xffu, ez = (eb >> 16) & 0xffu;
+  imask = eb >> 24;
+  childBase = __float_as_uint(n1.x);
+  primBase = __float_as_uint(n1.y);
+  const uint2 meta = make_uint2(__float_as_uint(n1.z), __float_as_uint(n1.w));
+  const uint2 qlx = make_uint2(__float_as_uint(n2.x), __float_as_uint(n2.y));
+  const uint2 qly = make_uint2(__float_as_uint(n2.z), __float_as_uint(n2.w));
+  const uint2 qlz = make_uint2(__float_as_uint(n3.x), __float_as_uint(n3.y));
+  const uint2 qhx = make_uint2(__float_as_uint(n3.z), __float_as_uint(n3.w));
+  const uint2 qhy = make_uint2(__float_as_uint(n4.x), __float_as_uint(n4.y));
+  const uint2 qhz = make_uint2(__float_as_uint(n4.z), __float_as_uint(n4.w));
+
+  const float sx = __uint_as_float(ex << 23) * r.invDir.x;
+  const float sy = __uint_as_float(ey << 23) * r.invDir.y;
+  const float sz = __uint_as_float(ez << 23) * r.invDir.z;
+  const float ox = (n0.x - r.org.x) * r.invDir.x;
+  const float oy = (n0.y - r.org.y) * r.invDir.y;
+  const float oz = (n0.z - r.org.z) * r.invDir.z;
+  // Outward slack on the far plane keeps the rounded slab test conservative
+  // (decoded planes carry a few roundings; 1e-6 relative covers them).
+  const float farScale = 1.000001f;
+
+  uint32_t hits = 0;
+#pragma unroll
+  for (int c = 0; c < 8; c++) {
+    const uint32_t m = byteOf(meta, c);
+    if (m == 0)
+      continue;
+    const float tx0 = fmaf((float)byteOf(qlx, c), sx, ox);
+    const float tx1 = fmaf((float)byteOf(qhx, c), sx, ox);
+    const float ty0 = fmaf((float)byteOf(qly, c), sy, oy);
+    const float ty1 = fmaf((float)byteOf(qhy, c), sy, oy);
+    const float tz0 = fmaf((float)byteOf(qlz, c), sz, oz);
+    const float tz1 = fmaf((float)byteOf(qhz, c), sz, oz);
+    const float tn = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)),
+        fmaxf(fminf(tz0, tz1), tmin));
+    const float tf = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)),
+                         fminf(fmaxf(tz0, tz1), tmax))
+        * farScale;
+    if (tn <= tf) {
+      if (imask & (1u << c))
+        hits |= 1u << (24 + (c ^ r.oct));
+      else
+        hits |= (m >> 5) << (m & 31);
+    }
+  }
+  return hits;
+}
+
+// Watertight triangle test. On a hit inside [tmin, tmax) writes t, u, v and
+// the front-face flag (det > 0 <=> dot(dir, cross(v1-v0, v2-v0)) < 0).
+__device__ __forceinline__ bool intersectTriangle(const TravRay &r,
+    f3 v0,
+    f3 v1,
+    f3 v2,
+    float tmin,
+    float tmax,
+    float &t,
+    float &u,
+    float &v,
+    bool &front)
+{
+  const f3 A = v0 - r.org;
+  const f3 B = v1 - r.org;
+  const f3 C = v2 - r.org;
+  const float Akz = get(A, r.kz), Bkz = get(B, r.kz), Ckz = get(C, r.kz);
+  const float Ax = get(A, r.kx) - r.Sx * Akz;
+  const float Ay = get(A, r.ky) - r.Sy * Akz;
+  const float Bx = get(B, r.kx) - r.Sx * Bkz;
+  const float By = get(B, r.ky) - r.Sy * Bkz;
+  const float Cx = get(C, r.kx) - r.Sx * Ckz;
+  const float Cy = get(C, r.ky) - r.Sy * Ckz;
+  // edge functions without contraction so shared edges agree exactly
+  float U = __fsub_rn(__fmul_rn(Cx, By), __fmul_rn(Cy, Bx));
+  float V = __fsub_rn(__fmul_rn(Ax, Cy), __fmul_rn(Ay, Cx));
+  float W = __fsub_rn(__fmul_rn(Bx, Ay), __fmul_rn(By, Ax));
+  if (U == 0.f || V == 0.f || W == 0.f) {
+    U = (float)((double)Cx * (double)By - (double)Cy * (double)Bx);
+    V = (float)((double)Ax * (double)Cy - (double)Ay * (double)Cx);
+    W = (float)((double)Bx * (double)Ay - (double)By * (double)Ax);
+  }
+  if ((U < 0.f || V < 0.f || W < 0.f) && (U > 0.f || V > 0.f || W > 0.f))
+    return false;
+  const float det = U + V + W;
+  if (det == 0.f)
+    return false;
+  const float Az = r.Sz * Akz;
+  const float Bz = r.Sz * Bkz;
+  const float Cz = r.Sz * Ckz;
+  const float T = U * Az + V * Bz + W * Cz;
+  const float rcp = 1.f / det;
+  const float tt = T * rcp;
+  if (!(tt >= tmin && tt < tmax))
+    return false;
+  t = tt;
+  u = V * rcp;
+  v = W * rcp;
+  front = det > 0.f;
+  return true;
+}
+
+// Reference sphere test (Intersectors_ptx.cu:74-99) in object space.
+__device__ __forceinline__ bool intersectSphere(
+    const TravRay &r, float4 cr, float tmin, float tmax, float &t)
+{
+  const f3 center = mk3(cr.x, cr.y, cr.z);
+  const float radius = cr.w;
+  const f3 d = r.dir;
+  const float rd2 = 1.f / dot(d, d);
+  const f3 CO = center - r.org;
+  const float projCO = dot(CO, d) * rd2;
+  const f3 perp = CO - projCO * d;
+  const float l2 = dot(perp, perp);
+  const float r2 = radius * radius;
+  if (l2 > r2)
+    return false;
+  const float td = sqrtf((r2 - l2) * rd2);
+  const float tt = projCO - td;
+  if (!(tt >= tmin && tt < tmax))
+    return false;
+  t = tt;
+  return true;
+}
+
+__device__ __forceinline__ void toObject(
+    TravRay &r, const InstanceRecord *inst, f3 worldOrg, f3 worldDir)
+{
+  const xfm34 m = inst->worldToObject;
+  setupRay(r, xfmPoint(m, worldOrg), xfmVector(m, worldDir));
+}
+
+// Material opacity as the any-hit programs see it (Matte init callable,
+// MatteShader_ptx.cu:38-49 + adjustedMaterialOpacity,
+// evalMaterialParameters.h:392-403).
+__device__ __forceinline__ float surfaceOpacity(
+    const WorldGPU &w, uint32_t surface)
+{
+  const MaterialGPU &m = w.materials[w.surfaces[surface].material];
+  if (m.alphaMode == ALPHA_OPAQUE)
+    return 1.f;
+  if (m.alphaMode == ALPHA_BLEND)
+    return m.opacity;
+  return m.opacity < m.cutoff ? 0.f : 1.f;
+}
+
+// MODE 0: closest hit. MODE 1: any-hit opacity accumulation
+// (accumulateValue(o, opacity, o); terminate at o >= 0.99), as the
+// __anyhit__shadow / __anyhit__ao programs do (DirectLight_ptx.cu:233-256,
+// AmbientOcclusion_ptx.cu:53-69).
+// Per-thread traversal counters (filled only by the counting kernels, which
+// pass a non-null pointer; the timed kernels pass nullptr and the counting
+// code folds away).
+struct TravStats
+{
+  uint32_t nodes; // BVH8 nodes visited (TLAS + BLAS)
+  uint32_t tris; // triangle tests
+  uint32_t spheres; // sphere tests
+  uint32_t instances; // BLAS entries
+  uint32_t rays; // traverse() calls
+};
+
+template <int MODE, bool STATS = false>
+__device__ __forceinline__ bool traverse(const WorldGPU &w,
+    f3 org,
+    f3 dir,
+    float tmin,
+    float tmax,
+    bool cullBackfaces,
+    bool geomCull,
+    Hit &hit,
+    float &opacity,
+    uint32_t *errorFlag,
+    TravStats &st)
+{
+  TravStats *stats = STATS ? &st : nullptr;
+  st.rays++;
+  TravRay r;
+  setupRay(r, org, dir);
+  const BVH8Node *nodes = w.tlasNodes;
+  bool inBlas = false;
+  uint32_t blasType = 0;
+  const void *prims = nullptr;
+  uint32_t instIdx = 0;
+  bool found = false;
+  opacity = 0.f;
+
+  uint2 stack[VRTX_TRAVERSAL_STACK];
+  int sp = 0;
+  uint2 cur = make_uint2(0u, 0x80000000u);
+  uint2 tri = make_uint2(0u, 0u);
+  if (w.numInstances == 0)
+    return false;
+
+  // A well-formed BVH ends the loop long before this bound; a corrupt one
+  // (cyclic child links) must not spin forever: give up and flag it.
+  for (uint32_t guard = 0;; guard++) {
+    if (guard > (1u << 22)) {
+      if (errorFlag)
+        atomicOr(errorFlag, 2u);
+      break;
+    }
+    if (tri.y) {
+      if (!inBlas) {
+        // enter the nearest-indexed instance of this leaf group
+        const uint32_t b = __ffs(tri.y) - 1;
+        tri.y &= tri.y - 1;
+        if (sp + 3 > VRTX_TRAVERSAL_STACK) {
+          if (errorFlag)
+            atomicOr(errorFlag, 1u);
+          tri.y = 0;
+          continue;
+        }
+        if (cur.y & 0xff000000u)
+          stack[sp++] = cur;
+        if (tri.y)
+          stack[sp++] = tri;
+        stack[sp++] = make_uint2(0u, 0u); // marker
+        instIdx = tri.x + b;
+        if (stats)
+          stats->instances++;
+        const InstanceRecord *inst = w.instances + instIdx;
+        const BLASDesc blas = w.blas[inst->blas];
+        toObject(r, inst, org, dir);
+        nodes = blas.nodes;
+        prims = blas.prims;
+        blasType = blas.type;
+        inBlas = true;
+        cur = make_uint2(0u, 0x80000000u);
+        tri.y = 0;
+        continue;
+      }
+      while (tri.y) {
+        const uint32_t b = __ffs(tri.y) - 1;
+        tri.y &= tri.y - 1;
+        const uint32_t rec = tri.x + b;
+        float t, u = 0.f, v = 0.f;
+        bool front = false;
+        uint32_t surface;
+        bool hitPrim;
+        if (blasType == GEOM_TRIANGLE) {
+          const float4 *tp =
+              reinterpret_cast<const float4 *>(prims) + (size_t)rec * 3;
+          const float4 a = __ldg(tp + 0);
+          const float4 bb = __ldg(tp + 1);
+          const float4 cc = __ldg(tp + 2);
+          if (stats)
+            stats->tris++;
+          hitPrim = intersectTriangle(r,
+              mk3(a.x, a.y, a.z),
+              mk3(bb.x, bb.y, bb.z),
+              mk3(cc.x, cc.y, cc.z),
+              tmin,
+              tmax,
+              t,
+              u,
+              v,
+              front);
+          if (hitPrim && !front
+              && (cullBackfaces || (geomCull && (__float_as_uint(cc.w) & 1u)))
+              && MODE == 0)
+            hitPrim = false;
+          surface = __float_as_uint(bb.w);
+        } else {
+          const SphereRecord *sp4 =
+              reinterpret_cast<const SphereRecord *>(prims) + rec;
+          const float4 cr = __ldg(&sp4->cr);
+          if (stats)
+            stats->spheres++;
+          hitPrim = intersectSphere(r, cr, tmin, tmax, t);
+          surface = __ldg(&sp4->surface);
+        }
+        if (!hitPrim)
+          continue;
+        if (MODE == 0) {
+          tmax = t;
+          hit.t = t;
+          hit.u = u;
+          hit.v = v;
+          hit.inst = instIdx;
+          hit.rec = rec;
+          hit.front = front ? 1u : 0u;
+          found = true;
+        } else {
+          const float o = w.allOpaque ? 1.f : surfaceOpacity(w, surface);
+          opacity += o * (1.f - opacity);
+          if (opacity >= 0.99f)
+            return true;
+        }
+      }
+      continue;
+    }
+
+    if (cur.y & 0xff000000u) {
+      const uint32_t bit = __ffs(cur.y >> 24) - 1;
+      cur.y &= ~(1u << (24 + bit));
+      const uint32_t slot = bit ^ r.oct;
+      const uint32_t idx =
+          cur.x + __popc(cur.y & 0xffu & ((1u << slot) - 1u));
+      if (cur.y & 0xff000000u) {
+        if (sp < VRTX_TRAVERSAL_STACK)
+          stack[sp++] = cur;
+        else if (errorFlag)
+          atomicOr(errorFlag, 1u);
+      }
+      uint32_t childBase, primBase, imask;
+      if (stats)
+        stats->nodes++;
+      const uint32_t hits = intersectNode(
+          nodes, idx, r, tmin, tmax, childBase, primBase, imask);
+      cur = make_uint2(childBase, (hits & 0xff000000u) | imask);
+      tri = make_uint2(primBase, hits & 0x00ffffffu);
+      continue;
+    }
+
+    // nothing pending: pop
+    if (sp == 0)
+      break;
+    const uint2 e = stack[--sp];
+    if (e.y == 0u) {
+      // marker: back to the world ray
+      setupRay(r, org, dir);
+      nodes = w.tlasNodes;
+      inBlas = false;
+      cur = make_uint2(0u, 0u);
+      continue;
+    }
+    if (e.y & 0xff000000u)
+      cur = e;
+    else {
+      cur = make_uint2(0u, 0u);
+      tri = e;
+    }
+  }
+  return MODE == 0 ? found : false;
+}
+
+} // namespace vrtx

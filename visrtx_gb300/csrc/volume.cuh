@@ -1,0 +1,365 @@
+// Scivis volume integration (device code): the fixed-step emission-absorption
+// marcher of the reference (devices/rtx/gpu/volumeIntegration.h:64-165,
+// 318-350) with two additions that leave its results unchanged:
+//  * samples whose macrocell majorant is 0 (no voxel the trilinear filter can
+//    reach in that cell maps to a non-zero TF alpha) are not fetched: their
+//    contribution is exactly zero (1 - pow(1 - 0, x) == 0), and the march
+//    position still advances by the same repeated float additions, so every
+//    later sample sits where the reference puts it;
+//  * the volume "TLAS" is a flat list scanned for the nearest entry, in
+//    place of the OptiX volume BVH (the lists here are short).
+#pragma once
+
+#include <curand_kernel.h>
+
+#include "gpu_types.h"
+
+namespace vrtx {
+
+typedef curandStatePhilox4_32_10_t RandState;
+
+struct VolumeHitG
+{
+  int entry; // index into WorldGPU::volumes
+  f3 localOrg, localDir;
+  float tlo, thi;
+};
+
+// Slab test in the volume's object space (Intersectors_ptx.cu:248-274),
+// clamped to the ray interval [tmin, tmax].
+__device__ __forceinline__ bool volumeSlab(const VolumeGPU &v,
+    f3 worldOrg,
+    f3 worldDir,
+    float tmin,
+    float tmax,
+    VolumeHitG &h)
+{
+  const f3 lo = xfmPoint(v.worldToObject, worldOrg);
+  const f3 ld = xfmVector(v.worldToObject, worldDir);
+  const f3 inv = mk3(1.f / ld.x, 1.f / ld.y, 1.f / ld.z);
+  const f3 mins = (v.bounds.lo - lo) * inv;
+  const f3 maxs = (v.bounds.hi - lo) * inv;
+  const f3 nears = fmin3(mins, maxs);
+  const f3 fars = fmax3(mins, maxs);
+  float t0 = compMax(nears);
+  float t1 = compMin(fars);
+  if (!(t0 < t1))
+    return false;
+  t0 = fmaxf(tmin, fminf(t0, tmax));
+  t1 = fmaxf(tmin, fminf(t1, tmax));
+  h.localOrg = lo;
+  h.localDir = ld;
+  h.tlo = t0;
+  h.thi = t1;
+  return true;
+}
+
+// Closest volume entry in [tmin, tmax], skipping `skip` (the reference's
+// lastVolID/lastInstID test).
+__device__ __forceinline__ bool intersectVolumes(const WorldGPU &w,
+    f3 org,
+    f3 dir,
+    float tmin,
+    float tmax,
+    int skip,
+    VolumeHitG &best)
+{
+  bool found = false;
+  for (uint32_t i = 0; i < w.numVolumes; i++) {
+    if ((int)i == skip)
+      continue;
+    VolumeHitG h;
+    if (volumeSlab(w.volumes[i], org, dir, tmin, tmax, h)) {
+      if (!found || h.tlo < best.tlo) {
+        best = h;
+        best.entry = (int)i;
+        found = true;
+      }
+    }
+  }
+  return found;
+}
+
+__device__ __forceinline__ float sampleField(const VolumeGPU &v, f3 p)
+{
+  const f3 c = ((p - v.origin) + 0.5f * v.spacing) * v.invSpacing;
+  return tex3D<float>(v.field, c.x, c.y, c.z);
+}
+
+__device__ __forceinline__ float4 classifySample(const VolumeGPU &v, float s)
+{
+  if (v.hasTF) {
+    // position(s, valueRange) (gpu_math.h): clamp, then scale
+    const float cs = fmaxf(v.valueLo, fminf(s, v.valueHi));
+    const float coord = (cs - v.valueLo) * (1.f / (v.valueHi - v.valueLo));
+    return tex1D<float4>(v.tf, coord);
+  }
+  return make_float4(
+      v.uniformColor.x, v.uniformColor.y, v.uniformColor.z, v.uniformOpacity);
+}
+
+__device__ __forceinline__ float cellMajorant(const VolumeGPU &v, f3 p)
+{
+  if (!v.majorants)
+    return 1.f;
+  // voxel-space position -> macrocell (16 voxels per cell edge)
+  const f3 q = (p - v.origin) * mk3(1.f / v.spacing.x, 1.f / v.spacing.y,
+                                    1.f / v.spacing.z);
+  const int cx = min(max((int)floorf(q.x * (1.f / 16.f)), 0), v.mcDims[0] - 1);
+  const int cy = min(max((int)floorf(q.y * (1.f / 16.f)), 0), v.mcDims[1] - 1);
+  const int cz = min(max((int)floorf(q.z * (1.f / 16.f)), 0), v.mcDims[2] - 1);
+  return __ldg(v.majorants
+      + ((size_t)cz * v.mcDims[1] + cy) * v.mcDims[0] + cx);
+}
+
+// rayMarchVolume + _rayMarchVolume (volumeIntegration.h:64-126): returns the
+// entry depth; accumulates into color (when non-null) and opacity.
+__device__ __forceinline__ float rayMarchVolume(const VolumeGPU &v,
+    const VolumeHitG &h,
+    RandState &rs,
+    f3 *color,
+    float &opacity,
+    float invSamplingRate)
+{
+  float lower = h.tlo;
+  const float upper = h.thi;
+  const float depth = lower;
+  lower += v.stepSize * curand_uniform(&rs); // first jitter (unscaled step)
+  const float stepSize = v.stepSize * invSamplingRate;
+  const float exponent = stepSize * v.oneOverUnitDistance;
+  lower += stepSize * curand_uniform(&rs); // second jitter
+  float transmittance = 1.f;
+  if (!(stepSize > 0.f))
+    return depth;
+  // bound the march (a ray through a 2^24-step box is not a real scene)
+  for (int guard = 0; guard < (1 << 24) && opacity < 0.99f && upper - lower >= 0.f;
+       guard++) {
+    const f3 p = h.localOrg + h.localDir * lower;
+    if (cellMajorant(v, p) > 0.f) {
+      const float s = sampleField(v, p);
+      if (!isnan(s)) {
+        const float4 co = classifySample(v, s);
+        const float stepT = powf(1.f - co.w, exponent);
+        const float a = transmittance * (1.f - stepT);
+        if (color)
+          *color += a * mk3(co.x, co.y, co.z);
+        opacity += a;
+        transmittance *= stepT;
+      }
+    }
+    lower += stepSize;
+  }
+  return depth;
+}
+
+// rayMarchAllVolumes (volumeIntegration.h:318-350).
+__device__ __forceinline__ float rayMarchAllVolumes(const WorldGPU &w,
+    RandState &rs,
+    f3 org,
+    f3 dir,
+    float tmin,
+    float tfar,
+    float invSamplingRate,
+    f3 &color,
+    float &opacity,
+    uint32_t &objID,
+    uint32_t &instID)
+{
+  float depth = tfar;
+  if (w.numVolumes == 0)
+    return depth;
+  bool firstHit = true;
+  int last = -1;
+  do {
+    VolumeHitG h;
+    if (!intersectVolumes(w, org, dir, tmin, tfar, last, h))
+      break;
+    const VolumeGPU &v = w.volumes[h.entry];
+    if (firstHit) {
+      objID = v.id;
+      instID = v.instId;
+      firstHit = false;
+    }
+    depth = fminf(depth, h.tlo);
+    h.thi = fminf(tfar, h.thi);
+    rayMarchVolume(v, h, rs, &color, opacity, invSamplingRate);
+    tmin = h.thi + 1e-3f;
+    last = h.entry;
+  } while (opacity < 0.99f);
+  return depth;
+}
+
+// volumeAttenuation for shadow rays (DirectLight_ptx.cu:45-52,245-255): the
+// any-hit march over every volume the shadow ray crosses, until >= 0.99.
+__device__ __forceinline__ float volumeAttenuation(const WorldGPU &w,
+    RandState &rs,
+    f3 org,
+    f3 dir,
+    float tmin,
+    float tmax,
+    float invSamplingRate)
+{
+  float a = 0.f;
+  for (uint32_t i = 0; i < w.numVolumes; i++) {
+    VolumeHitG h;
+    if (!volumeSlab(w.volumes[i], org, dir, tmin, tmax, h))
+      continue;
+    h.entry = (int)i;
+    rayMarchVolume(w.volumes[i], h, rs, nullptr, a, invSamplingRate);
+    if (a >= 0.99f)
+      break;
+  }
+  return a;
+}
+
+// dda3 (gpu/dda.h:44-122) over this library's macrocell grid: cells are 16
+// voxels from the field origin, so the Woodcock bound of a cell is the
+// conservative majorant built for it.
+template <typename F>
+__device__ __forceinline__ void dda3(
+    f3 org, f3 dir, float tlo, float thi, const int dims[3], box3 bounds, F func)
+{
+  const f3 rcp = mk3(dir.x != 0.f ? 1.f / dir.x : 0.f,
+      dir.y != 0.f ? 1.f / dir.y : 0.f,
+      dir.z != 0.f ? 1.f / dir.z : 0.f);
+  const f3 lo = (bounds.lo - org) * rcp;
+  const f3 hi = (bounds.hi - org) * rcp;
+  const f3 tnear = fmin3(lo, hi);
+  const f3 tfar = fmax3(lo, hi);
+  // projectOnGrid (gpu/uniformGrid.h:43-50)
+  const f3 V01 = (org - bounds.lo) * mk3(1.f / (bounds.hi.x - bounds.lo.x),
+                                         1.f / (bounds.hi.y - bounds.lo.y),
+                                         1.f / (bounds.hi.z - bounds.lo.z));
+  int cx = min(max((int)(V01.x * dims[0]), 0), dims[0] - 1);
+  int cy = min(max((int)(V01.y * dims[1]), 0), dims[1] - 1);
+  int cz = min(max((int)(V01.z * dims[2]), 0), dims[2] - 1);
+  const f3 dist = mk3((tfar.x - tnear.x) / dims[0],
+      (tfar.y - tnear.y) / dims[1],
+      (tfar.z - tnear.z) / dims[2]);
+  const int sx = dir.x > 0.f ? 1 : -1, sy = dir.y > 0.f ? 1 : -1,
+            sz = dir.z > 0.f ? 1 : -1;
+  const int stx = dir.x > 0.f ? dims[0] : -1, sty = dir.y > 0.f ? dims[1] : -1,
+            stz = dir.z > 0.f ? dims[2] : -1;
+  f3 tnext = mk3(dir.x > 0.f ? tnear.x + float(cx + 1) * dist.x
+                             : tnear.x + float(dims[0] - cx) * dist.x,
+      dir.y > 0.f ? tnear.y + float(cy + 1) * dist.y
+                  : tnear.y + float(dims[1] - cy) * dist.y,
+      dir.z > 0.f ? tnear.z + float(cz + 1) * dist.z
+                  : tnear.z + float(dims[2] - cz) * dist.z);
+  float t0 = fmaxf(tlo, 0.f);
+  for (int guard = 0; guard < 4 * (dims[0] + dims[1] + dims[2]) + 8; guard++) {
+    const float t1 = fminf(compMin(tnext), thi);
+    const size_t cell = ((size_t)cz * dims[1] + cy) * dims[0] + cx;
+    if (!func(cell, t0, t1))
+      return;
+    const float tc = compMin(tnext);
+    if (tnext.x == tc) {
+      tnext.x += dist.x;
+      cx += sx;
+      if (cx == stx)
+        break;
+    }
+    if (tnext.y == tc) {
+      tnext.y += dist.y;
+      cy += sy;
+      if (cy == sty)
+        break;
+    }
+    if (tnext.z == tc) {
+      tnext.z += dist.z;
+      cz += sz;
+      if (cz == stz)
+        break;
+    }
+    t0 = t1;
+  }
+}
+
+// _sampleDistance (volumeIntegration.h:167-238): Woodcock tracking inside
+// each DDA cell against the cell majorant, t -= log(1-u)/majorant*stepSize.
+__device__ __forceinline__ float sampleDistance(const VolumeGPU &v,
+    const VolumeHitG &h,
+    RandState &rs,
+    f3 &albedo,
+    float &extinction,
+    float &tr)
+{
+  const float stepSize = v.stepSize;
+  float t_out = h.thi;
+  tr = 1.f;
+  const f3 org = h.localOrg + h.localDir * h.tlo;
+  const float tlo = 0.f, thi = h.thi - h.tlo;
+  box3 gb;
+  gb.lo = v.origin;
+  gb.hi = v.origin
+      + mk3(16.f * v.mcDims[0] * v.spacing.x,
+          16.f * v.mcDims[1] * v.spacing.y,
+          16.f * v.mcDims[2] * v.spacing.z);
+  dda3(org, h.localDir, tlo, thi, v.mcDims, gb, [&](size_t cell, float t0, float t1) {
+    const float majorant = v.majorants ? __ldg(v.majorants + cell) : 1.f;
+    float t = t0;
+    while (true) {
+      if (majorant <= 0.f)
+        break;
+      t -= logf(1.f - curand_uniform(&rs)) / majorant * stepSize;
+      if (t >= t1)
+        break;
+      const f3 p = h.localOrg + h.localDir * (t + h.tlo);
+      const float s = sampleField(v, p);
+      if (!isnan(s)) {
+        const float4 co = classifySample(v, s);
+        albedo = mk3(co.x, co.y, co.z);
+        extinction = co.w;
+        const float u = curand_uniform(&rs);
+        if (extinction >= u * majorant) {
+          tr = 0.f;
+          t_out = t;
+          return false;
+        }
+      }
+    }
+    return true;
+  });
+  return t_out + h.tlo;
+}
+
+// sampleDistanceAllVolumes (volumeIntegration.h:352-389)
+__device__ __forceinline__ float sampleDistanceAllVolumes(const WorldGPU &w,
+    RandState &rs,
+    f3 org,
+    f3 dir,
+    float tmin,
+    float tfar,
+    f3 &albedo,
+    float &extinction,
+    float &transmittance,
+    uint32_t &objID,
+    uint32_t &instID)
+{
+  float depth = tfar;
+  transmittance = 1.f;
+  int last = -1;
+  for (uint32_t guard = 0; guard <= w.numVolumes; guard++) {
+    VolumeHitG h;
+    if (!intersectVolumes(w, org, dir, tmin, tfar, last, h))
+      break;
+    const VolumeGPU &v = w.volumes[h.entry];
+    h.thi = fminf(tfar, h.thi);
+    f3 alb = mk3(0.f, 0.f, 0.f);
+    float ext = 0.f, tr = 0.f;
+    const float d = sampleDistance(v, h, rs, alb, ext, tr);
+    if (d < depth) {
+      depth = d;
+      albedo = alb;
+      extinction = ext;
+      transmittance = tr;
+      objID = v.id;
+      instID = v.instId;
+    }
+    tmin = h.thi + 1e-3f;
+    last = h.entry;
+  }
+  return depth;
+}
+
+} // namespace vrtx
