@@ -149,9 +149,11 @@ class OracleScene:
             self.handle = None
 
     def render(self, frame_id=0, rows=None, volume_mode=0, tex_round=1, threads=0, accum=None,
-               depth=None, spec=None):
+               depth=None, spec=None, ids=None):
+        """ids: a previous result dict whose id buffers carry over (ids are
+        only rewritten where the depth improves)."""
         return _render_prepared(self.lib, self.handle, spec or self.spec, frame_id, rows,
-                                volume_mode, tex_round, threads, accum, depth)
+                                volume_mode, tex_round, threads, accum, depth, ids)
 
 
 def _scene_structs(spec):
@@ -231,7 +233,7 @@ def _scene_structs(spec):
 
 
 def _render_prepared(lib, handle, spec, frame_id, rows, volume_mode, tex_round, threads, accum,
-                     depth):
+                     depth, ids=None):
     c = spec.camera
     cam = OrcCamera()
     cam.type = 0 if c.type == "perspective" else 1
@@ -261,9 +263,9 @@ def _render_prepared(lib, handle, spec, frame_id, rows, volume_mode, tex_round, 
         "accum": np.zeros((H, W, 4), np.float32) if accum is None else accum,
         "color": np.zeros((H, W), np.uint32),
         "depth": np.full((H, W), np.finfo(np.float32).max, np.float32) if depth is None else depth,
-        "primitiveId": np.zeros((H, W), np.uint32),
-        "objectId": np.zeros((H, W), np.uint32),
-        "instanceId": np.zeros((H, W), np.uint32),
+        "primitiveId": np.zeros((H, W), np.uint32) if ids is None else ids["primitiveId"],
+        "objectId": np.zeros((H, W), np.uint32) if ids is None else ids["objectId"],
+        "instanceId": np.zeros((H, W), np.uint32) if ids is None else ids["instanceId"],
     }
     fr = OrcFrame()
     fr.width, fr.height, fr.frameID, fr.colorFormat = W, H, frame_id, 0

@@ -30,14 +30,19 @@ def render_gpu(dev, spec: scenes.SceneSpec, frames: int = 1):
 def render_oracle(spec: scenes.SceneSpec, frames: int = 1, **kw):
     from oracle import oracle as O
 
-    accum = None
-    depth = None
+    sc = O.OracleScene(spec)
+    prev = None
     out = None
-    for f in range(frames):
-        out = O.render(spec, frame_id=f * max(1, spec.renderer.pixel_samples)
-                       if spec.renderer.subtype != "raycast" else f,
-                       accum=accum, depth=depth, **kw)
-        accum, depth = out["accum"], out["depth"]
+    try:
+        for f in range(frames):
+            out = sc.render(frame_id=f * max(1, spec.renderer.pixel_samples)
+                            if spec.renderer.subtype != "raycast" else f,
+                            accum=None if prev is None else prev["accum"],
+                            depth=None if prev is None else prev["depth"],
+                            ids=None if prev is None else prev, **kw)
+            prev = out
+    finally:
+        sc.release()
     return out
 
 

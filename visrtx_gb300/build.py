@@ -48,12 +48,27 @@ def _stale(out: str, deps: list[str]) -> bool:
     return any(os.path.getmtime(d) > t for d in deps)
 
 
-def build(verbose: bool = False, ptxas_info: bool = False) -> str:
-    """Builds visrtx_gb300/lib/libvrtx.so if any source changed; returns its path."""
+def build(verbose: bool = False, ptxas_info: bool = False, defines: tuple = (),
+          lib_path: str | None = None, obj_dir: str | None = None) -> str:
+    """Builds visrtx_gb300/lib/libvrtx.so if any source changed; returns its
+    path. `defines` (e.g. ("VRTX_RENDER_MIN_BLOCKS=4",)) and a separate
+    lib_path/obj_dir build a tuning variant beside the default library."""
+    global OBJ, LIB
+    saved = (OBJ, LIB)
+    if lib_path:
+        LIB = lib_path
+        OBJ = obj_dir or os.path.join(os.path.dirname(lib_path), "_obj")
+    try:
+        return _build(verbose, ptxas_info, [f"-D{d}" for d in defines])
+    finally:
+        OBJ, LIB = saved
+
+
+def _build(verbose: bool, ptxas_info: bool, dflags: list) -> str:
     nvcc = _nvcc()
     cuda = _cuda_home(nvcc)
     os.makedirs(OBJ, exist_ok=True)
-    os.makedirs(LIBDIR, exist_ok=True)
+    os.makedirs(os.path.dirname(LIB), exist_ok=True)
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
     headers.append(os.path.join(ROOT, "include", "vrtx.h"))
     jobs = []
@@ -64,7 +79,7 @@ def build(verbose: bool = False, ptxas_info: bool = False) -> str:
         objs.append(o)
         if _stale(o, [s] + headers):
             cmd = [nvcc, *ARCH, "-lineinfo", "-O3", "-std=c++17", "--expt-relaxed-constexpr",
-                   "--extended-lambda", "-Xcompiler", "-fPIC", "-c", s, "-o", o]
+                   "--extended-lambda", "-Xcompiler", "-fPIC", *dflags, "-c", s, "-o", o]
             if ptxas_info:
                 cmd.insert(1, "-Xptxas=-v")
             jobs.append(cmd)

@@ -1624,6 +1624,8 @@ Frame::~Frame()
       cudaFree(errorFlag);
     if (stats)
       cudaFree(stats);
+    if (scratch)
+      cudaFree(scratch);
   }
 }
 
@@ -1710,6 +1712,7 @@ void Frame::commit()
     cudaMemset(stats, 0, 8 * sizeof(unsigned long long));
   }
   countTraversal = get<int32_t>("vrtx.countTraversal", VRTX_BOOL, 0) != 0;
+  forceMegakernel = get<int32_t>("vrtx.megakernel", VRTX_BOOL, 0) != 0;
   for (cudaEvent_t *e : {&evStart, &evEnd, &evKStart, &evKEnd})
     if (!*e)
       cudaEventCreate(e);
@@ -1798,12 +1801,34 @@ void Frame::render()
   P.stats = stats;
   cudaMemsetAsync(workCounter, 0, 4, s);
   cudaMemsetAsync(stats, 0, 8 * sizeof(unsigned long long), s);
-  const int blocks =
-      d->numSMs * renderOccupancyBlocks(P.renderer.type, countTraversal);
+  // The "ao" renderer over opaque surfaces (no volumes) runs as a
+  // wavefront (primary / any-hit / resolve kernels per sample); everything
+  // else runs the per-pixel integrator kernel.
+  const bool wavefront = P.renderer.type == RENDERER_AO && P.world.allOpaque
+      && P.world.numVolumes == 0 && !forceMegakernel;
+  cudaError_t err = cudaSuccess;
   cudaEventRecord(evKStart, s);
-  cudaError_t err = launchRender(P, blocks, countTraversal, s);
+  if (wavefront) {
+    const size_t need = aoWavefrontBytes(fb.w, fb.h, P.renderer.aoSamples);
+    if (need > scratchBytes) {
+      if (scratch)
+        cudaFreeAsync(scratch, s);
+      scratch = nullptr;
+      scratchBytes = 0;
+      err = cudaMallocAsync(&scratch, need, s);
+      if (err == cudaSuccess)
+        scratchBytes = need;
+    }
+    if (err == cudaSuccess)
+      err = launchAOWavefront(P, d->numSMs, countTraversal, scratch, s);
+    launches += 3 * std::max(P.renderer.numIterations, 1);
+  } else {
+    const int blocks =
+        d->numSMs * renderOccupancyBlocks(P.renderer.type, countTraversal);
+    err = launchRender(P, blocks, countTraversal, s);
+    launches++;
+  }
   cudaEventRecord(evKEnd, s);
-  launches++;
   if (err != cudaSuccess)
     report(VRTX_SEVERITY_ERROR, "render launch failed: %s", cudaGetErrorString(err));
   if (callback) {

@@ -337,6 +337,9 @@ struct Frame : Object
   uint32_t *errorFlag = nullptr;
   unsigned long long *stats = nullptr; // see FrameParams::stats
   bool countTraversal = false; // "vrtx.countTraversal": counting build
+  bool forceMegakernel = false; // "vrtx.megakernel": per-pixel kernel only
+  void *scratch = nullptr; // wavefront queues (stream-ordered allocation)
+  size_t scratchBytes = 0;
   bool nextFrameReset = true;
   uint64_t lastSeenStamp = 0;
   cudaEvent_t evStart = nullptr, evEnd = nullptr, evKStart = nullptr,

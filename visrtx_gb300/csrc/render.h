@@ -12,6 +12,16 @@ cudaError_t launchRender(
     const FrameParams &P, int gridBlocks, bool stats, cudaStream_t s);
 cudaError_t launchClearFrame(const FramebufferGPU &fb, cudaStream_t s);
 
+// Wavefront "ao" renderer (opaque materials, no volumes): per sample a
+// primary kernel, an any-hit kernel over the compacted AO ray queue and a
+// resolve kernel. scratch: aoWavefrontBytes() bytes of device memory.
+size_t aoWavefrontBytes(uint32_t w, uint32_t h, int aoSamples);
+cudaError_t launchAOWavefront(const FrameParams &P,
+    int numSMs,
+    bool stats,
+    void *scratch,
+    cudaStream_t s);
+
 // scene preparation (scene.cu)
 cudaError_t launchTriangleBoxes(const GeometryGPU *geoms,
     const uint2 *refs, // (surface, prim) per BLAS primitive
