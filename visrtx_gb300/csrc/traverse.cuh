@@ -52,7 +52,10 @@ __device__ __forceinline__ void setupRay(TravRay &r, f3 o, f3 d)
   r.org = o;
   r.dir = d;
   r.invDir = mk3(safeRcp(d.x), safeRcp(d.y), safeRcp(d.z));
-  r.oct = (d.x < 0.f ? 1u : 0u) | (d.y < 0.f ? 2u : 0u) | (d.z < 0.f ? 4u : 0u);
+  // sign bits (not d < 0) so that -0.0, whose reciprocal is negative, swaps
+  // its planes like any other negative component
+  r.oct = (signbit(d.x) ? 1u : 0u) | (signbit(d.y) ? 2u : 0u)
+      | (signbit(d.z) ? 4u : 0u);
   const float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
   int kz = 0;
   if (ay > ax)
@@ -81,8 +84,21 @@ __device__ __forceinline__ uint32_t byteOf(uint2 w, int i)
   return (word >> ((i & 3) * 8)) & 0xffu;
 }
 
+// 2^23 + b as a float, b = byte `i` of `w` (one byte permute)
+__device__ __forceinline__ float biasedByte(uint32_t w, uint32_t i)
+{
+  return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7650u | i));
+}
+
 // Tests the 8 child boxes of a node. Returns internal-child hits in bits
 // 24..31 (ranked) and leaf-primitive hits in bits 0..23.
+//
+// Per ray octant the near/far plane words are swapped once per node, so a
+// child's entry distance is max(near planes) and its exit min(far planes);
+// bytes become floats with one permute and one subtract, and the hit masks
+// are built without branches: a leaf child contributes (meta >> 5) << offset
+// and an internal child (meta = 0b001'(24 + slot)) its rank bit 24 +
+// (slot ^ octant).
 __device__ __forceinline__ uint32_t intersectNode(const BVH8Node *nodes,
     uint32_t idx,
     const TravRay &r,
@@ -99,21 +115,37 @@ __device__ __forceinline__ uint32_t intersectNode(const BVH8Node *nodes,
   const float4 n3 = __ldg(p + 3);
   const float4 n4 = __ldg(p + 4);
   const uint32_t eb = __float_as_uint(n0.w);
-  const uint32_t ex = eb & 0xffu, ey = (eb >> 8) & 0xffu, ez = (eb >> 16) & 0xffu;
   imask = eb >> 24;
   childBase = __float_as_uint(n1.x);
   primBase = __float_as_uint(n1.y);
-  const uint2 meta = make_uint2(__float_as_uint(n1.z), __float_as_uint(n1.w));
-  const uint2 qlx = make_uint2(__float_as_uint(n2.x), __float_as_uint(n2.y));
-  const uint2 qly = make_uint2(__float_as_uint(n2.z), __float_as_uint(n2.w));
-  const uint2 qlz = make_uint2(__float_as_uint(n3.x), __float_as_uint(n3.y));
-  const uint2 qhx = make_uint2(__float_as_uint(n3.z), __float_as_uint(n3.w));
-  const uint2 qhy = make_uint2(__float_as_uint(n4.x), __float_as_uint(n4.y));
-  const uint2 qhz = make_uint2(__float_as_uint(n4.z), __float_as_uint(n4.w));
-
-  const float sx = __uint_as_float(ex << 23) * r.invDir.x;
-  const float sy = __uint_as_float(ey << 23) * r.invDir.y;
-  const float sz = __uint_as_float(ez << 23) * r.invDir.z;
+  const uint32_t meta[2] = {__float_as_uint(n1.z), __float_as_uint(n1.w)};
+  // per axis: (lo word pair, hi word pair), swapped for a negative direction
+  uint32_t nx[2], fx[2], ny[2], fy[2], nz[2], fz[2];
+  {
+    const uint32_t lx0 = __float_as_uint(n2.x), lx1 = __float_as_uint(n2.y);
+    const uint32_t ly0 = __float_as_uint(n2.z), ly1 = __float_as_uint(n2.w);
+    const uint32_t lz0 = __float_as_uint(n3.x), lz1 = __float_as_uint(n3.y);
+    const uint32_t hx0 = __float_as_uint(n3.z), hx1 = __float_as_uint(n3.w);
+    const uint32_t hy0 = __float_as_uint(n4.x), hy1 = __float_as_uint(n4.y);
+    const uint32_t hz0 = __float_as_uint(n4.z), hz1 = __float_as_uint(n4.w);
+    const bool sx = r.oct & 1u, sy = r.oct & 2u, sz = r.oct & 4u;
+    nx[0] = sx ? hx0 : lx0;
+    nx[1] = sx ? hx1 : lx1;
+    fx[0] = sx ? lx0 : hx0;
+    fx[1] = sx ? lx1 : hx1;
+    ny[0] = sy ? hy0 : ly0;
+    ny[1] = sy ? hy1 : ly1;
+    fy[0] = sy ? ly0 : hy0;
+    fy[1] = sy ? ly1 : hy1;
+    nz[0] = sz ? hz0 : lz0;
+    nz[1] = sz ? hz1 : lz1;
+    fz[0] = sz ? lz0 : hz0;
+    fz[1] = sz ? lz1 : hz1;
+  }
+  const float bias = 8388608.f;
+  const float sx = __uint_as_float((eb & 0xffu) << 23) * r.invDir.x;
+  const float sy = __uint_as_float(((eb >> 8) & 0xffu) << 23) * r.invDir.y;
+  const float sz = __uint_as_float(((eb >> 16) & 0xffu) << 23) * r.invDir.z;
   const float ox = (n0.x - r.org.x) * r.invDir.x;
   const float oy = (n0.y - r.org.y) * r.invDir.y;
   const float oz = (n0.z - r.org.z) * r.invDir.z;
@@ -124,26 +156,20 @@ __device__ __forceinline__ uint32_t intersectNode(const BVH8Node *nodes,
   uint32_t hits = 0;
 #pragma unroll
   for (int c = 0; c < 8; c++) {
-    const uint32_t m = byteOf(meta, c);
-    if (m == 0)
-      continue;
-    const float tx0 = fmaf((float)byteOf(qlx, c), sx, ox);
-    const float tx1 = fmaf((float)byteOf(qhx, c), sx, ox);
-    const float ty0 = fmaf((float)byteOf(qly, c), sy, oy);
-    const float ty1 = fmaf((float)byteOf(qhy, c), sy, oy);
-    const float tz0 = fmaf((float)byteOf(qlz, c), sz, oz);
-    const float tz1 = fmaf((float)byteOf(qhz, c), sz, oz);
-    const float tn = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)),
-        fmaxf(fminf(tz0, tz1), tmin));
-    const float tf = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)),
-                         fminf(fmaxf(tz0, tz1), tmax))
-        * farScale;
-    if (tn <= tf) {
-      if (imask & (1u << c))
-        hits |= 1u << (24 + (c ^ r.oct));
-      else
-        hits |= (m >> 5) << (m & 31);
-    }
+    const int w = c >> 2;
+    const uint32_t b = (uint32_t)(c & 3);
+    const float tx0 = fmaf(biasedByte(nx[w], b) - bias, sx, ox);
+    const float tx1 = fmaf(biasedByte(fx[w], b) - bias, sx, ox);
+    const float ty0 = fmaf(biasedByte(ny[w], b) - bias, sy, oy);
+    const float ty1 = fmaf(biasedByte(fy[w], b) - bias, sy, oy);
+    const float tz0 = fmaf(biasedByte(nz[w], b) - bias, sz, oz);
+    const float tz1 = fmaf(biasedByte(fz[w], b) - bias, sz, oz);
+    const float tn = fmaxf(fmaxf(tx0, ty0), fmaxf(tz0, tmin));
+    const float tf = fminf(fminf(tx1, ty1), fminf(tz1, tmax)) * farScale;
+    const uint32_t m = (meta[w] >> (8 * b)) & 0xffu;
+    const uint32_t lo5 = m & 31u;
+    const uint32_t sh = lo5 ^ ((lo5 >= 24u) ? r.oct : 0u);
+    hits |= (tn <= tf ? (m >> 5) : 0u) << sh;
   }
   return hits;
 }
