@@ -1185,6 +1185,9 @@ void World::commit()
   zeroVolumes = objectArrayParam(this, "volume");
   zeroLights = objectArrayParam(this, "light");
   id = get<uint32_t>("id", VRTX_UINT32, ~0u);
+  // libvrtx tuning parameters: primitives per BVH8 leaf slot (1..3)
+  maxLeaf[GEOM_TRIANGLE] = get<int32_t>("vrtx.maxLeafTriangles", VRTX_INT32, 1);
+  maxLeaf[GEOM_SPHERE] = get<int32_t>("vrtx.maxLeafSpheres", VRTX_INT32, 1);
   if (!zeroGroup) {
     zeroGroup = new Group(Object::dev, VRTX_GROUP);
     zeroInstance = new Instance(Object::dev, VRTX_INSTANCE, "transform");
@@ -1358,7 +1361,7 @@ bool World::rebuild()
       BLASBuild b;
       b.type = (uint32_t)cls;
       b.numPrims = n;
-      cudaError_t err = buildBVH8(boxes, n, s, b.bvh);
+      cudaError_t err = buildBVH8(boxes, n, s, b.bvh, maxLeaf[cls]);
       if (err == cudaSuccess) {
         const size_t recBytes =
             cls == GEOM_TRIANGLE ? sizeof(TriRecord) : sizeof(SphereRecord);

@@ -282,6 +282,7 @@ struct World : Object
   Array *zeroSurfaces = nullptr, *zeroVolumes = nullptr, *zeroLights = nullptr;
   uint32_t id = ~0u;
   Group *zeroGroup = nullptr;
+  int maxLeaf[GEOM_NUM_TYPES] = {1, 1}; // single-primitive leaves: tight leaf boxes
   Instance *zeroInstance = nullptr;
 
   // built state
