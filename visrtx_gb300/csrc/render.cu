@@ -23,6 +23,10 @@
 #ifndef VRTX_RENDER_MIN_BLOCKS
 #define VRTX_RENDER_MIN_BLOCKS 1
 #endif
+// The same for the any-hit queue kernel (8: <= 64 registers per thread).
+#ifndef VRTX_TRACE_MIN_BLOCKS
+#define VRTX_TRACE_MIN_BLOCKS 8
+#endif
 
 namespace vrtx {
 
@@ -919,7 +923,7 @@ __global__ void __launch_bounds__(128) k_aoPrimary(const FrameParams P,
 }
 
 template <bool STATS>
-__global__ void __launch_bounds__(128) k_aoTrace(const FrameParams P,
+__global__ void __launch_bounds__(128, VRTX_TRACE_MIN_BLOCKS) k_aoTrace(const FrameParams P,
     const AORay *rays,
     const uint32_t *rayCount,
     float *weighted)
