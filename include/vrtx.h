@@ -332,6 +332,8 @@ typedef struct VRTXDMVolume {
   float *gradDensity;    /* fp32, same dims; backward only, may be NULL */
   float *gradTf;         /* fp32, tfSize x 4; backward only, may be NULL */
   float *gradOpacityScale; /* one fp32; backward only, may be NULL */
+  const float *opacityScaleDevice; /* when not NULL, read instead of
+                                      opacityScale (device scalar) */
 } VRTXDMVolume;
 
 typedef struct VRTXDMView {
@@ -372,6 +374,28 @@ VRTX_API int vrtxDMBackward(VRTXDevice d,
     int tileW,
     int tileH,
     void *stream);
+
+/* Plans: the volume/view descriptors uploaded once (stream-ordered on
+ * `stream`) so that vrtxDMPlanForward / vrtxDMPlanBackward issue only a
+ * counter reset and one kernel each, and can be captured into a CUDA graph.
+ * Buffers named in the descriptors must outlive the plan. Returns NULL
+ * after reporting invalid arguments. */
+typedef struct VRTXDMPlan_st *VRTXDMPlan;
+VRTX_API VRTXDMPlan vrtxDMPlanCreate(VRTXDevice d,
+    const VRTXDMVolume *volumes,
+    int numVolumes,
+    const VRTXDMView *views,
+    int numViews,
+    int tileW,
+    int tileH,
+    void *stream);
+VRTX_API int vrtxDMPlanForward(
+    VRTXDMPlan plan, float *image, float *state, void *stream);
+VRTX_API int vrtxDMPlanBackward(VRTXDMPlan plan,
+    const float *state,
+    const float *gradImage,
+    void *stream);
+VRTX_API void vrtxDMPlanRelease(VRTXDMPlan plan);
 
 #ifdef __cplusplus
 } /* extern "C" */

@@ -1,0 +1,186 @@
+"""GPU checks of the differentiable marcher against the FP64 CPU oracle:
+forward image RMS <= 1e-3, adjoint gradients within 1e-2 relative error,
+autograd plumbing, CUDA-graph capture of a plan, and one batched launch over
+uneven volumes/views against per-view launches."""
+import math
+
+import numpy as np
+import pytest
+import torch
+
+from visrtx_gb300 import dm, scenes as S
+
+pytestmark = pytest.mark.gpu
+
+
+def make_volume(n=(24, 20, 28), seed=0, dtype=torch.float32, blobs=5):
+    nx, ny, nz = n
+    d = S.gaussian_blobs((nx, ny, nz), n_blobs=blobs, seed=seed, sigma_scale=0.12)
+    color, op = S.tf_knots(seed, max_opacity=0.6)
+    tf = S.tf_table(color, op, 256)
+    dt = torch.tensor(d, device="cuda").to(dtype).contiguous()
+    tft = torch.tensor(tf, device="cuda").contiguous()
+    scale = torch.tensor([1.5], device="cuda", dtype=torch.float32)
+    # value range wider than the data: no sample sits on a TF-clamp kink
+    return dm.VolumeInput(dt, tft, scale, step=0.5, unit=1.0, value_range=(-0.5, 1.5))
+
+
+def views_for(v: dm.VolumeInput, k=2, res=(40, 32), vol=0, seed=0):
+    dirs = S.fibonacci_sphere(k)
+    return [dm.look_at_view(vol, v.dims, 2.0 * dirs[i], 50.0, res[0], res[1],
+                            background=(0.1, 0.2, 0.3)) for i in range(k)]
+
+
+def oracle_view(w: dm.View):
+    return {"width": w.width, "height": w.height, "eye": w.eye, "d00": w.d00, "du": w.du,
+            "dv": w.dv, "background": w.background}
+
+
+def ref_forward(v, views, grad=None):
+    from oracle import oracle as O
+
+    dens = v.density.float().cpu().numpy().astype(np.float64)
+    tf = v.tf.cpu().numpy().astype(np.float64)
+    imgs, gD, gT, gS = [], np.zeros_like(dens), np.zeros_like(tf), 0.0
+    off = 0
+    for w in views:
+        npx = w.width * w.height
+        if grad is None:
+            imgs.append(O.dm(dens, tf, oracle_view(w), float(v.scale.item()), v.step, v.unit,
+                             v.value_range).reshape(-1, 3))
+        else:
+            g = grad[off:off + npx].reshape(w.height, w.width, 3)
+            img, d1, t1, s1 = O.dm(dens, tf, oracle_view(w), float(v.scale.item()), v.step, v.unit,
+                                   v.value_range, grad_image=g)
+            imgs.append(img.reshape(-1, 3))
+            gD += d1
+            gT += t1
+            gS += s1
+        off += npx
+    return np.concatenate(imgs), gD, gT, gS
+
+
+def rel(a, b):
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30))
+
+
+@pytest.mark.parametrize("dtype", [torch.float32, torch.float16, torch.bfloat16])
+def test_forward_rms_vs_fp64(dtype):
+    v = make_volume(dtype=dtype)
+    views = views_for(v)
+    b = dm.Batch([v], views)
+    img, state = dm.forward(b)
+    ref, *_ = ref_forward(v, views)
+    rms = float(np.sqrt(np.mean((img.cpu().numpy() - ref) ** 2)))
+    print(dtype, "rms", rms)
+    assert rms <= 1e-3
+    assert 0.05 < float(img.mean()) < 1.0  # the views see the volume
+
+
+@pytest.mark.parametrize("dtype", [torch.float32, torch.float16])
+def test_adjoint_vs_fp64(dtype):
+    v = make_volume(dtype=dtype, seed=1)
+    views = views_for(v, k=2, seed=1)
+    b = dm.Batch([v], views)
+    img, state = dm.forward(b)
+    rng = np.random.default_rng(0)
+    g = rng.standard_normal((b.pixels, 3)).astype(np.float32)
+    grads = dm.backward(b, state, torch.tensor(g, device="cuda"))
+    _, gD, gT, gS = ref_forward(v, views, grad=g.astype(np.float64))
+    gd = grads[0][0].cpu().numpy()
+    gt = grads[0][1].cpu().numpy()
+    gs = float(grads[0][2].item())
+    print("density", rel(gd, gD), "tf", rel(gt, gT), "scale", abs(gs - gS) / abs(gS))
+    assert rel(gd, gD) <= 1e-2
+    assert rel(gt, gT) <= 1e-2
+    assert abs(gs - gS) <= 1e-2 * abs(gS)
+
+
+def test_autograd_function_matches_manual():
+    v = make_volume(seed=2)
+    v.density.requires_grad_(True)
+    v.tf.requires_grad_(True)
+    v.scale.requires_grad_(True)
+    views = views_for(v, seed=2)
+    b = dm.Batch([v], views)
+    img = dm.render(b)
+    target = torch.zeros_like(img)
+    loss = ((img - target) ** 2).sum()
+    loss.backward()
+    img2, state = dm.forward(b)
+    grads = dm.backward(b, state, 2.0 * (img2 - target))
+    torch.testing.assert_close(v.density.grad, grads[0][0], rtol=1e-4, atol=1e-6)
+    torch.testing.assert_close(v.tf.grad, grads[0][1], rtol=1e-4, atol=1e-6)
+
+
+def test_plan_cuda_graph_capture():
+    v = make_volume(seed=3, dtype=torch.float16)
+    views = views_for(v, k=3, seed=3)
+    b = dm.Batch([v], views)
+    p = dm.Plan(b)
+    g = torch.ones((b.pixels, 3), device="cuda")
+    p.forward()
+    ref_img = p.image.clone()
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(s):
+        p.forward()
+        p.backward(g)
+    torch.cuda.current_stream().wait_stream(s)
+    graph = torch.cuda.CUDAGraph()
+    for gd, gt, gs in p.grads:
+        gd.zero_(), gt.zero_(), gs.zero_()
+    with torch.cuda.graph(graph):
+        p.forward()
+        p.backward(g)
+    for gd, gt, gs in p.grads:
+        gd.zero_(), gt.zero_(), gs.zero_()
+    graph.replay()
+    torch.cuda.synchronize()
+    assert torch.equal(p.image, ref_img)
+    g1 = p.grads[0][0].clone()
+    for gd, gt, gs in p.grads:
+        gd.zero_(), gt.zero_(), gs.zero_()
+    graph.replay()
+    torch.cuda.synchronize()
+    torch.testing.assert_close(p.grads[0][0], g1, rtol=1e-4, atol=1e-6)
+    p.release()
+
+
+def test_batched_uneven_matches_per_view():
+    """One launch over 3 volumes of different shapes (bf16) and 7 views of
+    different resolutions equals one launch per view (images bitwise;
+    gradients up to atomic-order rounding)."""
+    vols = [make_volume(n, seed=i, dtype=torch.bfloat16)
+            for i, n in enumerate([(20, 24, 16), (33, 17, 25), (12, 30, 22)])]
+    views = []
+    res = [(32, 24), (16, 40), (48, 32), (24, 24), (40, 16), (32, 32), (8, 64)]
+    for i, r in enumerate(res):
+        vi = i % 3
+        views += views_for(vols[vi], k=1, res=r, vol=vi, seed=i)
+    batch = dm.Batch(vols, views, tile=(16, 8))
+    img, state = dm.forward(batch)
+    g = torch.randn((batch.pixels, 3), device="cuda", generator=torch.Generator("cuda").manual_seed(0))
+    grads = dm.backward(batch, state, g)
+    sum_grads = [[torch.zeros_like(t) for t in gv] for gv in grads]
+    for i, w in enumerate(views):
+        b1 = dm.Batch([vols[w.volume]], [dm.View(0, w.width, w.height, w.eye, w.d00, w.du, w.dv,
+                                                 w.background)])
+        i1, s1 = dm.forward(b1)
+        off = batch.offsets[i]
+        assert torch.equal(i1, img[off:off + b1.pixels])
+        g1 = dm.backward(b1, s1, g[off:off + b1.pixels].contiguous())
+        for k in range(3):
+            sum_grads[w.volume][k] += g1[0][k]
+    for vi in range(3):
+        for k in range(3):
+            torch.testing.assert_close(grads[vi][k], sum_grads[vi][k], rtol=1e-3, atol=1e-5)
+
+
+def test_autotune_returns_candidate(tmp_path):
+    v = make_volume(seed=4, dtype=torch.float16)
+    views = views_for(v, k=2, seed=4)
+    cache = str(tmp_path / "tune.json")
+    best = dm.autotune([v], views, candidates=[(16, 8), (32, 4)], reps=1, cache=cache)
+    assert best in [(16, 8), (32, 4)]
+    assert dm.autotune([v], views, candidates=[(16, 8), (32, 4)], cache=cache) == best

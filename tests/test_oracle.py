@@ -1,0 +1,194 @@
+"""CPU checks of the oracle itself: known-answer vectors for Philox4x32-10
+(the SC'11 paper's algorithm), curand-style stream semantics, the TF
+discretisation, single-ray analytic hits, sRGB endpoints, and an FP64
+central-difference check of the differentiable marcher's adjoint. GPU-dumped
+curand and texture outputs pin the RNG and filter emulation where fixtures
+exist (tests/golden/)."""
+import json
+import math
+import os
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from visrtx_gb300 import scenes as S
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def test_philox_known_answers():
+    # Random123 / Salmon et al. (SC'11) known-answer vectors for Philox4x32-10
+    assert [hex(x) for x in O.philox_block([0, 0, 0, 0], [0, 0])] == \
+        ["0x6627e8d5", "0xe169c58d", "0xbc57ac4c", "0x9b00dbd8"]
+    assert [hex(x) for x in O.philox_block([0xffffffff] * 4, [0xffffffff] * 2)] == \
+        ["0x408f276d", "0x41c83b0e", "0xa20bc7c6", "0x6d5451fd"]
+    assert [hex(x) for x in O.philox_block([0x243f6a88, 0x85a308d3, 0x13198a2e, 0x03707344],
+                                           [0xa4093822, 0x299f31d0])] == \
+        ["0xd16cfe09", "0x94fdcceb", "0x5001e420", "0x24126ea1"]
+
+
+def test_stream_offset_and_subsequence_semantics():
+    # skipping `offset` words equals drawing them
+    base = O.philox_stream(123, 0, 0, 0, 64)
+    for off in (1, 3, 4, 17):
+        assert np.array_equal(O.philox_stream(123, 0, off, 0, 20), base[off:off + 20])
+    # uniform4 consumes 4 consecutive words
+    u4 = O.philox_stream(9, 0, 8, 2, 8)
+    u1 = O.philox_stream(9, 0, 8, 1, 8)
+    assert np.array_equal(u4, u1)
+    # a different subsequence is a different stream
+    assert not np.array_equal(O.philox_stream(9, 1, 0, 0, 8), O.philox_stream(9, 0, 0, 0, 8))
+    # uniforms live in (0, 1]
+    u = O.philox_stream(5, 0, 0, 1, 4096)
+    assert u.min() > 0.0 and u.max() <= 1.0
+
+
+def test_curand_golden_if_present():
+    p = os.path.join(GOLDEN, "curand_philox.json")
+    if not os.path.exists(p):
+        pytest.skip("no GPU-captured curand fixture")
+    d = json.load(open(p))
+    for case in d["cases"]:
+        got = O.philox_stream(case["seed"], case["subsequence"], case["offset"], case["kind"],
+                              len(case["values"]))
+        want = np.array(case["values"], np.uint32 if case["kind"] == 0 else np.float32)
+        assert np.array_equal(got, want), case
+
+
+def test_texture_golden_if_present():
+    p = os.path.join(GOLDEN, "tex_filter.json")
+    if not os.path.exists(p):
+        pytest.skip("no GPU-captured texture fixture")
+    d = json.load(open(p))
+    vox = np.array(d["volume"], np.float32).reshape(d["dims"][::-1])
+    worst = 0.0
+    for c, want in zip(d["coords"], d["values"]):
+        got = O.tex3d(vox, c, d["round_mode"])
+        worst = max(worst, abs(got - want))
+    assert worst <= d["tolerance"]
+
+
+def test_tf_two_knot_ramp():
+    tf = O.discretize_tf(np.array([[0, 0, 0], [1, 1, 1]], np.float32),
+                         np.array([0.0, 1.0], np.float32), (0.0, 1.0))
+    x = np.arange(256) / 255.0
+    np.testing.assert_allclose(tf[:, 0], x, atol=1e-6)
+    np.testing.assert_allclose(tf[:, 3], x, atol=1e-6)
+
+
+def test_tf_value_range_outside_knots():
+    # positions spread over a valueRange other than [0, 1]
+    tf = O.discretize_tf(np.array([[1, 0, 0], [0, 0, 1], [0, 1, 0]], np.float32), None,
+                         (-2.0, 6.0), uniform_opacity=0.5)
+    assert tf[0, 0] == 1.0 and tf[-1, 1] == 1.0
+    assert np.allclose(tf[:, 3], 0.5)
+
+
+def single_triangle_spec(renderer="raycast"):
+    v = np.array([[0, 0, 2], [1, 0, 2], [0, 1, 2]], np.float32)
+    surf = S.SurfaceSpec("triangle", v, id=11)
+    cam = S.CameraSpec(type="orthographic", position=(0.25, 0.25, 0.0), direction=(0, 0, 1),
+                       height=0.01, aspect=1.0)
+    return S.SceneSpec([surf], [S.InstanceSpec([0], zero=True)], [], camera=cam,
+                       renderer=S.RendererSpec(renderer), width=2, height=2, world_id=5)
+
+
+def test_single_triangle_known_answer():
+    out = O.render(single_triangle_spec())
+    assert np.allclose(out["depth"], 2.0)
+    assert np.all(out["primitiveId"] == 0) and np.all(out["objectId"] == 11)
+    assert np.all(out["instanceId"] == 5)
+    # raycast lighting |dot(dir, Ns)| * ambientColor * 0.8 grey, sRGB packed
+    c = O.render(single_triangle_spec())["color"].view(np.uint8).reshape(2, 2, 4)
+    expect = round((0.8 ** 0.41666 * 1.055 - 0.055) * 255)
+    # tonemap / inverse tonemap round trip of 0.8 is exact to 1 ulp
+    assert np.all(np.abs(c[..., 0].astype(int) - expect) <= 1)
+
+
+def test_single_sphere_known_answer():
+    c = np.array([[0.0, 0.0, 5.0]], np.float32)
+    surf = S.SurfaceSpec("sphere", c, radii=np.array([1.0], np.float32), id=3)
+    cam = S.CameraSpec(type="orthographic", position=(0, 0, 0), direction=(0, 0, 1),
+                       height=0.001, aspect=1.0)
+    spec = S.SceneSpec([surf], [S.InstanceSpec([0], zero=True)], [], camera=cam,
+                       renderer=S.RendererSpec("raycast"), width=2, height=2)
+    out = O.render(spec)
+    assert np.allclose(out["depth"], 4.0, atol=1e-5)
+
+
+def test_constant_slab_transmittance():
+    """Constant density with a constant-alpha TF: opacity after the march
+    follows 1 - (1 - a)^(n step / unit) (clean FP64 mode, no jitter effects
+    beyond the sample count)."""
+    n = 16
+    field = np.full((n, n, n), 0.5, np.float32)
+    vol = S.VolumeSpec(field=field, color=np.ones((2, 3), np.float32),
+                       opacity=np.array([0.1, 0.1], np.float32), value_range=(0.0, 1.0))
+    cam = S.CameraSpec(type="orthographic", position=(7.5, 7.5, -5.0), direction=(0, 0, 1),
+                       height=0.01, aspect=1.0)
+    spec = S.SceneSpec([], [S.InstanceSpec([], zero=True)], [], [vol], camera=cam,
+                       renderer=S.RendererSpec("raycast", volume_sampling_rate=1.0,
+                                               background=(0, 0, 0, 0)), width=1, height=1)
+    out = O.render(spec, volume_mode=1)
+    alpha = out["accum"][0, 0, 3]
+    # 15 voxels of path at 0.5-voxel steps: 30 or 31 samples after jitter
+    lo = 1 - (1 - 0.1) ** (29 * 0.5)
+    hi = 1 - (1 - 0.1) ** (31 * 0.5)
+    assert lo - 1e-6 <= alpha <= hi + 1e-6
+
+
+def test_srgb_endpoints():
+    """Black and white survive the output path; alpha is linear."""
+    for bg, want in (((0.0, 0.0, 0.0, 1.0), (0, 0, 0, 255)), ((1.0, 1.0, 1.0, 1.0), (255, 255, 255, 255))):
+        spec = S.SceneSpec([], [S.InstanceSpec([], zero=True)], [], camera=S.CameraSpec(),
+                           renderer=S.RendererSpec("raycast", background=bg), width=1, height=1)
+        out = O.render(spec)
+        assert tuple(out["color"].view(np.uint8).reshape(4)) == want
+
+
+def test_dm_adjoint_matches_central_differences():
+    """FP64 oracle adjoint vs FP64 central finite differences of the FP64
+    forward loss, at random voxels, TF entries and the opacity scale."""
+    rng = np.random.default_rng(1)
+    d = S.gaussian_blobs((10, 9, 11), n_blobs=3, seed=3, sigma_scale=0.1).astype(np.float64)
+    color, op = S.tf_knots(3, max_opacity=0.5)
+    tf = S.tf_table(color, op, 16).astype(np.float64)
+    v = {"width": 12, "height": 10}
+    from visrtx_gb300 import dm as DM
+
+    view = DM.look_at_view(0, (11, 9, 10), (1.2, 0.8, 1.6), 55.0, 12, 10, (0.2, 0.1, 0.3))
+    v.update({"eye": view.eye, "d00": view.d00, "du": view.du, "dv": view.dv,
+              "background": view.background})
+    target = rng.random((10, 12, 3))
+    scale = 1.3
+
+    # a value range wider than the data keeps every sample off the clamp
+    # kinks of the TF coordinate (where one-sided slopes differ)
+    vr = (-0.5, 1.5)
+
+    def loss(dd, tt, ss):
+        img = O.dm(dd, tt, v, ss, 0.5, 1.0, vr)
+        return 0.5 * float(np.sum((img - target) ** 2))
+
+    img = O.dm(d, tf, v, scale, 0.5, 1.0, vr)
+    _, gD, gT, gS = O.dm(d, tf, v, scale, 0.5, 1.0, vr, grad_image=img - target)
+    h = 1e-6
+    idx = np.argwhere(np.abs(gD) > 1e-6 * np.abs(gD).max())
+    for k in rng.choice(len(idx), size=min(25, len(idx)), replace=False):
+        z, y, x = idx[k]
+        dp, dm_ = d.copy(), d.copy()
+        dp[z, y, x] += h
+        dm_[z, y, x] -= h
+        fd = (loss(dp, tf, scale) - loss(dm_, tf, scale)) / (2 * h)
+        assert abs(fd - gD[z, y, x]) <= 1e-4 * max(abs(fd), 1e-3), (z, y, x, fd, gD[z, y, x])
+    tidx = np.argwhere(np.abs(gT) > 1e-9)
+    for k in rng.choice(len(tidx), size=min(12, len(tidx)), replace=False):
+        i, c = tidx[k]
+        tp, tm = tf.copy(), tf.copy()
+        tp[i, c] += h
+        tm[i, c] -= h
+        fd = (loss(d, tp, scale) - loss(d, tm, scale)) / (2 * h)
+        assert abs(fd - gT[i, c]) <= 1e-4 * max(abs(fd), 1e-3), (i, c, fd, gT[i, c])
+    fd = (loss(d, tf, scale + h) - loss(d, tf, scale - h)) / (2 * h)
+    assert abs(fd - gS) <= 1e-4 * max(abs(fd), 1e-3)

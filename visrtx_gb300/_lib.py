@@ -98,6 +98,11 @@ SIGNATURES = {
     "vrtxDMBackward": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_int,
                                  C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int,
                                  C.c_void_p]),
+    "vrtxDMPlanCreate": (C.c_void_p, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_int,
+                                      C.c_int, C.c_int, C.c_void_p]),
+    "vrtxDMPlanForward": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "vrtxDMPlanBackward": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "vrtxDMPlanRelease": (None, [C.c_void_p]),
 }
 
 
@@ -107,7 +112,7 @@ class VRTXDMVolume(C.Structure):
         ("tf", C.c_void_p), ("tfSize", C.c_int), ("opacityScale", C.c_float),
         ("step", C.c_float), ("unitDistance", C.c_float), ("valueLo", C.c_float),
         ("valueHi", C.c_float), ("gradDensity", C.c_void_p), ("gradTf", C.c_void_p),
-        ("gradOpacityScale", C.c_void_p),
+        ("gradOpacityScale", C.c_void_p), ("opacityScaleDevice", C.c_void_p),
     ]
 
 

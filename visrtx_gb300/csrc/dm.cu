@@ -19,6 +19,7 @@
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
+#include <cstring>
 #include <vector>
 
 #include "../../include/vrtx.h"
@@ -42,6 +43,7 @@ struct DMVol
   float *gD;
   float *gTF;
   float *gS;
+  const float *scalePtr; // device scalar overriding `scale`
 };
 
 struct DMViewG
@@ -206,7 +208,9 @@ __global__ void __launch_bounds__(256) k_dmForward(const DMVol *vols,
     const int py = (int)(tile / vw.tilesX) * tileH + (int)threadIdx.x / tileW;
     if (px >= vw.w || py >= vw.h)
       continue;
-    const DMVol v = vols[vw.vol];
+    DMVol v = vols[vw.vol];
+    if (v.scalePtr)
+      v.scale = __ldg(v.scalePtr);
     const f3 d = viewRay(vw, px, py);
     float t0, t1;
     f3 C = mk3(0.f, 0.f, 0.f);
@@ -268,7 +272,9 @@ __global__ void __launch_bounds__(256) k_dmBackward(const DMVol *vols,
     if (it >= numItems)
       break;
     const DMViewG vw = views[findView(views, numViews, it)];
-    const DMVol v = vols[vw.vol];
+    DMVol v = vols[vw.vol];
+    if (v.scalePtr)
+      v.scale = __ldg(v.scalePtr);
     for (int i = threadIdx.x; i < v.tfSize * 4; i += blockDim.x)
       sTF[i] = 0.f;
     __syncthreads();
@@ -365,28 +371,30 @@ __global__ void __launch_bounds__(256) k_dmBackward(const DMVol *vols,
   }
 }
 
-struct Prepared
+// --- host side ----------------------------------------------------------------
+
+// Descriptors of one launch, validated and laid out for the device:
+// [counter (256 B) | DMVol x numVolumes | DMViewG x numViews].
+struct Layout
 {
-  DMVol *dVols = nullptr;
-  DMViewG *dViews = nullptr;
-  unsigned *counter = nullptr;
+  std::vector<uint8_t> bytes;
+  size_t offVols = 256, offViews = 0;
   unsigned numItems = 0;
   int type = 0;
   int maxTf = 0;
+  int numViews = 0;
+  int tileW = 0, tileH = 0;
 };
 
-int prepare(VRTXDevice dev,
-    const VRTXDMVolume *volumes,
+int layout(const VRTXDMVolume *volumes,
     int numVolumes,
     const VRTXDMView *views,
     int numViews,
     int tileW,
     int tileH,
-    cudaStream_t s,
-    Prepared &P,
+    Layout &L,
     const char **err)
 {
-  (void)dev;
   if (!volumes || numVolumes <= 0 || !views || numViews <= 0) {
     *err = "no volumes or no views";
     return -1;
@@ -410,12 +418,12 @@ int prepare(VRTXDevice dev,
       return -4;
     }
     if (i == 0)
-      P.type = v.densityType;
-    else if (v.densityType != P.type) {
+      L.type = v.densityType;
+    else if (v.densityType != L.type) {
       *err = "all volumes of one launch must share the density type";
       return -5;
     }
-    P.maxTf = v.tfSize > P.maxTf ? v.tfSize : P.maxTf;
+    L.maxTf = v.tfSize > L.maxTf ? v.tfSize : L.maxTf;
     DMVol &o = hv[i];
     o.density = v.density;
     o.type = v.densityType;
@@ -431,6 +439,7 @@ int prepare(VRTXDevice dev,
     o.gD = v.gradDensity;
     o.gTF = v.gradTf;
     o.gS = v.gradOpacityScale;
+    o.scalePtr = v.opacityScaleDevice;
   }
   std::vector<DMViewG> hw(numViews);
   unsigned items = 0;
@@ -456,22 +465,14 @@ int prepare(VRTXDevice dev,
     o.tileStart = items;
     items += (unsigned)(o.tilesX * tilesY);
   }
-  P.numItems = items;
-  // one stream-ordered block: [counter | volumes | views]
-  const size_t offV = 256, offW = offV + ((sizeof(DMVol) * numVolumes + 255) / 256) * 256;
-  const size_t bytes = offW + sizeof(DMViewG) * numViews;
-  uint8_t *blk = nullptr;
-  if (cudaMallocAsync((void **)&blk, bytes, s) != cudaSuccess) {
-    cudaGetLastError();
-    *err = "device allocation failed";
-    return -7;
-  }
-  P.counter = reinterpret_cast<unsigned *>(blk);
-  P.dVols = reinterpret_cast<DMVol *>(blk + offV);
-  P.dViews = reinterpret_cast<DMViewG *>(blk + offW);
-  cudaMemsetAsync(blk, 0, 256, s);
-  cudaMemcpyAsync(P.dVols, hv.data(), sizeof(DMVol) * numVolumes, cudaMemcpyHostToDevice, s);
-  cudaMemcpyAsync(P.dViews, hw.data(), sizeof(DMViewG) * numViews, cudaMemcpyHostToDevice, s);
+  L.numItems = items;
+  L.numViews = numViews;
+  L.tileW = tileW;
+  L.tileH = tileH;
+  L.offViews = L.offVols + ((sizeof(DMVol) * numVolumes + 255) / 256) * 256;
+  L.bytes.assign(L.offViews + sizeof(DMViewG) * numViews, 0);
+  std::memcpy(L.bytes.data() + L.offVols, hv.data(), sizeof(DMVol) * numVolumes);
+  std::memcpy(L.bytes.data() + L.offViews, hw.data(), sizeof(DMViewG) * numViews);
   return 0;
 }
 
@@ -484,25 +485,90 @@ int gridFor(const void *kernel, int threads, size_t smem)
   return sms * (per > 0 ? per : 1);
 }
 
-void reportErr(VRTXDevice d, const char *msg);
+// The forward kernel over a descriptor block already on the device.
+cudaError_t launchForward(const Layout &L, uint8_t *block, float *image, float *state,
+    cudaStream_t s)
+{
+  unsigned *counter = reinterpret_cast<unsigned *>(block);
+  const DMVol *vols = reinterpret_cast<const DMVol *>(block + L.offVols);
+  const DMViewG *views = reinterpret_cast<const DMViewG *>(block + L.offViews);
+  cudaMemsetAsync(counter, 0, 4, s);
+  const int threads = L.tileW * L.tileH;
+  switch (L.type) {
+  case VRTX_FLOAT16:
+    k_dmForward<__half><<<gridFor((const void *)k_dmForward<__half>, threads, 0), threads, 0, s>>>(
+        vols, views, L.numViews, L.numItems, counter, L.tileW, L.tileH, image, state);
+    break;
+  case VRTX_BFLOAT16:
+    k_dmForward<__nv_bfloat16><<<gridFor((const void *)k_dmForward<__nv_bfloat16>, threads, 0), threads, 0, s>>>(
+        vols, views, L.numViews, L.numItems, counter, L.tileW, L.tileH, image, state);
+    break;
+  default:
+    k_dmForward<float><<<gridFor((const void *)k_dmForward<float>, threads, 0), threads, 0, s>>>(
+        vols, views, L.numViews, L.numItems, counter, L.tileW, L.tileH, image, state);
+    break;
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launchBackward(const Layout &L, uint8_t *block, const float *state,
+    const float *gradImage, cudaStream_t s)
+{
+  unsigned *counter = reinterpret_cast<unsigned *>(block);
+  const DMVol *vols = reinterpret_cast<const DMVol *>(block + L.offVols);
+  const DMViewG *views = reinterpret_cast<const DMViewG *>(block + L.offViews);
+  cudaMemsetAsync(counter, 0, 4, s);
+  const int threads = L.tileW * L.tileH;
+  const size_t smem = sizeof(float) * 4 * L.maxTf;
+  switch (L.type) {
+  case VRTX_FLOAT16:
+    k_dmBackward<__half><<<gridFor((const void *)k_dmBackward<__half>, threads, smem), threads, smem, s>>>(
+        vols, views, L.numViews, L.numItems, counter, L.tileW, L.tileH, state, gradImage);
+    break;
+  case VRTX_BFLOAT16:
+    k_dmBackward<__nv_bfloat16><<<gridFor((const void *)k_dmBackward<__nv_bfloat16>, threads, smem), threads, smem, s>>>(
+        vols, views, L.numViews, L.numItems, counter, L.tileW, L.tileH, state, gradImage);
+    break;
+  default:
+    k_dmBackward<float><<<gridFor((const void *)k_dmBackward<float>, threads, smem), threads, smem, s>>>(
+        vols, views, L.numViews, L.numItems, counter, L.tileW, L.tileH, state, gradImage);
+    break;
+  }
+  return cudaGetLastError();
+}
+
+// Stream-ordered device copy of a layout (freed by the caller).
+uint8_t *upload(const Layout &L, cudaStream_t s)
+{
+  uint8_t *blk = nullptr;
+  if (cudaMallocAsync((void **)&blk, L.bytes.size(), s) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  cudaMemcpyAsync(blk, L.bytes.data(), L.bytes.size(), cudaMemcpyHostToDevice, s);
+  return blk;
+}
 
 } // namespace
-
 } // namespace vrtx
 
 // status reporting lives in device.cpp
 extern "C" void vrtxInternalReport(VRTXDevice d, int severity, const char *msg);
 
-namespace vrtx {
-namespace {
-void reportErr(VRTXDevice d, const char *msg)
+struct VRTXDMPlan_st
 {
-  vrtxInternalReport(d, VRTX_SEVERITY_ERROR, msg);
-}
-} // namespace
-} // namespace vrtx
+  VRTXDevice dev;
+  vrtx::Layout L;
+  uint8_t *block = nullptr;
+};
 
 using namespace vrtx;
+
+static int fail(VRTXDevice d, const char *msg, int rc)
+{
+  vrtxInternalReport(d, VRTX_SEVERITY_ERROR, msg);
+  return rc;
+}
 
 extern "C" {
 
@@ -518,38 +584,20 @@ VRTX_API int vrtxDMForward(VRTXDevice d,
     void *stream)
 {
   cudaStream_t s = (cudaStream_t)stream;
-  Prepared P;
+  if (!image || !state)
+    return fail(d, "vrtxDMForward: image and state are required", -1);
+  Layout L;
   const char *err = nullptr;
-  if (!image || !state) {
-    reportErr(d, "vrtxDMForward: image and state are required");
-    return -1;
-  }
-  int rc = prepare(d, volumes, numVolumes, views, numViews, tileW, tileH, s, P, &err);
-  if (rc) {
-    reportErr(d, err);
-    return rc;
-  }
-  const int threads = tileW * tileH;
-  switch (P.type) {
-  case VRTX_FLOAT16:
-    k_dmForward<__half><<<gridFor((const void *)k_dmForward<__half>, threads, 0), threads, 0, s>>>(
-        P.dVols, P.dViews, numViews, P.numItems, P.counter, tileW, tileH, image, state);
-    break;
-  case VRTX_BFLOAT16:
-    k_dmForward<__nv_bfloat16><<<gridFor((const void *)k_dmForward<__nv_bfloat16>, threads, 0), threads, 0, s>>>(
-        P.dVols, P.dViews, numViews, P.numItems, P.counter, tileW, tileH, image, state);
-    break;
-  default:
-    k_dmForward<float><<<gridFor((const void *)k_dmForward<float>, threads, 0), threads, 0, s>>>(
-        P.dVols, P.dViews, numViews, P.numItems, P.counter, tileW, tileH, image, state);
-    break;
-  }
-  const cudaError_t e = cudaGetLastError();
-  cudaFreeAsync(P.counter, s);
-  if (e != cudaSuccess) {
-    reportErr(d, cudaGetErrorString(e));
-    return -8;
-  }
+  const int rc = layout(volumes, numVolumes, views, numViews, tileW, tileH, L, &err);
+  if (rc)
+    return fail(d, err, rc);
+  uint8_t *blk = upload(L, s);
+  if (!blk)
+    return fail(d, "vrtxDMForward: device allocation failed", -7);
+  const cudaError_t e = launchForward(L, blk, image, state, s);
+  cudaFreeAsync(blk, s);
+  if (e != cudaSuccess)
+    return fail(d, cudaGetErrorString(e), -8);
   return 0;
 }
 
@@ -567,40 +615,80 @@ VRTX_API int vrtxDMBackward(VRTXDevice d,
 {
   (void)image;
   cudaStream_t s = (cudaStream_t)stream;
-  Prepared P;
+  if (!state || !gradImage)
+    return fail(d, "vrtxDMBackward: state and gradImage are required", -1);
+  Layout L;
   const char *err = nullptr;
-  if (!state || !gradImage) {
-    reportErr(d, "vrtxDMBackward: state and gradImage are required");
-    return -1;
-  }
-  int rc = prepare(d, volumes, numVolumes, views, numViews, tileW, tileH, s, P, &err);
-  if (rc) {
-    reportErr(d, err);
-    return rc;
-  }
-  const int threads = tileW * tileH;
-  const size_t smem = sizeof(float) * 4 * P.maxTf;
-  switch (P.type) {
-  case VRTX_FLOAT16:
-    k_dmBackward<__half><<<gridFor((const void *)k_dmBackward<__half>, threads, smem), threads, smem, s>>>(
-        P.dVols, P.dViews, numViews, P.numItems, P.counter, tileW, tileH, state, gradImage);
-    break;
-  case VRTX_BFLOAT16:
-    k_dmBackward<__nv_bfloat16><<<gridFor((const void *)k_dmBackward<__nv_bfloat16>, threads, smem), threads, smem, s>>>(
-        P.dVols, P.dViews, numViews, P.numItems, P.counter, tileW, tileH, state, gradImage);
-    break;
-  default:
-    k_dmBackward<float><<<gridFor((const void *)k_dmBackward<float>, threads, smem), threads, smem, s>>>(
-        P.dVols, P.dViews, numViews, P.numItems, P.counter, tileW, tileH, state, gradImage);
-    break;
-  }
-  const cudaError_t e = cudaGetLastError();
-  cudaFreeAsync(P.counter, s);
-  if (e != cudaSuccess) {
-    reportErr(d, cudaGetErrorString(e));
-    return -8;
-  }
+  const int rc = layout(volumes, numVolumes, views, numViews, tileW, tileH, L, &err);
+  if (rc)
+    return fail(d, err, rc);
+  uint8_t *blk = upload(L, s);
+  if (!blk)
+    return fail(d, "vrtxDMBackward: device allocation failed", -7);
+  const cudaError_t e = launchBackward(L, blk, state, gradImage, s);
+  cudaFreeAsync(blk, s);
+  if (e != cudaSuccess)
+    return fail(d, cudaGetErrorString(e), -8);
   return 0;
+}
+
+VRTX_API VRTXDMPlan vrtxDMPlanCreate(VRTXDevice d,
+    const VRTXDMVolume *volumes,
+    int numVolumes,
+    const VRTXDMView *views,
+    int numViews,
+    int tileW,
+    int tileH,
+    void *stream)
+{
+  auto *p = new VRTXDMPlan_st();
+  p->dev = d;
+  const char *err = nullptr;
+  if (layout(volumes, numVolumes, views, numViews, tileW, tileH, p->L, &err)) {
+    fail(d, err, -1);
+    delete p;
+    return nullptr;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  if (cudaMalloc((void **)&p->block, p->L.bytes.size()) != cudaSuccess) {
+    cudaGetLastError();
+    fail(d, "vrtxDMPlanCreate: device allocation failed", -7);
+    delete p;
+    return nullptr;
+  }
+  cudaMemcpyAsync(
+      p->block, p->L.bytes.data(), p->L.bytes.size(), cudaMemcpyHostToDevice, s);
+  cudaStreamSynchronize(s);
+  return p;
+}
+
+VRTX_API int vrtxDMPlanForward(
+    VRTXDMPlan plan, float *image, float *state, void *stream)
+{
+  if (!plan || !image || !state)
+    return -1;
+  const cudaError_t e =
+      launchForward(plan->L, plan->block, image, state, (cudaStream_t)stream);
+  return e == cudaSuccess ? 0 : fail(plan->dev, cudaGetErrorString(e), -8);
+}
+
+VRTX_API int vrtxDMPlanBackward(
+    VRTXDMPlan plan, const float *state, const float *gradImage, void *stream)
+{
+  if (!plan || !state || !gradImage)
+    return -1;
+  const cudaError_t e =
+      launchBackward(plan->L, plan->block, state, gradImage, (cudaStream_t)stream);
+  return e == cudaSuccess ? 0 : fail(plan->dev, cudaGetErrorString(e), -8);
+}
+
+VRTX_API void vrtxDMPlanRelease(VRTXDMPlan plan)
+{
+  if (!plan)
+    return;
+  if (plan->block)
+    cudaFree(plan->block);
+  delete plan;
 }
 
 } // extern "C"
