@@ -397,6 +397,31 @@ VRTX_API int vrtxDMPlanBackward(VRTXDMPlan plan,
     void *stream);
 VRTX_API void vrtxDMPlanRelease(VRTXDMPlan plan);
 
+/* The forward pass of vrtxDMForward for callers that cannot allocate
+ * device memory: code whose memory comes from an allocator that is not
+ * CUDA's (a host application's pool, a plugin sandbox), or code running
+ * where cudaMalloc must not be called. No counterpart in the reference
+ * (VisRTX has no gradient path).
+ *
+ * Same arguments and results as vrtxDMForward. It allocates nothing: its
+ * scratch (the launch counter and the volume/view descriptors) is one
+ * fixed-size device array inside the library, at most 64 volumes and 4096
+ * views per call (about 400 KB, held on every GPU that loads the library
+ * until the process exits); larger requests are rejected with an error.
+ * The first call on a device looks up that array's device address; make
+ * that first call before any stream capture. All calls share the array:
+ * calls that overlap on the GPU (unordered streams) race on it. */
+VRTX_API int vrtxDMForwardNoAlloc(VRTXDevice d,
+    const VRTXDMVolume *volumes,
+    int numVolumes,
+    const VRTXDMView *views,
+    int numViews,
+    float *image,
+    float *state,
+    int tileW,
+    int tileH,
+    void *stream);
+
 #ifdef __cplusplus
 } /* extern "C" */
 #endif

@@ -103,6 +103,8 @@ SIGNATURES = {
     "vrtxDMPlanForward": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "vrtxDMPlanBackward": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "vrtxDMPlanRelease": (None, [C.c_void_p]),
+    "vrtxDMForwardNoAlloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_int,
+                                       C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p]),
 }
 
 

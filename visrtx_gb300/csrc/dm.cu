@@ -20,6 +20,7 @@
 #include <cuda_fp16.h>
 
 #include <cstring>
+#include <mutex>
 #include <vector>
 
 #include "../../include/vrtx.h"
@@ -692,3 +693,94 @@ VRTX_API void vrtxDMPlanRelease(VRTXDMPlan plan)
 }
 
 } // extern "C"
+
+// ---------------------------------------------------------------------------
+// vrtxDMForwardNoAlloc: the forward pass for callers that cannot allocate
+// device memory (a host whose allocator is not CUDA's, code running where
+// cudaMalloc is not allowed).
+//
+// Its scratch -- the launch counter and the volume/view descriptors that
+// vrtxDMForward puts in a stream-ordered allocation -- lives in one
+// file-scope device array of fixed size instead. Every GPU that loads the
+// library holds that array until the process exits. Every call reuses it:
+// the counter is cleared and the descriptors are rewritten on each call, so
+// two calls that overlap on the GPU (different streams, no ordering) race
+// on it.
+// ---------------------------------------------------------------------------
+
+namespace {
+
+constexpr int kNoAllocMaxVolumes = 64;
+constexpr int kNoAllocMaxViews = 4096;
+constexpr size_t kNoAllocBytes = 256
+    + ((sizeof(vrtx::DMVol) * kNoAllocMaxVolumes + 255) / 256) * 256
+    + sizeof(vrtx::DMViewG) * kNoAllocMaxViews;
+
+__device__ __align__(256) uint8_t g_dmNoAllocScratch[kNoAllocBytes];
+
+// Device address of g_dmNoAllocScratch per device ordinal. The symbol's name
+// in host code is only a host-side stand-in; kernels need this address.
+std::mutex g_noAllocMutex;
+uint8_t *g_noAllocAddr[64] = {};
+
+uint8_t *noAllocScratch(VRTXDevice d)
+{
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
+    cudaGetLastError();
+    fail(d, "vrtxDMForwardNoAlloc: no current CUDA device", -9);
+    return nullptr;
+  }
+  std::lock_guard<std::mutex> lock(g_noAllocMutex);
+  if (!g_noAllocAddr[dev]) {
+    void *p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_dmNoAllocScratch);
+    if (e != cudaSuccess || !p) {
+      cudaGetLastError();
+      fail(d, "vrtxDMForwardNoAlloc: cudaGetSymbolAddress failed", -9);
+      return nullptr;
+    }
+    g_noAllocAddr[dev] = (uint8_t *)p;
+  }
+  return g_noAllocAddr[dev];
+}
+
+} // namespace
+
+extern "C" VRTX_API int vrtxDMForwardNoAlloc(VRTXDevice d,
+    const VRTXDMVolume *volumes,
+    int numVolumes,
+    const VRTXDMView *views,
+    int numViews,
+    float *image,
+    float *state,
+    int tileW,
+    int tileH,
+    void *stream)
+{
+  cudaStream_t s = (cudaStream_t)stream;
+  if (!image || !state)
+    return fail(d, "vrtxDMForwardNoAlloc: image and state are required", -1);
+  if (numVolumes > kNoAllocMaxVolumes || numViews > kNoAllocMaxViews)
+    return fail(d,
+        "vrtxDMForwardNoAlloc: at most 64 volumes and 4096 views per call",
+        -10);
+  Layout L;
+  const char *err = nullptr;
+  const int rc = layout(volumes, numVolumes, views, numViews, tileW, tileH, L, &err);
+  if (rc)
+    return fail(d, err, rc);
+  uint8_t *blk = noAllocScratch(d);
+  if (!blk)
+    return -9;
+  // the counter is zeroed by launchForward; descriptors overwrite the rest
+  if (cudaMemcpyAsync(blk, L.bytes.data(), L.bytes.size(), cudaMemcpyHostToDevice, s)
+      != cudaSuccess) {
+    cudaGetLastError();
+    return fail(d, "vrtxDMForwardNoAlloc: descriptor copy failed", -11);
+  }
+  const cudaError_t e = launchForward(L, blk, image, state, s);
+  if (e != cudaSuccess)
+    return fail(d, cudaGetErrorString(e), -8);
+  return 0;
+}
