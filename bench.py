@@ -51,6 +51,10 @@ def _args():
     p.add_argument("--e2e-steps", type=int, default=2)
     p.add_argument("--cpu-seconds", type=float, default=12.0)
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--workload", default="instanced",
+                   choices=["instanced", "volume", "dm", "batched"],
+                   help="instanced (default line) | volume | dm | batched")
+    p.add_argument("--dm-views", type=int, default=128)
     return p.parse_args()
 
 
@@ -206,6 +210,12 @@ def build_scene(dev, spec):
 def main():
     args = _args()
     ws, rank, local = _dist()
+    if args.workload != "instanced":
+        import bench_workloads as BW
+
+        {"volume": BW.run_volume, "dm": BW.run_dm, "batched": BW.run_batched}[args.workload](
+            args, ws, rank, local)
+        return
     if args.impl == "reference":
         run_reference(args, ws, rank)
         return

@@ -66,7 +66,15 @@ def test_texture_golden_if_present():
     for c, want in zip(d["coords"], d["values"]):
         got = O.tex3d(vox, c, d["round_mode"])
         worst = max(worst, abs(got - want))
-    assert worst <= d["tolerance"]
+    # 3D: the per-axis 8-bit-weight emulation stays within the recorded bound
+    # (it does not reproduce the hardware exactly)
+    assert worst <= d["tolerance"] and d["tolerance"] < 0.01
+    # 1D float4 (the TF path): round-to-nearest 8-bit weights match exactly
+    t1 = d["tex1"]
+    table = np.array(t1["table"], np.float32).reshape(-1, 4)
+    vals = np.array(t1["values"], np.float32).reshape(-1, 4)
+    for c, want in zip(t1["coords"], vals):
+        np.testing.assert_allclose(O.tex1d(table, c, 1), want, rtol=0, atol=1e-6)
 
 
 def test_tf_two_knot_ramp():

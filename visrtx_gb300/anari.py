@@ -217,8 +217,17 @@ class Device:
         a.type_code = L.ARRAY1D
         return a
 
-    def new_array3d(self, data: np.ndarray, elem_type: int | None = None) -> Array:
-        """3D array from a (nz, ny, nx) numpy array (x fastest)."""
+    def new_array3d(self, data, elem_type: int | None = None) -> Array:
+        """3D array from a (nz, ny, nx) numpy array (x fastest), or a CUDA
+        tensor of that shape (used in place, NV_ARRAY_CUDA)."""
+        if hasattr(data, "data_ptr") and getattr(data, "is_cuda", False):
+            nz, ny, nx = data.shape
+            et = elem_type or L.FLOAT32
+            h = self.lib.vrtxNewArray3D(self.h, C.c_void_p(data.data_ptr()), None, None, et,
+                                        nx, ny, nz)
+            a = Array(self, h, et, data)
+            a.type_code = L.ARRAY3D
+            return a
         arr = np.ascontiguousarray(data)
         if elem_type is None:
             elem_type = _NP_TYPES[(arr.dtype, 1)]
@@ -328,12 +337,13 @@ class Frame(Object):
     def stats(self) -> dict:
         """libvrtx traversal counters of the last render (see
         "vrtx.stats" in device.cpp)."""
-        buf = (C.c_uint64 * 6)()
+        buf = (C.c_uint64 * 8)()
         ok = self.device.lib.vrtxGetProperty(self.device.h, self.handle, b"vrtx.stats",
-                                             L.UINT64, buf, 48, L.WAIT)
+                                             L.UINT64, buf, 64, L.WAIT)
         if not ok:
             return {}
-        keys = ("rays", "nodes", "tri_tests", "sphere_tests", "blas_entries", "error_flags")
+        keys = ("rays", "nodes", "tri_tests", "sphere_tests", "blas_entries", "volume_samples",
+                "volume_fetches", "error_flags")
         return dict(zip(keys, (int(v) for v in buf)))
 
     def kernel_launches(self) -> int:

@@ -1936,17 +1936,18 @@ bool Frame::getProperty(
     std::memcpy(mem, &v, 4);
     return true;
   }
-  // libvrtx extension (no reference counterpart): traversal counters of the
-  // last render: rays traced, and with "vrtx.countTraversal" set also BVH8
-  // nodes visited, triangle tests, sphere tests, BLAS entries; then the
-  // traversal error flags (bit 0: stack overflow).
-  if (name == "vrtx.stats" && t == VRTX_UINT64 && size >= 48 && stats) {
+  // libvrtx extension (no reference counterpart): counters of the last
+  // render: rays traced; with "vrtx.countTraversal" set also BVH8 nodes
+  // visited, triangle tests, sphere tests, BLAS entries; volume march
+  // positions and fetched samples; then the traversal error flags (bit 0:
+  // stack overflow, bit 1: iteration bound).
+  if (name == "vrtx.stats" && t == VRTX_UINT64 && size >= 64 && stats) {
     wait();
-    unsigned long long v[6] = {};
-    cudaMemcpy(v, stats, 5 * sizeof(unsigned long long), cudaMemcpyDeviceToHost);
+    unsigned long long v[8] = {};
+    cudaMemcpy(v, stats, 7 * sizeof(unsigned long long), cudaMemcpyDeviceToHost);
     uint32_t flags = 0;
     cudaMemcpy(&flags, errorFlag, 4, cudaMemcpyDeviceToHost);
-    v[5] = flags;
+    v[7] = flags;
     std::memcpy(mem, v, sizeof(v));
     return true;
   }

@@ -249,6 +249,19 @@ struct WorldGPU
   uint32_t allOpaque; // every material is opaque: any-hit = first hit
 };
 
+// Per-thread work counters. Rays and volume samples are counted by every
+// kernel; node visits and primitive tests only by the counting builds.
+struct TravStats
+{
+  uint32_t nodes; // BVH8 nodes visited (TLAS + BLAS)
+  uint32_t tris; // triangle tests
+  uint32_t spheres; // sphere tests
+  uint32_t instances; // BLAS entries
+  uint32_t rays; // traversals
+  uint32_t samples; // volume march positions (the reference's samples)
+  uint32_t fetches; // of which fetched and classified (not skipped)
+};
+
 struct FrameParams
 {
   WorldGPU world;
@@ -258,7 +271,8 @@ struct FrameParams
   uint32_t *workCounter; // persistent scheduling counter (zeroed per launch)
   uint32_t *errorFlag; // bit 0: traversal stack overflow
   unsigned long long *stats; // [0] rays, [1] nodes, [2] tri tests,
-                             // [3] sphere tests, [4] BLAS entries
+                             // [3] sphere tests, [4] BLAS entries,
+                             // [5] volume samples, [6] volume fetches
   uint32_t numTilesX, numTilesY;
   uint32_t launchW, launchH; // checkerboarding halves these
 };

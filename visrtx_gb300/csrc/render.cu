@@ -291,7 +291,7 @@ __device__ __forceinline__ float4 shadeSurfaceDL(const FrameParams &P,
         1.f - surfaceAttenuation<STATS>(P, st, shadePoint, ldir, 0.f, ldist);
     const float volume_o = 1.f
         - volumeAttenuation(
-            w, rs, shadePoint, ldir, 0.f, ldist, rp.invVolumeSamplingRate);
+            w, rs, shadePoint, ldir, 0.f, ldist, rp.invVolumeSamplingRate, st);
     const float attenuation = surface_o * volume_o;
     const float NdotL = fmaxf(0.f, dot(hit.Ns, ldir));
     const f3 thisLight =
@@ -367,7 +367,8 @@ __device__ __forceinline__ void integrateSample(const FrameParams &P,
           color,
           opacity,
           vObjID,
-          vInstID);
+          vInstID,
+          st);
       if (firstHit) {
         const bool volumeFirst = vDepth < sh.t;
         if (volumeFirst) {
@@ -427,7 +428,8 @@ __device__ __forceinline__ void integrateSample(const FrameParams &P,
           color,
           opacity,
           vObjID,
-          vInstID);
+          vInstID,
+          st);
       if (firstHit) {
         depth = fminf(depth, volumeDepth);
         primID = 0;
@@ -712,7 +714,7 @@ __global__ void __launch_bounds__(128, VRTX_RENDER_MIN_BLOCKS) k_render(const Fr
 {
   const int lane = threadIdx.x & 31;
   const uint32_t numTiles = P.numTilesX * P.numTilesY;
-  TravStats st{0u, 0u, 0u, 0u, 0u};
+  TravStats st{0u, 0u, 0u, 0u, 0u, 0u, 0u};
   while (true) {
     uint32_t t = 0;
     if (lane == 0)
@@ -726,10 +728,17 @@ __global__ void __launch_bounds__(128, VRTX_RENDER_MIN_BLOCKS) k_render(const Fr
     if (lx < (int)P.launchW && ly < (int)P.launchH)
       renderPixel<RT, STATS>(P, st, lx, ly);
   }
-  // per-warp totals: rays always, traversal counters in the counting build
+  // per-warp totals: rays and volume samples always, traversal counters in
+  // the counting build
   const unsigned long long rays = warpSum(st.rays);
-  if (lane == 0)
+  const unsigned long long smp = warpSum(st.samples), fet = warpSum(st.fetches);
+  if (lane == 0) {
     atomicAdd(P.stats + 0, rays);
+    if (smp)
+      atomicAdd(P.stats + 5, smp);
+    if (fet)
+      atomicAdd(P.stats + 6, fet);
+  }
   if (STATS) {
     const unsigned long long n = warpSum(st.nodes), t = warpSum(st.tris),
                              sp = warpSum(st.spheres), in = warpSum(st.instances);
@@ -837,7 +846,7 @@ __global__ void __launch_bounds__(128) k_aoPrimary(const FrameParams P,
   const int x = computePixelX((int)lx, fb.checkerboardID);
   const int y = computePixelY((int)ly, fb.checkerboardID);
   const bool valid = lx < P.launchW && ly < P.launchH && x < (int)fb.w && y < (int)fb.h;
-  TravStats st{0u, 0u, 0u, 0u, 0u};
+  TravStats st{0u, 0u, 0u, 0u, 0u, 0u, 0u};
   uint32_t nRays = 0;
   RandState rs;
   AOPixel px;
@@ -929,7 +938,7 @@ __global__ void __launch_bounds__(128, VRTX_TRACE_MIN_BLOCKS) k_aoTrace(const Fr
     float *weighted)
 {
   const uint32_t n = *rayCount;
-  TravStats st{0u, 0u, 0u, 0u, 0u};
+  TravStats st{0u, 0u, 0u, 0u, 0u, 0u, 0u};
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += gridDim.x * blockDim.x) {
     const AORay r = rays[i];

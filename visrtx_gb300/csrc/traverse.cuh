@@ -274,18 +274,6 @@ __device__ __forceinline__ float surfaceOpacity(
 // (accumulateValue(o, opacity, o); terminate at o >= 0.99), as the
 // __anyhit__shadow / __anyhit__ao programs do (DirectLight_ptx.cu:233-256,
 // AmbientOcclusion_ptx.cu:53-69).
-// Per-thread traversal counters (filled only by the counting kernels, which
-// pass a non-null pointer; the timed kernels pass nullptr and the counting
-// code folds away).
-struct TravStats
-{
-  uint32_t nodes; // BVH8 nodes visited (TLAS + BLAS)
-  uint32_t tris; // triangle tests
-  uint32_t spheres; // sphere tests
-  uint32_t instances; // BLAS entries
-  uint32_t rays; // traverse() calls
-};
-
 template <int MODE, bool STATS = false>
 __device__ __forceinline__ bool traverse(const WorldGPU &w,
     f3 org,

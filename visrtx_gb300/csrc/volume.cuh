@@ -119,7 +119,8 @@ __device__ __forceinline__ float rayMarchVolume(const VolumeGPU &v,
     RandState &rs,
     f3 *color,
     float &opacity,
-    float invSamplingRate)
+    float invSamplingRate,
+    TravStats &st)
 {
   float lower = h.tlo;
   const float upper = h.thi;
@@ -135,7 +136,9 @@ __device__ __forceinline__ float rayMarchVolume(const VolumeGPU &v,
   for (int guard = 0; guard < (1 << 24) && opacity < 0.99f && upper - lower >= 0.f;
        guard++) {
     const f3 p = h.localOrg + h.localDir * lower;
+    st.samples++;
     if (cellMajorant(v, p) > 0.f) {
+      st.fetches++;
       const float s = sampleField(v, p);
       if (!isnan(s)) {
         const float4 co = classifySample(v, s);
@@ -163,7 +166,8 @@ __device__ __forceinline__ float rayMarchAllVolumes(const WorldGPU &w,
     f3 &color,
     float &opacity,
     uint32_t &objID,
-    uint32_t &instID)
+    uint32_t &instID,
+    TravStats &st)
 {
   float depth = tfar;
   if (w.numVolumes == 0)
@@ -182,7 +186,7 @@ __device__ __forceinline__ float rayMarchAllVolumes(const WorldGPU &w,
     }
     depth = fminf(depth, h.tlo);
     h.thi = fminf(tfar, h.thi);
-    rayMarchVolume(v, h, rs, &color, opacity, invSamplingRate);
+    rayMarchVolume(v, h, rs, &color, opacity, invSamplingRate, st);
     tmin = h.thi + 1e-3f;
     last = h.entry;
   } while (opacity < 0.99f);
@@ -197,7 +201,8 @@ __device__ __forceinline__ float volumeAttenuation(const WorldGPU &w,
     f3 dir,
     float tmin,
     float tmax,
-    float invSamplingRate)
+    float invSamplingRate,
+    TravStats &st)
 {
   float a = 0.f;
   for (uint32_t i = 0; i < w.numVolumes; i++) {
@@ -205,7 +210,7 @@ __device__ __forceinline__ float volumeAttenuation(const WorldGPU &w,
     if (!volumeSlab(w.volumes[i], org, dir, tmin, tmax, h))
       continue;
     h.entry = (int)i;
-    rayMarchVolume(w.volumes[i], h, rs, nullptr, a, invSamplingRate);
+    rayMarchVolume(w.volumes[i], h, rs, nullptr, a, invSamplingRate, st);
     if (a >= 0.99f)
       break;
   }

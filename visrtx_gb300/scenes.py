@@ -455,7 +455,8 @@ def build_on_device(dev, spec: SceneSpec, channels=("color", "depth", "primitive
     vols = []
     for v in spec.volumes:
         f = dev.new_spatial_field("structuredRegular")
-        f.set("data", arr3(np.ascontiguousarray(v.field, np.float32), L.FLOAT32))
+        fld = v.field if hasattr(v.field, "data_ptr") else np.ascontiguousarray(v.field, np.float32)
+        f.set("data", arr3(fld, L.FLOAT32))
         f.set("origin", tuple(map(float, v.origin)), L.FLOAT32_VEC3)
         f.set("spacing", tuple(map(float, v.spacing)), L.FLOAT32_VEC3)
         f.set("filter", v.filter)
