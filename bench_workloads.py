@@ -99,11 +99,13 @@ def _dm_problem(n=256, views=128, res=512, dtype=torch.float16, seed=0):
     d = S.gaussian_blobs((n, n, n), 32, seed, device="cuda")
     color, op = S.tf_knots(seed, max_opacity=0.25)
     tf = torch.tensor(S.tf_table(color, op, 256), device="cuda")
-    vol = dm.VolumeInput(d.to(dtype).contiguous(), tf, torch.tensor([1.0], device="cuda"),
+    scale = torch.tensor([1.0], device="cuda")
+    vol = dm.VolumeInput(d.to(dtype).contiguous(), tf, scale,
                          step=0.5, unit=1.0, value_range=(0.0, 1.0))
+    vol32 = dm.VolumeInput(d, tf, scale, step=0.5, unit=1.0, value_range=(0.0, 1.0), plain=True)
     dirs = S.fibonacci_sphere(views)
     vws = [dm.look_at_view(0, vol.dims, 2.0 * dirs[i], 45.0, res, res) for i in range(views)]
-    return vol, vws
+    return vol, vol32, vws
 
 
 def _time_steps(fn, steps, warmup, flush):
@@ -166,7 +168,7 @@ def _per_view_fp32_step(vols32, views):
     return body
 
 
-def _dm_line(name, workload, vols, views, args, local):
+def _dm_line(name, workload, vols, vols32, views, args, local):
     torch.cuda.set_device(local)
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
     cache = os.path.join(os.path.expanduser("~"), ".cache", "vrtx", "dm_tune.json")
@@ -176,9 +178,8 @@ def _dm_line(name, workload, vols, views, args, local):
     clocks.start()
     tb = _time_steps(graph.replay, args.steps, args.warmup, flush)
     clk = clocks.stop()
-    # the plain FP32 one-view-per-launch form on the same views
-    vols32 = [dm.VolumeInput(v.density.float().contiguous(), v.tf, v.scale, v.step, v.unit,
-                             v.value_range) for v in vols]
+    # the plain FP32 one-view-per-launch form on the same views (the FP32
+    # fields the low-precision copies were made from, direct atomics)
     body32 = _per_view_fp32_step(vols32, views)
     t32 = _time_steps(body32, max(1, args.steps // 2), 1, flush)
     # image error of the batched low-precision form against FP32
@@ -214,8 +215,8 @@ def run_dm(args, ws, rank, local):
     import __graft_entry__ as g
 
     g.build()
-    vol, views = _dm_problem(views=args.dm_views)
-    _dm_line("dm", f"dm256_fp16_{len(views)}views_512x512", [vol], views, args, local)
+    vol, vol32, views = _dm_problem(views=args.dm_views)
+    _dm_line("dm", f"dm256_fp16_{len(views)}views_512x512", [vol], [vol32], views, args, local)
 
 
 def run_batched(args, ws, rank, local):
@@ -224,19 +225,22 @@ def run_batched(args, ws, rank, local):
 
     g.build()
     rng = S.Rng(5, stream=17)
-    vols, views = [], []
+    vols, vols32, views = [], [], []
     res_choices = [256, 512, 1024]
     for i in range(64):
         dims = tuple(int(x) for x in rng.uniform(3, 64, 385).astype(int))
         d = S.gaussian_blobs(dims, 16, 100 + i, device="cuda", sigma_scale=max(dims) / 512)
         color, op = S.tf_knots(100 + i, max_opacity=0.25)
         tf = torch.tensor(S.tf_table(color, op, 256), device="cuda")
-        vols.append(dm.VolumeInput(d.to(torch.bfloat16).contiguous(), tf,
-                                   torch.tensor([1.0], device="cuda"), 0.5, 1.0, (0.0, 1.0)))
+        scale = torch.tensor([1.0], device="cuda")
+        vols.append(dm.VolumeInput(d.to(torch.bfloat16).contiguous(), tf, scale, 0.5, 1.0,
+                                   (0.0, 1.0)))
+        vols32.append(dm.VolumeInput(d, tf, scale, 0.5, 1.0, (0.0, 1.0), plain=True))
         nv = int(rng.uniform(1, 4, 33)[0])
         dirs = S.fibonacci_sphere(nv)
         for k in range(nv):
             w = res_choices[int(rng.uniform(1, 0, 3)[0])]
             h = res_choices[int(rng.uniform(1, 0, 3)[0])]
             views.append(dm.look_at_view(i, vols[-1].dims, 2.0 * dirs[k], 45.0, w, h))
-    _dm_line("batched", f"batched64_bf16_{len(views)}views_uneven", vols, views, args, local)
+    _dm_line("batched", f"batched64_bf16_{len(views)}views_uneven", vols, vols32, views, args,
+             local)

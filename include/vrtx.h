@@ -334,7 +334,14 @@ typedef struct VRTXDMVolume {
   float *gradOpacityScale; /* one fp32; backward only, may be NULL */
   const float *opacityScaleDevice; /* when not NULL, read instead of
                                       opacityScale (device scalar) */
+  int flags;             /* VRTX_DM_* bits, 0 by default */
 } VRTXDMVolume;
+
+/* Backward pass: one atomic add per gradient term per sample instead of
+ * per-thread run-length accumulation (consecutive samples of a ray that
+ * stay in one trilinear cell / one TF segment summed in registers first).
+ * Both give the same gradients up to float summation order. */
+#define VRTX_DM_PLAIN 1
 
 typedef struct VRTXDMView {
   int volume;            /* index into the volume array */

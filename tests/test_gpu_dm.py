@@ -77,9 +77,13 @@ def test_forward_rms_vs_fp64(dtype):
     assert 0.05 < float(img.mean()) < 1.0  # the views see the volume
 
 
-@pytest.mark.parametrize("dtype", [torch.float32, torch.float16])
-def test_adjoint_vs_fp64(dtype):
+@pytest.mark.parametrize("dtype,plain", [(torch.float32, False), (torch.float16, False),
+                                         (torch.float32, True)])
+def test_adjoint_vs_fp64(dtype, plain):
+    """Both gradient accumulation forms (run-length per thread, and one
+    atomic per term) against the FP64 oracle adjoint."""
     v = make_volume(dtype=dtype, seed=1)
+    v.plain = plain
     views = views_for(v, k=2, seed=1)
     b = dm.Batch([v], views)
     img, state = dm.forward(b)

@@ -108,6 +108,9 @@ SIGNATURES = {
 }
 
 
+DM_PLAIN = 1  # VRTX_DM_PLAIN
+
+
 class VRTXDMVolume(C.Structure):
     _fields_ = [
         ("density", C.c_void_p), ("densityType", C.c_int), ("dims", C.c_int * 3),
@@ -115,6 +118,7 @@ class VRTXDMVolume(C.Structure):
         ("step", C.c_float), ("unitDistance", C.c_float), ("valueLo", C.c_float),
         ("valueHi", C.c_float), ("gradDensity", C.c_void_p), ("gradTf", C.c_void_p),
         ("gradOpacityScale", C.c_void_p), ("opacityScaleDevice", C.c_void_p),
+        ("flags", C.c_int),
     ]
 
 

@@ -45,6 +45,7 @@ struct DMVol
   float *gTF;
   float *gS;
   const float *scalePtr; // device scalar overriding `scale`
+  int flags; // VRTX_DM_PLAIN: one atomic per gradient term
 };
 
 struct DMViewG
@@ -250,6 +251,40 @@ __global__ void __launch_bounds__(256) k_dmForward(const DMVol *vols,
   }
 }
 
+__device__ __forceinline__ void flushCell(float *G, const Tri &c, float acc[8])
+{
+  if (c.base == ~size_t(0))
+    return;
+  float *g = G + c.base;
+  const size_t off[8] = {0,
+      (size_t)c.sx,
+      (size_t)c.sy,
+      (size_t)c.sy + c.sx,
+      (size_t)c.sz,
+      (size_t)c.sz + c.sx,
+      (size_t)c.sz + c.sy,
+      (size_t)c.sz + c.sy + c.sx};
+#pragma unroll
+  for (int q = 0; q < 8; q++) {
+    if (acc[q] != 0.f)
+      atomicAdd(g + off[q], acc[q]);
+    acc[q] = 0.f;
+  }
+}
+
+__device__ __forceinline__ void flushTF(float *sTF, int seg, float acc[8])
+{
+  if (seg < 0)
+    return;
+  float *e = sTF + 4 * seg;
+#pragma unroll
+  for (int q = 0; q < 8; q++) {
+    if (acc[q] != 0.f)
+      atomicAdd(e + q, acc[q]);
+    acc[q] = 0.f;
+  }
+}
+
 template <typename T>
 __global__ void __launch_bounds__(256) k_dmBackward(const DMVol *vols,
     const DMViewG *views,
@@ -283,6 +318,13 @@ __global__ void __launch_bounds__(256) k_dmBackward(const DMVol *vols,
     const int px = (int)(tile % vw.tilesX) * tileW + (int)threadIdx.x % tileW;
     const int py = (int)(tile / vw.tilesX) * tileH + (int)threadIdx.x / tileW;
     float gScale = 0.f;
+    const bool plain = (v.flags & VRTX_DM_PLAIN) != 0;
+    // run-length gradient caches (one trilinear cell, one TF segment)
+    Tri cell;
+    cell.base = ~size_t(0);
+    float dacc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    int tfSeg = -1;
+    float tacc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
     if (px < vw.w && py < vw.h) {
       const size_t pix = (size_t)vw.pixOff + (size_t)py * vw.w + px;
       const int K = __float_as_int(state[2 * pix + 1]);
@@ -320,17 +362,32 @@ __global__ void __launch_bounds__(256) k_dmBackward(const DMVol *vols,
               araw < kAlphaMax ? dSigma * (-v.ratio / (1.f - alpha)) : 0.f;
           const float dA = dAlpha * v.scale;
           gScale += dAlpha * cl.c.w;
+          const float f0 = 1.f - cl.f, f1 = cl.f;
           if (v.gTF) {
-            const float f0 = 1.f - cl.f, f1 = cl.f;
-            float *e0 = sTF + 4 * cl.i0;
-            atomicAdd(e0 + 0, f0 * dc.x);
-            atomicAdd(e0 + 1, f0 * dc.y);
-            atomicAdd(e0 + 2, f0 * dc.z);
-            atomicAdd(e0 + 3, f0 * dA);
-            atomicAdd(e0 + 4, f1 * dc.x);
-            atomicAdd(e0 + 5, f1 * dc.y);
-            atomicAdd(e0 + 6, f1 * dc.z);
-            atomicAdd(e0 + 7, f1 * dA);
+            if (plain) {
+              float *e0 = sTF + 4 * cl.i0;
+              atomicAdd(e0 + 0, f0 * dc.x);
+              atomicAdd(e0 + 1, f0 * dc.y);
+              atomicAdd(e0 + 2, f0 * dc.z);
+              atomicAdd(e0 + 3, f0 * dA);
+              atomicAdd(e0 + 4, f1 * dc.x);
+              atomicAdd(e0 + 5, f1 * dc.y);
+              atomicAdd(e0 + 6, f1 * dc.z);
+              atomicAdd(e0 + 7, f1 * dA);
+            } else {
+              if (cl.i0 != tfSeg) {
+                flushTF(sTF, tfSeg, tacc);
+                tfSeg = cl.i0;
+              }
+              tacc[0] += f0 * dc.x;
+              tacc[1] += f0 * dc.y;
+              tacc[2] += f0 * dc.z;
+              tacc[3] += f0 * dA;
+              tacc[4] += f1 * dc.x;
+              tacc[5] += f1 * dc.y;
+              tacc[6] += f1 * dc.z;
+              tacc[7] += f1 * dA;
+            }
           }
           if (v.gD && cl.dxds != 0.f) {
             const float4 ea = __ldg(v.tf + cl.i0), eb = __ldg(v.tf + cl.i0 + 1);
@@ -339,19 +396,45 @@ __global__ void __launch_bounds__(256) k_dmBackward(const DMVol *vols,
             const float ds = dval * cl.dxds;
             if (ds != 0.f) {
               const float gx0 = 1.f - tr.fx, gy0 = 1.f - tr.fy, gz0 = 1.f - tr.fz;
-              float *G = v.gD + tr.base;
-              atomicAdd(G, ds * gx0 * gy0 * gz0);
-              atomicAdd(G + tr.sx, ds * tr.fx * gy0 * gz0);
-              atomicAdd(G + tr.sy, ds * gx0 * tr.fy * gz0);
-              atomicAdd(G + tr.sy + tr.sx, ds * tr.fx * tr.fy * gz0);
-              atomicAdd(G + tr.sz, ds * gx0 * gy0 * tr.fz);
-              atomicAdd(G + tr.sz + tr.sx, ds * tr.fx * gy0 * tr.fz);
-              atomicAdd(G + tr.sz + tr.sy, ds * gx0 * tr.fy * tr.fz);
-              atomicAdd(G + tr.sz + tr.sy + tr.sx, ds * tr.fx * tr.fy * tr.fz);
+              const float wt[8] = {gx0 * gy0 * gz0,
+                  tr.fx * gy0 * gz0,
+                  gx0 * tr.fy * gz0,
+                  tr.fx * tr.fy * gz0,
+                  gx0 * gy0 * tr.fz,
+                  tr.fx * gy0 * tr.fz,
+                  gx0 * tr.fy * tr.fz,
+                  tr.fx * tr.fy * tr.fz};
+              if (plain) {
+                float *G = v.gD + tr.base;
+                atomicAdd(G, ds * wt[0]);
+                atomicAdd(G + tr.sx, ds * wt[1]);
+                atomicAdd(G + tr.sy, ds * wt[2]);
+                atomicAdd(G + tr.sy + tr.sx, ds * wt[3]);
+                atomicAdd(G + tr.sz, ds * wt[4]);
+                atomicAdd(G + tr.sz + tr.sx, ds * wt[5]);
+                atomicAdd(G + tr.sz + tr.sy, ds * wt[6]);
+                atomicAdd(G + tr.sz + tr.sy + tr.sx, ds * wt[7]);
+              } else {
+                // consecutive samples mostly stay in one trilinear cell:
+                // accumulate there and commit when the ray leaves it
+                if (tr.base != cell.base) {
+                  flushCell(v.gD, cell, dacc);
+                  cell = tr;
+                }
+#pragma unroll
+                for (int q = 0; q < 8; q++)
+                  dacc[q] += ds * wt[q];
+              }
             }
           }
         }
       }
+    }
+    if (!plain) {
+      if (v.gTF)
+        flushTF(sTF, tfSeg, tacc);
+      if (v.gD)
+        flushCell(v.gD, cell, dacc);
     }
     // opacity-scale gradient: block reduction, one atomic per tile
     for (int o = 16; o > 0; o >>= 1)
@@ -441,6 +524,7 @@ int layout(const VRTXDMVolume *volumes,
     o.gTF = v.gradTf;
     o.gS = v.gradOpacityScale;
     o.scalePtr = v.opacityScaleDevice;
+    o.flags = v.flags;
   }
   std::vector<DMViewG> hw(numViews);
   unsigned items = 0;

@@ -96,6 +96,8 @@ class VolumeInput:
     step: float = 0.5
     unit: float = 1.0
     value_range: tuple = (0.0, 1.0)
+    # one atomic per gradient term (no per-thread run-length accumulation)
+    plain: bool = False
 
     @property
     def dims(self):
@@ -137,6 +139,7 @@ class Batch:
             o.step = v.step
             o.unitDistance = v.unit
             o.valueLo, o.valueHi = v.value_range
+            o.flags = L.DM_PLAIN if v.plain else 0
             if grads is not None:
                 gd, gt, gs = grads[i]
                 o.gradDensity = gd.data_ptr() if gd is not None else None
