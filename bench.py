@@ -138,6 +138,14 @@ def profile_traffic(name: str):
         return json.load(f).get("dram_bytes_per_launch")
 
 
+def trace_bytes(st: dict) -> float:
+    """Demand bytes of the AO any-hit kernel: per ray its 32-byte queue
+    record read and a 4-byte weighted result written, then the same
+    per-node / per-primitive / per-BLAS-entry bytes as algorithmic_bytes."""
+    return (st["rays"] * 36.0 + st["nodes"] * 80.0 + st["tri_tests"] * 36.0
+            + st["sphere_tests"] * 16.0 + st["blas_entries"] * 48.0)
+
+
 def algorithmic_bytes(st: dict) -> float:
     """Demand bytes of one frame: per ray a 32-byte ray + 20 bytes of output,
     80 bytes per BVH8 node visited, 36 per triangle tested (3 vertices), 16
@@ -248,7 +256,7 @@ def main():
         frame.render()
         frame.wait()
         return frame.get_property("duration", 240), frame.stats(), frame.kernel_ms(), \
-            frame.kernel_launches()
+            frame.kernel_launches(), frame.ao_trace()["ms"]
 
     for _ in range(args.warmup):
         one_frame()
@@ -262,12 +270,13 @@ def main():
         torch.distributed.barrier()
     torch.cuda.synchronize()
     clocks.start()
-    durs, rays, kms, launches = [], 0, [], 0
+    durs, rays, kms, tms, launches = [], 0, [], [], 0
     for _ in range(args.steps):
-        d, st, km, nl = one_frame()
+        d, st, km, nl, tm = one_frame()
         durs.append(d)
         rays += st["rays"]
         kms.append(km)
+        tms.append(tm)
         launches += nl
         assert st["error_flags"] == 0, st
     torch.cuda.synchronize()
@@ -289,21 +298,31 @@ def main():
     frame.render()
     frame.wait()
     cst = frame.stats()
+    tst = frame.ao_trace()
     frame.set("vrtx.countTraversal", False)
     frame.commit()
 
-    # roofline of the dominant kernel (the AO integrator)
+    # roofline of the dominant kernel, the AO any-hit kernel (one launch per
+    # sample over the compacted AO ray queue), timed with CUDA events around
+    # each of its launches on the library stream
     peaks = measured_peaks()
     k_ms = statistics.mean(kms)
-    bytes_frame = algorithmic_bytes(cst) * (rays / args.steps) / max(cst["rays"], 1)
-    achieved = bytes_frame / (k_ms / 1e3) / 1e9
+    trace_launch_ms = statistics.mean(tms) / args.spp
+    trace_launch_bytes = trace_bytes(tst) / args.spp
+    achieved = trace_launch_bytes / (trace_launch_ms / 1e3) / 1e9
     traffic = profile_traffic("k_aoTrace_" + WORKLOAD)
-    roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peaks["hbm_gbs"],
-                "unit": "GB/s", "frac": round(achieved / peaks["hbm_gbs"], 4),
+    frame_bytes = algorithmic_bytes(cst) * (rays / args.steps) / max(cst["rays"], 1)
+    roofline = {"bound": "hbm", "kernel": "k_aoTrace", "achieved": round(achieved, 1),
+                "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                "frac": round(achieved / peaks["hbm_gbs"], 4),
                 "traffic": traffic, "peak_source": peaks["source"],
-                "algorithmic_bytes_per_launch": bytes_frame,
-                "per_frame": {k: cst[k] for k in ("rays", "nodes", "tri_tests", "sphere_tests",
-                                                  "blas_entries")}}
+                "algorithmic_bytes_per_launch": trace_launch_bytes,
+                "launch_ms": round(trace_launch_ms, 4),
+                "share_of_frame_kernel_time": round(statistics.mean(tms) / k_ms, 4),
+                "per_launch": {k: tst[k] / args.spp for k in ("rays", "nodes", "tri_tests",
+                                                              "sphere_tests", "blas_entries")},
+                "frame": {"achieved": round(frame_bytes / (k_ms / 1e3) / 1e9, 1),
+                          "algorithmic_bytes": frame_bytes, "kernel_ms": round(k_ms, 3)}}
 
     # end to end through the C ABI with host buffers
     e2e_vals, h2d, d2h = [], 0, 0

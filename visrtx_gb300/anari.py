@@ -349,6 +349,18 @@ class Frame(Object):
     def kernel_launches(self) -> int:
         return int(self.device.lib.vrtxFrameKernelLaunches(self.device.h, self.handle))
 
+    def ao_trace(self) -> dict:
+        """The wavefront AO any-hit kernel alone in the last render: its
+        counters and the summed device time of its launches (ms)."""
+        buf = (C.c_uint64 * 5)()
+        ok = self.device.lib.vrtxGetProperty(self.device.h, self.handle, b"vrtx.aoTraceStats",
+                                             L.UINT64, buf, 40, L.WAIT)
+        ms = self.get_property("vrtx.aoTraceMilliseconds", L.FLOAT32)
+        keys = ("rays", "nodes", "tri_tests", "sphere_tests", "blas_entries")
+        out = dict(zip(keys, (int(v) for v in buf))) if ok else {}
+        out["ms"] = float(ms or 0.0)
+        return out
+
 
 def rgba8(color: np.ndarray) -> np.ndarray:
     """Unpacks UFIXED8 RGBA pixels (uint32, R in the low byte) to (..., 4) uint8."""

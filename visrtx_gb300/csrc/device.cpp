@@ -1621,6 +1621,8 @@ Frame::~Frame()
     for (cudaEvent_t e : {evStart, evEnd, evKStart, evKEnd})
       if (e)
         cudaEventDestroy(e);
+    for (cudaEvent_t e : traceEvents)
+      cudaEventDestroy(e);
     if (workCounter)
       cudaFree(workCounter);
     if (errorFlag)
@@ -1711,8 +1713,8 @@ void Frame::commit()
     cudaMemset(errorFlag, 0, 16);
   }
   if (!stats) {
-    cudaMalloc(&stats, 8 * sizeof(unsigned long long));
-    cudaMemset(stats, 0, 8 * sizeof(unsigned long long));
+    cudaMalloc(&stats, 16 * sizeof(unsigned long long));
+    cudaMemset(stats, 0, 16 * sizeof(unsigned long long));
   }
   countTraversal = get<int32_t>("vrtx.countTraversal", VRTX_BOOL, 0) != 0;
   forceMegakernel = get<int32_t>("vrtx.megakernel", VRTX_BOOL, 0) != 0;
@@ -1803,7 +1805,7 @@ void Frame::render()
   P.numTilesY = (P.launchH + 3) / 4;
   P.stats = stats;
   cudaMemsetAsync(workCounter, 0, 4, s);
-  cudaMemsetAsync(stats, 0, 8 * sizeof(unsigned long long), s);
+  cudaMemsetAsync(stats, 0, 16 * sizeof(unsigned long long), s);
   // The "ao" renderer over opaque surfaces (no volumes) runs as a
   // wavefront (primary / any-hit / resolve kernels per sample); everything
   // else runs the per-pixel integrator kernel.
@@ -1822,10 +1824,21 @@ void Frame::render()
       if (err == cudaSuccess)
         scratchBytes = need;
     }
+    const int n = std::max(P.renderer.numIterations, 1);
+    while ((int)traceEvents.size() < 2 * n) {
+      cudaEvent_t e = nullptr;
+      if (cudaEventCreate(&e) != cudaSuccess)
+        break;
+      traceEvents.push_back(e);
+    }
+    const bool timed = (int)traceEvents.size() >= 2 * n;
+    tracePairs = timed ? n : 0;
     if (err == cudaSuccess)
-      err = launchAOWavefront(P, d->numSMs, countTraversal, scratch, s);
+      err = launchAOWavefront(P, d->numSMs, countTraversal, scratch, s,
+          timed ? traceEvents.data() : nullptr);
     launches += 3 * std::max(P.renderer.numIterations, 1);
   } else {
+    tracePairs = 0;
     const int blocks =
         d->numSMs * renderOccupancyBlocks(P.renderer.type, countTraversal);
     err = launchRender(P, blocks, countTraversal, s);
@@ -1949,6 +1962,28 @@ bool Frame::getProperty(
     cudaMemcpy(&flags, errorFlag, 4, cudaMemcpyDeviceToHost);
     v[7] = flags;
     std::memcpy(mem, v, sizeof(v));
+    return true;
+  }
+  // libvrtx extension: the AO any-hit kernel alone (wavefront path): its
+  // counters [rays, nodes, tri tests, sphere tests, BLAS entries] and the
+  // summed device time of its launches in the last render (ms, 0 when the
+  // frame ran the per-pixel kernel).
+  if (name == "vrtx.aoTraceStats" && t == VRTX_UINT64 && size >= 40 && stats) {
+    wait();
+    unsigned long long v[5] = {};
+    cudaMemcpy(v, stats + 8, sizeof(v), cudaMemcpyDeviceToHost);
+    std::memcpy(mem, v, sizeof(v));
+    return true;
+  }
+  if (name == "vrtx.aoTraceMilliseconds" && t == VRTX_FLOAT32 && size >= 4) {
+    wait();
+    float total = 0.f;
+    for (int i = 0; i < tracePairs; i++) {
+      float ms = 0.f;
+      if (cudaEventElapsedTime(&ms, traceEvents[2 * i], traceEvents[2 * i + 1]) == cudaSuccess)
+        total += ms;
+    }
+    std::memcpy(mem, &total, 4);
     return true;
   }
   if (name == "nextFrameReset" && t == VRTX_BOOL && size >= 4) {

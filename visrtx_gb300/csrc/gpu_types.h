@@ -272,7 +272,8 @@ struct FrameParams
   uint32_t *errorFlag; // bit 0: traversal stack overflow
   unsigned long long *stats; // [0] rays, [1] nodes, [2] tri tests,
                              // [3] sphere tests, [4] BLAS entries,
-                             // [5] volume samples, [6] volume fetches
+                             // [5] volume samples, [6] volume fetches;
+                             // [8..12] = [0..4] of the AO any-hit kernel
   uint32_t numTilesX, numTilesY;
   uint32_t launchW, launchH; // checkerboarding halves these
 };

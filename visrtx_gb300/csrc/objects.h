@@ -345,6 +345,8 @@ struct Frame : Object
   uint64_t lastSeenStamp = 0;
   cudaEvent_t evStart = nullptr, evEnd = nullptr, evKStart = nullptr,
               evKEnd = nullptr;
+  std::vector<cudaEvent_t> traceEvents; // around each AO any-hit launch
+  int tracePairs = 0; // pairs recorded by the last render
   bool rendered = false;
   int launches = 0;
   std::vector<uint8_t> hostColor, hostDepth, hostPrim, hostObj, hostInst,

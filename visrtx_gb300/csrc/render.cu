@@ -961,9 +961,12 @@ __global__ void __launch_bounds__(128, VRTX_TRACE_MIN_BLOCKS) k_aoTrace(const Fr
     }
     weighted[i] = out;
   }
+  // the frame totals, and the same counts for this kernel alone ([8..12])
   const unsigned long long rs = warpSum(st.rays);
-  if ((threadIdx.x & 31) == 0)
+  if ((threadIdx.x & 31) == 0) {
     atomicAdd(P.stats + 0, rs);
+    atomicAdd(P.stats + 8, rs);
+  }
   if (STATS) {
     const unsigned long long nn = warpSum(st.nodes), t = warpSum(st.tris),
                              sp = warpSum(st.spheres), in = warpSum(st.instances);
@@ -972,6 +975,10 @@ __global__ void __launch_bounds__(128, VRTX_TRACE_MIN_BLOCKS) k_aoTrace(const Fr
       atomicAdd(P.stats + 2, t);
       atomicAdd(P.stats + 3, sp);
       atomicAdd(P.stats + 4, in);
+      atomicAdd(P.stats + 9, nn);
+      atomicAdd(P.stats + 10, t);
+      atomicAdd(P.stats + 11, sp);
+      atomicAdd(P.stats + 12, in);
     }
   }
 }
@@ -1067,7 +1074,8 @@ cudaError_t launchAOWavefront(const FrameParams &P,
     int numSMs,
     bool stats,
     void *scratch,
-    cudaStream_t s)
+    cudaStream_t s,
+    cudaEvent_t *traceEvents)
 {
   const size_t px = (size_t)P.fb.w * P.fb.h;
   const size_t nr = px * (size_t)max(P.renderer.aoSamples, 0);
@@ -1091,13 +1099,18 @@ cudaError_t launchAOWavefront(const FrameParams &P,
   const int n = max(P.renderer.numIterations, 1);
   for (int i = 0; i < n; i++) {
     cudaMemsetAsync(rayCount, 0, 4, s);
-    if (stats) {
+    if (stats)
       k_aoPrimary<true><<<grid, 128, 0, s>>>(P, i, consumed, pixels, rays, rayCount);
-      k_aoTrace<true><<<traceGrid, 128, 0, s>>>(P, rays, rayCount, weighted);
-    } else {
+    else
       k_aoPrimary<false><<<grid, 128, 0, s>>>(P, i, consumed, pixels, rays, rayCount);
+    if (traceEvents)
+      cudaEventRecord(traceEvents[2 * i], s);
+    if (stats)
+      k_aoTrace<true><<<traceGrid, 128, 0, s>>>(P, rays, rayCount, weighted);
+    else
       k_aoTrace<false><<<traceGrid, 128, 0, s>>>(P, rays, rayCount, weighted);
-    }
+    if (traceEvents)
+      cudaEventRecord(traceEvents[2 * i + 1], s);
     k_aoResolve<<<grid, 128, 0, s>>>(P, i, n, pixels, weighted);
   }
   return cudaGetLastError();

@@ -15,12 +15,14 @@ cudaError_t launchClearFrame(const FramebufferGPU &fb, cudaStream_t s);
 // Wavefront "ao" renderer (opaque materials, no volumes): per sample a
 // primary kernel, an any-hit kernel over the compacted AO ray queue and a
 // resolve kernel. scratch: aoWavefrontBytes() bytes of device memory.
+// traceEvents (optional): 2 per sample, recorded around each any-hit launch.
 size_t aoWavefrontBytes(uint32_t w, uint32_t h, int aoSamples);
 cudaError_t launchAOWavefront(const FrameParams &P,
     int numSMs,
     bool stats,
     void *scratch,
-    cudaStream_t s);
+    cudaStream_t s,
+    cudaEvent_t *traceEvents);
 
 // scene preparation (scene.cu)
 cudaError_t launchTriangleBoxes(const GeometryGPU *geoms,
