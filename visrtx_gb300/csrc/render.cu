@@ -24,6 +24,15 @@
 #define VRTX_RENDER_MIN_BLOCKS 1
 #endif
 // The same for the any-hit queue kernel (8: <= 64 registers per thread).
+#ifndef VRTX_AO_REFILL
+#define VRTX_AO_REFILL 4
+#endif
+
+// traversal stack entries of the AO any-hit kernel kept in shared memory
+#ifndef VRTX_AO_SHARED_STACK
+#define VRTX_AO_SHARED_STACK 16
+#endif
+
 #ifndef VRTX_TRACE_MIN_BLOCKS
 #define VRTX_TRACE_MIN_BLOCKS 8
 #endif
@@ -931,46 +940,85 @@ __global__ void __launch_bounds__(128) k_aoPrimary(const FrameParams P,
   }
 }
 
+// Any-hit pass over the compacted AO ray queue. Persistent: every lane
+// holds one ray; a lane whose ray has ended takes the next one from the
+// queue (one atomic per warp, once at least VRTX_AO_REFILL lanes wait, or
+// when the warp has no live ray), so a warp keeps most lanes busy instead
+// of waiting for its slowest ray. Each ray's result depends on that ray
+// alone: the queue order in which lanes take rays does not change it.
 template <bool STATS>
 __global__ void __launch_bounds__(128, VRTX_TRACE_MIN_BLOCKS) k_aoTrace(const FrameParams P,
     const AORay *rays,
     const uint32_t *rayCount,
+    uint32_t *fetchCounter,
     float *weighted)
 {
   const uint32_t n = *rayCount;
+  const uint32_t lane = threadIdx.x & 31u;
   TravStats st{0u, 0u, 0u, 0u, 0u, 0u, 0u};
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n;
-       i += gridDim.x * blockDim.x) {
-    const AORay r = rays[i];
-    float out = 0.f;
-    if (r.orgTmax.w >= 0.f) {
-      Hit h;
-      float att;
-      traverse<1, STATS>(P.world,
-          mk3(r.orgTmax.x, r.orgTmax.y, r.orgTmax.z),
-          mk3(r.dirWeight.x, r.dirWeight.y, r.dirWeight.z),
-          0.f,
-          r.orgTmax.w,
-          false,
-          false,
-          h,
-          att,
+#if VRTX_AO_SHARED_STACK > 0
+  __shared__ uint2 shStack[VRTX_AO_SHARED_STACK * 128];
+  SplitStack<VRTX_TRAVERSAL_STACK, VRTX_AO_SHARED_STACK, 128> stack;
+  stack.sh = shStack + threadIdx.x;
+#else
+  LocalStack<VRTX_TRAVERSAL_STACK> stack;
+#endif
+  OccState s;
+  uint32_t idx = 0;
+  bool live = false, exhausted = false;
+  while (true) {
+    const uint32_t want = __ballot_sync(0xffffffffu, !live && !exhausted);
+    const uint32_t busy = __ballot_sync(0xffffffffu, live);
+    if (want && (__popc(want) >= VRTX_AO_REFILL || busy == 0u)) {
+      const uint32_t leader = __ffs(want) - 1;
+      uint32_t base = 0;
+      if (lane == leader)
+        base = atomicAdd(fetchCounter, (uint32_t)__popc(want));
+      base = __shfl_sync(0xffffffffu, base, leader);
+      if ((want >> lane) & 1u) {
+        idx = base + __popc(want & ((1u << lane) - 1u));
+        if (idx >= n) {
+          exhausted = true;
+        } else {
+          const float4 o = __ldg(&rays[idx].orgTmax);
+          if (o.w < 0.f) {
+            weighted[idx] = 0.f; // zero weight: not traced
+          } else {
+            const float4 d = __ldg(&rays[idx].dirWeight);
+            st.rays++;
+            live = occlusionBegin(
+                P.world, s, mk3(o.x, o.y, o.z), mk3(d.x, d.y, d.z), o.w);
+            if (!live)
+              weighted[idx] = 0.f;
+          }
+        }
+      }
+    }
+    if (__all_sync(0xffffffffu, exhausted))
+      break;
+    if (live) {
+      const int r = occlusionStep<STATS, VRTX_TRAVERSAL_STACK>(P.world,
+          s,
+          stack,
+          reinterpret_cast<const float4 *>(rays + idx),
           P.errorFlag,
           st);
-      out = r.dirWeight.w * att;
+      if (r != OCC_CONTINUE) {
+        weighted[idx] = r == OCC_HIT ? __ldg(&rays[idx].dirWeight.w) : 0.f;
+        live = false;
+      }
     }
-    weighted[i] = out;
   }
   // the frame totals, and the same counts for this kernel alone ([8..12])
   const unsigned long long rs = warpSum(st.rays);
-  if ((threadIdx.x & 31) == 0) {
+  if (lane == 0) {
     atomicAdd(P.stats + 0, rs);
     atomicAdd(P.stats + 8, rs);
   }
   if (STATS) {
     const unsigned long long nn = warpSum(st.nodes), t = warpSum(st.tris),
                              sp = warpSum(st.spheres), in = warpSum(st.instances);
-    if ((threadIdx.x & 31) == 0) {
+    if (lane == 0) {
       atomicAdd(P.stats + 1, nn);
       atomicAdd(P.stats + 2, t);
       atomicAdd(P.stats + 3, sp);
@@ -1098,7 +1146,7 @@ cudaError_t launchAOWavefront(const FrameParams &P,
   const int traceGrid = numSMs * (occ > 0 ? occ : 1);
   const int n = max(P.renderer.numIterations, 1);
   for (int i = 0; i < n; i++) {
-    cudaMemsetAsync(rayCount, 0, 4, s);
+    cudaMemsetAsync(rayCount, 0, 8, s); // queue length, fetch counter
     if (stats)
       k_aoPrimary<true><<<grid, 128, 0, s>>>(P, i, consumed, pixels, rays, rayCount);
     else
@@ -1106,9 +1154,9 @@ cudaError_t launchAOWavefront(const FrameParams &P,
     if (traceEvents)
       cudaEventRecord(traceEvents[2 * i], s);
     if (stats)
-      k_aoTrace<true><<<traceGrid, 128, 0, s>>>(P, rays, rayCount, weighted);
+      k_aoTrace<true><<<traceGrid, 128, 0, s>>>(P, rays, rayCount, rayCount + 1, weighted);
     else
-      k_aoTrace<false><<<traceGrid, 128, 0, s>>>(P, rays, rayCount, weighted);
+      k_aoTrace<false><<<traceGrid, 128, 0, s>>>(P, rays, rayCount, rayCount + 1, weighted);
     if (traceEvents)
       cudaEventRecord(traceEvents[2 * i + 1], s);
     k_aoResolve<<<grid, 128, 0, s>>>(P, i, n, pixels, weighted);

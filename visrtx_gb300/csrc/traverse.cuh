@@ -84,21 +84,48 @@ __device__ __forceinline__ uint32_t byteOf(uint2 w, int i)
   return (word >> ((i & 3) * 8)) & 0xffu;
 }
 
-// 2^23 + b as a float, b = byte `i` of `w` (one byte permute)
-__device__ __forceinline__ float biasedByte(uint32_t w, uint32_t i)
+// 1 + b * 2^-15 as a float, b = byte `i` of `w` (one byte permute: b lands
+// in mantissa bits 8..15 under the exponent of 1.0)
+__device__ __forceinline__ float scaledByte(uint32_t w, uint32_t i)
 {
-  return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7650u | i));
+  return __uint_as_float(__byte_perm(w, 0x3F800000u, 0x7604u | (i << 4)));
+}
+
+// Three-input min / max (one instruction each on sm_100 and later; NaN
+// inputs are ignored like fminf / fmaxf ignore them).
+__device__ __forceinline__ float fmax3(float a, float b, float c)
+{
+  float d;
+  asm("max.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+  return d;
+}
+
+__device__ __forceinline__ float fmin3(float a, float b, float c)
+{
+  float d;
+  asm("min.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+  return d;
 }
 
 // Tests the 8 child boxes of a node. Returns internal-child hits in bits
 // 24..31 (ranked) and leaf-primitive hits in bits 0..23.
 //
+// Plane distances: with q a child's 8-bit plane, step = 2^e and the node
+// origin p, the plane's ray distance is (p + q step - org) invDir. Per axis
+// and node, S = 2^15 step invDir and O = (p - org) invDir - S; then
+// B = 1 + q 2^-15 comes out of one byte permute and the distance is the
+// single fma(B, S, O): B S = S + q step invDir exactly, so the only new
+// rounding is O's, at most |S| 2^-24 = |step invDir| / 512. Near planes use
+// O - |step invDir| / 32 and far planes O + |step invDir| / 32, which keeps
+// the test conservative with room to spare; the far distance also gets the
+// relative slack farScale (1e-6) for the roundings of O itself.
+//
 // Per ray octant the near/far plane words are swapped once per node, so a
-// child's entry distance is max(near planes) and its exit min(far planes);
-// bytes become floats with one permute and one subtract, and the hit masks
-// are built without branches: a leaf child contributes (meta >> 5) << offset
-// and an internal child (meta = 0b001'(24 + slot)) its rank bit 24 +
-// (slot ^ octant).
+// child's entry distance is max(near planes) and its exit min(far planes).
+// Hit masks are built without branches: the meta bytes of internal children
+// (0b001'(24 + slot)) get their slot XOR-ed with the octant once per node
+// (bytes whose bits 3 and 4 are both set), then every child contributes
+// (meta >> 5) << (meta & 31).
 __device__ __forceinline__ uint32_t intersectNode(const BVH8Node *nodes,
     uint32_t idx,
     const TravRay &r,
@@ -118,7 +145,12 @@ __device__ __forceinline__ uint32_t intersectNode(const BVH8Node *nodes,
   imask = eb >> 24;
   childBase = __float_as_uint(n1.x);
   primBase = __float_as_uint(n1.y);
-  const uint32_t meta[2] = {__float_as_uint(n1.z), __float_as_uint(n1.w)};
+  uint32_t meta[2] = {__float_as_uint(n1.z), __float_as_uint(n1.w)};
+#pragma unroll
+  for (int k = 0; k < 2; k++) {
+    const uint32_t internal = (meta[k] >> 3) & (meta[k] >> 4) & 0x01010101u;
+    meta[k] ^= internal * r.oct;
+  }
   // per axis: (lo word pair, hi word pair), swapped for a negative direction
   uint32_t nx[2], fx[2], ny[2], fy[2], nz[2], fz[2];
   {
@@ -142,15 +174,17 @@ __device__ __forceinline__ uint32_t intersectNode(const BVH8Node *nodes,
     fz[0] = sz ? lz0 : hz0;
     fz[1] = sz ? lz1 : hz1;
   }
-  const float bias = 8388608.f;
-  const float sx = __uint_as_float((eb & 0xffu) << 23) * r.invDir.x;
-  const float sy = __uint_as_float(((eb >> 8) & 0xffu) << 23) * r.invDir.y;
-  const float sz = __uint_as_float(((eb >> 16) & 0xffu) << 23) * r.invDir.z;
-  const float ox = (n0.x - r.org.x) * r.invDir.x;
-  const float oy = (n0.y - r.org.y) * r.invDir.y;
-  const float oz = (n0.z - r.org.z) * r.invDir.z;
-  // Outward slack on the far plane keeps the rounded slab test conservative
-  // (decoded planes carry a few roundings; 1e-6 relative covers them).
+  const float stx = __uint_as_float((eb & 0xffu) << 23) * r.invDir.x;
+  const float sty = __uint_as_float(((eb >> 8) & 0xffu) << 23) * r.invDir.y;
+  const float stz = __uint_as_float(((eb >> 16) & 0xffu) << 23) * r.invDir.z;
+  const float Sx = stx * 32768.f, Sy = sty * 32768.f, Sz = stz * 32768.f;
+  const float Ox = fmaf(n0.x - r.org.x, r.invDir.x, -Sx);
+  const float Oy = fmaf(n0.y - r.org.y, r.invDir.y, -Sy);
+  const float Oz = fmaf(n0.z - r.org.z, r.invDir.z, -Sz);
+  const float kSlack = 1.f / 32.f;
+  const float Onx = fmaf(-fabsf(stx), kSlack, Ox), Ofx = fmaf(fabsf(stx), kSlack, Ox);
+  const float Ony = fmaf(-fabsf(sty), kSlack, Oy), Ofy = fmaf(fabsf(sty), kSlack, Oy);
+  const float Onz = fmaf(-fabsf(stz), kSlack, Oz), Ofz = fmaf(fabsf(stz), kSlack, Oz);
   const float farScale = 1.000001f;
 
   uint32_t hits = 0;
@@ -158,18 +192,17 @@ __device__ __forceinline__ uint32_t intersectNode(const BVH8Node *nodes,
   for (int c = 0; c < 8; c++) {
     const int w = c >> 2;
     const uint32_t b = (uint32_t)(c & 3);
-    const float tx0 = fmaf(biasedByte(nx[w], b) - bias, sx, ox);
-    const float tx1 = fmaf(biasedByte(fx[w], b) - bias, sx, ox);
-    const float ty0 = fmaf(biasedByte(ny[w], b) - bias, sy, oy);
-    const float ty1 = fmaf(biasedByte(fy[w], b) - bias, sy, oy);
-    const float tz0 = fmaf(biasedByte(nz[w], b) - bias, sz, oz);
-    const float tz1 = fmaf(biasedByte(fz[w], b) - bias, sz, oz);
-    const float tn = fmaxf(fmaxf(tx0, ty0), fmaxf(tz0, tmin));
-    const float tf = fminf(fminf(tx1, ty1), fminf(tz1, tmax)) * farScale;
+    const float tx0 = fmaf(scaledByte(nx[w], b), Sx, Onx);
+    const float tx1 = fmaf(scaledByte(fx[w], b), Sx, Ofx);
+    const float ty0 = fmaf(scaledByte(ny[w], b), Sy, Ony);
+    const float ty1 = fmaf(scaledByte(fy[w], b), Sy, Ofy);
+    const float tz0 = fmaf(scaledByte(nz[w], b), Sz, Onz);
+    const float tz1 = fmaf(scaledByte(fz[w], b), Sz, Ofz);
+    const float tn = fmax3(tx0, ty0, fmaxf(tz0, tmin));
+    const float tf = fmin3(tx1, ty1, fminf(tz1, tmax)) * farScale;
     const uint32_t m = (meta[w] >> (8 * b)) & 0xffu;
-    const uint32_t lo5 = m & 31u;
-    const uint32_t sh = lo5 ^ ((lo5 >= 24u) ? r.oct : 0u);
-    hits |= (tn <= tf ? (m >> 5) : 0u) << sh;
+    if (tn <= tf)
+      hits |= __funnelshift_l(0u, m >> 5, m);
   }
   return hits;
 }
@@ -447,6 +480,216 @@ __device__ __forceinline__ bool traverse(const WorldGPU &w,
     }
   }
   return MODE == 0 ? found : false;
+}
+
+// ---------------------------------------------------------------------------
+// Resumable occlusion query over opaque geometry (the first primitive hit
+// ends the ray), for the wavefront AO kernel. Node order, primitive tests,
+// stack discipline, bounds and counters are those of traverse<1> on a world
+// whose surfaces are all opaque, so the answer (hit / no hit in [0, tmax))
+// and the TravStats counts are the same; the loop body is split out so that
+// a lane whose ray has ended can take a new ray while the rest of its warp
+// keeps traversing.
+// ---------------------------------------------------------------------------
+
+enum
+{
+  OCC_CONTINUE = 0,
+  OCC_HIT = 1,
+  OCC_MISS = 2
+};
+
+constexpr uint32_t OCC_TLAS = 0xffffffffu; // blasType while at instance level
+
+struct OccState
+{
+  TravRay r;
+  const BVH8Node *nodes;
+  const void *prims;
+  uint2 cur, tri;
+  float tmax;
+  int sp;
+  uint32_t blasType;
+  uint32_t guard;
+};
+
+// Traversal stack of one lane: plain per-thread (local memory) array.
+template <int N>
+struct LocalStack
+{
+  uint2 a[N];
+  __device__ __forceinline__ void put(int i, uint2 v)
+  {
+    a[i] = v;
+  }
+  __device__ __forceinline__ uint2 get(int i) const
+  {
+    return a[i];
+  }
+};
+
+// Traversal stack of one lane whose first S entries live in shared memory
+// (entry-major, one column per thread of a BLOCK-thread block, so lanes at
+// any depths hit distinct banks) and the rest in local memory.
+template <int N, int S, int BLOCK>
+struct SplitStack
+{
+  uint2 *sh; // &shared[threadIdx.x]; entry i at sh[i * BLOCK]
+  uint2 a[N - S];
+  __device__ __forceinline__ void put(int i, uint2 v)
+  {
+    if (i < S)
+      sh[i * BLOCK] = v;
+    else
+      a[i - S] = v;
+  }
+  __device__ __forceinline__ uint2 get(int i) const
+  {
+    return i < S ? sh[i * BLOCK] : a[i - S];
+  }
+};
+
+// Starts a query for world ray (org, dir) over [0, tmax); false when the
+// world has no instances (the query is then a miss).
+__device__ __forceinline__ bool occlusionBegin(
+    const WorldGPU &w, OccState &s, f3 org, f3 dir, float tmax)
+{
+  if (w.numInstances == 0)
+    return false;
+  setupRay(s.r, org, dir);
+  s.nodes = w.tlasNodes;
+  s.prims = nullptr;
+  s.cur = make_uint2(0u, 0x80000000u);
+  s.tri = make_uint2(0u, 0u);
+  s.tmax = tmax;
+  s.sp = 0;
+  s.blasType = OCC_TLAS;
+  s.guard = 0;
+  return true;
+}
+
+// One iteration of the traversal loop. `world` points at the ray's world
+// origin (xyz of [0]) and direction (xyz of [1]); they are re-read when the
+// ray enters or leaves an instance.
+template <bool STATS, int STACK, typename Stack>
+__device__ __forceinline__ int occlusionStep(const WorldGPU &w,
+    OccState &s,
+    Stack &stack,
+    const float4 *world,
+    uint32_t *errorFlag,
+    TravStats &st)
+{
+  if (s.guard++ > (1u << 22)) {
+    if (errorFlag)
+      atomicOr(errorFlag, 2u);
+    return OCC_MISS;
+  }
+  if (s.tri.y) {
+    if (s.blasType == OCC_TLAS) {
+      const uint32_t b = __ffs(s.tri.y) - 1;
+      s.tri.y &= s.tri.y - 1;
+      if (s.sp + 3 > STACK) {
+        if (errorFlag)
+          atomicOr(errorFlag, 1u);
+        s.tri.y = 0;
+        return OCC_CONTINUE;
+      }
+      if (s.cur.y & 0xff000000u)
+        stack.put(s.sp++, s.cur);
+      if (s.tri.y)
+        stack.put(s.sp++, s.tri);
+      stack.put(s.sp++, make_uint2(0u, 0u)); // marker
+      if (STATS)
+        st.instances++;
+      const InstanceRecord *inst = w.instances + (s.tri.x + b);
+      const BLASDesc blas = w.blas[inst->blas];
+      const float4 o = __ldg(world), d = __ldg(world + 1);
+      toObject(s.r, inst, mk3(o.x, o.y, o.z), mk3(d.x, d.y, d.z));
+      s.nodes = blas.nodes;
+      s.prims = blas.prims;
+      s.blasType = blas.type;
+      s.cur = make_uint2(0u, 0x80000000u);
+      s.tri.y = 0;
+      return OCC_CONTINUE;
+    }
+    while (s.tri.y) {
+      const uint32_t b = __ffs(s.tri.y) - 1;
+      s.tri.y &= s.tri.y - 1;
+      const uint32_t rec = s.tri.x + b;
+      float t;
+      bool hitPrim;
+      if (s.blasType == GEOM_TRIANGLE) {
+        const float4 *tp =
+            reinterpret_cast<const float4 *>(s.prims) + (size_t)rec * 3;
+        const float4 a = __ldg(tp + 0);
+        const float4 bb = __ldg(tp + 1);
+        const float4 cc = __ldg(tp + 2);
+        if (STATS)
+          st.tris++;
+        float u, v;
+        bool front;
+        hitPrim = intersectTriangle(s.r,
+            mk3(a.x, a.y, a.z),
+            mk3(bb.x, bb.y, bb.z),
+            mk3(cc.x, cc.y, cc.z),
+            0.f,
+            s.tmax,
+            t,
+            u,
+            v,
+            front);
+      } else {
+        const SphereRecord *sp4 =
+            reinterpret_cast<const SphereRecord *>(s.prims) + rec;
+        if (STATS)
+          st.spheres++;
+        hitPrim = intersectSphere(s.r, __ldg(&sp4->cr), 0.f, s.tmax, t);
+      }
+      if (hitPrim)
+        return OCC_HIT;
+    }
+    return OCC_CONTINUE;
+  }
+  if (s.cur.y & 0xff000000u) {
+    const uint32_t bit = __ffs(s.cur.y >> 24) - 1;
+    s.cur.y &= ~(1u << (24 + bit));
+    const uint32_t slot = bit ^ s.r.oct;
+    const uint32_t idx =
+        s.cur.x + __popc(s.cur.y & 0xffu & ((1u << slot) - 1u));
+    if (s.cur.y & 0xff000000u) {
+      if (s.sp < STACK)
+        stack.put(s.sp++, s.cur);
+      else if (errorFlag)
+        atomicOr(errorFlag, 1u);
+    }
+    uint32_t childBase, primBase, imask;
+    if (STATS)
+      st.nodes++;
+    const uint32_t hits = intersectNode(
+        s.nodes, idx, s.r, 0.f, s.tmax, childBase, primBase, imask);
+    s.cur = make_uint2(childBase, (hits & 0xff000000u) | imask);
+    s.tri = make_uint2(primBase, hits & 0x00ffffffu);
+    return OCC_CONTINUE;
+  }
+  if (s.sp == 0)
+    return OCC_MISS;
+  const uint2 e = stack.get(--s.sp);
+  if (e.y == 0u) {
+    // marker: back to the world ray
+    const float4 o = __ldg(world), d = __ldg(world + 1);
+    setupRay(s.r, mk3(o.x, o.y, o.z), mk3(d.x, d.y, d.z));
+    s.nodes = w.tlasNodes;
+    s.blasType = OCC_TLAS;
+    s.cur = make_uint2(0u, 0u);
+    return OCC_CONTINUE;
+  }
+  if (e.y & 0xff000000u)
+    s.cur = e;
+  else {
+    s.cur = make_uint2(0u, 0u);
+    s.tri = e;
+  }
+  return OCC_CONTINUE;
 }
 
 } // namespace vrtx
