@@ -916,6 +916,8 @@ struct Ctx
   int volMode;
   int texRound;
   uint64_t rays = 0;
+  // per volume: the reference's delta-tracking majorants (dpt only)
+  const std::vector<std::vector<float>> *dptMaj = nullptr;
 };
 
 float surfaceAttenuation(Ctx &C, V3 o, V3 d, float tmin, float tmax)
@@ -1155,6 +1157,231 @@ float volumeAttenuation(Ctx &C, const VolCtx &VC, Stream &rs, V3 o, V3 d, float 
   return a;
 }
 
+// ---------------------------------------------------------------------------
+// delta tracking for the dpt renderer
+// ---------------------------------------------------------------------------
+
+// float -> int32 the way the GPU converts: truncate, saturate, NaN -> 0
+int f2iSat(float x)
+{
+  if (std::isnan(x))
+    return 0;
+  if (x >= 2147483648.f)
+    return INT32_MAX;
+  if (x <= -2147483648.f)
+    return INT32_MIN;
+  return (int)x;
+}
+
+// projectOnGrid (gpu/uniformGrid.h:43-50), one axis
+int projectAxis(float v, float lo, float hi, int n)
+{
+  const float v01 = (v - lo) / (hi - lo);
+  return std::min(std::max(f2iSat(v01 * (float)n), 0), n - 1);
+}
+
+void volBounds(const OrcVolume &v, V3 &lo, V3 &hi)
+{
+  lo = ld3(v.origin, 0);
+  hi = lo
+      + v3((float)(v.dims[0] - 1) * v.spacing[0],
+          (float)(v.dims[1] - 1) * v.spacing[1],
+          (float)(v.dims[2] - 1) * v.spacing[2]);
+}
+
+// UniformGrid::init / buildGridGPU / computeMaxOpacitiesGPU
+// (scene/volume/space_skipping/UniformGrid.cu:44-258) as the reference
+// drives them (StructuredRegularField.cpp:205-212, TransferFunction1D.cpp:
+// 76-77): ceil(dims/16) cells over the field bounds; each cell's 8 taps sit
+// at the object-space points (id +- 0.5) / cellDims, go through the field
+// sampler, and their max is splatted (min/max) into every cell that the
+// cell's bounds project onto; the majorant is the max TF alpha over entries
+// [int(lo * 255), int(hi * 255) + 1] of the TF range [0, 1] (the default
+// argument), read at entry centres.
+void dptMajorants(const OrcVolume &v, int round, std::vector<float> &maj)
+{
+  const int md[3] = {(v.dims[0] + 15) / 16, (v.dims[1] + 15) / 16, (v.dims[2] + 15) / 16};
+  const size_t cells = (size_t)md[0] * md[1] * md[2];
+  std::vector<float> lo(cells, 1e30f), hi(cells, -1e30f);
+  V3 blo, bhi;
+  volBounds(v, blo, bhi);
+  const float ex = (bhi.x - blo.x) / (float)md[0];
+  const float ey = (bhi.y - blo.y) / (float)md[1];
+  const float ez = (bhi.z - blo.z) / (float)md[2];
+  for (int iz = 0; iz < md[2]; iz++)
+    for (int iy = 0; iy < md[1]; iy++)
+      for (int ix = 0; ix < md[0]; ix++) {
+        const float lx = blo.x + (float)ix * ex, ly = blo.y + (float)iy * ey,
+                    lz = blo.z + (float)iz * ez;
+        const float ux = lx + ex, uy = ly + ey, uz = lz + ez;
+        float value = -1e30f;
+        for (int k = 0; k < 8; k++) {
+          const float ox = (k == 1 || k == 2 || k == 5 || k == 6) ? 0.5f : -0.5f;
+          const float oy = (k == 2 || k == 3 || k == 6 || k == 7) ? 0.5f : -0.5f;
+          const float oz = k >= 4 ? 0.5f : -0.5f;
+          const V3 p = v3(((float)ix + ox) / (float)md[0], ((float)iy + oy) / (float)md[1],
+              ((float)iz + oz) / (float)md[2]);
+          value = std::fmax(value, sampleFieldParity(v, p, round));
+        }
+        const int x0 = projectAxis(lx, blo.x, bhi.x, md[0]);
+        const int x1 = projectAxis(ux, blo.x, bhi.x, md[0]);
+        const int y0 = projectAxis(ly, blo.y, bhi.y, md[1]);
+        const int y1 = projectAxis(uy, blo.y, bhi.y, md[1]);
+        const int z0 = projectAxis(lz, blo.z, bhi.z, md[2]);
+        const int z1 = projectAxis(uz, blo.z, bhi.z, md[2]);
+        for (int z = z0; z <= z1; z++)
+          for (int y = y0; y <= y1; y++)
+            for (int x = x0; x <= x1; x++) {
+              const size_t c = ((size_t)z * md[1] + y) * md[0] + x;
+              if (value < lo[c])
+                lo[c] = value;
+              if (value > hi[c])
+                hi[c] = value;
+            }
+      }
+  maj.assign(cells, 0.f);
+  for (size_t c = 0; c < cells; c++) {
+    if (hi[c] < lo[c])
+      continue;
+    if (!v.tf) {
+      maj[c] = v.uniformOpacity;
+      continue;
+    }
+    const int e0 = std::min(std::max(f2iSat(lo[c] * 255.f), 0), 255);
+    const int e1 = std::min(std::max((int)((uint32_t)f2iSat(hi[c] * 255.f) + 1u), 0), 255);
+    float m = 0.f;
+    for (int i = e0; i <= e1; i++) {
+      float co[4];
+      tex1dLinear(v.tf, 256, 4, ((float)i + 0.5f) / 256.f, round, co);
+      m = std::fmax(m, co[3]);
+    }
+    maj[c] = m;
+  }
+}
+
+// dda3 (gpu/dda.h:44-122): cell walk over `dims` cells spanning [blo, bhi];
+// the first-boundary distances are fused multiply-adds, as in the GPU code.
+template <typename F>
+void dda3(V3 org, V3 dir, float tlo, float thi, const int dims[3], V3 blo, V3 bhi, F func)
+{
+  const V3 rcp = v3(dir.x != 0.f ? 1.f / dir.x : 0.f, dir.y != 0.f ? 1.f / dir.y : 0.f,
+      dir.z != 0.f ? 1.f / dir.z : 0.f);
+  const V3 lo = (blo - org) * rcp;
+  const V3 hi = (bhi - org) * rcp;
+  const V3 tnear = v3(std::min(lo.x, hi.x), std::min(lo.y, hi.y), std::min(lo.z, hi.z));
+  const V3 tfar = v3(std::max(lo.x, hi.x), std::max(lo.y, hi.y), std::max(lo.z, hi.z));
+  int c[3] = {projectAxis(org.x, blo.x, bhi.x, dims[0]), projectAxis(org.y, blo.y, bhi.y, dims[1]),
+      projectAxis(org.z, blo.z, bhi.z, dims[2])};
+  const float dist[3] = {(tfar.x - tnear.x) / (float)dims[0],
+      (tfar.y - tnear.y) / (float)dims[1], (tfar.z - tnear.z) / (float)dims[2]};
+  const float dv[3] = {dir.x, dir.y, dir.z};
+  const float tn[3] = {tnear.x, tnear.y, tnear.z};
+  int step[3], stop[3];
+  float tnext[3];
+  for (int a = 0; a < 3; a++) {
+    step[a] = dv[a] > 0.f ? 1 : -1;
+    stop[a] = dv[a] > 0.f ? dims[a] : -1;
+    tnext[a] = std::fma((float)(dv[a] > 0.f ? c[a] + 1 : dims[a] - c[a]), dist[a], tn[a]);
+  }
+  float t0 = std::max(tlo, 0.f);
+  for (int guard = 0; guard < 4 * (dims[0] + dims[1] + dims[2]) + 8; guard++) {
+    const float tc = std::min(tnext[0], std::min(tnext[1], tnext[2]));
+    const float t1 = std::min(tc, thi);
+    const size_t cell = ((size_t)c[2] * dims[1] + c[1]) * dims[0] + c[0];
+    if (!func(cell, t0, t1))
+      return;
+    bool stopNow = false;
+    for (int a = 0; a < 3 && !stopNow; a++) {
+      if (tnext[a] == tc) {
+        tnext[a] += dist[a];
+        c[a] += step[a];
+        if (c[a] == stop[a])
+          stopNow = true;
+      }
+    }
+    if (stopNow)
+      break;
+    t0 = t1;
+  }
+}
+
+// _sampleDistance (volumeIntegration.h:167-238): Woodcock tracking per DDA
+// cell against the cell majorant, t -= log(1-u)/majorant*stepSize (a fused
+// multiply-add, as in the GPU code).
+float sampleDistance(Ctx &C, const OrcVolume &v, const std::vector<float> &maj,
+    const VolHit &h, Stream &rs, V3 &albedo, float &extinction, float &tr)
+{
+  const float stepSize = volStep(v);
+  float t_out = h.t1;
+  tr = 1.f;
+  const V3 org = v3(std::fma(h.ld.x, h.t0, h.lo.x), std::fma(h.ld.y, h.t0, h.lo.y),
+      std::fma(h.ld.z, h.t0, h.lo.z));
+  const int md[3] = {(v.dims[0] + 15) / 16, (v.dims[1] + 15) / 16, (v.dims[2] + 15) / 16};
+  V3 blo, bhi;
+  volBounds(v, blo, bhi);
+  dda3(org, h.ld, 0.f, h.t1 - h.t0, md, blo, bhi, [&](size_t cell, float t0, float t1) {
+    const float majorant = maj[cell];
+    float t = t0;
+    for (int guard = 0; guard < (1 << 20); guard++) {
+      if (majorant <= 0.f)
+        break;
+      const float lg = std::log(1.f - uniform(rs));
+      t = std::fma(-(lg / majorant), stepSize, t);
+      if (t >= t1)
+        break;
+      const float tt = t + h.t0;
+      const V3 p = v3(std::fma(h.ld.x, tt, h.lo.x), std::fma(h.ld.y, tt, h.lo.y),
+          std::fma(h.ld.z, tt, h.lo.z));
+      const float s = sampleFieldParity(v, p, C.texRound);
+      if (!std::isnan(s)) {
+        float co[4];
+        classifyParity(v, s, C.texRound, co);
+        albedo = v3(co[0], co[1], co[2]);
+        extinction = co[3];
+        const float u = uniform(rs);
+        if (extinction >= u * majorant) {
+          tr = 0.f;
+          t_out = t;
+          return false;
+        }
+      }
+    }
+    return true;
+  });
+  return t_out + h.t0;
+}
+
+// sampleDistanceAllVolumes (volumeIntegration.h:352-389)
+float sampleDistanceAllVolumes(Ctx &C, const VolCtx &VC, Stream &rs, V3 o, V3 d, float tmin,
+    float tfar, V3 &albedo, float &extinction, float &transmittance, uint32_t &objID,
+    uint32_t &instID)
+{
+  float depth = tfar;
+  transmittance = 1.f;
+  int last = -1;
+  for (int guard = 0; guard <= C.S->sc->numVolumes; guard++) {
+    VolHit h;
+    if (!intersectVolumes(C, VC, o, d, tmin, tfar, last, h))
+      break;
+    const OrcVolume &v = C.S->sc->volumes[h.entry];
+    h.t1 = std::min(tfar, h.t1);
+    V3 alb = v3(0, 0, 0);
+    float ext = 0.f, tr = 0.f;
+    const float dd = sampleDistance(C, v, (*C.dptMaj)[h.entry], h, rs, alb, ext, tr);
+    if (dd < depth) {
+      depth = dd;
+      albedo = alb;
+      extinction = ext;
+      transmittance = tr;
+      objID = v.id;
+      instID = v.instId;
+    }
+    tmin = h.t1 + 1e-3f;
+    last = h.entry;
+  }
+  return depth;
+}
+
 float matteOpacity(const OrcSurface &s)
 {
   return surfOpacity(s);
@@ -1371,28 +1598,67 @@ struct PathState
   V3 Lw;
 };
 
-Sample integrateDPT(Ctx &C, const CamPre &cam, Stream &rs, int px, int py, float invW,
-    float invH, PathState &pd)
+// computeOrthonormalBasis (gpu/gpu_util.h:210-222, Pixar ONB) applied to s
+V3 onbMul(V3 n, V3 s)
+{
+  const float sign = n.z >= 0.f ? 1.f : -1.f;
+  const float a = -1.f / (sign + n.z);
+  const float b = n.x * n.y * a;
+  const V3 u = v3(1.f + sign * n.x * n.x * a, sign * b, -sign * n.x);
+  const V3 w = v3(b, sign + n.y * n.y * a, -n.y);
+  return u * s.x + w * s.y + n * s.z;
+}
+
+// sampleUnitSphere (gpu/gpu_util.h:234-243)
+V3 sampleUnitSphere(Stream &rs, V3 n)
+{
+  const float cost = 1.f - 2.f * uniform(rs);
+  const float sint = std::sqrt(std::max(0.f, 1.f - cost * cost));
+  const float phi = 2.f * (float)M_PI * uniform(rs);
+  return onbMul(n, v3(sint * std::cos(phi), sint * std::sin(phi), -cost));
+}
+
+Sample integrateDPT(Ctx &C, const VolCtx &VC, const CamPre &cam, Stream &rs, int px, int py,
+    float invW, float invH, PathState &pd)
 {
   const OrcRenderer &R = *C.R;
   Ray ray = primaryRay(cam, rs, px, py, invW, invH, false);
   const V3 bg = v3(R.background[0], R.background[1], R.background[2]);
   Sample out{bg, 1.f, ray.tmax, ~0u, ~0u, ~0u};
+  const bool hasVolumes = C.S->sc->numVolumes > 0;
   while (true) {
     HitRec h;
     float unused;
     C.rays++;
     const bool found = trace<0>(*C.S, ray.org, ray.dir, ray.tmin, ray.tmax,
         R.cullTriangleBackfaces != 0, false, h, unused);
-    if (!found)
+    SHit sh{};
+    if (found)
+      sh = populate(*C.S, ray, h);
+    V3 volumeColor = v3(0, 0, 0);
+    float volumeOpacity = 0.f, Tr = 1.f;
+    uint32_t vObj = ~0u, vInst = ~0u;
+    const float tfar = found ? sh.t : ray.tmax;
+    const float volumeDepth = hasVolumes
+        ? sampleDistanceAllVolumes(C, VC, rs, ray.org, ray.dir, ray.tmin, tfar, volumeColor,
+              volumeOpacity, Tr, vObj, vInst)
+        : tfar;
+    const bool volumeHit = Tr < 1.f && (!found || volumeDepth < sh.t);
+    if (!found && !volumeHit)
       break;
-    const SHit sh = populate(*C.S, ray, h);
     if (pd.depth++ >= R.maxDepth) {
       pd.Lw = v3(0, 0, 0);
       break;
     }
-    const V3 pos = sh.P + (sh.eps * sh.Ng);
-    pd.Lw = pd.Lw * ld3(C.S->sc->surfaces[sh.surface].color, 0);
+    V3 pos, albedo;
+    if (!volumeHit) {
+      pos = sh.P + (sh.eps * sh.Ng);
+      albedo = ld3(C.S->sc->surfaces[sh.surface].color, 0);
+    } else {
+      pos = ray.org + volumeDepth * ray.dir;
+      albedo = volumeColor;
+    }
+    pd.Lw = pd.Lw * albedo;
     const float P = cmax(pd.Lw);
     if (P < .2f) {
       if (uniform(rs) > P) {
@@ -1401,8 +1667,13 @@ Sample integrateDPT(Ctx &C, const CamPre &cam, Stream &rs, int px, int py, float
       }
       pd.Lw = pd.Lw / P;
     }
-    const V3 sd = randomDir(rs, sh.Ns);
-    pd.Lw = pd.Lw * std::max(0.f, dot(sd, sh.Ng));
+    V3 sd;
+    if (!volumeHit) {
+      sd = randomDir(rs, sh.Ns);
+      pd.Lw = pd.Lw * std::max(0.f, dot(sd, sh.Ng));
+    } else {
+      sd = sampleUnitSphere(rs, -1.f * ray.dir);
+    }
     ray.org = pos;
     ray.dir = sd;
     ray.tmin = 0.f;
@@ -1451,6 +1722,13 @@ void orc_tex1d(const float *table, int n, int comps, float coord, int round, flo
 float orc_tex3d(const float *vox, const int dims[3], const float coord[3], int round)
 {
   return tex3dLinear(vox, dims, coord[0], coord[1], coord[2], round);
+}
+
+void orc_dpt_majorants(const OrcVolume *volume, int round, float *out)
+{
+  std::vector<float> m;
+  dptMajorants(*volume, round, m);
+  std::memcpy(out, m.data(), m.size() * sizeof(float));
 }
 
 // TransferFunction1D::discritizeTFData (TransferFunction1D.cpp:101-150) with
@@ -1595,6 +1873,10 @@ int orc_render_prepared(void *prepared, const OrcCamera *camera, const OrcRender
   const SceneCtx &S = ((OrcPrepared *)prepared)->S;
   const VolCtx &VC = ((OrcPrepared *)prepared)->VC;
   const CamPre cam = camSetup(*camera);
+  std::vector<std::vector<float>> dptMaj(S.sc->numVolumes);
+  if (renderer->type == 3)
+    for (int i = 0; i < S.sc->numVolumes; i++)
+      dptMajorants(S.sc->volumes[i], texRound, dptMaj[i]);
   OrcFrame &F = *frame;
   const int W = F.width, H = F.height;
   const float invW = 1.f / (float)W, invH = 1.f / (float)H;
@@ -1603,7 +1885,7 @@ int orc_render_prepared(void *prepared, const OrcCamera *camera, const OrcRender
   std::atomic<int> next{0};
   std::atomic<uint64_t> rays{0};
   auto worker = [&]() {
-    Ctx C{&S, renderer, volumeMode, texRound, 0};
+    Ctx C{&S, renderer, volumeMode, texRound, 0, &dptMaj};
     while (true) {
       const int t = next.fetch_add(1);
       if (t >= tilesX * tilesY)
@@ -1621,7 +1903,7 @@ int orc_render_prepared(void *prepared, const OrcCamera *camera, const OrcRender
           PathState pd{0, v3(1, 1, 1)};
           for (int i = 0; i < iters; i++) {
             const Sample s = renderer->type == 3
-                ? integrateDPT(C, cam, rs, x, y, invW, invH, pd)
+                ? integrateDPT(C, VC, cam, rs, x, y, invW, invH, pd)
                 : integrate(C, VC, cam, rs, x, y, invW, invH);
             float v[4] = {s.color.x, s.color.y, s.color.z, s.opacity};
             tonemap(v);

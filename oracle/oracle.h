@@ -99,6 +99,10 @@ typedef struct OrcVolume {
   float xfm[12];
 } OrcVolume;
 
+/* The reference's delta-tracking majorants of one volume (dpt renderer):
+ * ceil(dims/16) cells, x fastest (UniformGrid.cu). */
+void orc_dpt_majorants(const OrcVolume *volume, int round, float *out);
+
 typedef struct OrcScene {
   const OrcSurface *surfaces;
   int numSurfaces;

@@ -205,31 +205,47 @@ def _scene_structs(spec):
         lights[i].radiance = (C.c_float * 3)(*rad)
     vols = (OrcVolume * max(1, len(spec.volumes)))()
     for i, v in enumerate(spec.volumes):
-        f = np.ascontiguousarray(v.field, np.float32)
-        keep.append(f)
-        o = vols[i]
-        o.field = _ptr(f)
-        o.dims = (C.c_int * 3)(f.shape[2], f.shape[1], f.shape[0])
-        o.origin = (C.c_float * 3)(*map(float, v.origin))
-        o.spacing = (C.c_float * 3)(*map(float, v.spacing))
-        o.filterLinear = int(v.filter != "nearest")
-        if v.color is not None or v.opacity is not None:
-            tf = discretize_tf(v.color, v.opacity, v.value_range,
-                               v.uniform_opacity)
-            keep.append(tf)
-            o.tf = _ptr(tf)
-        o.valueRange = (C.c_float * 2)(*map(float, v.value_range))
-        o.unitDistance = v.unit_distance
-        o.uniformColor = (C.c_float * 3)(*map(float, v.uniform_color))
-        o.uniformOpacity = v.uniform_opacity
-        o.id = v.id & 0xFFFFFFFF
-        o.instId = spec.world_id & 0xFFFFFFFF
-        o.xfm = _rows(np.eye(4))
+        _pack_volume(v, vols[i], keep, spec.world_id)
     scene = OrcScene(C.cast(surfs, C.c_void_p), len(spec.surfaces), C.cast(inst_arr, C.c_void_p),
                      len(insts), C.cast(lights, C.c_void_p), len(spec.lights),
                      C.cast(vols, C.c_void_p), len(spec.volumes))
     keep += [surfs, inst_arr, lights, vols]
     return keep, scene
+
+
+def _pack_volume(v, o, keep, world_id):
+    f = np.ascontiguousarray(v.field, np.float32)
+    keep.append(f)
+    o.field = _ptr(f)
+    o.dims = (C.c_int * 3)(f.shape[2], f.shape[1], f.shape[0])
+    o.origin = (C.c_float * 3)(*map(float, v.origin))
+    o.spacing = (C.c_float * 3)(*map(float, v.spacing))
+    o.filterLinear = int(v.filter != "nearest")
+    if v.color is not None or v.opacity is not None:
+        tf = discretize_tf(v.color, v.opacity, v.value_range, v.uniform_opacity)
+        keep.append(tf)
+        o.tf = _ptr(tf)
+    o.valueRange = (C.c_float * 2)(*map(float, v.value_range))
+    o.unitDistance = v.unit_distance
+    o.uniformColor = (C.c_float * 3)(*map(float, v.uniform_color))
+    o.uniformOpacity = v.uniform_opacity
+    o.id = v.id & 0xFFFFFFFF
+    o.instId = world_id & 0xFFFFFFFF
+    o.xfm = _rows(np.eye(4))
+
+
+def dpt_majorants(vspec, tex_round: int = 1) -> np.ndarray:
+    """The reference's delta-tracking majorant grid of one volume (the dpt
+    renderer's Woodcock bound), shape (ceil(nz/16), ceil(ny/16), ceil(nx/16))."""
+    lib = load()
+    keep = []
+    o = OrcVolume()
+    _pack_volume(vspec, o, keep, 0)
+    nz, ny, nx = np.asarray(vspec.field).shape
+    md = ((nz + 15) // 16, (ny + 15) // 16, (nx + 15) // 16)
+    out = np.zeros(md, np.float32)
+    lib.orc_dpt_majorants(C.byref(o), C.c_int(tex_round), _ptr(out))
+    return out
 
 
 def _render_prepared(lib, handle, spec, frame_id, rows, volume_mode, tex_round, threads, accum,

@@ -200,3 +200,67 @@ def test_dm_adjoint_matches_central_differences():
         assert abs(fd - gT[i, c]) <= 1e-4 * max(abs(fd), 1e-3), (i, c, fd, gT[i, c])
     fd = (loss(d, tf, scale + h) - loss(d, tf, scale - h)) / (2 * h)
     assert abs(fd - gS) <= 1e-4 * max(abs(fd), 1e-3)
+
+
+def _tf_volume(field, value_range=(0.0, 1.0)):
+    color = np.array([[1, 0, 0], [0, 1, 0], [0, 0, 1]], np.float32)
+    opacity = np.linspace(0.05, 0.95, 7).astype(np.float32)
+    return S.VolumeSpec(field=field, color=color, opacity=opacity, value_range=value_range)
+
+
+def test_dpt_majorants_constant_field():
+    """Delta-tracking grid (UniformGrid.cu): a constant field c gives every
+    cell the range [c, c] and the majorant max(tf[int(255 c)].a,
+    tf[int(255 c) + 1].a); ceil(dims/16) cells per axis."""
+    field = np.full((20, 33, 40), 0.5, np.float32)
+    vol = _tf_volume(field)
+    m = O.dpt_majorants(vol)
+    assert m.shape == (2, 3, 3)
+    tf = O.discretize_tf(vol.color, vol.opacity, vol.value_range)
+    want = max(tf[127, 3], tf[128, 3])
+    np.testing.assert_array_equal(m, np.full(m.shape, want, np.float32))
+
+
+def test_dpt_majorants_follow_the_first_voxels():
+    """The reference feeds the taps (cell id +- 0.5) / cellDims to the field
+    sampler as object-space points, so every cell's range comes from the
+    field near voxel (0..1, 0..1, 0..1): a field that is 0 there and 1 elsewhere
+    yields the majorant of TF entries 0..1 in every cell (not a bound on the
+    cell's own values)."""
+    field = np.ones((48, 48, 48), np.float32)
+    field[:3, :3, :3] = 0.0
+    vol = _tf_volume(field)
+    m = O.dpt_majorants(vol)
+    tf = O.discretize_tf(vol.color, vol.opacity, vol.value_range)
+    np.testing.assert_array_equal(m, np.full(m.shape, max(tf[0, 3], tf[1, 3]), np.float32))
+
+
+def test_dpt_volume_renders_on_cpu():
+    """dpt over a volume-only scene: with majorant > 0 some paths scatter in
+    the medium (depth > 0 there), others escape to the background."""
+    # a thin medium (TF alpha ~0.05, about one collision per 9 voxels) so
+    # that most paths end before the depth limit. The view direction is not
+    # axis-aligned: the reference's cell walk (dda.h) gives a ray with a zero
+    # direction component an empty first cell and stops, so such rays never
+    # collide (kept here as it is).
+    field = np.zeros((24, 24, 24), np.float32)
+    vol = _tf_volume(field)
+    cam = S.CameraSpec(type="orthographic", position=(11.5, 11.5, -10.0),
+                       direction=(0.05, 0.03, 1.0), height=30.0, aspect=1.0)
+    spec = S.SceneSpec([], [S.InstanceSpec([], zero=True)], [], [vol], camera=cam,
+                       renderer=S.RendererSpec("dpt", pixel_samples=1, background=(0, 0, 0, 1),
+                                               ambient_radiance=1.0),
+                       width=16, height=16)
+    out = O.render(spec)
+    c = out["accum"][..., :3]
+    assert np.all(np.isfinite(c))
+    inside = c[4:12, 4:12].mean()
+    outside = c[0, 0].mean()
+    assert outside == 0.0 and inside > 0.0
+    assert out["rays"] > 16 * 16  # scattered paths continue
+
+    # an axis-aligned view sees no medium at all (see above)
+    spec.camera = S.CameraSpec(type="orthographic", position=(11.5, 11.5, -10.0),
+                               direction=(0, 0, 1), height=30.0, aspect=1.0)
+    out = O.render(spec)
+    assert out["rays"] == 16 * 16 and out["accum"][..., :3].max() == 0.0

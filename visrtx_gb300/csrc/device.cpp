@@ -816,9 +816,12 @@ void SpatialField::cleanup()
     cudaFreeArray(cuArray);
   if (ranges)
     cudaFree(ranges);
+  if (refRanges)
+    cudaFree(refRanges);
   tex = pointTex = 0;
   cuArray = nullptr;
   ranges = nullptr;
+  refRanges = nullptr;
   builtStamp = 0;
 }
 
@@ -931,6 +934,16 @@ bool SpatialField::ensureBuilt()
     return false;
   }
   launchMacrocellRanges(pointTex, dims, mcDims, ranges, s);
+  if (cudaMalloc(&refRanges, 2 * cells * sizeof(float)) != cudaSuccess) {
+    cudaGetLastError();
+    refRanges = nullptr;
+    return false;
+  }
+  const f3 invSpacing{1.f / (spacing.x * float(dims[0])),
+      1.f / (spacing.y * float(dims[1])),
+      1.f / (spacing.z * float(dims[2]))};
+  launchReferenceGridRanges(
+      tex, origin, spacing, invSpacing, bounds(), mcDims, refRanges, s);
   builtStamp = want;
   return cudaGetLastError() == cudaSuccess;
 }
@@ -955,10 +968,13 @@ void Volume::cleanup()
     cudaFree(tfDev);
   if (majorants)
     cudaFree(majorants);
+  if (dptMajorants)
+    cudaFree(dptMajorants);
   tfTex = 0;
   tfArray = nullptr;
   tfDev = nullptr;
   majorants = nullptr;
+  dptMajorants = nullptr;
   builtStamp = 0;
 }
 
@@ -1161,6 +1177,13 @@ bool Volume::ensureBuilt()
       uniformOpacity,
       majorants,
       s);
+  if (cudaMalloc(&dptMajorants, cells * sizeof(float)) != cudaSuccess) {
+    cudaGetLastError();
+    dptMajorants = nullptr;
+    return false;
+  }
+  launchReferenceMajorants(
+      field->refRanges, field->mcDims, tfTex, 256, uniformOpacity, dptMajorants, s);
   builtStamp = want;
   return cudaGetLastError() == cudaSuccess;
 }
@@ -1476,6 +1499,7 @@ bool World::rebuild()
         vg.instId = inst->userID(t);
         vg.worldToObject = r.worldToObject;
         vg.majorants = v->majorants;
+        vg.dptMajorants = v->dptMajorants;
         for (int k = 0; k < 3; k++) {
           vg.mcDims[k] = f->mcDims[k];
           vg.dims[k] = f->dims[k];

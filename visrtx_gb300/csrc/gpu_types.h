@@ -157,8 +157,12 @@ struct VolumeGPU
   uint32_t hasTF;
   uint32_t pad0;
   xfm34 worldToObject;
-  // conservative macrocell majorants (max TF opacity reachable in a cell)
+  // conservative macrocell majorants (max TF opacity reachable in a cell),
+  // 16-voxel cells from the origin: empty-space skipping of the marcher
   const float *majorants;
+  // the reference's delta-tracking majorants: mcDims cells spanning
+  // `bounds` (UniformGrid.cu), read by the dpt distance sampler
+  const float *dptMajorants;
   int mcDims[3];
   int dims[3]; // voxel dims
 };

@@ -196,6 +196,7 @@ struct SpatialField : Object
   int dims[3] = {0, 0, 0};
   int mcDims[3] = {0, 0, 0};
   float *ranges = nullptr; // 2 floats per macrocell
+  float *refRanges = nullptr; // delta-tracking grid ranges (reference rule)
   uint64_t builtStamp = 0;
   ~SpatialField() override;
   void commit() override;
@@ -223,6 +224,7 @@ struct Volume : Object
   cudaTextureObject_t tfTex = 0;
   float4 *tfDev = nullptr;
   float *majorants = nullptr;
+  float *dptMajorants = nullptr; // delta-tracking majorants (reference rule)
   uint64_t builtStamp = 0;
   ~Volume() override;
   void commit() override;

@@ -74,5 +74,22 @@ cudaError_t launchMacrocellMajorants(const float *ranges,
     float uniformOpacity,
     float *majorants,
     cudaStream_t s);
+// The reference's delta-tracking grid (UniformGrid.cu): per-cell value ranges
+// (2 floats per cell) and max TF opacities.
+cudaError_t launchReferenceGridRanges(cudaTextureObject_t field,
+    f3 origin,
+    f3 spacing,
+    f3 invSpacing,
+    box3 bounds,
+    const int mcDims[3],
+    float *ranges,
+    cudaStream_t s);
+cudaError_t launchReferenceMajorants(const float *ranges,
+    const int mcDims[3],
+    cudaTextureObject_t tf,
+    int tfSize,
+    float uniformOpacity,
+    float *majorants,
+    cudaStream_t s);
 
 } // namespace vrtx

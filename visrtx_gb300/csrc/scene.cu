@@ -212,7 +212,181 @@ __global__ void k_mcMajorants(const float *ranges,
   majorants[c] = m;
 }
 
+// --- delta-tracking grid (the reference's UniformGrid) -------------------
+//
+// UniformGrid::init/buildGrid/computeMaxOpacities
+// (scene/volume/space_skipping/UniformGrid.cu:44-258): ceil(dims/16) cells
+// spanning the field bounds [origin, origin + (dims - 1) spacing]. One
+// thread per cell takes the max of 8 field taps at the object-space points
+// (cell id +- 0.5) / cellDims (the reference passes these through the field
+// sampler as positions, so they land near the field's first voxels), and
+// splats it with float atomic min/max into every cell its bounds project
+// onto. The dpt distance sampler reads these majorants, so they follow the
+// reference's arithmetic, not the conservative skipping grid above.
+
+__device__ __forceinline__ void atomicMinFloat(float *a, float v)
+{
+  if (!(v == v))
+    return;
+  if (v >= 0.f)
+    atomicMin(reinterpret_cast<int *>(a), __float_as_int(v));
+  else
+    atomicMax(reinterpret_cast<unsigned *>(a), __float_as_uint(v));
+}
+
+__device__ __forceinline__ void atomicMaxFloat(float *a, float v)
+{
+  if (!(v == v))
+    return;
+  if (v >= 0.f)
+    atomicMax(reinterpret_cast<int *>(a), __float_as_int(v));
+  else
+    atomicMin(reinterpret_cast<unsigned *>(a), __float_as_uint(v));
+}
+
+__device__ __forceinline__ int projectAxis(float v, float lo, float hi, int n)
+{
+  // projectOnGrid (gpu/uniformGrid.h:43-50): float -> int truncates
+  const float v01 = __fdiv_rn(__fsub_rn(v, lo), __fsub_rn(hi, lo));
+  return min(max(__float2int_rz(__fmul_rn(v01, float(n))), 0), n - 1);
+}
+
+__global__ void k_refGridInit(float *ranges, int cells)
+{
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= cells)
+    return;
+  ranges[2 * c] = 1e30f;
+  ranges[2 * c + 1] = -1e30f;
+}
+
+__global__ void k_refGridRanges(cudaTextureObject_t field,
+    f3 origin,
+    f3 spacing,
+    f3 invSpacing,
+    box3 bounds,
+    int mx,
+    int my,
+    int mz,
+    float *ranges)
+{
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= mx * my * mz)
+    return;
+  const int ix = c % mx, iy = (c / mx) % my, iz = c / (mx * my);
+  const float ex = __fdiv_rn(__fsub_rn(bounds.hi.x, bounds.lo.x), float(mx));
+  const float ey = __fdiv_rn(__fsub_rn(bounds.hi.y, bounds.lo.y), float(my));
+  const float ez = __fdiv_rn(__fsub_rn(bounds.hi.z, bounds.lo.z), float(mz));
+  const float lx = __fadd_rn(bounds.lo.x, __fmul_rn(float(ix), ex));
+  const float ly = __fadd_rn(bounds.lo.y, __fmul_rn(float(iy), ey));
+  const float lz = __fadd_rn(bounds.lo.z, __fmul_rn(float(iz), ez));
+  const float ux = __fadd_rn(lx, ex), uy = __fadd_rn(ly, ey), uz = __fadd_rn(lz, ez);
+  float value = -1e30f;
+#pragma unroll
+  for (int k = 0; k < 8; k++) {
+    // tap order of the reference: (-,-,-) (+,-,-) (+,+,-) (-,+,-), then z+
+    const float ox = (k == 1 || k == 2 || k == 5 || k == 6) ? 0.5f : -0.5f;
+    const float oy = (k == 2 || k == 3 || k == 6 || k == 7) ? 0.5f : -0.5f;
+    const float oz = k >= 4 ? 0.5f : -0.5f;
+    const f3 p = mk3(__fdiv_rn(__fadd_rn(float(ix), ox), float(mx)),
+        __fdiv_rn(__fadd_rn(float(iy), oy), float(my)),
+        __fdiv_rn(__fadd_rn(float(iz), oz), float(mz)));
+    // sampleSpatialField.h:54-78: ((p - origin) + 0.5 spacing) * invSpacing
+    const float cx = __fmul_rn(
+        __fadd_rn(__fsub_rn(p.x, origin.x), __fmul_rn(0.5f, spacing.x)), invSpacing.x);
+    const float cy = __fmul_rn(
+        __fadd_rn(__fsub_rn(p.y, origin.y), __fmul_rn(0.5f, spacing.y)), invSpacing.y);
+    const float cz = __fmul_rn(
+        __fadd_rn(__fsub_rn(p.z, origin.z), __fmul_rn(0.5f, spacing.z)), invSpacing.z);
+    value = fmaxf(value, tex3D<float>(field, cx, cy, cz));
+  }
+  const int x0 = projectAxis(lx, bounds.lo.x, bounds.hi.x, mx);
+  const int x1 = projectAxis(ux, bounds.lo.x, bounds.hi.x, mx);
+  const int y0 = projectAxis(ly, bounds.lo.y, bounds.hi.y, my);
+  const int y1 = projectAxis(uy, bounds.lo.y, bounds.hi.y, my);
+  const int z0 = projectAxis(lz, bounds.lo.z, bounds.hi.z, mz);
+  const int z1 = projectAxis(uz, bounds.lo.z, bounds.hi.z, mz);
+  for (int z = z0; z <= z1; z++)
+    for (int y = y0; y <= y1; y++)
+      for (int x = x0; x <= x1; x++) {
+        float *r = ranges + 2 * (((size_t)z * my + y) * mx + x);
+        atomicMinFloat(r, value);
+        atomicMaxFloat(r + 1, value);
+      }
+}
+
+// computeMaxOpacitiesGPU (UniformGrid.cu:55-90) with the default TF range
+// [0, 1]: max TF alpha over entries [int(lo (N-1)), int(hi (N-1)) + 1],
+// read through the TF texture at entry centres.
+__global__ void k_refMajorants(const float *ranges,
+    int cells,
+    cudaTextureObject_t tf,
+    int tfSize,
+    float uniformOpacity,
+    float *majorants)
+{
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= cells)
+    return;
+  const float lo = ranges[2 * c], hi = ranges[2 * c + 1];
+  if (hi < lo) {
+    majorants[c] = 0.f;
+    return;
+  }
+  if (!tf) {
+    majorants[c] = uniformOpacity;
+    return;
+  }
+  const int n1 = tfSize - 1;
+  const int e0 = min(max(__float2int_rz(__fmul_rn(lo, float(n1))), 0), n1);
+  const int e1 = min(max(__float2int_rz(__fmul_rn(hi, float(n1))) + 1, 0), n1);
+  float m = 0.f;
+  for (int i = e0; i <= e1; i++)
+    m = fmaxf(m, tex1D<float4>(tf, __fdiv_rn(float(i) + 0.5f, float(tfSize))).w);
+  majorants[c] = m;
+}
+
 } // namespace
+
+cudaError_t launchReferenceGridRanges(cudaTextureObject_t field,
+    f3 origin,
+    f3 spacing,
+    f3 invSpacing,
+    box3 bounds,
+    const int mcDims[3],
+    float *ranges,
+    cudaStream_t s)
+{
+  const int cells = mcDims[0] * mcDims[1] * mcDims[2];
+  if (!cells)
+    return cudaSuccess;
+  k_refGridInit<<<(cells + 255) / 256, 256, 0, s>>>(ranges, cells);
+  k_refGridRanges<<<(cells + 127) / 128, 128, 0, s>>>(field,
+      origin,
+      spacing,
+      invSpacing,
+      bounds,
+      mcDims[0],
+      mcDims[1],
+      mcDims[2],
+      ranges);
+  return cudaGetLastError();
+}
+
+cudaError_t launchReferenceMajorants(const float *ranges,
+    const int mcDims[3],
+    cudaTextureObject_t tf,
+    int tfSize,
+    float uniformOpacity,
+    float *majorants,
+    cudaStream_t s)
+{
+  const int cells = mcDims[0] * mcDims[1] * mcDims[2];
+  if (cells)
+    k_refMajorants<<<(cells + 255) / 256, 256, 0, s>>>(
+        ranges, cells, tf, tfSize, uniformOpacity, majorants);
+  return cudaGetLastError();
+}
 
 cudaError_t launchTriangleBoxes(const GeometryGPU *geoms,
     const uint2 *refs,

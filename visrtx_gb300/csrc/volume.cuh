@@ -217,9 +217,9 @@ __device__ __forceinline__ float volumeAttenuation(const WorldGPU &w,
   return a;
 }
 
-// dda3 (gpu/dda.h:44-122) over this library's macrocell grid: cells are 16
-// voxels from the field origin, so the Woodcock bound of a cell is the
-// conservative majorant built for it.
+// dda3 (gpu/dda.h:44-122) over the delta-tracking grid (dims cells across
+// `bounds`). Multiply-adds are written as fma so that the cell boundaries
+// do not depend on the compiler's contraction choices.
 template <typename F>
 __device__ __forceinline__ void dda3(
     f3 org, f3 dir, float tlo, float thi, const int dims[3], box3 bounds, F func)
@@ -232,26 +232,35 @@ __device__ __forceinline__ void dda3(
   const f3 tnear = fmin3(lo, hi);
   const f3 tfar = fmax3(lo, hi);
   // projectOnGrid (gpu/uniformGrid.h:43-50)
-  const f3 V01 = (org - bounds.lo) * mk3(1.f / (bounds.hi.x - bounds.lo.x),
-                                         1.f / (bounds.hi.y - bounds.lo.y),
-                                         1.f / (bounds.hi.z - bounds.lo.z));
-  int cx = min(max((int)(V01.x * dims[0]), 0), dims[0] - 1);
-  int cy = min(max((int)(V01.y * dims[1]), 0), dims[1] - 1);
-  int cz = min(max((int)(V01.z * dims[2]), 0), dims[2] - 1);
-  const f3 dist = mk3((tfar.x - tnear.x) / dims[0],
-      (tfar.y - tnear.y) / dims[1],
-      (tfar.z - tnear.z) / dims[2]);
+  int cx = min(max(__float2int_rz(__fmul_rn(__fdiv_rn(org.x - bounds.lo.x,
+                                                bounds.hi.x - bounds.lo.x),
+                                       float(dims[0]))),
+                   0),
+      dims[0] - 1);
+  int cy = min(max(__float2int_rz(__fmul_rn(__fdiv_rn(org.y - bounds.lo.y,
+                                                bounds.hi.y - bounds.lo.y),
+                                       float(dims[1]))),
+                   0),
+      dims[1] - 1);
+  int cz = min(max(__float2int_rz(__fmul_rn(__fdiv_rn(org.z - bounds.lo.z,
+                                                bounds.hi.z - bounds.lo.z),
+                                       float(dims[2]))),
+                   0),
+      dims[2] - 1);
+  const f3 dist = mk3(__fdiv_rn(tfar.x - tnear.x, float(dims[0])),
+      __fdiv_rn(tfar.y - tnear.y, float(dims[1])),
+      __fdiv_rn(tfar.z - tnear.z, float(dims[2])));
   const int sx = dir.x > 0.f ? 1 : -1, sy = dir.y > 0.f ? 1 : -1,
             sz = dir.z > 0.f ? 1 : -1;
   const int stx = dir.x > 0.f ? dims[0] : -1, sty = dir.y > 0.f ? dims[1] : -1,
             stz = dir.z > 0.f ? dims[2] : -1;
-  f3 tnext = mk3(dir.x > 0.f ? tnear.x + float(cx + 1) * dist.x
-                             : tnear.x + float(dims[0] - cx) * dist.x,
-      dir.y > 0.f ? tnear.y + float(cy + 1) * dist.y
-                  : tnear.y + float(dims[1] - cy) * dist.y,
-      dir.z > 0.f ? tnear.z + float(cz + 1) * dist.z
-                  : tnear.z + float(dims[2] - cz) * dist.z);
+  f3 tnext = mk3(
+      __fmaf_rn(float(dir.x > 0.f ? cx + 1 : dims[0] - cx), dist.x, tnear.x),
+      __fmaf_rn(float(dir.y > 0.f ? cy + 1 : dims[1] - cy), dist.y, tnear.y),
+      __fmaf_rn(float(dir.z > 0.f ? cz + 1 : dims[2] - cz), dist.z, tnear.z));
   float t0 = fmaxf(tlo, 0.f);
+  // every pass steps at least one axis; a cell walk ends within the sum of
+  // the dims (the bound only guards against NaN coordinates)
   for (int guard = 0; guard < 4 * (dims[0] + dims[1] + dims[2]) + 8; guard++) {
     const float t1 = fminf(compMin(tnext), thi);
     const size_t cell = ((size_t)cz * dims[1] + cy) * dims[0] + cx;
@@ -292,24 +301,26 @@ __device__ __forceinline__ float sampleDistance(const VolumeGPU &v,
   const float stepSize = v.stepSize;
   float t_out = h.thi;
   tr = 1.f;
-  const f3 org = h.localOrg + h.localDir * h.tlo;
+  const f3 org = mk3(__fmaf_rn(h.localDir.x, h.tlo, h.localOrg.x),
+      __fmaf_rn(h.localDir.y, h.tlo, h.localOrg.y),
+      __fmaf_rn(h.localDir.z, h.tlo, h.localOrg.z));
   const float tlo = 0.f, thi = h.thi - h.tlo;
-  box3 gb;
-  gb.lo = v.origin;
-  gb.hi = v.origin
-      + mk3(16.f * v.mcDims[0] * v.spacing.x,
-          16.f * v.mcDims[1] * v.spacing.y,
-          16.f * v.mcDims[2] * v.spacing.z);
-  dda3(org, h.localDir, tlo, thi, v.mcDims, gb, [&](size_t cell, float t0, float t1) {
-    const float majorant = v.majorants ? __ldg(v.majorants + cell) : 1.f;
+  dda3(org, h.localDir, tlo, thi, v.mcDims, v.bounds, [&](size_t cell, float t0, float t1) {
+    const float majorant = v.dptMajorants ? __ldg(v.dptMajorants + cell) : 1.f;
     float t = t0;
-    while (true) {
+    // a cell ends after finitely many draws (t grows by a positive amount
+    // each time unless a draw is exactly 0); the bound only guards that
+    for (int guard = 0; guard < (1 << 20); guard++) {
       if (majorant <= 0.f)
         break;
-      t -= logf(1.f - curand_uniform(&rs)) / majorant * stepSize;
+      const float lg = logf(1.f - curand_uniform(&rs));
+      t = __fmaf_rn(-__fdiv_rn(lg, majorant), stepSize, t);
       if (t >= t1)
         break;
-      const f3 p = h.localOrg + h.localDir * (t + h.tlo);
+      const float tt = t + h.tlo;
+      const f3 p = mk3(__fmaf_rn(h.localDir.x, tt, h.localOrg.x),
+          __fmaf_rn(h.localDir.y, tt, h.localOrg.y),
+          __fmaf_rn(h.localDir.z, tt, h.localOrg.z));
       const float s = sampleField(v, p);
       if (!isnan(s)) {
         const float4 co = classifySample(v, s);
