@@ -103,9 +103,11 @@ def _dm_problem(n=256, views=128, res=512, dtype=torch.float16, seed=0):
     vol = dm.VolumeInput(d.to(dtype).contiguous(), tf, scale,
                          step=0.5, unit=1.0, value_range=(0.0, 1.0))
     vol32 = dm.VolumeInput(d, tf, scale, step=0.5, unit=1.0, value_range=(0.0, 1.0), plain=True)
+    tgt = dm.VolumeInput(S.gaussian_blobs((n, n, n), 32, seed + 1, device="cuda"), tf, scale,
+                         step=0.5, unit=1.0, value_range=(0.0, 1.0))
     dirs = S.fibonacci_sphere(views)
     vws = [dm.look_at_view(0, vol.dims, 2.0 * dirs[i], 45.0, res, res) for i in range(views)]
-    return vol, vol32, vws
+    return vol, vol32, tgt, vws
 
 
 def _time_steps(fn, steps, warmup, flush):
@@ -124,12 +126,11 @@ def _time_steps(fn, steps, warmup, flush):
     return ts
 
 
-def _batched_step(vols, views, tile):
+def _batched_step(vols, views, tile, target):
     """One forward + L2 loss gradient + backward through a plan, captured
     in a CUDA graph."""
     b = dm.Batch(vols, views, tile)
     p = dm.Plan(b)
-    target = torch.zeros_like(p.image)
     grad = torch.empty_like(p.image)
 
     def body():
@@ -153,8 +154,11 @@ def _batched_step(vols, views, tile):
     return p, graph, target
 
 
-def _per_view_fp32_step(vols32, views):
-    targets = [None] * len(views)
+def _per_view_fp32_step(vols32, views, target):
+    targets, off = [], 0
+    for w in views:
+        targets.append(target[off:off + w.width * w.height])
+        off += w.width * w.height
 
     def body():
         for i, w in enumerate(views):
@@ -162,25 +166,31 @@ def _per_view_fp32_step(vols32, views):
             b = dm.Batch([v], [dm.View(0, w.width, w.height, w.eye, w.d00, w.du, w.dv,
                                        w.background)], (16, 8))
             img, st = dm.forward(b)
-            if targets[i] is None:
-                targets[i] = torch.zeros_like(img)
             dm.backward(b, st, 2.0 * (img - targets[i]))
     return body
 
 
-def _dm_line(name, workload, vols, vols32, views, args, local):
+def _targets(target_vols, views):
+    """Target images of the L2 loss: every view rendered (FP32) from the
+    second seeded volume of its slot."""
+    img, _ = dm.forward(dm.Batch(target_vols, views, (16, 8)))
+    return img
+
+
+def _dm_line(name, workload, vols, vols32, targets, views, args, local):
     torch.cuda.set_device(local)
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+    target = _targets(targets, views)
     cache = os.path.join(os.path.expanduser("~"), ".cache", "vrtx", "dm_tune.json")
     tile = dm.autotune(vols, views, reps=1, cache=cache)
-    p, graph, _ = _batched_step(vols, views, tile)
+    p, graph, _ = _batched_step(vols, views, tile, target)
     clocks = ClockSampler(local)
     clocks.start()
     tb = _time_steps(graph.replay, args.steps, args.warmup, flush)
     clk = clocks.stop()
     # the plain FP32 one-view-per-launch form on the same views (the FP32
     # fields the low-precision copies were made from, direct atomics)
-    body32 = _per_view_fp32_step(vols32, views)
+    body32 = _per_view_fp32_step(vols32, views, target)
     t32 = _time_steps(body32, max(1, args.steps // 2), 1, flush)
     # image error of the batched low-precision form against FP32
     b32 = dm.Batch(vols32, views, tile)
@@ -215,8 +225,9 @@ def run_dm(args, ws, rank, local):
     import __graft_entry__ as g
 
     g.build()
-    vol, vol32, views = _dm_problem(views=args.dm_views)
-    _dm_line("dm", f"dm256_fp16_{len(views)}views_512x512", [vol], [vol32], views, args, local)
+    vol, vol32, tgt, views = _dm_problem(views=args.dm_views)
+    _dm_line("dm", f"dm256_fp16_{len(views)}views_512x512", [vol], [vol32], [tgt], views, args,
+             local)
 
 
 def run_batched(args, ws, rank, local):
@@ -225,7 +236,7 @@ def run_batched(args, ws, rank, local):
 
     g.build()
     rng = S.Rng(5, stream=17)
-    vols, vols32, views = [], [], []
+    vols, vols32, tgts, views = [], [], [], []
     res_choices = [256, 512, 1024]
     for i in range(64):
         dims = tuple(int(x) for x in rng.uniform(3, 64, 385).astype(int))
@@ -236,11 +247,13 @@ def run_batched(args, ws, rank, local):
         vols.append(dm.VolumeInput(d.to(torch.bfloat16).contiguous(), tf, scale, 0.5, 1.0,
                                    (0.0, 1.0)))
         vols32.append(dm.VolumeInput(d, tf, scale, 0.5, 1.0, (0.0, 1.0), plain=True))
+        t = S.gaussian_blobs(dims, 16, 5000 + i, device="cuda", sigma_scale=max(dims) / 512)
+        tgts.append(dm.VolumeInput(t, tf, scale, 0.5, 1.0, (0.0, 1.0)))
         nv = int(rng.uniform(1, 4, 33)[0])
         dirs = S.fibonacci_sphere(nv)
         for k in range(nv):
             w = res_choices[int(rng.uniform(1, 0, 3)[0])]
             h = res_choices[int(rng.uniform(1, 0, 3)[0])]
             views.append(dm.look_at_view(i, vols[-1].dims, 2.0 * dirs[k], 45.0, w, h))
-    _dm_line("batched", f"batched64_bf16_{len(views)}views_uneven", vols, vols32, views, args,
-             local)
+    _dm_line("batched", f"batched64_bf16_{len(views)}views_uneven", vols, vols32, tgts, views,
+             args, local)

@@ -251,25 +251,60 @@ __global__ void __launch_bounds__(256) k_dmForward(const DMVol *vols,
   }
 }
 
-__device__ __forceinline__ void flushCell(float *G, const Tri &c, float acc[8])
+// Vector reduction of 4 consecutive floats (16-byte aligned), one L2 atomic
+// operation instead of four.
+__device__ __forceinline__ void redAddV4(float *p, float a, float b, float c, float d)
+{
+  asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(
+                   __cvta_generic_to_global(p)),
+               "f"(a),
+               "f"(b),
+               "f"(c),
+               "f"(d)
+               : "memory");
+}
+
+// Adds (a, b) at p[0] and p[dx] (dx 0 or 1).
+__device__ __forceinline__ void redPair(float *p, float a, float b, int dx, bool vec)
+{
+  if (a == 0.f && b == 0.f)
+    return;
+  if (dx == 0) {
+    atomicAdd(p, a + b);
+    return;
+  }
+  const unsigned lane = (unsigned)(reinterpret_cast<uintptr_t>(p) >> 2) & 3u;
+  if (!vec || lane == 3u) {
+    if (a != 0.f)
+      atomicAdd(p, a);
+    if (b != 0.f)
+      atomicAdd(p + 1, b);
+    return;
+  }
+  float *q = p - lane;
+  redAddV4(q,
+      lane == 0u ? a : 0.f,
+      lane == 0u ? b : (lane == 1u ? a : 0.f),
+      lane == 1u ? b : (lane == 2u ? a : 0.f),
+      lane == 2u ? b : 0.f);
+}
+
+// Commits a trilinear cell's 8 corner accumulators: the x-pairs of its four
+// (y, z) rows go out as one 16-byte vector reduction each when the pair
+// sits inside an aligned float4 (`vec`: the gradient array is 16-byte
+// aligned), else as scalar atomics.
+__device__ __forceinline__ void flushCell(float *G, const Tri &c, float acc[8], bool vec)
 {
   if (c.base == ~size_t(0))
     return;
   float *g = G + c.base;
-  const size_t off[8] = {0,
-      (size_t)c.sx,
-      (size_t)c.sy,
-      (size_t)c.sy + c.sx,
-      (size_t)c.sz,
-      (size_t)c.sz + c.sx,
-      (size_t)c.sz + c.sy,
-      (size_t)c.sz + c.sy + c.sx};
+  redPair(g, acc[0], acc[1], c.sx, vec);
+  redPair(g + c.sy, acc[2], acc[3], c.sx, vec);
+  redPair(g + c.sz, acc[4], acc[5], c.sx, vec);
+  redPair(g + c.sz + c.sy, acc[6], acc[7], c.sx, vec);
 #pragma unroll
-  for (int q = 0; q < 8; q++) {
-    if (acc[q] != 0.f)
-      atomicAdd(g + off[q], acc[q]);
+  for (int q = 0; q < 8; q++)
     acc[q] = 0.f;
-  }
 }
 
 __device__ __forceinline__ void flushTF(float *sTF, int seg, float acc[8])
@@ -285,8 +320,51 @@ __device__ __forceinline__ void flushTF(float *sTF, int seg, float acc[8])
   }
 }
 
+// Commits a block's TF gradient (shared memory, one float4 per entry: a
+// vector reduction per entry when gTF is 16-byte aligned) and its opacity-
+// scale gradient (block reduction, one atomic). All threads of the block
+// call it; it synchronises the block.
+__device__ __forceinline__ void commitBlockGrads(
+    const DMVol &v, const float *sTF, float *sScale, float gScale)
+{
+  for (int o = 16; o > 0; o >>= 1)
+    gScale += __shfl_xor_sync(0xffffffffu, gScale, o);
+  __syncthreads(); // sTF complete; sScale free
+  if ((threadIdx.x & 31) == 0)
+    sScale[threadIdx.x >> 5] = gScale;
+  __syncthreads();
+  if (threadIdx.x == 0 && v.gS) {
+    float sum = 0.f;
+    for (int i = 0; i < (int)(blockDim.x >> 5); i++)
+      sum += sScale[i];
+    atomicAdd(v.gS, sum);
+  }
+  if (v.gTF) {
+    const bool vec = (reinterpret_cast<uintptr_t>(v.gTF) & 15u) == 0;
+    for (int e = threadIdx.x; e < v.tfSize; e += blockDim.x) {
+      const float a = sTF[4 * e], b = sTF[4 * e + 1], c = sTF[4 * e + 2],
+                  d = sTF[4 * e + 3];
+      if (a == 0.f && b == 0.f && c == 0.f && d == 0.f)
+        continue;
+      if (vec) {
+        redAddV4(v.gTF + 4 * e, a, b, c, d);
+      } else {
+        atomicAdd(v.gTF + 4 * e, a);
+        atomicAdd(v.gTF + 4 * e + 1, b);
+        atomicAdd(v.gTF + 4 * e + 2, c);
+        atomicAdd(v.gTF + 4 * e + 3, d);
+      }
+    }
+  }
+  __syncthreads(); // sTF may be cleared next
+}
+
+#ifndef VRTX_DM_BWD_MIN_BLOCKS
+#define VRTX_DM_BWD_MIN_BLOCKS 3
+#endif
+
 template <typename T>
-__global__ void __launch_bounds__(256) k_dmBackward(const DMVol *vols,
+__global__ void __launch_bounds__(256, VRTX_DM_BWD_MIN_BLOCKS) k_dmBackward(const DMVol *vols,
     const DMViewG *views,
     int numViews,
     unsigned numItems,
@@ -296,29 +374,43 @@ __global__ void __launch_bounds__(256) k_dmBackward(const DMVol *vols,
     const float *state,
     const float *gradImage)
 {
-  extern __shared__ float sTF[]; // tfSize x 4 per tile
+  extern __shared__ float sTF[]; // tfSize x 4: TF gradient of one volume
   __shared__ unsigned item;
   __shared__ float sScale[8];
+  // The block's TF and opacity-scale gradients stay in shared memory and
+  // registers across consecutive work items of the same volume and are
+  // committed when the volume changes and at exit.
+  int curVol = -1;
+  float gScale = 0.f;
   while (true) {
     __syncthreads();
     if (threadIdx.x == 0)
       item = atomicAdd(counter, 1u);
     __syncthreads();
     const unsigned it = item;
+    const int nextVol =
+        it < numItems ? views[findView(views, numViews, it)].vol : -1;
+    if (nextVol != curVol) {
+      if (curVol >= 0)
+        commitBlockGrads(vols[curVol], sTF, sScale, gScale);
+      gScale = 0.f;
+      curVol = nextVol;
+      if (curVol >= 0)
+        for (int i = threadIdx.x; i < vols[curVol].tfSize * 4; i += blockDim.x)
+          sTF[i] = 0.f;
+      __syncthreads();
+    }
     if (it >= numItems)
       break;
     const DMViewG vw = views[findView(views, numViews, it)];
     DMVol v = vols[vw.vol];
     if (v.scalePtr)
       v.scale = __ldg(v.scalePtr);
-    for (int i = threadIdx.x; i < v.tfSize * 4; i += blockDim.x)
-      sTF[i] = 0.f;
-    __syncthreads();
     const unsigned tile = it - vw.tileStart;
     const int px = (int)(tile % vw.tilesX) * tileW + (int)threadIdx.x % tileW;
     const int py = (int)(tile / vw.tilesX) * tileH + (int)threadIdx.x / tileW;
-    float gScale = 0.f;
     const bool plain = (v.flags & VRTX_DM_PLAIN) != 0;
+    const bool vecD = (reinterpret_cast<uintptr_t>(v.gD) & 15u) == 0;
     // run-length gradient caches (one trilinear cell, one TF segment)
     Tri cell;
     cell.base = ~size_t(0);
@@ -418,7 +510,7 @@ __global__ void __launch_bounds__(256) k_dmBackward(const DMVol *vols,
                 // consecutive samples mostly stay in one trilinear cell:
                 // accumulate there and commit when the ray leaves it
                 if (tr.base != cell.base) {
-                  flushCell(v.gD, cell, dacc);
+                  flushCell(v.gD, cell, dacc, vecD);
                   cell = tr;
                 }
 #pragma unroll
@@ -434,24 +526,8 @@ __global__ void __launch_bounds__(256) k_dmBackward(const DMVol *vols,
       if (v.gTF)
         flushTF(sTF, tfSeg, tacc);
       if (v.gD)
-        flushCell(v.gD, cell, dacc);
+        flushCell(v.gD, cell, dacc, vecD);
     }
-    // opacity-scale gradient: block reduction, one atomic per tile
-    for (int o = 16; o > 0; o >>= 1)
-      gScale += __shfl_xor_sync(0xffffffffu, gScale, o);
-    if ((threadIdx.x & 31) == 0)
-      sScale[threadIdx.x >> 5] = gScale;
-    __syncthreads();
-    if (threadIdx.x == 0 && v.gS) {
-      float sum = 0.f;
-      for (int i = 0; i < (int)(blockDim.x >> 5); i++)
-        sum += sScale[i];
-      atomicAdd(v.gS, sum);
-    }
-    if (v.gTF)
-      for (int i = threadIdx.x; i < v.tfSize * 4; i += blockDim.x)
-        if (sTF[i] != 0.f)
-          atomicAdd(v.gTF + i, sTF[i]);
   }
 }
 
