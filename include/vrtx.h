@@ -355,7 +355,7 @@ typedef struct VRTXDMView {
 /* Forward. image: 3 floats per pixel. state: 2 floats per pixel (final
  * log-transmittance, and the sample count stored as an int32 bit pattern);
  * the backward pass reads it. tileW x tileH pixels per work item
- * (tileW * tileH a multiple of 32, at most 1024). Returns 0, or a negative
+ * (tileW * tileH a multiple of 32, at most 256). Returns 0, or a negative
  * code after reporting the error through the device's status callback. */
 VRTX_API int vrtxDMForward(VRTXDevice d,
     const VRTXDMVolume *volumes,

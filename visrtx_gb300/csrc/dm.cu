@@ -264,7 +264,10 @@ __device__ __forceinline__ void redAddV4(float *p, float a, float b, float c, fl
                : "memory");
 }
 
-// Adds (a, b) at p[0] and p[dx] (dx 0 or 1).
+// Adds (a, b) at p[0] and p[dx] (dx 0 or 1). With `vec` (16-byte aligned
+// array) the pair goes out as one vector reduction on the aligned float4
+// holding p[0], plus a second on the next float4 when p[0] is its last
+// element.
 __device__ __forceinline__ void redPair(float *p, float a, float b, int dx, bool vec)
 {
   if (a == 0.f && b == 0.f)
@@ -273,20 +276,22 @@ __device__ __forceinline__ void redPair(float *p, float a, float b, int dx, bool
     atomicAdd(p, a + b);
     return;
   }
-  const unsigned lane = (unsigned)(reinterpret_cast<uintptr_t>(p) >> 2) & 3u;
-  if (!vec || lane == 3u) {
+  if (!vec) {
     if (a != 0.f)
       atomicAdd(p, a);
     if (b != 0.f)
       atomicAdd(p + 1, b);
     return;
   }
+  const unsigned lane = (unsigned)(reinterpret_cast<uintptr_t>(p) >> 2) & 3u;
   float *q = p - lane;
   redAddV4(q,
       lane == 0u ? a : 0.f,
       lane == 0u ? b : (lane == 1u ? a : 0.f),
       lane == 1u ? b : (lane == 2u ? a : 0.f),
-      lane == 2u ? b : 0.f);
+      lane == 2u ? b : (lane == 3u ? a : 0.f));
+  if (lane == 3u)
+    redAddV4(q + 4, b, 0.f, 0.f, 0.f);
 }
 
 // Commits a trilinear cell's 8 corner accumulators: the x-pairs of its four
@@ -307,25 +312,60 @@ __device__ __forceinline__ void flushCell(float *G, const Tri &c, float acc[8], 
     acc[q] = 0.f;
 }
 
-__device__ __forceinline__ void flushTF(float *sTF, int seg, float acc[8])
+// TF gradients live in one shared-memory copy per warp (float4 per entry).
+// Lanes that add to the same entry at the same time are grouped with
+// match.any; each group's leader sums its peers' values with shuffles and
+// does one plain read-modify-write of the float4, so no shared-memory
+// atomics are needed (float atomics on shared memory are much slower than
+// this on the hardware measured).
+__device__ __forceinline__ void addEntry(float4 *wTF, int e, float4 v, unsigned mask)
 {
-  if (seg < 0)
-    return;
-  float *e = sTF + 4 * seg;
-#pragma unroll
-  for (int q = 0; q < 8; q++) {
-    if (acc[q] != 0.f)
-      atomicAdd(e + q, acc[q]);
-    acc[q] = 0.f;
+  const unsigned lane = threadIdx.x & 31u;
+  const unsigned peers = __match_any_sync(mask, e);
+  const unsigned leader = __ffs(peers) - 1;
+  if (peers != (1u << lane)) {
+    float4 tot = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (unsigned rest = peers; rest; rest &= rest - 1) {
+      const int l = __ffs(rest) - 1;
+      tot.x += __shfl_sync(peers, v.x, l);
+      tot.y += __shfl_sync(peers, v.y, l);
+      tot.z += __shfl_sync(peers, v.z, l);
+      tot.w += __shfl_sync(peers, v.w, l);
+    }
+    v = tot;
+  }
+  if (lane == leader && e >= 0) {
+    float4 o = wTF[e];
+    o.x += v.x;
+    o.y += v.y;
+    o.z += v.z;
+    o.w += v.w;
+    wTF[e] = o;
   }
 }
 
-// Commits a block's TF gradient (shared memory, one float4 per entry: a
-// vector reduction per entry when gTF is 16-byte aligned) and its opacity-
-// scale gradient (block reduction, one atomic). All threads of the block
-// call it; it synchronises the block.
+// Adds a segment's 8 accumulators to entries seg and seg + 1 of this warp's
+// copy (entries seg in one pass, seg + 1 in the next, so that one lane's
+// seg + 1 and another's seg never race) and clears them.
+__device__ __forceinline__ void flushTF(float4 *wTF, int seg, float acc[8])
+{
+  const unsigned mask = __activemask();
+  const bool has = seg >= 0;
+  addEntry(wTF, has ? seg : -1, make_float4(acc[0], acc[1], acc[2], acc[3]), mask);
+  __syncwarp(mask);
+  addEntry(wTF, has ? seg + 1 : -2, make_float4(acc[4], acc[5], acc[6], acc[7]), mask);
+  __syncwarp(mask);
+#pragma unroll
+  for (int q = 0; q < 8; q++)
+    acc[q] = 0.f;
+}
+
+// Commits a block's TF gradient (the sum of its warps' shared-memory
+// copies; one vector reduction per entry when gTF is 16-byte aligned) and
+// its opacity-scale gradient (block reduction, one atomic). All threads of
+// the block call it; it synchronises the block.
 __device__ __forceinline__ void commitBlockGrads(
-    const DMVol &v, const float *sTF, float *sScale, float gScale)
+    const DMVol &v, const float4 *sTF, int tfStride, float *sScale, float gScale)
 {
   for (int o = 16; o > 0; o >>= 1)
     gScale += __shfl_xor_sync(0xffffffffu, gScale, o);
@@ -333,26 +373,33 @@ __device__ __forceinline__ void commitBlockGrads(
   if ((threadIdx.x & 31) == 0)
     sScale[threadIdx.x >> 5] = gScale;
   __syncthreads();
+  const int warps = (int)(blockDim.x >> 5);
   if (threadIdx.x == 0 && v.gS) {
     float sum = 0.f;
-    for (int i = 0; i < (int)(blockDim.x >> 5); i++)
+    for (int i = 0; i < warps; i++)
       sum += sScale[i];
     atomicAdd(v.gS, sum);
   }
   if (v.gTF) {
     const bool vec = (reinterpret_cast<uintptr_t>(v.gTF) & 15u) == 0;
     for (int e = threadIdx.x; e < v.tfSize; e += blockDim.x) {
-      const float a = sTF[4 * e], b = sTF[4 * e + 1], c = sTF[4 * e + 2],
-                  d = sTF[4 * e + 3];
-      if (a == 0.f && b == 0.f && c == 0.f && d == 0.f)
+      float4 t = sTF[e];
+      for (int w = 1; w < warps; w++) {
+        const float4 u = sTF[w * tfStride + e];
+        t.x += u.x;
+        t.y += u.y;
+        t.z += u.z;
+        t.w += u.w;
+      }
+      if (t.x == 0.f && t.y == 0.f && t.z == 0.f && t.w == 0.f)
         continue;
       if (vec) {
-        redAddV4(v.gTF + 4 * e, a, b, c, d);
+        redAddV4(v.gTF + 4 * e, t.x, t.y, t.z, t.w);
       } else {
-        atomicAdd(v.gTF + 4 * e, a);
-        atomicAdd(v.gTF + 4 * e + 1, b);
-        atomicAdd(v.gTF + 4 * e + 2, c);
-        atomicAdd(v.gTF + 4 * e + 3, d);
+        atomicAdd(v.gTF + 4 * e, t.x);
+        atomicAdd(v.gTF + 4 * e + 1, t.y);
+        atomicAdd(v.gTF + 4 * e + 2, t.z);
+        atomicAdd(v.gTF + 4 * e + 3, t.w);
       }
     }
   }
@@ -371,10 +418,14 @@ __global__ void __launch_bounds__(256, VRTX_DM_BWD_MIN_BLOCKS) k_dmBackward(cons
     unsigned *counter,
     int tileW,
     int tileH,
+    int tfMax,
     const float *state,
     const float *gradImage)
 {
-  extern __shared__ float sTF[]; // tfSize x 4: TF gradient of one volume
+  // TF gradient of one volume: one copy of tfStride float4 entries per warp
+  extern __shared__ float4 sTF[];
+  const int tfStride = tfMax;
+  float4 *wTF = sTF + (threadIdx.x >> 5) * tfStride;
   __shared__ unsigned item;
   __shared__ float sScale[8];
   // The block's TF and opacity-scale gradients stay in shared memory and
@@ -392,12 +443,12 @@ __global__ void __launch_bounds__(256, VRTX_DM_BWD_MIN_BLOCKS) k_dmBackward(cons
         it < numItems ? views[findView(views, numViews, it)].vol : -1;
     if (nextVol != curVol) {
       if (curVol >= 0)
-        commitBlockGrads(vols[curVol], sTF, sScale, gScale);
+        commitBlockGrads(vols[curVol], sTF, tfStride, sScale, gScale);
       gScale = 0.f;
       curVol = nextVol;
       if (curVol >= 0)
-        for (int i = threadIdx.x; i < vols[curVol].tfSize * 4; i += blockDim.x)
-          sTF[i] = 0.f;
+        for (int i = threadIdx.x; i < (int)(blockDim.x >> 5) * tfStride; i += blockDim.x)
+          sTF[i] = make_float4(0.f, 0.f, 0.f, 0.f);
       __syncthreads();
     }
     if (it >= numItems)
@@ -457,7 +508,7 @@ __global__ void __launch_bounds__(256, VRTX_DM_BWD_MIN_BLOCKS) k_dmBackward(cons
           const float f0 = 1.f - cl.f, f1 = cl.f;
           if (v.gTF) {
             if (plain) {
-              float *e0 = sTF + 4 * cl.i0;
+              float *e0 = reinterpret_cast<float *>(wTF + cl.i0);
               atomicAdd(e0 + 0, f0 * dc.x);
               atomicAdd(e0 + 1, f0 * dc.y);
               atomicAdd(e0 + 2, f0 * dc.z);
@@ -468,7 +519,7 @@ __global__ void __launch_bounds__(256, VRTX_DM_BWD_MIN_BLOCKS) k_dmBackward(cons
               atomicAdd(e0 + 7, f1 * dA);
             } else {
               if (cl.i0 != tfSeg) {
-                flushTF(sTF, tfSeg, tacc);
+                flushTF(wTF, tfSeg, tacc);
                 tfSeg = cl.i0;
               }
               tacc[0] += f0 * dc.x;
@@ -524,7 +575,7 @@ __global__ void __launch_bounds__(256, VRTX_DM_BWD_MIN_BLOCKS) k_dmBackward(cons
     }
     if (!plain) {
       if (v.gTF)
-        flushTF(sTF, tfSeg, tacc);
+        flushTF(wTF, tfSeg, tacc);
       if (v.gD)
         flushCell(v.gD, cell, dacc, vecD);
     }
@@ -680,19 +731,20 @@ cudaError_t launchBackward(const Layout &L, uint8_t *block, const float *state,
   const DMViewG *views = reinterpret_cast<const DMViewG *>(block + L.offViews);
   cudaMemsetAsync(counter, 0, 4, s);
   const int threads = L.tileW * L.tileH;
-  const size_t smem = sizeof(float) * 4 * L.maxTf;
+  // one float4 TF-gradient copy per warp
+  const size_t smem = sizeof(float4) * (size_t)(threads / 32) * L.maxTf;
   switch (L.type) {
   case VRTX_FLOAT16:
     k_dmBackward<__half><<<gridFor((const void *)k_dmBackward<__half>, threads, smem), threads, smem, s>>>(
-        vols, views, L.numViews, L.numItems, counter, L.tileW, L.tileH, state, gradImage);
+        vols, views, L.numViews, L.numItems, counter, L.tileW, L.tileH, L.maxTf, state, gradImage);
     break;
   case VRTX_BFLOAT16:
     k_dmBackward<__nv_bfloat16><<<gridFor((const void *)k_dmBackward<__nv_bfloat16>, threads, smem), threads, smem, s>>>(
-        vols, views, L.numViews, L.numItems, counter, L.tileW, L.tileH, state, gradImage);
+        vols, views, L.numViews, L.numItems, counter, L.tileW, L.tileH, L.maxTf, state, gradImage);
     break;
   default:
     k_dmBackward<float><<<gridFor((const void *)k_dmBackward<float>, threads, smem), threads, smem, s>>>(
-        vols, views, L.numViews, L.numItems, counter, L.tileW, L.tileH, state, gradImage);
+        vols, views, L.numViews, L.numItems, counter, L.tileW, L.tileH, L.maxTf, state, gradImage);
     break;
   }
   return cudaGetLastError();
