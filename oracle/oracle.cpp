@@ -1442,6 +1442,7 @@ struct Sample
   float opacity;
   float depth;
   uint32_t prim, obj, inst;
+  V3 albedo, normal; // accumResults' albedo and normal arguments
 };
 
 // default/directLight, raycast and ao raygen bodies
@@ -1456,6 +1457,7 @@ Sample integrate(Ctx &C, const VolCtx &VC, const CamPre &cam, Stream &rs, int px
   Ray ray = primaryRay(cam, rs, px, py, invW, invH, rt == 1);
   const float tmax = ray.tmax;
   V3 outC = v3(0, 0, 0);
+  V3 outN = ray.dir; // outputNormal: the ray direction on a miss
   float outO = 0.f, depth = 1e30f;
   uint32_t prim = ~0u, obj = ~0u, inst = ~0u;
   bool first = true;
@@ -1475,11 +1477,16 @@ Sample integrate(Ctx &C, const VolCtx &VC, const CamPre &cam, Stream &rs, int px
           C, VC, rs, ray.org, ray.dir, ray.tmin, sh.t, invRate, color, opacity, vo, vi);
       if (first) {
         if (vDepth < sh.t) {
+          outN = -1.f * ray.dir;
           depth = vDepth;
           prim = 0;
           obj = vo;
           inst = vi;
         } else {
+          // directLight reports Ns, raycast and ao Ng
+          // (DirectLight_ptx.cu:351, Raycast_ptx.cu:114,
+          // AmbientOcclusion_ptx.cu:144)
+          outN = rt == 0 ? sh.Ns : sh.Ng;
           depth = sh.t;
           prim = sh.primId;
           obj = sh.objId;
@@ -1535,7 +1542,7 @@ Sample integrate(Ctx &C, const VolCtx &VC, const CamPre &cam, Stream &rs, int px
       break;
     }
   }
-  return Sample{outC, outO, depth, prim, obj, inst};
+  return Sample{outC, outO, depth, prim, obj, inst, outC, outN};
 }
 
 // --- output (gpu/gpu_util.h:321-443) ---------------------------------------
@@ -1624,7 +1631,9 @@ Sample integrateDPT(Ctx &C, const VolCtx &VC, const CamPre &cam, Stream &rs, int
   const OrcRenderer &R = *C.R;
   Ray ray = primaryRay(cam, rs, px, py, invW, invH, false);
   const V3 bg = v3(R.background[0], R.background[1], R.background[2]);
-  Sample out{bg, 1.f, ray.tmax, ~0u, ~0u, ~0u};
+  // outColor (the background) and the primary ray direction go to the
+  // albedo and normal channels
+  Sample out{bg, 1.f, ray.tmax, ~0u, ~0u, ~0u, bg, ray.dir};
   const bool hasVolumes = C.S->sc->numVolumes > 0;
   while (true) {
     HitRec h;
@@ -1880,8 +1889,12 @@ int orc_render_prepared(void *prepared, const OrcCamera *camera, const OrcRender
   OrcFrame &F = *frame;
   const int W = F.width, H = F.height;
   const float invW = 1.f / (float)W, invH = 1.f / (float)H;
-  const int rb = std::max(0, F.rowBegin), re = std::min(H, F.rowEnd);
-  const int tilesX = (W + 15) / 16, tilesY = (re - rb + 15) / 16;
+  // checkerboarding (createScreenSample.h:38-46): the launch covers every
+  // other pixel in x and y, offset by the checkerboard id
+  const int cb = F.checkerboardID;
+  const int LW = cb >= 0 ? (W + 1) / 2 : W, LH = cb >= 0 ? (H + 1) / 2 : H;
+  const int rb = std::max(0, F.rowBegin), re = std::min(LH, F.rowEnd);
+  const int tilesX = (LW + 15) / 16, tilesY = (re - rb + 15) / 16;
   std::atomic<int> next{0};
   std::atomic<uint64_t> rays{0};
   auto worker = [&]() {
@@ -1891,8 +1904,12 @@ int orc_render_prepared(void *prepared, const OrcCamera *camera, const OrcRender
       if (t >= tilesX * tilesY)
         break;
       const int tx = t % tilesX, ty = t / tilesX;
-      for (int y = rb + ty * 16; y < std::min(re, rb + ty * 16 + 16); y++)
-        for (int x = tx * 16; x < std::min(W, tx * 16 + 16); x++) {
+      for (int ly = rb + ty * 16; ly < std::min(re, rb + ty * 16 + 16); ly++)
+        for (int lx = tx * 16; lx < std::min(LW, tx * 16 + 16); lx++) {
+          const int x = cb < 0 ? lx : lx * 2 + (cb & 1);
+          const int y = cb < 0 ? ly : ly * 2 + ((cb >> 1) & 1);
+          if (x >= W || y >= H)
+            continue;
           Stream rs;
           rs.init((uint64_t)(y * W + x), 0, (uint64_t)F.frameID * 512ull);
           const size_t idx = (size_t)y * W + x;
@@ -1909,6 +1926,16 @@ int orc_render_prepared(void *prepared, const OrcCamera *camera, const OrcRender
             tonemap(v);
             for (int c = 0; c < 4; c++)
               acc[c] += v[c];
+            if (F.albedo) {
+              F.albedo[3 * idx] += s.albedo.x;
+              F.albedo[3 * idx + 1] += s.albedo.y;
+              F.albedo[3 * idx + 2] += s.albedo.z;
+            }
+            if (F.normal) {
+              F.normal[3 * idx] += s.normal.x;
+              F.normal[3 * idx + 1] += s.normal.y;
+              F.normal[3 * idx + 2] += s.normal.z;
+            }
             if (!F.depth || s.depth < cur) {
               cur = s.depth;
               if (F.depth)
@@ -1919,6 +1946,18 @@ int orc_render_prepared(void *prepared, const OrcCamera *camera, const OrcRender
                 F.objId[idx] = s.obj;
               if (F.instId)
                 F.instId[idx] = s.inst;
+            }
+            // accumResults (gpu_util.h:393-443): the output is written after
+            // every sample; on the first checkerboard pass of a fresh frame
+            // (sample frame id 0) it is also splatted to the 2x2 block's
+            // three other pixels, which this pass does not render
+            if (cb == 0 && F.frameID + i == 0) {
+              if (x + 1 < W)
+                writeColor(F, acc, idx + 1, i);
+              if (y + 1 < H)
+                writeColor(F, acc, idx + W, i);
+              if (x + 1 < W && y + 1 < H)
+                writeColor(F, acc, idx + W + 1, i);
             }
           }
           std::memcpy(F.accum + 4 * idx, acc, 16);

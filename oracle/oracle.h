@@ -139,7 +139,7 @@ typedef struct OrcFrame {
   int width, height;
   int frameID; /* sample index base (RNG offset = frameID * 512) */
   int colorFormat; /* 0 sRGB rgba8, 1 linear rgba8, 2 float4 */
-  int rowBegin, rowEnd; /* rows to render */
+  int rowBegin, rowEnd; /* launch rows to render */
   /* outputs (full-frame buffers; only rows in range are written) */
   float *accum; /* float4, in/out */
   void *color; /* u32 or float4 */
@@ -147,6 +147,8 @@ typedef struct OrcFrame {
   uint32_t *primId, *objId, *instId;
   /* statistics: rays traced (primary + secondary) */
   uint64_t raysTraced;
+  int checkerboardID; /* -1: off; 0..3: which pixel of each 2x2 block */
+  float *albedo, *normal; /* vec3 accumulations (in/out) or NULL */
 } OrcFrame;
 
 /* Renders rows [rowBegin, rowEnd). volumeMode 0: parity (texture

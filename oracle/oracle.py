@@ -80,7 +80,8 @@ class OrcFrame(C.Structure):
                 ("colorFormat", C.c_int), ("rowBegin", C.c_int), ("rowEnd", C.c_int),
                 ("accum", C.c_void_p), ("color", C.c_void_p), ("depth", C.c_void_p),
                 ("primId", C.c_void_p), ("objId", C.c_void_p), ("instId", C.c_void_p),
-                ("raysTraced", C.c_uint64)]
+                ("raysTraced", C.c_uint64), ("checkerboardID", C.c_int),
+                ("albedo", C.c_void_p), ("normal", C.c_void_p)]
 
 
 class OrcDMVolume(C.Structure):
@@ -149,11 +150,15 @@ class OracleScene:
             self.handle = None
 
     def render(self, frame_id=0, rows=None, volume_mode=0, tex_round=1, threads=0, accum=None,
-               depth=None, spec=None, ids=None):
-        """ids: a previous result dict whose id buffers carry over (ids are
-        only rewritten where the depth improves)."""
+               depth=None, spec=None, ids=None, checkerboard_id=-1, channels=False):
+        """ids: a previous result dict whose id buffers (and colour, albedo
+        and normal accumulations) carry over: ids are only rewritten where
+        the depth improves, and a checkerboard pass leaves the other pixels'
+        colour as it was. channels: also accumulate the albedo and normal
+        channels."""
         return _render_prepared(self.lib, self.handle, spec or self.spec, frame_id, rows,
-                                volume_mode, tex_round, threads, accum, depth, ids)
+                                volume_mode, tex_round, threads, accum, depth, ids,
+                                checkerboard_id, channels)
 
 
 def _scene_structs(spec):
@@ -249,7 +254,7 @@ def dpt_majorants(vspec, tex_round: int = 1) -> np.ndarray:
 
 
 def _render_prepared(lib, handle, spec, frame_id, rows, volume_mode, tex_round, threads, accum,
-                     depth, ids=None):
+                     depth, ids=None, checkerboard_id=-1, channels=False):
     c = spec.camera
     cam = OrcCamera()
     cam.type = 0 if c.type == "perspective" else 1
@@ -271,7 +276,8 @@ def _render_prepared(lib, handle, spec, frame_id, rows, volume_mode, tex_round, 
     ren.occlusionDistance = r.ao_distance
     ren.cullTriangleBackfaces = int(bool(r.cull))
     ren.volumeSamplingRate = r.volume_sampling_rate
-    ren.pixelSamples = r.pixel_samples
+    # checkerboarding forces one sample per pass (Renderer.cpp:168-169)
+    ren.pixelSamples = 1 if r.checkerboard else r.pixel_samples
     ren.ambientSamples = r.ambient_samples if ren.type in (0, 2) else 0
     ren.maxDepth = r.max_depth
     W, H = spec.width, spec.height
@@ -283,6 +289,12 @@ def _render_prepared(lib, handle, spec, frame_id, rows, volume_mode, tex_round, 
         "objectId": np.zeros((H, W), np.uint32) if ids is None else ids["objectId"],
         "instanceId": np.zeros((H, W), np.uint32) if ids is None else ids["instanceId"],
     }
+    if ids is not None and "color" in ids:
+        out["color"] = ids["color"]
+    if channels:
+        for ch in ("albedo", "normal"):
+            out[ch] = (ids[ch] if ids is not None and ch in ids
+                       else np.zeros((H, W, 3), np.float32))
     fr = OrcFrame()
     fr.width, fr.height, fr.frameID, fr.colorFormat = W, H, frame_id, 0
     fr.rowBegin, fr.rowEnd = (0, H) if rows is None else rows
@@ -292,6 +304,9 @@ def _render_prepared(lib, handle, spec, frame_id, rows, volume_mode, tex_round, 
     fr.primId = _ptr(out["primitiveId"])
     fr.objId = _ptr(out["objectId"])
     fr.instId = _ptr(out["instanceId"])
+    fr.checkerboardID = checkerboard_id
+    fr.albedo = _ptr(out.get("albedo"))
+    fr.normal = _ptr(out.get("normal"))
     rc = lib.orc_render_prepared(handle, C.byref(cam), C.byref(ren), C.byref(fr),
                                  C.c_int(volume_mode), C.c_int(tex_round), C.c_int(threads))
     assert rc == 0

@@ -14,35 +14,59 @@ ID_FRAC = 1e-4
 DEPTH_REL = 1e-5
 
 
-def render_gpu(dev, spec: scenes.SceneSpec, frames: int = 1):
-    frame, world, keep = scenes.build_on_device(dev, spec)
+def render_gpu(dev, spec: scenes.SceneSpec, frames: int = 1, channels: bool = False):
+    chans = ("color", "depth", "primitiveId", "objectId", "instanceId")
+    if channels:
+        chans += ("albedo", "normal")
+    frame, world, keep = scenes.build_on_device(dev, spec, channels=chans)
     for _ in range(frames):
         frame.render()
     frame.wait()
-    out = {ch: frame.map("channel." + ch)
-           for ch in ("color", "depth", "primitiveId", "objectId", "instanceId")}
+    out = {ch: frame.map("channel." + ch) for ch in chans}
     out["frame"] = frame
     out["world"] = world
     out["keep"] = keep
     return out
 
 
-def render_oracle(spec: scenes.SceneSpec, frames: int = 1, **kw):
+def oracle_frame_ids(spec: scenes.SceneSpec, frames: int):
+    """(frameID, checkerboardID) of each render call, as Frame::newFrame
+    advances them (Frame.cu:590-660): with checkerboarding the frame id
+    grows by one after checkerboard pass 3, else by pixelSamples."""
+    r = spec.renderer
+    out = []
+    for f in range(frames):
+        if r.checkerboard:
+            out.append((f // 4, f % 4))
+        elif r.subtype == "raycast":
+            out.append((f, -1))
+        else:
+            out.append((f * max(1, r.pixel_samples), -1))
+    return out
+
+
+def render_oracle(spec: scenes.SceneSpec, frames: int = 1, channels: bool = False, **kw):
+    """The oracle's frames; with `channels` the albedo and normal outputs are
+    returned as the reference maps them (accumulation / (frameID + 1))."""
     from oracle import oracle as O
 
     sc = O.OracleScene(spec)
     prev = None
     out = None
+    fid = 0
     try:
-        for f in range(frames):
-            out = sc.render(frame_id=f * max(1, spec.renderer.pixel_samples)
-                            if spec.renderer.subtype != "raycast" else f,
+        for fid, cb in oracle_frame_ids(spec, frames):
+            out = sc.render(frame_id=fid,
                             accum=None if prev is None else prev["accum"],
                             depth=None if prev is None else prev["depth"],
-                            ids=None if prev is None else prev, **kw)
+                            ids=prev, checkerboard_id=cb, channels=channels, **kw)
             prev = out
     finally:
         sc.release()
+    if channels:
+        out = dict(out)
+        for ch in ("albedo", "normal"):
+            out[ch] = out[ch] * np.float32(1.0 / (fid + 1))
     return out
 
 

@@ -140,6 +140,45 @@ def test_accumulation_frames(device):
     assert g["frame"].get_property("numSamples", L.INT32) == 4
 
 
+@pytest.mark.parametrize("renderer", ["default", "ao"])
+def test_checkerboard_frames(device, renderer):
+    """Checkerboarding: four passes per frame id over every other pixel in
+    x and y, with the first pass of a fresh frame splatting its colour to
+    the rest of each 2x2 block (createScreenSample.h:38-46,
+    gpu_util.h:424-442). Six passes cover ids 0..3 and the next frame."""
+    spec = soup(renderer, n=5000, w=47, h=33, ambient_samples=2 if renderer == "ao" else 0)
+    spec.renderer.checkerboard = True
+    for frames in (1, 6):
+        g = render_gpu(device, spec, frames=frames)
+        r = render_oracle(spec, frames=frames)
+        compare(g, r)
+        if frames == 1:
+            # the splat filled the pixels this pass did not render
+            c = g["color"].reshape(33, 47)
+            assert np.array_equal(c[0::2, 1::2], c[0::2, 0:46:2])
+
+
+@pytest.mark.parametrize("renderer", ["default", "raycast", "ao", "dpt"])
+def test_albedo_normal_channels(device, renderer):
+    """channel.albedo / channel.normal: per-sample accumulations of
+    accumResults' albedo (the sample colour; dpt: the background) and normal
+    (directLight Ns, raycast/ao Ng, -dir in front of a volume, dir on a
+    miss), mapped as accumulation / (frameID + 1) (Frame.cu:518-557)."""
+    spec = soup(renderer, n=5000, w=48, h=32, ambient_samples=2 if renderer == "ao" else 0,
+                pixel_samples=1 if renderer == "raycast" else 2)
+    frames = 1 if renderer == "raycast" else 2
+    g = render_gpu(device, spec, frames=frames, channels=True)
+    r = render_oracle(spec, frames=frames, channels=True)
+    compare(g, r)
+    same = np.ones(g["primitiveId"].shape, bool)
+    for ch in ("primitiveId", "objectId", "instanceId"):
+        same &= g[ch] == r[ch]
+    for ch in ("albedo", "normal"):
+        assert g[ch].shape == (32, 48, 3), ch
+        np.testing.assert_allclose(g[ch][same], r[ch][same], rtol=1e-4, atol=1e-5, err_msg=ch)
+    assert np.abs(g["normal"]).max() > 0.1
+
+
 def test_orthographic(device):
     spec = soup("raycast", n=5000, w=64, h=64)
     spec.camera = S.CameraSpec(type="orthographic", position=(0.5, 0.5, -1.0),

@@ -1728,8 +1728,17 @@ void Frame::commit()
   fb.primID = cPrim ? (uint32_t *)alloc(3, n * 4) : nullptr;
   fb.objID = cObj ? (uint32_t *)alloc(4, n * 4) : nullptr;
   fb.instID = cInst ? (uint32_t *)alloc(5, n * 4) : nullptr;
-  fb.albedo = albedoType == VRTX_FLOAT32_VEC3 ? (f3 *)alloc(6, n * 12) : nullptr;
-  fb.normal = normalType == VRTX_FLOAT32_VEC3 ? (f3 *)alloc(7, n * 12) : nullptr;
+  // The reference enables these accumulations for ANARI_FLOAT32
+  // (Frame.cu:116-117); FLOAT32_VEC3, the channel's element type, is
+  // accepted too. Slots 8/9 hold the averaged copies that map returns.
+  const bool wantAlbedo = albedoType == VRTX_FLOAT32 || albedoType == VRTX_FLOAT32_VEC3;
+  const bool wantNormal = normalType == VRTX_FLOAT32 || normalType == VRTX_FLOAT32_VEC3;
+  fb.albedo = wantAlbedo ? (f3 *)alloc(6, n * 12) : nullptr;
+  fb.normal = wantNormal ? (f3 *)alloc(7, n * 12) : nullptr;
+  if (wantAlbedo)
+    alloc(8, n * 12);
+  if (wantNormal)
+    alloc(9, n * 12);
   if (!workCounter)
     cudaMalloc(&workCounter, 16);
   if (!errorFlag) {
@@ -1924,16 +1933,21 @@ const void *Frame::map(
     src = fb.instID;
     bytes = n * 4;
     host = &hostInst;
-  } else if (base == "channel.albedo" && fb.albedo) {
+  } else if ((base == "channel.albedo" && fb.albedo && buffers[8])
+      || (base == "channel.normal" && fb.normal && buffers[9])) {
+    // mapAlbedoBuffer / mapNormalBuffer (Frame.cu:518-557): the
+    // accumulation times 1 / (frameID + 1), into a separate buffer
+    const bool alb = base == "channel.albedo";
     t = VRTX_FLOAT32_VEC3;
-    src = fb.albedo;
+    src = buffers[alb ? 8 : 9];
     bytes = n * 12;
-    host = &hostAlbedo;
-  } else if (base == "channel.normal" && fb.normal) {
-    t = VRTX_FLOAT32_VEC3;
-    src = fb.normal;
-    bytes = n * 12;
-    host = &hostNormal;
+    host = alb ? &hostAlbedo : &hostNormal;
+    launchScale3(alb ? fb.albedo : fb.normal,
+        (f3 *)src,
+        n,
+        1.f / float(fb.frameID + 1),
+        Object::dev->stream);
+    cudaStreamSynchronize(Object::dev->stream);
   }
   if (t == VRTX_UNKNOWN || !src) {
     *w = *h = 0;

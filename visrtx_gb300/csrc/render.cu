@@ -1213,6 +1213,20 @@ cudaError_t launchRender(
   return cudaGetLastError();
 }
 
+__global__ void k_scale3(const f3 *in, f3 *out, size_t n, float scale)
+{
+  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i < n)
+    out[i] = in[i] * scale;
+}
+
+cudaError_t launchScale3(const f3 *in, f3 *out, size_t n, float scale, cudaStream_t s)
+{
+  if (n)
+    k_scale3<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(in, out, n, scale);
+  return cudaGetLastError();
+}
+
 cudaError_t launchClearFrame(const FramebufferGPU &fb, cudaStream_t s)
 {
   k_clearFrame<<<1216, 256, 0, s>>>(fb);

@@ -11,6 +11,8 @@ int renderOccupancyBlocks(int rendererType, bool stats);
 cudaError_t launchRender(
     const FrameParams &P, int gridBlocks, bool stats, cudaStream_t s);
 cudaError_t launchClearFrame(const FramebufferGPU &fb, cudaStream_t s);
+// out[i] = in[i] * scale for n vec3 elements (albedo / normal map)
+cudaError_t launchScale3(const f3 *in, f3 *out, size_t n, float scale, cudaStream_t s);
 
 // Wavefront "ao" renderer (opaque materials, no volumes): per sample a
 // primary kernel, an any-hit kernel over the compacted AO ray queue and a

@@ -361,6 +361,7 @@ class RendererSpec:
     pixel_samples: int = 1
     ambient_samples: int = 1
     max_depth: int = 5
+    checkerboard: bool = False
 
     def resolved_ambient(self) -> float:
         if self.ambient_radiance is not None:
@@ -534,6 +535,7 @@ def build_on_device(dev, spec: SceneSpec, channels=("color", "depth", "primitive
     ren.set("pixelSamples", int(r.pixel_samples))
     ren.set("ambientSamples", int(r.ambient_samples))
     ren.set("maxDepth", int(r.max_depth))
+    ren.set("checkerboarding", bool(r.checkerboard))
     ren.commit()
 
     fr = dev.new_frame()
@@ -544,6 +546,9 @@ def build_on_device(dev, spec: SceneSpec, channels=("color", "depth", "primitive
             fr.set("channel.depth", DataType(L.FLOAT32))
         elif ch in ("primitiveId", "objectId", "instanceId"):
             fr.set("channel." + ch, DataType(L.UINT32))
+        elif ch in ("albedo", "normal"):
+            # the reference enables these for ANARI_FLOAT32 (Frame.cu:116-117)
+            fr.set("channel." + ch, DataType(L.FLOAT32))
     fr.set("renderer", ren).set("camera", cam).set("world", world)
     fr.commit()
     keep += [world, cam, ren]
