@@ -1873,7 +1873,9 @@ void Frame::render()
   } else {
     tracePairs = 0;
     const int blocks =
-        d->numSMs * renderOccupancyBlocks(P.renderer.type, countTraversal);
+        d->numSMs
+        * renderOccupancyBlocks(
+            P.renderer.type, countTraversal, P.world.numInstances > 0);
     err = launchRender(P, blocks, countTraversal, s);
     launches++;
   }

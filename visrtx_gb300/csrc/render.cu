@@ -33,6 +33,12 @@
 #define VRTX_AO_SHARED_STACK 16
 #endif
 
+// blocks per SM the per-pixel kernel is compiled for on worlds without
+// surfaces (volume-only frames)
+#ifndef VRTX_VOLUME_MIN_BLOCKS
+#define VRTX_VOLUME_MIN_BLOCKS 10
+#endif
+
 #ifndef VRTX_TRACE_MIN_BLOCKS
 #define VRTX_TRACE_MIN_BLOCKS 8
 #endif
@@ -323,7 +329,10 @@ struct SampleOut
   uint32_t primID, objID, instID;
 };
 
-template <int RT, bool STATS>
+// SURF = false: the world has no surface instances, so the surface
+// traversal (and every shading branch behind a surface hit) compiles away;
+// volume-only frames then run with far fewer registers per thread.
+template <int RT, bool STATS, bool SURF>
 __device__ __forceinline__ void integrateSample(const FrameParams &P,
     TravStats &st,
     RandState &rs,
@@ -349,7 +358,10 @@ __device__ __forceinline__ void integrateSample(const FrameParams &P,
     ray.tmax = tmax;
     Hit h;
     float unused;
-    const bool found = traverse<0, STATS>(w,
+    // a primary / path ray against an empty surface set still counts
+    if (!SURF)
+      st.rays++;
+    const bool found = SURF && traverse<0, STATS>(w,
         ray.org,
         ray.dir,
         ray.tmin,
@@ -493,7 +505,7 @@ struct PathData
   f3 Lw;
 };
 
-template <bool STATS>
+template <bool STATS, bool SURF>
 __device__ __forceinline__ void integrateDPT(const FrameParams &P,
     TravStats &st,
     RandState &rs,
@@ -516,7 +528,10 @@ __device__ __forceinline__ void integrateDPT(const FrameParams &P,
   while (true) {
     Hit h;
     float unused;
-    const bool found = traverse<0, STATS>(w,
+    // a primary / path ray against an empty surface set still counts
+    if (!SURF)
+      st.rays++;
+    const bool found = SURF && traverse<0, STATS>(w,
         ray.org,
         ray.dir,
         ray.tmin,
@@ -639,7 +654,7 @@ __device__ __forceinline__ void writeOutputColor(
     fb.outColorF[idx] = c;
 }
 
-template <int RT, bool STATS>
+template <int RT, bool STATS, bool SURF>
 __device__ __forceinline__ void renderPixel(
     const FrameParams &P, TravStats &st, int lx, int ly)
 {
@@ -666,9 +681,9 @@ __device__ __forceinline__ void renderPixel(
   for (int i = 0; i < iters; i++) {
     SampleOut s;
     if (RT == RENDERER_DPT)
-      integrateDPT<STATS>(P, st, rs, x, y, pd, s);
+      integrateDPT<STATS, SURF>(P, st, rs, x, y, pd, s);
     else
-      integrateSample<RT, STATS>(P, st, rs, x, y, s);
+      integrateSample<RT, STATS, SURF>(P, st, rs, x, y, s);
     const float4 tm = tonemap(make_float4(s.color.x, s.color.y, s.color.z, s.opacity));
     acc.x += tm.x;
     acc.y += tm.y;
@@ -718,8 +733,9 @@ __device__ __forceinline__ unsigned long long warpSum(unsigned long long v)
   return v;
 }
 
-template <int RT, bool STATS>
-__global__ void __launch_bounds__(128, VRTX_RENDER_MIN_BLOCKS) k_render(const FrameParams P)
+template <int RT, bool STATS, bool SURF>
+__global__ void __launch_bounds__(128, SURF ? VRTX_RENDER_MIN_BLOCKS : VRTX_VOLUME_MIN_BLOCKS)
+    k_render(const FrameParams P)
 {
   const int lane = threadIdx.x & 31;
   const uint32_t numTiles = P.numTilesX * P.numTilesY;
@@ -735,7 +751,7 @@ __global__ void __launch_bounds__(128, VRTX_RENDER_MIN_BLOCKS) k_render(const Fr
     const int lx = (int)(tx * 8 + (lane & 7));
     const int ly = (int)(ty * 4 + (lane >> 3));
     if (lx < (int)P.launchW && ly < (int)P.launchH)
-      renderPixel<RT, STATS>(P, st, lx, ly);
+      renderPixel<RT, STATS, SURF>(P, st, lx, ly);
   }
   // per-warp totals: rays and volume samples always, traversal counters in
   // the counting build
@@ -1164,52 +1180,63 @@ cudaError_t launchAOWavefront(const FrameParams &P,
   return cudaGetLastError();
 }
 
-template <int RT, bool STATS>
+template <int RT, bool STATS, bool SURF>
 static void launchOne(const FrameParams &P, int *occ, int grid, cudaStream_t s)
 {
   if (occ)
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(occ, k_render<RT, STATS>, 128, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(occ, k_render<RT, STATS, SURF>, 128, 0);
   else
-    k_render<RT, STATS><<<grid, 128, 0, s>>>(P);
+    k_render<RT, STATS, SURF><<<grid, 128, 0, s>>>(P);
 }
 
-template <bool STATS>
+template <bool STATS, bool SURF>
 static void dispatch(const FrameParams &P, int type, int *occ, int grid, cudaStream_t s)
 {
   switch (type) {
   case RENDERER_RAYCAST:
-    launchOne<RENDERER_RAYCAST, STATS>(P, occ, grid, s);
+    launchOne<RENDERER_RAYCAST, STATS, SURF>(P, occ, grid, s);
     break;
   case RENDERER_AO:
-    launchOne<RENDERER_AO, STATS>(P, occ, grid, s);
+    launchOne<RENDERER_AO, STATS, SURF>(P, occ, grid, s);
     break;
   case RENDERER_DPT:
-    launchOne<RENDERER_DPT, STATS>(P, occ, grid, s);
+    launchOne<RENDERER_DPT, STATS, SURF>(P, occ, grid, s);
     break;
   default:
-    launchOne<RENDERER_DIRECT_LIGHT, STATS>(P, occ, grid, s);
+    launchOne<RENDERER_DIRECT_LIGHT, STATS, SURF>(P, occ, grid, s);
     break;
   }
 }
 
-int renderOccupancyBlocks(int rendererType, bool stats)
+template <bool STATS>
+static void dispatchSurf(
+    const FrameParams &P, int type, bool surf, int *occ, int grid, cudaStream_t s)
+{
+  if (surf)
+    dispatch<STATS, true>(P, type, occ, grid, s);
+  else
+    dispatch<STATS, false>(P, type, occ, grid, s);
+}
+
+int renderOccupancyBlocks(int rendererType, bool stats, bool surfaces)
 {
   int blocks = 0;
   FrameParams dummy{};
   if (stats)
-    dispatch<true>(dummy, rendererType, &blocks, 0, 0);
+    dispatchSurf<true>(dummy, rendererType, surfaces, &blocks, 0, 0);
   else
-    dispatch<false>(dummy, rendererType, &blocks, 0, 0);
+    dispatchSurf<false>(dummy, rendererType, surfaces, &blocks, 0, 0);
   return blocks > 0 ? blocks : 1;
 }
 
 cudaError_t launchRender(
     const FrameParams &P, int gridBlocks, bool stats, cudaStream_t s)
 {
+  const bool surf = P.world.numInstances > 0;
   if (stats)
-    dispatch<true>(P, P.renderer.type, nullptr, gridBlocks, s);
+    dispatchSurf<true>(P, P.renderer.type, surf, nullptr, gridBlocks, s);
   else
-    dispatch<false>(P, P.renderer.type, nullptr, gridBlocks, s);
+    dispatchSurf<false>(P, P.renderer.type, surf, nullptr, gridBlocks, s);
   return cudaGetLastError();
 }
 

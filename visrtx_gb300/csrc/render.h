@@ -6,7 +6,7 @@
 namespace vrtx {
 
 // integrator (render.cu)
-int renderOccupancyBlocks(int rendererType, bool stats);
+int renderOccupancyBlocks(int rendererType, bool stats, bool surfaces);
 // stats: the counting build (node visits, primitive tests, BLAS entries)
 cudaError_t launchRender(
     const FrameParams &P, int gridBlocks, bool stats, cudaStream_t s);
