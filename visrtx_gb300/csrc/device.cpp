@@ -1168,6 +1168,13 @@ bool Volume::ensureBuilt()
     majorants = nullptr;
     return false;
   }
+  unsigned *dEmpty = nullptr;
+  unsigned empty = 0;
+  if (cudaMalloc(&dEmpty, sizeof(unsigned)) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  cudaMemsetAsync(dEmpty, 0, sizeof(unsigned), s);
   launchMacrocellMajorants(field->ranges,
       field->mcDims,
       tfDev,
@@ -1176,7 +1183,14 @@ bool Volume::ensureBuilt()
       valueRange[1],
       uniformOpacity,
       majorants,
+      dEmpty,
       s);
+  cudaMemcpyAsync(&empty, dEmpty, sizeof(unsigned), cudaMemcpyDeviceToHost, s);
+  cudaStreamSynchronize(s);
+  cudaFree(dEmpty);
+  // without empty cells the skipping grid never skips: the marcher then
+  // does not consult it
+  hasEmptyCells = empty > 0;
   if (cudaMalloc(&dptMajorants, cells * sizeof(float)) != cudaSuccess) {
     cudaGetLastError();
     dptMajorants = nullptr;
@@ -1498,7 +1512,7 @@ bool World::rebuild()
         vg.id = v->id;
         vg.instId = inst->userID(t);
         vg.worldToObject = r.worldToObject;
-        vg.majorants = v->majorants;
+        vg.majorants = v->hasEmptyCells ? v->majorants : nullptr;
         vg.dptMajorants = v->dptMajorants;
         for (int k = 0; k < 3; k++) {
           vg.mcDims[k] = f->mcDims[k];

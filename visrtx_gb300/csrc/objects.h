@@ -225,6 +225,7 @@ struct Volume : Object
   float4 *tfDev = nullptr;
   float *majorants = nullptr;
   float *dptMajorants = nullptr; // delta-tracking majorants (reference rule)
+  bool hasEmptyCells = false; // some skipping-grid cell has majorant 0
   uint64_t builtStamp = 0;
   ~Volume() override;
   void commit() override;

@@ -36,7 +36,7 @@
 // blocks per SM the per-pixel kernel is compiled for on worlds without
 // surfaces (volume-only frames)
 #ifndef VRTX_VOLUME_MIN_BLOCKS
-#define VRTX_VOLUME_MIN_BLOCKS 10
+#define VRTX_VOLUME_MIN_BLOCKS 8
 #endif
 
 #ifndef VRTX_TRACE_MIN_BLOCKS

@@ -75,6 +75,7 @@ cudaError_t launchMacrocellMajorants(const float *ranges,
     float valueHi,
     float uniformOpacity,
     float *majorants,
+    unsigned *emptyCells, // incremented once per cell with majorant 0
     cudaStream_t s);
 // The reference's delta-tracking grid (UniformGrid.cu): per-cell value ranges
 // (2 floats per cell) and max TF opacities.

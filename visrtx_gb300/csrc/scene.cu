@@ -183,7 +183,8 @@ __global__ void k_mcMajorants(const float *ranges,
     float vlo,
     float vhi,
     float uniformOpacity,
-    float *majorants)
+    float *majorants,
+    unsigned *emptyCells)
 {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= numCells)
@@ -191,6 +192,7 @@ __global__ void k_mcMajorants(const float *ranges,
   const float lo = ranges[2 * c], hi = ranges[2 * c + 1];
   if (!(lo <= hi)) { // empty or all-NaN cell
     majorants[c] = 0.f;
+    atomicAdd(emptyCells, 1u);
     return;
   }
   if (!tf) {
@@ -210,6 +212,8 @@ __global__ void k_mcMajorants(const float *ranges,
   for (int e = e0; e <= e1; e++)
     m = fmaxf(m, tf[e].w);
   majorants[c] = m;
+  if (m == 0.f)
+    atomicAdd(emptyCells, 1u);
 }
 
 // --- delta-tracking grid (the reference's UniformGrid) -------------------
@@ -475,6 +479,7 @@ cudaError_t launchMacrocellMajorants(const float *ranges,
     float valueHi,
     float uniformOpacity,
     float *majorants,
+    unsigned *emptyCells,
     cudaStream_t s)
 {
   const int cells = mcDims[0] * mcDims[1] * mcDims[2];
@@ -486,7 +491,8 @@ cudaError_t launchMacrocellMajorants(const float *ranges,
         valueLo,
         valueHi,
         uniformOpacity,
-        majorants);
+        majorants,
+        emptyCells);
   return cudaGetLastError();
 }
 

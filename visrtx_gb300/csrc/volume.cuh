@@ -132,14 +132,28 @@ __device__ __forceinline__ float rayMarchVolume(const VolumeGPU &v,
   float transmittance = 1.f;
   if (!(stepSize > 0.f))
     return depth;
+  // Software-pipelined: the field fetch for the next position is issued
+  // before the current sample is classified, so the two dependent texture
+  // reads of consecutive samples overlap. Positions, the order of the
+  // accumulation and the stopping rule are those of the plain loop.
+  f3 p = h.localOrg + h.localDir * lower;
+  bool want = cellMajorant(v, p) > 0.f;
+  float s = want ? sampleField(v, p) : 0.f;
   // bound the march (a ray through a 2^24-step box is not a real scene)
   for (int guard = 0; guard < (1 << 24) && opacity < 0.99f && upper - lower >= 0.f;
        guard++) {
-    const f3 p = h.localOrg + h.localDir * lower;
     st.samples++;
-    if (cellMajorant(v, p) > 0.f) {
+    const float next = lower + stepSize;
+    bool wantNext = false;
+    float sNext = 0.f;
+    if (upper - next >= 0.f) {
+      const f3 pn = h.localOrg + h.localDir * next;
+      wantNext = cellMajorant(v, pn) > 0.f;
+      if (wantNext)
+        sNext = sampleField(v, pn);
+    }
+    if (want) {
       st.fetches++;
-      const float s = sampleField(v, p);
       if (!isnan(s)) {
         const float4 co = classifySample(v, s);
         const float stepT = powf(1.f - co.w, exponent);
@@ -150,7 +164,9 @@ __device__ __forceinline__ float rayMarchVolume(const VolumeGPU &v,
         transmittance *= stepT;
       }
     }
-    lower += stepSize;
+    lower = next;
+    want = wantNext;
+    s = sNext;
   }
   return depth;
 }
