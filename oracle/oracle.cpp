@@ -395,10 +395,40 @@ struct SceneCtx
   bool allOpaque = true;
 };
 
+// Quad.cpp:115-141: quad (x, y, z, w) becomes triangles (x, y, w) and
+// (z, w, y); without an index quad q uses vertices 4q .. 4q + 3
+void quadTri(const OrcSurface &s, uint32_t k, uint32_t &i0, uint32_t &i1, uint32_t &i2)
+{
+  const uint32_t q = k / 2;
+  uint32_t x, y, z, w;
+  if (s.indices) {
+    x = s.indices[4 * q];
+    y = s.indices[4 * q + 1];
+    z = s.indices[4 * q + 2];
+    w = s.indices[4 * q + 3];
+  } else {
+    x = 4 * q;
+    y = x + 1;
+    z = x + 2;
+    w = x + 3;
+  }
+  if (k % 2 == 0) {
+    i0 = x;
+    i1 = y;
+    i2 = w;
+  } else {
+    i0 = z;
+    i1 = w;
+    i2 = y;
+  }
+}
+
 void triVerts(const OrcSurface &s, uint32_t p, V3 &a, V3 &b, V3 &c)
 {
   uint32_t i0, i1, i2;
-  if (s.indices) {
+  if (s.type == 2) {
+    quadTri(s, p, i0, i1, i2);
+  } else if (s.indices) {
     i0 = s.indices[3 * p];
     i1 = s.indices[3 * p + 1];
     i2 = s.indices[3 * p + 2];
@@ -419,11 +449,54 @@ void sphereOf(const OrcSurface &s, uint32_t p, V3 &c, float &r)
   r = s.radii ? s.radii[i] : s.radius;
 }
 
+// The segment of a cylinder (3), cone (4) or curve (5) primitive
+// (Intersectors_ptx.cu:100-246, populateHit.h:292-303, Curve.cpp:88-113)
+void segmentOf(const OrcSurface &s, uint32_t p, V3 &p0, float &r0, V3 &p1, float &r1)
+{
+  uint32_t i0, i1;
+  if (s.type == 5) {
+    i0 = s.indices ? s.indices[p] : p;
+    i1 = i0 + 1;
+  } else {
+    i0 = s.indices ? s.indices[2 * p] : 2 * p;
+    i1 = s.indices ? s.indices[2 * p + 1] : 2 * p + 1;
+  }
+  p0 = ld3(s.vertices, i0);
+  p1 = ld3(s.vertices, i1);
+  if (s.type == 3) {
+    r0 = r1 = std::fabs(s.radii ? s.radii[p] : s.radius);
+  } else if (s.type == 4) {
+    r0 = s.radii[i0];
+    r1 = s.radii[i1];
+  } else {
+    r0 = s.radii ? s.radii[i0] : s.radius;
+    r1 = s.radii ? s.radii[i1] : s.radius;
+  }
+}
+
 Box primBox(const OrcScene *sc, const Prim &pr)
 {
   const OrcSurface &s = sc->surfaces[pr.surface];
   Box b;
-  if (s.type == 0) {
+  if (s.type >= 3) {
+    V3 p0, p1;
+    float r0, r1;
+    segmentOf(s, pr.prim, p0, r0, p1, r1);
+    if (s.type == 5) {
+      b.ext(p0 - v3(r0, r0, r0));
+      b.ext(p0 + v3(r0, r0, r0));
+      b.ext(p1 - v3(r1, r1, r1));
+      b.ext(p1 + v3(r1, r1, r1));
+    } else {
+      const float m = std::max(r0, r1);
+      b.ext(p0 - v3(m, m, m));
+      b.ext(p0 + v3(m, m, m));
+      b.ext(p1 - v3(m, m, m));
+      b.ext(p1 + v3(m, m, m));
+    }
+    return b;
+  }
+  if (s.type == 0 || s.type == 2) {
     V3 a, bb, c;
     triVerts(s, pr.prim, a, bb, c);
     b.ext(a);
@@ -646,6 +719,189 @@ bool hitSphere(const RayPre &r, V3 center, float radius, float tmin, float tmax,
   return true;
 }
 
+// intersectCylinder (scene/Intersectors_ptx.cu:100-175): reports side
+// entry, side exit (between the end planes), then the nearer cap disk
+template <typename F>
+void cylinderReports(const RayPre &r, V3 p0, V3 p1, float radius, bool caps, F &&report)
+{
+  const V3 ro = r.o, rd = r.d;
+  const V3 sv = p1 - p0;
+  const V3 sxd = cross(sv, rd);
+  const float a = dot(sxd, sxd);
+  if (a == 0.f)
+    return;
+  const V3 f = p0 - ro;
+  const V3 sxf = cross(sv, f);
+  const float ra = 1.f / a;
+  const float ts = dot(sxd, sxf) * ra;
+  const V3 fp = f - ts * rd;
+  const float s2 = dot(sv, sv);
+  const V3 perp = cross(sv, fp);
+  const float c = (radius * radius) * s2 - dot(perp, perp);
+  if (c < 0.f)
+    return;
+  const float td = std::sqrt(c * ra);
+  const float tin = ts - td, tout = ts + td;
+  const float sf = dot(sv, f), sd = dot(sv, rd);
+  const float u_in = (tin * sd - sf) * (1.f / s2);
+  const V3 N_in = -td * rd - fp - u_in * sv;
+  const float u_out = (tout * sd - sf) * (1.f / s2);
+  const V3 N_out = td * rd - fp - u_out * sv;
+  if (sd != 0.f) {
+    const float rsd = 1.f / sd;
+    const float tA = sf * rsd;
+    const float tB = tA + s2 * rsd;
+    const float capIn = std::min(tA, tB), capOut = std::max(tA, tB);
+    if (tin > capIn && tin < capOut)
+      report(tin, N_in, u_in);
+    if (tout > capIn && tout < capOut)
+      report(tout, N_out, u_out);
+  } else if (sf <= 0.f && sf >= -s2) {
+    report(tin, N_in, u_in);
+    report(tout, N_out, u_out);
+  }
+  if (caps) {
+    const float ca = s2 - sd * sd;
+    const float cb = s2 * dot(-f, rd) + (sf * sd);
+    const float cc = s2 * dot(-f, -f) - (sf * sf) - (radius * radius * s2);
+    float h = cb * cb - ca * cc;
+    if (h < 0.f)
+      return;
+    h = std::sqrt(h);
+    const float y = ((-cb - h) / ca) * sd - sf;
+    const float d = ((y < 0.f ? 0.f : s2) + sf) / sd;
+    if (std::fabs(cb + ca * d) < h) {
+      const float sg = y > 0.f ? 1.f : (y < 0.f ? -1.f : 0.f);
+      report(d, sv * sg / s2, y < 0.f ? 0.f : 1.f);
+    }
+  }
+}
+
+// intersectCone (scene/Intersectors_ptx.cu:177-246)
+template <typename F>
+void coneReports(const RayPre &r, V3 p0, float ra, V3 p1, float rb, F &&report)
+{
+  const V3 ro = r.o, rd = r.d;
+  const V3 ba = p1 - p0, oa = ro - p0, ob = ro - p1;
+  const float m0 = dot(ba, ba), m1 = dot(oa, ba), m2 = dot(ob, ba), m3 = dot(rd, ba);
+  if (m1 < 0.f) {
+    const V3 q = oa * m3 - rd * m1;
+    if (dot(q, q) < (ra * ra * m3 * m3))
+      report(-m1 / m3, -ba * (1.f / std::sqrt(m0)), 0.f);
+  } else if (m2 > 0.f) {
+    const V3 q = ob * m3 - rd * m2;
+    if (dot(q, q) < (rb * rb * m3 * m3))
+      report(-m2 / m3, ba * (1.f / std::sqrt(m0)), 1.f);
+  }
+  const float m4 = dot(rd, oa), m5 = dot(oa, oa);
+  const float rr = ra - rb;
+  const float hy = m0 + rr * rr;
+  const float k2 = m0 * m0 - m3 * m3 * hy;
+  const float k1 = m0 * m0 * m4 - m1 * m3 * hy + m0 * ra * (rr * m3 * 1.0f);
+  const float k0 = m0 * m0 * m5 - m1 * m1 * hy + m0 * ra * (rr * m1 * 2.0f - m0 * ra);
+  const float h = k1 * k1 - k2 * k0;
+  if (h < 0.f)
+    return;
+  const float t = (-k1 - std::sqrt(h)) / k2;
+  const float y = m1 + t * m3;
+  if (y > 0.f && y < m0)
+    report(t, normalize(m0 * (m0 * (oa + t * rd) + rr * ba * ra) - ba * hy * y), y / m0);
+}
+
+// Round linear curve segment: the libvrtx definition (OptiX's own test is
+// closed) -- the union of the two end balls and their tangent cone, entered
+// at the smallest entry root of its convex parts; a ray starting inside
+// reports nothing. Same arithmetic as the GPU test.
+template <typename F>
+void curveReports(const RayPre &r, V3 pa, float ra, V3 pb, float rb, float tmin, F &&report)
+{
+  const V3 d = r.d;
+  const float dd = dot(d, d);
+  const float shift = dot(pa - r.o, d) / dd;
+  const V3 o = r.o + d * shift;
+  const V3 ba = pb - pa;
+  const float L2 = dot(ba, ba);
+  const V3 oa = o - pa, ob = o - pb;
+  float best = 3.0e38f, bestU = 0.f;
+  {
+    const V3 oa0 = r.o - pa, ob0 = r.o - pb;
+    if (dot(oa0, oa0) < ra * ra || dot(ob0, ob0) < rb * rb)
+      return;
+    const float Lq = std::sqrt(L2);
+    if (L2 > 0.f) {
+      const float sn = (ra - rb) / Lq;
+      const float c2 = 1.f - sn * sn;
+      const V3 w0 = ba / Lq;
+      const float z = dot(oa0, w0);
+      const V3 q = oa0 - w0 * z;
+      const float A = ra - sn * z;
+      if (c2 > 0.f && z >= ra * sn && z <= Lq + rb * sn && A >= 0.f && c2 * dot(q, q) < A * A)
+        return;
+    }
+  }
+  // end balls, each from the ray point closest to its own centre
+  auto ball = [&](V3 c, float rad, float u) {
+    const float sc = dot(c - r.o, d) / dd;
+    const V3 oc = (r.o + d * sc) - c;
+    const float bq = dot(oc, d), cq = dot(oc, oc) - rad * rad;
+    const float disc = bq * bq - dd * cq;
+    if (disc < 0.f)
+      return;
+    const float t = sc + (-bq - std::sqrt(disc)) / dd;
+    if (t < best && t >= tmin) {
+      best = t;
+      bestU = u;
+    }
+  };
+  ball(pa, ra, 0.f);
+  ball(pb, rb, 1.f);
+  const float L = std::sqrt(L2);
+  const float sinp = (ra - rb) / L;
+  const float cos2 = 1.f - sinp * sinp;
+  if (L2 > 0.f && cos2 > 0.f) {
+    const V3 w = ba / L;
+    const float z0 = dot(oa, w), dz = dot(d, w);
+    const V3 q0 = oa - z0 * w, dq = d - dz * w;
+    const float zA = ra * sinp, zB = L + rb * sinp;
+    const float A0 = ra - sinp * z0, A1 = -sinp * dz;
+    const float qq = dot(q0, q0);
+    const float a = cos2 * dot(dq, dq) - A1 * A1;
+    const float b = cos2 * dot(q0, dq) - A0 * A1;
+    const float c = cos2 * qq - A0 * A0;
+    const float disc = b * b - a * c;
+    if (a != 0.f && disc >= 0.f) {
+      const float sq = std::sqrt(disc);
+      const float t0 = (-b - sq) / a, t1 = (-b + sq) / a;
+      for (int k = 0; k < 2; k++) {
+        const float t = k == 0 ? std::min(t0, t1) : std::max(t0, t1);
+        const float z = z0 + t * dz;
+        const float tg = shift + t;
+        if (a * t + b < 0.f && z >= zA && z <= zB && A0 + A1 * t >= 0.f && tg < best
+            && tg >= tmin) {
+          best = tg;
+          bestU = (z - zA) / (zB - zA);
+        }
+      }
+    }
+  }
+  if (best < 3.0e38f)
+    report(best, v3(0, 0, 0), bestU);
+}
+
+template <typename F>
+void segmentReports(const RayPre &r, const OrcSurface &s, uint32_t prim, float tmin, F &&report)
+{
+  V3 p0, p1;
+  float r0, r1;
+  segmentOf(s, prim, p0, r0, p1, r1);
+  if (s.type == 3)
+    cylinderReports(r, p0, p1, r0, s.caps != 0, report);
+  else if (s.type == 4)
+    coneReports(r, p0, r0, p1, r1, report);
+  else
+    curveReports(r, p0, r0, p1, r1, tmin, report);
+}
+
 bool hitBox(const Box &b, const RayPre &r, float tmin, float tmax)
 {
   float t0 = tmin, t1 = tmax;
@@ -669,6 +925,7 @@ struct HitRec
   int surface;
   uint32_t prim;
   bool front;
+  V3 n; // cylinder / cone: the reported object-space normal
 };
 
 float surfOpacity(const OrcSurface &s)
@@ -713,7 +970,39 @@ bool trace(const SceneCtx &S, V3 org, V3 dir, float tmin, float tmax, bool cullR
         const OrcSurface &s = S.sc->surfaces[p.surface];
         float t, u = 0.f, v = 0.f;
         bool front = false, ok;
-        if (s.type == 0) {
+        if (s.type >= 3) {
+          // every report inside [tmin, tmax) is an intersection
+          bool done = false;
+          segmentReports(r, s, p.prim, tmin, [&](float tt, V3 nn, float uu) {
+            if (done || !(tt >= tmin && tt <= tmax))
+              return;
+            if (tt == tmax) {
+              // exact ties within one instance go to the lower (surface,
+              // primitive), as the GPU traversal decides them
+              if (MODE != 0 || !found || hit.inst != ii)
+                return;
+              // (the GPU keeps one structure per primitive class)
+              const OrcSurface &hs = S.sc->surfaces[hit.surface];
+              if (hs.type != s.type)
+                return;
+              if (!(p.surface < hit.surface || (p.surface == hit.surface && p.prim < hit.prim)))
+                return;
+            }
+            if (MODE == 0) {
+              tmax = tt;
+              hit = HitRec{tt, uu, 0.f, ii, p.surface, p.prim, true, nn};
+              found = true;
+            } else {
+              opacity += surfOpacity(s) * (1.f - opacity);
+              if (opacity >= 0.99f)
+                done = true;
+            }
+          });
+          if (MODE == 1 && done)
+            return true;
+          continue;
+        }
+        if (s.type == 0 || s.type == 2) {
           V3 a, b, c;
           triVerts(s, p.prim, a, b, c);
           ok = hitTriangle(r, a, b, c, tmin, tmax, t, u, v, front);
@@ -729,7 +1018,7 @@ bool trace(const SceneCtx &S, V3 org, V3 dir, float tmin, float tmax, bool cullR
           continue;
         if (MODE == 0) {
           tmax = t;
-          hit = HitRec{t, u, v, ii, p.surface, p.prim, front};
+          hit = HitRec{t, u, v, ii, p.surface, p.prim, front, v3(0, 0, 0)};
           found = true;
         } else {
           opacity += surfOpacity(s) * (1.f - opacity);
@@ -863,7 +1152,29 @@ SHit populate(const SceneCtx &S, const Ray &ray, const HitRec &h)
   sh.objId = s.id;
   sh.instId = in.userId;
   V3 Ng, Ns;
-  if (s.type == 0) {
+  if (s.type == 2) {
+    // QUAD case (populateHit.h:267-279)
+    V3 a, b, c;
+    triVerts(s, h.prim, a, b, c);
+    Ng = cross(b - a, c - a);
+    if (!h.front)
+      Ng = -Ng;
+    Ns = Ng;
+  } else if (s.type == 3 || s.type == 4) {
+    Ng = Ns = h.n;
+  } else if (s.type == 5) {
+    // CURVE case with curveSurfaceNormal (curveHelpers.h:91-107)
+    V3 p0, p1;
+    float r0, r1;
+    segmentOf(s, h.prim, p0, r0, p1, r1);
+    const V3 dv = p1 - p0;
+    const float rad = r0 + (r1 - r0) * h.u;
+    const V3 ps = xPoint(S.w2o[h.inst], sh.P);
+    V3 o1 = ps - (p0 + h.u * dv);
+    o1 = o1 - (dot(o1, dv) / dot(dv, dv)) * dv;
+    o1 = o1 * (rad / std::sqrt(dot(o1, o1)));
+    Ng = Ns = normalize(o1);
+  } else if (s.type == 0) {
     V3 a, b, c;
     triVerts(s, h.prim, a, b, c);
     Ng = normalize(cross(b - a, c - a));

@@ -54,13 +54,17 @@ float orc_tex3d(const float *vox, const int dims[3], const float coord[3], int r
 /* --- scene ---------------------------------------------------------------- */
 
 typedef struct OrcSurface {
-  int type; /* 0 triangle, 1 sphere */
+  int type; /* 0 triangle, 1 sphere, 2 quad, 3 cylinder, 4 cone, 5 curve */
   const float *vertices; /* vec3 */
-  const uint32_t *indices; /* uvec3 per triangle or u32 per sphere; NULL */
-  uint32_t numPrims;
+  /* uvec3 per triangle, uvec4 per quad, uvec2 per cylinder / cone, u32 per
+   * sphere / curve; NULL: implicit */
+  const uint32_t *indices;
+  uint32_t numPrims; /* quads count two triangles each */
   const float *normals; /* vertex.normal (vec3) or NULL */
   const uint32_t *primIds; /* primitive.id or NULL */
-  const float *radii; /* sphere per-vertex radius or NULL */
+  /* per-vertex radius (sphere, cone, curve) or per-primitive radius
+   * (cylinder), or NULL */
+  const float *radii;
   float radius;
   int cullBackfaces;
   uint32_t id; /* Surface id */
@@ -68,6 +72,7 @@ typedef struct OrcSurface {
   float opacity;
   int alphaMode; /* 0 opaque, 1 blend, 2 mask */
   float cutoff;
+  int caps; /* cylinder end caps */
 } OrcSurface;
 
 typedef struct OrcInstance {

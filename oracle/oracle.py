@@ -34,7 +34,7 @@ class OrcSurface(C.Structure):
                 ("numPrims", C.c_uint32), ("normals", C.c_void_p), ("primIds", C.c_void_p),
                 ("radii", C.c_void_p), ("radius", C.c_float), ("cullBackfaces", C.c_int),
                 ("id", C.c_uint32), ("color", C.c_float * 3), ("opacity", C.c_float),
-                ("alphaMode", C.c_int), ("cutoff", C.c_float)]
+                ("alphaMode", C.c_int), ("cutoff", C.c_float), ("caps", C.c_int)]
 
 
 class OrcInstance(C.Structure):
@@ -99,6 +99,7 @@ class OrcDMView(C.Structure):
 _RENDERERS = {"default": 0, "directLight": 0, "raycast": 1, "ao": 2, "dpt": 3,
               "diffuse_pathtracer": 3}
 _ALPHA = {"opaque": 0, "blend": 1, "mask": 2}
+_SURFACE_TYPES = {"triangle": 0, "sphere": 1, "quad": 2, "cylinder": 3, "cone": 4, "curve": 5}
 
 
 def _ptr(a):
@@ -166,7 +167,7 @@ def _scene_structs(spec):
     surfs = (OrcSurface * max(1, len(spec.surfaces)))()
     for i, s in enumerate(spec.surfaces):
         o = surfs[i]
-        o.type = 0 if s.type == "triangle" else 1
+        o.type = _SURFACE_TYPES[s.type]
         v = np.ascontiguousarray(s.vertices, np.float32)
         keep.append(v)
         o.vertices = _ptr(v)
@@ -188,6 +189,7 @@ def _scene_structs(spec):
         o.opacity = s.opacity
         o.alphaMode = _ALPHA[s.alpha_mode]
         o.cutoff = s.cutoff
+        o.caps = int(bool(s.caps))
     insts = []
     for ins in spec.instances:
         if not ins.surfaces:

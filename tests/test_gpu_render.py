@@ -179,6 +179,87 @@ def test_albedo_normal_channels(device, renderer):
     assert np.abs(g["normal"]).max() > 0.1
 
 
+def geometry_zoo(kind, seed=3):
+    """A few hundred primitives of one of the geometry subtypes beside
+    triangles and spheres, in a unit-ish cluster in front of the camera."""
+    rng = np.random.default_rng(seed)
+    n = 300
+    if kind == "quad":
+        p0 = rng.uniform(-1, 1, (n, 3))
+        e1 = rng.normal(0, 0.08, (n, 3))
+        e2 = rng.normal(0, 0.08, (n, 3))
+        v = np.stack([p0, p0 + e1, p0 + e1 + e2, p0 + e2], 1).reshape(-1, 3).astype(np.float32)
+        half = n // 2
+        surfs = [S.SurfaceSpec("quad", v[:4 * half], id=31),
+                 # indexed, with the quads' corners listed in another order
+                 S.SurfaceSpec("quad", v[4 * half:], id=32,
+                               indices=(np.arange(4 * (n - half)).reshape(-1, 4)[:, [1, 2, 3, 0]]
+                                        ).astype(np.uint32))]
+    elif kind in ("cylinder", "cone"):
+        a = rng.uniform(-1, 1, (n, 3))
+        b = a + rng.normal(0, 0.15, (n, 3))
+        v = np.stack([a, b], 1).reshape(-1, 3).astype(np.float32)
+        half = n // 2
+        if kind == "cylinder":
+            surfs = [S.SurfaceSpec("cylinder", v[:2 * half], id=41, radius=0.03, caps=True),
+                     S.SurfaceSpec("cylinder", v[2 * half:], id=42,
+                                   radii=rng.uniform(0.01, 0.05, n - half).astype(np.float32),
+                                   caps=False)]
+        else:
+            r = rng.uniform(0.005, 0.06, 2 * n).astype(np.float32)
+            idx = np.arange(2 * (n - half)).reshape(-1, 2)[:, ::-1].astype(np.uint32)
+            surfs = [S.SurfaceSpec("cone", v[:2 * half], id=51, radii=r[:2 * half]),
+                     S.SurfaceSpec("cone", v[2 * half:], id=52, radii=r[2 * half:], indices=idx)]
+    else:  # curve: random-walk strands
+        strands, per = 20, 16
+        pts = []
+        for k in range(strands):
+            p = rng.uniform(-1, 1, 3)
+            for i in range(per):
+                pts.append(p.copy())
+                p = p + rng.normal(0, 0.08, 3)
+        v = np.asarray(pts, np.float32)
+        rad = rng.uniform(0.01, 0.04, len(v)).astype(np.float32)
+        # segments within each strand, by their first vertex
+        idx = np.array([k * per + i for k in range(strands) for i in range(per - 1)], np.uint32)
+        surfs = [S.SurfaceSpec("curve", v, id=61, radii=rad, indices=idx),
+                 # no index: segments 0 .. n/2 - 1 from vertex i to i + 1
+                 S.SurfaceSpec("curve", v[:64] + np.float32(0.3), id=62, radius=0.02)]
+    cam = S.CameraSpec(position=(0.2, 0.3, -4.0), direction=(0.0, -0.05, 1.0),
+                       fovy=math.radians(40), aspect=1.5)
+    return S.SceneSpec(surfs, [S.InstanceSpec(list(range(len(surfs))), zero=True)],
+                       [S.LightSpec(direction=(0.3, -1.0, 0.6))], camera=cam,
+                       renderer=S.RendererSpec("raycast"), width=120, height=80)
+
+
+@pytest.mark.parametrize("kind", ["quad", "cylinder", "cone", "curve"])
+@pytest.mark.parametrize("renderer", ["raycast", "default", "ao"])
+def test_geometry_subtypes(device, kind, renderer):
+    """Quads (two triangles each, Quad.cpp:115-141), cylinders and cones
+    (the reference's intersectors, Intersectors_ptx.cu:100-246) and round
+    linear curves (this library's swept-sphere test) against the oracle:
+    ids, depth, colour and the populated normals through shading."""
+    spec = geometry_zoo(kind)
+    spec.renderer = S.RendererSpec(renderer, ambient_samples=2 if renderer == "ao" else 0,
+                                   pixel_samples=1)
+    g = render_gpu(device, spec)
+    r = render_oracle(spec)
+    if kind == "cone":
+        # The reference's cone test solves a quadratic whose coefficients
+        # are products of squared dot products (k2, k1, k0 ~ |ba|^4): the
+        # cancellation turns a one-ulp difference in the primary ray's
+        # direction (GPU and oracle round the camera arithmetic
+        # differently) into up to ~1e-4 relative in t and in the normal.
+        # Both sides evaluate the test itself without contraction, so ids
+        # still agree.
+        rep = compare(g, r, allow_ids=3, depth_rel=3e-4, color_tol=8)
+    else:
+        rep = compare(g, r, allow_ids=3)
+    hit = g["depth"] < 1e29
+    assert hit.mean() > 0.05, "the primitives cover part of the frame"
+    print(kind, renderer, rep, hit.mean())
+
+
 def test_orthographic(device):
     spec = soup("raycast", n=5000, w=64, h=64)
     spec.camera = S.CameraSpec(type="orthographic", position=(0.5, 0.5, -1.0),

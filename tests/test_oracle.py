@@ -267,3 +267,41 @@ def test_dpt_volume_renders_on_cpu():
                                direction=(0, 0, 1), height=30.0, aspect=1.0)
     out = O.render(spec)
     assert out["rays"] == 16 * 16 and out["accum"][..., :3].max() == 0.0
+
+
+def _one_prim_depth(surf, origin=(0.0, 0.0, -5.0), direction=(0.0, 0.0, 1.0)):
+    cam = S.CameraSpec(type="orthographic", position=origin, direction=direction,
+                       height=1e-3, aspect=1.0)
+    spec = S.SceneSpec([surf], [S.InstanceSpec([0], zero=True)], [], camera=cam,
+                       renderer=S.RendererSpec("raycast"), width=1, height=1, world_id=0)
+    return float(O.render(spec)["depth"][0, 0])
+
+
+def test_segment_and_quad_known_answers():
+    """Single-ray hits on the geometry subtypes beside triangles and spheres:
+    a cylinder across the ray (distance minus radius), its cap disk seen
+    along the axis, a cone's wide end disk, a constant-radius curve segment
+    (a capsule), and a quad (two triangles)."""
+    cyl = S.SurfaceSpec("cylinder", np.array([[-1, 0, 0], [1, 0, 0]], np.float32), radius=0.25)
+    assert abs(_one_prim_depth(cyl) - 4.75) < 1e-5
+    capped = S.SurfaceSpec("cylinder", np.array([[0, 0, 0], [0, 0, 1]], np.float32),
+                           radius=0.25, caps=True)
+    tilt = (0.01, 0.0, 1.0)  # through the cap disk, not parallel to the axis
+    assert abs(_one_prim_depth(capped, direction=tilt) - 5.0 * np.sqrt(1.0001)) < 1e-5
+    open_cyl = S.SurfaceSpec("cylinder", np.array([[0, 0, 0], [0, 0, 1]], np.float32),
+                             radius=0.25, caps=False)
+    assert _one_prim_depth(open_cyl, direction=tilt) > 1e29  # into the open tube
+    # a ray exactly along the axis: (s x d)^2 == 0 ends the reference's test
+    # before the caps (Intersectors_ptx.cu:120-121)
+    assert _one_prim_depth(capped) > 1e29
+    cone = S.SurfaceSpec("cone", np.array([[0, 0, 0], [0, 0, 1]], np.float32),
+                         radii=np.array([0.5, 0.1], np.float32))
+    assert abs(_one_prim_depth(cone) - 5.0) < 1e-5
+    capsule = S.SurfaceSpec("curve", np.array([[-1, 0, 0], [1, 0, 0]], np.float32),
+                            indices=np.array([0], np.uint32), radius=0.3)
+    assert abs(_one_prim_depth(capsule) - 4.7) < 1e-5
+    # the capsule's end ball, seen along the axis
+    assert abs(_one_prim_depth(capsule, origin=(-5.0, 0.0, 0.0), direction=(1, 0, 0)) - 3.7) < 1e-5
+    quad = S.SurfaceSpec("quad", np.array([[-1, -1, 2], [1, -1, 2], [1, 1, 2], [-1, 1, 2]],
+                                          np.float32))
+    assert abs(_one_prim_depth(quad) - 7.0) < 1e-5

@@ -510,16 +510,85 @@ static Array *arrayParam(Object *o, const char *name, int elemType)
   return a;
 }
 
+Geometry::~Geometry()
+{
+  if (quadIndices && Object::dev->initOk)
+    cudaFree(quadIndices);
+}
+
+int Geometry::geomClass() const
+{
+  if (subtype == "sphere")
+    return GEOM_SPHERE;
+  if (subtype == "cylinder")
+    return GEOM_CYLINDER;
+  if (subtype == "cone")
+    return GEOM_CONE;
+  if (subtype == "curve")
+    return GEOM_CURVE;
+  return GEOM_TRIANGLE; // triangle, quad
+}
+
+uint32_t Geometry::kind() const
+{
+  if (subtype == "quad")
+    return KIND_QUAD;
+  if (subtype == "sphere")
+    return KIND_SPHERE;
+  if (subtype == "cylinder")
+    return KIND_CYLINDER;
+  if (subtype == "cone")
+    return KIND_CONE;
+  if (subtype == "curve")
+    return KIND_CURVE;
+  return KIND_TRIANGLE;
+}
+
+// Parameters per subtype: Triangle.cpp, Quad.cpp:40-47, Sphere.cu:45-55,
+// Cylinder.cpp:42-51, Cone.cpp:40-48, Curve.cpp:45-53.
 void Geometry::commit()
 {
   vertex = arrayParam(this, "vertex.position", VRTX_FLOAT32_VEC3);
+  normal = normalFV = radius = index = nullptr;
+  cull = caps = false;
+  const uint32_t nv = vertex ? (uint32_t)vertex->count() : 0;
   if (subtype == "sphere") {
     index = arrayParam(this, "primitive.index", VRTX_UINT32);
     radius = arrayParam(this, "vertex.radius", VRTX_FLOAT32);
     globalRadius = get<float>("radius", VRTX_FLOAT32, 0.01f);
-    normal = normalFV = nullptr;
-    numPrims = index ? (uint32_t)index->count()
-                     : (vertex ? (uint32_t)vertex->count() : 0);
+    numPrims = index ? (uint32_t)index->count() : nv;
+  } else if (subtype == "cylinder") {
+    index = arrayParam(this, "primitive.index", VRTX_UINT32_VEC2);
+    radius = arrayParam(this, "primitive.radius", VRTX_FLOAT32);
+    globalRadius = get<float>("radius", VRTX_FLOAT32, 1.f);
+    caps = getString("caps", "none") != "none";
+    numPrims = index ? (uint32_t)index->count() : nv / 2;
+  } else if (subtype == "cone") {
+    index = arrayParam(this, "primitive.index", VRTX_UINT32_VEC2);
+    radius = arrayParam(this, "vertex.radius", VRTX_FLOAT32);
+    if (!radius)
+      report(VRTX_SEVERITY_WARNING,
+          "missing required parameter 'vertex.radius' on cone geometry");
+    numPrims = index ? (uint32_t)index->count() : nv / 2;
+  } else if (subtype == "curve") {
+    index = arrayParam(this, "primitive.index", VRTX_UINT32);
+    radius = arrayParam(this, "vertex.radius", VRTX_FLOAT32);
+    globalRadius = get<float>("radius", VRTX_FLOAT32, 1.f);
+    // without an index the reference numbers segments 0 .. n/2 - 1, each
+    // from vertex i to i + 1 (Curve.cpp:88-99)
+    numPrims = index ? (uint32_t)index->count() : nv / 2;
+  } else if (subtype == "quad") {
+    index = arrayParam(this, "primitive.index", VRTX_UINT32_VEC4);
+    normal = arrayParam(this, "vertex.normal", VRTX_FLOAT32_VEC3);
+    cull = get<int32_t>("cullBackfaces", VRTX_BOOL, 0) != 0;
+    if (!index && nv % 4 != 0) {
+      report(VRTX_SEVERITY_ERROR,
+          "'vertex.position' on quad geometry is a non-multiple of 4 without "
+          "'primitive.index' present");
+      vertex = nullptr;
+    }
+    // two triangles per quad (Quad.cpp:115-141)
+    numPrims = 2 * (index ? (uint32_t)index->count() : nv / 4);
   } else {
     if (subtype != "triangle")
       report(VRTX_SEVERITY_WARNING,
@@ -528,10 +597,8 @@ void Geometry::commit()
     index = arrayParam(this, "primitive.index", VRTX_UINT32_VEC3);
     normal = arrayParam(this, "vertex.normal", VRTX_FLOAT32_VEC3);
     normalFV = arrayParam(this, "faceVarying.normal", VRTX_FLOAT32_VEC3);
-    radius = nullptr;
     cull = get<int32_t>("cullBackfaces", VRTX_BOOL, 0) != 0;
-    numPrims = index ? (uint32_t)index->count()
-                     : (vertex ? (uint32_t)(vertex->count() / 3) : 0);
+    numPrims = index ? (uint32_t)index->count() : nv / 3;
   }
   primId = arrayParam(this, "primitive.id", VRTX_UINT32);
   if (!vertex)
@@ -542,7 +609,12 @@ void Geometry::commit()
 
 bool Geometry::isValid() const
 {
-  return vertex != nullptr && (subtype == "triangle" || subtype == "sphere");
+  if (!vertex)
+    return false;
+  if (subtype == "cone")
+    return radius != nullptr;
+  return subtype == "triangle" || subtype == "sphere" || subtype == "quad"
+      || subtype == "cylinder" || subtype == "curve";
 }
 
 uint64_t Geometry::deepStamp() const
@@ -558,15 +630,35 @@ GeometryGPU Geometry::gpuData()
 {
   GeometryGPU g{};
   g.type = (uint32_t)geomClass();
+  g.kind = kind();
   g.numPrims = numPrims;
   g.vertices = vertex ? (const f3 *)vertex->deviceData() : nullptr;
   g.indices = index ? (const uint32_t *)index->deviceData() : nullptr;
+  if (g.kind == KIND_QUAD) {
+    const uint64_t want = deepStamp();
+    if (!quadIndices || quadStamp < want) {
+      if (quadIndices)
+        cudaFree(quadIndices);
+      quadIndices = nullptr;
+      if (numPrims
+          && cudaMalloc(&quadIndices, sizeof(uint32_t) * 3 * (size_t)numPrims)
+              == cudaSuccess) {
+        launchQuadIndices(g.indices, numPrims / 2, quadIndices, Object::dev->stream);
+        quadStamp = want;
+      } else {
+        cudaGetLastError();
+        quadIndices = nullptr;
+      }
+    }
+    g.indices = quadIndices;
+  }
   g.normals = normal ? (const f3 *)normal->deviceData() : nullptr;
   g.normalsFV = normalFV ? (const f3 *)normalFV->deviceData() : nullptr;
   g.primIds = primId ? (const uint32_t *)primId->deviceData() : nullptr;
   g.radii = radius ? (const float *)radius->deviceData() : nullptr;
   g.radius = globalRadius;
   g.cullBackfaces = cull ? 1u : 0u;
+  g.caps = caps ? 1u : 0u;
   return g;
 }
 
@@ -1369,10 +1461,11 @@ bool World::rebuild()
   SurfaceGPU *dSurfs = uploadVec(this, hSurfs, s);
 
   // BLAS per (group, primitive class)
-  std::map<Group *, std::array<int, 2>> groupBlas;
+  std::map<Group *, std::array<int, GEOM_NUM_TYPES>> groupBlas;
   std::vector<BLASDesc> hBlas;
   for (Group *g : groups) {
-    std::array<int, 2> ids{-1, -1};
+    std::array<int, GEOM_NUM_TYPES> ids;
+    ids.fill(-1);
     for (int cls = 0; cls < GEOM_NUM_TYPES; cls++) {
       uint32_t n = 0;
       for (Surface *sf : groupSurfaces[g])
@@ -1393,15 +1486,18 @@ bool World::rebuild()
       }
       if (cls == GEOM_TRIANGLE)
         launchTriangleBoxes(dGeoms, refs, dSurfs, n, boxes, s);
-      else
+      else if (cls == GEOM_SPHERE)
         launchSphereBoxes(dGeoms, refs, dSurfs, n, boxes, s);
+      else
+        launchSegmentBoxes(dGeoms, refs, dSurfs, n, boxes, s);
       BLASBuild b;
       b.type = (uint32_t)cls;
       b.numPrims = n;
       cudaError_t err = buildBVH8(boxes, n, s, b.bvh, maxLeaf[cls]);
       if (err == cudaSuccess) {
-        const size_t recBytes =
-            cls == GEOM_TRIANGLE ? sizeof(TriRecord) : sizeof(SphereRecord);
+        const size_t recBytes = cls == GEOM_TRIANGLE
+            ? sizeof(TriRecord)
+            : (cls == GEOM_SPHERE ? sizeof(SphereRecord) : sizeof(SegRecord));
         cudaMallocAsync(&b.records, recBytes * b.bvh.numPrims, s);
         if (cls == GEOM_TRIANGLE)
           launchGatherTriangles(dGeoms,
@@ -1411,13 +1507,21 @@ bool World::rebuild()
               b.bvh.numPrims,
               (TriRecord *)b.records,
               s);
-        else
+        else if (cls == GEOM_SPHERE)
           launchGatherSpheres(dGeoms,
               refs,
               dSurfs,
               b.bvh.primOrder,
               b.bvh.numPrims,
               (SphereRecord *)b.records,
+              s);
+        else
+          launchGatherSegments(dGeoms,
+              refs,
+              dSurfs,
+              b.bvh.primOrder,
+              b.bvh.numPrims,
+              (SegRecord *)b.records,
               s);
       }
       cudaFreeAsync(refs, s);

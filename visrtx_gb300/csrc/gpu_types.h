@@ -15,26 +15,49 @@ namespace vrtx {
 // Scene registries
 // ---------------------------------------------------------------------------
 
+// Primitive classes, one bottom-level structure each per group (the
+// reference builds one GAS per class: triangles, curves, user primitives).
+// Cylinders and cones are user primitives there; here each has its own
+// structure because its leaf records and test differ.
 enum GeomType : uint32_t
 {
-  GEOM_TRIANGLE = 0,
+  GEOM_TRIANGLE = 0, // triangles and quads
   GEOM_SPHERE = 1,
-  GEOM_NUM_TYPES = 2
+  GEOM_CYLINDER = 2,
+  GEOM_CONE = 3,
+  GEOM_CURVE = 4, // round linear curve segments
+  GEOM_NUM_TYPES = 5
+};
+
+// Geometry subtype, where it changes the hit population
+enum GeomKind : uint32_t
+{
+  KIND_TRIANGLE = 0,
+  KIND_QUAD = 1,
+  KIND_SPHERE = 2,
+  KIND_CYLINDER = 3,
+  KIND_CONE = 4,
+  KIND_CURVE = 5
 };
 
 struct GeometryGPU
 {
-  uint32_t type;
+  uint32_t type; // GeomType (the class)
   uint32_t numPrims;
-  const f3 *vertices; // triangle: vertex.position; sphere: vertex.position
+  const f3 *vertices; // vertex.position
   const uint32_t *indices; // triangle: uvec3 per prim or NULL (soup);
-                           // sphere: primitive.index or NULL
+                           // quad: the generated uvec3 pairs (Quad.cpp:
+                           // 115-141); sphere / curve: primitive.index or
+                           // NULL; cylinder / cone: uvec2 per prim or NULL
   const f3 *normals; // triangle vertex.normal or NULL
   const f3 *normalsFV; // triangle faceVarying.normal or NULL
   const uint32_t *primIds; // primitive.id or NULL
-  const float *radii; // sphere vertex.radius or NULL
-  float radius; // sphere uniform radius (default 0.01, Sphere.cu:52)
+  const float *radii; // sphere / cone / curve vertex.radius, cylinder
+                      // primitive.radius, or NULL
+  float radius; // uniform radius (sphere 0.01, cylinder / curve 1)
   uint32_t cullBackfaces; // VISRTX_TRIANGLE_BACK_FACE_CULLING extension
+  uint32_t kind; // GeomKind
+  uint32_t caps; // cylinder "caps" != "none"
 };
 
 enum AlphaMode : int
@@ -115,11 +138,22 @@ struct alignas(16) SphereRecord
   uint32_t pad[2];
 };
 
-// One bottom-level structure: a group's triangles or a group's spheres.
+// Cylinder / cone / curve leaf record: a segment with its end radii.
+struct alignas(16) SegRecord
+{
+  float4 a; // p0, radius at p0 (cylinder: its one radius)
+  float4 b; // p1, radius at p1
+  uint32_t primID; // primitive index within the geometry
+  uint32_t surface; // global surface index
+  uint32_t caps; // cylinder end caps
+  uint32_t pad;
+};
+
+// One bottom-level structure: one primitive class of a group.
 struct BLASDesc
 {
   const BVH8Node *nodes;
-  const void *prims; // TriRecord* or SphereRecord*
+  const void *prims; // TriRecord*, SphereRecord* or SegRecord*
   uint32_t type; // GeomType
   uint32_t numPrims;
   box3 bounds;

@@ -145,18 +145,21 @@ struct Camera : Object
 struct Geometry : Object
 {
   using Object::Object;
+  ~Geometry() override;
   Array *vertex = nullptr, *index = nullptr, *normal = nullptr,
         *normalFV = nullptr, *primId = nullptr, *radius = nullptr;
   float globalRadius = 0.01f;
   bool cull = false;
+  bool caps = false;
   uint32_t numPrims = 0;
+  // quads: generated triangle indices (2 per quad) on the device
+  uint32_t *quadIndices = nullptr;
+  uint64_t quadStamp = 0;
   void commit() override;
   bool isValid() const override;
   uint64_t deepStamp() const override;
-  int geomClass() const
-  {
-    return subtype == "sphere" ? GEOM_SPHERE : GEOM_TRIANGLE;
-  }
+  int geomClass() const;
+  uint32_t kind() const;
   GeometryGPU gpuData();
 };
 
@@ -285,7 +288,7 @@ struct World : Object
   Array *zeroSurfaces = nullptr, *zeroVolumes = nullptr, *zeroLights = nullptr;
   uint32_t id = ~0u;
   Group *zeroGroup = nullptr;
-  int maxLeaf[GEOM_NUM_TYPES] = {1, 1}; // single-primitive leaves: tight leaf boxes
+  int maxLeaf[GEOM_NUM_TYPES] = {1, 1, 1, 1, 1}; // single-primitive leaves
   Instance *zeroInstance = nullptr;
 
   // built state

@@ -150,33 +150,42 @@ __device__ __forceinline__ void populateSurfaceHit(
     const f3 v0 = mk3(tr.v0.x, tr.v0.y, tr.v0.z);
     const f3 v1 = mk3(tr.v1.x, tr.v1.y, tr.v1.z);
     const f3 v2 = mk3(tr.v2.x, tr.v2.y, tr.v2.z);
-    Ng = normalize(cross(v1 - v0, v2 - v0));
-    if (!h.front)
-      Ng = -Ng;
     const GeometryGPU &g = w.geometries[w.surfaces[sh.surface].geometry];
-    const float b0 = 1.f - h.u - h.v, b1 = h.u, b2 = h.v;
-    if (g.normalsFV) {
-      const uint32_t i0 = sh.primID * 3;
-      Ns = b0 * g.normalsFV[i0] + b1 * g.normalsFV[i0 + 1]
-          + b2 * g.normalsFV[i0 + 2];
-    } else if (g.normals) {
-      uint32_t i0, i1, i2;
-      if (g.indices) {
-        i0 = g.indices[3 * sh.primID];
-        i1 = g.indices[3 * sh.primID + 1];
-        i2 = g.indices[3 * sh.primID + 2];
-      } else {
-        i0 = 3 * sh.primID;
-        i1 = i0 + 1;
-        i2 = i0 + 2;
-      }
-      Ns = b0 * g.normals[i0] + b1 * g.normals[i1] + b2 * g.normals[i2];
-    } else
+    if (g.kind == KIND_QUAD) {
+      // QUAD case (populateHit.h:267-279): unnormalised face normal, no
+      // vertex normals
+      Ng = cross(v1 - v0, v2 - v0);
+      if (!h.front)
+        Ng = -Ng;
       Ns = Ng;
-    Ns = normalize(Ns);
-    if (dot(Ng, Ns) < 0.f)
-      Ns = -Ns;
-  } else {
+    } else {
+      Ng = normalize(cross(v1 - v0, v2 - v0));
+      if (!h.front)
+        Ng = -Ng;
+      const float b0 = 1.f - h.u - h.v, b1 = h.u, b2 = h.v;
+      if (g.normalsFV) {
+        const uint32_t i0 = sh.primID * 3;
+        Ns = b0 * g.normalsFV[i0] + b1 * g.normalsFV[i0 + 1]
+            + b2 * g.normalsFV[i0 + 2];
+      } else if (g.normals) {
+        uint32_t i0, i1, i2;
+        if (g.indices) {
+          i0 = g.indices[3 * sh.primID];
+          i1 = g.indices[3 * sh.primID + 1];
+          i2 = g.indices[3 * sh.primID + 2];
+        } else {
+          i0 = 3 * sh.primID;
+          i1 = i0 + 1;
+          i2 = i0 + 2;
+        }
+        Ns = b0 * g.normals[i0] + b1 * g.normals[i1] + b2 * g.normals[i2];
+      } else
+        Ns = Ng;
+      Ns = normalize(Ns);
+      if (dot(Ng, Ns) < 0.f)
+        Ns = -Ns;
+    }
+  } else if (blas.type == GEOM_SPHERE) {
     const SphereRecord sr =
         reinterpret_cast<const SphereRecord *>(blas.prims)[h.rec];
     sh.primID = sr.primID;
@@ -185,6 +194,25 @@ __device__ __forceinline__ void populateSurfaceHit(
     const f3 ld = xfmVector(inst.worldToObject, ray.dir);
     const f3 hp = lo + h.t * ld;
     Ng = Ns = hp - mk3(sr.cr.x, sr.cr.y, sr.cr.z);
+  } else {
+    const SegRecord sr = reinterpret_cast<const SegRecord *>(blas.prims)[h.rec];
+    sh.primID = sr.primID;
+    sh.surface = sr.surface;
+    if (blas.type == GEOM_CURVE) {
+      // CURVE case (populateHit.h:292-303) with curveSurfaceNormal
+      // (gpu/curveHelpers.h:91-107) at the object-space hit point
+      const f3 p0 = mk3(sr.a.x, sr.a.y, sr.a.z);
+      const f3 d = mk3(sr.b.x, sr.b.y, sr.b.z) - p0;
+      const float rad = sr.a.w + (sr.b.w - sr.a.w) * h.u;
+      const f3 ps = xfmPoint(inst.worldToObject, sh.hitpoint);
+      f3 o1 = ps - (p0 + h.u * d);
+      o1 = o1 - (dot(o1, d) / dot(d, d)) * d;
+      o1 = o1 * (rad / sqrtf(dot(o1, o1)));
+      Ng = Ns = normalize(o1);
+    } else {
+      // SPHERE / CONE / CYLINDER case: the intersector's normal attribute
+      Ng = Ns = h.n;
+    }
   }
   sh.Ng = normalize(xfmNormalTransposed(inst.worldToObject, Ng));
   sh.Ns = normalize(xfmNormalTransposed(inst.worldToObject, Ns));

@@ -55,6 +55,23 @@ cudaError_t launchGatherSpheres(const GeometryGPU *geoms,
     cudaStream_t s);
 cudaError_t launchFillRefs(uint32_t surface, uint32_t count, uint2 *out,
     cudaStream_t s);
+// cylinders, cones and curves
+cudaError_t launchSegmentBoxes(const GeometryGPU *geoms,
+    const uint2 *refs,
+    const SurfaceGPU *surfaces,
+    uint32_t n,
+    box3 *boxes,
+    cudaStream_t s);
+cudaError_t launchGatherSegments(const GeometryGPU *geoms,
+    const uint2 *refs,
+    const SurfaceGPU *surfaces,
+    const uint32_t *order,
+    uint32_t n,
+    SegRecord *out,
+    cudaStream_t s);
+// two triangles per quad (idx4: uvec4 per quad or NULL)
+cudaError_t launchQuadIndices(
+    const uint32_t *idx4, uint32_t numQuads, uint32_t *out, cudaStream_t s);
 
 // Conservative macrocell majorants of a structured-regular field through a
 // TF table (scene.cu). Cells are 16^3 voxels from the origin; a cell's value

@@ -118,6 +118,120 @@ __global__ void k_gatherSpheres(const GeometryGPU *geoms,
   out[i] = s;
 }
 
+// The segment of a cylinder, cone or curve primitive: end points and end
+// radii, indexed as the reference's intersectors and hit population read
+// them (Intersectors_ptx.cu:100-246, populateHit.h:292-303): cylinders and
+// cones take a uvec2 per primitive (default 2i, 2i + 1), curves the index of
+// the first vertex (default i); a cylinder has one |radius| per primitive or
+// the uniform one, a cone per-vertex radii, a curve per-vertex radii or the
+// uniform one (Curve.cpp:101-113).
+__device__ __forceinline__ void segmentOf(
+    const GeometryGPU &g, uint32_t prim, f3 &p0, float &r0, f3 &p1, float &r1)
+{
+  uint32_t i0, i1;
+  if (g.kind == KIND_CURVE) {
+    i0 = g.indices ? g.indices[prim] : prim;
+    i1 = i0 + 1;
+  } else {
+    i0 = g.indices ? g.indices[2 * prim] : 2 * prim;
+    i1 = g.indices ? g.indices[2 * prim + 1] : 2 * prim + 1;
+  }
+  p0 = g.vertices[i0];
+  p1 = g.vertices[i1];
+  if (g.kind == KIND_CYLINDER) {
+    r0 = r1 = fabsf(g.radii ? g.radii[prim] : g.radius);
+  } else if (g.kind == KIND_CONE) {
+    r0 = g.radii[i0];
+    r1 = g.radii[i1];
+  } else {
+    r0 = g.radii ? g.radii[i0] : g.radius;
+    r1 = g.radii ? g.radii[i1] : g.radius;
+  }
+}
+
+// Boxes as Cylinder.cpp:91-98 and Cone.cpp:95-103 build them; a curve
+// segment's box encloses its two end spheres.
+__global__ void k_segBoxes(const GeometryGPU *geoms,
+    const uint2 *refs,
+    const SurfaceGPU *surfaces,
+    uint32_t n,
+    box3 *boxes)
+{
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n)
+    return;
+  const uint2 r = refs[i];
+  const GeometryGPU &g = geoms[surfaces[r.x].geometry];
+  f3 p0, p1;
+  float r0, r1;
+  segmentOf(g, r.y, p0, r0, p1, r1);
+  box3 b;
+  if (g.kind == KIND_CURVE) {
+    const f3 e0 = mk3(r0, r0, r0), e1 = mk3(r1, r1, r1);
+    b.lo = fmin3(p0 - e0, p1 - e1);
+    b.hi = fmax3(p0 + e0, p1 + e1);
+  } else {
+    const float m = fmaxf(r0, r1);
+    const f3 e = mk3(m, m, m);
+    b.lo = fmin3(p0, p1) - e;
+    b.hi = fmax3(p0, p1) + e;
+  }
+  boxes[i] = b;
+}
+
+__global__ void k_gatherSegs(const GeometryGPU *geoms,
+    const uint2 *refs,
+    const SurfaceGPU *surfaces,
+    const uint32_t *order,
+    uint32_t n,
+    SegRecord *out)
+{
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n)
+    return;
+  const uint2 r = refs[order[i]];
+  const GeometryGPU &g = geoms[surfaces[r.x].geometry];
+  f3 p0, p1;
+  float r0, r1;
+  segmentOf(g, r.y, p0, r0, p1, r1);
+  SegRecord rec;
+  rec.a = make_float4(p0.x, p0.y, p0.z, r0);
+  rec.b = make_float4(p1.x, p1.y, p1.z, r1);
+  rec.primID = r.y;
+  rec.surface = r.x;
+  rec.caps = g.caps;
+  rec.pad = 0;
+  out[i] = rec;
+}
+
+// Quad.cpp:115-141: quad (x, y, z, w) -> triangles (x, y, w), (z, w, y);
+// without an index, quad i uses vertices 4i .. 4i + 3
+__global__ void k_quadIndices(const uint32_t *idx4, uint32_t numQuads, uint32_t *out)
+{
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= numQuads)
+    return;
+  uint32_t x, y, z, w;
+  if (idx4) {
+    x = idx4[4 * i];
+    y = idx4[4 * i + 1];
+    z = idx4[4 * i + 2];
+    w = idx4[4 * i + 3];
+  } else {
+    x = 4 * i;
+    y = x + 1;
+    z = x + 2;
+    w = x + 3;
+  }
+  uint32_t *o = out + 6 * (size_t)i;
+  o[0] = x;
+  o[1] = y;
+  o[2] = w;
+  o[3] = z;
+  o[4] = w;
+  o[5] = y;
+}
+
 __global__ void k_fillRefs(uint32_t surface, uint32_t count, uint2 *out)
 {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -413,6 +527,39 @@ cudaError_t launchSphereBoxes(const GeometryGPU *geoms,
 {
   if (n)
     k_sphereBoxes<<<(n + 255) / 256, 256, 0, s>>>(geoms, refs, surfaces, n, boxes);
+  return cudaGetLastError();
+}
+
+cudaError_t launchSegmentBoxes(const GeometryGPU *geoms,
+    const uint2 *refs,
+    const SurfaceGPU *surfaces,
+    uint32_t n,
+    box3 *boxes,
+    cudaStream_t s)
+{
+  if (n)
+    k_segBoxes<<<(n + 255) / 256, 256, 0, s>>>(geoms, refs, surfaces, n, boxes);
+  return cudaGetLastError();
+}
+
+cudaError_t launchGatherSegments(const GeometryGPU *geoms,
+    const uint2 *refs,
+    const SurfaceGPU *surfaces,
+    const uint32_t *order,
+    uint32_t n,
+    SegRecord *out,
+    cudaStream_t s)
+{
+  if (n)
+    k_gatherSegs<<<(n + 255) / 256, 256, 0, s>>>(geoms, refs, surfaces, order, n, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launchQuadIndices(
+    const uint32_t *idx4, uint32_t numQuads, uint32_t *out, cudaStream_t s)
+{
+  if (numQuads)
+    k_quadIndices<<<(numQuads + 255) / 256, 256, 0, s>>>(idx4, numQuads, out);
   return cudaGetLastError();
 }
 

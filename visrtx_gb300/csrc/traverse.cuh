@@ -32,6 +32,7 @@ struct Hit
   uint32_t inst; // TLAS leaf (InstanceRecord) index
   uint32_t rec; // primitive record index in the instance's BLAS
   uint32_t front; // triangle front-face hit
+  f3 n; // cylinder / cone: the reported object-space normal
 };
 
 struct TravRay
@@ -282,6 +283,305 @@ __device__ __forceinline__ bool intersectSphere(
   return true;
 }
 
+// ---------------------------------------------------------------------------
+// Segment primitives. Each test calls report(t, normal, u) for every
+// intersection the reference's program would report, in its order; the
+// caller applies the [tmin, tmax) filter (optixReportIntersection's) and
+// keeps the closest (closest hit) or accumulates each (any hit).
+// ---------------------------------------------------------------------------
+
+// Arithmetic of the segment tests: every operation rounded on its own (no
+// fused multiply-add), in the order the source expressions give, so that
+// the results do not depend on the compiler's contraction choices. (The
+// cone's quartic-derived coefficients cancel heavily; a contracted and a
+// plain evaluation can disagree in the fourth digit of t.)
+namespace seg {
+__device__ __forceinline__ float xmul(float a, float b)
+{
+  return __fmul_rn(a, b);
+}
+__device__ __forceinline__ float xadd(float a, float b)
+{
+  return __fadd_rn(a, b);
+}
+__device__ __forceinline__ float xsub(float a, float b)
+{
+  return __fsub_rn(a, b);
+}
+__device__ __forceinline__ float xdiv(float a, float b)
+{
+  return __fdiv_rn(a, b);
+}
+__device__ __forceinline__ float xsqrt(float a)
+{
+  return __fsqrt_rn(a);
+}
+__device__ __forceinline__ f3 xsub(f3 a, f3 b)
+{
+  return mk3(xsub(a.x, b.x), xsub(a.y, b.y), xsub(a.z, b.z));
+}
+__device__ __forceinline__ f3 xadd(f3 a, f3 b)
+{
+  return mk3(xadd(a.x, b.x), xadd(a.y, b.y), xadd(a.z, b.z));
+}
+__device__ __forceinline__ f3 xmul(f3 a, float s)
+{
+  return mk3(xmul(a.x, s), xmul(a.y, s), xmul(a.z, s));
+}
+__device__ __forceinline__ f3 xdiv(f3 a, float s)
+{
+  return mk3(xdiv(a.x, s), xdiv(a.y, s), xdiv(a.z, s));
+}
+__device__ __forceinline__ f3 xneg(f3 a)
+{
+  return mk3(-a.x, -a.y, -a.z);
+}
+__device__ __forceinline__ float xdot(f3 a, f3 b)
+{
+  return xadd(xadd(xmul(a.x, b.x), xmul(a.y, b.y)), xmul(a.z, b.z));
+}
+__device__ __forceinline__ f3 xcross(f3 a, f3 b)
+{
+  return mk3(xsub(xmul(a.y, b.z), xmul(a.z, b.y)),
+      xsub(xmul(a.z, b.x), xmul(a.x, b.z)),
+      xsub(xmul(a.x, b.y), xmul(a.y, b.x)));
+}
+__device__ __forceinline__ f3 xnorm(f3 v)
+{
+  return xmul(v, xdiv(1.f, xsqrt(xdot(v, v))));
+}
+} // namespace seg
+
+// intersectCylinder (scene/Intersectors_ptx.cu:100-175): the side entry and
+// exit between the end planes, then with caps the nearer cap disk.
+template <typename F>
+__device__ __forceinline__ void cylinderReports(
+    const TravRay &r, float4 A, float4 B, bool caps, F &&report)
+{
+  using namespace seg;
+  const f3 p0 = mk3(A.x, A.y, A.z), p1 = mk3(B.x, B.y, B.z);
+  const float radius = A.w;
+  const f3 ro = r.org, rd = r.dir;
+  const f3 s = xsub(p1, p0);
+  const f3 sxd = xcross(s, rd);
+  const float a = xdot(sxd, sxd);
+  if (a == 0.f)
+    return;
+  const f3 f = xsub(p0, ro);
+  const f3 sxf = xcross(s, f);
+  const float ra = xdiv(1.f, a);
+  const float ts = xmul(xdot(sxd, sxf), ra);
+  const f3 fp = xsub(f, xmul(rd, ts));
+  const float s2 = xdot(s, s);
+  const f3 perp = xcross(s, fp);
+  const float c = xsub(xmul(xmul(radius, radius), s2), xdot(perp, perp));
+  if (c < 0.f)
+    return;
+  const float td = xsqrt(xmul(c, ra));
+  const float tin = xsub(ts, td);
+  const float tout = xadd(ts, td);
+  const float sf = xdot(s, f);
+  const float sd = xdot(s, rd);
+  const float is2 = xdiv(1.f, s2);
+  const float u_in = xmul(xsub(xmul(tin, sd), sf), is2);
+  const f3 N_in = xsub(xsub(xmul(rd, -td), fp), xmul(s, u_in));
+  const float u_out = xmul(xsub(xmul(tout, sd), sf), is2);
+  const f3 N_out = xsub(xsub(xmul(rd, td), fp), xmul(s, u_out));
+  if (sd != 0.f) {
+    const float rsd = xdiv(1.f, sd);
+    const float tA = xmul(sf, rsd);
+    const float tB = xadd(tA, xmul(s2, rsd));
+    const float capIn = fminf(tA, tB);
+    const float capOut = fmaxf(tA, tB);
+    if (tin > capIn && tin < capOut)
+      report(tin, N_in, u_in);
+    if (tout > capIn && tout < capOut)
+      report(tout, N_out, u_out);
+  } else if (sf <= 0.f && sf >= -s2) {
+    report(tin, N_in, u_in);
+    report(tout, N_out, u_out);
+  }
+  if (caps) {
+    const f3 nf = xneg(f);
+    const float ca = xsub(s2, xmul(sd, sd));
+    const float cb = xadd(xmul(s2, xdot(nf, rd)), xmul(sf, sd));
+    const float cc =
+        xsub(xsub(xmul(s2, xdot(nf, nf)), xmul(sf, sf)), xmul(xmul(radius, radius), s2));
+    float h = xsub(xmul(cb, cb), xmul(ca, cc));
+    if (h < 0.f)
+      return;
+    h = xsqrt(h);
+    const float y = xsub(xmul(xdiv(xsub(-cb, h), ca), sd), sf);
+    const float d = xdiv(xadd(y < 0.f ? 0.f : s2, sf), sd);
+    if (fabsf(xadd(cb, xmul(ca, d))) < h) {
+      const float sg = y > 0.f ? 1.f : (y < 0.f ? -1.f : 0.f);
+      report(d, xdiv(xmul(s, sg), s2), y < 0.f ? 0.f : 1.f);
+    }
+  }
+}
+
+// intersectCone (scene/Intersectors_ptx.cu:177-246): the end disk on the
+// ray's side (reported first), then the lateral surface.
+template <typename F>
+__device__ __forceinline__ void coneReports(const TravRay &r, float4 A, float4 B, F &&report)
+{
+  using namespace seg;
+  const f3 p0 = mk3(A.x, A.y, A.z), p1 = mk3(B.x, B.y, B.z);
+  const float ra = A.w, rb = B.w;
+  const f3 ro = r.org, rd = r.dir;
+  const f3 ba = xsub(p1, p0);
+  const f3 oa = xsub(ro, p0);
+  const f3 ob = xsub(ro, p1);
+  const float m0 = xdot(ba, ba);
+  const float m1 = xdot(oa, ba);
+  const float m2 = xdot(ob, ba);
+  const float m3 = xdot(rd, ba);
+  if (m1 < 0.f) {
+    const f3 q = xsub(xmul(oa, m3), xmul(rd, m1));
+    if (xdot(q, q) < xmul(xmul(xmul(ra, ra), m3), m3))
+      report(xdiv(-m1, m3), xmul(xneg(ba), xdiv(1.f, xsqrt(m0))), 0.f);
+  } else if (m2 > 0.f) {
+    const f3 q = xsub(xmul(ob, m3), xmul(rd, m2));
+    if (xdot(q, q) < xmul(xmul(xmul(rb, rb), m3), m3))
+      report(xdiv(-m2, m3), xmul(ba, xdiv(1.f, xsqrt(m0))), 1.f);
+  }
+  const float m4 = xdot(rd, oa);
+  const float m5 = xdot(oa, oa);
+  const float rr = xsub(ra, rb);
+  const float hy = xadd(m0, xmul(rr, rr));
+  const float m00 = xmul(m0, m0);
+  const float k2 = xsub(m00, xmul(xmul(m3, m3), hy));
+  const float k1 = xadd(xsub(xmul(m00, m4), xmul(xmul(m1, m3), hy)), xmul(xmul(m0, ra), xmul(xmul(rr, m3), 1.0f)));
+  const float k0 = xadd(xsub(xmul(m00, m5), xmul(xmul(m1, m1), hy)),
+      xmul(xmul(m0, ra), xsub(xmul(xmul(rr, m1), 2.0f), xmul(m0, ra))));
+  const float h = xsub(xmul(k1, k1), xmul(k2, k0));
+  if (h < 0.f)
+    return;
+  const float t = xdiv(xsub(-k1, xsqrt(h)), k2);
+  const float y = xadd(m1, xmul(t, m3));
+  if (y > 0.f && y < m0) {
+    const f3 pt = xadd(oa, xmul(rd, t));
+    const f3 n = xsub(xmul(xadd(xmul(pt, m0), xmul(xmul(ba, rr), ra)), m0), xmul(xmul(ba, hy), y));
+    report(t, xnorm(n), xdiv(y, m0));
+  }
+}
+
+// Round linear curve segment (OPTIX_PRIMITIVE_TYPE_ROUND_LINEAR, whose test
+// is closed): the solid swept by a sphere whose radius varies linearly from
+// (p0, r0) to (p1, r1), i.e. the two end balls joined by their tangent cone.
+// A ray from outside enters this union where it first enters one of its
+// convex parts, so the entry is the smallest of the two balls' near roots
+// and the tangent cone's entry root (axial range between the tangent
+// circles, correct nappe, crossing inwards) at or after tmin. One report, at
+// that entry; a ray starting inside the solid reports nothing (like the
+// sphere test). u is the hit's position between the tangent circles (0 / 1
+// on the end balls).
+template <typename F>
+__device__ __forceinline__ void curveReports(
+    const TravRay &r, float4 A, float4 B, float tmin, F &&report)
+{
+  using namespace seg;
+  const f3 pa = mk3(A.x, A.y, A.z), pb = mk3(B.x, B.y, B.z);
+  const float ra = A.w, rb = B.w;
+  const f3 d = r.dir;
+  const float dd = xdot(d, d);
+  // the tangent cone is solved from the ray point closest to pa (a
+  // well-conditioned quadratic); t = shift + the local root
+  const float shift = xdiv(xdot(xsub(pa, r.org), d), dd);
+  const f3 o = xadd(r.org, xmul(d, shift));
+  const f3 ba = xsub(pb, pa);
+  const float L2 = xdot(ba, ba);
+  const f3 oa = xsub(o, pa), ob = xsub(o, pb);
+  float best = 3.0e38f, bestU = 0.f;
+  // a ray starting inside the solid reports nothing
+  {
+    const f3 oa0 = xsub(r.org, pa), ob0 = xsub(r.org, pb);
+    if (xdot(oa0, oa0) < xmul(ra, ra) || xdot(ob0, ob0) < xmul(rb, rb))
+      return;
+    const float Lq = xsqrt(L2);
+    if (L2 > 0.f) {
+      const float sn = xdiv(xsub(ra, rb), Lq);
+      const float c2 = xsub(1.f, xmul(sn, sn));
+      const f3 w0 = xdiv(ba, Lq);
+      const float z = xdot(oa0, w0);
+      const f3 q = xsub(oa0, xmul(w0, z));
+      const float A = xsub(ra, xmul(sn, z));
+      if (c2 > 0.f && z >= xmul(ra, sn) && z <= xadd(Lq, xmul(rb, sn)) && A >= 0.f
+          && xmul(c2, xdot(q, q)) < xmul(A, A))
+        return;
+    }
+  }
+  // End balls, each solved from the ray point closest to its own centre, so
+  // that two segments sharing a ball compute the same t for it (exact ties,
+  // decided by the caller).
+  auto ball = [&](f3 c, float rad, float u) {
+    const float sc = xdiv(xdot(xsub(c, r.org), d), dd);
+    const f3 oc = xsub(xadd(r.org, xmul(d, sc)), c);
+    const float bq = xdot(oc, d), cq = xsub(xdot(oc, oc), xmul(rad, rad));
+    const float disc = xsub(xmul(bq, bq), xmul(dd, cq));
+    if (disc < 0.f)
+      return;
+    const float t = xadd(sc, xdiv(xsub(-bq, xsqrt(disc)), dd));
+    if (t < best && t >= tmin) {
+      best = t;
+      bestU = u;
+    }
+  };
+  ball(pa, ra, 0.f);
+  ball(pb, rb, 1.f);
+  const float L = xsqrt(L2);
+  const float sinp = xdiv(xsub(ra, rb), L);
+  const float cos2 = xsub(1.f, xmul(sinp, sinp));
+  if (L2 > 0.f && cos2 > 0.f) {
+    const f3 w = xdiv(ba, L);
+    const float z0 = xdot(oa, w), dz = xdot(d, w);
+    const f3 q0 = xsub(oa, xmul(w, z0)), dq = xsub(d, xmul(w, dz));
+    const float zA = xmul(ra, sinp), zB = xadd(L, xmul(rb, sinp));
+    const float A0 = xsub(ra, xmul(sinp, z0)), A1 = xmul(-sinp, dz);
+    const float qq = xdot(q0, q0);
+    const float a = xsub(xmul(cos2, xdot(dq, dq)), xmul(A1, A1));
+    const float b = xsub(xmul(cos2, xdot(q0, dq)), xmul(A0, A1));
+    const float c = xsub(xmul(cos2, qq), xmul(A0, A0));
+    const float disc = xsub(xmul(b, b), xmul(a, c));
+    if (a != 0.f && disc >= 0.f) {
+      const float sq = xsqrt(disc);
+      const float t0 = xdiv(xsub(-b, sq), a), t1 = xdiv(xadd(-b, sq), a);
+      for (int k = 0; k < 2; k++) {
+        const float t = k == 0 ? fminf(t0, t1) : fmaxf(t0, t1);
+        const float z = xadd(z0, xmul(t, dz));
+        const float tg = xadd(shift, t);
+        if (xadd(xmul(a, t), b) < 0.f && z >= zA && z <= zB && xadd(A0, xmul(A1, t)) >= 0.f
+            && tg < best && tg >= tmin) {
+          best = tg;
+          bestU = xdiv(xsub(z, zA), xsub(zB, zA));
+        }
+      }
+    }
+  }
+  if (best < 3.0e38f) {
+    // the reference's normal (curveSurfaceNormal) depends on the hit point
+    // only; the hit population computes it
+    report(best, mk3(0.f, 0.f, 0.f), bestU);
+  }
+}
+
+// Dispatch over a segment record; `cls` is the BLAS class. (tmin: the curve
+// test looks for the first entry at or after it.)
+template <typename F>
+__device__ __forceinline__ void segmentReports(
+    const TravRay &r, uint32_t cls, const float4 *rec, float tmin, F &&report)
+{
+  const float4 A = __ldg(rec), B = __ldg(rec + 1);
+  if (cls == GEOM_CYLINDER) {
+    const uint32_t caps = __ldg(reinterpret_cast<const uint32_t *>(rec + 2) + 2);
+    cylinderReports(r, A, B, caps != 0u, report);
+  } else if (cls == GEOM_CONE) {
+    coneReports(r, A, B, report);
+  } else {
+    curveReports(r, A, B, tmin, report);
+  }
+}
+
 __device__ __forceinline__ void toObject(
     TravRay &r, const InstanceRecord *inst, f3 worldOrg, f3 worldDir)
 {
@@ -408,7 +708,7 @@ __device__ __forceinline__ bool traverse(const WorldGPU &w,
               && MODE == 0)
             hitPrim = false;
           surface = __float_as_uint(bb.w);
-        } else {
+        } else if (blasType == GEOM_SPHERE) {
           const SphereRecord *sp4 =
               reinterpret_cast<const SphereRecord *>(prims) + rec;
           const float4 cr = __ldg(&sp4->cr);
@@ -416,6 +716,52 @@ __device__ __forceinline__ bool traverse(const WorldGPU &w,
             stats->spheres++;
           hitPrim = intersectSphere(r, cr, tmin, tmax, t);
           surface = __ldg(&sp4->surface);
+        } else {
+          // cylinder / cone / curve: every report inside [tmin, tmax) is an
+          // intersection; closest hit keeps the nearest, any hit
+          // accumulates each
+          const float4 *sr = reinterpret_cast<const float4 *>(prims) + (size_t)rec * 3;
+          if (stats)
+            stats->spheres++;
+          const uint32_t segSurface = __ldg(reinterpret_cast<const uint32_t *>(sr + 2) + 1);
+          bool done = false;
+          const uint32_t segPrim = __ldg(reinterpret_cast<const uint32_t *>(sr + 2));
+          segmentReports(r, blasType, sr, tmin, [&](float tt, f3 n, float uu) {
+            if (done || !(tt >= tmin && tt <= tmax))
+              return;
+            if (tt == tmax) {
+              // Exact ties (curve segments meeting in a shared end ball
+              // report the same t) go to the lower (surface, primitive) of
+              // the same instance, so the result does not depend on the
+              // traversal order. Anything else keeps the earlier hit.
+              if (MODE != 0 || !found || hit.inst != instIdx)
+                return;
+              const uint32_t *cur = reinterpret_cast<const uint32_t *>(
+                  reinterpret_cast<const float4 *>(prims) + (size_t)hit.rec * 3 + 2);
+              const uint32_t cPrim = __ldg(cur), cSurf = __ldg(cur + 1);
+              if (!(segSurface < cSurf || (segSurface == cSurf && segPrim < cPrim)))
+                return;
+            }
+            if (MODE == 0) {
+              tmax = tt;
+              hit.t = tt;
+              hit.u = uu;
+              hit.v = 0.f;
+              hit.n = n;
+              hit.inst = instIdx;
+              hit.rec = rec;
+              hit.front = 1u;
+              found = true;
+            } else {
+              const float o = w.allOpaque ? 1.f : surfaceOpacity(w, segSurface);
+              opacity += o * (1.f - opacity);
+              if (opacity >= 0.99f)
+                done = true;
+            }
+          });
+          if (MODE == 1 && done)
+            return true;
+          continue;
         }
         if (!hitPrim)
           continue;
@@ -642,12 +988,22 @@ __device__ __forceinline__ int occlusionStep(const WorldGPU &w,
             u,
             v,
             front);
-      } else {
+      } else if (s.blasType == GEOM_SPHERE) {
         const SphereRecord *sp4 =
             reinterpret_cast<const SphereRecord *>(s.prims) + rec;
         if (STATS)
           st.spheres++;
         hitPrim = intersectSphere(s.r, __ldg(&sp4->cr), 0.f, s.tmax, t);
+      } else {
+        const float4 *sr = reinterpret_cast<const float4 *>(s.prims) + (size_t)rec * 3;
+        if (STATS)
+          st.spheres++;
+        hitPrim = false;
+        const float tmaxOcc = s.tmax;
+        segmentReports(s.r, s.blasType, sr, 0.f, [&](float tt, f3, float) {
+          if (tt >= 0.f && tt < tmaxOcc)
+            hitPrim = true;
+        });
       }
       if (hitPrim)
         return OCC_HIT;

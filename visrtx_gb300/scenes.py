@@ -282,13 +282,17 @@ from dataclasses import dataclass, field as _field
 
 @dataclass
 class SurfaceSpec:
-    type: str  # "triangle" | "sphere"
+    type: str  # "triangle" | "quad" | "sphere" | "cylinder" | "cone" | "curve"
     vertices: np.ndarray  # (n, 3) float32
-    indices: np.ndarray | None = None  # (m, 3) uint32 (triangle) / (m,) uint32 (sphere)
+    # triangle (m, 3), quad (m, 4), cylinder / cone (m, 2), sphere / curve (m,)
+    indices: np.ndarray | None = None
     normals: np.ndarray | None = None
     prim_ids: np.ndarray | None = None
+    # sphere / cone / curve: per vertex ("vertex.radius"); cylinder: per
+    # primitive ("primitive.radius")
     radii: np.ndarray | None = None
-    radius: float = 0.01
+    radius: float = 0.01  # "radius" (sphere 0.01; cylinder / curve take 1 by default)
+    caps: bool = False  # cylinder "caps"
     cull: bool = False
     id: int = 0xFFFFFFFF
     color: tuple = (0.8, 0.8, 0.8)
@@ -298,9 +302,17 @@ class SurfaceSpec:
 
     @property
     def num_prims(self) -> int:
-        if self.indices is not None:
-            return len(self.indices)
-        return len(self.vertices) // 3 if self.type == "triangle" else len(self.vertices)
+        """Primitives as the device numbers them (a quad is two triangles;
+        an unindexed curve has n/2 segments, Curve.cpp:88-99)."""
+        n = len(self.indices) if self.indices is not None else None
+        v = len(self.vertices)
+        if self.type == "triangle":
+            return n if n is not None else v // 3
+        if self.type == "quad":
+            return 2 * (n if n is not None else v // 4)
+        if self.type in ("cylinder", "cone", "curve"):
+            return n if n is not None else v // 2
+        return n if n is not None else v
 
 
 @dataclass
@@ -407,22 +419,22 @@ def build_on_device(dev, spec: SceneSpec, channels=("color", "depth", "primitive
         g.set("vertex.position", arr(np.ascontiguousarray(s.vertices, np.float32),
                                                L.FLOAT32_VEC3))
         if s.indices is not None:
-            if s.type == "triangle":
-                g.set("primitive.index", arr(np.ascontiguousarray(s.indices, np.uint32),
-                                                       L.UINT32_VEC3))
-            else:
-                g.set("primitive.index", arr(np.ascontiguousarray(s.indices, np.uint32),
-                                                       L.UINT32))
+            itype = {"triangle": L.UINT32_VEC3, "quad": L.UINT32_VEC4,
+                     "cylinder": L.UINT32_VEC2, "cone": L.UINT32_VEC2}.get(s.type, L.UINT32)
+            g.set("primitive.index", arr(np.ascontiguousarray(s.indices, np.uint32), itype))
         if s.normals is not None:
             g.set("vertex.normal", arr(np.ascontiguousarray(s.normals, np.float32),
                                                  L.FLOAT32_VEC3))
         if s.prim_ids is not None:
             g.set("primitive.id", arr(np.ascontiguousarray(s.prim_ids, np.uint32), L.UINT32))
-        if s.type == "sphere":
+        if s.type in ("sphere", "cone", "curve", "cylinder"):
             if s.radii is not None:
-                g.set("vertex.radius", arr(np.ascontiguousarray(s.radii, np.float32),
-                                                     L.FLOAT32))
-            g.set("radius", float(s.radius))
+                name = "primitive.radius" if s.type == "cylinder" else "vertex.radius"
+                g.set(name, arr(np.ascontiguousarray(s.radii, np.float32), L.FLOAT32))
+            if s.type != "cone":
+                g.set("radius", float(s.radius))
+        if s.type == "cylinder" and s.caps:
+            g.set("caps", "both")
         if s.cull:
             g.set("cullBackfaces", True)
         g.commit()
