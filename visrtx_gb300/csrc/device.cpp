@@ -1669,6 +1669,10 @@ bool World::rebuild()
   gpu.volumes = uploadVec(this, vols, s);
   gpu.numVolumes = (uint32_t)vols.size();
   gpu.allOpaque = allOpaque ? 1u : 0u;
+  gpu.hasSegments = 0u;
+  for (const BLASDesc &b : hBlas)
+    if (b.type >= GEOM_CYLINDER)
+      gpu.hasSegments = 1u;
   const cudaError_t err = cudaStreamSynchronize(s);
   builtStamp = deepStamp();
   buildMs = std::chrono::duration<float, std::milli>(

@@ -285,6 +285,7 @@ struct WorldGPU
   const VolumeGPU *volumes;
   uint32_t numVolumes;
   uint32_t allOpaque; // every material is opaque: any-hit = first hit
+  uint32_t hasSegments; // some BLAS holds cylinders, cones or curves
 };
 
 // Per-thread work counters. Rays and volume samples are counted by every

@@ -885,7 +885,7 @@ __device__ __forceinline__ uint32_t warpAppend(uint32_t *counter, uint32_t n)
   return base + before;
 }
 
-template <bool STATS>
+template <bool STATS, bool SEG>
 __global__ void __launch_bounds__(128) k_aoPrimary(const FrameParams P,
     int sampleIdx,
     uint32_t *consumed,
@@ -917,7 +917,7 @@ __global__ void __launch_bounds__(128) k_aoPrimary(const FrameParams P,
     Ray ray = makePrimaryRay(P, rs, x, y, false, sx, sy);
     Hit h;
     float unused;
-    const bool found = traverse<0, STATS>(P.world,
+    const bool found = traverse<0, STATS, SEG>(P.world,
         ray.org,
         ray.dir,
         ray.tmin,
@@ -990,7 +990,7 @@ __global__ void __launch_bounds__(128) k_aoPrimary(const FrameParams P,
 // when the warp has no live ray), so a warp keeps most lanes busy instead
 // of waiting for its slowest ray. Each ray's result depends on that ray
 // alone: the queue order in which lanes take rays does not change it.
-template <bool STATS>
+template <bool STATS, bool SEG>
 __global__ void __launch_bounds__(128, VRTX_TRACE_MIN_BLOCKS) k_aoTrace(const FrameParams P,
     const AORay *rays,
     const uint32_t *rayCount,
@@ -1041,7 +1041,7 @@ __global__ void __launch_bounds__(128, VRTX_TRACE_MIN_BLOCKS) k_aoTrace(const Fr
     if (__all_sync(0xffffffffu, exhausted))
       break;
     if (live) {
-      const int r = occlusionStep<STATS, VRTX_TRAVERSAL_STACK>(P.world,
+      const int r = occlusionStep<STATS, VRTX_TRAVERSAL_STACK, decltype(stack), SEG>(P.world,
           s,
           stack,
           reinterpret_cast<const float4 *>(rays + idx),
@@ -1162,6 +1162,38 @@ size_t aoWavefrontBytes(uint32_t w, uint32_t h, int aoSamples)
   return px * (sizeof(AOPixel) + sizeof(uint32_t)) + rays * (sizeof(AORay) + 4) + 1024;
 }
 
+// The per-sample launches of the wavefront AO renderer for one (stats,
+// segment primitives) combination.
+template <bool STATS, bool SEG>
+static void aoSamples(const FrameParams &P,
+    dim3 grid,
+    int numSMs,
+    uint32_t *consumed,
+    AOPixel *pixels,
+    AORay *rays,
+    uint32_t *rayCount,
+    float *weighted,
+    cudaStream_t s,
+    cudaEvent_t *traceEvents)
+{
+  int occ = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_aoTrace<STATS, SEG>, 128, 0);
+  const int traceGrid = numSMs * (occ > 0 ? occ : 1);
+  const int n = max(P.renderer.numIterations, 1);
+  for (int i = 0; i < n; i++) {
+    cudaMemsetAsync(rayCount, 0, 8, s); // queue length, fetch counter
+    // the primary pass keeps the general traversal (the per-pixel kernel's),
+    // so both forms of the renderer produce the same hits bit for bit
+    k_aoPrimary<STATS, true><<<grid, 128, 0, s>>>(P, i, consumed, pixels, rays, rayCount);
+    if (traceEvents)
+      cudaEventRecord(traceEvents[2 * i], s);
+    k_aoTrace<STATS, SEG><<<traceGrid, 128, 0, s>>>(P, rays, rayCount, rayCount + 1, weighted);
+    if (traceEvents)
+      cudaEventRecord(traceEvents[2 * i + 1], s);
+    k_aoResolve<<<grid, 128, 0, s>>>(P, i, n, pixels, weighted);
+  }
+}
+
 cudaError_t launchAOWavefront(const FrameParams &P,
     int numSMs,
     bool stats,
@@ -1182,28 +1214,17 @@ cudaError_t launchAOWavefront(const FrameParams &P,
   p += ((nr * sizeof(AORay) + 255) / 256) * 256;
   float *weighted = (float *)p;
   const dim3 grid((P.launchW + 7) / 8, (P.launchH + 15) / 16);
-  int occ = 0;
-  if (stats)
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_aoTrace<true>, 128, 0);
-  else
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_aoTrace<false>, 128, 0);
-  const int traceGrid = numSMs * (occ > 0 ? occ : 1);
-  const int n = max(P.renderer.numIterations, 1);
-  for (int i = 0; i < n; i++) {
-    cudaMemsetAsync(rayCount, 0, 8, s); // queue length, fetch counter
-    if (stats)
-      k_aoPrimary<true><<<grid, 128, 0, s>>>(P, i, consumed, pixels, rays, rayCount);
+  const bool seg = P.world.hasSegments != 0;
+  if (stats) {
+    if (seg)
+      aoSamples<true, true>(P, grid, numSMs, consumed, pixels, rays, rayCount, weighted, s, traceEvents);
     else
-      k_aoPrimary<false><<<grid, 128, 0, s>>>(P, i, consumed, pixels, rays, rayCount);
-    if (traceEvents)
-      cudaEventRecord(traceEvents[2 * i], s);
-    if (stats)
-      k_aoTrace<true><<<traceGrid, 128, 0, s>>>(P, rays, rayCount, rayCount + 1, weighted);
+      aoSamples<true, false>(P, grid, numSMs, consumed, pixels, rays, rayCount, weighted, s, traceEvents);
+  } else {
+    if (seg)
+      aoSamples<false, true>(P, grid, numSMs, consumed, pixels, rays, rayCount, weighted, s, traceEvents);
     else
-      k_aoTrace<false><<<traceGrid, 128, 0, s>>>(P, rays, rayCount, rayCount + 1, weighted);
-    if (traceEvents)
-      cudaEventRecord(traceEvents[2 * i + 1], s);
-    k_aoResolve<<<grid, 128, 0, s>>>(P, i, n, pixels, weighted);
+      aoSamples<false, false>(P, grid, numSMs, consumed, pixels, rays, rayCount, weighted, s, traceEvents);
   }
   return cudaGetLastError();
 }

@@ -607,7 +607,10 @@ __device__ __forceinline__ float surfaceOpacity(
 // (accumulateValue(o, opacity, o); terminate at o >= 0.99), as the
 // __anyhit__shadow / __anyhit__ao programs do (DirectLight_ptx.cu:233-256,
 // AmbientOcclusion_ptx.cu:53-69).
-template <int MODE, bool STATS = false>
+// SEG = false compiles the cylinder / cone / curve branch out (worlds
+// without such primitives: WorldGPU::hasSegments == 0), which keeps the
+// loop's register allocation that of triangles and spheres.
+template <int MODE, bool STATS = false, bool SEG = true>
 __device__ __forceinline__ bool traverse(const WorldGPU &w,
     f3 org,
     f3 dir,
@@ -716,7 +719,7 @@ __device__ __forceinline__ bool traverse(const WorldGPU &w,
             stats->spheres++;
           hitPrim = intersectSphere(r, cr, tmin, tmax, t);
           surface = __ldg(&sp4->surface);
-        } else {
+        } else if (SEG) {
           // cylinder / cone / curve: every report inside [tmin, tmax) is an
           // intersection; closest hit keeps the nearest, any hit
           // accumulates each
@@ -762,6 +765,9 @@ __device__ __forceinline__ bool traverse(const WorldGPU &w,
           if (MODE == 1 && done)
             return true;
           continue;
+        } else {
+          hitPrim = false;
+          surface = 0;
         }
         if (!hitPrim)
           continue;
@@ -829,6 +835,18 @@ __device__ __forceinline__ bool traverse(const WorldGPU &w,
     }
   }
   return MODE == 0 ? found : false;
+}
+
+// Any report of a cylinder / cone / curve in [0, tmax).
+__device__ __forceinline__ bool segmentOccludes(
+    const TravRay &r, uint32_t cls, const float4 *rec, float tmax)
+{
+  bool hit = false;
+  segmentReports(r, cls, rec, 0.f, [&](float tt, f3, float) {
+    if (tt >= 0.f && tt < tmax)
+      hit = true;
+  });
+  return hit;
 }
 
 // ---------------------------------------------------------------------------
@@ -921,7 +939,7 @@ __device__ __forceinline__ bool occlusionBegin(
 // One iteration of the traversal loop. `world` points at the ray's world
 // origin (xyz of [0]) and direction (xyz of [1]); they are re-read when the
 // ray enters or leaves an instance.
-template <bool STATS, int STACK, typename Stack>
+template <bool STATS, int STACK, typename Stack, bool SEG = true>
 __device__ __forceinline__ int occlusionStep(const WorldGPU &w,
     OccState &s,
     Stack &stack,
@@ -994,16 +1012,13 @@ __device__ __forceinline__ int occlusionStep(const WorldGPU &w,
         if (STATS)
           st.spheres++;
         hitPrim = intersectSphere(s.r, __ldg(&sp4->cr), 0.f, s.tmax, t);
-      } else {
+      } else if (SEG) {
         const float4 *sr = reinterpret_cast<const float4 *>(s.prims) + (size_t)rec * 3;
         if (STATS)
           st.spheres++;
+        hitPrim = segmentOccludes(s.r, s.blasType, sr, s.tmax);
+      } else {
         hitPrim = false;
-        const float tmaxOcc = s.tmax;
-        segmentReports(s.r, s.blasType, sr, 0.f, [&](float tt, f3, float) {
-          if (tt >= 0.f && tt < tmaxOcc)
-            hitPrim = true;
-        });
       }
       if (hitPrim)
         return OCC_HIT;
