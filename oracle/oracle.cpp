@@ -1129,6 +1129,8 @@ struct SHit
   float eps;
   uint32_t primId, objId, instId;
   int surface;
+  uint32_t prim; // geometry-local primitive index
+  float u, v; // triangle barycentrics; segments: u
 };
 
 // epsilonFrom (gpu/gpu_util.h:245-250)
@@ -1148,6 +1150,9 @@ SHit populate(const SceneCtx &S, const Ray &ray, const HitRec &h)
   sh.P = ray.org + h.t * ray.dir;
   sh.eps = epsilonFrom(sh.P, ray.dir, h.t);
   sh.surface = h.surface;
+  sh.prim = h.prim;
+  sh.u = h.u;
+  sh.v = h.v;
   sh.primId = s.primIds ? s.primIds[h.prim] : h.prim;
   sh.objId = s.id;
   sh.instId = in.userId;
@@ -1698,6 +1703,170 @@ float matteOpacity(const OrcSurface &s)
   return surfOpacity(s);
 }
 
+// --- geometry attributes and material parameters
+// (gpu/evalMaterialParameters.h:60-374, MatteShader_ptx.cu:38-49) ---
+
+struct V4
+{
+  float x, y, z, w;
+};
+inline V4 v4add(V4 a, V4 b)
+{
+  return {a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w};
+}
+inline V4 v4sub(V4 a, V4 b)
+{
+  return {a.x - b.x, a.y - b.y, a.z - b.z, a.w - b.w};
+}
+inline V4 v4mul(V4 a, float s)
+{
+  return {a.x * s, a.y * s, a.z * s, a.w * s};
+}
+
+float srgbChannel(float c)
+{
+  const float x = std::min(std::max(c, 0.f), 1.f);
+  return x < 0.0031308f ? x * 12.92f : std::pow(x, 0.41666f) * 1.055f - 0.055f;
+}
+
+V4 attrValue(const OrcAttr &a, uint32_t offset, V4 uf)
+{
+  if (!a.data || offset == 0xFFFFFFFFu)
+    return uf;
+  switch (a.type) {
+  case 240:
+    return {((const float *)a.data)[offset], 0.f, 0.f, 1.f};
+  case 241: {
+    const float *p = (const float *)a.data + 2 * (size_t)offset;
+    return {p[0], p[1], 0.f, 1.f};
+  }
+  case 242: {
+    const float *p = (const float *)a.data + 3 * (size_t)offset;
+    return {p[0], p[1], p[2], 1.f};
+  }
+  case 243: {
+    const float *p = (const float *)a.data + 4 * (size_t)offset;
+    return {p[0], p[1], p[2], p[3]};
+  }
+  case 221:
+    return {((const uint8_t *)a.data)[offset] / 255.f, 0.f, 0.f, 1.f};
+  case 223:
+    return {((const uint16_t *)a.data)[offset] / 65535.f, 0.f, 0.f, 1.f};
+  case 260:
+  case 261: {
+    const uint8_t *p = (const uint8_t *)a.data + 4 * (size_t)offset;
+    V4 r{p[0] / 255.f, p[1] / 255.f, p[2] / 255.f, p[3] / 255.f};
+    if (a.type == 261)
+      r = {srgbChannel(r.x), srgbChannel(r.y), srgbChannel(r.z), r.w};
+    return r;
+  }
+  default:
+    return uf;
+  }
+}
+
+// readAttributeValue: per-vertex values interpolated per subtype, then
+// per-primitive values, then the uniform value
+V4 readAttribute(const SceneCtx &S, const SHit &sh, int id)
+{
+  const OrcSurface &s = S.sc->surfaces[sh.surface];
+  const V4 uf{s.uattr[id][0], s.uattr[id][1], s.uattr[id][2], s.uattr[id][3]};
+  const OrcAttr &ap = s.vattr[id];
+  const uint32_t prim = sh.prim;
+  if (ap.data) {
+    const float b0 = 1.f - sh.u - sh.v, b1 = sh.u, b2 = sh.v;
+    if (s.type == 0) {
+      uint32_t i0, i1, i2;
+      if (s.indices) {
+        i0 = s.indices[3 * prim];
+        i1 = s.indices[3 * prim + 1];
+        i2 = s.indices[3 * prim + 2];
+      } else {
+        i0 = 3 * prim;
+        i1 = i0 + 1;
+        i2 = i0 + 2;
+      }
+      return v4add(v4add(v4mul(attrValue(ap, i0, uf), b0), v4mul(attrValue(ap, i1, uf), b1)),
+          v4mul(attrValue(ap, i2, uf), b2));
+    }
+    if (s.type == 2) {
+      const uint32_t pair = prim & ~1u;
+      uint32_t x, y, w, z, d0, d1;
+      quadTri(s, pair, x, y, w);
+      quadTri(s, pair + 1, z, d0, d1);
+      const V4 v0 = attrValue(ap, x, uf), v1 = attrValue(ap, y, uf);
+      const V4 v2 = attrValue(ap, z, uf), v3 = attrValue(ap, w, uf);
+      const float qu = (prim & 1u) ? b1 : 1.f - b1;
+      const float qv = (prim & 1u) ? b2 : 1.f - b2;
+      const V4 l0 = v4add(v1, v4mul(v4sub(v0, v1), qu));
+      const V4 l1 = v4add(v2, v4mul(v4sub(v3, v2), qu));
+      return v4add(l1, v4mul(v4sub(l0, l1), qv));
+    }
+    if (s.type == 3 || s.type == 4) {
+      const uint32_t i0 = s.indices ? s.indices[2 * prim] : 2 * prim;
+      const uint32_t i1 = s.indices ? s.indices[2 * prim + 1] : 2 * prim + 1;
+      return v4add(v4mul(attrValue(ap, i0, uf), 1.f - sh.u), v4mul(attrValue(ap, i1, uf), sh.u));
+    }
+    if (s.type == 5) {
+      const uint32_t i0 = s.indices ? s.indices[prim] : prim;
+      return v4add(v4mul(attrValue(ap, i0, uf), 1.f - sh.u), v4mul(attrValue(ap, i0 + 1, uf), sh.u));
+    }
+    const uint32_t i = s.indices ? s.indices[prim] : prim;
+    return attrValue(ap, i, uf);
+  }
+  const OrcAttr &pp = s.pattr[id];
+  if (pp.data)
+    return attrValue(pp, s.type == 2 ? prim / 2 : prim, uf);
+  return uf;
+}
+
+V4 materialParam(const SceneCtx &S, const SHit &sh, int src, V4 value)
+{
+  switch (src) {
+  case 0:
+    return value;
+  case 1:
+  case 2:
+  case 3:
+  case 4:
+    return readAttribute(S, sh, src - 1);
+  case 5:
+    return readAttribute(S, sh, 4);
+  case 6:
+  case 8:
+    return {sh.P.x, sh.P.y, sh.P.z, 1.f};
+  case 7:
+  case 9:
+    return {sh.Ns.x, sh.Ns.y, sh.Ns.z, 1.f};
+  default:
+    return {0.f, 0.f, 0.f, 0.f};
+  }
+}
+
+struct Matte
+{
+  V3 base;
+  float opacity;
+};
+
+Matte matteAt(const SceneCtx &S, const SHit &sh)
+{
+  const OrcSurface &s = S.sc->surfaces[sh.surface];
+  Matte m;
+  float op;
+  if (s.colorSrc == 0 && s.opacitySrc == 0) {
+    m.base = ld3(s.color, 0);
+    op = s.colorW * s.opacity;
+  } else {
+    const V4 c = materialParam(S, sh, s.colorSrc, {s.color[0], s.color[1], s.color[2], s.colorW});
+    const float o = materialParam(S, sh, s.opacitySrc, {s.opacity, 0.f, 0.f, 1.f}).x;
+    m.base = v3(c.x, c.y, c.z);
+    op = c.w * o;
+  }
+  m.opacity = s.alphaMode == 0 ? 1.f : (s.alphaMode == 1 ? op : (op < s.cutoff ? 0.f : 1.f));
+  return m;
+}
+
 // shadeSurface (renderer/DirectLight_ptx.cu:73-224), matte material
 // (shaders/MatteShader_ptx.cu:38-80), directional/point lights
 // (gpu/sampleLight.h:60-90)
@@ -1711,8 +1880,9 @@ void shadeDL(Ctx &C, const VolCtx &VC, Stream &rs, const Ray &ray, const SHit &h
       ? computeAO(C, rs, hit, R.occlusionDistance, R.ambientSamples)
       : 1.f;
   V3 contrib = v3(0, 0, 0);
-  const V3 base = ld3(s.color, 0);
-  const float opacity = matteOpacity(s);
+  const Matte mt = matteAt(*C.S, hit);
+  const V3 base = mt.base;
+  const float opacity = mt.opacity;
   if (R.ambientRadiance > 0.f)
     contrib = ld3(R.ambientColor, 0) * R.ambientRadiance * base;
   for (int l = 0; l < C.S->sc->numLights; l++) {
@@ -1821,15 +1991,17 @@ Sample integrate(Ctx &C, const VolCtx &VC, const CamPre &cam, Stream &rs, int px
         opacity += sr[3] * (1.f - opacity);
       } else if (rt == 1) {
         const V3 lighting = std::fabs(dot(ray.dir, sh.Ns)) * ld3(R.ambientColor, 0);
-        color = color + (ld3(s.color, 0) * lighting) * (1.f - opacity);
-        opacity += matteOpacity(s) * (1.f - opacity);
+        const Matte mt = matteAt(*C.S, sh);
+        color = color + (mt.base * lighting) * (1.f - opacity);
+        opacity += mt.opacity * (1.f - opacity);
       } else {
         const float ao = R.ambientSamples > 0
             ? computeAO(C, rs, sh, R.occlusionDistance, R.ambientSamples)
             : 1.f;
         const V3 lighting = ao * R.ambientRadiance * ld3(R.ambientColor, 0);
-        color = color + (ld3(s.color, 0) * lighting) * (1.f - opacity);
-        opacity += matteOpacity(s) * (1.f - opacity);
+        const Matte mt = matteAt(*C.S, sh);
+        color = color + (mt.base * lighting) * (1.f - opacity);
+        opacity += mt.opacity * (1.f - opacity);
       }
       color = color * opacity;
       outC = outC + color * (1.f - outO);
@@ -1973,7 +2145,7 @@ Sample integrateDPT(Ctx &C, const VolCtx &VC, const CamPre &cam, Stream &rs, int
     V3 pos, albedo;
     if (!volumeHit) {
       pos = sh.P + (sh.eps * sh.Ng);
-      albedo = ld3(C.S->sc->surfaces[sh.surface].color, 0);
+      albedo = matteAt(*C.S, sh).base;
     } else {
       pos = ray.org + volumeDepth * ray.dir;
       albedo = volumeColor;

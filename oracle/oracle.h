@@ -53,6 +53,15 @@ float orc_tex3d(const float *vox, const int dims[3], const float coord[3], int r
 
 /* --- scene ---------------------------------------------------------------- */
 
+/* A geometry attribute array: element type code (this library's VRTX_*
+ * values: 240..243 float32 x1..x4, 221 ufixed8, 223 ufixed16, 260 ufixed8
+ * x4, 261 sRGB ufixed8 x4) and channel count; data NULL: absent. */
+typedef struct OrcAttr {
+  const void *data;
+  int type;
+  int channels;
+} OrcAttr;
+
 typedef struct OrcSurface {
   int type; /* 0 triangle, 1 sphere, 2 quad, 3 cylinder, 4 cone, 5 curve */
   const float *vertices; /* vec3 */
@@ -73,6 +82,14 @@ typedef struct OrcSurface {
   int alphaMode; /* 0 opaque, 1 blend, 2 mask */
   float cutoff;
   int caps; /* cylinder end caps */
+  /* attributes: slots attribute0..3, color */
+  OrcAttr vattr[5]; /* vertex.* */
+  OrcAttr pattr[5]; /* primitive.* */
+  float uattr[5][4]; /* uniform (default 0, 0, 0, 1) */
+  /* matte parameter sources: 0 value, 1..4 attribute0..3, 5 color,
+   * 6 worldPosition, 7 worldNormal, 8 objectPosition, 9 objectNormal */
+  int colorSrc, opacitySrc;
+  float colorW; /* w of the colour value */
 } OrcSurface;
 
 typedef struct OrcInstance {

@@ -29,12 +29,24 @@ def load() -> C.CDLL:
     return _lib
 
 
+class OrcAttr(C.Structure):
+    _fields_ = [("data", C.c_void_p), ("type", C.c_int), ("channels", C.c_int)]
+
+
 class OrcSurface(C.Structure):
     _fields_ = [("type", C.c_int), ("vertices", C.c_void_p), ("indices", C.c_void_p),
                 ("numPrims", C.c_uint32), ("normals", C.c_void_p), ("primIds", C.c_void_p),
                 ("radii", C.c_void_p), ("radius", C.c_float), ("cullBackfaces", C.c_int),
                 ("id", C.c_uint32), ("color", C.c_float * 3), ("opacity", C.c_float),
-                ("alphaMode", C.c_int), ("cutoff", C.c_float), ("caps", C.c_int)]
+                ("alphaMode", C.c_int), ("cutoff", C.c_float), ("caps", C.c_int),
+                ("vattr", OrcAttr * 5), ("pattr", OrcAttr * 5), ("uattr", (C.c_float * 4) * 5),
+                ("colorSrc", C.c_int), ("opacitySrc", C.c_int), ("colorW", C.c_float)]
+
+
+_ATTR_SLOTS = ("attribute0", "attribute1", "attribute2", "attribute3", "color")
+_PARAM_SOURCES = {"attribute0": 1, "attribute1": 2, "attribute2": 3, "attribute3": 4, "color": 5,
+                  "worldPosition": 6, "worldNormal": 7, "objectPosition": 8, "objectNormal": 9}
+_ATTR_CHANNELS = {240: 1, 241: 2, 242: 3, 243: 4, 221: 1, 223: 1, 260: 4, 261: 4}
 
 
 class OrcInstance(C.Structure):
@@ -185,8 +197,32 @@ def _scene_structs(spec):
         o.radius = s.radius
         o.cullBackfaces = int(bool(s.cull))
         o.id = s.id & 0xFFFFFFFF
-        o.color = (C.c_float * 3)(*map(float, s.color))
-        o.opacity = s.opacity
+        if isinstance(s.color, str):
+            o.colorSrc = _PARAM_SOURCES[s.color]
+            o.color = (C.c_float * 3)(0.8, 0.8, 0.8)
+            o.colorW = 1.0
+        else:
+            o.color = (C.c_float * 3)(*map(float, s.color[:3]))
+            o.colorW = float(s.color[3]) if len(s.color) == 4 else 1.0
+        if isinstance(s.opacity, str):
+            o.opacitySrc = _PARAM_SOURCES[s.opacity]
+            o.opacity = 1.0
+        else:
+            o.opacity = s.opacity
+        from visrtx_gb300.scenes import attr_type
+        for k, slot in enumerate(_ATTR_SLOTS):
+            o.uattr[k] = (C.c_float * 4)(0.0, 0.0, 0.0, 1.0)
+            for prefix, dst in (("vertex.", o.vattr), ("primitive.", o.pattr)):
+                a = s.attrs.get(prefix + slot)
+                if a is not None:
+                    a = np.ascontiguousarray(a)
+                    keep.append(a)
+                    t = attr_type(a)
+                    dst[k].data = _ptr(a)
+                    dst[k].type = t
+                    dst[k].channels = _ATTR_CHANNELS[t]
+            if slot in s.attrs:
+                o.uattr[k] = (C.c_float * 4)(*map(float, s.attrs[slot]))
         o.alphaMode = _ALPHA[s.alpha_mode]
         o.cutoff = s.cutoff
         o.caps = int(bool(s.caps))

@@ -260,6 +260,68 @@ def test_geometry_subtypes(device, kind, renderer):
     print(kind, renderer, rep, hit.mean())
 
 
+ATTRIBUTE_CASES = {
+    # subtype, material colour source, attribute key, attribute maker
+    "triangle-vertex-color-f4": ("triangle", "color", "vertex.color",
+                                 lambda rng, n: rng.random((n, 4)).astype(np.float32)),
+    "triangle-prim-attr0-u8": ("triangle", "attribute0", "primitive.attribute0",
+                               lambda rng, n: rng.integers(0, 256, (n, 4)).astype(np.uint8)),
+    "triangle-uniform-attr2": ("triangle", "attribute2", "attribute2", None),
+    "triangle-world-normal": ("triangle", "worldNormal", None, None),
+    "quad-vertex-attr1-f3": ("quad", "attribute1", "vertex.attribute1",
+                             lambda rng, n: rng.random((n, 3)).astype(np.float32)),
+    "sphere-vertex-color-u8": ("sphere", "color", "vertex.color",
+                               lambda rng, n: rng.integers(0, 256, (n, 4)).astype(np.uint8)),
+    "cylinder-vertex-color-f2": ("cylinder", "color", "vertex.color",
+                                 lambda rng, n: rng.random((n, 2)).astype(np.float32)),
+    "cone-prim-attr3-f1": ("cone", "attribute3", "primitive.attribute3",
+                           lambda rng, n: rng.random(n).astype(np.float32)),
+    "curve-vertex-color-f4": ("curve", "color", "vertex.color",
+                              lambda rng, n: rng.random((n, 4)).astype(np.float32)),
+}
+
+
+@pytest.mark.parametrize("case", sorted(ATTRIBUTE_CASES))
+def test_material_attributes(device, case):
+    """Matte colour from geometry attributes (readAttributeValue: per-vertex
+    values interpolated per subtype with the hit's barycentrics / curve and
+    cylinder parameter, per-primitive values, uniform values) and from hit
+    quantities, against the oracle."""
+    kind, src, key, make = ATTRIBUTE_CASES[case]
+    rng = np.random.default_rng(11)
+    if kind == "triangle":
+        spec = soup("raycast", n=3000, w=96, h=72)
+        surf = spec.surfaces[0]
+    elif kind == "sphere":
+        c, rad = S.random_spheres(3000, seed=4)
+        surf = S.SurfaceSpec("sphere", c * 0.1, radii=rad * 5, id=5)
+        cam = S.CameraSpec(position=(0.0, 0.0, -3.0), direction=(0.0, 0.0, 1.0),
+                           fovy=math.radians(45), aspect=1.5)
+        spec = S.SceneSpec([surf], [S.InstanceSpec([0], zero=True)], [], camera=cam,
+                           renderer=S.RendererSpec("raycast"), width=96, height=64)
+    else:
+        spec = geometry_zoo(kind)
+        spec.surfaces = spec.surfaces[:1]
+        spec.instances = [S.InstanceSpec([0], zero=True)]
+        surf = spec.surfaces[0]
+    surf.color = src
+    if key is not None and "." in key:
+        n = (surf.num_prims // (2 if kind == "quad" else 1)) if key.startswith("primitive.") \
+            else len(surf.vertices)
+        surf.attrs = {key: make(rng, n)}
+    elif key is not None:
+        surf.attrs = {key: (0.2, 0.7, 0.4, 1.0)}
+    g = render_gpu(device, spec)
+    r = render_oracle(spec)
+    rep = compare(g, r, allow_ids=3, **({"depth_rel": 3e-4, "color_tol": 8} if kind == "cone" else {}))
+    from visrtx_gb300 import anari
+
+    hit = g["depth"] < 1e29
+    c = anari.rgba8(g["color"])[..., :3][hit]
+    assert hit.mean() > 0.02 and c.std() > 1.0, "the attribute varies the colour"
+    print(case, rep)
+
+
 def test_orthographic(device):
     spec = soup("raycast", n=5000, w=64, h=64)
     spec.camera = S.CameraSpec(type="orthographic", position=(0.5, 0.5, -1.0),

@@ -510,6 +510,41 @@ static Array *arrayParam(Object *o, const char *name, int elemType)
   return a;
 }
 
+// Channels of an attribute element type this device reads (0: not one)
+static uint32_t attrChannels(int t)
+{
+  switch (t) {
+  case VRTX_FLOAT32:
+  case VRTX_UFIXED8:
+  case VRTX_UFIXED16:
+    return 1;
+  case VRTX_FLOAT32_VEC2:
+    return 2;
+  case VRTX_FLOAT32_VEC3:
+    return 3;
+  case VRTX_FLOAT32_VEC4:
+  case VRTX_UFIXED8_VEC4:
+  case VRTX_UFIXED8_RGBA_SRGB:
+    return 4;
+  default:
+    return 0;
+  }
+}
+
+static Array *attrArray(Object *o, const std::string &name)
+{
+  auto *a = static_cast<Array *>(o->getObject(name, VRTX_ARRAY1D));
+  if (!a)
+    return nullptr;
+  if (!attrChannels(a->elemType)) {
+    o->report(VRTX_SEVERITY_WARNING,
+        "'%s' array has an element type this device does not read; ignored",
+        name.c_str());
+    return nullptr;
+  }
+  return a;
+}
+
 Geometry::~Geometry()
 {
   if (quadIndices && Object::dev->initOk)
@@ -601,6 +636,18 @@ void Geometry::commit()
     numPrims = index ? (uint32_t)index->count() : nv / 3;
   }
   primId = arrayParam(this, "primitive.id", VRTX_UINT32);
+  // attributes (Geometry.cpp:108-126,152-171): vertex.* per subtype,
+  // primitive.*, and uniform FLOAT32_VEC4 values
+  static const char *names[NUM_ATTRS] = {
+      "attribute0", "attribute1", "attribute2", "attribute3", "color"};
+  for (int k = 0; k < NUM_ATTRS; k++) {
+    vattr[k] = attrArray(this, std::string("vertex.") + names[k]);
+    pattr[k] = attrArray(this, std::string("primitive.") + names[k]);
+    float u[4] = {0.f, 0.f, 0.f, 1.f};
+    if (has(names[k], VRTX_FLOAT32_VEC4))
+      std::memcpy(u, params[names[k]].bytes.data(), 16);
+    uattr[k] = make_float4(u[0], u[1], u[2], u[3]);
+  }
   if (!vertex)
     report(VRTX_SEVERITY_WARNING,
         "missing required parameter 'vertex.position' on %s geometry",
@@ -623,6 +670,10 @@ uint64_t Geometry::deepStamp() const
   for (const Array *a : {vertex, index, normal, normalFV, primId, radius})
     if (a)
       s = std::max(s, a->deepStamp());
+  for (int k = 0; k < NUM_ATTRS; k++)
+    for (const Array *a : {vattr[k], pattr[k]})
+      if (a)
+        s = std::max(s, a->deepStamp());
   return s;
 }
 
@@ -659,6 +710,16 @@ GeometryGPU Geometry::gpuData()
   g.radius = globalRadius;
   g.cullBackfaces = cull ? 1u : 0u;
   g.caps = caps ? 1u : 0u;
+  for (int k = 0; k < NUM_ATTRS; k++) {
+    for (int which = 0; which < 2; which++) {
+      Array *a = which ? pattr[k] : vattr[k];
+      AttrGPU &o = which ? g.pattr[k] : g.vattr[k];
+      o.data = a ? a->deviceData() : nullptr;
+      o.type = a ? (uint32_t)a->elemType : 0u;
+      o.channels = a ? attrChannels(a->elemType) : 0u;
+    }
+    g.uattr[k] = uattr[k];
+  }
   return g;
 }
 
@@ -678,7 +739,41 @@ void Material::commit()
   else if (has("color", VRTX_FLOAT32_VEC3))
     std::memcpy(c, params["color"].bytes.data(), 12);
   gpu.color = f3{c[0], c[1], c[2]};
-  gpu.opacity = c[3] * get<float>("opacity", VRTX_FLOAT32, 1.f);
+  gpu.colorValue = make_float4(c[0], c[1], c[2], c[3]);
+  gpu.opacityValue = get<float>("opacity", VRTX_FLOAT32, 1.f);
+  gpu.opacity = c[3] * gpu.opacityValue;
+  // a string names an attribute or a hit quantity (populateMaterialParameter,
+  // Material.cpp)
+  auto source = [&](const char *name) -> uint32_t {
+    if (!has(name, VRTX_STRING))
+      return PARAM_VALUE;
+    const std::string a = getString(name, "");
+    if (a == "attribute0")
+      return PARAM_ATTRIB_0;
+    if (a == "attribute1")
+      return PARAM_ATTRIB_0 + 1;
+    if (a == "attribute2")
+      return PARAM_ATTRIB_0 + 2;
+    if (a == "attribute3")
+      return PARAM_ATTRIB_0 + 3;
+    if (a == "color")
+      return PARAM_ATTRIB_COLOR;
+    if (a == "worldPosition")
+      return PARAM_WORLD_POSITION;
+    if (a == "worldNormal")
+      return PARAM_WORLD_NORMAL;
+    if (a == "objectPosition")
+      return PARAM_OBJECT_POSITION;
+    if (a == "objectNormal")
+      return PARAM_OBJECT_NORMAL;
+    report(VRTX_SEVERITY_WARNING,
+        "unknown attribute '%s' for material parameter '%s'",
+        a.c_str(),
+        name);
+    return PARAM_VALUE;
+  };
+  gpu.colorSrc = source("color");
+  gpu.opacitySrc = source("opacity");
   gpu.cutoff = get<float>("alphaCutoff", VRTX_FLOAT32, 0.5f);
   const std::string mode = getString("alphaMode", "opaque");
   gpu.alphaMode = mode == "blend" ? ALPHA_BLEND

@@ -40,6 +40,19 @@ enum GeomKind : uint32_t
   KIND_CURVE = 5
 };
 
+// One geometry attribute array (Geometry.cpp:152-171): element type code
+// (VRTX_FLOAT32.._VEC4, VRTX_UFIXED8 / _VEC4 / _RGBA_SRGB, VRTX_UFIXED16)
+// and its channel count; data == NULL: not given.
+struct AttrGPU
+{
+  const void *data;
+  uint32_t type;
+  uint32_t channels;
+};
+
+// Attribute slots in the reference's order: attribute0..3, color
+constexpr int NUM_ATTRS = 5;
+
 struct GeometryGPU
 {
   uint32_t type; // GeomType (the class)
@@ -58,6 +71,9 @@ struct GeometryGPU
   uint32_t cullBackfaces; // VISRTX_TRIANGLE_BACK_FACE_CULLING extension
   uint32_t kind; // GeomKind
   uint32_t caps; // cylinder "caps" != "none"
+  AttrGPU vattr[NUM_ATTRS]; // vertex.attribute0..3, vertex.color
+  AttrGPU pattr[NUM_ATTRS]; // primitive.attribute0..3, primitive.color
+  float4 uattr[NUM_ATTRS]; // uniform attribute0..3, color (default 0,0,0,1)
 };
 
 enum AlphaMode : int
@@ -67,13 +83,30 @@ enum AlphaMode : int
   ALPHA_MASK = 2
 };
 
+// Where a material parameter comes from (MaterialParameterType of the
+// reference): its value, a geometry attribute, or a hit quantity.
+enum ParamSource : uint32_t
+{
+  PARAM_VALUE = 0,
+  PARAM_ATTRIB_0 = 1, // .. PARAM_ATTRIB_3 = 4
+  PARAM_ATTRIB_COLOR = 5,
+  PARAM_WORLD_POSITION = 6,
+  PARAM_WORLD_NORMAL = 7,
+  PARAM_OBJECT_POSITION = 8,
+  PARAM_OBJECT_NORMAL = 9
+};
+
 struct MaterialGPU
 {
-  f3 color; // matte "color" (default 0.8 grey, Matte.cpp:44)
-  float opacity; // color.w * opacity, before the alpha mode
+  f3 color; // matte "color" value (default 0.8 grey, Matte.cpp:44)
+  float opacity; // color.w * opacity of the values, before the alpha mode
   int alphaMode;
   float cutoff;
-  int pad[2];
+  uint32_t colorSrc; // ParamSource of "color"
+  uint32_t opacitySrc; // ParamSource of "opacity"
+  float4 colorValue; // the "color" value with its w
+  float opacityValue; // the "opacity" value
+  uint32_t pad[3];
 };
 
 struct SurfaceGPU

@@ -152,6 +152,8 @@ struct Geometry : Object
   bool cull = false;
   bool caps = false;
   uint32_t numPrims = 0;
+  Array *vattr[NUM_ATTRS] = {}, *pattr[NUM_ATTRS] = {};
+  float4 uattr[NUM_ATTRS] = {};
   // quads: generated triangle indices (2 per quad) on the device
   uint32_t *quadIndices = nullptr;
   uint64_t quadStamp = 0;

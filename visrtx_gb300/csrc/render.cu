@@ -122,6 +122,7 @@ struct SurfaceHit
   uint32_t primID; // geometry-local primitive index (OptiX primID)
   uint32_t surface;
   uint32_t instUserId;
+  float u, v; // triangle barycentrics (v1, v2 weights); segments: u
 };
 
 // epsilonFrom (gpu_util.h:245-250)
@@ -139,6 +140,8 @@ __device__ __forceinline__ void populateSurfaceHit(
   const InstanceRecord &inst = w.instances[h.inst];
   const BLASDesc &blas = w.blas[inst.blas];
   sh.t = h.t;
+  sh.u = h.u;
+  sh.v = h.v;
   sh.hitpoint = ray.org + h.t * ray.dir;
   sh.epsilon = epsilonFrom(sh.hitpoint, ray.dir, h.t);
   sh.instUserId = inst.userId;
@@ -232,16 +235,181 @@ struct MatteState
   float opacity;
 };
 
-__device__ __forceinline__ MatteState matteInit(
-    const WorldGPU &w, uint32_t surface)
+// --- geometry attributes and material parameters ---------------------------
+
+__device__ __forceinline__ float4 f4add(float4 a, float4 b)
 {
-  const MaterialGPU &m = w.materials[w.surfaces[surface].material];
+  return make_float4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w);
+}
+__device__ __forceinline__ float4 f4sub(float4 a, float4 b)
+{
+  return make_float4(a.x - b.x, a.y - b.y, a.z - b.z, a.w - b.w);
+}
+__device__ __forceinline__ float4 f4mul(float4 a, float s)
+{
+  return make_float4(a.x * s, a.y * s, a.z * s, a.w * s);
+}
+
+// glm::convertLinearToSRGB (gamma 0.41666) on one channel
+__device__ __forceinline__ float srgbEncode(float c)
+{
+  const float x = fminf(fmaxf(c, 0.f), 1.f);
+  return x < 0.0031308f ? x * 12.92f : powf(x, 0.41666f) * 1.055f - 0.055f;
+}
+
+// getAttributeValue (gpu/evalMaterialParameters.h:60-99): element `offset`
+// of an attribute array as a vec4 (missing channels 0, alpha 1; fixed-point
+// normalised; sRGB8 values passed through the linear-to-sRGB conversion as
+// the reference does)
+__device__ __forceinline__ float4 attrValue(const AttrGPU &a, uint32_t offset, float4 uf)
+{
+  if (!a.data || offset == 0xFFFFFFFFu)
+    return uf;
+  switch (a.type) {
+  case 240: { // FLOAT32
+    const float *p = (const float *)a.data;
+    return make_float4(p[offset], 0.f, 0.f, 1.f);
+  }
+  case 241: { // FLOAT32_VEC2
+    const float *p = (const float *)a.data + 2 * (size_t)offset;
+    return make_float4(p[0], p[1], 0.f, 1.f);
+  }
+  case 242: { // FLOAT32_VEC3
+    const float *p = (const float *)a.data + 3 * (size_t)offset;
+    return make_float4(p[0], p[1], p[2], 1.f);
+  }
+  case 243: // FLOAT32_VEC4
+    return ((const float4 *)a.data)[offset];
+  case 221: { // UFIXED8
+    const uint8_t *p = (const uint8_t *)a.data;
+    return make_float4(p[offset] / 255.f, 0.f, 0.f, 1.f);
+  }
+  case 223: { // UFIXED16
+    const uint16_t *p = (const uint16_t *)a.data;
+    return make_float4(p[offset] / 65535.f, 0.f, 0.f, 1.f);
+  }
+  case 260: // UFIXED8_VEC4
+  case 261: { // UFIXED8_RGBA_SRGB
+    const uint8_t *p = (const uint8_t *)a.data + 4 * (size_t)offset;
+    float4 r = make_float4(p[0] / 255.f, p[1] / 255.f, p[2] / 255.f, p[3] / 255.f);
+    if (a.type == 261)
+      r = make_float4(srgbEncode(r.x), srgbEncode(r.y), srgbEncode(r.z), r.w);
+    return r;
+  }
+  default:
+    return uf;
+  }
+}
+
+// readAttributeValue (gpu/evalMaterialParameters.h:131-263) for attribute
+// slot `id` (0..3 attribute0..3, 4 color): per-vertex values interpolated
+// per subtype, then per-primitive values, then the geometry's uniform value.
+// (Instance attributes and face-varying attributes are not read.)
+__device__ __forceinline__ float4 readAttribute(
+    const WorldGPU &w, const SurfaceHit &sh, int id)
+{
+  const GeometryGPU &g = w.geometries[w.surfaces[sh.surface].geometry];
+  const float4 uf = g.uattr[id];
+  const AttrGPU &ap = g.vattr[id];
+  const uint32_t prim = sh.primID;
+  if (ap.data) {
+    const float b0 = 1.f - sh.u - sh.v, b1 = sh.u, b2 = sh.v;
+    switch (g.kind) {
+    case KIND_TRIANGLE: {
+      uint32_t i0, i1, i2;
+      if (g.indices) {
+        i0 = g.indices[3 * prim];
+        i1 = g.indices[3 * prim + 1];
+        i2 = g.indices[3 * prim + 2];
+      } else {
+        i0 = 3 * prim;
+        i1 = i0 + 1;
+        i2 = i0 + 2;
+      }
+      return f4add(f4add(f4mul(attrValue(ap, i0, uf), b0), f4mul(attrValue(ap, i1, uf), b1)),
+          f4mul(attrValue(ap, i2, uf), b2));
+    }
+    case KIND_QUAD: {
+      // corners (x, y, w, z) of the quad from its two triangles
+      const uint32_t pair = prim & ~1u;
+      const uint32_t x = g.indices[3 * pair], y = g.indices[3 * pair + 1],
+                     wI = g.indices[3 * pair + 2], z = g.indices[3 * (pair + 1)];
+      const float4 v0 = attrValue(ap, x, uf), v1 = attrValue(ap, y, uf);
+      const float4 v2 = attrValue(ap, z, uf), v3 = attrValue(ap, wI, uf);
+      const float qu = (prim & 1u) ? b1 : 1.f - b1;
+      const float qv = (prim & 1u) ? b2 : 1.f - b2;
+      const float4 l0 = f4add(v1, f4mul(f4sub(v0, v1), qu));
+      const float4 l1 = f4add(v2, f4mul(f4sub(v3, v2), qu));
+      return f4add(l1, f4mul(f4sub(l0, l1), qv));
+    }
+    case KIND_CYLINDER:
+    case KIND_CONE: {
+      const uint32_t i0 = g.indices ? g.indices[2 * prim] : 2 * prim;
+      const uint32_t i1 = g.indices ? g.indices[2 * prim + 1] : 2 * prim + 1;
+      // uvw = (0, u, 1 - u)
+      return f4add(f4mul(attrValue(ap, i0, uf), 1.f - sh.u), f4mul(attrValue(ap, i1, uf), sh.u));
+    }
+    case KIND_CURVE: {
+      const uint32_t i0 = g.indices ? g.indices[prim] : prim;
+      return f4add(f4mul(attrValue(ap, i0, uf), 1.f - sh.u), f4mul(attrValue(ap, i0 + 1, uf), sh.u));
+    }
+    default: { // sphere
+      const uint32_t i = g.indices ? g.indices[prim] : prim;
+      return attrValue(ap, i, uf);
+    }
+    }
+  }
+  const AttrGPU &pp = g.pattr[id];
+  if (pp.data)
+    return attrValue(pp, g.kind == KIND_QUAD ? prim / 2 : prim, uf);
+  return uf;
+}
+
+// getMaterialParameter (gpu/evalMaterialParameters.h:336-374)
+__device__ __forceinline__ float4 materialParam(
+    const WorldGPU &w, const SurfaceHit &sh, uint32_t src, float4 value)
+{
+  switch (src) {
+  case PARAM_VALUE:
+    return value;
+  case PARAM_ATTRIB_0:
+  case PARAM_ATTRIB_0 + 1:
+  case PARAM_ATTRIB_0 + 2:
+  case PARAM_ATTRIB_0 + 3:
+    return readAttribute(w, sh, (int)(src - PARAM_ATTRIB_0));
+  case PARAM_ATTRIB_COLOR:
+    return readAttribute(w, sh, 4);
+  case PARAM_WORLD_POSITION:
+  case PARAM_OBJECT_POSITION: // world space, as the reference
+    return make_float4(sh.hitpoint.x, sh.hitpoint.y, sh.hitpoint.z, 1.f);
+  case PARAM_WORLD_NORMAL:
+  case PARAM_OBJECT_NORMAL:
+    return make_float4(sh.Ns.x, sh.Ns.y, sh.Ns.z, 1.f);
+  default:
+    return make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+}
+
+// Matte init (MatteShader_ptx.cu:38-49): colour and opacity parameters,
+// opacity = adjustedMaterialOpacity(color.w * opacity.x)
+__device__ __forceinline__ MatteState matteInit(const WorldGPU &w, const SurfaceHit &sh)
+{
+  const MaterialGPU &m = w.materials[w.surfaces[sh.surface].material];
   MatteState s;
-  s.baseColor = m.color;
+  float op;
+  if (m.colorSrc == PARAM_VALUE && m.opacitySrc == PARAM_VALUE) {
+    s.baseColor = m.color;
+    op = m.opacity;
+  } else {
+    const float4 c = materialParam(w, sh, m.colorSrc, m.colorValue);
+    const float o =
+        materialParam(w, sh, m.opacitySrc, make_float4(m.opacityValue, 0.f, 0.f, 1.f)).x;
+    s.baseColor = mk3(c.x, c.y, c.z);
+    op = c.w * o;
+  }
   s.opacity = m.alphaMode == ALPHA_OPAQUE
       ? 1.f
-      : (m.alphaMode == ALPHA_BLEND ? m.opacity
-                                    : (m.opacity < m.cutoff ? 0.f : 1.f));
+      : (m.alphaMode == ALPHA_BLEND ? op : (op < m.cutoff ? 0.f : 1.f));
   return s;
 }
 
@@ -310,7 +478,7 @@ __device__ __forceinline__ float4 shadeSurfaceDL(const FrameParams &P,
       ? computeAO<STATS>(P, st, rs, hit, rp.occlusionDistance, rp.aoSamples)
       : 1.f;
   f3 contrib = mk3(0.f, 0.f, 0.f);
-  const MatteState ms = matteInit(w, hit.surface);
+  const MatteState ms = matteInit(w, hit);
   const float opacity = ms.opacity;
   if (rp.ambientIntensity > 0.f)
     contrib = rp.ambientColor * rp.ambientIntensity * ms.baseColor;
@@ -448,7 +616,7 @@ __device__ __forceinline__ void integrateSample(const FrameParams &P,
         color += srgb * (1.f - opacity);
         opacity += sr.w * (1.f - opacity);
       } else if (RT == RENDERER_RAYCAST) {
-        const MatteState ms = matteInit(w, sh.surface);
+        const MatteState ms = matteInit(w, sh);
         const f3 lighting = fabsf(dot(ray.dir, sh.Ns)) * rp.ambientColor;
         color += (ms.baseColor * lighting) * (1.f - opacity);
         opacity += ms.opacity * (1.f - opacity);
@@ -456,7 +624,7 @@ __device__ __forceinline__ void integrateSample(const FrameParams &P,
         const float aoFactor = rp.aoSamples > 0
             ? computeAO<STATS>(P, st, rs, sh, rp.occlusionDistance, rp.aoSamples)
             : 1.f;
-        const MatteState ms = matteInit(w, sh.surface);
+        const MatteState ms = matteInit(w, sh);
         const f3 lighting = aoFactor * rp.ambientIntensity * rp.ambientColor;
         color += (ms.baseColor * lighting) * (1.f - opacity);
         opacity += ms.opacity * (1.f - opacity);
@@ -602,7 +770,7 @@ __device__ __forceinline__ void integrateDPT(const FrameParams &P,
     f3 pos;
     if (!volumeHit) {
       pos = sh.hitpoint + (sh.epsilon * sh.Ng);
-      albedo = matteInit(w, sh.surface).baseColor;
+      albedo = matteInit(w, sh).baseColor;
     } else {
       pos = ray.org + volumeDepth * ray.dir;
       albedo = volumeColor;
@@ -651,11 +819,9 @@ __device__ __forceinline__ float4 inverseTonemap(float4 v)
   return make_float4(v.x / d, v.y / d, v.z / d, v.w);
 }
 
-// glm::convertLinearToSRGB (gamma 0.41666) on one channel
 __device__ __forceinline__ float linearToSrgb(float c)
 {
-  const float x = fminf(fmaxf(c, 0.f), 1.f);
-  return x < 0.0031308f ? x * 12.92f : powf(x, 0.41666f) * 1.055f - 0.055f;
+  return srgbEncode(c);
 }
 
 __device__ __forceinline__ uint32_t packUnorm4x8(float4 v)
@@ -936,7 +1102,7 @@ __global__ void __launch_bounds__(128) k_aoPrimary(const FrameParams P,
       px.prim = geometryPrimId(P.world, sh);
       px.obj = P.world.surfaces[sh.surface].id;
       px.inst = sh.instUserId;
-      px.base = matteInit(P.world, sh.surface).baseColor;
+      px.base = matteInit(P.world, sh).baseColor;
       px.normal = sh.Ng;
       px.weights = 0.f;
       org = sh.hitpoint + (sh.epsilon * sh.Ng);

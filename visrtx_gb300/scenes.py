@@ -293,10 +293,14 @@ class SurfaceSpec:
     radii: np.ndarray | None = None
     radius: float = 0.01  # "radius" (sphere 0.01; cylinder / curve take 1 by default)
     caps: bool = False  # cylinder "caps"
+    # geometry attributes: "vertex.<slot>" / "primitive.<slot>" -> array,
+    # "<slot>" -> uniform 4-tuple; slots attribute0..3, color. Arrays:
+    # float32 (n,) / (n, 2..4), uint8 (n,) / (n, 4), uint16 (n,)
+    attrs: dict = _field(default_factory=dict)
     cull: bool = False
     id: int = 0xFFFFFFFF
-    color: tuple = (0.8, 0.8, 0.8)
-    opacity: float = 1.0
+    color: tuple | str = (0.8, 0.8, 0.8)  # value, or an attribute / hit quantity name
+    opacity: float | str = 1.0
     alpha_mode: str = "opaque"
     cutoff: float = 0.5
 
@@ -394,6 +398,20 @@ class SceneSpec:
     world_id: int = 0xFFFFFFFF
 
 
+def attr_type(a: np.ndarray) -> int:
+    """Element type code of an attribute array (see SurfaceSpec.attrs)."""
+    from . import _lib as L
+
+    comps = 1 if a.ndim == 1 else a.shape[1]
+    if a.dtype == np.float32:
+        return {1: L.FLOAT32, 2: L.FLOAT32_VEC2, 3: L.FLOAT32_VEC3, 4: L.FLOAT32_VEC4}[comps]
+    if a.dtype == np.uint8:
+        return {1: L.UFIXED8, 4: L.UFIXED8_VEC4}[comps]
+    if a.dtype == np.uint16 and comps == 1:
+        return L.UFIXED16
+    raise ValueError(f"attribute arrays of {a.dtype} x {comps} are not supported")
+
+
 def build_on_device(dev, spec: SceneSpec, channels=("color", "depth", "primitiveId",
                                                       "objectId", "instanceId")):
     """Creates the spec's ANARI objects on an anari.Device; returns
@@ -435,12 +453,22 @@ def build_on_device(dev, spec: SceneSpec, channels=("color", "depth", "primitive
                 g.set("radius", float(s.radius))
         if s.type == "cylinder" and s.caps:
             g.set("caps", "both")
+        for key, val in s.attrs.items():
+            if "." in key:
+                a = np.ascontiguousarray(val)
+                g.set(key, arr(a, attr_type(a)))
+            else:
+                g.set(key, tuple(float(c) for c in val), L.FLOAT32_VEC4)
         if s.cull:
             g.set("cullBackfaces", True)
         g.commit()
         m = dev.new_material("matte")
-        m.set("color", tuple(float(c) for c in s.color), L.FLOAT32_VEC3)
-        m.set("opacity", float(s.opacity))
+        if isinstance(s.color, str):
+            m.set("color", s.color)
+        else:
+            m.set("color", tuple(float(c) for c in s.color),
+                  L.FLOAT32_VEC4 if len(s.color) == 4 else L.FLOAT32_VEC3)
+        m.set("opacity", s.opacity if isinstance(s.opacity, str) else float(s.opacity))
         m.set("alphaMode", s.alpha_mode)
         m.set("alphaCutoff", float(s.cutoff))
         m.commit()
