@@ -1820,11 +1820,109 @@ V4 readAttribute(const SceneCtx &S, const SHit &sh, int id)
   return uf;
 }
 
-V4 materialParam(const SceneCtx &S, const SHit &sh, int src, V4 value)
+// Texture lookup with normalised coordinates, float4 texels: address modes
+// clamp / wrap / mirror, point or linear filtering (8-bit weights,
+// round-to-nearest, as the emulation of the TF path)
+int wrapIndex(int i, int n, int mode)
+{
+  if (mode == 1) {
+    i %= n;
+    return i < 0 ? i + n : i;
+  }
+  if (mode == 2) {
+    const int p = 2 * n;
+    int m = i % p;
+    if (m < 0)
+      m += p;
+    return m < n ? m : p - 1 - m;
+  }
+  return std::min(std::max(i, 0), n - 1);
+}
+
+float wrapCoord(float c, int mode)
+{
+  if (mode == 1)
+    return c - std::floor(c);
+  if (mode == 2) {
+    const float f = std::floor(c);
+    const float r = c - f;
+    return ((long long)f % 2 != 0) ? 1.f - r : r;
+  }
+  return c;
+}
+
+V4 texSample(const OrcSampler &sm, int ndim, const float tc[3])
+{
+  int i0[3] = {0, 0, 0}, i1[3] = {0, 0, 0};
+  float w[3] = {0.f, 0.f, 0.f};
+  for (int k = 0; k < ndim; k++) {
+    const int n = sm.dims[k];
+    const float c = wrapCoord(tc[k], sm.wrap[k]);
+    if (sm.filter == 0) {
+      i0[k] = i1[k] = wrapIndex((int)std::floor(c * (float)n), n, sm.wrap[k]);
+    } else {
+      const float x = c * (float)n - 0.5f;
+      const float fl = std::floor(x);
+      w[k] = quantW(x - fl, 1);
+      i0[k] = wrapIndex((int)fl, n, sm.wrap[k]);
+      i1[k] = wrapIndex((int)fl + 1, n, sm.wrap[k]);
+    }
+  }
+  auto at = [&](int x, int y, int z, int c) {
+    return sm.image[4 * (((size_t)z * sm.dims[1] + y) * sm.dims[0] + x) + c];
+  };
+  float out[4];
+  for (int c = 0; c < 4; c++) {
+    const float c00 = (1.f - w[0]) * at(i0[0], i0[1], i0[2], c) + w[0] * at(i1[0], i0[1], i0[2], c);
+    if (ndim == 1) {
+      out[c] = c00;
+      continue;
+    }
+    const float c10 = (1.f - w[0]) * at(i0[0], i1[1], i0[2], c) + w[0] * at(i1[0], i1[1], i0[2], c);
+    const float c0 = (1.f - w[1]) * c00 + w[1] * c10;
+    if (ndim == 2) {
+      out[c] = c0;
+      continue;
+    }
+    const float c01 = (1.f - w[0]) * at(i0[0], i0[1], i1[2], c) + w[0] * at(i1[0], i0[1], i1[2], c);
+    const float c11 = (1.f - w[0]) * at(i0[0], i1[1], i1[2], c) + w[0] * at(i1[0], i1[1], i1[2], c);
+    const float c1 = (1.f - w[1]) * c01 + w[1] * c11;
+    out[c] = (1.f - w[2]) * c0 + w[2] * c1;
+  }
+  return {out[0], out[1], out[2], out[3]};
+}
+
+// glm mat4 * vec4 (pairwise sums of the column products) + offset
+V4 affine4(const float *m, V4 v, const float *o)
+{
+  float r[4];
+  for (int i = 0; i < 4; i++)
+    r[i] = (m[i] * v.x + m[4 + i] * v.y) + (m[8 + i] * v.z + m[12 + i] * v.w);
+  return {r[0] + o[0], r[1] + o[1], r[2] + o[2], r[3] + o[3]};
+}
+
+// evaluateSampler (gpu/evalMaterialParameters.h:291-334)
+V4 evaluateSampler(const SceneCtx &S, const SHit &sh, const OrcSampler &sm)
+{
+  V4 r{0.f, 0.f, 0.f, 1.f};
+  const V4 tc = affine4(sm.inT, readAttribute(S, sh, sm.attribute), sm.inO);
+  const float t3[3] = {tc.x, tc.y, tc.z};
+  if (sm.type >= 1 && sm.type <= 3 && sm.image)
+    r = texSample(sm, sm.type, t3);
+  else if (sm.type == 5)
+    r = attrValue(sm.prim, sh.prim + sm.primOffset, r);
+  else if (sm.type == 4)
+    r = tc;
+  return affine4(sm.outT, r, sm.outO);
+}
+
+V4 materialParam(const SceneCtx &S, const SHit &sh, int src, V4 value, const OrcSampler *sm)
 {
   switch (src) {
   case 0:
     return value;
+  case 10:
+    return evaluateSampler(S, sh, *sm);
   case 1:
   case 2:
   case 3:
@@ -1858,8 +1956,10 @@ Matte matteAt(const SceneCtx &S, const SHit &sh)
     m.base = ld3(s.color, 0);
     op = s.colorW * s.opacity;
   } else {
-    const V4 c = materialParam(S, sh, s.colorSrc, {s.color[0], s.color[1], s.color[2], s.colorW});
-    const float o = materialParam(S, sh, s.opacitySrc, {s.opacity, 0.f, 0.f, 1.f}).x;
+    const V4 c = materialParam(
+        S, sh, s.colorSrc, {s.color[0], s.color[1], s.color[2], s.colorW}, &s.colorSampler);
+    const float o =
+        materialParam(S, sh, s.opacitySrc, {s.opacity, 0.f, 0.f, 1.f}, &s.opacitySampler).x;
     m.base = v3(c.x, c.y, c.z);
     op = c.w * o;
   }

@@ -62,6 +62,23 @@ typedef struct OrcAttr {
   int channels;
 } OrcAttr;
 
+/* A material sampler: type 1 image1D, 2 image2D, 3 image3D, 4 transform,
+ * 5 primitive; input attribute slot; column-major in / out maps; the image
+ * as float4 texels (x fastest) with its dims, filter (0 nearest, 1 linear)
+ * and wrap modes (0 clampToEdge, 1 repeat, 2 mirrorRepeat); or the
+ * primitive array and offset. */
+typedef struct OrcSampler {
+  int type;
+  int attribute;
+  float inT[16], inO[4], outT[16], outO[4];
+  const float *image;
+  int dims[3];
+  int filter;
+  int wrap[3];
+  OrcAttr prim;
+  uint32_t primOffset;
+} OrcSampler;
+
 typedef struct OrcSurface {
   int type; /* 0 triangle, 1 sphere, 2 quad, 3 cylinder, 4 cone, 5 curve */
   const float *vertices; /* vec3 */
@@ -88,8 +105,9 @@ typedef struct OrcSurface {
   float uattr[5][4]; /* uniform (default 0, 0, 0, 1) */
   /* matte parameter sources: 0 value, 1..4 attribute0..3, 5 color,
    * 6 worldPosition, 7 worldNormal, 8 objectPosition, 9 objectNormal */
-  int colorSrc, opacitySrc;
+  int colorSrc, opacitySrc; /* 10: the sampler below */
   float colorW; /* w of the colour value */
+  OrcSampler colorSampler, opacitySampler;
 } OrcSurface;
 
 typedef struct OrcInstance {

@@ -33,6 +33,13 @@ class OrcAttr(C.Structure):
     _fields_ = [("data", C.c_void_p), ("type", C.c_int), ("channels", C.c_int)]
 
 
+class OrcSampler(C.Structure):
+    _fields_ = [("type", C.c_int), ("attribute", C.c_int), ("inT", C.c_float * 16),
+                ("inO", C.c_float * 4), ("outT", C.c_float * 16), ("outO", C.c_float * 4),
+                ("image", C.c_void_p), ("dims", C.c_int * 3), ("filter", C.c_int),
+                ("wrap", C.c_int * 3), ("prim", OrcAttr), ("primOffset", C.c_uint32)]
+
+
 class OrcSurface(C.Structure):
     _fields_ = [("type", C.c_int), ("vertices", C.c_void_p), ("indices", C.c_void_p),
                 ("numPrims", C.c_uint32), ("normals", C.c_void_p), ("primIds", C.c_void_p),
@@ -40,13 +47,63 @@ class OrcSurface(C.Structure):
                 ("id", C.c_uint32), ("color", C.c_float * 3), ("opacity", C.c_float),
                 ("alphaMode", C.c_int), ("cutoff", C.c_float), ("caps", C.c_int),
                 ("vattr", OrcAttr * 5), ("pattr", OrcAttr * 5), ("uattr", (C.c_float * 4) * 5),
-                ("colorSrc", C.c_int), ("opacitySrc", C.c_int), ("colorW", C.c_float)]
+                ("colorSrc", C.c_int), ("opacitySrc", C.c_int), ("colorW", C.c_float),
+                ("colorSampler", OrcSampler), ("opacitySampler", OrcSampler)]
 
 
 _ATTR_SLOTS = ("attribute0", "attribute1", "attribute2", "attribute3", "color")
 _PARAM_SOURCES = {"attribute0": 1, "attribute1": 2, "attribute2": 3, "attribute3": 4, "color": 5,
                   "worldPosition": 6, "worldNormal": 7, "objectPosition": 8, "objectNormal": 9}
 _ATTR_CHANNELS = {240: 1, 241: 2, 242: 3, 243: 4, 221: 1, 223: 1, 260: 4, 261: 4}
+_SAMPLER_TYPES = {"image1D": 1, "image2D": 2, "image3D": 3, "transform": 4, "primitive": 5}
+_WRAP = {"clampToEdge": 0, "repeat": 1, "mirrorRepeat": 2}
+_SAMPLER_SLOTS = {"attribute0": 0, "attribute1": 1, "attribute2": 2, "attribute3": 3, "color": 4}
+
+
+def _column_major(m):
+    m = np.eye(4, dtype=np.float32) if m is None else np.asarray(m, np.float32).reshape(4, 4)
+    return (C.c_float * 16)(*np.ascontiguousarray(m.T).ravel().tolist())
+
+
+def _pack_sampler(o, sp, keep):
+    """Fills an OrcSampler from a SamplerSpec. Image texels are staged as
+    float4 the way the device stages them: missing channels 0 (alpha 1),
+    8- and 16-bit values divided by 255 / 65535 in float32."""
+    from visrtx_gb300.scenes import attr_type
+
+    o.type = _SAMPLER_TYPES[sp.type]
+    o.attribute = _SAMPLER_SLOTS[sp.attribute]
+    o.inT = _column_major(sp.in_transform)
+    o.outT = _column_major(sp.out_transform)
+    o.inO = (C.c_float * 4)(*map(float, sp.in_offset))
+    o.outO = (C.c_float * 4)(*map(float, sp.out_offset))
+    nd = sp.image_dims
+    if nd:
+        tex, c = sp.texels()
+        img = np.asarray(sp.image)
+        n = tex.shape[0]
+        t4 = np.zeros((n, 4), np.float32)
+        t4[:, 3] = 1.0
+        src = tex.reshape(n, c)
+        if src.dtype == np.float32:
+            t4[:, :c] = src
+        else:
+            scale = np.float32(65535.0 if src.dtype == np.uint16 else 255.0)
+            t4[:, :c] = src.astype(np.float32) / scale
+        keep.append(t4)
+        o.image = _ptr(t4)
+        shape = img.shape[:nd][::-1]
+        o.dims = (C.c_int * 3)(*(list(shape) + [1] * (3 - nd)))
+        o.filter = 0 if sp.filter == "nearest" else 1
+        o.wrap = (C.c_int * 3)(*[_WRAP[w] for w in sp.wrap])
+    elif sp.type == "primitive":
+        a = np.ascontiguousarray(sp.array)
+        keep.append(a)
+        t = attr_type(a)
+        o.prim.data = _ptr(a)
+        o.prim.type = t
+        o.prim.channels = _ATTR_CHANNELS[t]
+        o.primOffset = int(sp.offset)
 
 
 class OrcInstance(C.Structure):
@@ -197,14 +254,24 @@ def _scene_structs(spec):
         o.radius = s.radius
         o.cullBackfaces = int(bool(s.cull))
         o.id = s.id & 0xFFFFFFFF
-        if isinstance(s.color, str):
+        from visrtx_gb300.scenes import SamplerSpec
+        if isinstance(s.color, SamplerSpec):
+            o.colorSrc = 10
+            _pack_sampler(o.colorSampler, s.color, keep)
+            o.color = (C.c_float * 3)(0.8, 0.8, 0.8)
+            o.colorW = 1.0
+        elif isinstance(s.color, str):
             o.colorSrc = _PARAM_SOURCES[s.color]
             o.color = (C.c_float * 3)(0.8, 0.8, 0.8)
             o.colorW = 1.0
         else:
             o.color = (C.c_float * 3)(*map(float, s.color[:3]))
             o.colorW = float(s.color[3]) if len(s.color) == 4 else 1.0
-        if isinstance(s.opacity, str):
+        if isinstance(s.opacity, SamplerSpec):
+            o.opacitySrc = 10
+            _pack_sampler(o.opacitySampler, s.opacity, keep)
+            o.opacity = 1.0
+        elif isinstance(s.opacity, str):
             o.opacitySrc = _PARAM_SOURCES[s.opacity]
             o.opacity = 1.0
         else:

@@ -217,9 +217,23 @@ class Device:
         a.type_code = L.ARRAY1D
         return a
 
+    def new_array2d(self, data, elem_type: int | None = None) -> Array:
+        """2D array from a (ny, nx) or (ny, nx, c) numpy array (x fastest);
+        `elem_type` gives the element type of c-channel data."""
+        arr = np.ascontiguousarray(data)
+        if elem_type is None:
+            elem_type = _NP_TYPES[(arr.dtype, arr.shape[2] if arr.ndim == 3 else 1)]
+        ny, nx = arr.shape[:2]
+        h = self.lib.vrtxNewArray2D(self.h, arr.ctypes.data_as(C.c_void_p), None, None,
+                                    elem_type, nx, ny)
+        a = Array(self, h, elem_type, arr)
+        a.type_code = L.ARRAY2D
+        return a
+
     def new_array3d(self, data, elem_type: int | None = None) -> Array:
-        """3D array from a (nz, ny, nx) numpy array (x fastest), or a CUDA
-        tensor of that shape (used in place, NV_ARRAY_CUDA)."""
+        """3D array from a (nz, ny, nx) or (nz, ny, nx, c) numpy array (x
+        fastest), or a CUDA tensor of shape (nz, ny, nx) (used in place,
+        NV_ARRAY_CUDA)."""
         if hasattr(data, "data_ptr") and getattr(data, "is_cuda", False):
             nz, ny, nx = data.shape
             et = elem_type or L.FLOAT32
@@ -230,8 +244,8 @@ class Device:
             return a
         arr = np.ascontiguousarray(data)
         if elem_type is None:
-            elem_type = _NP_TYPES[(arr.dtype, 1)]
-        nz, ny, nx = arr.shape
+            elem_type = _NP_TYPES[(arr.dtype, arr.shape[3] if arr.ndim == 4 else 1)]
+        nz, ny, nx = arr.shape[:3]
         h = self.lib.vrtxNewArray3D(self.h, arr.ctypes.data_as(C.c_void_p), None, None,
                                     elem_type, nx, ny, nz)
         a = Array(self, h, elem_type, arr)
@@ -265,6 +279,9 @@ class Device:
 
     def new_volume(self, subtype="transferFunction1D"):
         return self._obj(Object, self.lib.vrtxNewVolume, L.VOLUME, subtype)
+
+    def new_sampler(self, subtype="image2D"):
+        return self._obj(Object, self.lib.vrtxNewSampler, L.SAMPLER, subtype)
 
     def new_surface(self):
         return self._obj(Object, self.lib.vrtxNewSurface, L.SURFACE)

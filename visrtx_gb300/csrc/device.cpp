@@ -774,10 +774,237 @@ void Material::commit()
   };
   gpu.colorSrc = source("color");
   gpu.opacitySrc = source("opacity");
+  colorSampler = static_cast<Sampler *>(getObject("color", VRTX_SAMPLER));
+  opacitySampler = static_cast<Sampler *>(getObject("opacity", VRTX_SAMPLER));
+  if (colorSampler)
+    gpu.colorSrc = PARAM_SAMPLER;
+  if (opacitySampler)
+    gpu.opacitySrc = PARAM_SAMPLER;
   gpu.cutoff = get<float>("alphaCutoff", VRTX_FLOAT32, 0.5f);
   const std::string mode = getString("alphaMode", "opaque");
   gpu.alphaMode = mode == "blend" ? ALPHA_BLEND
                                   : (mode == "mask" ? ALPHA_MASK : ALPHA_OPAQUE);
+}
+
+uint64_t Material::deepStamp() const
+{
+  uint64_t s = commitStamp;
+  for (const Sampler *sm : {colorSampler, opacitySampler})
+    if (sm)
+      s = std::max(s, sm->deepStamp());
+  return s;
+}
+
+// ---------------------------------------------------------------------------
+// Sampler (Sampler.cpp:68-95, Image1D/2D/3D.cpp, TransformSampler.cpp,
+// PrimitiveSampler.cpp)
+// ---------------------------------------------------------------------------
+
+Sampler::~Sampler()
+{
+  cleanup();
+}
+
+void Sampler::cleanup()
+{
+  if (Object::dev->initOk) {
+    if (tex)
+      cudaDestroyTextureObject(tex);
+    if (cuArray)
+      cudaFreeArray(cuArray);
+  }
+  tex = 0;
+  cuArray = nullptr;
+  builtStamp = 0;
+}
+
+uint32_t Sampler::type() const
+{
+  if (subtype == "image1D")
+    return SAMPLER_IMAGE1D;
+  if (subtype == "image2D")
+    return SAMPLER_IMAGE2D;
+  if (subtype == "image3D")
+    return SAMPLER_IMAGE3D;
+  if (subtype == "transform")
+    return SAMPLER_TRANSFORM;
+  if (subtype == "primitive")
+    return SAMPLER_PRIMITIVE;
+  return SAMPLER_NONE;
+}
+
+void Sampler::commit()
+{
+  const std::string a = getString("inAttribute", "attribute0");
+  attribute = a == "attribute1" ? 1u
+      : a == "attribute2"       ? 2u
+      : a == "attribute3"       ? 3u
+      : a == "color"            ? 4u
+                                : 0u;
+  const float ident[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};
+  std::memcpy(inT, ident, sizeof(ident));
+  std::memcpy(outT, ident, sizeof(ident));
+  if (has("inTransform", VRTX_FLOAT32_MAT4))
+    std::memcpy(inT, params["inTransform"].bytes.data(), 64);
+  if (has("outTransform", VRTX_FLOAT32_MAT4))
+    std::memcpy(outT, params["outTransform"].bytes.data(), 64);
+  float o[4] = {0, 0, 0, 0};
+  if (has("inOffset", VRTX_FLOAT32_VEC4))
+    std::memcpy(o, params["inOffset"].bytes.data(), 16);
+  inO = make_float4(o[0], o[1], o[2], o[3]);
+  float q[4] = {0, 0, 0, 0};
+  if (has("outOffset", VRTX_FLOAT32_VEC4))
+    std::memcpy(q, params["outOffset"].bytes.data(), 16);
+  outO = make_float4(q[0], q[1], q[2], q[3]);
+  filter = getString("filter", "linear");
+  // image1D reads "wrapMode", image2D / image3D "wrapMode1/2/3"
+  wrap[0] = getString(type() == SAMPLER_IMAGE1D ? "wrapMode" : "wrapMode1", "clampToEdge");
+  wrap[1] = getString("wrapMode2", "clampToEdge");
+  wrap[2] = getString("wrapMode3", "clampToEdge");
+  image = nullptr;
+  primArray = nullptr;
+  const uint32_t t = type();
+  if (t == SAMPLER_IMAGE1D)
+    image = static_cast<Array *>(getObject("image", VRTX_ARRAY1D));
+  else if (t == SAMPLER_IMAGE2D)
+    image = static_cast<Array *>(getObject("image", VRTX_ARRAY2D));
+  else if (t == SAMPLER_IMAGE3D)
+    image = static_cast<Array *>(getObject("image", VRTX_ARRAY3D));
+  else if (t == SAMPLER_PRIMITIVE) {
+    primArray = static_cast<Array *>(getObject("array", VRTX_ARRAY1D));
+    primOffset = (uint32_t)get<uint64_t>("offset", VRTX_UINT64, get<uint32_t>("offset", VRTX_UINT32, 0u));
+  } else if (t == SAMPLER_NONE)
+    report(VRTX_SEVERITY_WARNING, "sampler subtype '%s' is not supported", subtype.c_str());
+  if ((t == SAMPLER_IMAGE1D || t == SAMPLER_IMAGE2D || t == SAMPLER_IMAGE3D) && !image)
+    report(VRTX_SEVERITY_WARNING, "missing required parameter 'image' on %s sampler",
+        subtype.c_str());
+}
+
+bool Sampler::isValid() const
+{
+  const uint32_t t = type();
+  if (t == SAMPLER_TRANSFORM)
+    return true;
+  if (t == SAMPLER_PRIMITIVE)
+    return primArray != nullptr;
+  return t != SAMPLER_NONE && image != nullptr;
+}
+
+uint64_t Sampler::deepStamp() const
+{
+  uint64_t s = commitStamp;
+  for (const Array *a : {image, primArray})
+    if (a)
+      s = std::max(s, a->deepStamp());
+  return s;
+}
+
+static cudaTextureAddressMode addressMode(const std::string &w)
+{
+  // stringToAddressMode (utility/CudaImageTexture.cpp:129-137)
+  if (w == "repeat")
+    return cudaAddressModeWrap;
+  if (w == "mirrorRepeat")
+    return cudaAddressModeMirror;
+  return cudaAddressModeClamp;
+}
+
+// Image samplers: the image as a float4 cudaArray (missing channels 0, alpha
+// 1; 8-bit values normalised, sRGB ones linearised as the reference's float
+// staging does), with a normalised-coordinate texture of the sampler's
+// filter and wrap modes.
+bool Sampler::ensureBuilt()
+{
+  const uint32_t t = type();
+  if (t != SAMPLER_IMAGE1D && t != SAMPLER_IMAGE2D && t != SAMPLER_IMAGE3D)
+    return true;
+  if (!image)
+    return false;
+  const uint64_t want = deepStamp();
+  if (builtStamp >= want && tex)
+    return true;
+  cleanup();
+  const uint32_t ch = attrChannels(image->elemType);
+  if (!ch) {
+    report(VRTX_SEVERITY_WARNING, "image sampler: unsupported image element type");
+    return false;
+  }
+  const size_t n = (size_t)image->n[0] * image->n[1] * image->n[2];
+  std::vector<float> staging(4 * n);
+  std::vector<uint8_t> host(image->bytes());
+  cudaMemcpy(host.data(), image->deviceData(), host.size(), cudaMemcpyDefault);
+  auto srgbToLinear = [](float c) {
+    return c <= 0.04045f ? c / 12.92f : std::pow((c + 0.055f) / 1.055f, 2.4f);
+  };
+  for (size_t i = 0; i < n; i++) {
+    float v[4] = {0.f, 0.f, 0.f, 1.f};
+    const int et = image->elemType;
+    if (et >= VRTX_FLOAT32 && et <= VRTX_FLOAT32_VEC4)
+      std::memcpy(v, host.data() + i * ch * 4, ch * 4);
+    else if (et == VRTX_UFIXED16)
+      v[0] = ((const uint16_t *)host.data())[i] / 65535.f;
+    else {
+      const uint8_t *p = host.data() + i * ch;
+      for (uint32_t c = 0; c < ch; c++)
+        v[c] = p[c] / 255.f;
+      if (et == VRTX_UFIXED8_RGBA_SRGB)
+        for (int c = 0; c < 3; c++)
+          v[c] = srgbToLinear(v[c]);
+    }
+    std::memcpy(&staging[4 * i], v, 16);
+  }
+  cudaChannelFormatDesc desc = cudaCreateChannelDesc(32, 32, 32, 32, cudaChannelFormatKindFloat);
+  const cudaExtent ext = make_cudaExtent(image->n[0],
+      t >= SAMPLER_IMAGE2D ? image->n[1] : 0,
+      t == SAMPLER_IMAGE3D ? image->n[2] : 0);
+  if (cudaMalloc3DArray(&cuArray, &desc, ext) != cudaSuccess) {
+    cudaGetLastError();
+    cuArray = nullptr;
+    report(VRTX_SEVERITY_ERROR, "image sampler: cudaMalloc3DArray failed");
+    return false;
+  }
+  cudaMemcpy3DParms cp{};
+  cp.srcPtr = make_cudaPitchedPtr(staging.data(), image->n[0] * 16, image->n[0],
+      t >= SAMPLER_IMAGE2D ? image->n[1] : 1);
+  cp.dstArray = cuArray;
+  cp.extent = make_cudaExtent(image->n[0],
+      t >= SAMPLER_IMAGE2D ? image->n[1] : 1,
+      t == SAMPLER_IMAGE3D ? image->n[2] : 1);
+  cp.kind = cudaMemcpyHostToDevice;
+  cudaMemcpy3D(&cp);
+  cudaResourceDesc rd{};
+  rd.resType = cudaResourceTypeArray;
+  rd.res.array.array = cuArray;
+  cudaTextureDesc td{};
+  for (int k = 0; k < 3; k++)
+    td.addressMode[k] = addressMode(wrap[k]);
+  td.filterMode = filter == "nearest" ? cudaFilterModePoint : cudaFilterModeLinear;
+  td.readMode = cudaReadModeElementType;
+  td.normalizedCoords = 1;
+  cudaCreateTextureObject(&tex, &rd, &td, nullptr);
+  builtStamp = want;
+  return cudaGetLastError() == cudaSuccess;
+}
+
+SamplerGPU Sampler::gpuData() const
+{
+  SamplerGPU g{};
+  g.type = type();
+  g.attribute = attribute;
+  g.tex = tex;
+  std::memcpy(g.inT, inT, 64);
+  std::memcpy(g.outT, outT, 64);
+  g.inO = inO;
+  g.outO = outO;
+  if (primArray) {
+    g.prim.data = const_cast<Array *>(primArray)->deviceData();
+    g.prim.type = (uint32_t)primArray->elemType;
+    g.prim.channels = attrChannels(primArray->elemType);
+    if (!g.prim.channels)
+      g.prim.data = nullptr;
+  }
+  g.primOffset = primOffset;
+  return g;
 }
 
 void Light::commit()
@@ -828,7 +1055,7 @@ uint64_t Surface::deepStamp() const
   if (geometry)
     s = std::max(s, geometry->deepStamp());
   if (material)
-    s = std::max(s, material->commitStamp);
+    s = std::max(s, material->deepStamp());
   return s;
 }
 
@@ -1541,9 +1768,33 @@ bool World::rebuild()
   for (Geometry *g : geoms)
     hGeoms.push_back(g->gpuData());
   std::vector<MaterialGPU> hMats;
+  std::vector<SamplerGPU> hSamplers;
+  std::map<Sampler *, uint32_t> samplerIdx;
+  auto samplerSlot = [&](Sampler *sm) -> uint32_t {
+    if (!sm || !sm->isValid() || !sm->ensureBuilt())
+      return ~0u;
+    auto it = samplerIdx.find(sm);
+    if (it != samplerIdx.end())
+      return it->second;
+    const uint32_t k = (uint32_t)hSamplers.size();
+    samplerIdx[sm] = k;
+    hSamplers.push_back(sm->gpuData());
+    return k;
+  };
   bool allOpaque = true;
   for (Material *m : mats) {
-    hMats.push_back(m->gpu);
+    MaterialGPU mg = m->gpu;
+    if (mg.colorSrc == PARAM_SAMPLER) {
+      mg.colorSampler = samplerSlot(m->colorSampler);
+      if (mg.colorSampler == ~0u)
+        mg.colorSrc = PARAM_VALUE;
+    }
+    if (mg.opacitySrc == PARAM_SAMPLER) {
+      mg.opacitySampler = samplerSlot(m->opacitySampler);
+      if (mg.opacitySampler == ~0u)
+        mg.opacitySrc = PARAM_VALUE;
+    }
+    hMats.push_back(mg);
     if (m->gpu.alphaMode != ALPHA_OPAQUE)
       allOpaque = false;
   }
@@ -1553,6 +1804,7 @@ bool World::rebuild()
         geomIdx[sf->geometry], matIdx[sf->material], sf->id, 0u});
   GeometryGPU *dGeoms = uploadVec(this, hGeoms, s);
   MaterialGPU *dMats = uploadVec(this, hMats, s);
+  SamplerGPU *dSamplers = hSamplers.empty() ? nullptr : uploadVec(this, hSamplers, s);
   SurfaceGPU *dSurfs = uploadVec(this, hSurfs, s);
 
   // BLAS per (group, primitive class)
@@ -1759,6 +2011,7 @@ bool World::rebuild()
   gpu.surfaces = dSurfs;
   gpu.geometries = dGeoms;
   gpu.materials = dMats;
+  gpu.samplers = dSamplers;
   gpu.lights = uploadVec(this, lights, s);
   gpu.numLights = (uint32_t)lights.size();
   gpu.volumes = uploadVec(this, vols, s);
@@ -2496,7 +2749,7 @@ VRTX_API VRTXObject vrtxNewRenderer(VRTXDevice d, const char *st)
 }
 VRTX_API VRTXObject vrtxNewSampler(VRTXDevice d, const char *st)
 {
-  return newObj<Object>(d, VRTX_SAMPLER, st);
+  return newObj<Sampler>(d, VRTX_SAMPLER, st);
 }
 VRTX_API VRTXObject vrtxNewSpatialField(VRTXDevice d, const char *st)
 {

@@ -93,7 +93,35 @@ enum ParamSource : uint32_t
   PARAM_WORLD_POSITION = 6,
   PARAM_WORLD_NORMAL = 7,
   PARAM_OBJECT_POSITION = 8,
-  PARAM_OBJECT_NORMAL = 9
+  PARAM_OBJECT_NORMAL = 9,
+  PARAM_SAMPLER = 10
+};
+
+enum SamplerType : uint32_t
+{
+  SAMPLER_NONE = 0,
+  SAMPLER_IMAGE1D = 1,
+  SAMPLER_IMAGE2D = 2,
+  SAMPLER_IMAGE3D = 3,
+  SAMPLER_TRANSFORM = 4,
+  SAMPLER_PRIMITIVE = 5
+};
+
+// A material sampler (SamplerGPUData of the reference): its input attribute
+// slot, input / output affine maps (column-major 4x4 + offset), and an image
+// texture (float4, normalised coordinates) or a primitive array.
+struct SamplerGPU
+{
+  uint32_t type; // SamplerType
+  uint32_t attribute; // 0..3 attribute0..3, 4 color
+  cudaTextureObject_t tex;
+  float inT[16];
+  float4 inO;
+  float outT[16];
+  float4 outO;
+  AttrGPU prim; // primitive sampler: the array
+  uint32_t primOffset;
+  uint32_t pad;
 };
 
 struct MaterialGPU
@@ -106,7 +134,9 @@ struct MaterialGPU
   uint32_t opacitySrc; // ParamSource of "opacity"
   float4 colorValue; // the "color" value with its w
   float opacityValue; // the "opacity" value
-  uint32_t pad[3];
+  uint32_t colorSampler; // index into WorldGPU::samplers (PARAM_SAMPLER)
+  uint32_t opacitySampler;
+  uint32_t pad;
 };
 
 struct SurfaceGPU
@@ -319,6 +349,7 @@ struct WorldGPU
   uint32_t numVolumes;
   uint32_t allOpaque; // every material is opaque: any-hit = first hit
   uint32_t hasSegments; // some BLAS holds cylinders, cones or curves
+  const SamplerGPU *samplers; // the materials' samplers
 };
 
 // Per-thread work counters. Rays and volume samples are counted by every

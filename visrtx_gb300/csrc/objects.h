@@ -165,11 +165,39 @@ struct Geometry : Object
   GeometryGPU gpuData();
 };
 
+// Material samplers (scene/surface/material/sampler/*.cpp): image1D /
+// image2D / image3D (float4 texture from the image array), transform,
+// primitive.
+struct Sampler : Object
+{
+  using Object::Object;
+  ~Sampler() override;
+  Array *image = nullptr, *primArray = nullptr;
+  std::string filter = "linear";
+  std::string wrap[3] = {"clampToEdge", "clampToEdge", "clampToEdge"};
+  uint32_t attribute = 0;
+  float inT[16], outT[16];
+  float4 inO{0.f, 0.f, 0.f, 0.f}, outO{0.f, 0.f, 0.f, 0.f};
+  uint32_t primOffset = 0;
+  cudaArray_t cuArray = nullptr;
+  cudaTextureObject_t tex = 0;
+  uint64_t builtStamp = 0;
+  void commit() override;
+  bool isValid() const override;
+  uint64_t deepStamp() const override;
+  void cleanup();
+  bool ensureBuilt();
+  SamplerGPU gpuData() const;
+  uint32_t type() const;
+};
+
 struct Material : Object
 {
   using Object::Object;
   MaterialGPU gpu{};
+  Sampler *colorSampler = nullptr, *opacitySampler = nullptr;
   void commit() override;
+  uint64_t deepStamp() const override;
 };
 
 struct Light : Object

@@ -237,17 +237,21 @@ struct MatteState
 
 // --- geometry attributes and material parameters ---------------------------
 
+// attribute arithmetic, rounded per operation (no contraction) so that
+// interpolated values feeding sampler coordinates are build-independent
 __device__ __forceinline__ float4 f4add(float4 a, float4 b)
 {
-  return make_float4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w);
+  return make_float4(
+      __fadd_rn(a.x, b.x), __fadd_rn(a.y, b.y), __fadd_rn(a.z, b.z), __fadd_rn(a.w, b.w));
 }
 __device__ __forceinline__ float4 f4sub(float4 a, float4 b)
 {
-  return make_float4(a.x - b.x, a.y - b.y, a.z - b.z, a.w - b.w);
+  return make_float4(
+      __fsub_rn(a.x, b.x), __fsub_rn(a.y, b.y), __fsub_rn(a.z, b.z), __fsub_rn(a.w, b.w));
 }
 __device__ __forceinline__ float4 f4mul(float4 a, float s)
 {
-  return make_float4(a.x * s, a.y * s, a.z * s, a.w * s);
+  return make_float4(__fmul_rn(a.x, s), __fmul_rn(a.y, s), __fmul_rn(a.z, s), __fmul_rn(a.w, s));
 }
 
 // glm::convertLinearToSRGB (gamma 0.41666) on one channel
@@ -365,13 +369,63 @@ __device__ __forceinline__ float4 readAttribute(
   return uf;
 }
 
+// column-major 4x4 times a vec4, plus an offset (glm's mat4 * vec4 sums
+// the column products pairwise: (c0 + c1) + (c2 + c3)); rounded per
+// operation, without contraction, so image lookups see the same coordinates
+// on every build
+__device__ __forceinline__ float4 affine4(const float *m, float4 v, float4 o)
+{
+  float r[4];
+#pragma unroll
+  for (int i = 0; i < 4; i++)
+    r[i] = __fadd_rn(__fadd_rn(__fmul_rn(m[i], v.x), __fmul_rn(m[4 + i], v.y)),
+        __fadd_rn(__fmul_rn(m[8 + i], v.z), __fmul_rn(m[12 + i], v.w)));
+  return make_float4(
+      __fadd_rn(r[0], o.x), __fadd_rn(r[1], o.y), __fadd_rn(r[2], o.z), __fadd_rn(r[3], o.w));
+}
+
+// evaluateSampler (gpu/evalMaterialParameters.h:291-334): the input
+// attribute through the input map, an image lookup / the primitive array /
+// the mapped value itself, then the output map
+__device__ __forceinline__ float4 evaluateSampler(
+    const WorldGPU &w, const SurfaceHit &sh, const SamplerGPU &sm)
+{
+  float4 r = make_float4(0.f, 0.f, 0.f, 1.f);
+  const float4 tc = affine4(sm.inT, readAttribute(w, sh, (int)sm.attribute), sm.inO);
+  switch (sm.type) {
+  case SAMPLER_IMAGE1D:
+    r = tex1D<float4>(sm.tex, tc.x);
+    break;
+  case SAMPLER_IMAGE2D:
+    r = tex2D<float4>(sm.tex, tc.x, tc.y);
+    break;
+  case SAMPLER_IMAGE3D:
+    r = tex3D<float4>(sm.tex, tc.x, tc.y, tc.z);
+    break;
+  case SAMPLER_PRIMITIVE:
+    r = attrValue(sm.prim, sh.primID + sm.primOffset, r);
+    break;
+  case SAMPLER_TRANSFORM:
+    r = tc;
+    break;
+  default:
+    break;
+  }
+  return affine4(sm.outT, r, sm.outO);
+}
+
 // getMaterialParameter (gpu/evalMaterialParameters.h:336-374)
-__device__ __forceinline__ float4 materialParam(
-    const WorldGPU &w, const SurfaceHit &sh, uint32_t src, float4 value)
+__device__ __forceinline__ float4 materialParam(const WorldGPU &w,
+    const SurfaceHit &sh,
+    uint32_t src,
+    float4 value,
+    uint32_t sampler)
 {
   switch (src) {
   case PARAM_VALUE:
     return value;
+  case PARAM_SAMPLER:
+    return evaluateSampler(w, sh, w.samplers[sampler]);
   case PARAM_ATTRIB_0:
   case PARAM_ATTRIB_0 + 1:
   case PARAM_ATTRIB_0 + 2:
@@ -401,9 +455,13 @@ __device__ __forceinline__ MatteState matteInit(const WorldGPU &w, const Surface
     s.baseColor = m.color;
     op = m.opacity;
   } else {
-    const float4 c = materialParam(w, sh, m.colorSrc, m.colorValue);
-    const float o =
-        materialParam(w, sh, m.opacitySrc, make_float4(m.opacityValue, 0.f, 0.f, 1.f)).x;
+    const float4 c = materialParam(w, sh, m.colorSrc, m.colorValue, m.colorSampler);
+    const float o = materialParam(w,
+        sh,
+        m.opacitySrc,
+        make_float4(m.opacityValue, 0.f, 0.f, 1.f),
+        m.opacitySampler)
+                        .x;
     s.baseColor = mk3(c.x, c.y, c.z);
     op = c.w * o;
   }

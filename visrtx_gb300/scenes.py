@@ -281,6 +281,38 @@ from dataclasses import dataclass, field as _field
 
 
 @dataclass
+class SamplerSpec:
+    """A material sampler (sampler/Image1D.cpp, Image2D.cpp, Image3D.cpp,
+    TransformSampler.cpp, PrimitiveSampler.cpp): "image1D" / "image2D" /
+    "image3D" over `image` ((n[, c]) / (ny, nx[, c]) / (nz, ny, nx[, c]);
+    float32 x1-4, uint8 x1 / x4, uint16 x1), "transform", or "primitive" over
+    `array` (an attribute-typed array read at primID + offset). Transforms
+    are 4x4 in row-major (math) layout."""
+    type: str
+    image: np.ndarray | None = None
+    array: np.ndarray | None = None
+    offset: int = 0
+    attribute: str = "attribute0"
+    filter: str = "linear"
+    wrap: tuple = ("clampToEdge", "clampToEdge", "clampToEdge")
+    in_transform: np.ndarray | None = None
+    in_offset: tuple = (0.0, 0.0, 0.0, 0.0)
+    out_transform: np.ndarray | None = None
+    out_offset: tuple = (0.0, 0.0, 0.0, 0.0)
+
+    @property
+    def image_dims(self) -> int:
+        return int(self.type[5]) if self.type.startswith("image") else 0
+
+    def texels(self) -> tuple[np.ndarray, int]:
+        """The image as (texels, channels): texels reshaped to (n, c)."""
+        nd = self.image_dims
+        img = np.ascontiguousarray(self.image)
+        c = img.shape[nd] if img.ndim > nd else 1
+        return img.reshape(-1, c) if c > 1 else img.reshape(-1), c
+
+
+@dataclass
 class SurfaceSpec:
     type: str  # "triangle" | "quad" | "sphere" | "cylinder" | "cone" | "curve"
     vertices: np.ndarray  # (n, 3) float32
@@ -299,8 +331,9 @@ class SurfaceSpec:
     attrs: dict = _field(default_factory=dict)
     cull: bool = False
     id: int = 0xFFFFFFFF
-    color: tuple | str = (0.8, 0.8, 0.8)  # value, or an attribute / hit quantity name
-    opacity: float | str = 1.0
+    # value, an attribute / hit quantity name, or a SamplerSpec
+    color: tuple | str | SamplerSpec = (0.8, 0.8, 0.8)
+    opacity: float | str | SamplerSpec = 1.0
     alpha_mode: str = "opaque"
     cutoff: float = 0.5
 
@@ -431,6 +464,37 @@ def build_on_device(dev, spec: SceneSpec, channels=("color", "depth", "primitive
         keep.append(x)
         return x
 
+    def sampler(sp: SamplerSpec):
+        smp = dev.new_sampler(sp.type)
+        nd = sp.image_dims
+        if nd:
+            tex, _ = sp.texels()
+            img = np.ascontiguousarray(sp.image)
+            et = attr_type(tex)
+            a = (dev.new_array(tex, et) if nd == 1 else
+                 dev.new_array2d(img, et) if nd == 2 else dev.new_array3d(img, et))
+            keep.append(a)
+            smp.set("image", a)
+            smp.set("filter", sp.filter)
+            if nd == 1:
+                smp.set("wrapMode", sp.wrap[0])
+            else:
+                for k in range(nd):
+                    smp.set(f"wrapMode{k + 1}", sp.wrap[k])
+        elif sp.type == "primitive":
+            a = np.ascontiguousarray(sp.array)
+            smp.set("array", arr(a, attr_type(a)))
+            smp.set("offset", int(sp.offset), L.UINT32)
+        smp.set("inAttribute", sp.attribute)
+        for name, mat in (("inTransform", sp.in_transform), ("outTransform", sp.out_transform)):
+            if mat is not None:
+                smp.set(name, np.asarray(mat, np.float32), L.FLOAT32_MAT4)
+        smp.set("inOffset", tuple(map(float, sp.in_offset)), L.FLOAT32_VEC4)
+        smp.set("outOffset", tuple(map(float, sp.out_offset)), L.FLOAT32_VEC4)
+        smp.commit()
+        keep.append(smp)
+        return smp
+
     surfs = []
     for s in spec.surfaces:
         g = dev.new_geometry(s.type)
@@ -463,12 +527,17 @@ def build_on_device(dev, spec: SceneSpec, channels=("color", "depth", "primitive
             g.set("cullBackfaces", True)
         g.commit()
         m = dev.new_material("matte")
-        if isinstance(s.color, str):
+        if isinstance(s.color, SamplerSpec):
+            m.set("color", sampler(s.color))
+        elif isinstance(s.color, str):
             m.set("color", s.color)
         else:
             m.set("color", tuple(float(c) for c in s.color),
                   L.FLOAT32_VEC4 if len(s.color) == 4 else L.FLOAT32_VEC3)
-        m.set("opacity", s.opacity if isinstance(s.opacity, str) else float(s.opacity))
+        if isinstance(s.opacity, SamplerSpec):
+            m.set("opacity", sampler(s.opacity))
+        else:
+            m.set("opacity", s.opacity if isinstance(s.opacity, str) else float(s.opacity))
         m.set("alphaMode", s.alpha_mode)
         m.set("alphaCutoff", float(s.cutoff))
         m.commit()
