@@ -52,8 +52,9 @@ def _args():
     p.add_argument("--cpu-seconds", type=float, default=12.0)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--workload", default="instanced",
-                   choices=["instanced", "volume", "dm", "batched"],
-                   help="instanced (default line) | volume | dm | batched")
+                   choices=["instanced", "volume", "nanovdb", "dm", "batched"],
+                   help="instanced (default line) | volume | nanovdb | dm | batched")
+    p.add_argument("--nvdb-type", default="fp16", choices=["float", "fp4", "fp8", "fp16", "fpn"])
     p.add_argument("--dm-views", type=int, default=128)
     return p.parse_args()
 
@@ -221,7 +222,8 @@ def main():
     if args.workload != "instanced":
         import bench_workloads as BW
 
-        {"volume": BW.run_volume, "dm": BW.run_dm, "batched": BW.run_batched}[args.workload](
+        {"volume": BW.run_volume, "nanovdb": BW.run_nanovdb, "dm": BW.run_dm,
+         "batched": BW.run_batched}[args.workload](
             args, ws, rank, local)
         return
     if args.impl == "reference":

@@ -72,6 +72,8 @@ typedef enum VRTXDataType {
 
   VRTX_INT32 = 200,
   VRTX_INT32_VEC2 = 201,
+  VRTX_INT8 = 202,
+  VRTX_UINT8 = 203, /* raw bytes, e.g. a NanoVDB grid buffer */
   VRTX_UINT32 = 210,
   VRTX_UINT32_VEC2 = 211,
   VRTX_UINT32_VEC3 = 212,

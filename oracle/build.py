@@ -1,8 +1,13 @@
-"""Builds the CPU oracle (test infrastructure) into oracle/_build/liboracle.so.
+"""Builds the CPU oracle (test infrastructure) into oracle/_build/liboracle.so,
+and, where the reference tree is present, oracle/_ref/libnvdbref.so.
 
-The reference itself cannot be compiled here (its device path needs OptiX
-headers fetched at configure time and the ANARI-SDK, neither present), so
-there is no oracle/_ref build; see oracle.h for the parity status.
+The reference's renderer cannot be compiled here (its device path needs
+OptiX headers fetched at configure time and the ANARI-SDK, neither present);
+see oracle.h for the parity status. The NanoVDB library it vendors
+(external/nanovdb, header-only) does compile with g++ alone: ref_nvdb.cpp
+drives its grid builder, sampler and validator, compiled from the headers
+where they lie under the reference tree, with the output only in
+oracle/_ref/. The GPU machine has no reference tree and never builds it.
 """
 from __future__ import annotations
 
@@ -30,5 +35,31 @@ def build() -> str:
     return LIB
 
 
+REF_TREE = "/root/reference"
+REF_OUT = os.path.join(HERE, "_ref")
+REF_LIB = os.path.join(REF_OUT, "libnvdbref.so")
+
+
+def build_ref() -> str | None:
+    """oracle/_ref/libnvdbref.so from ref_nvdb.cpp and the reference's vendored
+    NanoVDB headers; None when the reference tree is absent."""
+    inc = os.path.join(REF_TREE, "external", "nanovdb", "include")
+    if not os.path.isdir(inc):
+        return None
+    src = os.path.join(HERE, "ref_nvdb.cpp")
+    os.makedirs(REF_OUT, exist_ok=True)
+    if os.path.exists(REF_LIB) and os.path.getmtime(REF_LIB) >= os.path.getmtime(src):
+        return REF_LIB
+    tmp = REF_LIB + ".tmp"
+    cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off",
+           "-I", inc, "-o", tmp, src, "-lpthread"]
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError("oracle/_ref build failed:\n" + res.stdout + res.stderr)
+    os.replace(tmp, REF_LIB)
+    return REF_LIB
+
+
 if __name__ == "__main__":
     print(build())
+    print(build_ref())

@@ -1269,16 +1269,16 @@ struct VolHit
   float t0, t1;
 };
 
+void volBounds(const OrcVolume &v, V3 &lo, V3 &hi);
+void gridDims(const OrcVolume &v, int d[3]);
+
 bool volumeSlab(const OrcVolume &v, const X34 &w2o, V3 o, V3 d, float tmin, float tmax,
     VolHit &h)
 {
   const V3 lo = xPoint(w2o, o), ld = xVec(w2o, d);
   const V3 inv = v3(1.f / ld.x, 1.f / ld.y, 1.f / ld.z);
-  const V3 blo = ld3(v.origin, 0);
-  const V3 bhi = blo
-      + v3((float)(v.dims[0] - 1) * v.spacing[0],
-          (float)(v.dims[1] - 1) * v.spacing[1],
-          (float)(v.dims[2] - 1) * v.spacing[2]);
+  V3 blo, bhi;
+  volBounds(v, blo, bhi);
   const V3 mins = (blo - lo) * inv, maxs = (bhi - lo) * inv;
   const V3 nr = v3(std::min(mins.x, maxs.x), std::min(mins.y, maxs.y), std::min(mins.z, maxs.z));
   const V3 fr = v3(std::max(mins.x, maxs.x), std::max(mins.y, maxs.y), std::max(mins.z, maxs.z));
@@ -1299,8 +1299,185 @@ struct VolCtx
   std::vector<X34> w2o;
 };
 
+// ---------------------------------------------------------------------------
+// NanoVDB grids (the layout of the NanoVDB version the reference vendors,
+// external/nanovdb/include/nanovdb/NanoVDB.h, 32.7): GridData 672 B, then
+// TreeData 64 B whose mNodeOffset[3] locates the RootData; RootData 64 B
+// (index bbox, tile count, background, stats) followed by 32-byte tiles
+// (key, child offset from the RootData, state, value); upper nodes (32^3
+// entries: child mask at 4128, table of 8-byte entries at 8256), lower
+// nodes (16^3: child mask at 544, table at 1088) whose table entries hold a
+// child offset from the node or a tile value; leaves (8^3) whose values
+// start at byte 96 (float) or whose codes do (Fp4/Fp8/Fp16/FpN, decoded as
+// code * quantum + minimum with the minimum at 80 and the quantum at 84).
+// ---------------------------------------------------------------------------
+
+struct Nvdb
+{
+  const uint8_t *grid = nullptr, *root = nullptr;
+  uint32_t type = 0, tiles = 0;
+  float background = 0.f;
+  float inv[9], vec[3];
+  double wlo[3], whi[3], voxel[3];
+  int ilo[3], ihi[3];
+};
+
+template <typename T>
+T rd(const uint8_t *p)
+{
+  T v;
+  std::memcpy(&v, p, sizeof(T));
+  return v;
+}
+
+bool nvdbOpen(const uint8_t *g, Nvdb &n)
+{
+  if (!g)
+    return false;
+  const uint64_t magic = rd<uint64_t>(g);
+  if (magic != 0x304244566F6E614EULL && magic != 0x314244566F6E614EULL)
+    return false;
+  if ((rd<uint32_t>(g + 16) >> 21) != 32u) // major version
+    return false;
+  n.grid = g;
+  n.type = rd<uint32_t>(g + 636);
+  if (n.type != 1 && (n.type < 13 || n.type > 16))
+    return false;
+  for (int k = 0; k < 9; k++)
+    n.inv[k] = rd<float>(g + 296 + 36 + 4 * k);
+  for (int k = 0; k < 3; k++) {
+    n.vec[k] = rd<float>(g + 296 + 72 + 4 * k);
+    n.wlo[k] = rd<double>(g + 560 + 8 * k);
+    n.whi[k] = rd<double>(g + 584 + 8 * k);
+    n.voxel[k] = rd<double>(g + 608 + 8 * k);
+  }
+  n.root = g + 672 + rd<int64_t>(g + 672 + 24);
+  for (int k = 0; k < 3; k++) {
+    n.ilo[k] = rd<int32_t>(n.root + 4 * k);
+    n.ihi[k] = rd<int32_t>(n.root + 12 + 4 * k);
+  }
+  n.tiles = rd<uint32_t>(n.root + 24);
+  n.background = rd<float>(n.root + 28);
+  return true;
+}
+
+bool maskBit(const uint8_t *mask, uint32_t i)
+{
+  return (rd<uint64_t>(mask + 8 * (i >> 6)) >> (i & 63)) & 1u;
+}
+
+// LeafData<float / Fp4 / Fp8 / Fp16 / FpN>::getValue (NanoVDB.h:3880-4031)
+float nvdbLeafValue(const Nvdb &n, const uint8_t *leaf, uint32_t i, int fused)
+{
+  if (n.type == 1)
+    return rd<float>(leaf + 96 + 4 * i);
+  uint32_t code;
+  if (n.type == 13)
+    code = (leaf[96 + (i >> 1)] >> ((i & 1) << 2)) & 15u;
+  else if (n.type == 14)
+    code = leaf[96 + i];
+  else if (n.type == 15)
+    code = rd<uint16_t>(leaf + 96 + 2 * i);
+  else {
+    const uint32_t b = leaf[15] >> 5; // log2 of the bit width
+    const uint32_t w = rd<uint32_t>(leaf + 96 + 4 * (i >> (5 - b)));
+    code = (w >> ((i & ((32u >> b) - 1u)) << b)) & ((1u << (1u << b)) - 1u);
+  }
+  const float mn = rd<float>(leaf + 80), q = rd<float>(leaf + 84);
+  return fused ? std::fma((float)code, q, mn) : (float)code * q + mn;
+}
+
+// RootNode / InternalNode / LeafNode getValue (NanoVDB.h:2947, 3528)
+float nvdbValue(const Nvdb &n, int x, int y, int z, int fused)
+{
+  const uint64_t key = (uint64_t)((uint32_t)z >> 12) | ((uint64_t)((uint32_t)y >> 12) << 21)
+      | ((uint64_t)((uint32_t)x >> 12) << 42);
+  const uint8_t *tile = nullptr;
+  for (uint32_t t = 0; t < n.tiles; t++) {
+    const uint8_t *p = n.root + 64 + 32 * t;
+    if (rd<uint64_t>(p) == key) {
+      tile = p;
+      break;
+    }
+  }
+  if (!tile)
+    return n.background;
+  const int64_t child = rd<int64_t>(tile + 8);
+  if (!child)
+    return rd<float>(tile + 20);
+  const uint8_t *up = n.root + child;
+  const uint32_t nu = (((uint32_t)x & 4095u) >> 7) << 10 | (((uint32_t)y & 4095u) >> 7) << 5
+      | (((uint32_t)z & 4095u) >> 7);
+  if (!maskBit(up + 4128, nu))
+    return rd<float>(up + 8256 + 8 * nu);
+  const uint8_t *lo = up + rd<int64_t>(up + 8256 + 8 * nu);
+  const uint32_t nl = (((uint32_t)x & 127u) >> 3) << 8 | (((uint32_t)y & 127u) >> 3) << 4
+      | (((uint32_t)z & 127u) >> 3);
+  if (!maskBit(lo + 544, nl))
+    return rd<float>(lo + 1088 + 8 * nl);
+  const uint8_t *leaf = lo + rd<int64_t>(lo + 1088 + 8 * nl);
+  const uint32_t i = ((uint32_t)x & 7u) << 6 | ((uint32_t)y & 7u) << 3 | ((uint32_t)z & 7u);
+  return nvdbLeafValue(n, leaf, i, fused);
+}
+
+// SpatialFieldSampler<nanovdb::Grid> (gpu/sampleSpatialField.h:80-109):
+// worldToIndexF (Map::applyInverseMapF: the location as double minus the
+// float translation, cast to float, then the float inverse matrix through
+// fmaf, math/Math.h matMult), then SampleFromVoxels<_, 1>: floor, the
+// 2x2x2 stencil, and lerps a + w (b - a) over z, then y, then x
+// (math/SampleFromVoxels.h:200-245,400-407).
+float nvdbSample(const Nvdb &n, V3 p, int fused)
+{
+  const float dx = (float)((double)p.x - (double)n.vec[0]);
+  const float dy = (float)((double)p.y - (double)n.vec[1]);
+  const float dz = (float)((double)p.z - (double)n.vec[2]);
+  const float ix = std::fma(dx, n.inv[0], std::fma(dy, n.inv[1], dz * n.inv[2]));
+  const float iy = std::fma(dx, n.inv[3], std::fma(dy, n.inv[4], dz * n.inv[5]));
+  const float iz = std::fma(dx, n.inv[6], std::fma(dy, n.inv[7], dz * n.inv[8]));
+  const double fx = std::floor((double)ix), fy = std::floor((double)iy), fz = std::floor((double)iz);
+  const float ux = (float)((double)ix - fx), uy = (float)((double)iy - fy),
+              uz = (float)((double)iz - fz);
+  const int i = (int32_t)fx, j = (int32_t)fy, k = (int32_t)fz;
+  float v[2][2][2];
+  for (int a = 0; a < 2; a++)
+    for (int b = 0; b < 2; b++)
+      for (int c = 0; c < 2; c++)
+        v[a][b][c] = nvdbValue(n, i + a, j + b, k + c, fused);
+  auto lerp = [&](float a, float b, float w) {
+    return fused ? std::fma(w, b - a, a) : a + w * (b - a);
+  };
+  return lerp(lerp(lerp(v[0][0][0], v[0][0][1], uz), lerp(v[0][1][0], v[0][1][1], uz), uy),
+      lerp(lerp(v[1][0][0], v[1][0][1], uz), lerp(v[1][1][0], v[1][1][1], uz), uy),
+      ux);
+}
+
+// the same lookup in FP64 (exact weights and interpolation; the clean marcher)
+double nvdbSampleExact(const Nvdb &n, double px, double py, double pz)
+{
+  const double ix = (px - n.vec[0]) * n.inv[0] + (py - n.vec[1]) * n.inv[1]
+      + (pz - n.vec[2]) * n.inv[2];
+  const double iy = (px - n.vec[0]) * n.inv[3] + (py - n.vec[1]) * n.inv[4]
+      + (pz - n.vec[2]) * n.inv[5];
+  const double iz = (px - n.vec[0]) * n.inv[6] + (py - n.vec[1]) * n.inv[7]
+      + (pz - n.vec[2]) * n.inv[8];
+  const double fx = std::floor(ix), fy = std::floor(iy), fz = std::floor(iz);
+  const double ux = ix - fx, uy = iy - fy, uz = iz - fz;
+  const int i = (int)fx, j = (int)fy, k = (int)fz;
+  double r = 0.0;
+  for (int a = 0; a < 2; a++)
+    for (int b = 0; b < 2; b++)
+      for (int c = 0; c < 2; c++)
+        r += (a ? ux : 1.0 - ux) * (b ? uy : 1.0 - uy) * (c ? uz : 1.0 - uz)
+            * (double)nvdbValue(n, i + a, j + b, k + c, 1);
+  return r;
+}
+
 float sampleFieldParity(const OrcVolume &v, V3 p, int round)
 {
+  if (v.nvdb) {
+    Nvdb n;
+    return nvdbOpen(v.nvdb, n) ? nvdbSample(n, p, 1) : 0.f;
+  }
   const V3 sp = ld3(v.spacing, 0);
   const V3 inv = v3(1.f / (sp.x * (float)v.dims[0]), 1.f / (sp.y * (float)v.dims[1]),
       1.f / (sp.z * (float)v.dims[2]));
@@ -1326,6 +1503,10 @@ void classifyParity(const OrcVolume &v, float s, int round, float out[4])
 
 float volStep(const OrcVolume &v)
 {
+  // NvdbRegularField::stepSize (NvdbRegularField.cpp:119-122): min voxel / 2
+  Nvdb n;
+  if (v.nvdb && nvdbOpen(v.nvdb, n))
+    return std::min((float)n.voxel[0], std::min((float)n.voxel[1], (float)n.voxel[2])) / 2.f;
   return std::min(v.spacing[0] / 2.f, std::min(v.spacing[1] / 2.f, v.spacing[2] / 2.f));
 }
 
@@ -1376,12 +1557,18 @@ float rayMarchVolume(Ctx &C, const OrcVolume &v, const VolHit &h, Stream &rs, V3
     const double px = (double)h.lo.x + (double)h.ld.x * lo;
     const double py = (double)h.lo.y + (double)h.ld.y * lo;
     const double pz = (double)h.lo.z + (double)h.ld.z * lo;
-    const double cx = ((px - v.origin[0]) + 0.5 * sx) / (sx * v.dims[0]);
-    const double cy = ((py - v.origin[1]) + 0.5 * sy) / (sy * v.dims[1]);
-    const double cz = ((pz - v.origin[2]) + 0.5 * sz) / (sz * v.dims[2]);
-    const double s = v.filterLinear
-        ? tex3dExact(v.field, v.dims, cx, cy, cz)
-        : (double)tex3dPoint(v.field, v.dims, (float)cx, (float)cy, (float)cz);
+    double s;
+    Nvdb nv;
+    if (v.nvdb && nvdbOpen(v.nvdb, nv)) {
+      s = nvdbSampleExact(nv, px, py, pz);
+    } else {
+      const double cx = ((px - v.origin[0]) + 0.5 * sx) / (sx * v.dims[0]);
+      const double cy = ((py - v.origin[1]) + 0.5 * sy) / (sy * v.dims[1]);
+      const double cz = ((pz - v.origin[2]) + 0.5 * sz) / (sz * v.dims[2]);
+      s = v.filterLinear
+          ? tex3dExact(v.field, v.dims, cx, cy, cz)
+          : (double)tex3dPoint(v.field, v.dims, (float)cx, (float)cy, (float)cz);
+    }
     if (!std::isnan(s)) {
       double co[4];
       if (v.tf) {
@@ -1498,6 +1685,13 @@ int projectAxis(float v, float lo, float hi, int n)
 
 void volBounds(const OrcVolume &v, V3 &lo, V3 &hi)
 {
+  // NvdbRegularField::bounds: the grid's world bbox as float
+  Nvdb n;
+  if (v.nvdb && nvdbOpen(v.nvdb, n)) {
+    lo = v3((float)n.wlo[0], (float)n.wlo[1], (float)n.wlo[2]);
+    hi = v3((float)n.whi[0], (float)n.whi[1], (float)n.whi[2]);
+    return;
+  }
   lo = ld3(v.origin, 0);
   hi = lo
       + v3((float)(v.dims[0] - 1) * v.spacing[0],
@@ -1514,9 +1708,25 @@ void volBounds(const OrcVolume &v, V3 &lo, V3 &hi)
 // cell's bounds project onto; the majorant is the max TF alpha over entries
 // [int(lo * 255), int(hi * 255) + 1] of the TF range [0, 1] (the default
 // argument), read at entry centres.
+// The grid dims are the field's voxel dims, or for a NanoVDB field its index
+// bbox extent (NvdbRegularField::buildGrid, NvdbRegularField.cpp:141-149).
+void gridDims(const OrcVolume &v, int d[3])
+{
+  Nvdb n;
+  if (v.nvdb && nvdbOpen(v.nvdb, n)) {
+    for (int k = 0; k < 3; k++)
+      d[k] = n.ihi[k] - n.ilo[k] + 1;
+    return;
+  }
+  for (int k = 0; k < 3; k++)
+    d[k] = v.dims[k];
+}
+
 void dptMajorants(const OrcVolume &v, int round, std::vector<float> &maj)
 {
-  const int md[3] = {(v.dims[0] + 15) / 16, (v.dims[1] + 15) / 16, (v.dims[2] + 15) / 16};
+  int gd[3];
+  gridDims(v, gd);
+  const int md[3] = {(gd[0] + 15) / 16, (gd[1] + 15) / 16, (gd[2] + 15) / 16};
   const size_t cells = (size_t)md[0] * md[1] * md[2];
   std::vector<float> lo(cells, 1e30f), hi(cells, -1e30f);
   V3 blo, bhi;
@@ -1632,7 +1842,9 @@ float sampleDistance(Ctx &C, const OrcVolume &v, const std::vector<float> &maj,
   tr = 1.f;
   const V3 org = v3(std::fma(h.ld.x, h.t0, h.lo.x), std::fma(h.ld.y, h.t0, h.lo.y),
       std::fma(h.ld.z, h.t0, h.lo.z));
-  const int md[3] = {(v.dims[0] + 15) / 16, (v.dims[1] + 15) / 16, (v.dims[2] + 15) / 16};
+  int gd[3];
+  gridDims(v, gd);
+  const int md[3] = {(gd[0] + 15) / 16, (gd[1] + 15) / 16, (gd[2] + 15) / 16};
   V3 blo, bhi;
   volBounds(v, blo, bhi);
   dda3(org, h.ld, 0.f, h.t1 - h.t0, md, blo, bhi, [&](size_t cell, float t0, float t1) {
@@ -2314,6 +2526,16 @@ void orc_tex1d(const float *table, int n, int comps, float coord, int round, flo
 float orc_tex3d(const float *vox, const int dims[3], const float coord[3], int round)
 {
   return tex3dLinear(vox, dims, coord[0], coord[1], coord[2], round);
+}
+
+int orc_nvdb_sample(const uint8_t *grid, const float *xyz, int n, int fused, float *out)
+{
+  Nvdb g;
+  if (!nvdbOpen(grid, g))
+    return -1;
+  for (int i = 0; i < n; i++)
+    out[i] = nvdbSample(g, v3(xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]), fused);
+  return 0;
 }
 
 void orc_dpt_majorants(const OrcVolume *volume, int round, float *out)

@@ -51,6 +51,18 @@ void orc_tex1d(const float *table, int n, int comps, float coord, int round,
     float *out);
 float orc_tex3d(const float *vox, const int dims[3], const float coord[3], int round);
 
+/* --- NanoVDB fields ------------------------------------------------------ */
+
+/* Samples a NanoVDB grid buffer (NanoVDB 32.7 layout; leaf codecs float,
+ * Fp4, Fp8, Fp16, FpN) at n world-space points the way the reference's
+ * field sampler does (gpu/sampleSpatialField.h:80-109: the grid's float
+ * inverse map, then first-order interpolation of the 2x2x2 voxel stencil).
+ * fused = 0 rounds the leaf decode and the interpolation separately, as the
+ * NanoVDB library compiled for the host does; fused = 1 evaluates them as
+ * fused multiply-adds, as the reference's device build (and libvrtx) does.
+ * Returns 0, or -1 for a buffer this reader does not accept. */
+int orc_nvdb_sample(const uint8_t *grid, const float *xyz, int n, int fused, float *out);
+
 /* --- scene ---------------------------------------------------------------- */
 
 /* A geometry attribute array: element type code (this library's VRTX_*
@@ -137,6 +149,9 @@ typedef struct OrcVolume {
   uint32_t id;
   uint32_t instId;
   float xfm[12];
+  /* non-NULL: a NanoVDB field (the grid buffer); field, dims, origin,
+   * spacing and filterLinear are then unused */
+  const uint8_t *nvdb;
 } OrcVolume;
 
 /* The reference's delta-tracking majorants of one volume (dpt renderer):

@@ -121,7 +121,8 @@ class OrcVolume(C.Structure):
                 ("spacing", C.c_float * 3), ("filterLinear", C.c_int), ("tf", C.c_void_p),
                 ("valueRange", C.c_float * 2), ("unitDistance", C.c_float),
                 ("uniformColor", C.c_float * 3), ("uniformOpacity", C.c_float),
-                ("id", C.c_uint32), ("instId", C.c_uint32), ("xfm", C.c_float * 12)]
+                ("id", C.c_uint32), ("instId", C.c_uint32), ("xfm", C.c_float * 12),
+                ("nvdb", C.c_void_p)]
 
 
 class OrcScene(C.Structure):
@@ -324,10 +325,15 @@ def _scene_structs(spec):
 
 
 def _pack_volume(v, o, keep, world_id):
-    f = np.ascontiguousarray(v.field, np.float32)
-    keep.append(f)
-    o.field = _ptr(f)
-    o.dims = (C.c_int * 3)(f.shape[2], f.shape[1], f.shape[0])
+    if v.nvdb is not None:
+        g = np.ascontiguousarray(v.nvdb, np.uint8)
+        keep.append(g)
+        o.nvdb = _ptr(g)
+    else:
+        f = np.ascontiguousarray(v.field, np.float32)
+        keep.append(f)
+        o.field = _ptr(f)
+        o.dims = (C.c_int * 3)(f.shape[2], f.shape[1], f.shape[0])
     o.origin = (C.c_float * 3)(*map(float, v.origin))
     o.spacing = (C.c_float * 3)(*map(float, v.spacing))
     o.filterLinear = int(v.filter != "nearest")
@@ -344,6 +350,19 @@ def _pack_volume(v, o, keep, world_id):
     o.xfm = _rows(np.eye(4))
 
 
+def nvdb_sample(grid, xyz, fused: bool = True) -> np.ndarray:
+    """Samples a NanoVDB grid buffer at world-space points (n, 3) the way the
+    reference's field sampler does; fused=False rounds like NanoVDB compiled
+    for the host, fused=True like the device build."""
+    lib = load()
+    g = np.ascontiguousarray(grid, np.uint8)
+    p = np.ascontiguousarray(xyz, np.float32).reshape(-1, 3)
+    out = np.zeros(len(p), np.float32)
+    if lib.orc_nvdb_sample(_ptr(g), _ptr(p), C.c_int(len(p)), C.c_int(int(fused)), _ptr(out)) != 0:
+        raise ValueError("not a NanoVDB grid this reader accepts")
+    return out
+
+
 def dpt_majorants(vspec, tex_round: int = 1) -> np.ndarray:
     """The reference's delta-tracking majorant grid of one volume (the dpt
     renderer's Woodcock bound), shape (ceil(nz/16), ceil(ny/16), ceil(nx/16))."""
@@ -351,7 +370,13 @@ def dpt_majorants(vspec, tex_round: int = 1) -> np.ndarray:
     keep = []
     o = OrcVolume()
     _pack_volume(vspec, o, keep, 0)
-    nz, ny, nx = np.asarray(vspec.field).shape
+    if vspec.nvdb is not None:
+        from visrtx_gb300.nanovdb import grid_info
+
+        lo, hi = grid_info(vspec.nvdb)["index_bbox"]
+        nx, ny, nz = (h - l + 1 for l, h in zip(lo, hi))
+    else:
+        nz, ny, nx = np.asarray(vspec.field).shape
     md = ((nz + 15) // 16, (ny + 15) // 16, (nx + 15) // 16)
     out = np.zeros(md, np.float32)
     lib.orc_dpt_majorants(C.byref(o), C.c_int(tex_round), _ptr(out))

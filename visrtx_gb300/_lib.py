@@ -22,7 +22,7 @@ OBJECT = 100
 ARRAY1D, ARRAY2D, ARRAY3D = 101, 102, 103
 CAMERA, FRAME, GEOMETRY, GROUP, INSTANCE, LIGHT, MATERIAL, RENDERER = range(104, 112)
 SURFACE, SAMPLER, SPATIAL_FIELD, VOLUME, WORLD = range(112, 117)
-INT32, INT32_VEC2 = 200, 201
+INT32, INT32_VEC2, INT8, UINT8 = 200, 201, 202, 203
 UINT32, UINT32_VEC2, UINT32_VEC3, UINT32_VEC4 = 210, 211, 212, 213
 UINT64 = 214
 FIXED8, UFIXED8, FIXED16, UFIXED16 = 220, 221, 222, 223

@@ -20,7 +20,8 @@ LIBDIR = os.path.join(HERE, "lib")
 LIB = os.path.join(LIBDIR, "libvrtx.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_SOURCES = ["bvh.cu", "scene.cu", "render.cu", "dm.cu"]
+CU_SOURCES = ["bvh.cu", "scene.cu", "render.cu", "render_counting.cu", "render_volume.cu", "render_ao.cu",
+              "dm.cu"]
 CPP_SOURCES = ["device.cpp"]
 
 

@@ -57,6 +57,8 @@ size_t sizeOfType(int t)
     return 16;
   case VRTX_FIXED8:
   case VRTX_UFIXED8:
+  case VRTX_INT8:
+  case VRTX_UINT8:
     return 1;
   case VRTX_FIXED16:
   case VRTX_UFIXED16:
@@ -1232,15 +1234,34 @@ void SpatialField::cleanup()
     cudaFree(ranges);
   if (refRanges)
     cudaFree(refRanges);
+  if (gridDev)
+    cudaFree(gridDev);
   tex = pointTex = 0;
   cuArray = nullptr;
   ranges = nullptr;
   refRanges = nullptr;
+  gridDev = nullptr;
+  nvdbGPU = NvdbGPU{};
   builtStamp = 0;
 }
 
 void SpatialField::commit()
 {
+  nanovdb = subtype == "nanovdb";
+  if (nanovdb) {
+    // NvdbRegularField::commitParameters (NvdbRegularField.cpp:63-67)
+    filter = getString("filter", "linear");
+    data = static_cast<Array *>(getObject("data", VRTX_ARRAY1D));
+    if (!data)
+      report(VRTX_SEVERITY_WARNING,
+          "missing required parameter 'data' on NanoVDB regular spatial field");
+    else if (data->elemType != VRTX_UINT8)
+      report(VRTX_SEVERITY_WARNING,
+          "invalid data array type encountered in NanoVDB spatial field (%d)",
+          data->elemType);
+    builtStamp = 0;
+    return;
+  }
   if (subtype != "structuredRegular")
     report(VRTX_SEVERITY_WARNING,
         "spatial field subtype '%s' is not supported",
@@ -1263,6 +1284,8 @@ static bool validFieldType(int t)
 
 bool SpatialField::isValid() const
 {
+  if (nanovdb)
+    return data && data->elemType == VRTX_UINT8;
   return data && validFieldType(data->elemType);
 }
 
@@ -1273,6 +1296,8 @@ uint64_t SpatialField::deepStamp() const
 
 box3 SpatialField::bounds() const
 {
+  if (nanovdb)
+    return gridBounds; // the grid's world bbox (NvdbRegularField.cpp:105-108)
   if (!isValid())
     return box3{{0.f, 0.f, 0.f}, {1.f, 1.f, 1.f}};
   return box3{origin,
@@ -1284,7 +1309,178 @@ box3 SpatialField::bounds() const
 
 float SpatialField::stepSize() const
 {
+  if (nanovdb) // NvdbRegularField::stepSize: compMin(voxelSize) / 2
+    return std::min(gridVoxel.x, std::min(gridVoxel.y, gridVoxel.z)) / 2.f;
   return std::min(spacing.x / 2.f, std::min(spacing.y / 2.f, spacing.z / 2.f));
+}
+
+// Host-side check of a NanoVDB grid buffer before any kernel reads it: the
+// header (magic, major version 32, one grid, a leaf codec the marcher
+// dispatches: float, Fp4, Fp8, Fp16, FpN), and every root tile, internal
+// slot and leaf the tree links to lying inside the buffer on a 32-byte
+// boundary (NanoVDB's alignment), so the device walk never leaves it.
+static bool checkNanovdb(const uint8_t *b, size_t size, std::string &why)
+{
+  auto rd64 = [&](size_t o) {
+    uint64_t v;
+    std::memcpy(&v, b + o, 8);
+    return v;
+  };
+  auto rd32 = [&](size_t o) {
+    uint32_t v;
+    std::memcpy(&v, b + o, 4);
+    return v;
+  };
+  if (size < 672 + 64 + 64) {
+    why = "buffer smaller than a grid header";
+    return false;
+  }
+  const uint64_t magic = rd64(0);
+  if (magic != 0x304244566F6E614EULL && magic != 0x314244566F6E614EULL) {
+    why = "not a NanoVDB grid (magic number)";
+    return false;
+  }
+  if ((rd32(16) >> 21) != 32u) {
+    why = "unsupported NanoVDB major version";
+    return false;
+  }
+  if (rd32(28) != 1u) {
+    why = "VisRTX NanoVDB support's a single grid per file";
+    return false;
+  }
+  const uint32_t type = rd32(636);
+  if (type != 1u && (type < 13u || type > 16u)) {
+    why = "unsupported NanoVDB grid type (float, Fp4, Fp8, Fp16 and FpN are)";
+    return false;
+  }
+  const uint64_t gridSize = rd64(32);
+  if (gridSize > size) {
+    why = "grid size exceeds the buffer";
+    return false;
+  }
+  const int64_t rootOff = (int64_t)rd64(672 + 24);
+  auto inside = [&](int64_t off, size_t len) {
+    return off >= 0 && (off & 31) == 0 && (uint64_t)off + len <= gridSize;
+  };
+  const int64_t root = 672 + rootOff;
+  if (!inside(root, 64)) {
+    why = "root node outside the buffer";
+    return false;
+  }
+  const uint32_t tiles = rd32(root + 24);
+  if (!inside(root, 64 + 32ull * tiles)) {
+    why = "root tiles outside the buffer";
+    return false;
+  }
+  const size_t fixedLeaf = type == 1u ? 96 + 2048
+      : type == 13u                   ? 96 + 256
+      : type == 14u                   ? 96 + 512
+      : type == 15u                   ? 96 + 1024
+                                      : 0;
+  for (uint32_t t = 0; t < tiles; t++) {
+    const int64_t child = (int64_t)rd64(root + 64 + 32 * t + 8);
+    if (!child)
+      continue;
+    const int64_t up = root + child;
+    if (!inside(up, 270400)) {
+      why = "upper node outside the buffer";
+      return false;
+    }
+    for (uint32_t nu = 0; nu < 32768; nu++) {
+      if (!((rd64(up + 4128 + 8 * (nu >> 6)) >> (nu & 63)) & 1))
+        continue;
+      const int64_t lo = up + (int64_t)rd64(up + 8256 + 8 * nu);
+      if (!inside(lo, 33856)) {
+        why = "lower node outside the buffer";
+        return false;
+      }
+      for (uint32_t nl = 0; nl < 4096; nl++) {
+        if (!((rd64(lo + 544 + 8 * (nl >> 6)) >> (nl & 63)) & 1))
+          continue;
+        const int64_t leaf = lo + (int64_t)rd64(lo + 1088 + 8 * nl);
+        if (!inside(leaf, 96)) {
+          why = "leaf outside the buffer";
+          return false;
+        }
+        const size_t len = fixedLeaf ? fixedLeaf : 96 + (64u << (b[leaf + 15] >> 5));
+        if ((b[leaf + 15] >> 5) > 4 || !inside(leaf, len)) {
+          why = "leaf outside the buffer";
+          return false;
+        }
+      }
+    }
+  }
+  return true;
+}
+
+// NvdbRegularField::finalize / buildGrid (NvdbRegularField.cpp:69-149): the
+// grid copied to device memory, the bounds and voxel size from its header,
+// and the delta-tracking grid over its index bbox.
+bool SpatialField::buildNanovdb()
+{
+  cudaStream_t s = Object::dev->stream;
+  const size_t size = data->bytes();
+  std::vector<uint8_t> host(size);
+  if (const void *h = data->hostData())
+    std::memcpy(host.data(), h, size);
+  else if (const void *d = data->deviceData())
+    cudaMemcpy(host.data(), d, size, cudaMemcpyDeviceToHost);
+  else
+    return false;
+  std::string why;
+  if (!checkNanovdb(host.data(), size, why)) {
+    report(VRTX_SEVERITY_WARNING, "NanoVDB spatial field: %s", why.c_str());
+    return false;
+  }
+  if (cudaMalloc(&gridDev, size) != cudaSuccess) {
+    cudaGetLastError();
+    gridDev = nullptr;
+    report(VRTX_SEVERITY_ERROR, "device allocation of %zu bytes failed", size);
+    return false;
+  }
+  cudaMemcpyAsync(gridDev, host.data(), size, cudaMemcpyHostToDevice, s);
+  auto rdf = [&](size_t o) {
+    float v;
+    std::memcpy(&v, host.data() + o, 4);
+    return v;
+  };
+  auto rdd = [&](size_t o) {
+    double v;
+    std::memcpy(&v, host.data() + o, 8);
+    return v;
+  };
+  auto rdi = [&](size_t o) {
+    int32_t v;
+    std::memcpy(&v, host.data() + o, 4);
+    return v;
+  };
+  int64_t rootOff;
+  std::memcpy(&rootOff, host.data() + 672 + 24, 8);
+  const size_t root = 672 + (size_t)rootOff;
+  nvdbGPU.root = gridDev + root;
+  std::memcpy(&nvdbGPU.type, host.data() + 636, 4);
+  std::memcpy(&nvdbGPU.tiles, host.data() + root + 24, 4);
+  nvdbGPU.background = rdf(root + 28);
+  for (int k = 0; k < 9; k++)
+    nvdbGPU.inv[k] = rdf(296 + 36 + 4 * k);
+  for (int k = 0; k < 3; k++)
+    nvdbGPU.vec[k] = rdf(296 + 72 + 4 * k);
+  gridBounds = box3{{float(rdd(560)), float(rdd(568)), float(rdd(576))},
+      {float(rdd(584)), float(rdd(592)), float(rdd(600))}};
+  gridVoxel = f3{float(rdd(608)), float(rdd(616)), float(rdd(624))};
+  for (int k = 0; k < 3; k++)
+    dims[k] = rdi(root + 12 + 4 * k) - rdi(root + 4 * k) + 1; // indexBBox().dim()
+  mcDims[0] = (dims[0] + 15) / 16;
+  mcDims[1] = (dims[1] + 15) / 16;
+  mcDims[2] = (dims[2] + 15) / 16;
+  const size_t cells = (size_t)mcDims[0] * mcDims[1] * mcDims[2];
+  if (cudaMalloc(&refRanges, 2 * cells * sizeof(float)) != cudaSuccess) {
+    cudaGetLastError();
+    refRanges = nullptr;
+    return false;
+  }
+  launchReferenceGridRangesNanovdb(nvdbGPU, gridBounds, mcDims, refRanges, s);
+  return cudaGetLastError() == cudaSuccess;
 }
 
 bool SpatialField::ensureBuilt()
@@ -1292,9 +1488,15 @@ bool SpatialField::ensureBuilt()
   if (!isValid())
     return false;
   const uint64_t want = deepStamp();
-  if (builtStamp >= want && tex)
+  if (builtStamp && builtStamp >= want)
     return true;
   cleanup();
+  if (nanovdb) {
+    if (!buildNanovdb())
+      return false;
+    builtStamp = want;
+    return true;
+  }
   cudaStream_t s = Object::dev->stream;
   const int et = data->elemType;
   dims[0] = (int)data->n[0];
@@ -1539,7 +1741,7 @@ bool Volume::ensureBuilt()
   if (!isValid() || !field->ensureBuilt())
     return false;
   const uint64_t want = deepStamp();
-  if (builtStamp >= want && majorants)
+  if (builtStamp && builtStamp >= want)
     return true;
   cleanup();
   cudaStream_t s = Object::dev->stream;
@@ -1577,6 +1779,19 @@ bool Volume::ensureBuilt()
   }
   const size_t cells =
       (size_t)field->mcDims[0] * field->mcDims[1] * field->mcDims[2];
+  hasEmptyCells = false;
+  if (!field->ranges) {
+    // no skipping grid (NanoVDB fields): only the delta-tracking majorants
+    if (cudaMalloc(&dptMajorants, cells * sizeof(float)) != cudaSuccess) {
+      cudaGetLastError();
+      dptMajorants = nullptr;
+      return false;
+    }
+    launchReferenceMajorants(
+        field->refRanges, field->mcDims, tfTex, 256, uniformOpacity, dptMajorants, s);
+    builtStamp = want;
+    return cudaGetLastError() == cudaSuccess;
+  }
   if (cudaMalloc(&majorants, cells * sizeof(float)) != cudaSuccess) {
     cudaGetLastError();
     majorants = nullptr;
@@ -1946,6 +2161,8 @@ bool World::rebuild()
         SpatialField *f = v->field;
         VolumeGPU vg{};
         vg.field = f->tex;
+        vg.fieldKind = f->nanovdb ? FIELD_NANOVDB : FIELD_STRUCTURED_REGULAR;
+        vg.nvdb = f->nvdbGPU;
         vg.tf = v->tfTex;
         vg.hasTF = v->tfTex ? 1u : 0u;
         vg.origin = f->origin;
@@ -2017,6 +2234,10 @@ bool World::rebuild()
   gpu.volumes = uploadVec(this, vols, s);
   gpu.numVolumes = (uint32_t)vols.size();
   gpu.allOpaque = allOpaque ? 1u : 0u;
+  gpu.hasNanovdb = 0u;
+  for (const VolumeGPU &v : vols)
+    if (v.fieldKind == FIELD_NANOVDB)
+      gpu.hasNanovdb = 1u;
   gpu.hasSegments = 0u;
   for (const BLASDesc &b : hBlas)
     if (b.type >= GEOM_CYLINDER)
@@ -2344,8 +2565,10 @@ void Frame::render()
     tracePairs = 0;
     const int blocks =
         d->numSMs
-        * renderOccupancyBlocks(
-            P.renderer.type, countTraversal, P.world.numInstances > 0);
+        * renderOccupancyBlocks(P.renderer.type,
+            countTraversal,
+            P.world.numInstances > 0,
+            P.world.hasNanovdb != 0);
     err = launchRender(P, blocks, countTraversal, s);
     launches++;
   }

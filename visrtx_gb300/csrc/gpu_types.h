@@ -236,6 +236,27 @@ struct alignas(16) InstanceRecord
 // Volumes
 // ---------------------------------------------------------------------------
 
+enum FieldKind : uint32_t
+{
+  FIELD_STRUCTURED_REGULAR = 0,
+  FIELD_NANOVDB = 1
+};
+
+// A NanoVDB grid in device memory (spatial_field/NvdbRegularField.cpp): the
+// RootData of the grid buffer, its leaf codec (NanoVDB GridType: 1 float,
+// 13 Fp4, 14 Fp8, 15 Fp16, 16 FpN), root tile count, background value and
+// the float world -> index map (3x3 inverse matrix, row-major as stored,
+// and translation).
+struct NvdbGPU
+{
+  const uint8_t *root;
+  uint32_t type;
+  uint32_t tiles;
+  float background;
+  float inv[9];
+  float vec[3];
+};
+
 struct VolumeGPU
 {
   cudaTextureObject_t field; // 3D texture, normalised coords, clamp
@@ -252,7 +273,7 @@ struct VolumeGPU
   uint32_t id; // Volume "id"
   uint32_t instId; // instance user id
   uint32_t hasTF;
-  uint32_t pad0;
+  uint32_t fieldKind; // FieldKind
   xfm34 worldToObject;
   // conservative macrocell majorants (max TF opacity reachable in a cell),
   // 16-voxel cells from the origin: empty-space skipping of the marcher
@@ -262,6 +283,7 @@ struct VolumeGPU
   const float *dptMajorants;
   int mcDims[3];
   int dims[3]; // voxel dims
+  NvdbGPU nvdb; // FIELD_NANOVDB
 };
 
 // ---------------------------------------------------------------------------
@@ -350,6 +372,8 @@ struct WorldGPU
   uint32_t allOpaque; // every material is opaque: any-hit = first hit
   uint32_t hasSegments; // some BLAS holds cylinders, cones or curves
   const SamplerGPU *samplers; // the materials' samplers
+  uint32_t hasNanovdb; // some volume samples a NanoVDB field
+  uint32_t pad0;
 };
 
 // Per-thread work counters. Rays and volume samples are counted by every

@@ -221,6 +221,11 @@ struct Surface : Object
 struct SpatialField : Object
 {
   using Object::Object;
+  bool nanovdb = false; // subtype "nanovdb" (NvdbRegularField.cpp)
+  uint8_t *gridDev = nullptr; // device copy of the NanoVDB grid buffer
+  NvdbGPU nvdbGPU{};
+  box3 gridBounds{{0.f, 0.f, 0.f}, {1.f, 1.f, 1.f}};
+  f3 gridVoxel{1.f, 1.f, 1.f};
   Array *data = nullptr;
   f3 origin{0.f, 0.f, 0.f}, spacing{1.f, 1.f, 1.f};
   std::string filter = "linear";
@@ -237,6 +242,7 @@ struct SpatialField : Object
   uint64_t deepStamp() const override;
   void cleanup();
   bool ensureBuilt();
+  bool buildNanovdb();
   box3 bounds() const;
   float stepSize() const;
 };

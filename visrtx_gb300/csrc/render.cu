@@ -1,1032 +1,11 @@
-// Integrator kernels: one persistent kernel per renderer subtype.
-//
-// Each thread renders one pixel for all pixelSamples iterations, exactly as
-// the reference's raygen programs do (one launch index per pixel, RNG state
-// curand_init(y*w + x, 0, frameID*512) carried across the sample loop,
-// createScreenSample.h:48-65), so the Philox stream each pixel consumes is
-// the reference's. Warps pull 8x4 pixel tiles from a global counter (a
-// per-warp work queue), which balances cheap background tiles against
-// expensive ones without a second launch.
-//
-// Renderers follow:
-//   directLight/default  renderer/DirectLight_ptx.cu:73-224, 294-418
-//   raycast              renderer/Raycast_ptx.cu:60-179
-//   ao                   renderer/AmbientOcclusion_ptx.cu:86-220
-//   dpt                  renderer/DiffusePathTracer_ptx.cu:82-215
-// with the output path of gpu/gpu_util.h:321-443.
-#include "render.h"
-#include "traverse.cuh"
-#include "volume.cuh"
-
-// Minimum resident 128-thread blocks per SM requested from ptxas for the
-// integrator kernels (caps registers per thread at 65536 / (128 * value)).
-#ifndef VRTX_RENDER_MIN_BLOCKS
-#define VRTX_RENDER_MIN_BLOCKS 1
-#endif
-// The same for the any-hit queue kernel (8: <= 64 registers per thread).
-#ifndef VRTX_AO_REFILL
-#define VRTX_AO_REFILL 4
-#endif
-
-// traversal stack entries of the AO any-hit kernel kept in shared memory
-#ifndef VRTX_AO_SHARED_STACK
-#define VRTX_AO_SHARED_STACK 16
-#endif
-
-// blocks per SM the per-pixel kernel is compiled for on worlds without
-// surfaces (volume-only frames)
-#ifndef VRTX_VOLUME_MIN_BLOCKS
-#define VRTX_VOLUME_MIN_BLOCKS 8
-#endif
-
-#ifndef VRTX_TRACE_MIN_BLOCKS
-#define VRTX_TRACE_MIN_BLOCKS 8
-#endif
+// Per-pixel integrator launches for worlds with surfaces (and volumes), the
+// frame clear, and the dispatch of every render launch; the kernels and
+// device code are in render_impl.cuh.
+#include "render_impl.cuh"
 
 namespace vrtx {
 
 namespace {
-
-constexpr float kFltMax = 3.402823466e+38f;
-
-// --- ray generation ----------------------------------------------------------
-
-__device__ __forceinline__ int computePixelX(int idx, int cb)
-{
-  return cb < 0 ? idx : idx * 2 + (cb & 0x1);
-}
-__device__ __forceinline__ int computePixelY(int idy, int cb)
-{
-  return cb < 0 ? idy : idy * 2 + ((cb >> 1) & 0x1);
-}
-
-__device__ __forceinline__ float mixf(float a, float b, float t)
-{
-  return a * (1.f - t) + b * t;
-}
-
-struct Ray
-{
-  f3 org, dir;
-  float tmin, tmax;
-};
-
-// makePrimaryRay + cameraCreateRay (gpu/cameraCreateRay.h:38-81)
-__device__ __forceinline__ Ray makePrimaryRay(const FrameParams &P,
-    RandState &rs,
-    int px,
-    int py,
-    bool centerPixel,
-    float &screenX,
-    float &screenY)
-{
-  const float4 r = curand_uniform4(&rs);
-  const float sx0 = centerPixel ? (float)px : (float)px + r.x;
-  const float sy0 = centerPixel ? (float)py : (float)py + r.y;
-  screenX = sx0 * P.fb.invW;
-  screenY = sy0 * P.fb.invH;
-  const CameraGPU &c = P.camera;
-  const float sx = mixf(c.region[0], c.region[2], screenX);
-  const float sy = mixf(c.region[1], c.region[3], screenY);
-  Ray ray;
-  ray.tmin = 0.f;
-  ray.tmax = kFltMax;
-  if (c.type == CAMERA_PERSPECTIVE) {
-    ray.org = c.pos;
-    ray.dir = c.dir00 + sx * c.dirDu + sy * c.dirDv;
-    if (c.scaledAperture > 0.f) {
-      // uniformSampleDisk (gpu_math.h)
-      const float rr = sqrtf(r.z) * c.scaledAperture;
-      const float phi = 2.f * float(M_PI) * r.w;
-      const float lx = rr * cosf(phi), ly = rr * sinf(phi);
-      const f3 lp = (lx * c.dirDu) + ((ly * c.aspect) * c.dirDv);
-      ray.org += lp;
-      ray.dir = ray.dir - lp;
-    }
-    ray.dir = normalize(ray.dir);
-  } else {
-    ray.dir = c.dir;
-    ray.org = c.pos00 + sx * c.posDu + sy * c.posDv;
-  }
-  return ray;
-}
-
-// --- hit population ----------------------------------------------------------
-
-struct SurfaceHit
-{
-  float t;
-  f3 hitpoint;
-  f3 Ng, Ns;
-  float epsilon;
-  uint32_t primID; // geometry-local primitive index (OptiX primID)
-  uint32_t surface;
-  uint32_t instUserId;
-  float u, v; // triangle barycentrics (v1, v2 weights); segments: u
-};
-
-// epsilonFrom (gpu_util.h:245-250)
-__device__ __forceinline__ float epsilonFrom(f3 P, f3 dir, float t)
-{
-  const f3 aP = fabs3(P);
-  const float m = fmaxf(fmaxf(fmaxf(aP.x, aP.y), aP.z), compMax(fabs3(dir)) * t);
-  return m * 0x1.fp-21f;
-}
-
-// populateSurfaceHit + computeTangentSpace (gpu/populateHit.h:200-368)
-__device__ __forceinline__ void populateSurfaceHit(
-    const WorldGPU &w, const Ray &ray, const Hit &h, SurfaceHit &sh)
-{
-  const InstanceRecord &inst = w.instances[h.inst];
-  const BLASDesc &blas = w.blas[inst.blas];
-  sh.t = h.t;
-  sh.u = h.u;
-  sh.v = h.v;
-  sh.hitpoint = ray.org + h.t * ray.dir;
-  sh.epsilon = epsilonFrom(sh.hitpoint, ray.dir, h.t);
-  sh.instUserId = inst.userId;
-  f3 Ng, Ns;
-  if (blas.type == GEOM_TRIANGLE) {
-    const TriRecord tr = reinterpret_cast<const TriRecord *>(blas.prims)[h.rec];
-    sh.primID = __float_as_uint(tr.v0.w);
-    sh.surface = __float_as_uint(tr.v1.w);
-    const f3 v0 = mk3(tr.v0.x, tr.v0.y, tr.v0.z);
-    const f3 v1 = mk3(tr.v1.x, tr.v1.y, tr.v1.z);
-    const f3 v2 = mk3(tr.v2.x, tr.v2.y, tr.v2.z);
-    const GeometryGPU &g = w.geometries[w.surfaces[sh.surface].geometry];
-    if (g.kind == KIND_QUAD) {
-      // QUAD case (populateHit.h:267-279): unnormalised face normal, no
-      // vertex normals
-      Ng = cross(v1 - v0, v2 - v0);
-      if (!h.front)
-        Ng = -Ng;
-      Ns = Ng;
-    } else {
-      Ng = normalize(cross(v1 - v0, v2 - v0));
-      if (!h.front)
-        Ng = -Ng;
-      const float b0 = 1.f - h.u - h.v, b1 = h.u, b2 = h.v;
-      if (g.normalsFV) {
-        const uint32_t i0 = sh.primID * 3;
-        Ns = b0 * g.normalsFV[i0] + b1 * g.normalsFV[i0 + 1]
-            + b2 * g.normalsFV[i0 + 2];
-      } else if (g.normals) {
-        uint32_t i0, i1, i2;
-        if (g.indices) {
-          i0 = g.indices[3 * sh.primID];
-          i1 = g.indices[3 * sh.primID + 1];
-          i2 = g.indices[3 * sh.primID + 2];
-        } else {
-          i0 = 3 * sh.primID;
-          i1 = i0 + 1;
-          i2 = i0 + 2;
-        }
-        Ns = b0 * g.normals[i0] + b1 * g.normals[i1] + b2 * g.normals[i2];
-      } else
-        Ns = Ng;
-      Ns = normalize(Ns);
-      if (dot(Ng, Ns) < 0.f)
-        Ns = -Ns;
-    }
-  } else if (blas.type == GEOM_SPHERE) {
-    const SphereRecord sr =
-        reinterpret_cast<const SphereRecord *>(blas.prims)[h.rec];
-    sh.primID = sr.primID;
-    sh.surface = sr.surface;
-    const f3 lo = xfmPoint(inst.worldToObject, ray.org);
-    const f3 ld = xfmVector(inst.worldToObject, ray.dir);
-    const f3 hp = lo + h.t * ld;
-    Ng = Ns = hp - mk3(sr.cr.x, sr.cr.y, sr.cr.z);
-  } else {
-    const SegRecord sr = reinterpret_cast<const SegRecord *>(blas.prims)[h.rec];
-    sh.primID = sr.primID;
-    sh.surface = sr.surface;
-    if (blas.type == GEOM_CURVE) {
-      // CURVE case (populateHit.h:292-303) with curveSurfaceNormal
-      // (gpu/curveHelpers.h:91-107) at the object-space hit point
-      const f3 p0 = mk3(sr.a.x, sr.a.y, sr.a.z);
-      const f3 d = mk3(sr.b.x, sr.b.y, sr.b.z) - p0;
-      const float rad = sr.a.w + (sr.b.w - sr.a.w) * h.u;
-      const f3 ps = xfmPoint(inst.worldToObject, sh.hitpoint);
-      f3 o1 = ps - (p0 + h.u * d);
-      o1 = o1 - (dot(o1, d) / dot(d, d)) * d;
-      o1 = o1 * (rad / sqrtf(dot(o1, o1)));
-      Ng = Ns = normalize(o1);
-    } else {
-      // SPHERE / CONE / CYLINDER case: the intersector's normal attribute
-      Ng = Ns = h.n;
-    }
-  }
-  sh.Ng = normalize(xfmNormalTransposed(inst.worldToObject, Ng));
-  sh.Ns = normalize(xfmNormalTransposed(inst.worldToObject, Ns));
-}
-
-// computeGeometryPrimId (gpu_util.h:309-315)
-__device__ __forceinline__ uint32_t geometryPrimId(
-    const WorldGPU &w, const SurfaceHit &sh)
-{
-  const GeometryGPU &g = w.geometries[w.surfaces[sh.surface].geometry];
-  return g.primIds ? g.primIds[sh.primID] : sh.primID;
-}
-
-struct MatteState
-{
-  f3 baseColor;
-  float opacity;
-};
-
-// --- geometry attributes and material parameters ---------------------------
-
-// attribute arithmetic, rounded per operation (no contraction) so that
-// interpolated values feeding sampler coordinates are build-independent
-__device__ __forceinline__ float4 f4add(float4 a, float4 b)
-{
-  return make_float4(
-      __fadd_rn(a.x, b.x), __fadd_rn(a.y, b.y), __fadd_rn(a.z, b.z), __fadd_rn(a.w, b.w));
-}
-__device__ __forceinline__ float4 f4sub(float4 a, float4 b)
-{
-  return make_float4(
-      __fsub_rn(a.x, b.x), __fsub_rn(a.y, b.y), __fsub_rn(a.z, b.z), __fsub_rn(a.w, b.w));
-}
-__device__ __forceinline__ float4 f4mul(float4 a, float s)
-{
-  return make_float4(__fmul_rn(a.x, s), __fmul_rn(a.y, s), __fmul_rn(a.z, s), __fmul_rn(a.w, s));
-}
-
-// glm::convertLinearToSRGB (gamma 0.41666) on one channel
-__device__ __forceinline__ float srgbEncode(float c)
-{
-  const float x = fminf(fmaxf(c, 0.f), 1.f);
-  return x < 0.0031308f ? x * 12.92f : powf(x, 0.41666f) * 1.055f - 0.055f;
-}
-
-// getAttributeValue (gpu/evalMaterialParameters.h:60-99): element `offset`
-// of an attribute array as a vec4 (missing channels 0, alpha 1; fixed-point
-// normalised; sRGB8 values passed through the linear-to-sRGB conversion as
-// the reference does)
-__device__ __forceinline__ float4 attrValue(const AttrGPU &a, uint32_t offset, float4 uf)
-{
-  if (!a.data || offset == 0xFFFFFFFFu)
-    return uf;
-  switch (a.type) {
-  case 240: { // FLOAT32
-    const float *p = (const float *)a.data;
-    return make_float4(p[offset], 0.f, 0.f, 1.f);
-  }
-  case 241: { // FLOAT32_VEC2
-    const float *p = (const float *)a.data + 2 * (size_t)offset;
-    return make_float4(p[0], p[1], 0.f, 1.f);
-  }
-  case 242: { // FLOAT32_VEC3
-    const float *p = (const float *)a.data + 3 * (size_t)offset;
-    return make_float4(p[0], p[1], p[2], 1.f);
-  }
-  case 243: // FLOAT32_VEC4
-    return ((const float4 *)a.data)[offset];
-  case 221: { // UFIXED8
-    const uint8_t *p = (const uint8_t *)a.data;
-    return make_float4(p[offset] / 255.f, 0.f, 0.f, 1.f);
-  }
-  case 223: { // UFIXED16
-    const uint16_t *p = (const uint16_t *)a.data;
-    return make_float4(p[offset] / 65535.f, 0.f, 0.f, 1.f);
-  }
-  case 260: // UFIXED8_VEC4
-  case 261: { // UFIXED8_RGBA_SRGB
-    const uint8_t *p = (const uint8_t *)a.data + 4 * (size_t)offset;
-    float4 r = make_float4(p[0] / 255.f, p[1] / 255.f, p[2] / 255.f, p[3] / 255.f);
-    if (a.type == 261)
-      r = make_float4(srgbEncode(r.x), srgbEncode(r.y), srgbEncode(r.z), r.w);
-    return r;
-  }
-  default:
-    return uf;
-  }
-}
-
-// readAttributeValue (gpu/evalMaterialParameters.h:131-263) for attribute
-// slot `id` (0..3 attribute0..3, 4 color): per-vertex values interpolated
-// per subtype, then per-primitive values, then the geometry's uniform value.
-// (Instance attributes and face-varying attributes are not read.)
-__device__ __forceinline__ float4 readAttribute(
-    const WorldGPU &w, const SurfaceHit &sh, int id)
-{
-  const GeometryGPU &g = w.geometries[w.surfaces[sh.surface].geometry];
-  const float4 uf = g.uattr[id];
-  const AttrGPU &ap = g.vattr[id];
-  const uint32_t prim = sh.primID;
-  if (ap.data) {
-    const float b0 = 1.f - sh.u - sh.v, b1 = sh.u, b2 = sh.v;
-    switch (g.kind) {
-    case KIND_TRIANGLE: {
-      uint32_t i0, i1, i2;
-      if (g.indices) {
-        i0 = g.indices[3 * prim];
-        i1 = g.indices[3 * prim + 1];
-        i2 = g.indices[3 * prim + 2];
-      } else {
-        i0 = 3 * prim;
-        i1 = i0 + 1;
-        i2 = i0 + 2;
-      }
-      return f4add(f4add(f4mul(attrValue(ap, i0, uf), b0), f4mul(attrValue(ap, i1, uf), b1)),
-          f4mul(attrValue(ap, i2, uf), b2));
-    }
-    case KIND_QUAD: {
-      // corners (x, y, w, z) of the quad from its two triangles
-      const uint32_t pair = prim & ~1u;
-      const uint32_t x = g.indices[3 * pair], y = g.indices[3 * pair + 1],
-                     wI = g.indices[3 * pair + 2], z = g.indices[3 * (pair + 1)];
-      const float4 v0 = attrValue(ap, x, uf), v1 = attrValue(ap, y, uf);
-      const float4 v2 = attrValue(ap, z, uf), v3 = attrValue(ap, wI, uf);
-      const float qu = (prim & 1u) ? b1 : 1.f - b1;
-      const float qv = (prim & 1u) ? b2 : 1.f - b2;
-      const float4 l0 = f4add(v1, f4mul(f4sub(v0, v1), qu));
-      const float4 l1 = f4add(v2, f4mul(f4sub(v3, v2), qu));
-      return f4add(l1, f4mul(f4sub(l0, l1), qv));
-    }
-    case KIND_CYLINDER:
-    case KIND_CONE: {
-      const uint32_t i0 = g.indices ? g.indices[2 * prim] : 2 * prim;
-      const uint32_t i1 = g.indices ? g.indices[2 * prim + 1] : 2 * prim + 1;
-      // uvw = (0, u, 1 - u)
-      return f4add(f4mul(attrValue(ap, i0, uf), 1.f - sh.u), f4mul(attrValue(ap, i1, uf), sh.u));
-    }
-    case KIND_CURVE: {
-      const uint32_t i0 = g.indices ? g.indices[prim] : prim;
-      return f4add(f4mul(attrValue(ap, i0, uf), 1.f - sh.u), f4mul(attrValue(ap, i0 + 1, uf), sh.u));
-    }
-    default: { // sphere
-      const uint32_t i = g.indices ? g.indices[prim] : prim;
-      return attrValue(ap, i, uf);
-    }
-    }
-  }
-  const AttrGPU &pp = g.pattr[id];
-  if (pp.data)
-    return attrValue(pp, g.kind == KIND_QUAD ? prim / 2 : prim, uf);
-  return uf;
-}
-
-// column-major 4x4 times a vec4, plus an offset (glm's mat4 * vec4 sums
-// the column products pairwise: (c0 + c1) + (c2 + c3)); rounded per
-// operation, without contraction, so image lookups see the same coordinates
-// on every build
-__device__ __forceinline__ float4 affine4(const float *m, float4 v, float4 o)
-{
-  float r[4];
-#pragma unroll
-  for (int i = 0; i < 4; i++)
-    r[i] = __fadd_rn(__fadd_rn(__fmul_rn(m[i], v.x), __fmul_rn(m[4 + i], v.y)),
-        __fadd_rn(__fmul_rn(m[8 + i], v.z), __fmul_rn(m[12 + i], v.w)));
-  return make_float4(
-      __fadd_rn(r[0], o.x), __fadd_rn(r[1], o.y), __fadd_rn(r[2], o.z), __fadd_rn(r[3], o.w));
-}
-
-// evaluateSampler (gpu/evalMaterialParameters.h:291-334): the input
-// attribute through the input map, an image lookup / the primitive array /
-// the mapped value itself, then the output map
-__device__ __forceinline__ float4 evaluateSampler(
-    const WorldGPU &w, const SurfaceHit &sh, const SamplerGPU &sm)
-{
-  float4 r = make_float4(0.f, 0.f, 0.f, 1.f);
-  const float4 tc = affine4(sm.inT, readAttribute(w, sh, (int)sm.attribute), sm.inO);
-  switch (sm.type) {
-  case SAMPLER_IMAGE1D:
-    r = tex1D<float4>(sm.tex, tc.x);
-    break;
-  case SAMPLER_IMAGE2D:
-    r = tex2D<float4>(sm.tex, tc.x, tc.y);
-    break;
-  case SAMPLER_IMAGE3D:
-    r = tex3D<float4>(sm.tex, tc.x, tc.y, tc.z);
-    break;
-  case SAMPLER_PRIMITIVE:
-    r = attrValue(sm.prim, sh.primID + sm.primOffset, r);
-    break;
-  case SAMPLER_TRANSFORM:
-    r = tc;
-    break;
-  default:
-    break;
-  }
-  return affine4(sm.outT, r, sm.outO);
-}
-
-// getMaterialParameter (gpu/evalMaterialParameters.h:336-374)
-__device__ __forceinline__ float4 materialParam(const WorldGPU &w,
-    const SurfaceHit &sh,
-    uint32_t src,
-    float4 value,
-    uint32_t sampler)
-{
-  switch (src) {
-  case PARAM_VALUE:
-    return value;
-  case PARAM_SAMPLER:
-    return evaluateSampler(w, sh, w.samplers[sampler]);
-  case PARAM_ATTRIB_0:
-  case PARAM_ATTRIB_0 + 1:
-  case PARAM_ATTRIB_0 + 2:
-  case PARAM_ATTRIB_0 + 3:
-    return readAttribute(w, sh, (int)(src - PARAM_ATTRIB_0));
-  case PARAM_ATTRIB_COLOR:
-    return readAttribute(w, sh, 4);
-  case PARAM_WORLD_POSITION:
-  case PARAM_OBJECT_POSITION: // world space, as the reference
-    return make_float4(sh.hitpoint.x, sh.hitpoint.y, sh.hitpoint.z, 1.f);
-  case PARAM_WORLD_NORMAL:
-  case PARAM_OBJECT_NORMAL:
-    return make_float4(sh.Ns.x, sh.Ns.y, sh.Ns.z, 1.f);
-  default:
-    return make_float4(0.f, 0.f, 0.f, 0.f);
-  }
-}
-
-// Matte init (MatteShader_ptx.cu:38-49): colour and opacity parameters,
-// opacity = adjustedMaterialOpacity(color.w * opacity.x)
-__device__ __forceinline__ MatteState matteInit(const WorldGPU &w, const SurfaceHit &sh)
-{
-  const MaterialGPU &m = w.materials[w.surfaces[sh.surface].material];
-  MatteState s;
-  float op;
-  if (m.colorSrc == PARAM_VALUE && m.opacitySrc == PARAM_VALUE) {
-    s.baseColor = m.color;
-    op = m.opacity;
-  } else {
-    const float4 c = materialParam(w, sh, m.colorSrc, m.colorValue, m.colorSampler);
-    const float o = materialParam(w,
-        sh,
-        m.opacitySrc,
-        make_float4(m.opacityValue, 0.f, 0.f, 1.f),
-        m.opacitySampler)
-                        .x;
-    s.baseColor = mk3(c.x, c.y, c.z);
-    op = c.w * o;
-  }
-  s.opacity = m.alphaMode == ALPHA_OPAQUE
-      ? 1.f
-      : (m.alphaMode == ALPHA_BLEND ? op : (op < m.cutoff ? 0.f : 1.f));
-  return s;
-}
-
-__device__ __forceinline__ bool anyNan(f3 v)
-{
-  return isnan(v.x) || isnan(v.y) || isnan(v.z);
-}
-
-template <bool STATS>
-__device__ __forceinline__ float surfaceAttenuation(const FrameParams &P,
-    TravStats &st,
-    f3 org,
-    f3 dir,
-    float tmin,
-    float tmax)
-{
-  Hit h;
-  float o;
-  traverse<1, STATS>(
-      P.world, org, dir, tmin, tmax, false, false, h, o, P.errorFlag, st);
-  return o;
-}
-
-// randomDir(rs, normal) (gpu_util.h:190-208)
-__device__ __forceinline__ f3 randomDir(RandState &rs, f3 n)
-{
-  const float4 r = curand_uniform4(&rs);
-  const f3 d = normalize(mk3(2.f * r.x - 1.f, 2.f * r.y - 1.f, 2.f * r.z - 1.f));
-  return dot(d, n) > 0.f ? d : -d;
-}
-
-// computeAO (gpu/computeAO.h:38-60)
-template <bool STATS>
-__device__ __forceinline__ float computeAO(const FrameParams &P,
-    TravStats &st,
-    RandState &rs,
-    const SurfaceHit &hit,
-    float dist,
-    int numSamples)
-{
-  float weights = 0.f;
-  float hits = 0.f;
-  const f3 org = hit.hitpoint + (hit.epsilon * hit.Ng);
-  for (int i = 0; i < numSamples; i++) {
-    const f3 dir = randomDir(rs, hit.Ns);
-    const float weight = fmaxf(0.f, dot(dir, hit.Ns));
-    weights += weight;
-    if (weight != 0.f)
-      hits += weight * surfaceAttenuation<STATS>(P, st, org, dir, 0.f, dist);
-  }
-  return weights > 0.f ? 1.f - hits / weights : 0.f;
-}
-
-// shadeSurface (DirectLight_ptx.cu:73-224) for matte + directional/point
-template <bool STATS>
-__device__ __forceinline__ float4 shadeSurfaceDL(const FrameParams &P,
-    TravStats &st,
-    RandState &rs,
-    const Ray &ray,
-    const SurfaceHit &hit)
-{
-  const RendererGPU &rp = P.renderer;
-  const WorldGPU &w = P.world;
-  const f3 shadePoint = hit.hitpoint + (hit.epsilon * hit.Ns);
-  const float aoFactor = rp.aoSamples > 0
-      ? computeAO<STATS>(P, st, rs, hit, rp.occlusionDistance, rp.aoSamples)
-      : 1.f;
-  f3 contrib = mk3(0.f, 0.f, 0.f);
-  const MatteState ms = matteInit(w, hit);
-  const float opacity = ms.opacity;
-  if (rp.ambientIntensity > 0.f)
-    contrib = rp.ambientColor * rp.ambientIntensity * ms.baseColor;
-  for (uint32_t l = 0; l < w.numLights; l++) {
-    const LightGPU &L = w.lights[l];
-    f3 ldir;
-    float ldist;
-    f3 radiance;
-    if (L.type == LIGHT_DIRECTIONAL) {
-      ldir = L.dirToLight;
-      ldist = __int_as_float(0x7f800000); // +inf
-      radiance = L.radiance;
-    } else {
-      const f3 d = L.position - hit.hitpoint;
-      ldist = sqrtf(dot(d, d));
-      ldir = d / ldist;
-      radiance = L.radiance * (1.f / (ldist * ldist));
-    }
-    const float pdf = 1.f;
-    const float surface_o =
-        1.f - surfaceAttenuation<STATS>(P, st, shadePoint, ldir, 0.f, ldist);
-    const float volume_o = 1.f
-        - volumeAttenuation(
-            w, rs, shadePoint, ldir, 0.f, ldist, rp.invVolumeSamplingRate, st);
-    const float attenuation = surface_o * volume_o;
-    const float NdotL = fmaxf(0.f, dot(hit.Ns, ldir));
-    const f3 thisLight =
-        ms.baseColor * float(M_1_PI) * NdotL * radiance / pdf;
-    if (anyNan(thisLight))
-      continue;
-    contrib += thisLight * attenuation;
-  }
-  contrib *= aoFactor;
-  return make_float4(contrib.x, contrib.y, contrib.z, opacity);
-}
-
-struct SampleOut
-{
-  f3 color;
-  float opacity;
-  f3 albedo; // value accumulated into the albedo channel
-  f3 normal;
-  float depth;
-  uint32_t primID, objID, instID;
-};
-
-// SURF = false: the world has no surface instances, so the surface
-// traversal (and every shading branch behind a surface hit) compiles away;
-// volume-only frames then run with far fewer registers per thread.
-template <int RT, bool STATS, bool SURF>
-__device__ __forceinline__ void integrateSample(const FrameParams &P,
-    TravStats &st,
-    RandState &rs,
-    int px,
-    int py,
-    SampleOut &o)
-{
-  const RendererGPU &rp = P.renderer;
-  const WorldGPU &w = P.world;
-  float scrX, scrY;
-  Ray ray =
-      makePrimaryRay(P, rs, px, py, RT == RENDERER_RAYCAST, scrX, scrY);
-  const float tmax = ray.tmax;
-  f3 outputColor = mk3(0.f, 0.f, 0.f);
-  f3 outputNormal = ray.dir;
-  float outputOpacity = 0.f;
-  float depth = 1e30f;
-  uint32_t primID = ~0u, objID = ~0u, instID = ~0u;
-  bool firstHit = true;
-  const bool cull = rp.cullTriangleBF != 0;
-
-  while (outputOpacity < 0.99f) {
-    ray.tmax = tmax;
-    Hit h;
-    float unused;
-    // a primary / path ray against an empty surface set still counts
-    if (!SURF)
-      st.rays++;
-    const bool found = SURF && traverse<0, STATS>(w,
-        ray.org,
-        ray.dir,
-        ray.tmin,
-        ray.tmax,
-        cull,
-        true,
-        h,
-        unused,
-        P.errorFlag,
-        st);
-    f3 color = mk3(0.f, 0.f, 0.f);
-    float opacity = 0.f;
-    if (found) {
-      SurfaceHit sh;
-      populateSurfaceHit(w, ray, h, sh);
-      uint32_t vObjID = ~0u, vInstID = ~0u;
-      const float vDepth = rayMarchAllVolumes(w,
-          rs,
-          ray.org,
-          ray.dir,
-          ray.tmin,
-          sh.t,
-          rp.invVolumeSamplingRate,
-          color,
-          opacity,
-          vObjID,
-          vInstID,
-          st);
-      if (firstHit) {
-        const bool volumeFirst = vDepth < sh.t;
-        if (volumeFirst) {
-          outputNormal = -ray.dir;
-          depth = vDepth;
-          primID = 0;
-          objID = vObjID;
-          instID = vInstID;
-        } else {
-          outputNormal = RT == RENDERER_DIRECT_LIGHT ? sh.Ns : sh.Ng;
-          depth = sh.t;
-          primID = geometryPrimId(w, sh);
-          objID = w.surfaces[sh.surface].id;
-          instID = sh.instUserId;
-        }
-        firstHit = false;
-      }
-      if (RT == RENDERER_DIRECT_LIGHT) {
-        const float4 sr = shadeSurfaceDL<STATS>(P, st, rs, ray, sh);
-        const f3 srgb = mk3(sr.x, sr.y, sr.z);
-        if (anyNan(srgb)) {
-          color = mk3(0.f, 0.f, 0.f);
-          opacity = 0.f;
-        } else {
-          color = srgb;
-          opacity = sr.w;
-        }
-        color += srgb * (1.f - opacity);
-        opacity += sr.w * (1.f - opacity);
-      } else if (RT == RENDERER_RAYCAST) {
-        const MatteState ms = matteInit(w, sh);
-        const f3 lighting = fabsf(dot(ray.dir, sh.Ns)) * rp.ambientColor;
-        color += (ms.baseColor * lighting) * (1.f - opacity);
-        opacity += ms.opacity * (1.f - opacity);
-      } else { // AO
-        const float aoFactor = rp.aoSamples > 0
-            ? computeAO<STATS>(P, st, rs, sh, rp.occlusionDistance, rp.aoSamples)
-            : 1.f;
-        const MatteState ms = matteInit(w, sh);
-        const f3 lighting = aoFactor * rp.ambientIntensity * rp.ambientColor;
-        color += (ms.baseColor * lighting) * (1.f - opacity);
-        opacity += ms.opacity * (1.f - opacity);
-      }
-      color *= opacity;
-      outputColor += color * (1.f - outputOpacity);
-      outputOpacity += opacity * (1.f - outputOpacity);
-      ray.tmin = sh.t + sh.epsilon;
-    } else {
-      uint32_t vObjID = ~0u, vInstID = ~0u;
-      const float volumeDepth = rayMarchAllVolumes(w,
-          rs,
-          ray.org,
-          ray.dir,
-          ray.tmin,
-          ray.tmax,
-          rp.invVolumeSamplingRate,
-          color,
-          opacity,
-          vObjID,
-          vInstID,
-          st);
-      if (firstHit) {
-        depth = fminf(depth, volumeDepth);
-        primID = 0;
-        objID = vObjID;
-        instID = vInstID;
-      }
-      color *= opacity;
-      const float4 bg = rp.background;
-      color += mk3(bg.x, bg.y, bg.z) * (1.f - opacity);
-      opacity += bg.w * (1.f - opacity);
-      outputColor += color * (1.f - outputOpacity);
-      outputOpacity += opacity * (1.f - outputOpacity);
-      break;
-    }
-  }
-  o.color = outputColor;
-  o.albedo = outputColor;
-  o.opacity = outputOpacity;
-  o.normal = outputNormal;
-  o.depth = depth;
-  o.primID = primID;
-  o.objID = objID;
-  o.instID = instID;
-}
-
-// computeOrthonormalBasis (gpu_util.h:210-222), Pixar ONB
-__device__ __forceinline__ f3 onbMul(f3 n, f3 s)
-{
-  const float sign = n.z >= 0.f ? 1.f : -1.f;
-  const float a = -1.f / (sign + n.z);
-  const float b = n.x * n.y * a;
-  const f3 u = mk3(1.f + sign * n.x * n.x * a, sign * b, -sign * n.x);
-  const f3 v = mk3(b, sign + n.y * n.y * a, -n.y);
-  return u * s.x + v * s.y + n * s.z;
-}
-
-// sampleUnitSphere (gpu_util.h:236-243)
-__device__ __forceinline__ f3 sampleUnitSphere(RandState &rs, f3 n)
-{
-  const float cost = 1.f - 2.f * curand_uniform(&rs);
-  const float sint = sqrtf(fmaxf(0.f, 1.f - cost * cost));
-  const float phi = 2.f * float(M_PI) * curand_uniform(&rs);
-  return onbMul(n, mk3(sint * cosf(phi), sint * sinf(phi), -cost));
-}
-
-// Diffuse path tracer raygen body (DiffusePathTracer_ptx.cu:82-215). The
-// path state (depth, Lw) lives across the pixel's sample loop, as in the
-// reference, where PathData is declared outside it.
-struct PathData
-{
-  int depth;
-  f3 Lw;
-};
-
-template <bool STATS, bool SURF>
-__device__ __forceinline__ void integrateDPT(const FrameParams &P,
-    TravStats &st,
-    RandState &rs,
-    int px,
-    int py,
-    PathData &pd,
-    SampleOut &o)
-{
-  const RendererGPU &rp = P.renderer;
-  const WorldGPU &w = P.world;
-  float scrX, scrY;
-  Ray ray = makePrimaryRay(P, rs, px, py, false, scrX, scrY);
-  const float tmax = ray.tmax;
-  const float4 bg = rp.background;
-  o.color = mk3(bg.x, bg.y, bg.z); // albedo channel value (outColor)
-  o.normal = ray.dir;
-  o.depth = tmax;
-  o.primID = o.objID = o.instID = ~0u;
-  const bool cull = rp.cullTriangleBF != 0;
-  while (true) {
-    Hit h;
-    float unused;
-    // a primary / path ray against an empty surface set still counts
-    if (!SURF)
-      st.rays++;
-    const bool found = SURF && traverse<0, STATS>(w,
-        ray.org,
-        ray.dir,
-        ray.tmin,
-        ray.tmax,
-        cull,
-        false,
-        h,
-        unused,
-        P.errorFlag,
-        st);
-    SurfaceHit sh;
-    if (found)
-      populateSurfaceHit(w, ray, h, sh);
-    f3 volumeColor = mk3(0.f, 0.f, 0.f);
-    float volumeOpacity = 0.f, Tr = 0.f;
-    uint32_t vObjID = ~0u, vInstID = ~0u;
-    const float volumeDepth = w.numVolumes
-        ? sampleDistanceAllVolumes(w,
-              rs,
-              ray.org,
-              ray.dir,
-              ray.tmin,
-              found ? sh.t : ray.tmax,
-              volumeColor,
-              volumeOpacity,
-              Tr,
-              vObjID,
-              vInstID)
-        : (found ? sh.t : ray.tmax);
-    if (!w.numVolumes)
-      Tr = 1.f;
-    const bool volumeHit = Tr < 1.f && (!found || volumeDepth < sh.t);
-    if (!found && !volumeHit)
-      break;
-    if (pd.depth++ >= rp.maxDepth) {
-      pd.Lw = mk3(0.f, 0.f, 0.f);
-      break;
-    }
-    f3 albedo;
-    f3 pos;
-    if (!volumeHit) {
-      pos = sh.hitpoint + (sh.epsilon * sh.Ng);
-      albedo = matteInit(w, sh).baseColor;
-    } else {
-      pos = ray.org + volumeDepth * ray.dir;
-      albedo = volumeColor;
-    }
-    pd.Lw *= albedo;
-    const float Pr = compMax(pd.Lw);
-    if (Pr < .2f) {
-      if (curand_uniform(&rs) > Pr) {
-        pd.Lw = mk3(0.f, 0.f, 0.f);
-        break;
-      }
-      pd.Lw = pd.Lw / Pr;
-    }
-    f3 scatterDir;
-    if (!volumeHit) {
-      scatterDir = randomDir(rs, sh.Ns);
-      pd.Lw *= fmaxf(0.f, dot(scatterDir, sh.Ng));
-    } else
-      scatterDir = sampleUnitSphere(rs, -ray.dir);
-    ray.org = pos;
-    ray.dir = scatterDir;
-    ray.tmin = 0.f;
-    ray.tmax = rp.occlusionDistance;
-  }
-  const f3 Ld = mk3(rp.ambientIntensity, rp.ambientIntensity, rp.ambientIntensity);
-  const f3 color = pd.depth ? pd.Lw * Ld : mk3(bg.x, bg.y, bg.z);
-  // accumResults gets (color, 1) and outColor (the background) as albedo
-  const f3 albedoOut = o.color;
-  o.color = color;
-  o.opacity = 1.f;
-  o.albedo = albedoOut;
-}
-
-// --- output ------------------------------------------------------------------
-
-__device__ __forceinline__ float4 tonemap(float4 v)
-{
-  const float m = fmaxf(0.f, fmaxf(v.x, fmaxf(v.y, v.z)));
-  const float d = 1.f + m;
-  return make_float4(v.x / d, v.y / d, v.z / d, v.w);
-}
-
-__device__ __forceinline__ float4 inverseTonemap(float4 v)
-{
-  const float d = fmaxf(1e-12f, 1.f - fmaxf(v.x, fmaxf(v.y, v.z)));
-  return make_float4(v.x / d, v.y / d, v.z / d, v.w);
-}
-
-__device__ __forceinline__ float linearToSrgb(float c)
-{
-  return srgbEncode(c);
-}
-
-__device__ __forceinline__ uint32_t packUnorm4x8(float4 v)
-{
-  const uint32_t r = (uint32_t)roundf(fminf(fmaxf(v.x, 0.f), 1.f) * 255.f);
-  const uint32_t g = (uint32_t)roundf(fminf(fmaxf(v.y, 0.f), 1.f) * 255.f);
-  const uint32_t b = (uint32_t)roundf(fminf(fmaxf(v.z, 0.f), 1.f) * 255.f);
-  const uint32_t a = (uint32_t)roundf(fminf(fmaxf(v.w, 0.f), 1.f) * 255.f);
-  return r | (g << 8) | (b << 16) | (a << 24);
-}
-
-__device__ __forceinline__ void writeOutputColor(
-    const FramebufferGPU &fb, float4 accum, uint32_t idx, int frameIDOffset)
-{
-  const float n = float(fb.frameID + frameIDOffset + 1);
-  const float4 c =
-      inverseTonemap(make_float4(accum.x / n, accum.y / n, accum.z / n, accum.w / n));
-  if (fb.format == FORMAT_SRGB)
-    fb.outColorU[idx] = packUnorm4x8(make_float4(
-        linearToSrgb(c.x), linearToSrgb(c.y), linearToSrgb(c.z), c.w));
-  else if (fb.format == FORMAT_UINT)
-    fb.outColorU[idx] = packUnorm4x8(c);
-  else
-    fb.outColorF[idx] = c;
-}
-
-template <int RT, bool STATS, bool SURF>
-__device__ __forceinline__ void renderPixel(
-    const FrameParams &P, TravStats &st, int lx, int ly)
-{
-  const FramebufferGPU &fb = P.fb;
-  const int x = computePixelX(lx, fb.checkerboardID);
-  const int y = computePixelY(ly, fb.checkerboardID);
-  if (x >= (int)fb.w || y >= (int)fb.h)
-    return;
-  RandState rs;
-  curand_init((unsigned long long)(y * (int)fb.w + x),
-      0ull,
-      (unsigned long long)fb.frameID * 512ull,
-      &rs);
-  const uint32_t idx = (uint32_t)x + (uint32_t)y * fb.w;
-  float4 acc = fb.accum[idx];
-  float curDepth = fb.depth ? fb.depth[idx] : 0.f;
-  bool idsDirty = false;
-  uint32_t oPrim = 0, oObj = 0, oInst = 0;
-  f3 albedoAcc = mk3(0.f, 0.f, 0.f), normalAcc = mk3(0.f, 0.f, 0.f);
-  const int iters = RT == RENDERER_RAYCAST ? 1 : P.renderer.numIterations;
-  PathData pd;
-  pd.depth = 0;
-  pd.Lw = mk3(1.f, 1.f, 1.f);
-  for (int i = 0; i < iters; i++) {
-    SampleOut s;
-    if (RT == RENDERER_DPT)
-      integrateDPT<STATS, SURF>(P, st, rs, x, y, pd, s);
-    else
-      integrateSample<RT, STATS, SURF>(P, st, rs, x, y, s);
-    const float4 tm = tonemap(make_float4(s.color.x, s.color.y, s.color.z, s.opacity));
-    acc.x += tm.x;
-    acc.y += tm.y;
-    acc.z += tm.z;
-    acc.w += tm.w;
-    albedoAcc += s.albedo;
-    normalAcc += s.normal;
-    if (!fb.depth || s.depth < curDepth) {
-      curDepth = s.depth;
-      oPrim = s.primID;
-      oObj = s.objID;
-      oInst = s.instID;
-      idsDirty = true;
-    }
-  }
-  fb.accum[idx] = acc;
-  if (fb.albedo)
-    fb.albedo[idx] += albedoAcc;
-  if (fb.normal)
-    fb.normal[idx] += normalAcc;
-  if (idsDirty) {
-    if (fb.depth)
-      fb.depth[idx] = curDepth;
-    if (fb.primID)
-      fb.primID[idx] = oPrim;
-    if (fb.objID)
-      fb.objID[idx] = oObj;
-    if (fb.instID)
-      fb.instID[idx] = oInst;
-  }
-  writeOutputColor(fb, acc, idx, iters - 1);
-  if (fb.checkerboardID == 0 && fb.frameID + iters - 1 == 0) {
-    // first-frame 2x2 splat (gpu_util.h:424-442)
-    if (x + 1 < (int)fb.w)
-      writeOutputColor(fb, acc, idx + 1, iters - 1);
-    if (y + 1 < (int)fb.h)
-      writeOutputColor(fb, acc, idx + fb.w, iters - 1);
-    if (x + 1 < (int)fb.w && y + 1 < (int)fb.h)
-      writeOutputColor(fb, acc, idx + fb.w + 1, iters - 1);
-  }
-}
-
-__device__ __forceinline__ unsigned long long warpSum(unsigned long long v)
-{
-  for (int o = 16; o > 0; o >>= 1)
-    v += __shfl_xor_sync(0xffffffffu, v, o);
-  return v;
-}
-
-template <int RT, bool STATS, bool SURF>
-__global__ void __launch_bounds__(128, SURF ? VRTX_RENDER_MIN_BLOCKS : VRTX_VOLUME_MIN_BLOCKS)
-    k_render(const FrameParams P)
-{
-  const int lane = threadIdx.x & 31;
-  const uint32_t numTiles = P.numTilesX * P.numTilesY;
-  TravStats st{0u, 0u, 0u, 0u, 0u, 0u, 0u};
-  while (true) {
-    uint32_t t = 0;
-    if (lane == 0)
-      t = atomicAdd(P.workCounter, 1u);
-    t = __shfl_sync(0xffffffffu, t, 0);
-    if (t >= numTiles)
-      break;
-    const uint32_t tx = t % P.numTilesX, ty = t / P.numTilesX;
-    const int lx = (int)(tx * 8 + (lane & 7));
-    const int ly = (int)(ty * 4 + (lane >> 3));
-    if (lx < (int)P.launchW && ly < (int)P.launchH)
-      renderPixel<RT, STATS, SURF>(P, st, lx, ly);
-  }
-  // per-warp totals: rays and volume samples always, traversal counters in
-  // the counting build
-  const unsigned long long rays = warpSum(st.rays);
-  const unsigned long long smp = warpSum(st.samples), fet = warpSum(st.fetches);
-  if (lane == 0) {
-    atomicAdd(P.stats + 0, rays);
-    if (smp)
-      atomicAdd(P.stats + 5, smp);
-    if (fet)
-      atomicAdd(P.stats + 6, fet);
-  }
-  if (STATS) {
-    const unsigned long long n = warpSum(st.nodes), t = warpSum(st.tris),
-                             sp = warpSum(st.spheres), in = warpSum(st.instances);
-    if (lane == 0) {
-      atomicAdd(P.stats + 1, n);
-      atomicAdd(P.stats + 2, t);
-      atomicAdd(P.stats + 3, sp);
-      atomicAdd(P.stats + 4, in);
-    }
-  }
-}
 
 __global__ void k_clearFrame(FramebufferGPU fb)
 {
@@ -1049,467 +28,44 @@ __global__ void k_clearFrame(FramebufferGPU fb)
   }
 }
 
-// ---------------------------------------------------------------------------
-// Wavefront form of the "ao" renderer (opaque materials, no volumes).
-//
-// The reference runs one raygen per pixel that loops over pixelSamples and,
-// per hit, traces ambientSamples any-hit rays inline
-// (AmbientOcclusion_ptx.cu:86-220, computeAO.h:38-60). Inline, lanes whose
-// camera ray missed sit idle while their neighbours trace 16 occlusion rays,
-// and the warp runs at a fraction of its width. Here every sample is three
-// kernels:
-//   k_aoPrimary  camera ray + closest hit; draws the AO directions and
-//                appends the rays to a compacted queue (16 slots per hit
-//                pixel, reserved with one atomic per warp);
-//   k_aoTrace    one thread per queued ray, any-hit traversal only (a
-//                small kernel with room for many warps per SM);
-//   k_aoResolve  sums weight * attenuation in ray order, shades, and
-//                accumulates exactly as accumResults does.
-// Each pixel's Philox stream is re-entered at its consumed offset
-// (curand_init(seed, 0, frameID*512 + consumed)), which is the position the
-// reference's single long-lived state has reached at that point, so every
-// random number lands where the reference draws it.
-// ---------------------------------------------------------------------------
-
-struct AOPixel
-{
-  float depth;
-  uint32_t prim, obj, inst;
-  f3 base; // matte colour of the hit (unused on a miss)
-  float weights; // sum of AO weights; < 0 marks a miss
-  f3 normal; // outputNormal (Ng of the hit, or the ray direction)
-  uint32_t rayBase;
-};
-
-struct AORay
-{
-  float4 orgTmax; // org.xyz, tmax (< 0: weight 0, not traced)
-  float4 dirWeight; // dir.xyz, weight
-};
-
-__device__ __forceinline__ uint32_t warpAppend(uint32_t *counter, uint32_t n)
-{
-  // one atomic per warp: exclusive prefix of n over the active lanes
-  const uint32_t mask = __activemask();
-  const int lane = threadIdx.x & 31;
-  uint32_t total = 0, before = 0;
-  for (int l = 0; l < 32; l++) {
-    if (!((mask >> l) & 1u))
-      continue;
-    const uint32_t v = __shfl_sync(mask, n, l);
-    if (l < lane)
-      before += v;
-    total += v;
-  }
-  const int leader = __ffs(mask) - 1;
-  uint32_t base = 0;
-  if (lane == leader && total)
-    base = atomicAdd(counter, total);
-  base = __shfl_sync(mask, base, leader);
-  return base + before;
-}
-
-template <bool STATS, bool SEG>
-__global__ void __launch_bounds__(128) k_aoPrimary(const FrameParams P,
-    int sampleIdx,
-    uint32_t *consumed,
-    AOPixel *pixels,
-    AORay *rays,
-    uint32_t *rayCount)
-{
-  const uint32_t lx = blockIdx.x * 8 + (threadIdx.x & 7);
-  const uint32_t ly = blockIdx.y * 16 + (threadIdx.x >> 3);
-  const FramebufferGPU &fb = P.fb;
-  const int x = computePixelX((int)lx, fb.checkerboardID);
-  const int y = computePixelY((int)ly, fb.checkerboardID);
-  const bool valid = lx < P.launchW && ly < P.launchH && x < (int)fb.w && y < (int)fb.h;
-  TravStats st{0u, 0u, 0u, 0u, 0u, 0u, 0u};
-  uint32_t nRays = 0;
-  RandState rs;
-  AOPixel px;
-  px.weights = -1.f;
-  f3 org = mk3(0.f, 0.f, 0.f), Ns = mk3(0.f, 0.f, 1.f);
-  uint32_t idx = 0;
-  if (valid) {
-    idx = (uint32_t)x + (uint32_t)y * fb.w;
-    const uint32_t used = sampleIdx ? consumed[idx] : 0u;
-    curand_init((unsigned long long)(y * (int)fb.w + x),
-        0ull,
-        (unsigned long long)fb.frameID * 512ull + used,
-        &rs);
-    float sx, sy;
-    Ray ray = makePrimaryRay(P, rs, x, y, false, sx, sy);
-    Hit h;
-    float unused;
-    const bool found = traverse<0, STATS, SEG>(P.world,
-        ray.org,
-        ray.dir,
-        ray.tmin,
-        ray.tmax,
-        P.renderer.cullTriangleBF != 0,
-        true,
-        h,
-        unused,
-        P.errorFlag,
-        st);
-    uint32_t draws = 4;
-    if (found) {
-      SurfaceHit sh;
-      populateSurfaceHit(P.world, ray, h, sh);
-      px.depth = sh.t;
-      px.prim = geometryPrimId(P.world, sh);
-      px.obj = P.world.surfaces[sh.surface].id;
-      px.inst = sh.instUserId;
-      px.base = matteInit(P.world, sh).baseColor;
-      px.normal = sh.Ng;
-      px.weights = 0.f;
-      org = sh.hitpoint + (sh.epsilon * sh.Ng);
-      Ns = sh.Ns;
-      nRays = (uint32_t)max(P.renderer.aoSamples, 0);
-      draws += 4 * nRays;
-    } else {
-      px.depth = fminf(1e30f, ray.tmax);
-      px.prim = 0u;
-      px.obj = ~0u;
-      px.inst = ~0u;
-      px.normal = ray.dir;
-    }
-    consumed[idx] = used + draws;
-  }
-  const uint32_t base = warpAppend(rayCount, nRays);
-  if (valid) {
-    px.rayBase = base;
-    for (uint32_t i = 0; i < nRays; i++) {
-      const f3 dir = randomDir(rs, Ns);
-      const float weight = fmaxf(0.f, dot(dir, Ns));
-      px.weights += weight;
-      AORay r;
-      r.orgTmax = make_float4(
-          org.x, org.y, org.z, weight != 0.f ? P.renderer.occlusionDistance : -1.f);
-      r.dirWeight = make_float4(dir.x, dir.y, dir.z, weight);
-      rays[base + i] = r;
-    }
-    pixels[idx] = px;
-  }
-  if (STATS || true) {
-    const unsigned long long r = warpSum(valid ? st.rays : 0u);
-    if ((threadIdx.x & 31) == 0)
-      atomicAdd(P.stats + 0, r);
-  }
-  if (STATS) {
-    const unsigned long long n = warpSum(st.nodes), t = warpSum(st.tris),
-                             sp = warpSum(st.spheres), in = warpSum(st.instances);
-    if ((threadIdx.x & 31) == 0) {
-      atomicAdd(P.stats + 1, n);
-      atomicAdd(P.stats + 2, t);
-      atomicAdd(P.stats + 3, sp);
-      atomicAdd(P.stats + 4, in);
-    }
-  }
-}
-
-// Any-hit pass over the compacted AO ray queue. Persistent: every lane
-// holds one ray; a lane whose ray has ended takes the next one from the
-// queue (one atomic per warp, once at least VRTX_AO_REFILL lanes wait, or
-// when the warp has no live ray), so a warp keeps most lanes busy instead
-// of waiting for its slowest ray. Each ray's result depends on that ray
-// alone: the queue order in which lanes take rays does not change it.
-template <bool STATS, bool SEG>
-__global__ void __launch_bounds__(128, VRTX_TRACE_MIN_BLOCKS) k_aoTrace(const FrameParams P,
-    const AORay *rays,
-    const uint32_t *rayCount,
-    uint32_t *fetchCounter,
-    float *weighted)
-{
-  const uint32_t n = *rayCount;
-  const uint32_t lane = threadIdx.x & 31u;
-  TravStats st{0u, 0u, 0u, 0u, 0u, 0u, 0u};
-#if VRTX_AO_SHARED_STACK > 0
-  __shared__ uint2 shStack[VRTX_AO_SHARED_STACK * 128];
-  SplitStack<VRTX_TRAVERSAL_STACK, VRTX_AO_SHARED_STACK, 128> stack;
-  stack.sh = shStack + threadIdx.x;
-#else
-  LocalStack<VRTX_TRAVERSAL_STACK> stack;
-#endif
-  OccState s;
-  uint32_t idx = 0;
-  bool live = false, exhausted = false;
-  while (true) {
-    const uint32_t want = __ballot_sync(0xffffffffu, !live && !exhausted);
-    const uint32_t busy = __ballot_sync(0xffffffffu, live);
-    if (want && (__popc(want) >= VRTX_AO_REFILL || busy == 0u)) {
-      const uint32_t leader = __ffs(want) - 1;
-      uint32_t base = 0;
-      if (lane == leader)
-        base = atomicAdd(fetchCounter, (uint32_t)__popc(want));
-      base = __shfl_sync(0xffffffffu, base, leader);
-      if ((want >> lane) & 1u) {
-        idx = base + __popc(want & ((1u << lane) - 1u));
-        if (idx >= n) {
-          exhausted = true;
-        } else {
-          const float4 o = __ldg(&rays[idx].orgTmax);
-          if (o.w < 0.f) {
-            weighted[idx] = 0.f; // zero weight: not traced
-          } else {
-            const float4 d = __ldg(&rays[idx].dirWeight);
-            st.rays++;
-            live = occlusionBegin(
-                P.world, s, mk3(o.x, o.y, o.z), mk3(d.x, d.y, d.z), o.w);
-            if (!live)
-              weighted[idx] = 0.f;
-          }
-        }
-      }
-    }
-    if (__all_sync(0xffffffffu, exhausted))
-      break;
-    if (live) {
-      const int r = occlusionStep<STATS, VRTX_TRAVERSAL_STACK, decltype(stack), SEG>(P.world,
-          s,
-          stack,
-          reinterpret_cast<const float4 *>(rays + idx),
-          P.errorFlag,
-          st);
-      if (r != OCC_CONTINUE) {
-        weighted[idx] = r == OCC_HIT ? __ldg(&rays[idx].dirWeight.w) : 0.f;
-        live = false;
-      }
-    }
-  }
-  // the frame totals, and the same counts for this kernel alone ([8..12])
-  const unsigned long long rs = warpSum(st.rays);
-  if (lane == 0) {
-    atomicAdd(P.stats + 0, rs);
-    atomicAdd(P.stats + 8, rs);
-  }
-  if (STATS) {
-    const unsigned long long nn = warpSum(st.nodes), t = warpSum(st.tris),
-                             sp = warpSum(st.spheres), in = warpSum(st.instances);
-    if (lane == 0) {
-      atomicAdd(P.stats + 1, nn);
-      atomicAdd(P.stats + 2, t);
-      atomicAdd(P.stats + 3, sp);
-      atomicAdd(P.stats + 4, in);
-      atomicAdd(P.stats + 9, nn);
-      atomicAdd(P.stats + 10, t);
-      atomicAdd(P.stats + 11, sp);
-      atomicAdd(P.stats + 12, in);
-    }
-  }
-}
-
-__global__ void __launch_bounds__(128) k_aoResolve(const FrameParams P,
-    int sampleIdx,
-    int numSamples,
-    const AOPixel *pixels,
-    const float *weighted)
-{
-  const uint32_t lx = blockIdx.x * 8 + (threadIdx.x & 7);
-  const uint32_t ly = blockIdx.y * 16 + (threadIdx.x >> 3);
-  const FramebufferGPU &fb = P.fb;
-  const int x = computePixelX((int)lx, fb.checkerboardID);
-  const int y = computePixelY((int)ly, fb.checkerboardID);
-  if (lx >= P.launchW || ly >= P.launchH || x >= (int)fb.w || y >= (int)fb.h)
-    return;
-  const RendererGPU &rp = P.renderer;
-  const uint32_t idx = (uint32_t)x + (uint32_t)y * fb.w;
-  const AOPixel px = pixels[idx];
-  f3 outputColor;
-  float outputOpacity;
-  if (px.weights >= 0.f) {
-    float hits = 0.f;
-    const int n = max(rp.aoSamples, 0);
-    for (int i = 0; i < n; i++)
-      hits += weighted[px.rayBase + i];
-    const float aoFactor =
-        n > 0 ? (px.weights > 0.f ? 1.f - hits / px.weights : 0.f) : 1.f;
-    const f3 lighting = aoFactor * rp.ambientIntensity * rp.ambientColor;
-    f3 color = mk3(0.f, 0.f, 0.f);
-    float opacity = 0.f;
-    color += (px.base * lighting) * (1.f - opacity);
-    opacity += 1.f * (1.f - opacity);
-    color *= opacity;
-    outputColor = mk3(0.f, 0.f, 0.f) + color * (1.f - 0.f);
-    outputOpacity = 0.f + opacity * (1.f - 0.f);
-  } else {
-    f3 color = mk3(0.f, 0.f, 0.f);
-    float opacity = 0.f;
-    color *= opacity;
-    const float4 bg = rp.background;
-    color += mk3(bg.x, bg.y, bg.z) * (1.f - opacity);
-    opacity += bg.w * (1.f - opacity);
-    outputColor = mk3(0.f, 0.f, 0.f) + color * (1.f - 0.f);
-    outputOpacity = 0.f + opacity * (1.f - 0.f);
-  }
-  float4 acc = fb.accum[idx];
-  const float4 tm = tonemap(make_float4(
-      outputColor.x, outputColor.y, outputColor.z, outputOpacity));
-  acc.x += tm.x;
-  acc.y += tm.y;
-  acc.z += tm.z;
-  acc.w += tm.w;
-  fb.accum[idx] = acc;
-  if (fb.albedo)
-    fb.albedo[idx] += outputColor;
-  if (fb.normal)
-    fb.normal[idx] += px.normal;
-  if (!fb.depth || px.depth < fb.depth[idx]) {
-    if (fb.depth)
-      fb.depth[idx] = px.depth;
-    if (fb.primID)
-      fb.primID[idx] = px.prim;
-    if (fb.objID)
-      fb.objID[idx] = px.obj;
-    if (fb.instID)
-      fb.instID[idx] = px.inst;
-  }
-  if (sampleIdx == numSamples - 1) {
-    writeOutputColor(fb, acc, idx, sampleIdx);
-    if (fb.checkerboardID == 0 && fb.frameID + sampleIdx == 0) {
-      if (x + 1 < (int)fb.w)
-        writeOutputColor(fb, acc, idx + 1, sampleIdx);
-      if (y + 1 < (int)fb.h)
-        writeOutputColor(fb, acc, idx + fb.w, sampleIdx);
-      if (x + 1 < (int)fb.w && y + 1 < (int)fb.h)
-        writeOutputColor(fb, acc, idx + fb.w + 1, sampleIdx);
-    }
-  }
-}
-
 } // namespace
 
-size_t aoWavefrontBytes(uint32_t w, uint32_t h, int aoSamples)
-{
-  const size_t px = (size_t)w * h;
-  const size_t rays = px * (size_t)max(aoSamples, 0);
-  return px * (sizeof(AOPixel) + sizeof(uint32_t)) + rays * (sizeof(AORay) + 4) + 1024;
-}
-
-// The per-sample launches of the wavefront AO renderer for one (stats,
-// segment primitives) combination.
-template <bool STATS, bool SEG>
-static void aoSamples(const FrameParams &P,
-    dim3 grid,
-    int numSMs,
-    uint32_t *consumed,
-    AOPixel *pixels,
-    AORay *rays,
-    uint32_t *rayCount,
-    float *weighted,
-    cudaStream_t s,
-    cudaEvent_t *traceEvents)
-{
-  int occ = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_aoTrace<STATS, SEG>, 128, 0);
-  const int traceGrid = numSMs * (occ > 0 ? occ : 1);
-  const int n = max(P.renderer.numIterations, 1);
-  for (int i = 0; i < n; i++) {
-    cudaMemsetAsync(rayCount, 0, 8, s); // queue length, fetch counter
-    // the primary pass keeps the general traversal (the per-pixel kernel's),
-    // so both forms of the renderer produce the same hits bit for bit
-    k_aoPrimary<STATS, true><<<grid, 128, 0, s>>>(P, i, consumed, pixels, rays, rayCount);
-    if (traceEvents)
-      cudaEventRecord(traceEvents[2 * i], s);
-    k_aoTrace<STATS, SEG><<<traceGrid, 128, 0, s>>>(P, rays, rayCount, rayCount + 1, weighted);
-    if (traceEvents)
-      cudaEventRecord(traceEvents[2 * i + 1], s);
-    k_aoResolve<<<grid, 128, 0, s>>>(P, i, n, pixels, weighted);
-  }
-}
-
-cudaError_t launchAOWavefront(const FrameParams &P,
-    int numSMs,
+static void dispatchAll(const FrameParams &P,
+    int type,
     bool stats,
-    void *scratch,
-    cudaStream_t s,
-    cudaEvent_t *traceEvents)
+    bool surfaces,
+    bool nanovdb,
+    int *occ,
+    int grid,
+    cudaStream_t s)
 {
-  const size_t px = (size_t)P.fb.w * P.fb.h;
-  const size_t nr = px * (size_t)max(P.renderer.aoSamples, 0);
-  uint8_t *p = (uint8_t *)scratch;
-  uint32_t *rayCount = (uint32_t *)p;
-  p += 256;
-  uint32_t *consumed = (uint32_t *)p;
-  p += ((px * 4 + 255) / 256) * 256;
-  AOPixel *pixels = (AOPixel *)p;
-  p += ((px * sizeof(AOPixel) + 255) / 256) * 256;
-  AORay *rays = (AORay *)p;
-  p += ((nr * sizeof(AORay) + 255) / 256) * 256;
-  float *weighted = (float *)p;
-  const dim3 grid((P.launchW + 7) / 8, (P.launchH + 15) / 16);
-  const bool seg = P.world.hasSegments != 0;
-  if (stats) {
-    if (seg)
-      aoSamples<true, true>(P, grid, numSMs, consumed, pixels, rays, rayCount, weighted, s, traceEvents);
-    else
-      aoSamples<true, false>(P, grid, numSMs, consumed, pixels, rays, rayCount, weighted, s, traceEvents);
-  } else {
-    if (seg)
-      aoSamples<false, true>(P, grid, numSMs, consumed, pixels, rays, rayCount, weighted, s, traceEvents);
-    else
-      aoSamples<false, false>(P, grid, numSMs, consumed, pixels, rays, rayCount, weighted, s, traceEvents);
-  }
-  return cudaGetLastError();
-}
-
-template <int RT, bool STATS, bool SURF>
-static void launchOne(const FrameParams &P, int *occ, int grid, cudaStream_t s)
-{
-  if (occ)
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(occ, k_render<RT, STATS, SURF>, 128, 0);
+  if (!surfaces)
+    dispatchVolumeOnly(P, type, stats, nanovdb, occ, grid, s);
+  else if (stats)
+    dispatchSurfaceCounting(P, type, occ, grid, s);
   else
-    k_render<RT, STATS, SURF><<<grid, 128, 0, s>>>(P);
+    dispatchSurface<false>(P, type, occ, grid, s);
 }
 
-template <bool STATS, bool SURF>
-static void dispatch(const FrameParams &P, int type, int *occ, int grid, cudaStream_t s)
-{
-  switch (type) {
-  case RENDERER_RAYCAST:
-    launchOne<RENDERER_RAYCAST, STATS, SURF>(P, occ, grid, s);
-    break;
-  case RENDERER_AO:
-    launchOne<RENDERER_AO, STATS, SURF>(P, occ, grid, s);
-    break;
-  case RENDERER_DPT:
-    launchOne<RENDERER_DPT, STATS, SURF>(P, occ, grid, s);
-    break;
-  default:
-    launchOne<RENDERER_DIRECT_LIGHT, STATS, SURF>(P, occ, grid, s);
-    break;
-  }
-}
-
-template <bool STATS>
-static void dispatchSurf(
-    const FrameParams &P, int type, bool surf, int *occ, int grid, cudaStream_t s)
-{
-  if (surf)
-    dispatch<STATS, true>(P, type, occ, grid, s);
-  else
-    dispatch<STATS, false>(P, type, occ, grid, s);
-}
-
-int renderOccupancyBlocks(int rendererType, bool stats, bool surfaces)
+int renderOccupancyBlocks(int rendererType, bool stats, bool surfaces, bool nanovdb)
 {
   int blocks = 0;
   FrameParams dummy{};
-  if (stats)
-    dispatchSurf<true>(dummy, rendererType, surfaces, &blocks, 0, 0);
-  else
-    dispatchSurf<false>(dummy, rendererType, surfaces, &blocks, 0, 0);
+  dispatchAll(dummy, rendererType, stats, surfaces, nanovdb, &blocks, 0, 0);
   return blocks > 0 ? blocks : 1;
 }
 
 cudaError_t launchRender(
     const FrameParams &P, int gridBlocks, bool stats, cudaStream_t s)
 {
-  const bool surf = P.world.numInstances > 0;
-  if (stats)
-    dispatchSurf<true>(P, P.renderer.type, surf, nullptr, gridBlocks, s);
-  else
-    dispatchSurf<false>(P, P.renderer.type, surf, nullptr, gridBlocks, s);
+  dispatchAll(P,
+      P.renderer.type,
+      stats,
+      P.world.numInstances > 0,
+      P.world.hasNanovdb != 0,
+      nullptr,
+      gridBlocks,
+      s);
   return cudaGetLastError();
 }
 

@@ -6,7 +6,20 @@
 namespace vrtx {
 
 // integrator (render.cu)
-int renderOccupancyBlocks(int rendererType, bool stats, bool surfaces);
+int renderOccupancyBlocks(int rendererType, bool stats, bool surfaces, bool nanovdb);
+// the counting build of the per-pixel kernels for worlds with surfaces
+// (render_counting.cu): launches, or with occ set reports blocks per SM
+void dispatchSurfaceCounting(
+    const FrameParams &P, int type, int *occ, int grid, cudaStream_t s);
+// the per-pixel kernels of volume-only worlds (render_volume.cu): launches,
+// or with occ set reports resident blocks per SM
+void dispatchVolumeOnly(const FrameParams &P,
+    int type,
+    bool stats,
+    bool nanovdb,
+    int *occ,
+    int grid,
+    cudaStream_t s);
 // stats: the counting build (node visits, primitive tests, BLAS entries)
 cudaError_t launchRender(
     const FrameParams &P, int gridBlocks, bool stats, cudaStream_t s);
@@ -104,6 +117,9 @@ cudaError_t launchReferenceGridRanges(cudaTextureObject_t field,
     const int mcDims[3],
     float *ranges,
     cudaStream_t s);
+// the same grid over a NanoVDB field
+cudaError_t launchReferenceGridRangesNanovdb(
+    const NvdbGPU &grid, box3 bounds, const int mcDims[3], float *ranges, cudaStream_t s);
 cudaError_t launchReferenceMajorants(const float *ranges,
     const int mcDims[3],
     cudaTextureObject_t tf,

@@ -8,6 +8,7 @@
 // treated as texture coordinates, which does not bound the voxels a sample
 // can see; skipping cells needs a bound that does, so every voxel of the
 // cell plus a one-voxel apron is read.
+#include "nvdb.cuh"
 #include "render.h"
 
 namespace vrtx {
@@ -378,15 +379,38 @@ __global__ void k_refGridInit(float *ranges, int cells)
   ranges[2 * c + 1] = -1e30f;
 }
 
-__global__ void k_refGridRanges(cudaTextureObject_t field,
-    f3 origin,
-    f3 spacing,
-    f3 invSpacing,
-    box3 bounds,
-    int mx,
-    int my,
-    int mz,
-    float *ranges)
+// The field sampler the reference grid build goes through: the structured
+// field's texture at ((p - origin) + 0.5 spacing) * invSpacing
+// (sampleSpatialField.h:54-78), or a NanoVDB grid (sampleSpatialField.h:
+// 80-109).
+struct RefTextureTap
+{
+  cudaTextureObject_t field;
+  f3 origin, spacing, invSpacing;
+  __device__ __forceinline__ float operator()(f3 p) const
+  {
+    const float cx = __fmul_rn(
+        __fadd_rn(__fsub_rn(p.x, origin.x), __fmul_rn(0.5f, spacing.x)), invSpacing.x);
+    const float cy = __fmul_rn(
+        __fadd_rn(__fsub_rn(p.y, origin.y), __fmul_rn(0.5f, spacing.y)), invSpacing.y);
+    const float cz = __fmul_rn(
+        __fadd_rn(__fsub_rn(p.z, origin.z), __fmul_rn(0.5f, spacing.z)), invSpacing.z);
+    return tex3D<float>(field, cx, cy, cz);
+  }
+};
+
+struct RefNanovdbTap
+{
+  NvdbGPU grid;
+  __device__ __forceinline__ float operator()(f3 p) const
+  {
+    nvdb::Accessor a;
+    return nvdb::sample(grid, a, p);
+  }
+};
+
+template <typename Tap>
+__global__ void k_refGridRanges(Tap tap, box3 bounds, int mx, int my, int mz, float *ranges)
 {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= mx * my * mz)
@@ -409,14 +433,7 @@ __global__ void k_refGridRanges(cudaTextureObject_t field,
     const f3 p = mk3(__fdiv_rn(__fadd_rn(float(ix), ox), float(mx)),
         __fdiv_rn(__fadd_rn(float(iy), oy), float(my)),
         __fdiv_rn(__fadd_rn(float(iz), oz), float(mz)));
-    // sampleSpatialField.h:54-78: ((p - origin) + 0.5 spacing) * invSpacing
-    const float cx = __fmul_rn(
-        __fadd_rn(__fsub_rn(p.x, origin.x), __fmul_rn(0.5f, spacing.x)), invSpacing.x);
-    const float cy = __fmul_rn(
-        __fadd_rn(__fsub_rn(p.y, origin.y), __fmul_rn(0.5f, spacing.y)), invSpacing.y);
-    const float cz = __fmul_rn(
-        __fadd_rn(__fsub_rn(p.z, origin.z), __fmul_rn(0.5f, spacing.z)), invSpacing.z);
-    value = fmaxf(value, tex3D<float>(field, cx, cy, cz));
+    value = fmaxf(value, tap(p));
   }
   const int x0 = projectAxis(lx, bounds.lo.x, bounds.hi.x, mx);
   const int x1 = projectAxis(ux, bounds.lo.x, bounds.hi.x, mx);
@@ -479,15 +496,25 @@ cudaError_t launchReferenceGridRanges(cudaTextureObject_t field,
   if (!cells)
     return cudaSuccess;
   k_refGridInit<<<(cells + 255) / 256, 256, 0, s>>>(ranges, cells);
-  k_refGridRanges<<<(cells + 127) / 128, 128, 0, s>>>(field,
-      origin,
-      spacing,
-      invSpacing,
+  k_refGridRanges<<<(cells + 127) / 128, 128, 0, s>>>(
+      RefTextureTap{field, origin, spacing, invSpacing},
       bounds,
       mcDims[0],
       mcDims[1],
       mcDims[2],
       ranges);
+  return cudaGetLastError();
+}
+
+cudaError_t launchReferenceGridRangesNanovdb(
+    const NvdbGPU &grid, box3 bounds, const int mcDims[3], float *ranges, cudaStream_t s)
+{
+  const int cells = mcDims[0] * mcDims[1] * mcDims[2];
+  if (!cells)
+    return cudaSuccess;
+  k_refGridInit<<<(cells + 255) / 256, 256, 0, s>>>(ranges, cells);
+  k_refGridRanges<<<(cells + 127) / 128, 128, 0, s>>>(
+      RefNanovdbTap{grid}, bounds, mcDims[0], mcDims[1], mcDims[2], ranges);
   return cudaGetLastError();
 }
 

@@ -13,6 +13,7 @@
 #include <curand_kernel.h>
 
 #include "gpu_types.h"
+#include "nvdb.cuh"
 
 namespace vrtx {
 
@@ -86,6 +87,25 @@ __device__ __forceinline__ float sampleField(const VolumeGPU &v, f3 p)
   return tex3D<float>(v.field, c.x, c.y, c.z);
 }
 
+// Field samplers the marchers are instantiated on (the reference's
+// SpatialFieldSampler specialisations, gpu/sampleSpatialField.h:48-109).
+struct TextureField
+{
+  __device__ __forceinline__ float operator()(const VolumeGPU &v, f3 p)
+  {
+    return sampleField(v, p);
+  }
+};
+
+struct NanovdbField
+{
+  nvdb::Accessor acc;
+  __device__ __forceinline__ float operator()(const VolumeGPU &v, f3 p)
+  {
+    return nvdb::sample(v.nvdb, acc, p);
+  }
+};
+
 __device__ __forceinline__ float4 classifySample(const VolumeGPU &v, float s)
 {
   if (v.hasTF) {
@@ -114,7 +134,9 @@ __device__ __forceinline__ float cellMajorant(const VolumeGPU &v, f3 p)
 
 // rayMarchVolume + _rayMarchVolume (volumeIntegration.h:64-126): returns the
 // entry depth; accumulates into color (when non-null) and opacity.
-__device__ __forceinline__ float rayMarchVolume(const VolumeGPU &v,
+template <typename Field>
+__device__ __forceinline__ float rayMarchVolumeF(const VolumeGPU &v,
+    Field &field,
     const VolumeHitG &h,
     RandState &rs,
     f3 *color,
@@ -138,7 +160,7 @@ __device__ __forceinline__ float rayMarchVolume(const VolumeGPU &v,
   // accumulation and the stopping rule are those of the plain loop.
   f3 p = h.localOrg + h.localDir * lower;
   bool want = cellMajorant(v, p) > 0.f;
-  float s = want ? sampleField(v, p) : 0.f;
+  float s = want ? field(v, p) : 0.f;
   // bound the march (a ray through a 2^24-step box is not a real scene)
   for (int guard = 0; guard < (1 << 24) && opacity < 0.99f && upper - lower >= 0.f;
        guard++) {
@@ -150,7 +172,7 @@ __device__ __forceinline__ float rayMarchVolume(const VolumeGPU &v,
       const f3 pn = h.localOrg + h.localDir * next;
       wantNext = cellMajorant(v, pn) > 0.f;
       if (wantNext)
-        sNext = sampleField(v, pn);
+        sNext = field(v, pn);
     }
     if (want) {
       st.fetches++;
@@ -171,7 +193,27 @@ __device__ __forceinline__ float rayMarchVolume(const VolumeGPU &v,
   return depth;
 }
 
+// the field-type dispatch of rayMarchVolume (volumeIntegration.h:104-165);
+// NV = false compiles the texture field only (worlds without NanoVDB fields)
+template <bool NV = true>
+__device__ __forceinline__ float rayMarchVolume(const VolumeGPU &v,
+    const VolumeHitG &h,
+    RandState &rs,
+    f3 *color,
+    float &opacity,
+    float invSamplingRate,
+    TravStats &st)
+{
+  if (NV && v.fieldKind == FIELD_NANOVDB) {
+    NanovdbField f;
+    return rayMarchVolumeF(v, f, h, rs, color, opacity, invSamplingRate, st);
+  }
+  TextureField f;
+  return rayMarchVolumeF(v, f, h, rs, color, opacity, invSamplingRate, st);
+}
+
 // rayMarchAllVolumes (volumeIntegration.h:318-350).
+template <bool NV = true>
 __device__ __forceinline__ float rayMarchAllVolumes(const WorldGPU &w,
     RandState &rs,
     f3 org,
@@ -202,7 +244,7 @@ __device__ __forceinline__ float rayMarchAllVolumes(const WorldGPU &w,
     }
     depth = fminf(depth, h.tlo);
     h.thi = fminf(tfar, h.thi);
-    rayMarchVolume(v, h, rs, &color, opacity, invSamplingRate, st);
+    rayMarchVolume<NV>(v, h, rs, &color, opacity, invSamplingRate, st);
     tmin = h.thi + 1e-3f;
     last = h.entry;
   } while (opacity < 0.99f);
@@ -307,7 +349,9 @@ __device__ __forceinline__ void dda3(
 
 // _sampleDistance (volumeIntegration.h:167-238): Woodcock tracking inside
 // each DDA cell against the cell majorant, t -= log(1-u)/majorant*stepSize.
-__device__ __forceinline__ float sampleDistance(const VolumeGPU &v,
+template <typename Field>
+__device__ __forceinline__ float sampleDistanceF(const VolumeGPU &v,
+    Field &field,
     const VolumeHitG &h,
     RandState &rs,
     f3 &albedo,
@@ -337,7 +381,7 @@ __device__ __forceinline__ float sampleDistance(const VolumeGPU &v,
       const f3 p = mk3(__fmaf_rn(h.localDir.x, tt, h.localOrg.x),
           __fmaf_rn(h.localDir.y, tt, h.localOrg.y),
           __fmaf_rn(h.localDir.z, tt, h.localOrg.z));
-      const float s = sampleField(v, p);
+      const float s = field(v, p);
       if (!isnan(s)) {
         const float4 co = classifySample(v, s);
         albedo = mk3(co.x, co.y, co.z);
@@ -355,7 +399,25 @@ __device__ __forceinline__ float sampleDistance(const VolumeGPU &v,
   return t_out + h.tlo;
 }
 
+// the field-type dispatch of sampleDistance (volumeIntegration.h:240-300)
+template <bool NV = true>
+__device__ __forceinline__ float sampleDistance(const VolumeGPU &v,
+    const VolumeHitG &h,
+    RandState &rs,
+    f3 &albedo,
+    float &extinction,
+    float &tr)
+{
+  if (NV && v.fieldKind == FIELD_NANOVDB) {
+    NanovdbField f;
+    return sampleDistanceF(v, f, h, rs, albedo, extinction, tr);
+  }
+  TextureField f;
+  return sampleDistanceF(v, f, h, rs, albedo, extinction, tr);
+}
+
 // sampleDistanceAllVolumes (volumeIntegration.h:352-389)
+template <bool NV = true>
 __device__ __forceinline__ float sampleDistanceAllVolumes(const WorldGPU &w,
     RandState &rs,
     f3 org,
@@ -379,7 +441,7 @@ __device__ __forceinline__ float sampleDistanceAllVolumes(const WorldGPU &w,
     h.thi = fminf(tfar, h.thi);
     f3 alb = mk3(0.f, 0.f, 0.f);
     float ext = 0.f, tr = 0.f;
-    const float d = sampleDistance(v, h, rs, alb, ext, tr);
+    const float d = sampleDistance<NV>(v, h, rs, alb, ext, tr);
     if (d < depth) {
       depth = d;
       albedo = alb;

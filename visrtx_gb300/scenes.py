@@ -371,7 +371,7 @@ class LightSpec:
 
 @dataclass
 class VolumeSpec:
-    field: np.ndarray  # (nz, ny, nx) float32
+    field: np.ndarray | None  # (nz, ny, nx) float32; None for a NanoVDB field
     origin: tuple = (0.0, 0.0, 0.0)
     spacing: tuple = (1.0, 1.0, 1.0)
     filter: str = "linear"
@@ -382,6 +382,9 @@ class VolumeSpec:
     id: int = 0xFFFFFFFF
     uniform_color: tuple = (1.0, 1.0, 1.0)
     uniform_opacity: float = 1.0
+    # a NanoVDB grid buffer (uint8, see nanovdb.build_grid): the volume's
+    # field is then a "nanovdb" spatial field and `field` is unused
+    nvdb: np.ndarray | None = None
 
 
 @dataclass
@@ -564,12 +567,18 @@ def build_on_device(dev, spec: SceneSpec, channels=("color", "depth", "primitive
 
     vols = []
     for v in spec.volumes:
-        f = dev.new_spatial_field("structuredRegular")
-        fld = v.field if hasattr(v.field, "data_ptr") else np.ascontiguousarray(v.field, np.float32)
-        f.set("data", arr3(fld, L.FLOAT32))
-        f.set("origin", tuple(map(float, v.origin)), L.FLOAT32_VEC3)
-        f.set("spacing", tuple(map(float, v.spacing)), L.FLOAT32_VEC3)
-        f.set("filter", v.filter)
+        if v.nvdb is not None:
+            f = dev.new_spatial_field("nanovdb")
+            f.set("data", arr(np.ascontiguousarray(v.nvdb, np.uint8), L.UINT8))
+            f.set("filter", v.filter)
+        else:
+            f = dev.new_spatial_field("structuredRegular")
+            fld = v.field if hasattr(v.field, "data_ptr") else np.ascontiguousarray(v.field,
+                                                                                    np.float32)
+            f.set("data", arr3(fld, L.FLOAT32))
+            f.set("origin", tuple(map(float, v.origin)), L.FLOAT32_VEC3)
+            f.set("spacing", tuple(map(float, v.spacing)), L.FLOAT32_VEC3)
+            f.set("filter", v.filter)
         f.commit()
         vol = dev.new_volume("transferFunction1D")
         vol.set("value", f)
@@ -699,6 +708,30 @@ def instanced_spec(subdiv: int = 8, n_inst: int = 64, n_spheres: int = 1_000_000
                        background=(0.1, 0.1, 0.1, 1.0))
     return SceneSpec([mesh, sph], insts, [LightSpec(direction=(0.2, -1.0, 0.5))], camera=cam,
                      renderer=ren, width=width, height=height, world_id=0)
+
+
+def nanovdb_volume_spec(grid: np.ndarray, width: int = 1920, height: int = 1080,
+                        renderer: str = "raycast", sampling_rate: float = 1.0,
+                        seed: int = 0) -> SceneSpec:
+    """Volume-only scene over a NanoVDB grid buffer (nanovdb.build_grid): the
+    seeded TF of volume_spec, the orbit camera framed on the grid's world
+    bbox."""
+    from .nanovdb import grid_info
+
+    lo, hi = (np.asarray(b, np.float64) for b in grid_info(grid)["world_bbox"])
+    color, op = tf_knots(seed)
+    vol = VolumeSpec(field=None, nvdb=np.asarray(grid, np.uint8), color=color, opacity=op,
+                     value_range=(0.0, 1.0), id=9)
+    center = (lo + hi) / 2
+    R = 1.75 * float((hi - lo).max())
+    pos = orbit_position(tuple(center), R, 30.0, 20.0)
+    _, d, _ = look_at(pos, tuple(center))
+    cam = CameraSpec(position=tuple(pos), direction=tuple(d), fovy=math.radians(40.0),
+                     aspect=width / height)
+    ren = RendererSpec(subtype=renderer, volume_sampling_rate=sampling_rate,
+                       background=(0.0, 0.0, 0.0, 1.0), ambient_samples=0)
+    return SceneSpec([], [InstanceSpec([], zero=True)], [], [vol], camera=cam, renderer=ren,
+                     width=width, height=height)
 
 
 def volume_spec(n: int = 512, n_blobs: int = 64, seed: int = 0, width: int = 1920,
