@@ -534,6 +534,24 @@ def test_nanovdb_golden_grids(device, gtype):
     print(gtype, rep)
 
 
+@pytest.mark.parametrize("gtype", ["float", "fp4", "fpn"])
+def test_nanovdb_brick_cache_matches_walk(device, gtype):
+    """The brick cache (every leaf's values plus a one-voxel apron, filled by
+    the tree walk) gives the same frames as walking the tree per tap, bit
+    for bit ("vrtx.brickCache" false on the field)."""
+    spec = nvdb_volume(gtype, renderer="default")
+    a = render_gpu(device, spec)
+    frame, world, keep = S.build_on_device(device, spec)
+    fields = [o for o in keep if getattr(o, "subtype", "") == "nanovdb"]
+    assert len(fields) == 1
+    fields[0].set("vrtx.brickCache", False)
+    fields[0].commit()
+    frame.render()
+    frame.wait()
+    for ch in ("color", "depth", "primitiveId", "objectId", "instanceId"):
+        assert np.array_equal(a[ch], frame.map("channel." + ch)), ch
+
+
 def test_nanovdb_fp64_rms(device):
     """NanoVDB volume colour against the clean FP64 marcher: RMS <= 1e-3."""
     spec = nvdb_volume("float", sparse=False)

@@ -1236,6 +1236,15 @@ void SpatialField::cleanup()
     cudaFree(refRanges);
   if (gridDev)
     cudaFree(gridDev);
+  if (bricks)
+    cudaFree(bricks);
+  if (brickTable)
+    cudaFree(brickTable);
+  if (blockFill)
+    cudaFree(blockFill);
+  bricks = nullptr;
+  brickTable = nullptr;
+  blockFill = nullptr;
   tex = pointTex = 0;
   cuArray = nullptr;
   ranges = nullptr;
@@ -1252,6 +1261,8 @@ void SpatialField::commit()
     // NvdbRegularField::commitParameters (NvdbRegularField.cpp:63-67)
     filter = getString("filter", "linear");
     data = static_cast<Array *>(getObject("data", VRTX_ARRAY1D));
+    // libvrtx tuning parameter: the brick cache (on by default)
+    useBricks = get<int32_t>("vrtx.brickCache", VRTX_BOOL, 1) != 0;
     if (!data)
       report(VRTX_SEVERITY_WARNING,
           "missing required parameter 'data' on NanoVDB regular spatial field");
@@ -1319,7 +1330,8 @@ float SpatialField::stepSize() const
 // dispatches: float, Fp4, Fp8, Fp16, FpN), and every root tile, internal
 // slot and leaf the tree links to lying inside the buffer on a 32-byte
 // boundary (NanoVDB's alignment), so the device walk never leaves it.
-static bool checkNanovdb(const uint8_t *b, size_t size, std::string &why)
+static bool checkNanovdb(
+    const uint8_t *b, size_t size, std::string &why, std::vector<int32_t> *leafOrigins)
 {
   auto rd64 = [&](size_t o) {
     uint64_t v;
@@ -1378,9 +1390,14 @@ static bool checkNanovdb(const uint8_t *b, size_t size, std::string &why)
       : type == 15u                   ? 96 + 1024
                                       : 0;
   for (uint32_t t = 0; t < tiles; t++) {
+    const uint64_t key = rd64(root + 64 + 32 * t);
     const int64_t child = (int64_t)rd64(root + 64 + 32 * t + 8);
     if (!child)
       continue;
+    // RootData::KeyToCoord: 21 bits per axis, x highest
+    const int32_t ux = int32_t(uint32_t((key >> 42) & 0x1FFFFF) << 12);
+    const int32_t uy = int32_t(uint32_t((key >> 21) & 0x1FFFFF) << 12);
+    const int32_t uz = int32_t(uint32_t(key & 0x1FFFFF) << 12);
     const int64_t up = root + child;
     if (!inside(up, 270400)) {
       why = "upper node outside the buffer";
@@ -1407,6 +1424,11 @@ static bool checkNanovdb(const uint8_t *b, size_t size, std::string &why)
           why = "leaf outside the buffer";
           return false;
         }
+        if (leafOrigins) {
+          leafOrigins->push_back(ux + int32_t(((nu >> 10) & 31u) << 7) + int32_t(((nl >> 8) & 15u) << 3));
+          leafOrigins->push_back(uy + int32_t(((nu >> 5) & 31u) << 7) + int32_t(((nl >> 4) & 15u) << 3));
+          leafOrigins->push_back(uz + int32_t((nu & 31u) << 7) + int32_t((nl & 15u) << 3));
+        }
       }
     }
   }
@@ -1428,7 +1450,8 @@ bool SpatialField::buildNanovdb()
   else
     return false;
   std::string why;
-  if (!checkNanovdb(host.data(), size, why)) {
+  std::vector<int32_t> origins;
+  if (!checkNanovdb(host.data(), size, why, &origins)) {
     report(VRTX_SEVERITY_WARNING, "NanoVDB spatial field: %s", why.c_str());
     return false;
   }
@@ -1479,8 +1502,106 @@ bool SpatialField::buildNanovdb()
     refRanges = nullptr;
     return false;
   }
+  if (useBricks)
+    buildNanovdbBricks(origins);
   launchReferenceGridRangesNanovdb(nvdbGPU, gridBounds, mcDims, refRanges, s);
   return cudaGetLastError() == cudaSuccess;
+}
+
+// The brick cache of a NanoVDB field, a dense table over leaf-block
+// coordinates (the blocks of every leaf plus one block below on each axis,
+// x fastest) whose entries are
+//   slot >= 0  a brick: the block's 8^3 values and the one-voxel apron on
+//              the +x/+y/+z sides, 9^3 floats with x slowest;
+//   -2         a block whose 9^3 region holds one value (in blockFill);
+// every value produced by the device tree walk itself. A stencil then reads
+// one brick (or one value) whatever leaves or tiles it straddles, with the
+// walk's values bit for bit. Leaf blocks get bricks; other blocks are
+// classified on the device and get a brick only where their region is not
+// constant. Skipped (the sampler walks the tree) when the table would exceed
+// 2^26 entries or the bricks do not fit.
+void SpatialField::buildNanovdbBricks(const std::vector<int32_t> &origins)
+{
+  const size_t n = origins.size() / 3;
+  if (!n)
+    return;
+  int32_t lo[3] = {INT32_MAX, INT32_MAX, INT32_MAX}, hi[3] = {INT32_MIN, INT32_MIN, INT32_MIN};
+  for (size_t i = 0; i < n; i++)
+    for (int k = 0; k < 3; k++) {
+      lo[k] = std::min(lo[k], (origins[3 * i + k] >> 3) - 1);
+      hi[k] = std::max(hi[k], origins[3 * i + k] >> 3);
+    }
+  const size_t dims[3] = {size_t(hi[0] - lo[0] + 1), size_t(hi[1] - lo[1] + 1),
+      size_t(hi[2] - lo[2] + 1)};
+  const size_t entries = dims[0] * dims[1] * dims[2];
+  if (entries > (size_t(1) << 26))
+    return;
+  std::vector<int32_t> table(entries, kBlockUnclassified);
+  for (size_t i = 0; i < n; i++) {
+    const size_t bx = size_t((origins[3 * i] >> 3) - lo[0]);
+    const size_t by = size_t((origins[3 * i + 1] >> 3) - lo[1]);
+    const size_t bz = size_t((origins[3 * i + 2] >> 3) - lo[2]);
+    table[(bz * dims[1] + by) * dims[0] + bx] = int32_t(i);
+  }
+  cudaStream_t s = Object::dev->stream;
+  auto fail = [&]() {
+    cudaGetLastError();
+    report(VRTX_SEVERITY_PERFORMANCE_WARNING,
+        "NanoVDB brick cache not built; sampling walks the tree");
+    for (void *p : {(void *)brickTable, (void *)bricks, (void *)blockFill})
+      if (p)
+        cudaFree(p);
+    brickTable = nullptr;
+    bricks = nullptr;
+    blockFill = nullptr;
+  };
+  if (cudaMalloc(&brickTable, entries * sizeof(int32_t)) != cudaSuccess
+      || cudaMalloc(&blockFill, entries * sizeof(float)) != cudaSuccess) {
+    fail();
+    return;
+  }
+  NvdbGPU g = nvdbGPU;
+  for (int k = 0; k < 3; k++) {
+    g.blockLo[k] = lo[k];
+    g.blockDims[k] = (int)dims[k];
+  }
+  // classify the blocks without a leaf: constant region or brick
+  cudaMemcpyAsync(brickTable, table.data(), entries * sizeof(int32_t), cudaMemcpyHostToDevice, s);
+  launchNanovdbClassifyBlocks(g, (uint32_t)entries, brickTable, blockFill, s);
+  cudaMemcpyAsync(table.data(), brickTable, entries * sizeof(int32_t), cudaMemcpyDeviceToHost, s);
+  cudaStreamSynchronize(s);
+  std::vector<int32_t> brickOrigins(origins);
+  for (size_t e = 0; e < entries; e++) {
+    if (table[e] != kBlockNeedsBrick)
+      continue;
+    table[e] = int32_t(brickOrigins.size() / 3);
+    const size_t bx = e % dims[0], by = (e / dims[0]) % dims[1], bz = e / (dims[0] * dims[1]);
+    brickOrigins.push_back((lo[0] + int32_t(bx)) * 8);
+    brickOrigins.push_back((lo[1] + int32_t(by)) * 8);
+    brickOrigins.push_back((lo[2] + int32_t(bz)) * 8);
+  }
+  const size_t slots = brickOrigins.size() / 3;
+  int32_t *dOrigins = nullptr;
+  if (cudaMalloc(&bricks, slots * 729 * sizeof(float)) != cudaSuccess
+      || cudaMalloc(&dOrigins, brickOrigins.size() * sizeof(int32_t)) != cudaSuccess) {
+    if (dOrigins)
+      cudaFree(dOrigins);
+    fail();
+    return;
+  }
+  cudaMemcpyAsync(brickTable, table.data(), entries * sizeof(int32_t), cudaMemcpyHostToDevice, s);
+  cudaMemcpyAsync(dOrigins,
+      brickOrigins.data(),
+      brickOrigins.size() * sizeof(int32_t),
+      cudaMemcpyHostToDevice,
+      s);
+  launchNanovdbBricks(nvdbGPU, dOrigins, (uint32_t)slots, bricks, s);
+  cudaStreamSynchronize(s);
+  cudaFree(dOrigins);
+  g.bricks = bricks;
+  g.brickTable = brickTable;
+  g.blockFill = blockFill;
+  nvdbGPU = g;
 }
 
 bool SpatialField::ensureBuilt()

@@ -255,7 +255,21 @@ struct NvdbGPU
   float background;
   float inv[9];
   float vec[3];
+  // brick cache (null: walk the tree): a dense table over leaf-block
+  // coordinates [blockLo, blockLo + blockDims) (x fastest) giving each
+  // block's brick slot (its 8^3 values and the one-voxel apron on the +
+  // sides, 9^3 floats with x slowest) or kBlockConstant (the whole 9^3
+  // region holds blockFill[block])
+  const float *bricks;
+  const int32_t *brickTable;
+  const float *blockFill;
+  int blockLo[3];
+  int blockDims[3];
 };
+
+constexpr int32_t kBlockConstant = -2;
+constexpr int32_t kBlockUnclassified = -3; // while the cache is built
+constexpr int32_t kBlockNeedsBrick = -4; // while the cache is built
 
 struct VolumeGPU
 {

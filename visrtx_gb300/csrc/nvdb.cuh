@@ -16,7 +16,10 @@
 // The sample is the world -> index map (the float inverse matrix applied
 // through fmaf), floor, the 2x2x2 stencil, and lerps a + w (b - a) over z,
 // y, x (math/SampleFromVoxels.h:200-245), written as the fused multiply-adds
-// the reference's device build contracts them to.
+// the reference's device build contracts them to. The stencil comes from the
+// field's brick cache where one covers it (every leaf's values plus a
+// one-voxel apron, filled by this walk when the field is built), else from
+// the walk itself.
 #pragma once
 
 #include "gpu_types.h"
@@ -65,9 +68,9 @@ __device__ __forceinline__ float leafValue(const uint8_t *leaf, uint32_t type, u
   return fmaf(float(code), ldf(leaf + kLeafQuantum), ldf(leaf + kLeafMin));
 }
 
-// A per-thread read accessor: the last leaf and lower node visited, so the
-// taps of a stencil (and of consecutive samples) inside one leaf cost one
-// load each (NanoVDB's ReadAccessor caches the same levels).
+// A read accessor: the last leaf and lower node visited, so the taps of a
+// stencil inside one leaf cost one load each (NanoVDB's ReadAccessor caches
+// the same levels).
 struct Accessor
 {
   const uint8_t *leaf = nullptr;
@@ -76,11 +79,13 @@ struct Accessor
   int ox = 0, oy = 0, oz = 0; // lower node origin
 };
 
-// RootNode / InternalNode / LeafNode getValue (NanoVDB.h:2947, 3528)
-__device__ __forceinline__ float value(const NvdbGPU &g, Accessor &a, int x, int y, int z)
+// The leaf holding voxel (x, y, z) through the accessor's cache, or nullptr
+// when no leaf covers it: `fill` is then the value of the whole leaf-sized
+// region (a tile value of an internal node or the root, or the background).
+// the walk from the lower-node cache or the root (once per leaf a ray enters)
+__device__ __forceinline__ const uint8_t *walkToLeaf(
+    const NvdbGPU &g, Accessor &a, int x, int y, int z, float &fill)
 {
-  if (a.leaf && (x & ~7) == a.lx && (y & ~7) == a.ly && (z & ~7) == a.lz)
-    return leafValue(a.leaf, g.type, uint32_t((x & 7) << 6 | (y & 7) << 3 | (z & 7)));
   const uint8_t *lower;
   if (a.lower && (x & ~127) == a.ox && (y & ~127) == a.oy && (z & ~127) == a.oz) {
     lower = a.lower;
@@ -95,16 +100,22 @@ __device__ __forceinline__ float value(const NvdbGPU &g, Accessor &a, int x, int
         break;
       }
     }
-    if (!tile)
-      return g.background;
+    if (!tile) {
+      fill = g.background;
+      return nullptr;
+    }
     const int64_t child = (int64_t)ld64(tile + 8);
-    if (!child)
-      return ldf(tile + 20);
+    if (!child) {
+      fill = ldf(tile + 20);
+      return nullptr;
+    }
     const uint8_t *up = g.root + child;
     const uint32_t nu = uint32_t((x & 4095) >> 7) << 10 | uint32_t((y & 4095) >> 7) << 5
         | uint32_t((z & 4095) >> 7);
-    if (!childBit(up + kUpperChildMask, nu))
-      return ldf(up + kUpperTable + 8 * nu);
+    if (!childBit(up + kUpperChildMask, nu)) {
+      fill = ldf(up + kUpperTable + 8 * nu);
+      return nullptr;
+    }
     lower = up + (int64_t)ld64(up + kUpperTable + 8 * nu);
     a.lower = lower;
     a.ox = x & ~127;
@@ -113,14 +124,79 @@ __device__ __forceinline__ float value(const NvdbGPU &g, Accessor &a, int x, int
   }
   const uint32_t nl = uint32_t((x & 127) >> 3) << 8 | uint32_t((y & 127) >> 3) << 4
       | uint32_t((z & 127) >> 3);
-  if (!childBit(lower + kLowerChildMask, nl))
-    return ldf(lower + kLowerTable + 8 * nl);
+  if (!childBit(lower + kLowerChildMask, nl)) {
+    fill = ldf(lower + kLowerTable + 8 * nl);
+    return nullptr;
+  }
   const uint8_t *leaf = lower + (int64_t)ld64(lower + kLowerTable + 8 * nl);
   a.leaf = leaf;
   a.lx = x & ~7;
   a.ly = y & ~7;
   a.lz = z & ~7;
-  return leafValue(leaf, g.type, uint32_t((x & 7) << 6 | (y & 7) << 3 | (z & 7)));
+  return leaf;
+}
+
+__device__ __forceinline__ const uint8_t *leafAt(
+    const NvdbGPU &g, Accessor &a, int x, int y, int z, float &fill)
+{
+  if (a.leaf && (x & ~7) == a.lx && (y & ~7) == a.ly && (z & ~7) == a.lz)
+    return a.leaf;
+  return walkToLeaf(g, a, x, y, z, fill);
+}
+
+// The 2x2x2 stencil at leaf offset n (x, y, z all below 7 within the leaf):
+// offsets n + {0, 1, 8, 9, 64, 65, 72, 73}, decoded with the leaf's
+// minimum and quantum read once.
+__device__ __forceinline__ void leafStencil(
+    const uint8_t *leaf, uint32_t type, uint32_t n, float v[8])
+{
+  const uint32_t off[8] = {0u, 1u, 8u, 9u, 64u, 65u, 72u, 73u};
+  if (type == 1u) {
+    const float *f = reinterpret_cast<const float *>(leaf + kLeafData) + n;
+#pragma unroll
+    for (int c = 0; c < 8; c++)
+      v[c] = __ldg(f + off[c]);
+    return;
+  }
+  const float mn = ldf(leaf + kLeafMin), q = ldf(leaf + kLeafQuantum);
+  uint32_t code[8];
+  if (type == 14u) {
+    const uint8_t *b = leaf + kLeafData + n;
+#pragma unroll
+    for (int c = 0; c < 8; c++)
+      code[c] = __ldg(b + off[c]);
+  } else if (type == 15u) {
+    const unsigned short *h = reinterpret_cast<const unsigned short *>(leaf + kLeafData) + n;
+#pragma unroll
+    for (int c = 0; c < 8; c++)
+      code[c] = __ldg(h + off[c]);
+  } else if (type == 13u) {
+#pragma unroll
+    for (int c = 0; c < 8; c++) {
+      const uint32_t i = n + off[c];
+      code[c] = (__ldg(leaf + kLeafData + (i >> 1)) >> ((i & 1u) << 2)) & 15u;
+    }
+  } else {
+    const uint32_t b = __ldg(leaf + 15) >> 5;
+    const unsigned int *w = reinterpret_cast<const unsigned int *>(leaf + kLeafData);
+    const uint32_t lanes = (32u >> b) - 1u, mask = (1u << (1u << b)) - 1u;
+#pragma unroll
+    for (int c = 0; c < 8; c++) {
+      const uint32_t i = n + off[c];
+      code[c] = (__ldg(w + (i >> (5u - b))) >> ((i & lanes) << b)) & mask;
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < 8; c++)
+    v[c] = fmaf(float(code[c]), q, mn);
+}
+
+// RootNode / InternalNode / LeafNode getValue (NanoVDB.h:2947, 3528)
+__device__ __forceinline__ float value(const NvdbGPU &g, Accessor &a, int x, int y, int z)
+{
+  float fill = 0.f;
+  const uint8_t *leaf = leafAt(g, a, x, y, z, fill);
+  return leaf ? leafValue(leaf, g.type, uint32_t((x & 7) << 6 | (y & 7) << 3 | (z & 7))) : fill;
 }
 
 __device__ __forceinline__ float lerp(float a, float b, float w)
@@ -128,11 +204,67 @@ __device__ __forceinline__ float lerp(float a, float b, float w)
   return fmaf(w, __fsub_rn(b, a), a);
 }
 
+// A stencil that straddles leaf boundaries: each tap through the accessor,
+// in a loop that is not unrolled so the walk is emitted once (about a third
+// of the samples of a march take this path).
+__device__ __forceinline__ float stencilAcrossLeaves(
+    const NvdbGPU &g, Accessor &a, int i, int j, int k, float ux, float uy, float uz)
+{
+  float v[8];
+#pragma unroll 1
+  for (int c = 0; c < 8; c++)
+    v[c] = value(g, a, i + (c >> 2), j + ((c >> 1) & 1), k + (c & 1));
+  // v: (0,0,0) (0,0,1) (0,1,0) (0,1,1) (1,0,0) (1,0,1) (1,1,0) (1,1,1)
+  return lerp(lerp(lerp(v[0], v[1], uz), lerp(v[2], v[3], uz), uy),
+      lerp(lerp(v[4], v[5], uz), lerp(v[6], v[7], uz), uy),
+      ux);
+}
+
+// The stencil at index (i, j, k) by walking the tree (blocks the brick
+// cache does not cover, or fields built without it).
+__device__ __forceinline__ float stencilByWalk(
+    const NvdbGPU &g, Accessor &a, int i, int j, int k, float ux, float uy, float uz)
+{
+  if ((i & 7) != 7 && (j & 7) != 7 && (k & 7) != 7) {
+    // the whole stencil lies in one leaf-sized block: one lookup
+    float fill = 0.f;
+    const uint8_t *leaf = leafAt(g, a, i, j, k, fill);
+    float v[8];
+    if (leaf) {
+      leafStencil(leaf, g.type, uint32_t((i & 7) << 6 | (j & 7) << 3 | (k & 7)), v);
+    } else {
+#pragma unroll
+      for (int c = 0; c < 8; c++)
+        v[c] = fill;
+    }
+    // v: (0,0,0) (0,0,1) (0,1,0) (0,1,1) (1,0,0) (1,0,1) (1,1,0) (1,1,1)
+    return lerp(lerp(lerp(v[0], v[1], uz), lerp(v[2], v[3], uz), uy),
+        lerp(lerp(v[4], v[5], uz), lerp(v[6], v[7], uz), uy),
+        ux);
+  }
+  return stencilAcrossLeaves(g, a, i, j, k, ux, uy, uz);
+}
+
+// The same out of line with its own accessor: with the brick cache the walk
+// is rare (outside the table), and keeping it out of the march leaves the
+// march's registers to the brick path. (Fields too large for the cache walk
+// from the root at every sample.)
+static __device__ __noinline__ float stencilByWalkOutOfLine(
+    const NvdbGPU *g, int i, int j, int k, float ux, float uy, float uz)
+{
+  Accessor a;
+  return stencilByWalk(*g, a, i, j, k, ux, uy, uz);
+}
+
 // The sample at object-space location p. The reference subtracts the float
 // translation from the location in double and rounds to float; for two
 // float operands that equals the float subtraction (one rounding of the
 // exact difference), which is what is computed here.
-__device__ __forceinline__ float sample(const NvdbGPU &g, Accessor &a, f3 p)
+// The sample at object-space location p. The reference subtracts the float
+// translation from the location in double and rounds to float; for two
+// float operands that equals the float subtraction (one rounding of the
+// exact difference), which is what is computed here.
+__device__ __forceinline__ float sample(const NvdbGPU &g, f3 p)
 {
   const float dx = __fsub_rn(p.x, g.vec[0]);
   const float dy = __fsub_rn(p.y, g.vec[1]);
@@ -143,18 +275,26 @@ __device__ __forceinline__ float sample(const NvdbGPU &g, Accessor &a, f3 p)
   const float fx = floorf(ix), fy = floorf(iy), fz = floorf(iz);
   const float ux = __fsub_rn(ix, fx), uy = __fsub_rn(iy, fy), uz = __fsub_rn(iz, fz);
   const int i = int(fx), j = int(fy), k = int(fz);
-  // stencil order of TrilinearSampler::stencil
-  const float v000 = value(g, a, i, j, k);
-  const float v001 = value(g, a, i, j, k + 1);
-  const float v011 = value(g, a, i, j + 1, k + 1);
-  const float v010 = value(g, a, i, j + 1, k);
-  const float v100 = value(g, a, i + 1, j, k);
-  const float v101 = value(g, a, i + 1, j, k + 1);
-  const float v111 = value(g, a, i + 1, j + 1, k + 1);
-  const float v110 = value(g, a, i + 1, j + 1, k);
-  return lerp(lerp(lerp(v000, v001, uz), lerp(v010, v011, uz), uy),
-      lerp(lerp(v100, v101, uz), lerp(v110, v111, uz), uy),
-      ux);
+  if (g.bricks) {
+    // the brick cache: the block's 9^3 values hold the whole stencil
+    const int bx = (i >> 3) - g.blockLo[0], by = (j >> 3) - g.blockLo[1],
+              bz = (k >> 3) - g.blockLo[2];
+    if ((unsigned)bx < (unsigned)g.blockDims[0] && (unsigned)by < (unsigned)g.blockDims[1]
+        && (unsigned)bz < (unsigned)g.blockDims[2]) {
+      const int e = (bz * g.blockDims[1] + by) * g.blockDims[0] + bx;
+      const int slot = __ldg(g.brickTable + e);
+      if (slot >= 0) {
+        const float *b = g.bricks + size_t(slot) * 729 + ((i & 7) * 81 + (j & 7) * 9 + (k & 7));
+        return lerp(lerp(lerp(__ldg(b), __ldg(b + 1), uz), lerp(__ldg(b + 9), __ldg(b + 10), uz), uy),
+            lerp(lerp(__ldg(b + 81), __ldg(b + 82), uz), lerp(__ldg(b + 90), __ldg(b + 91), uz), uy),
+            ux);
+      }
+      // a constant region: every lerp of equal values returns that value
+      if (slot == kBlockConstant)
+        return __ldg(g.blockFill + e);
+    }
+  }
+  return stencilByWalkOutOfLine(&g, i, j, k, ux, uy, uz);
 }
 
 } // namespace nvdb

@@ -223,6 +223,10 @@ struct SpatialField : Object
   using Object::Object;
   bool nanovdb = false; // subtype "nanovdb" (NvdbRegularField.cpp)
   uint8_t *gridDev = nullptr; // device copy of the NanoVDB grid buffer
+  float *bricks = nullptr; // NanoVDB brick cache (9^3 floats per leaf)
+  int32_t *brickTable = nullptr; // block -> brick slot, or -2: constant
+  float *blockFill = nullptr; // the value of constant blocks
+  bool useBricks = true; // "vrtx.brickCache"
   NvdbGPU nvdbGPU{};
   box3 gridBounds{{0.f, 0.f, 0.f}, {1.f, 1.f, 1.f}};
   f3 gridVoxel{1.f, 1.f, 1.f};
@@ -243,6 +247,7 @@ struct SpatialField : Object
   void cleanup();
   bool ensureBuilt();
   bool buildNanovdb();
+  void buildNanovdbBricks(const std::vector<int32_t> &leafOrigins);
   box3 bounds() const;
   float stepSize() const;
 };

@@ -117,6 +117,15 @@ cudaError_t launchReferenceGridRanges(cudaTextureObject_t field,
     const int mcDims[3],
     float *ranges,
     cudaStream_t s);
+// the brick cache of a NanoVDB field: 9^3 values per leaf (origins: 3 ints
+// per leaf) evaluated by the device tree walk
+cudaError_t launchNanovdbBricks(
+    const NvdbGPU &grid, const int32_t *origins, uint32_t leaves, float *bricks, cudaStream_t s);
+// classifies the unclassified blocks of a NanoVDB brick table: kBlockConstant
+// (fill written) where the block's 9^3 region holds one value, else
+// kBlockNeedsBrick
+cudaError_t launchNanovdbClassifyBlocks(
+    const NvdbGPU &grid, uint32_t entries, int32_t *table, float *fill, cudaStream_t s);
 // the same grid over a NanoVDB field
 cudaError_t launchReferenceGridRangesNanovdb(
     const NvdbGPU &grid, box3 bounds, const int mcDims[3], float *ranges, cudaStream_t s);

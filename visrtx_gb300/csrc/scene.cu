@@ -404,8 +404,7 @@ struct RefNanovdbTap
   NvdbGPU grid;
   __device__ __forceinline__ float operator()(f3 p) const
   {
-    nvdb::Accessor a;
-    return nvdb::sample(grid, a, p);
+    return nvdb::sample(grid, p);
   }
 };
 
@@ -503,6 +502,84 @@ cudaError_t launchReferenceGridRanges(cudaTextureObject_t field,
       mcDims[1],
       mcDims[2],
       ranges);
+  return cudaGetLastError();
+}
+
+namespace {
+
+// one block per leaf, 729 threads: the 9^3 padded brick through the tree
+// walk (the brick cache reads are then the walk's values)
+__global__ void __launch_bounds__(729) k_nanovdbBricks(
+    NvdbGPU grid, const int32_t *origins, uint32_t leaves, float *bricks)
+{
+  const uint32_t leaf = blockIdx.x;
+  if (leaf >= leaves)
+    return;
+  const int t = threadIdx.x; // dx * 81 + dy * 9 + dz
+  const int dx = t / 81, dy = (t / 9) % 9, dz = t % 9;
+  grid.bricks = nullptr; // evaluate through the tree
+  nvdb::Accessor a;
+  bricks[size_t(leaf) * 729 + t] = nvdb::value(grid,
+      a,
+      origins[3 * leaf] + dx,
+      origins[3 * leaf + 1] + dy,
+      origins[3 * leaf + 2] + dz);
+}
+
+// one 256-thread block per table entry still unclassified: is the block's
+// 9^3 region one value (compared bitwise)?
+__global__ void __launch_bounds__(256) k_nanovdbClassifyBlocks(
+    NvdbGPU grid, uint32_t entries, int32_t *table, float *fill)
+{
+  const uint32_t e = blockIdx.x;
+  if (e >= entries || table[e] != kBlockUnclassified)
+    return;
+  const int bx = int(e % uint32_t(grid.blockDims[0]));
+  const int by = int((e / uint32_t(grid.blockDims[0])) % uint32_t(grid.blockDims[1]));
+  const int bz = int(e / (uint32_t(grid.blockDims[0]) * uint32_t(grid.blockDims[1])));
+  const int ox = (grid.blockLo[0] + bx) * 8, oy = (grid.blockLo[1] + by) * 8,
+            oz = (grid.blockLo[2] + bz) * 8;
+  grid.bricks = nullptr; // evaluate through the tree
+  __shared__ int varies;
+  __shared__ float first;
+  nvdb::Accessor a;
+  if (threadIdx.x == 0) {
+    first = nvdb::value(grid, a, ox, oy, oz);
+    // a lerp of equal values returns the value itself only when it is
+    // finite and not -0 (fmaf(w, 0, -0) is +0): other regions keep a brick
+    varies = (!isfinite(first) || __float_as_uint(first) == 0x80000000u) ? 1 : 0;
+  }
+  __syncthreads();
+  const uint32_t ref = __float_as_uint(first);
+  for (int t = threadIdx.x; t < 729; t += blockDim.x) {
+    const float v = nvdb::value(grid, a, ox + t / 81, oy + (t / 9) % 9, oz + t % 9);
+    if (__float_as_uint(v) != ref)
+      varies = 1;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    table[e] = varies ? kBlockNeedsBrick : kBlockConstant;
+    fill[e] = first;
+  }
+}
+
+} // namespace
+
+cudaError_t launchNanovdbClassifyBlocks(
+    const NvdbGPU &grid, uint32_t entries, int32_t *table, float *fill, cudaStream_t s)
+{
+  if (!entries)
+    return cudaSuccess;
+  k_nanovdbClassifyBlocks<<<entries, 256, 0, s>>>(grid, entries, table, fill);
+  return cudaGetLastError();
+}
+
+cudaError_t launchNanovdbBricks(
+    const NvdbGPU &grid, const int32_t *origins, uint32_t leaves, float *bricks, cudaStream_t s)
+{
+  if (!leaves)
+    return cudaSuccess;
+  k_nanovdbBricks<<<leaves, 729, 0, s>>>(grid, origins, leaves, bricks);
   return cudaGetLastError();
 }
 

@@ -99,10 +99,9 @@ struct TextureField
 
 struct NanovdbField
 {
-  nvdb::Accessor acc;
   __device__ __forceinline__ float operator()(const VolumeGPU &v, f3 p)
   {
-    return nvdb::sample(v.nvdb, acc, p);
+    return nvdb::sample(v.nvdb, p);
   }
 };
 
