@@ -385,9 +385,22 @@ struct InstBVH
   std::vector<Prim> prims;
 };
 
+// HDRI::finalize / generateCDFTables (scene/light/HDRI.cu:98-170,218-319):
+// luminance weighted by the row's sin(theta), row sums, marginal and
+// conditional inclusive scans (in order), normalised by their last entries,
+// pdf weight total / (2 pi^2 W H), and the rotation rows (right, forward, up)
+struct HdriPre
+{
+  std::vector<float> marginal, conditional;
+  float pdfWeight = 0.f;
+  float rot[9];
+};
+
 struct SceneCtx
 {
   const OrcScene *sc;
+  std::vector<HdriPre> hdri; // per light (filled for hdri lights)
+  int hdriIndex = -1; // the first hdri light
   std::vector<InstBVH> unique; // one per distinct surface range
   std::vector<const InstBVH *> bvh; // per instance
   std::vector<X34> w2o, o2w;
@@ -2157,12 +2170,25 @@ struct Matte
 {
   V3 base;
   float opacity;
+  int type; // 0 matte, 1 physicallyBased
+  float metallic, roughness, ior;
 };
 
+// the material's init callable (MatteShader_ptx.cu:38-49,
+// PhysicallyBasedShader_ptx.cu:41-58)
 Matte matteAt(const SceneCtx &S, const SHit &sh)
 {
   const OrcSurface &s = S.sc->surfaces[sh.surface];
   Matte m;
+  m.type = s.materialType;
+  m.ior = s.ior;
+  m.metallic = m.roughness = 0.f;
+  if (s.materialType == 1) {
+    m.metallic = materialParam(S, sh, s.metallicSrc, {s.metallic, 0.f, 0.f, 1.f},
+        &s.metallicSampler).x;
+    m.roughness = materialParam(S, sh, s.roughnessSrc, {s.roughness, 0.f, 0.f, 1.f},
+        &s.roughnessSampler).x;
+  }
   float op;
   if (s.colorSrc == 0 && s.opacitySrc == 0) {
     m.base = ld3(s.color, 0);
@@ -2179,50 +2205,280 @@ Matte matteAt(const SceneCtx &S, const SHit &sh)
   return m;
 }
 
-// shadeSurface (renderer/DirectLight_ptx.cu:73-224), matte material
-// (shaders/MatteShader_ptx.cu:38-80), directional/point lights
-// (gpu/sampleLight.h:60-90)
+// --- lights (gpu/sampleLight.h) and material evaluation ------------------
+
+struct LightSample
+{
+  V3 radiance, dir;
+  float dist, pdf;
+};
+
+// the HDRI texture: float4 texels (rgb, 1), linear filtering with 8-bit
+// weights, normalised coordinates, x repeat, y clamp (HDRI.cu:121-122)
+V3 hdriTexel(const OrcLight &L, float u, float v)
+{
+  const int W = L.hdriW, H = L.hdriH;
+  const float cu = u - std::floor(u); // repeat
+  const float xs = cu * (float)W - 0.5f, ys = v * (float)H - 0.5f;
+  const float fx = std::floor(xs), fy = std::floor(ys);
+  const float a = quantW(xs - fx, 1), b = quantW(ys - fy, 1);
+  auto wrapX = [&](int i) {
+    i %= W;
+    return i < 0 ? i + W : i;
+  };
+  auto clampY = [&](int j) { return std::min(std::max(j, 0), H - 1); };
+  const int x0 = wrapX((int)fx), x1 = wrapX((int)fx + 1);
+  const int y0 = clampY((int)fy), y1 = clampY((int)fy + 1);
+  float out[3];
+  for (int c = 0; c < 3; c++) {
+    auto at = [&](int x, int y) { return L.hdri[3 * ((size_t)y * W + x) + c]; };
+    const float r0 = (1.f - a) * at(x0, y0) + a * at(x1, y0);
+    const float r1 = (1.f - a) * at(x0, y1) + a * at(x1, y1);
+    out[c] = (1.f - b) * r0 + b * r1;
+  }
+  return v3(out[0], out[1], out[2]);
+}
+
+// sampleHDRI(ld, rayDir) (gpu_util.h:275-288)
+V3 hdriRadiance(const SceneCtx &S, int li, V3 dir)
+{
+  const OrcLight &L = S.sc->lights[li];
+  const float *R = S.hdri[li].rot;
+  const V3 d = v3(std::fma(R[2], dir.z, std::fma(R[1], dir.y, R[0] * dir.x)),
+      std::fma(R[5], dir.z, std::fma(R[4], dir.y, R[3] * dir.x)),
+      std::fma(R[8], dir.z, std::fma(R[7], dir.y, R[6] * dir.x)));
+  const float theta = std::acos(std::min(std::max(d.z, -1.f), 1.f));
+  const float pp = std::atan2(d.y, d.x);
+  const float phi = pp < 0.f ? pp + 2.f * (float)M_PI : pp;
+  return hdriTexel(L, phi * (1.f / (2.f * (float)M_PI)), theta * (1.f / (float)M_PI));
+}
+
+// getBackground (gpu_util.h:298-307): a visible HDRI light, else the colour
+V4 backgroundOf(const Ctx &C, V3 dir)
+{
+  const SceneCtx &S = *C.S;
+  if (S.hdriIndex >= 0 && S.sc->lights[S.hdriIndex].hdriVisible) {
+    const V3 r = hdriRadiance(S, S.hdriIndex, dir);
+    return {r.x, r.y, r.z, 1.f};
+  }
+  return {C.R->background[0], C.R->background[1], C.R->background[2], C.R->background[3]};
+}
+
+// cub::LowerBound: the first entry not below u
+int lowerBound(const float *cdf, int n, float u)
+{
+  int lo = 0, count = n;
+  while (count > 0) {
+    const int half = count >> 1;
+    if (cdf[lo + half] < u) {
+      lo += half + 1;
+      count -= half + 1;
+    } else {
+      count = half;
+    }
+  }
+  return lo;
+}
+
+// sampleHDRILight (sampleLight.h:110-149)
+LightSample sampleHDRILight(const SceneCtx &S, int li, Stream &rs)
+{
+  const OrcLight &L = S.sc->lights[li];
+  const HdriPre &hp = S.hdri[li];
+  const int W = L.hdriW, H = L.hdriH;
+  const int y = lowerBound(hp.marginal.data(), H, uniform(rs));
+  const int x = lowerBound(hp.conditional.data() + (size_t)std::min(y, H - 1) * W, W, uniform(rs));
+  const float u = std::min(std::max(((float)x + 0.5f) / (float)W, 0.f), 1.f);
+  const float v = std::min(std::max(((float)y + 0.5f) / (float)H, 0.f), 1.f);
+  const float theta = (float)M_PI * v, phi = (float)M_PI * (2.f * u);
+  const V3 rad = hdriTexel(L, u, v);
+  LightSample ls;
+  ls.pdf = (rad.x * 0.2126f + rad.y * 0.7152f + rad.z * 0.0722f) * hp.pdfWeight;
+  const float st = std::sin(theta);
+  const V3 sd = v3(st * std::cos(phi), st * std::sin(phi), std::cos(theta));
+  const float *R = hp.rot;
+  ls.dir = v3(std::fma(sd.z, R[6], std::fma(sd.y, R[3], sd.x * R[0])),
+      std::fma(sd.z, R[7], std::fma(sd.y, R[4], sd.x * R[1])),
+      std::fma(sd.z, R[8], std::fma(sd.y, R[5], sd.x * R[2])));
+  ls.dist = 1e20f;
+  ls.radiance = rad * L.hdriScale;
+  return ls;
+}
+
+// sampleLight (sampleLight.h:60-173); lights are given in world space
+LightSample sampleLight(const SceneCtx &S, int li, V3 hitP, Stream &rs)
+{
+  const OrcLight &L = S.sc->lights[li];
+  LightSample ls;
+  ls.pdf = 1.f;
+  if (L.type == 0) {
+    ls.dir = -1.f * normalize(ld3(L.direction, 0));
+    ls.dist = INFINITY;
+    ls.radiance = ld3(L.radiance, 0);
+  } else if (L.type == 1) {
+    const V3 d = ld3(L.position, 0) - hitP;
+    ls.dist = std::sqrt(dot(d, d));
+    ls.dir = normalize(d);
+    ls.radiance = ld3(L.radiance, 0);
+  } else if (L.type == 2) {
+    // the distance is taken of the normalised direction (sampleLight.h:87-88)
+    ls.dir = normalize(ld3(L.position, 0) - hitP);
+    ls.dist = std::sqrt(dot(ls.dir, ls.dir));
+    float spot = dot(normalize(ld3(L.direction, 0)), -1.f * ls.dir);
+    if (spot < L.cosOuter)
+      spot = 0.f;
+    else if (spot > L.cosInner)
+      spot = 1.f;
+    else {
+      spot = (spot - L.cosOuter) / (L.cosInner - L.cosOuter);
+      spot = spot * spot * (3.f - 2.f * spot);
+    }
+    ls.radiance = ld3(L.radiance, 0) * spot;
+  } else {
+    ls = sampleHDRILight(S, li, rs);
+  }
+  return ls;
+}
+
+inline float heavisideF(float x)
+{
+  return x < 0.f ? 0.f : 1.f;
+}
+
+// shadeSurface (MatteShader_ptx.cu:72-80, PhysicallyBasedShader_ptx.cu:98-149)
+V3 shadeMaterial(const Matte &m, V3 Ns, const LightSample &ls, V3 outgoing)
+{
+  if (m.type != 1) {
+    const float NdotL = std::max(0.f, dot(Ns, ls.dir));
+    return m.base * (float)M_1_PI * NdotL * ls.radiance / ls.pdf;
+  }
+  const V3 H = normalize(ls.dir + outgoing);
+  const float NdotH = dot(Ns, H), NdotL = dot(Ns, ls.dir), NdotV = dot(Ns, outgoing);
+  const float VdotH = dot(outgoing, H), LdotH = dot(ls.dir, H);
+  const float q = (1.f - m.ior) / (1.f + m.ior);
+  const float f0s = q * q;
+  const V3 f0 = v3(f0s, f0s, f0s) * (1.f - m.metallic) + m.base * m.metallic;
+  const float e = 1.f - std::fabs(VdotH);
+  const float fw = e * e * e * e * e;
+  const V3 F = f0 + (v3(1.f, 1.f, 1.f) - f0) * fw;
+  const V3 diffuseColor = m.base * (1.f - m.metallic) + v3(0.f, 0.f, 0.f) * m.metallic;
+  const V3 diffuseBRDF =
+      (v3(1.f, 1.f, 1.f) - F) * (float)M_1_PI * diffuseColor * std::max(0.f, NdotL);
+  const float alpha = (m.roughness * m.roughness) * m.opacity;
+  const float a2 = alpha * alpha;
+  const float dd = NdotH * NdotH * (a2 - 1.f) + 1.f;
+  const float D = (a2 * heavisideF(NdotH)) / ((float)M_PI * (dd * dd));
+  const float G = ((2.f * std::fabs(NdotL) * heavisideF(LdotH))
+                      / (std::fabs(NdotL) + std::sqrt(a2 + (1.f - a2) * NdotL * NdotL)))
+      * ((2.f * std::fabs(NdotV) * heavisideF(VdotH))
+          / (std::fabs(NdotV) + std::sqrt(a2 + (1.f - a2) * NdotV * NdotV)));
+  const float denom = 4.f * std::fabs(NdotV) * std::fabs(NdotL);
+  const V3 spec = denom != 0.f ? (F * D * G) / denom : v3(0.f, 0.f, 0.f);
+  return (diffuseBRDF + spec) * ls.radiance / ls.pdf;
+}
+
+V3 onbMul(V3 n, V3 s);
+
+// nextRay (MatteShader_ptx.cu:51-57: none; PhysicallyBasedShader_ptx.cu:
+// 60-84 with uniformSampleCone gpu_math.h:299-312)
+bool nextRay(const Matte &m, V3 Ns, V3 rayDir, Stream &rs, V3 &dir, V3 &weight)
+{
+  if (m.type != 1) {
+    dir = v3(0.f, 0.f, 0.f);
+    weight = v3(0.f, 0.f, 0.f);
+    return false;
+  }
+  const V3 refl = rayDir - 2.f * dot(rayDir, Ns) * Ns;
+  const float cosThetaMax = 1.f - m.roughness * m.roughness;
+  const float s0 = uniform(rs), s1 = uniform(rs), s2 = uniform(rs);
+  const float phi = (float)(2.0 * M_PI * (double)s0);
+  const float cosTheta = (1.f - s1) + s1 * cosThetaMax;
+  const float sinTheta = std::sqrt(1.f - cosTheta * cosTheta);
+  const float d = std::pow(s2, 1.f / 3.f);
+  const V3 cone = v3(d * sinTheta * std::cos(phi), d * sinTheta * std::sin(phi), d * cosTheta);
+  dir = onbMul(normalize(refl), cone);
+  weight = m.base * m.metallic;
+  return true;
+}
+
+// shadeSurface (renderer/DirectLight_ptx.cu:73-224): ambient, every light
+// (sampleLight.h:60-173) with surface and volume attenuation, AO, then the
+// bounce rays of the material's nextRay up to maxRayDepth
 void shadeDL(Ctx &C, const VolCtx &VC, Stream &rs, const Ray &ray, const SHit &hit,
     float out[4])
 {
   const OrcRenderer &R = *C.R;
-  const OrcSurface &s = C.S->sc->surfaces[hit.surface];
-  const V3 shadePoint = hit.P + (hit.eps * hit.Ns);
+  const SceneCtx &S = *C.S;
+  V3 shadePoint = hit.P + (hit.eps * hit.Ns);
   const float aoFactor = R.ambientSamples > 0
       ? computeAO(C, rs, hit, R.occlusionDistance, R.ambientSamples)
       : 1.f;
   V3 contrib = v3(0, 0, 0);
-  const Matte mt = matteAt(*C.S, hit);
-  const V3 base = mt.base;
+  Matte mt = matteAt(S, hit);
   const float opacity = mt.opacity;
   if (R.ambientRadiance > 0.f)
-    contrib = ld3(R.ambientColor, 0) * R.ambientRadiance * base;
-  for (int l = 0; l < C.S->sc->numLights; l++) {
-    const OrcLight &L = C.S->sc->lights[l];
-    V3 ldir, rad;
-    float dist;
-    if (L.type == 0) {
-      ldir = -normalize(ld3(L.direction, 0));
-      dist = INFINITY;
-      rad = ld3(L.radiance, 0);
-    } else {
-      const V3 dd = ld3(L.position, 0) - hit.P;
-      dist = std::sqrt(dot(dd, dd));
-      ldir = dd / dist;
-      rad = ld3(L.radiance, 0) * (1.f / (dist * dist));
-    }
-    const float so = 1.f - surfaceAttenuation(C, shadePoint, ldir, 0.f, dist);
+    contrib = ld3(R.ambientColor, 0) * R.ambientRadiance * mt.base;
+  const float invRate = 1.f / std::min(std::max(R.volumeSamplingRate, 1e-3f), 10.f);
+  for (int l = 0; l < S.sc->numLights; l++) {
+    const LightSample ls = sampleLight(S, l, hit.P, rs);
+    if (ls.pdf == 0.f)
+      continue;
+    const float so = 1.f - surfaceAttenuation(C, shadePoint, ls.dir, 0.f, ls.dist);
     const float vo = 1.f
-        - volumeAttenuation(C, VC, rs, shadePoint, ldir, 0.f, dist,
-            1.f / std::min(std::max(R.volumeSamplingRate, 1e-3f), 10.f));
+        - volumeAttenuation(C, VC, rs, shadePoint, ls.dir, 0.f, ls.dist, invRate);
     const float att = so * vo;
-    const float NdotL = std::max(0.f, dot(hit.Ns, ldir));
-    const V3 tl = base * (float)M_1_PI * NdotL * rad / 1.f;
+    const V3 tl = shadeMaterial(mt, hit.Ns, ls, -1.f * ray.dir);
     if (std::isnan(tl.x) || std::isnan(tl.y) || std::isnan(tl.z))
       continue;
     contrib = contrib + tl * att;
   }
   contrib = contrib * aoFactor;
+  V3 weight = v3(1.f, 1.f, 1.f);
+  V3 bounceDir = ray.dir, Ns = hit.Ns;
+  for (int depth = 0; depth < R.maxRayDepth; depth++) {
+    V3 nd, nw;
+    nextRay(mt, Ns, bounceDir, rs, nd, nw);
+    if (!(std::fabs(nd.x) > 1.0e-8f && std::fabs(nd.y) > 1.0e-8f && std::fabs(nd.z) > 1.0e-8f))
+      break;
+    weight = weight * nw;
+    if (weight.x < 1.0e-12f && weight.y < 1.0e-12f && weight.z < 1.0e-12f)
+      break;
+    Ray br;
+    br.org = shadePoint;
+    br.dir = normalize(nd);
+    br.tmin = 0.f;
+    br.tmax = 3.402823466e+38f;
+    HitRec h;
+    float unused;
+    C.rays++;
+    const bool found = trace<0>(S, br.org, br.dir, br.tmin, br.tmax,
+        R.cullTriangleBackfaces != 0, true, h, unused);
+    bounceDir = br.dir;
+    if (found) {
+      const SHit bh = populate(S, br, h);
+      shadePoint = bh.P + (bh.eps * bh.Ns);
+      LightSample ls;
+      if (S.hdriIndex >= 0 && S.sc->lights[S.hdriIndex].hdriVisible) {
+        ls = sampleHDRILight(S, S.hdriIndex, rs);
+      } else {
+        const V4 bg = backgroundOf(C, br.dir);
+        ls.radiance = v3(bg.x, bg.y, bg.z);
+        ls.dir = br.dir;
+        ls.dist = 1.f;
+        ls.pdf = 1.f;
+      }
+      mt = matteAt(S, bh);
+      Ns = bh.Ns;
+      const V3 c = shadeMaterial(mt, bh.Ns, ls, -1.f * br.dir);
+      if (std::isnan(c.x) || std::isnan(c.y) || std::isnan(c.z))
+        break;
+      contrib = contrib + c * weight;
+    } else {
+      const V4 bg = backgroundOf(C, br.dir);
+      contrib = contrib + v3(bg.x, bg.y, bg.z) * weight;
+      break;
+    }
+  }
   out[0] = contrib.x;
   out[1] = contrib.y;
   out[2] = contrib.z;
@@ -2330,8 +2586,9 @@ Sample integrate(Ctx &C, const VolCtx &VC, const CamPre &cam, Stream &rs, int px
         inst = vi;
       }
       color = color * opacity;
-      color = color + v3(R.background[0], R.background[1], R.background[2]) * (1.f - opacity);
-      opacity += R.background[3] * (1.f - opacity);
+      const V4 bg = backgroundOf(C, ray.dir);
+      color = color + v3(bg.x, bg.y, bg.z) * (1.f - opacity);
+      opacity += bg.w * (1.f - opacity);
       outC = outC + color * (1.f - outO);
       outO += opacity * (1.f - outO);
       break;
@@ -2425,7 +2682,8 @@ Sample integrateDPT(Ctx &C, const VolCtx &VC, const CamPre &cam, Stream &rs, int
 {
   const OrcRenderer &R = *C.R;
   Ray ray = primaryRay(cam, rs, px, py, invW, invH, false);
-  const V3 bg = v3(R.background[0], R.background[1], R.background[2]);
+  const V4 bg4 = backgroundOf(C, ray.dir);
+  const V3 bg = v3(bg4.x, bg4.y, bg4.z);
   // outColor (the background) and the primary ray direction go to the
   // albedo and normal channels
   Sample out{bg, 1.f, ray.tmax, ~0u, ~0u, ~0u, bg, ray.dir};
@@ -2636,6 +2894,57 @@ void *orc_prepare(const OrcScene *scene)
     if (which[i] < 0) {
       which[i] = (int)ranges.size();
       ranges.push_back(r);
+    }
+  }
+  // hdri lights: CDF tables and rotation (HDRI.cu), the first is the world's
+  S.hdri.resize(scene->numLights);
+  for (int li = 0; li < scene->numLights; li++) {
+    const OrcLight &L = scene->lights[li];
+    if (L.type != 3 || !L.hdri || L.hdriW < 1 || L.hdriH < 1)
+      continue;
+    if (S.hdriIndex < 0)
+      S.hdriIndex = li;
+    HdriPre &hp = S.hdri[li];
+    const int W = L.hdriW, H = L.hdriH;
+    std::vector<float> lum((size_t)W * H), rowSums(H);
+    for (int y = 0; y < H; y++) {
+      const float sinTheta = std::sin((float)M_PI * ((float)y + 0.5f) / (float)H);
+      for (int x = 0; x < W; x++) {
+        const float *c = L.hdri + 3 * ((size_t)y * W + x);
+        lum[(size_t)y * W + x] = sinTheta * (c[0] * 0.2126f + c[1] * 0.7152f + c[2] * 0.0722f);
+      }
+      float sum = 0.f;
+      for (int x = 0; x < W; x++)
+        sum += lum[(size_t)y * W + x];
+      rowSums[y] = sum;
+    }
+    hp.marginal.resize(H);
+    hp.conditional.resize((size_t)W * H);
+    float acc = 0.f;
+    for (int y = 0; y < H; y++)
+      hp.marginal[y] = acc += rowSums[y];
+    for (int y = 0; y < H; y++) {
+      float r = 0.f;
+      for (int x = 0; x < W; x++)
+        hp.conditional[(size_t)y * W + x] = r += lum[(size_t)y * W + x];
+    }
+    const float total = hp.marginal[H - 1];
+    hp.pdfWeight = total / (2.0f * (float)M_PI * (float)M_PI * (float)W * (float)H);
+    for (int y = 0; y < H; y++)
+      hp.marginal[y] = hp.marginal[y] / total;
+    for (int y = 0; y < H; y++) {
+      const float rt = hp.conditional[(size_t)y * W + W - 1];
+      for (int x = 0; x < W; x++)
+        hp.conditional[(size_t)y * W + x] = hp.conditional[(size_t)y * W + x] / rt;
+    }
+    const V3 up = -1.f * normalize(ld3(L.hdriUp, 0));
+    const V3 forward = -1.f * normalize(cross(up, ld3(L.hdriDirection, 0)));
+    const V3 right = normalize(cross(forward, up));
+    const V3 rows[3] = {right, forward, up};
+    for (int r = 0; r < 3; r++) {
+      hp.rot[3 * r] = rows[r].x;
+      hp.rot[3 * r + 1] = rows[r].y;
+      hp.rot[3 * r + 2] = rows[r].z;
     }
   }
   S.unique.resize(ranges.size());

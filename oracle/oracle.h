@@ -120,6 +120,11 @@ typedef struct OrcSurface {
   int colorSrc, opacitySrc; /* 10: the sampler below */
   float colorW; /* w of the colour value */
   OrcSampler colorSampler, opacitySampler;
+  /* 0 matte, 1 physicallyBased (color = baseColor) */
+  int materialType;
+  float metallic, roughness, ior;
+  int metallicSrc, roughnessSrc;
+  OrcSampler metallicSampler, roughnessSampler;
 } OrcSurface;
 
 typedef struct OrcInstance {
@@ -130,10 +135,18 @@ typedef struct OrcInstance {
 } OrcInstance;
 
 typedef struct OrcLight {
-  int type; /* 0 directional, 1 point */
-  float direction[3]; /* world-space direction of travel */
+  int type; /* 0 directional, 1 point, 2 spot, 3 hdri */
+  float direction[3]; /* directional: direction of travel; spot: its axis */
   float position[3];
-  float radiance[3];
+  float radiance[3]; /* color * irradiance / intensity */
+  float cosOuter, cosInner; /* spot */
+  /* hdri: W x H float RGB radiance (x fastest), direction, up, scale,
+   * visibility */
+  const float *hdri;
+  int hdriW, hdriH;
+  float hdriDirection[3], hdriUp[3];
+  float hdriScale;
+  int hdriVisible;
 } OrcLight;
 
 typedef struct OrcVolume {
@@ -188,6 +201,7 @@ typedef struct OrcRenderer {
   int pixelSamples;
   int ambientSamples;
   int maxDepth;
+  int maxRayDepth; /* bounce rays of the default renderer */
 } OrcRenderer;
 
 typedef struct OrcFrame {

@@ -48,13 +48,17 @@ class OrcSurface(C.Structure):
                 ("alphaMode", C.c_int), ("cutoff", C.c_float), ("caps", C.c_int),
                 ("vattr", OrcAttr * 5), ("pattr", OrcAttr * 5), ("uattr", (C.c_float * 4) * 5),
                 ("colorSrc", C.c_int), ("opacitySrc", C.c_int), ("colorW", C.c_float),
-                ("colorSampler", OrcSampler), ("opacitySampler", OrcSampler)]
+                ("colorSampler", OrcSampler), ("opacitySampler", OrcSampler),
+                ("materialType", C.c_int), ("metallic", C.c_float), ("roughness", C.c_float),
+                ("ior", C.c_float), ("metallicSrc", C.c_int), ("roughnessSrc", C.c_int),
+                ("metallicSampler", OrcSampler), ("roughnessSampler", OrcSampler)]
 
 
 _ATTR_SLOTS = ("attribute0", "attribute1", "attribute2", "attribute3", "color")
 _PARAM_SOURCES = {"attribute0": 1, "attribute1": 2, "attribute2": 3, "attribute3": 4, "color": 5,
                   "worldPosition": 6, "worldNormal": 7, "objectPosition": 8, "objectNormal": 9}
 _ATTR_CHANNELS = {240: 1, 241: 2, 242: 3, 243: 4, 221: 1, 223: 1, 260: 4, 261: 4}
+_LIGHT_TYPES = {"directional": 0, "point": 1, "spot": 2, "hdri": 3}
 _SAMPLER_TYPES = {"image1D": 1, "image2D": 2, "image3D": 3, "transform": 4, "primitive": 5}
 _WRAP = {"clampToEdge": 0, "repeat": 1, "mirrorRepeat": 2}
 _SAMPLER_SLOTS = {"attribute0": 0, "attribute1": 1, "attribute2": 2, "attribute3": 3, "color": 4}
@@ -113,7 +117,10 @@ class OrcInstance(C.Structure):
 
 class OrcLight(C.Structure):
     _fields_ = [("type", C.c_int), ("direction", C.c_float * 3), ("position", C.c_float * 3),
-                ("radiance", C.c_float * 3)]
+                ("radiance", C.c_float * 3), ("cosOuter", C.c_float), ("cosInner", C.c_float),
+                ("hdri", C.c_void_p), ("hdriW", C.c_int), ("hdriH", C.c_int),
+                ("hdriDirection", C.c_float * 3), ("hdriUp", C.c_float * 3),
+                ("hdriScale", C.c_float), ("hdriVisible", C.c_int)]
 
 
 class OrcVolume(C.Structure):
@@ -142,7 +149,8 @@ class OrcRenderer(C.Structure):
     _fields_ = [("type", C.c_int), ("background", C.c_float * 4), ("ambientColor", C.c_float * 3),
                 ("ambientRadiance", C.c_float), ("occlusionDistance", C.c_float),
                 ("cullTriangleBackfaces", C.c_int), ("volumeSamplingRate", C.c_float),
-                ("pixelSamples", C.c_int), ("ambientSamples", C.c_int), ("maxDepth", C.c_int)]
+                ("pixelSamples", C.c_int), ("ambientSamples", C.c_int), ("maxDepth", C.c_int),
+                ("maxRayDepth", C.c_int)]
 
 
 class OrcFrame(C.Structure):
@@ -277,6 +285,19 @@ def _scene_structs(spec):
             o.opacity = 1.0
         else:
             o.opacity = s.opacity
+        o.materialType = 1 if s.material == "physicallyBased" else 0
+        o.ior = float(s.ior)
+        for name in ("metallic", "roughness"):
+            val = getattr(s, name)
+            if isinstance(val, SamplerSpec):
+                setattr(o, name + "Src", 10)
+                _pack_sampler(getattr(o, name + "Sampler"), val, keep)
+                setattr(o, name, 1.0)
+            elif isinstance(val, str):
+                setattr(o, name + "Src", _PARAM_SOURCES[val])
+                setattr(o, name, 1.0)
+            else:
+                setattr(o, name, float(val))
         from visrtx_gb300.scenes import attr_type
         for k, slot in enumerate(_ATTR_SLOTS):
             o.uattr[k] = (C.c_float * 4)(0.0, 0.0, 0.0, 1.0)
@@ -309,11 +330,26 @@ def _scene_structs(spec):
     inst_arr = (OrcInstance * max(1, len(insts)))(*insts)
     lights = (OrcLight * max(1, len(spec.lights)))()
     for i, l in enumerate(spec.lights):
-        lights[i].type = 0 if l.type == "directional" else 1
-        lights[i].direction = (C.c_float * 3)(*map(float, l.direction))
-        lights[i].position = (C.c_float * 3)(*map(float, l.position))
-        rad = [float(np.float32(c) * np.float32(l.irradiance)) for c in l.color]
-        lights[i].radiance = (C.c_float * 3)(*rad)
+        o = lights[i]
+        o.type = _LIGHT_TYPES[l.type]
+        o.direction = (C.c_float * 3)(*map(float, l.direction))
+        o.position = (C.c_float * 3)(*map(float, l.position))
+        level = np.float32(max(0.0, l.irradiance))
+        rad = [float(np.float32(c) * level) for c in l.color]
+        o.radiance = (C.c_float * 3)(*rad)
+        if l.type == "spot":
+            inner = np.float32(l.opening_angle) - np.float32(2.0) * np.float32(l.falloff_angle)
+            o.cosOuter = float(np.cos(np.float32(l.opening_angle)))
+            o.cosInner = float(np.cos(inner))
+        if l.type == "hdri":
+            img = np.ascontiguousarray(l.radiance, np.float32)
+            keep.append(img)
+            o.hdri = _ptr(img)
+            o.hdriH, o.hdriW = img.shape[0], img.shape[1]
+            o.hdriDirection = (C.c_float * 3)(*map(float, l.hdri_direction))
+            o.hdriUp = (C.c_float * 3)(*map(float, l.hdri_up))
+            o.hdriScale = float(l.scale)
+            o.hdriVisible = int(bool(l.visible))
     vols = (OrcVolume * max(1, len(spec.volumes)))()
     for i, v in enumerate(spec.volumes):
         _pack_volume(v, vols[i], keep, spec.world_id)
@@ -410,6 +446,7 @@ def _render_prepared(lib, handle, spec, frame_id, rows, volume_mode, tex_round, 
     ren.pixelSamples = 1 if r.checkerboard else r.pixel_samples
     ren.ambientSamples = r.ambient_samples if ren.type in (0, 2) else 0
     ren.maxDepth = r.max_depth
+    ren.maxRayDepth = r.max_ray_depth
     W, H = spec.width, spec.height
     out = {
         "accum": np.zeros((H, W, 4), np.float32) if accum is None else accum,

@@ -729,23 +729,18 @@ GeometryGPU Geometry::gpuData()
 // Material (Matte.cpp:39-53) and Light (Directional.cpp:38-55, Light.cpp)
 // ---------------------------------------------------------------------------
 
+// Matte::commitParameters (Matte.cpp:39-53) and PBR::commitParameters
+// (PBR.cpp:39-62): each parameter a value, a sampler or a string naming an
+// attribute / hit quantity (populateMaterialParameter, Material.cpp)
 void Material::commit()
 {
-  if (subtype != "matte")
+  const bool pbr = subtype == "physicallyBased";
+  if (subtype != "matte" && !pbr)
     report(VRTX_SEVERITY_WARNING,
         "material subtype '%s' is evaluated as matte",
         subtype.c_str());
-  float c[4] = {0.8f, 0.8f, 0.8f, 1.f};
-  if (has("color", VRTX_FLOAT32_VEC4))
-    std::memcpy(c, params["color"].bytes.data(), 16);
-  else if (has("color", VRTX_FLOAT32_VEC3))
-    std::memcpy(c, params["color"].bytes.data(), 12);
-  gpu.color = f3{c[0], c[1], c[2]};
-  gpu.colorValue = make_float4(c[0], c[1], c[2], c[3]);
-  gpu.opacityValue = get<float>("opacity", VRTX_FLOAT32, 1.f);
-  gpu.opacity = c[3] * gpu.opacityValue;
-  // a string names an attribute or a hit quantity (populateMaterialParameter,
-  // Material.cpp)
+  gpu = MaterialGPU{};
+  gpu.type = pbr ? MATERIAL_PBR : MATERIAL_MATTE;
   auto source = [&](const char *name) -> uint32_t {
     if (!has(name, VRTX_STRING))
       return PARAM_VALUE;
@@ -774,14 +769,33 @@ void Material::commit()
         name);
     return PARAM_VALUE;
   };
-  gpu.colorSrc = source("color");
-  gpu.opacitySrc = source("opacity");
-  colorSampler = static_cast<Sampler *>(getObject("color", VRTX_SAMPLER));
-  opacitySampler = static_cast<Sampler *>(getObject("opacity", VRTX_SAMPLER));
-  if (colorSampler)
-    gpu.colorSrc = PARAM_SAMPLER;
-  if (opacitySampler)
-    gpu.opacitySrc = PARAM_SAMPLER;
+  const char *colorName = pbr ? "baseColor" : "color";
+  float c[4] = {0.8f, 0.8f, 0.8f, 1.f};
+  if (has(colorName, VRTX_FLOAT32_VEC4))
+    std::memcpy(c, params[colorName].bytes.data(), 16);
+  else if (has(colorName, VRTX_FLOAT32_VEC3))
+    std::memcpy(c, params[colorName].bytes.data(), 12);
+  gpu.color = f3{c[0], c[1], c[2]};
+  const float op = get<float>("opacity", VRTX_FLOAT32, 1.f);
+  gpu.opacity = c[3] * op;
+  const char *names[MP_COUNT] = {colorName, "opacity", "metallic", "roughness"};
+  const float4 values[MP_COUNT] = {make_float4(c[0], c[1], c[2], c[3]),
+      make_float4(op, 0.f, 0.f, 1.f),
+      make_float4(get<float>("metallic", VRTX_FLOAT32, 1.f), 0.f, 0.f, 1.f),
+      make_float4(get<float>("roughness", VRTX_FLOAT32, 1.f), 0.f, 0.f, 1.f)};
+  const int slots = pbr ? MP_COUNT : 2;
+  for (int k = 0; k < MP_COUNT; k++) {
+    samplers[k] = nullptr;
+    gpu.params[k].value = values[k];
+    gpu.params[k].src = PARAM_VALUE;
+    if (k >= slots)
+      continue;
+    gpu.params[k].src = source(names[k]);
+    samplers[k] = static_cast<Sampler *>(getObject(names[k], VRTX_SAMPLER));
+    if (samplers[k])
+      gpu.params[k].src = PARAM_SAMPLER;
+  }
+  gpu.ior = get<float>("ior", VRTX_FLOAT32, 1.5f);
   gpu.cutoff = get<float>("alphaCutoff", VRTX_FLOAT32, 0.5f);
   const std::string mode = getString("alphaMode", "opaque");
   gpu.alphaMode = mode == "blend" ? ALPHA_BLEND
@@ -791,7 +805,7 @@ void Material::commit()
 uint64_t Material::deepStamp() const
 {
   uint64_t s = commitStamp;
-  for (const Sampler *sm : {colorSampler, opacitySampler})
+  for (const Sampler *sm : samplers)
     if (sm)
       s = std::max(s, sm->deepStamp());
   return s;
@@ -1009,13 +1023,69 @@ SamplerGPU Sampler::gpuData() const
   return g;
 }
 
+Light::~Light()
+{
+  cleanup();
+}
+
+void Light::cleanup()
+{
+  if (gpu.hdriTex)
+    cudaDestroyTextureObject(gpu.hdriTex);
+  if (cuArray)
+    cudaFreeArray(cuArray);
+  if (cdfs)
+    cudaFree(cdfs);
+  gpu.hdriTex = 0;
+  gpu.marginalCDF = gpu.conditionalCDF = nullptr;
+  cuArray = nullptr;
+  cdfs = nullptr;
+  builtStamp = 0;
+}
+
+// Light::commitParameters and the subtypes (Directional.cpp:38-55,
+// Point.cpp:38-55, Spot.cpp:38-70, HDRI.cu:92-131)
 void Light::commit()
 {
   const f3 color = get<f3>("color", VRTX_FLOAT32_VEC3, f3{1.f, 1.f, 1.f});
+  auto intensity = [&]() {
+    const float power = get<float>("power", VRTX_FLOAT32, 1.f);
+    return std::min(std::max(get<float>("intensity", VRTX_FLOAT32, power), 0.f),
+        3.402823466e+38f);
+  };
+  const LightGPU old = gpu;
+  gpu = LightGPU{};
+  gpu.hdriTex = old.hdriTex;
+  gpu.marginalCDF = old.marginalCDF;
+  gpu.conditionalCDF = old.conditionalCDF;
+  radiance = nullptr;
+  builtStamp = 0;
   if (subtype == "point") {
     gpu.type = LIGHT_POINT;
     gpu.position = get<f3>("position", VRTX_FLOAT32_VEC3, f3{0.f, 0.f, 0.f});
-    gpu.radiance = color * std::max(0.f, get<float>("intensity", VRTX_FLOAT32, 1.f));
+    gpu.radiance = color * intensity();
+  } else if (subtype == "spot") {
+    gpu.type = LIGHT_SPOT;
+    gpu.position = get<f3>("position", VRTX_FLOAT32_VEC3, f3{0.f, 0.f, 0.f});
+    gpu.spotDir = normalize(get<f3>("direction", VRTX_FLOAT32_VEC3, f3{0.f, 0.f, -1.f}));
+    const float opening = get<float>("openingAngle", VRTX_FLOAT32, float(M_PI));
+    const float falloff = get<float>("falloffAngle", VRTX_FLOAT32, 0.1f);
+    const float inner = opening - 2.f * falloff;
+    if (inner < 0.f)
+      report(VRTX_SEVERITY_WARNING, "falloffAngle should be smaller than half of openingAngle");
+    gpu.cosOuter = std::cos(opening);
+    gpu.cosInner = std::cos(inner);
+    gpu.radiance = color * intensity();
+  } else if (subtype == "hdri") {
+    gpu.type = LIGHT_HDRI;
+    radiance = static_cast<Array *>(getObject("radiance", VRTX_ARRAY2D));
+    if (!radiance)
+      report(VRTX_SEVERITY_WARNING, "missing required parameter 'radiance' on HDRI light");
+    hdriDirection = get<f3>("direction", VRTX_FLOAT32_VEC3, f3{1.f, 0.f, 0.f});
+    hdriUp = get<f3>("up", VRTX_FLOAT32_VEC3, f3{0.f, 0.f, 1.f});
+    gpu.hdriScale = get<float>("scale", VRTX_FLOAT32, 1.f);
+    gpu.visible = get<int32_t>("visible", VRTX_BOOL, 1) != 0 ? 1u : 0u;
+    gpu.radiance = color;
   } else {
     if (subtype != "directional")
       report(VRTX_SEVERITY_WARNING,
@@ -1029,6 +1099,126 @@ void Light::commit()
     gpu.dirToLight = -d; // transformed per instance at world build
     gpu.radiance = color * irr;
   }
+}
+
+bool Light::isValid() const
+{
+  if (gpu.type != LIGHT_HDRI)
+    return true;
+  return radiance && radiance->elemType == VRTX_FLOAT32_VEC3;
+}
+
+uint64_t Light::deepStamp() const
+{
+  return std::max(commitStamp, radiance ? radiance->deepStamp() : 0);
+}
+
+// HDRI::finalize / gpuData / generateCDFTables (HDRI.cu:98-170, 218-319):
+// the radiance as a float4 texture (linear, x repeat, y clamp); luminance
+// weighted by sin(theta) of each row; row sums; marginal and per-row
+// conditional inclusive scans, normalised by their last entries; the pdf
+// weight total / (2 pi^2 W H); the rotation rows (right, forward, up). The
+// scans run here in order (the reference's device scans associate
+// differently; the tables differ only by rounding).
+bool Light::ensureBuilt()
+{
+  if (gpu.type != LIGHT_HDRI)
+    return true;
+  if (!isValid()) {
+    if (radiance)
+      report(VRTX_SEVERITY_WARNING, "HDRI radiance must be a FLOAT32_VEC3 Array2D");
+    return false;
+  }
+  const uint64_t want = deepStamp();
+  if (builtStamp && builtStamp >= want)
+    return true;
+  cleanup();
+  const int W = (int)radiance->n[0], H = (int)radiance->n[1];
+  if (W < 1 || H < 1)
+    return false;
+  std::vector<float> rgb((size_t)W * H * 3);
+  if (const void *h = radiance->hostData())
+    std::memcpy(rgb.data(), h, rgb.size() * sizeof(float));
+  else
+    cudaMemcpy(rgb.data(), radiance->deviceData(), rgb.size() * sizeof(float),
+        cudaMemcpyDeviceToHost);
+  std::vector<float> lum((size_t)W * H), rowSums(H), cdf((size_t)H + (size_t)W * H);
+  for (int y = 0; y < H; y++) {
+    const float sinTheta = std::sin(float(M_PI) * (float(y) + 0.5f) / float(H));
+    for (int x = 0; x < W; x++) {
+      const float *p = &rgb[3 * ((size_t)y * W + x)];
+      lum[(size_t)y * W + x] = sinTheta * (p[0] * 0.2126f + p[1] * 0.7152f + p[2] * 0.0722f);
+    }
+    float sum = 0.f;
+    for (int x = 0; x < W; x++)
+      sum += lum[(size_t)y * W + x];
+    rowSums[y] = sum;
+  }
+  float *marginal = cdf.data(), *conditional = cdf.data() + H;
+  float acc = 0.f;
+  for (int y = 0; y < H; y++)
+    marginal[y] = acc += rowSums[y];
+  for (int y = 0; y < H; y++) {
+    float r = 0.f;
+    for (int x = 0; x < W; x++)
+      conditional[(size_t)y * W + x] = r += lum[(size_t)y * W + x];
+  }
+  const float total = marginal[H - 1];
+  gpu.pdfWeight = total / (2.0f * float(M_PI) * float(M_PI) * float(W) * float(H));
+  for (int y = 0; y < H; y++)
+    marginal[y] = marginal[y] / total;
+  for (int y = 0; y < H; y++) {
+    const float rowTotal = conditional[(size_t)y * W + W - 1];
+    for (int x = 0; x < W; x++)
+      conditional[(size_t)y * W + x] = conditional[(size_t)y * W + x] / rowTotal;
+  }
+  if (cudaMalloc(&cdfs, cdf.size() * sizeof(float)) != cudaSuccess) {
+    cudaGetLastError();
+    cdfs = nullptr;
+    return false;
+  }
+  cudaMemcpy(cdfs, cdf.data(), cdf.size() * sizeof(float), cudaMemcpyHostToDevice);
+  std::vector<float> rgba((size_t)W * H * 4);
+  for (size_t i = 0; i < (size_t)W * H; i++) {
+    rgba[4 * i] = rgb[3 * i];
+    rgba[4 * i + 1] = rgb[3 * i + 1];
+    rgba[4 * i + 2] = rgb[3 * i + 2];
+    rgba[4 * i + 3] = 1.f;
+  }
+  cudaChannelFormatDesc desc = cudaCreateChannelDesc(32, 32, 32, 32, cudaChannelFormatKindFloat);
+  if (cudaMallocArray(&cuArray, &desc, W, H) != cudaSuccess) {
+    cudaGetLastError();
+    cuArray = nullptr;
+    return false;
+  }
+  cudaMemcpy2DToArray(cuArray, 0, 0, rgba.data(), W * 16, W * 16, H, cudaMemcpyHostToDevice);
+  cudaResourceDesc rd{};
+  rd.resType = cudaResourceTypeArray;
+  rd.res.array.array = cuArray;
+  cudaTextureDesc td{};
+  td.addressMode[0] = cudaAddressModeWrap;
+  td.addressMode[1] = cudaAddressModeClamp;
+  td.filterMode = cudaFilterModeLinear;
+  td.readMode = cudaReadModeElementType;
+  td.normalizedCoords = 1;
+  cudaCreateTextureObject(&gpu.hdriTex, &rd, &td, nullptr);
+  gpu.marginalCDF = cdfs;
+  gpu.conditionalCDF = cdfs + H;
+  gpu.hdriW = (uint32_t)W;
+  gpu.hdriH = (uint32_t)H;
+  // up = -normalize(up); forward = -normalize(cross(up, direction));
+  // right = normalize(cross(forward, up)); rows (right, forward, up)
+  const f3 up = -normalize(hdriUp);
+  const f3 forward = -normalize(cross(up, hdriDirection));
+  const f3 right = normalize(cross(forward, up));
+  const f3 rows[3] = {right, forward, up};
+  for (int r = 0; r < 3; r++) {
+    gpu.hdriRot[3 * r] = rows[r].x;
+    gpu.hdriRot[3 * r + 1] = rows[r].y;
+    gpu.hdriRot[3 * r + 2] = rows[r].z;
+  }
+  builtStamp = want;
+  return cudaGetLastError() == cudaSuccess;
 }
 
 // ---------------------------------------------------------------------------
@@ -2120,15 +2310,12 @@ bool World::rebuild()
   bool allOpaque = true;
   for (Material *m : mats) {
     MaterialGPU mg = m->gpu;
-    if (mg.colorSrc == PARAM_SAMPLER) {
-      mg.colorSampler = samplerSlot(m->colorSampler);
-      if (mg.colorSampler == ~0u)
-        mg.colorSrc = PARAM_VALUE;
-    }
-    if (mg.opacitySrc == PARAM_SAMPLER) {
-      mg.opacitySampler = samplerSlot(m->opacitySampler);
-      if (mg.opacitySampler == ~0u)
-        mg.opacitySrc = PARAM_VALUE;
+    for (int k = 0; k < MP_COUNT; k++) {
+      if (mg.params[k].src != PARAM_SAMPLER)
+        continue;
+      mg.params[k].sampler = samplerSlot(m->samplers[k]);
+      if (mg.params[k].sampler == ~0u)
+        mg.params[k].src = PARAM_VALUE;
     }
     hMats.push_back(mg);
     if (m->gpu.alphaMode != ALPHA_OPAQUE)
@@ -2234,6 +2421,7 @@ bool World::rebuild()
   std::vector<InstanceRecord> recs;
   std::vector<box3> recBoxes;
   std::vector<LightGPU> lights;
+  int hdriIndex = -1;
   std::vector<VolumeGPU> vols;
   worldBounds = emptyBox();
   for (Instance *inst : insts) {
@@ -2259,8 +2447,15 @@ bool World::rebuild()
         extend(worldBounds, wb);
       }
       for (Light *l : gl) {
+        if (!l->ensureBuilt())
+          continue;
         LightGPU lg = l->gpu;
-        if (lg.type == LIGHT_DIRECTIONAL)
+        if (lg.type == LIGHT_HDRI) {
+          // the first HDRI light is the world's (World.cpp:466-480); its
+          // instance transform is not applied (sampleLight.h:110-149)
+          if (hdriIndex < 0)
+            hdriIndex = (int)lights.size();
+        } else if (lg.type == LIGHT_DIRECTIONAL)
           lg.dirToLight = f3{m[0] * l->gpu.dirToLight.x + m[1] * l->gpu.dirToLight.y
                   + m[2] * l->gpu.dirToLight.z,
               m[4] * l->gpu.dirToLight.x + m[5] * l->gpu.dirToLight.y
@@ -2352,6 +2547,7 @@ bool World::rebuild()
   gpu.samplers = dSamplers;
   gpu.lights = uploadVec(this, lights, s);
   gpu.numLights = (uint32_t)lights.size();
+  gpu.hdri = hdriIndex;
   gpu.volumes = uploadVec(this, vols, s);
   gpu.numVolumes = (uint32_t)vols.size();
   gpu.allOpaque = allOpaque ? 1u : 0u;

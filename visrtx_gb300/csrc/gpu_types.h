@@ -124,19 +124,43 @@ struct SamplerGPU
   uint32_t pad;
 };
 
+enum MaterialType : uint32_t
+{
+  MATERIAL_MATTE = 0, // "matte" (Matte.cpp, shaders/MatteShader_ptx.cu)
+  MATERIAL_PBR = 1 // "physicallyBased" (PBR.cpp, PhysicallyBasedShader_ptx.cu)
+};
+
+// material parameter slots: matte reads color and opacity, physicallyBased
+// all four ("baseColor" in the color slot)
+enum MaterialParamSlot : int
+{
+  MP_COLOR = 0,
+  MP_OPACITY = 1,
+  MP_METALLIC = 2,
+  MP_ROUGHNESS = 3,
+  MP_COUNT = 4
+};
+
+// one material parameter (MaterialParameter, gpu_objects.h): its value, the
+// ParamSource that supplies it and, for PARAM_SAMPLER, the index into
+// WorldGPU::samplers
+struct MaterialParamGPU
+{
+  float4 value;
+  uint32_t src;
+  uint32_t sampler;
+  uint32_t pad[2];
+};
+
 struct MaterialGPU
 {
-  f3 color; // matte "color" value (default 0.8 grey, Matte.cpp:44)
-  float opacity; // color.w * opacity of the values, before the alpha mode
+  uint32_t type; // MaterialType
   int alphaMode;
   float cutoff;
-  uint32_t colorSrc; // ParamSource of "color"
-  uint32_t opacitySrc; // ParamSource of "opacity"
-  float4 colorValue; // the "color" value with its w
-  float opacityValue; // the "opacity" value
-  uint32_t colorSampler; // index into WorldGPU::samplers (PARAM_SAMPLER)
-  uint32_t opacitySampler;
-  uint32_t pad;
+  float ior; // physicallyBased "ior" (1.5)
+  f3 color; // the color value's rgb (default 0.8 grey, Matte.cpp:44)
+  float opacity; // color.w * opacity of the values, before the alpha mode
+  MaterialParamGPU params[MP_COUNT];
 };
 
 struct SurfaceGPU
@@ -150,15 +174,30 @@ struct SurfaceGPU
 enum LightType : int
 {
   LIGHT_DIRECTIONAL = 0,
-  LIGHT_POINT = 1
+  LIGHT_POINT = 1,
+  LIGHT_SPOT = 2,
+  LIGHT_HDRI = 3
 };
 
 struct LightGPU
 {
   int type;
   f3 dirToLight; // directional: xfmVec(xfm, -direction) (sampleLight.h:60-70)
-  f3 radiance; // color * irradiance (or intensity for point)
-  f3 position; // point light
+  f3 radiance; // color * irradiance (directional) or * intensity (point, spot)
+  f3 position; // point, spot (instance-transformed)
+  f3 spotDir; // spot: normalize(direction), not instance-transformed
+  float cosOuter, cosInner; // spot: cos(openingAngle), cos(opening - 2 falloff)
+  // hdri (HDRI.cu): radiance texture (linear, x repeat, y clamp), the
+  // normalised marginal (H) and conditional (H x W) CDFs, the rotation whose
+  // rows are (right, forward, up), scale, pdf weight, visibility
+  cudaTextureObject_t hdriTex;
+  const float *marginalCDF;
+  const float *conditionalCDF;
+  uint32_t hdriW, hdriH;
+  float hdriRot[9];
+  float hdriScale;
+  float pdfWeight;
+  uint32_t visible;
 };
 
 // ---------------------------------------------------------------------------
@@ -387,7 +426,7 @@ struct WorldGPU
   uint32_t hasSegments; // some BLAS holds cylinders, cones or curves
   const SamplerGPU *samplers; // the materials' samplers
   uint32_t hasNanovdb; // some volume samples a NanoVDB field
-  uint32_t pad0;
+  int hdri; // index into lights of the world's HDRI light, -1: none
 };
 
 // Per-thread work counters. Rays and volume samples are counted by every

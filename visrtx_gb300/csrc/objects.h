@@ -195,7 +195,7 @@ struct Material : Object
 {
   using Object::Object;
   MaterialGPU gpu{};
-  Sampler *colorSampler = nullptr, *opacitySampler = nullptr;
+  Sampler *samplers[MP_COUNT] = {nullptr, nullptr, nullptr, nullptr};
   void commit() override;
   uint64_t deepStamp() const override;
 };
@@ -204,7 +204,18 @@ struct Light : Object
 {
   using Object::Object;
   LightGPU gpu{};
+  // hdri (HDRI.cu): the radiance image, its texture and CDF tables
+  Array *radiance = nullptr;
+  f3 hdriDirection{1.f, 0.f, 0.f}, hdriUp{0.f, 0.f, 1.f};
+  cudaArray_t cuArray = nullptr;
+  float *cdfs = nullptr; // marginal (H) then conditional (H x W)
+  uint64_t builtStamp = 0;
+  ~Light() override;
   void commit() override;
+  bool isValid() const override;
+  uint64_t deepStamp() const override;
+  void cleanup();
+  bool ensureBuilt();
 };
 
 struct Surface : Object

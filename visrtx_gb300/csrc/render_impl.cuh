@@ -243,10 +243,13 @@ __device__ __forceinline__ uint32_t geometryPrimId(
   return g.primIds ? g.primIds[sh.primID] : sh.primID;
 }
 
+// The shading state of a hit (MatteShadingState / PhysicallyBasedShadingState)
 struct MatteState
 {
   f3 baseColor;
   float opacity;
+  uint32_t type; // MaterialType
+  float metallic, roughness, ior; // physicallyBased
 };
 
 // --- geometry attributes and material parameters ---------------------------
@@ -458,31 +461,262 @@ __device__ __forceinline__ float4 materialParam(const WorldGPU &w,
   }
 }
 
-// Matte init (MatteShader_ptx.cu:38-49): colour and opacity parameters,
-// opacity = adjustedMaterialOpacity(color.w * opacity.x)
+__device__ __forceinline__ float4 materialParamSlot(
+    const WorldGPU &w, const SurfaceHit &sh, const MaterialGPU &m, int slot)
+{
+  const MaterialParamGPU &p = m.params[slot];
+  return materialParam(w, sh, p.src, p.value, p.sampler);
+}
+
+// The material's init callable (MatteShader_ptx.cu:38-49,
+// PhysicallyBasedShader_ptx.cu:41-58): colour and opacity parameters,
+// opacity = adjustedMaterialOpacity(color.w * opacity.x); physicallyBased
+// also reads metallic, roughness and ior.
 __device__ __forceinline__ MatteState matteInit(const WorldGPU &w, const SurfaceHit &sh)
 {
   const MaterialGPU &m = w.materials[w.surfaces[sh.surface].material];
   MatteState s;
   float op;
-  if (m.colorSrc == PARAM_VALUE && m.opacitySrc == PARAM_VALUE) {
+  if (m.params[MP_COLOR].src == PARAM_VALUE && m.params[MP_OPACITY].src == PARAM_VALUE) {
     s.baseColor = m.color;
     op = m.opacity;
   } else {
-    const float4 c = materialParam(w, sh, m.colorSrc, m.colorValue, m.colorSampler);
-    const float o = materialParam(w,
-        sh,
-        m.opacitySrc,
-        make_float4(m.opacityValue, 0.f, 0.f, 1.f),
-        m.opacitySampler)
-                        .x;
+    const float4 c = materialParamSlot(w, sh, m, MP_COLOR);
+    const float o = materialParamSlot(w, sh, m, MP_OPACITY).x;
     s.baseColor = mk3(c.x, c.y, c.z);
     op = c.w * o;
   }
   s.opacity = m.alphaMode == ALPHA_OPAQUE
       ? 1.f
       : (m.alphaMode == ALPHA_BLEND ? op : (op < m.cutoff ? 0.f : 1.f));
+  s.type = m.type;
+  s.metallic = s.roughness = 0.f;
+  s.ior = m.ior;
+  if (m.type == MATERIAL_PBR) {
+    s.metallic = materialParamSlot(w, sh, m, MP_METALLIC).x;
+    s.roughness = materialParamSlot(w, sh, m, MP_ROUGHNESS).x;
+  }
   return s;
+}
+
+// --- lights (gpu/sampleLight.h) ---------------------------------------------
+
+struct LightSample
+{
+  f3 radiance;
+  f3 dir;
+  float dist;
+  float pdf;
+};
+
+// glm::normalize: v * (1 / sqrt(dot(v, v)))
+__device__ __forceinline__ f3 glmNormalize(f3 v)
+{
+  return v * (1.f / sqrtf(dot(v, v)));
+}
+
+// the HDRI radiance texture at uv (sampleHDRI, gpu_util.h:270-273)
+__device__ __forceinline__ f3 hdriAt(const LightGPU &L, float u, float v)
+{
+  const float4 t = tex2D<float4>(L.hdriTex, u, v);
+  return mk3(t.x, t.y, t.z);
+}
+
+// sampleHDRI(ld, rayDir) (gpu_util.h:275-288): the direction through the
+// light's rotation, then spherical coordinates as texture coordinates
+__device__ __forceinline__ f3 hdriRadiance(const LightGPU &L, f3 dir)
+{
+  const float *R = L.hdriRot;
+  const f3 d = mk3(fmaf(R[2], dir.z, fmaf(R[1], dir.y, R[0] * dir.x)),
+      fmaf(R[5], dir.z, fmaf(R[4], dir.y, R[3] * dir.x)),
+      fmaf(R[8], dir.z, fmaf(R[7], dir.y, R[6] * dir.x)));
+  // sphericalCoordsFromDirection (gpu_math.h:254-261)
+  const float theta = acosf(fminf(fmaxf(d.z, -1.f), 1.f));
+  const float p = atan2f(d.y, d.x);
+  const float phi = p < 0.f ? p + 2.f * float(M_PI) : p;
+  const float u = phi * (1.f / (2.f * float(M_PI)));
+  const float v = theta * (1.f / float(M_PI));
+  return hdriAt(L, u, v);
+}
+
+// getBackground (gpu_util.h:298-307): a visible HDRI, else the colour
+__device__ __forceinline__ float4 backgroundOf(const FrameParams &P, f3 dir)
+{
+  const WorldGPU &w = P.world;
+  if (w.hdri >= 0 && w.lights[w.hdri].visible) {
+    const f3 r = hdriRadiance(w.lights[w.hdri], dir);
+    return make_float4(r.x, r.y, r.z, 1.f);
+  }
+  return P.renderer.background;
+}
+
+// inverseSampleCDF (sampleLight.h:105-108): the first entry not below u
+// (cub::LowerBound)
+__device__ __forceinline__ int lowerBound(const float *cdf, int n, float u)
+{
+  int lo = 0, count = n;
+  while (count > 0) {
+    const int half = count >> 1;
+    if (__ldg(cdf + lo + half) < u) {
+      lo += half + 1;
+      count -= half + 1;
+    } else {
+      count = half;
+    }
+  }
+  return lo;
+}
+
+// sampleHDRILight (sampleLight.h:110-149)
+__device__ __forceinline__ LightSample sampleHDRILight(const LightGPU &L, RandState &rs)
+{
+  const int W = (int)L.hdriW, H = (int)L.hdriH;
+  const int y = lowerBound(L.marginalCDF, H, curand_uniform(&rs));
+  // (a row index past the table only follows from a NaN CDF; clamped so
+  // nothing reads outside it)
+  const int x = lowerBound(L.conditionalCDF + (size_t)min(y, H - 1) * W, W, curand_uniform(&rs));
+  const float u = fminf(fmaxf((float(x) + 0.5f) / float(W), 0.f), 1.f);
+  const float v = fminf(fmaxf((float(y) + 0.5f) / float(H), 0.f), 1.f);
+  const float theta = float(M_PI) * v, phi = float(M_PI) * (2.f * u);
+  const f3 radiance = hdriAt(L, u, v);
+  LightSample ls;
+  ls.pdf = (radiance.x * 0.2126f + radiance.y * 0.7152f + radiance.z * 0.0722f) * L.pdfWeight;
+  // sphericalCoordsToDirection, then row vector times the rotation
+  const float sinTheta = sinf(theta);
+  const f3 sd = mk3(sinTheta * cosf(phi), sinTheta * sinf(phi), cosf(theta));
+  const float *R = L.hdriRot;
+  ls.dir = mk3(fmaf(sd.z, R[6], fmaf(sd.y, R[3], sd.x * R[0])),
+      fmaf(sd.z, R[7], fmaf(sd.y, R[4], sd.x * R[1])),
+      fmaf(sd.z, R[8], fmaf(sd.y, R[5], sd.x * R[2])));
+  ls.dist = 1e20f;
+  ls.radiance = radiance * L.hdriScale;
+  return ls;
+}
+
+// sampleLight (sampleLight.h:60-173) for a world-space hit point
+__device__ __forceinline__ LightSample sampleLight(const LightGPU &L, f3 hitpoint, RandState &rs)
+{
+  LightSample ls;
+  ls.pdf = 1.f;
+  if (L.type == LIGHT_DIRECTIONAL) {
+    ls.dir = L.dirToLight;
+    ls.dist = __int_as_float(0x7f800000); // +inf
+    ls.radiance = L.radiance;
+  } else if (L.type == LIGHT_POINT) {
+    const f3 d = L.position - hitpoint;
+    ls.dist = sqrtf(dot(d, d));
+    ls.dir = glmNormalize(d);
+    ls.radiance = L.radiance;
+  } else if (L.type == LIGHT_SPOT) {
+    // the distance is taken of the normalised direction (sampleLight.h:87-88)
+    ls.dir = glmNormalize(L.position - hitpoint);
+    ls.dist = sqrtf(dot(ls.dir, ls.dir));
+    float spot = dot(L.spotDir, -ls.dir);
+    if (spot < L.cosOuter)
+      spot = 0.f;
+    else if (spot > L.cosInner)
+      spot = 1.f;
+    else {
+      spot = (spot - L.cosOuter) / (L.cosInner - L.cosOuter);
+      spot = spot * spot * (3.f - 2.f * spot);
+    }
+    ls.radiance = L.radiance * spot;
+  } else {
+    ls = sampleHDRILight(L, rs);
+  }
+  return ls;
+}
+
+// --- material evaluation (MatteShader_ptx.cu, PhysicallyBasedShader_ptx.cu)
+
+__device__ __forceinline__ float pow2f(float f)
+{
+  return f * f;
+}
+
+__device__ __forceinline__ float pow5f(float f)
+{
+  return f * f * f * f * f;
+}
+
+__device__ __forceinline__ float heavisidef(float x)
+{
+  return x < 0.f ? 0.f : 1.f;
+}
+
+// shadeSurface: matte Lambert, or the physicallyBased Fresnel-Schlick +
+// GGX + Smith model (PhysicallyBasedShader_ptx.cu:98-149)
+__device__ __forceinline__ f3 shadeMaterial(
+    const MatteState &s, f3 Ns, const LightSample &ls, f3 outgoing)
+{
+  if (s.type != MATERIAL_PBR) {
+    const float NdotL = fmaxf(0.f, dot(Ns, ls.dir));
+    return s.baseColor * float(M_1_PI) * NdotL * ls.radiance / ls.pdf;
+  }
+  const f3 H = glmNormalize(ls.dir + outgoing);
+  const float NdotH = dot(Ns, H);
+  const float NdotL = dot(Ns, ls.dir);
+  const float NdotV = dot(Ns, outgoing);
+  const float VdotH = dot(outgoing, H);
+  const float LdotH = dot(ls.dir, H);
+  const float f0s = pow2f((1.f - s.ior) / (1.f + s.ior));
+  // glm::mix(a, b, t) = a * (1 - t) + b * t
+  const f3 f0 = mk3(f0s, f0s, f0s) * (1.f - s.metallic) + s.baseColor * s.metallic;
+  const float fw = pow5f(1.f - fabsf(VdotH));
+  const f3 F = f0 + (mk3(1.f, 1.f, 1.f) - f0) * fw;
+  const f3 diffuseColor = s.baseColor * (1.f - s.metallic) + mk3(0.f, 0.f, 0.f) * s.metallic;
+  const f3 diffuseBRDF =
+      (mk3(1.f, 1.f, 1.f) - F) * float(M_1_PI) * diffuseColor * fmaxf(0.f, NdotL);
+  const float alpha = pow2f(s.roughness) * s.opacity;
+  const float a2 = alpha * alpha;
+  const float D = (a2 * heavisidef(NdotH))
+      / (float(M_PI) * pow2f(NdotH * NdotH * (a2 - 1.f) + 1.f));
+  const float G = ((2.f * fabsf(NdotL) * heavisidef(LdotH))
+                      / (fabsf(NdotL) + sqrtf(a2 + (1.f - a2) * NdotL * NdotL)))
+      * ((2.f * fabsf(NdotV) * heavisidef(VdotH))
+          / (fabsf(NdotV) + sqrtf(a2 + (1.f - a2) * NdotV * NdotV)));
+  const float denom = 4.f * fabsf(NdotV) * fabsf(NdotL);
+  const f3 specularBRDF = denom != 0.f ? (F * D * G) / denom : mk3(0.f, 0.f, 0.f);
+  return (diffuseBRDF + specularBRDF) * ls.radiance / ls.pdf;
+}
+
+struct NextRay
+{
+  f3 dir;
+  f3 weight;
+};
+
+// nextRay: none for matte; for physicallyBased a direction in the cone of
+// cos = 1 - roughness^2 around the mirror direction, weighted by
+// baseColor * metallic (PhysicallyBasedShader_ptx.cu:60-84,
+// uniformSampleCone gpu_math.h:299-312, computeOrthonormalBasis)
+__device__ __forceinline__ NextRay materialNextRay(
+    const MatteState &s, f3 Ns, f3 rayDir, RandState &rs)
+{
+  NextRay r;
+  if (s.type != MATERIAL_PBR) {
+    r.dir = mk3(0.f, 0.f, 0.f);
+    r.weight = mk3(0.f, 0.f, 0.f);
+    return r;
+  }
+  const f3 refl = rayDir - 2.f * dot(rayDir, Ns) * Ns;
+  const float cosThetaMax = 1.f - s.roughness * s.roughness;
+  const float s0 = curand_uniform(&rs), s1 = curand_uniform(&rs), s2 = curand_uniform(&rs);
+  // phi in double (2.0f * M_PI promotes), then its float sine and cosine
+  const float phi = float(2.0 * M_PI * double(s0));
+  const float cosTheta = (1.f - s1) + s1 * cosThetaMax;
+  const float sinTheta = sqrtf(1.f - cosTheta * cosTheta);
+  const float d = powf(s2, 1.f / 3.f);
+  const f3 cone = mk3(d * sinTheta * cosf(phi), d * sinTheta * sinf(phi), d * cosTheta);
+  const f3 n = glmNormalize(refl);
+  const float sign = n.z >= 0.f ? 1.f : -1.f;
+  const float a = -1.f / (sign + n.z);
+  const float b = n.x * n.y * a;
+  const f3 u = mk3(1.f + sign * n.x * n.x * a, sign * b, -sign * n.x);
+  const f3 v = mk3(b, sign + n.y * n.y * a, -n.y);
+  r.dir = u * cone.x + v * cone.y + n * cone.z;
+  r.weight = s.baseColor * s.metallic;
+  return r;
 }
 
 __device__ __forceinline__ bool anyNan(f3 v)
@@ -545,45 +779,89 @@ __device__ __forceinline__ float4 shadeSurfaceDL(const FrameParams &P,
 {
   const RendererGPU &rp = P.renderer;
   const WorldGPU &w = P.world;
-  const f3 shadePoint = hit.hitpoint + (hit.epsilon * hit.Ns);
+  f3 shadePoint = hit.hitpoint + (hit.epsilon * hit.Ns);
   const float aoFactor = rp.aoSamples > 0
       ? computeAO<STATS>(P, st, rs, hit, rp.occlusionDistance, rp.aoSamples)
       : 1.f;
   f3 contrib = mk3(0.f, 0.f, 0.f);
-  const MatteState ms = matteInit(w, hit);
+  MatteState ms = matteInit(w, hit);
   const float opacity = ms.opacity;
   if (rp.ambientIntensity > 0.f)
     contrib = rp.ambientColor * rp.ambientIntensity * ms.baseColor;
   for (uint32_t l = 0; l < w.numLights; l++) {
-    const LightGPU &L = w.lights[l];
-    f3 ldir;
-    float ldist;
-    f3 radiance;
-    if (L.type == LIGHT_DIRECTIONAL) {
-      ldir = L.dirToLight;
-      ldist = __int_as_float(0x7f800000); // +inf
-      radiance = L.radiance;
-    } else {
-      const f3 d = L.position - hit.hitpoint;
-      ldist = sqrtf(dot(d, d));
-      ldir = d / ldist;
-      radiance = L.radiance * (1.f / (ldist * ldist));
-    }
-    const float pdf = 1.f;
+    const LightSample ls = sampleLight(w.lights[l], hit.hitpoint, rs);
+    if (ls.pdf == 0.f)
+      continue;
     const float surface_o =
-        1.f - surfaceAttenuation<STATS>(P, st, shadePoint, ldir, 0.f, ldist);
+        1.f - surfaceAttenuation<STATS>(P, st, shadePoint, ls.dir, 0.f, ls.dist);
     const float volume_o = 1.f
         - volumeAttenuation(
-            w, rs, shadePoint, ldir, 0.f, ldist, rp.invVolumeSamplingRate, st);
+            w, rs, shadePoint, ls.dir, 0.f, ls.dist, rp.invVolumeSamplingRate, st);
     const float attenuation = surface_o * volume_o;
-    const float NdotL = fmaxf(0.f, dot(hit.Ns, ldir));
-    const f3 thisLight =
-        ms.baseColor * float(M_1_PI) * NdotL * radiance / pdf;
+    const f3 thisLight = shadeMaterial(ms, hit.Ns, ls, -ray.dir);
     if (anyNan(thisLight))
       continue;
     contrib += thisLight * attenuation;
   }
   contrib *= aoFactor;
+  // bounce rays (DirectLight_ptx.cu:154-222): the material's next ray, up to
+  // maxRayDepth closest hits, each shaded by the HDRI light or by the
+  // background seen along the bounce; matte materials give no next ray
+  f3 weight = mk3(1.f, 1.f, 1.f);
+  f3 bounceDir = ray.dir;
+  f3 Ns = hit.Ns;
+  for (int depth = 0; depth < rp.maxRayDepth; depth++) {
+    const NextRay nr = materialNextRay(ms, Ns, bounceDir, rs);
+    if (!(fabsf(nr.dir.x) > 1.0e-8f && fabsf(nr.dir.y) > 1.0e-8f && fabsf(nr.dir.z) > 1.0e-8f))
+      break;
+    weight = weight * nr.weight;
+    if (weight.x < 1.0e-12f && weight.y < 1.0e-12f && weight.z < 1.0e-12f)
+      break;
+    Ray br;
+    br.org = shadePoint;
+    br.dir = glmNormalize(nr.dir);
+    br.tmin = 0.f;
+    br.tmax = 3.402823466e+38f;
+    Hit h;
+    float unused;
+    const bool found = traverse<0, STATS>(w,
+        br.org,
+        br.dir,
+        br.tmin,
+        br.tmax,
+        rp.cullTriangleBF != 0,
+        true,
+        h,
+        unused,
+        P.errorFlag,
+        st);
+    bounceDir = br.dir;
+    if (found) {
+      SurfaceHit bh;
+      populateSurfaceHit(w, br, h, bh);
+      shadePoint = bh.hitpoint + (bh.epsilon * bh.Ns);
+      LightSample ls;
+      if (w.hdri >= 0 && w.lights[w.hdri].visible) {
+        ls = sampleHDRILight(w.lights[w.hdri], rs);
+      } else {
+        const float4 bg = backgroundOf(P, br.dir);
+        ls.radiance = mk3(bg.x, bg.y, bg.z);
+        ls.dir = br.dir;
+        ls.dist = 1.f;
+        ls.pdf = 1.f;
+      }
+      ms = matteInit(w, bh);
+      Ns = bh.Ns;
+      const f3 c = shadeMaterial(ms, bh.Ns, ls, -br.dir);
+      if (anyNan(c))
+        break;
+      contrib += c * weight;
+    } else {
+      const float4 bg = backgroundOf(P, br.dir);
+      contrib += mk3(bg.x, bg.y, bg.z) * weight;
+      break;
+    }
+  }
   return make_float4(contrib.x, contrib.y, contrib.z, opacity);
 }
 
@@ -726,7 +1004,7 @@ __device__ __forceinline__ void integrateSample(const FrameParams &P,
         instID = vInstID;
       }
       color *= opacity;
-      const float4 bg = rp.background;
+      const float4 bg = backgroundOf(P, ray.dir);
       color += mk3(bg.x, bg.y, bg.z) * (1.f - opacity);
       opacity += bg.w * (1.f - opacity);
       outputColor += color * (1.f - outputOpacity);
@@ -787,7 +1065,7 @@ __device__ __forceinline__ void integrateDPT(const FrameParams &P,
   float scrX, scrY;
   Ray ray = makePrimaryRay(P, rs, px, py, false, scrX, scrY);
   const float tmax = ray.tmax;
-  const float4 bg = rp.background;
+  const float4 bg = backgroundOf(P, ray.dir);
   o.color = mk3(bg.x, bg.y, bg.z); // albedo channel value (outColor)
   o.normal = ray.dir;
   o.depth = tmax;

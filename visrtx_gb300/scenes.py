@@ -336,6 +336,12 @@ class SurfaceSpec:
     opacity: float | str | SamplerSpec = 1.0
     alpha_mode: str = "opaque"
     cutoff: float = 0.5
+    # "matte" or "physicallyBased" (color is then "baseColor"); metallic and
+    # roughness: a value, an attribute / hit quantity name or a SamplerSpec
+    material: str = "matte"
+    metallic: float | str | SamplerSpec = 1.0
+    roughness: float | str | SamplerSpec = 1.0
+    ior: float = 1.5
 
     @property
     def num_prims(self) -> int:
@@ -362,11 +368,22 @@ class InstanceSpec:
 
 @dataclass
 class LightSpec:
+    """A light (scene/light/*.cpp): "directional" (direction, irradiance),
+    "point" / "spot" (position, intensity = `irradiance`; spot: direction,
+    opening_angle, falloff_angle) or "hdri" (radiance (H, W, 3) float32,
+    hdri_direction, hdri_up, scale, visible)."""
     type: str = "directional"
     direction: tuple = (0.0, 0.0, -1.0)
     color: tuple = (1.0, 1.0, 1.0)
     irradiance: float = 1.0
     position: tuple = (0.0, 0.0, 0.0)
+    opening_angle: float = math.pi
+    falloff_angle: float = 0.1
+    radiance: np.ndarray | None = None
+    hdri_direction: tuple = (1.0, 0.0, 0.0)
+    hdri_up: tuple = (0.0, 0.0, 1.0)
+    scale: float = 1.0
+    visible: bool = True
 
 
 @dataclass
@@ -413,6 +430,7 @@ class RendererSpec:
     pixel_samples: int = 1
     ambient_samples: int = 1
     max_depth: int = 5
+    max_ray_depth: int = 5  # bounce rays of the default renderer ("maxRayDepth")
     checkerboard: bool = False
 
     def resolved_ambient(self) -> float:
@@ -529,14 +547,25 @@ def build_on_device(dev, spec: SceneSpec, channels=("color", "depth", "primitive
         if s.cull:
             g.set("cullBackfaces", True)
         g.commit()
-        m = dev.new_material("matte")
+        m = dev.new_material(s.material)
+        cname = "baseColor" if s.material == "physicallyBased" else "color"
         if isinstance(s.color, SamplerSpec):
-            m.set("color", sampler(s.color))
+            m.set(cname, sampler(s.color))
         elif isinstance(s.color, str):
-            m.set("color", s.color)
+            m.set(cname, s.color)
         else:
-            m.set("color", tuple(float(c) for c in s.color),
+            m.set(cname, tuple(float(c) for c in s.color),
                   L.FLOAT32_VEC4 if len(s.color) == 4 else L.FLOAT32_VEC3)
+        if s.material == "physicallyBased":
+            for name in ("metallic", "roughness"):
+                val = getattr(s, name)
+                if isinstance(val, SamplerSpec):
+                    m.set(name, sampler(val))
+                elif isinstance(val, str):
+                    m.set(name, val)
+                else:
+                    m.set(name, float(val))
+            m.set("ior", float(s.ior))
         if isinstance(s.opacity, SamplerSpec):
             m.set("opacity", sampler(s.opacity))
         else:
@@ -558,9 +587,22 @@ def build_on_device(dev, spec: SceneSpec, channels=("color", "depth", "primitive
         if l.type == "directional":
             lt.set("direction", tuple(map(float, l.direction)), L.FLOAT32_VEC3)
             lt.set("irradiance", float(l.irradiance))
+        elif l.type == "hdri":
+            img = np.ascontiguousarray(l.radiance, np.float32)
+            a2 = dev.new_array2d(img, L.FLOAT32_VEC3)
+            keep.append(a2)
+            lt.set("radiance", a2)
+            lt.set("direction", tuple(map(float, l.hdri_direction)), L.FLOAT32_VEC3)
+            lt.set("up", tuple(map(float, l.hdri_up)), L.FLOAT32_VEC3)
+            lt.set("scale", float(l.scale))
+            lt.set("visible", bool(l.visible))
         else:
             lt.set("position", tuple(map(float, l.position)), L.FLOAT32_VEC3)
             lt.set("intensity", float(l.irradiance))
+            if l.type == "spot":
+                lt.set("direction", tuple(map(float, l.direction)), L.FLOAT32_VEC3)
+                lt.set("openingAngle", float(l.opening_angle))
+                lt.set("falloffAngle", float(l.falloff_angle))
         lt.commit()
         lights.append(lt)
         keep.append(lt)
@@ -653,6 +695,7 @@ def build_on_device(dev, spec: SceneSpec, channels=("color", "depth", "primitive
     ren.set("pixelSamples", int(r.pixel_samples))
     ren.set("ambientSamples", int(r.ambient_samples))
     ren.set("maxDepth", int(r.max_depth))
+    ren.set("maxRayDepth", int(r.max_ray_depth))
     ren.set("checkerboarding", bool(r.checkerboard))
     ren.commit()
 
