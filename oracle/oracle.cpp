@@ -1106,12 +1106,16 @@ inline float mixf(float a, float b, float t)
 
 // makePrimaryRay + cameraCreateRay (gpu/cameraCreateRay.h:38-81)
 Ray primaryRay(const CamPre &c, Stream &rs, int px, int py, float invW, float invH,
-    bool centerPixel)
+    bool centerPixel, float *screen = nullptr)
 {
   float r[4];
   uniform4(rs, r);
   const float sx0 = (centerPixel ? (float)px : (float)px + r[0]) * invW;
   const float sy0 = (centerPixel ? (float)py : (float)py + r[1]) * invH;
+  if (screen) {
+    screen[0] = sx0;
+    screen[1] = sy0;
+  }
   const float sx = mixf(c.region[0], c.region[2], sx0);
   const float sy = mixf(c.region[1], c.region[3], sy0);
   Ray ray;
@@ -2253,14 +2257,60 @@ V3 hdriRadiance(const SceneCtx &S, int li, V3 dir)
   return hdriTexel(L, phi * (1.f / (2.f * (float)M_PI)), theta * (1.f / (float)M_PI));
 }
 
-// getBackground (gpu_util.h:298-307): a visible HDRI light, else the colour
-V4 backgroundOf(const Ctx &C, V3 dir)
+// the background image as the device stages it (acquireCUDAArrayUint8,
+// utility/CudaImageTexture.cpp:43-93): RGBA8, float components truncated
+// from c * 255 (clamped), sRGB bytes linearised, alpha 255 for three channels
+uint8_t bgTexel(const OrcRenderer &R, size_t i, int c)
+{
+  const int nc = R.bgType == 242 ? 3 : 4;
+  if (c >= nc)
+    return 255;
+  if (R.bgType == 242 || R.bgType == 243) {
+    const float s = ((const float *)R.bgImage)[i * nc + c] * 255.f;
+    return (uint8_t)(s >= 255.f ? 255.f : (s > 0.f ? s : 0.f));
+  }
+  const uint8_t b = ((const uint8_t *)R.bgImage)[i * 4 + c];
+  if (R.bgType == 261 && c < 3) {
+    const float x = b / 255.f;
+    const float lin = x <= 0.04045f ? x * 0.07739938080495356f
+                                    : std::pow((x + 0.055f) * 0.94786729857819905f, 2.4f);
+    return (uint8_t)(lin * 255.f);
+  }
+  return b;
+}
+
+// normalised-float reads of the RGBA8 image: linear, clamped, normalised
+// coordinates, 8-bit weights
+V4 bgImageAt(const OrcRenderer &R, float u, float v)
+{
+  const int W = R.bgW, H = R.bgH;
+  const float xs = u * (float)W - 0.5f, ys = v * (float)H - 0.5f;
+  const float fx = std::floor(xs), fy = std::floor(ys);
+  const float a = quantW(xs - fx, 1), b = quantW(ys - fy, 1);
+  auto cx = [&](int i) { return std::min(std::max(i, 0), W - 1); };
+  auto cy = [&](int j) { return std::min(std::max(j, 0), H - 1); };
+  const int x0 = cx((int)fx), x1 = cx((int)fx + 1), y0 = cy((int)fy), y1 = cy((int)fy + 1);
+  float out[4];
+  for (int c = 0; c < 4; c++) {
+    auto at = [&](int x, int y) { return bgTexel(R, (size_t)y * W + x, c) / 255.f; };
+    const float r0 = (1.f - a) * at(x0, y0) + a * at(x1, y0);
+    const float r1 = (1.f - a) * at(x0, y1) + a * at(x1, y1);
+    out[c] = (1.f - b) * r0 + b * r1;
+  }
+  return {out[0], out[1], out[2], out[3]};
+}
+
+// getBackground (gpu_util.h:290-307): a visible HDRI light, else the
+// background image at loc, else the colour
+V4 backgroundOf(const Ctx &C, V3 dir, float lx, float ly)
 {
   const SceneCtx &S = *C.S;
   if (S.hdriIndex >= 0 && S.sc->lights[S.hdriIndex].hdriVisible) {
     const V3 r = hdriRadiance(S, S.hdriIndex, dir);
     return {r.x, r.y, r.z, 1.f};
   }
+  if (C.R->bgImage && C.R->bgW > 0 && C.R->bgH > 0)
+    return bgImageAt(*C.R, lx, ly);
   return {C.R->background[0], C.R->background[1], C.R->background[2], C.R->background[3]};
 }
 
@@ -2405,7 +2455,7 @@ bool nextRay(const Matte &m, V3 Ns, V3 rayDir, Stream &rs, V3 &dir, V3 &weight)
 // (sampleLight.h:60-173) with surface and volume attenuation, AO, then the
 // bounce rays of the material's nextRay up to maxRayDepth
 void shadeDL(Ctx &C, const VolCtx &VC, Stream &rs, const Ray &ray, const SHit &hit,
-    float out[4])
+    int px, int py, float out[4])
 {
   const OrcRenderer &R = *C.R;
   const SceneCtx &S = *C.S;
@@ -2461,7 +2511,8 @@ void shadeDL(Ctx &C, const VolCtx &VC, Stream &rs, const Ray &ray, const SHit &h
       if (S.hdriIndex >= 0 && S.sc->lights[S.hdriIndex].hdriVisible) {
         ls = sampleHDRILight(S, S.hdriIndex, rs);
       } else {
-        const V4 bg = backgroundOf(C, br.dir);
+        // the bounce reads the background at the pixel position
+        const V4 bg = backgroundOf(C, br.dir, (float)px, (float)py);
         ls.radiance = v3(bg.x, bg.y, bg.z);
         ls.dir = br.dir;
         ls.dist = 1.f;
@@ -2474,7 +2525,7 @@ void shadeDL(Ctx &C, const VolCtx &VC, Stream &rs, const Ray &ray, const SHit &h
         break;
       contrib = contrib + c * weight;
     } else {
-      const V4 bg = backgroundOf(C, br.dir);
+      const V4 bg = backgroundOf(C, br.dir, (float)px, (float)py);
       contrib = contrib + v3(bg.x, bg.y, bg.z) * weight;
       break;
     }
@@ -2503,7 +2554,8 @@ Sample integrate(Ctx &C, const VolCtx &VC, const CamPre &cam, Stream &rs, int px
   const OrcRenderer &R = *C.R;
   const int rt = R.type;
   const float invRate = 1.f / std::min(std::max(R.volumeSamplingRate, 1e-3f), 10.f);
-  Ray ray = primaryRay(cam, rs, px, py, invW, invH, rt == 1);
+  float scr[2];
+  Ray ray = primaryRay(cam, rs, px, py, invW, invH, rt == 1, scr);
   const float tmax = ray.tmax;
   V3 outC = v3(0, 0, 0);
   V3 outN = ray.dir; // outputNormal: the ray direction on a miss
@@ -2546,7 +2598,7 @@ Sample integrate(Ctx &C, const VolCtx &VC, const CamPre &cam, Stream &rs, int px
       const OrcSurface &s = C.S->sc->surfaces[sh.surface];
       if (rt == 0) {
         float sr[4];
-        shadeDL(C, VC, rs, ray, sh, sr);
+        shadeDL(C, VC, rs, ray, sh, px, py, sr);
         const V3 srgb = v3(sr[0], sr[1], sr[2]);
         if (std::isnan(sr[0]) || std::isnan(sr[1]) || std::isnan(sr[2])) {
           color = v3(0, 0, 0);
@@ -2586,7 +2638,7 @@ Sample integrate(Ctx &C, const VolCtx &VC, const CamPre &cam, Stream &rs, int px
         inst = vi;
       }
       color = color * opacity;
-      const V4 bg = backgroundOf(C, ray.dir);
+      const V4 bg = backgroundOf(C, ray.dir, scr[0], scr[1]);
       color = color + v3(bg.x, bg.y, bg.z) * (1.f - opacity);
       opacity += bg.w * (1.f - opacity);
       outC = outC + color * (1.f - outO);
@@ -2681,8 +2733,9 @@ Sample integrateDPT(Ctx &C, const VolCtx &VC, const CamPre &cam, Stream &rs, int
     float invW, float invH, PathState &pd)
 {
   const OrcRenderer &R = *C.R;
-  Ray ray = primaryRay(cam, rs, px, py, invW, invH, false);
-  const V4 bg4 = backgroundOf(C, ray.dir);
+  float scr[2];
+  Ray ray = primaryRay(cam, rs, px, py, invW, invH, false, scr);
+  const V4 bg4 = backgroundOf(C, ray.dir, scr[0], scr[1]);
   const V3 bg = v3(bg4.x, bg4.y, bg4.z);
   // outColor (the background) and the primary ray direction go to the
   // albedo and normal channels

@@ -202,6 +202,11 @@ typedef struct OrcRenderer {
   int ambientSamples;
   int maxDepth;
   int maxRayDepth; /* bounce rays of the default renderer */
+  /* background image (W x H, x fastest) of element type bgType (this
+   * library's codes: 242/243 float32 x3/x4, 260 ufixed8 x4, 261 sRGB8 x4),
+   * NULL: the background colour */
+  const void *bgImage;
+  int bgType, bgW, bgH;
 } OrcRenderer;
 
 typedef struct OrcFrame {

@@ -150,7 +150,8 @@ class OrcRenderer(C.Structure):
                 ("ambientRadiance", C.c_float), ("occlusionDistance", C.c_float),
                 ("cullTriangleBackfaces", C.c_int), ("volumeSamplingRate", C.c_float),
                 ("pixelSamples", C.c_int), ("ambientSamples", C.c_int), ("maxDepth", C.c_int),
-                ("maxRayDepth", C.c_int)]
+                ("maxRayDepth", C.c_int), ("bgImage", C.c_void_p), ("bgType", C.c_int),
+                ("bgW", C.c_int), ("bgH", C.c_int)]
 
 
 class OrcFrame(C.Structure):
@@ -447,6 +448,13 @@ def _render_prepared(lib, handle, spec, frame_id, rows, volume_mode, tex_round, 
     ren.ambientSamples = r.ambient_samples if ren.type in (0, 2) else 0
     ren.maxDepth = r.max_depth
     ren.maxRayDepth = r.max_ray_depth
+    bg_keep = None
+    if r.background_image is not None:
+        from visrtx_gb300.scenes import background_image_type
+        bg_keep = np.ascontiguousarray(r.background_image)
+        ren.bgImage = bg_keep.ctypes.data_as(C.c_void_p)
+        ren.bgType = background_image_type(bg_keep, r.background_srgb)
+        ren.bgH, ren.bgW = bg_keep.shape[0], bg_keep.shape[1]
     W, H = spec.width, spec.height
     out = {
         "accum": np.zeros((H, W, 4), np.float32) if accum is None else accum,

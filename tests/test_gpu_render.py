@@ -744,3 +744,36 @@ def test_hdri_background(device, renderer):
     miss = g["depth"] >= 1e29
     bg = anari.rgba8(g["color"])[..., :3][miss].astype(np.float64)
     assert miss.any() and bg.std() > 2.0, "the environment varies across the background"
+
+
+@pytest.mark.parametrize("case", ["float3-raycast", "srgb8-default-pbr", "float4-ao"])
+def test_background_image(device, case):
+    """The renderer's "background" given as an image (Renderer.cpp:152-175):
+    RGBA8-staged (utility/CudaImageTexture.cpp), read with linear filtering
+    at each sample's screen position; the default renderer's bounce rays
+    read it at the pixel position (DirectLight_ptx.cu:196-216)."""
+    fmt, renderer = case.split("-")[:2]
+    rng = np.random.default_rng(9)
+    yy, xx = np.meshgrid(np.linspace(0, 1, 12), np.linspace(0, 1, 20), indexing="ij")
+    base = np.stack([xx, yy, 0.5 * (xx + yy)], -1)
+    if fmt == "float3":
+        img = (base * 0.9).astype(np.float32)
+    elif fmt == "float4":
+        img = np.concatenate([base, np.ones_like(xx)[..., None]], -1).astype(np.float32)
+    else:
+        img = np.concatenate([base * 255, rng.integers(200, 256, xx.shape)[..., None]],
+                             -1).astype(np.uint8)
+    spec = lit_scene("physicallyBased" if case.endswith("pbr") else "matte", "directional",
+                     renderer=renderer)
+    spec.renderer.background_image = img
+    spec.renderer.background_srgb = fmt == "srgb8"
+    spec.renderer.ambient_samples = 2 if renderer == "ao" else 0
+    g = render_gpu(device, spec)
+    r = render_oracle(spec)
+    rep = compare(g, r, allow_ids=3, color_tol=3)
+    from visrtx_gb300 import anari
+
+    miss = g["depth"] >= 1e29
+    bg = anari.rgba8(g["color"])[..., :3][miss].astype(np.float64)
+    assert miss.any() and bg.std() > 5.0, "the image varies across the background"
+    print(case, rep)

@@ -2588,6 +2588,105 @@ bool World::getProperty(
 // .cpp, Raycast.cpp, DiffusePathTracer.cpp)
 // ---------------------------------------------------------------------------
 
+Renderer::~Renderer()
+{
+  if (gpu.backgroundTex)
+    cudaDestroyTextureObject(gpu.backgroundTex);
+  if (bgArray)
+    cudaFreeArray(bgArray);
+}
+
+uint64_t Renderer::deepStamp() const
+{
+  return std::max(commitStamp, bgImage ? bgImage->deepStamp() : 0);
+}
+
+// Renderer::finalize with Array2D::acquireCUDAArrayUint8
+// (utility/CudaImageTexture.cpp:43-93,139-190): the image staged as RGBA8
+// (float components truncated from c * 255, clamped to [0, 255] here;
+// sRGB-encoded bytes linearised first; three channels get alpha 255), a
+// normalised-float, linear, clamped texture read at the sample's screen
+// position
+bool Renderer::ensureBackground()
+{
+  if (!bgImage) {
+    if (gpu.backgroundTex)
+      cudaDestroyTextureObject(gpu.backgroundTex);
+    if (bgArray)
+      cudaFreeArray(bgArray);
+    gpu.backgroundTex = 0;
+    bgArray = nullptr;
+    return true;
+  }
+  const uint64_t want = deepStamp();
+  if (bgStamp && bgStamp >= want && gpu.backgroundTex)
+    return true;
+  if (gpu.backgroundTex)
+    cudaDestroyTextureObject(gpu.backgroundTex);
+  if (bgArray)
+    cudaFreeArray(bgArray);
+  gpu.backgroundTex = 0;
+  bgArray = nullptr;
+  const int et = bgImage->elemType;
+  const int nc = et == VRTX_FLOAT32_VEC3 ? 3
+      : (et == VRTX_FLOAT32_VEC4 || et == VRTX_UFIXED8_VEC4 || et == VRTX_UFIXED8_RGBA_SRGB) ? 4
+                                                                                            : 0;
+  if (!nc) {
+    report(VRTX_SEVERITY_WARNING,
+        "background image: element type %d is not supported (FLOAT32_VEC3/4, "
+        "UFIXED8_VEC4, UFIXED8_RGBA_SRGB are)",
+        et);
+    return false;
+  }
+  const size_t W = bgImage->n[0], H = bgImage->n[1];
+  std::vector<uint8_t> raw(bgImage->bytes());
+  if (const void *h = bgImage->hostData())
+    std::memcpy(raw.data(), h, raw.size());
+  else
+    cudaMemcpy(raw.data(), bgImage->deviceData(), raw.size(), cudaMemcpyDeviceToHost);
+  std::vector<uint8_t> rgba(W * H * 4);
+  for (size_t i = 0; i < W * H; i++) {
+    for (int c = 0; c < 4; c++) {
+      uint8_t v = 255;
+      if (c < nc) {
+        if (et == VRTX_FLOAT32_VEC3 || et == VRTX_FLOAT32_VEC4) {
+          float f;
+          std::memcpy(&f, raw.data() + 4 * (i * nc + c), 4);
+          const float s = f * 255.f;
+          v = (uint8_t)(s >= 255.f ? 255.f : (s > 0.f ? s : 0.f));
+        } else if (et == VRTX_UFIXED8_RGBA_SRGB && c < 3) {
+          // glm::convertSRGBToLinear
+          const float x = raw[i * 4 + c] / 255.f;
+          const float lin = x <= 0.04045f ? x * 0.07739938080495356f
+                                          : std::pow((x + 0.055f) * 0.94786729857819905f, 2.4f);
+          v = (uint8_t)(lin * 255.f);
+        } else {
+          v = raw[i * 4 + c];
+        }
+      }
+      rgba[i * 4 + c] = v;
+    }
+  }
+  cudaChannelFormatDesc desc = cudaCreateChannelDesc<uchar4>();
+  if (cudaMallocArray(&bgArray, &desc, W, H) != cudaSuccess) {
+    cudaGetLastError();
+    bgArray = nullptr;
+    return false;
+  }
+  cudaMemcpy2DToArray(bgArray, 0, 0, rgba.data(), W * 4, W * 4, H, cudaMemcpyHostToDevice);
+  cudaResourceDesc rd{};
+  rd.resType = cudaResourceTypeArray;
+  rd.res.array.array = bgArray;
+  cudaTextureDesc td{};
+  td.addressMode[0] = td.addressMode[1] = cudaAddressModeClamp;
+  td.filterMode = cudaFilterModeLinear;
+  td.readMode = cudaReadModeNormalizedFloat;
+  td.normalizedCoords = 1;
+  cudaCreateTextureObject(&gpu.backgroundTex, &rd, &td, nullptr);
+  bgStamp = want;
+  return cudaGetLastError() == cudaSuccess;
+}
+
 void Renderer::commit()
 {
   RendererGPU &r = gpu;
@@ -2611,6 +2710,8 @@ void Renderer::commit()
   if (has("background", VRTX_FLOAT32_VEC4))
     std::memcpy(bg, params["background"].bytes.data(), 16);
   r.background = make_float4(bg[0], bg[1], bg[2], bg[3]);
+  bgImage = static_cast<Array *>(getObject("background", VRTX_ARRAY2D));
+  bgStamp = 0;
   spp = get<int32_t>("pixelSamples", VRTX_INT32, 1);
   r.maxRayDepth = get<int32_t>("maxRayDepth", VRTX_INT32, 5);
   r.ambientColor = get<f3>("ambientColor", VRTX_FLOAT32_VEC3, f3{1.f, 1.f, 1.f});
@@ -2836,6 +2937,7 @@ void Frame::render()
   FrameParams P{};
   P.world = world->gpu;
   P.camera = camera->gpu;
+  renderer->ensureBackground();
   P.renderer = renderer->gpu;
   P.fb = fb;
   P.workCounter = workCounter;
@@ -2850,8 +2952,10 @@ void Frame::render()
   // The "ao" renderer over opaque surfaces (no volumes) runs as a
   // wavefront (primary / any-hit / resolve kernels per sample); everything
   // else runs the per-pixel integrator kernel.
+  // (a background image is read at each sample's jittered screen position,
+  // which the wavefront's resolve does not keep: such frames run per pixel)
   const bool wavefront = P.renderer.type == RENDERER_AO && P.world.allOpaque
-      && P.world.numVolumes == 0 && !forceMegakernel;
+      && P.world.numVolumes == 0 && !forceMegakernel && !P.renderer.backgroundTex;
   cudaError_t err = cudaSuccess;
   cudaEventRecord(evKStart, s);
   if (wavefront) {

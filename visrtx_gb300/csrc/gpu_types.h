@@ -382,6 +382,9 @@ struct RendererGPU
   int aoSamples;
   int maxDepth; // dpt
   float lightFalloff;
+  // background image (RGBA8, normalised float reads, linear, clamp), 0:
+  // the background colour
+  cudaTextureObject_t backgroundTex;
 };
 
 enum FrameFormat : int

@@ -372,8 +372,15 @@ struct Renderer : Object
   int spp = 1;
   int sampleLimit = 128;
   bool checkerboard = false;
+  // "background" given as an Array2D image (Renderer.cpp:152-175)
+  Array *bgImage = nullptr;
+  cudaArray_t bgArray = nullptr;
+  uint64_t bgStamp = 0;
+  ~Renderer() override;
   void commit() override;
   bool isValid() const override;
+  uint64_t deepStamp() const override;
+  bool ensureBackground();
 };
 
 struct Frame : Object

@@ -293,7 +293,9 @@ __global__ void __launch_bounds__(128) k_aoResolve(const FrameParams P,
     f3 color = mk3(0.f, 0.f, 0.f);
     float opacity = 0.f;
     color *= opacity;
-    const float4 bg = backgroundOf(P, px.normal); // a miss keeps the ray direction
+    // a miss keeps the ray direction (frames with a background image do
+    // not take this path)
+    const float4 bg = backgroundOf(P, px.normal, 0.f, 0.f);
     color += mk3(bg.x, bg.y, bg.z) * (1.f - opacity);
     opacity += bg.w * (1.f - opacity);
     outputColor = mk3(0.f, 0.f, 0.f) + color * (1.f - 0.f);

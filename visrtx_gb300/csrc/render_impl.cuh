@@ -539,14 +539,17 @@ __device__ __forceinline__ f3 hdriRadiance(const LightGPU &L, f3 dir)
   return hdriAt(L, u, v);
 }
 
-// getBackground (gpu_util.h:298-307): a visible HDRI, else the colour
-__device__ __forceinline__ float4 backgroundOf(const FrameParams &P, f3 dir)
+// getBackground (gpu_util.h:290-307): a visible HDRI, else the background
+// image at loc (normalised coordinates), else the colour
+__device__ __forceinline__ float4 backgroundOf(const FrameParams &P, f3 dir, float lx, float ly)
 {
   const WorldGPU &w = P.world;
   if (w.hdri >= 0 && w.lights[w.hdri].visible) {
     const f3 r = hdriRadiance(w.lights[w.hdri], dir);
     return make_float4(r.x, r.y, r.z, 1.f);
   }
+  if (P.renderer.backgroundTex)
+    return tex2D<float4>(P.renderer.backgroundTex, lx, ly);
   return P.renderer.background;
 }
 
@@ -775,7 +778,9 @@ __device__ __forceinline__ float4 shadeSurfaceDL(const FrameParams &P,
     TravStats &st,
     RandState &rs,
     const Ray &ray,
-    const SurfaceHit &hit)
+    const SurfaceHit &hit,
+    int px,
+    int py)
 {
   const RendererGPU &rp = P.renderer;
   const WorldGPU &w = P.world;
@@ -844,7 +849,9 @@ __device__ __forceinline__ float4 shadeSurfaceDL(const FrameParams &P,
       if (w.hdri >= 0 && w.lights[w.hdri].visible) {
         ls = sampleHDRILight(w.lights[w.hdri], rs);
       } else {
-        const float4 bg = backgroundOf(P, br.dir);
+        // the bounce reads the background at the pixel position
+        // (DirectLight_ptx.cu:196-200, ss.pixel)
+        const float4 bg = backgroundOf(P, br.dir, float(px), float(py));
         ls.radiance = mk3(bg.x, bg.y, bg.z);
         ls.dir = br.dir;
         ls.dist = 1.f;
@@ -857,7 +864,7 @@ __device__ __forceinline__ float4 shadeSurfaceDL(const FrameParams &P,
         break;
       contrib += c * weight;
     } else {
-      const float4 bg = backgroundOf(P, br.dir);
+      const float4 bg = backgroundOf(P, br.dir, float(px), float(py));
       contrib += mk3(bg.x, bg.y, bg.z) * weight;
       break;
     }
@@ -954,7 +961,7 @@ __device__ __forceinline__ void integrateSample(const FrameParams &P,
         firstHit = false;
       }
       if (RT == RENDERER_DIRECT_LIGHT) {
-        const float4 sr = shadeSurfaceDL<STATS>(P, st, rs, ray, sh);
+        const float4 sr = shadeSurfaceDL<STATS>(P, st, rs, ray, sh, px, py);
         const f3 srgb = mk3(sr.x, sr.y, sr.z);
         if (anyNan(srgb)) {
           color = mk3(0.f, 0.f, 0.f);
@@ -1004,7 +1011,7 @@ __device__ __forceinline__ void integrateSample(const FrameParams &P,
         instID = vInstID;
       }
       color *= opacity;
-      const float4 bg = backgroundOf(P, ray.dir);
+      const float4 bg = backgroundOf(P, ray.dir, scrX, scrY);
       color += mk3(bg.x, bg.y, bg.z) * (1.f - opacity);
       opacity += bg.w * (1.f - opacity);
       outputColor += color * (1.f - outputOpacity);
@@ -1065,7 +1072,7 @@ __device__ __forceinline__ void integrateDPT(const FrameParams &P,
   float scrX, scrY;
   Ray ray = makePrimaryRay(P, rs, px, py, false, scrX, scrY);
   const float tmax = ray.tmax;
-  const float4 bg = backgroundOf(P, ray.dir);
+  const float4 bg = backgroundOf(P, ray.dir, scrX, scrY);
   o.color = mk3(bg.x, bg.y, bg.z); // albedo channel value (outColor)
   o.normal = ray.dir;
   o.depth = tmax;

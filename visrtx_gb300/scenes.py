@@ -432,6 +432,10 @@ class RendererSpec:
     max_depth: int = 5
     max_ray_depth: int = 5  # bounce rays of the default renderer ("maxRayDepth")
     checkerboard: bool = False
+    # "background" as an image: (H, W, 3|4) float32 or (H, W, 4) uint8
+    # (sRGB-encoded when background_srgb)
+    background_image: np.ndarray | None = None
+    background_srgb: bool = False
 
     def resolved_ambient(self) -> float:
         if self.ambient_radiance is not None:
@@ -450,6 +454,17 @@ class SceneSpec:
     width: int = 64
     height: int = 64
     world_id: int = 0xFFFFFFFF
+
+
+def background_image_type(img: np.ndarray, srgb: bool = False) -> int:
+    """Element type code of a background image (RendererSpec.background_image)."""
+    from . import _lib as L
+
+    if img.dtype == np.float32 and img.shape[-1] in (3, 4):
+        return L.FLOAT32_VEC3 if img.shape[-1] == 3 else L.FLOAT32_VEC4
+    if img.dtype == np.uint8 and img.shape[-1] == 4:
+        return L.UFIXED8_RGBA_SRGB if srgb else L.UFIXED8_VEC4
+    raise ValueError("background images are (H, W, 3|4) float32 or (H, W, 4) uint8")
 
 
 def attr_type(a: np.ndarray) -> int:
@@ -685,7 +700,13 @@ def build_on_device(dev, spec: SceneSpec, channels=("color", "depth", "primitive
 
     r = spec.renderer
     ren = dev.new_renderer(r.subtype)
-    ren.set("background", tuple(map(float, r.background)), L.FLOAT32_VEC4)
+    if r.background_image is not None:
+        img = np.ascontiguousarray(r.background_image)
+        bga = dev.new_array2d(img, background_image_type(img, r.background_srgb))
+        keep.append(bga)
+        ren.set("background", bga)
+    else:
+        ren.set("background", tuple(map(float, r.background)), L.FLOAT32_VEC4)
     ren.set("ambientColor", tuple(map(float, r.ambient_color)), L.FLOAT32_VEC3)
     if r.ambient_radiance is not None:
         ren.set("ambientRadiance", float(r.ambient_radiance))
