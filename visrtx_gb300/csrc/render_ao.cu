@@ -67,7 +67,7 @@ __device__ __forceinline__ uint32_t warpAppend(uint32_t *counter, uint32_t n)
 }
 
 template <bool STATS, bool SEG>
-__global__ void __launch_bounds__(128) k_aoPrimary(const FrameParams P,
+__global__ void __launch_bounds__(128, VRTX_PRIMARY_MIN_BLOCKS) k_aoPrimary(const FrameParams P,
     int sampleIdx,
     uint32_t *consumed,
     AOPixel *pixels,

@@ -53,6 +53,11 @@
 #define VRTX_NANOVDB_MIN_BLOCKS 4
 #endif
 
+// the same for the wavefront AO's primary (closest-hit) kernel
+#ifndef VRTX_PRIMARY_MIN_BLOCKS
+#define VRTX_PRIMARY_MIN_BLOCKS 1
+#endif
+
 #ifndef VRTX_TRACE_MIN_BLOCKS
 #define VRTX_TRACE_MIN_BLOCKS 8
 #endif
