@@ -44,26 +44,26 @@ struct AORay
   float4 dirWeight; // dir.xyz, weight
 };
 
-__device__ __forceinline__ uint32_t warpAppend(uint32_t *counter, uint32_t n)
+// Queue slots for the whole warp at once (all 32 lanes call it; the full
+// mask makes them converge): one atomic, each lane's slots after the lanes
+// below it, so the warp's rays form one contiguous block.
+__device__ __forceinline__ uint32_t warpAppendAll(uint32_t *counter, uint32_t n)
 {
-  // one atomic per warp: exclusive prefix of n over the active lanes
-  const uint32_t mask = __activemask();
-  const int lane = threadIdx.x & 31;
-  uint32_t total = 0, before = 0;
-  for (int l = 0; l < 32; l++) {
-    if (!((mask >> l) & 1u))
-      continue;
-    const uint32_t v = __shfl_sync(mask, n, l);
-    if (l < lane)
-      before += v;
-    total += v;
+  const uint32_t full = 0xffffffffu;
+  const uint32_t lane = threadIdx.x & 31u;
+  uint32_t incl = n;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const uint32_t v = __shfl_up_sync(full, incl, d);
+    if ((int)lane >= d)
+      incl += v;
   }
-  const int leader = __ffs(mask) - 1;
+  const uint32_t total = __shfl_sync(full, incl, 31);
   uint32_t base = 0;
-  if (lane == leader && total)
+  if (lane == 31 && total)
     base = atomicAdd(counter, total);
-  base = __shfl_sync(mask, base, leader);
-  return base + before;
+  base = __shfl_sync(full, base, 31);
+  return base + incl - n;
 }
 
 template <bool STATS, bool SEG>
@@ -133,7 +133,7 @@ __global__ void __launch_bounds__(128, VRTX_PRIMARY_MIN_BLOCKS) k_aoPrimary(cons
     }
     consumed[idx] = used + draws;
   }
-  const uint32_t base = warpAppend(rayCount, nRays);
+  const uint32_t base = warpAppendAll(rayCount, nRays);
   if (valid) {
     px.rayBase = base;
     for (uint32_t i = 0; i < nRays; i++) {
