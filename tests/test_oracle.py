@@ -406,3 +406,25 @@ def test_nvdb_fpn_bit_widths():
         widths.add(w)
         off += 96 + (64 << w)
     assert widths == {0, 1, 2, 3}, widths
+
+
+def test_nvdb_writer_edge_cases():
+    """Empty grids (no active voxel: header, tree and an empty root) and a
+    single voxel far from the origin at negative coordinates."""
+    from visrtx_gb300 import nanovdb as NV
+
+    for gtype in NVDB_TYPES:
+        buf = NV.build_grid(np.zeros((4, 5, 6), np.float32), grid_type=gtype)
+        info = NV.grid_info(buf)
+        assert buf.size == 672 + 64 + 64 and info["leaves"] == 0 and info["voxels"] == 0
+        assert np.all(O.nvdb_sample(buf, np.zeros((3, 3), np.float32)) == 0.0)
+    buf = NV.build_grid(np.full((1, 1, 1), 0.5, np.float32), index_origin=(-5000, 3, -1),
+                        voxel_size=2.0)
+    info = NV.grid_info(buf)
+    assert info["index_bbox"] == ((-5000, 3, -1), (-5000, 3, -1))
+    assert info["world_bbox"] == ((-10000.0, 6.0, -2.0), (-9998.0, 8.0, 0.0))
+    # at the voxel, and half a voxel towards +x (lerp with the background 0)
+    got = O.nvdb_sample(buf, np.array([[-10000.0, 6.0, -2.0], [-9999.0, 6.0, -2.0]], np.float32))
+    np.testing.assert_array_equal(got, np.array([0.5, 0.25], np.float32))
+    with pytest.raises(ValueError):
+        NV.build_grid(np.zeros((2, 2, 2), np.float32), grid_type="half")
