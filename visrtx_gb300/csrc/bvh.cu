@@ -4,9 +4,18 @@
 //  * The binary tree is the Karras (HPG 2012) radix tree over 63-bit Morton
 //    codes; equal codes are disambiguated by the sorted index, so the tree is
 //    well formed for any input.
+//  * Before the collapse, a bottom-up pass solves the SAH-optimal collapse
+//    of the binary tree into 8-wide nodes (Ylitie, Karras and Laine, HPG
+//    2017): C(n, i), the cost of representing subtree n by at most i
+//    children of a wide node, from C(n, 1) = a leaf (<= maxLeafPrims
+//    primitives: A(n) * count * C_PRIM) or a wide node (A(n) * C_NODE +
+//    D(n, 8)), and C(n, i) = min(C(n, i - 1), D(n, i)) with the distribution
+//    D(n, j) = min_k C(left, k) + C(right, j - k); each node keeps its
+//    choices (the split k per i, and whether D is taken) in one word.
 //  * The collapse runs level by level: every thread takes one task (a binary
-//    subtree root and the BVH8 slot it fills), opens up to 8 children by
-//    repeatedly splitting the child with the largest surface area, turns
+//    subtree root and the BVH8 slot it fills), takes its children from the
+//    SAH choices (or, with VRTX_BVH_SAH 0, opens up to 8 children by
+//    repeatedly splitting the child with the largest surface area), turns
 //    subtrees of <= maxLeafPrims primitives into leaves, assigns children to
 //    slots so that the slot index XOR the ray octant gives a near-to-far
 //    order, quantises child boxes outward, and appends one task per internal
@@ -227,6 +236,100 @@ __global__ void k_refit(int n,
   }
 }
 
+// --- SAH-optimal collapse costs ---------------------------------------------
+
+#ifndef VRTX_BVH_SAH
+#define VRTX_BVH_SAH 1
+#endif
+
+#ifndef VRTX_SAH_PRIM_COST
+#define VRTX_SAH_PRIM_COST 0.3f
+#endif
+constexpr float kCostNode = 1.0f; // a wide-node test
+constexpr float kCostPrim = VRTX_SAH_PRIM_COST; // a primitive test
+
+// decision word: 4 bits per i = 2..8 at bit 4 (i - 2): the split k (1..7)
+// of D(n, i) in bits 0-2, bit 3 set when C(n, i) takes D(n, i) (else it is
+// C(n, i - 1)); i = 8 is the wide-node distribution of C(n, 1)
+__device__ __forceinline__ uint32_t decSplit(uint32_t d, int i)
+{
+  return (d >> (4 * (i - 2))) & 7u;
+}
+
+__device__ __forceinline__ bool decTakesD(uint32_t d, int i)
+{
+  return (d >> (4 * (i - 2) + 3)) & 1u;
+}
+
+__global__ void k_sahCosts(int n,
+    const uint32_t *sortedIdx,
+    const box3 *boxes,
+    const uint32_t *left,
+    const uint32_t *right,
+    const uint32_t *parentInternal,
+    const uint32_t *parentLeaf,
+    const box3 *internalBoxes,
+    const uint32_t *internalCount,
+    int maxLeaf,
+    float *cost, // 7 per internal node: C(n, 1..7)
+    uint32_t *dec,
+    uint32_t *flags)
+{
+  const int i0 = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i0 >= n || n < 2)
+    return;
+  uint32_t p = parentLeaf[i0];
+  while (p != NONE) {
+    __threadfence();
+    if (atomicAdd(&flags[p], 1u) == 0)
+      return;
+    __threadfence();
+    float cc[2][8];
+    const uint32_t kids[2] = {left[p], right[p]};
+    for (int k = 0; k < 2; k++) {
+      const uint32_t r = kids[k];
+      if (r & LEAF_BIT) {
+        const float c = halfArea(boxes[sortedIdx[r & ~LEAF_BIT]]) * kCostPrim;
+        for (int i = 1; i < 8; i++)
+          cc[k][i] = c;
+      } else {
+        for (int i = 1; i < 8; i++)
+          cc[k][i] = __ldcg(cost + (size_t)r * 7 + (i - 1));
+      }
+    }
+    float D[9];
+    uint32_t kBest[9];
+    for (int j = 2; j <= 8; j++) {
+      float best = 3.4e38f;
+      uint32_t bk = 1;
+      for (int k = 1; k < j; k++) {
+        const float c = cc[0][min(k, 7)] + cc[1][min(j - k, 7)];
+        if (c < best) {
+          best = c;
+          bk = (uint32_t)k;
+        }
+      }
+      D[j] = best;
+      kBest[j] = bk;
+    }
+    const float area = halfArea(loadBoxL2(internalBoxes + p));
+    const uint32_t cnt = __ldcg(internalCount + p);
+    float C = cnt <= (uint32_t)maxLeaf ? area * (float)cnt * kCostPrim
+                                       : area * kCostNode + D[8];
+    uint32_t d = (kBest[8] | 8u) << (4 * 6);
+    cost[(size_t)p * 7] = C;
+    for (int i = 2; i <= 7; i++) {
+      const bool takeD = D[i] < C;
+      if (takeD)
+        C = D[i];
+      d |= (kBest[i] | (takeD ? 8u : 0u)) << (4 * (i - 2));
+      cost[(size_t)p * 7 + (i - 1)] = C;
+    }
+    dec[p] = d;
+    p = parentInternal[p];
+  }
+}
+
 // --- collapse to BVH8 -------------------------------------------------------
 
 struct CollapseArgs
@@ -244,6 +347,7 @@ struct CollapseArgs
   uint32_t numTasks;
   uint2 *tasksOut;
   int maxLeaf;
+  const uint32_t *dec; // SAH choices (null: largest-area opening)
 };
 
 __device__ __forceinline__ box3 refBox(const CollapseArgs &a, uint32_t r)
@@ -284,12 +388,43 @@ __global__ void k_collapse(CollapseArgs a)
   if (task.x & LEAF_BIT) {
     c[0] = task.x;
     nc = 1;
+  } else if (a.dec) {
+    // the SAH choices: distribute 8 slots over the subtree; a binary node
+    // given j >= 2 slots splits per its decision for j (falling back to
+    // fewer slots where that is cheaper), given 1 it becomes one child
+    uint32_t ref[8];
+    int slots[8];
+    int sp = 0;
+    nc = 0;
+    const uint32_t k8 = decSplit(a.dec[task.x], 8);
+    ref[sp] = a.right[task.x];
+    slots[sp++] = 8 - (int)k8;
+    ref[sp] = a.left[task.x];
+    slots[sp++] = (int)k8;
+    while (sp > 0 && nc < 8) {
+      const uint32_t m = ref[--sp];
+      int j = slots[sp];
+      if (!(m & LEAF_BIT)) {
+        const uint32_t dm = a.dec[m];
+        while (j >= 2 && !decTakesD(dm, j))
+          j--;
+        if (j >= 2 && sp + 2 <= 8) {
+          const int kk = (int)decSplit(dm, j);
+          ref[sp] = a.right[m];
+          slots[sp++] = j - kk;
+          ref[sp] = a.left[m];
+          slots[sp++] = kk;
+          continue;
+        }
+      }
+      c[nc++] = m;
+    }
   } else {
     c[0] = a.left[task.x];
     c[1] = a.right[task.x];
     nc = 2;
   }
-  while (nc < 8) {
+  while (!a.dec && nc < 8) {
     int best = -1;
     float bestA = -1.f;
     for (int i = 0; i < nc; i++) {
@@ -474,6 +609,8 @@ cudaError_t buildBVH8(const box3 *d_boxes,
   uint32_t *left = nullptr, *right = nullptr, *parI = nullptr, *parL = nullptr;
   box3 *iBoxes = nullptr;
   uint32_t *iCount = nullptr, *flags = nullptr, *counters = nullptr;
+  float *sahCost = nullptr;
+  uint32_t *sahDec = nullptr;
   uint2 *tasksA = nullptr, *tasksB = nullptr;
   box3 hostAll;
   uint32_t hostCounters[3];
@@ -531,6 +668,24 @@ cudaError_t buildBVH8(const box3 *d_boxes,
         iBoxes,
         iCount,
         flags);
+    if (VRTX_BVH_SAH) {
+      VRTX_TRY(dalloc(&sahCost, (size_t)n * 7, stream));
+      VRTX_TRY(dalloc(&sahDec, n, stream));
+      VRTX_TRY(cudaMemsetAsync(flags, 0, sizeof(uint32_t) * n, stream));
+      k_sahCosts<<<(n + T - 1) / T, T, 0, stream>>>((int)n,
+          valsSorted,
+          d_boxes,
+          left,
+          right,
+          parI,
+          parL,
+          iBoxes,
+          iCount,
+          maxLeafPrims,
+          sahCost,
+          sahDec,
+          flags);
+    }
   }
 
   VRTX_TRY(dalloc(&out.nodes, n, stream));
@@ -569,6 +724,7 @@ cudaError_t buildBVH8(const box3 *d_boxes,
       ca.numTasks = numTasks;
       ca.tasksOut = tasksB;
       ca.maxLeaf = maxLeafPrims;
+      ca.dec = sahDec;
       k_collapse<<<(numTasks + 127) / 128, 128, 0, stream>>>(ca);
       VRTX_TRY(cudaMemcpyAsync(hostCounters,
           counters,
@@ -605,6 +761,8 @@ fail:
   cudaFreeAsync(iBoxes, stream);
   cudaFreeAsync(iCount, stream);
   cudaFreeAsync(flags, stream);
+  cudaFreeAsync(sahCost, stream);
+  cudaFreeAsync(sahDec, stream);
   cudaFreeAsync(counters, stream);
   cudaFreeAsync(tasksA, stream);
   cudaFreeAsync(tasksB, stream);
