@@ -807,3 +807,49 @@ def test_pbr_parameters_from_attributes_and_samplers(device, renderer):
     hit = g["depth"] < 1e29
     assert anari.rgba8(g["color"])[..., :3][hit].std() > 5.0
     print(renderer, rep)
+
+
+def test_objects_from_many_threads(device):
+    """Objects created, set and committed from eight host threads at once
+    (the reference's TestMultiThreadedObjectCreation): every handle is valid
+    and the frame built from them renders as a single-threaded build does."""
+    import threading
+
+    from visrtx_gb300 import anari
+
+    spec = soup("raycast", n=2000, w=48, h=32)
+    base = render_gpu(device, spec)
+    made, errors = [], []
+
+    def work(k):
+        try:
+            for i in range(25):
+                g = device.new_geometry("sphere")
+                a = device.new_array(np.random.default_rng(k * 100 + i).random((8, 3))
+                                     .astype(np.float32), L.FLOAT32_VEC3)
+                g.set("vertex.position", a)
+                g.commit()
+                m = device.new_material("matte")
+                m.commit()
+                sf = device.new_surface()
+                sf.set("geometry", g).set("material", m)
+                sf.commit()
+                made.append((g, a, m, sf))
+        except Exception as e:  # noqa: BLE001
+            errors.append(repr(e))
+
+    threads = [threading.Thread(target=work, args=(k,)) for k in range(8)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    assert not errors, errors
+    assert len(made) == 200 and all(o.handle.value for quad in made for o in quad)
+    again = render_gpu(device, spec)
+    for ch in ("color", "depth", "primitiveId"):
+        assert np.array_equal(base[ch], again[ch]), ch
+    for quad in made:
+        for o in quad:
+            o.release()
+    assert not device.errors()
+    del anari
