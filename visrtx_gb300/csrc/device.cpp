@@ -4,7 +4,7 @@
 // array/, camera/, frame/Frame.cu, renderer/Renderer.cpp, scene/) for the
 // hot path: same subtypes, parameter names, defaults and error behaviour
 // (status callback, null handles, skipped renders), with OptiX replaced by
-// the kernels of bvh.cu / scene.cu / render.cu.
+// the kernels of bvh.cu, scene.cu and the render*.cu units.
 #include <algorithm>
 #include <array>
 #include <chrono>

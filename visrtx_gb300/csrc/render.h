@@ -5,7 +5,7 @@
 
 namespace vrtx {
 
-// integrator (render.cu)
+// integrators (render.cu dispatches every per-pixel launch)
 int renderOccupancyBlocks(int rendererType, bool stats, bool surfaces, bool nanovdb);
 // the counting build of the per-pixel kernels for worlds with surfaces
 // (render_counting.cu): launches, or with occ set reports blocks per SM
