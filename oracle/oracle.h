@@ -15,7 +15,10 @@
  * arithmetic at its boundary is pinned separately: Philox4x32-10 against the
  * SC'11 paper's algorithm and against curand outputs captured on the GPU,
  * and the texture-filter emulation against tex1D/tex3D outputs captured on
- * the GPU (tests/golden/).
+ * the GPU (tests/golden/). NanoVDB field sampling is pinned to the NanoVDB
+ * library the reference vendors (external/nanovdb): its builder made the
+ * golden grids and its sampler the golden values, which the reader here
+ * reproduces bit for bit (oracle/ref_nvdb.cpp, tests/golden/nvdb_golden.npz).
  */
 #ifndef VRTX_ORACLE_H
 #define VRTX_ORACLE_H
