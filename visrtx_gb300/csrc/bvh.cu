@@ -344,8 +344,10 @@ struct CollapseArgs
   uint32_t *primOrder;
   uint32_t *counters; // [0] nodes, [1] prims, [2] out tasks
   const uint2 *tasksIn;
-  uint32_t numTasks;
+  const uint32_t *numTasks; // this level's task count (device)
+  uint32_t capacity; // tasks a level can hold
   uint2 *tasksOut;
+  uint32_t *numTasksOut; // the next level's task count (device)
   int maxLeaf;
   const uint32_t *dec; // SAH choices (null: largest-area opening)
 };
@@ -375,11 +377,8 @@ __device__ __forceinline__ uint32_t quantExp(float lo, float hi)
   return min(max(e, 1u), 254u);
 }
 
-__global__ void k_collapse(CollapseArgs a)
+__device__ __forceinline__ void collapseTask(const CollapseArgs &a, uint32_t tid)
 {
-  const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
-  if (tid >= a.numTasks)
-    return;
   const uint2 task = a.tasksIn[tid];
   const uint32_t nodeIdx = task.y;
 
@@ -499,7 +498,7 @@ __global__ void k_collapse(CollapseArgs a)
   const uint32_t primBase =
       numLeafPrims ? atomicAdd(&a.counters[1], (uint32_t)numLeafPrims) : 0u;
   const uint32_t taskBase =
-      numInternal ? atomicAdd(&a.counters[2], (uint32_t)numInternal) : 0u;
+      numInternal ? atomicAdd(a.numTasksOut, (uint32_t)numInternal) : 0u;
 
   BVH8Node node;
   node.px = nb.lo.x;
@@ -566,6 +565,16 @@ __global__ void k_collapse(CollapseArgs a)
   a.nodes[nodeIdx] = node;
 }
 
+// One level of the collapse: the task count comes from the device, so levels
+// are queued without a host round trip (grid-stride over the tasks).
+__global__ void k_collapse(CollapseArgs a)
+{
+  const uint32_t num = min(*a.numTasks, a.capacity);
+  for (uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x; tid < num;
+       tid += gridDim.x * blockDim.x)
+    collapseTask(a, tid);
+}
+
 __global__ void k_iota(uint32_t *v, uint32_t n)
 {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -613,7 +622,7 @@ cudaError_t buildBVH8(const box3 *d_boxes,
   uint32_t *sahDec = nullptr;
   uint2 *tasksA = nullptr, *tasksB = nullptr;
   box3 hostAll;
-  uint32_t hostCounters[3];
+  uint32_t hostCounters[4];
 
   VRTX_TRY(dalloc(&pCent, nbPartial, stream));
   VRTX_TRY(dalloc(&pAll, nbPartial, stream));
@@ -694,49 +703,59 @@ cudaError_t buildBVH8(const box3 *d_boxes,
   VRTX_TRY(dalloc(&tasksA, n, stream));
   VRTX_TRY(dalloc(&tasksB, n, stream));
   {
-    // root task: binary root -> BVH8 node 0
+    // root task: binary root -> BVH8 node 0; counters: [0] nodes, [1] prims,
+    // [2] and [3] the task counts of alternate levels
     const uint2 root = make_uint2(n > 1 ? 0u : LEAF_BIT, 0u);
-    const uint32_t init[4] = {1u, 0u, 0u, 0u};
+    const uint32_t init[4] = {1u, 0u, 1u, 0u};
     VRTX_TRY(cudaMemcpyAsync(
         tasksA, &root, sizeof(uint2), cudaMemcpyHostToDevice, stream));
     VRTX_TRY(cudaMemcpyAsync(
         counters, init, sizeof(init), cudaMemcpyHostToDevice, stream));
-    VRTX_TRY(cudaStreamSynchronize(stream));
   }
   {
-    uint32_t numTasks = 1;
-    for (int level = 0; numTasks > 0; level++) {
-      if (level > 512 || numTasks > n) {
+    // levels in batches of 8 between host checks of the task count
+    const uint32_t grid = (uint32_t)std::min<size_t>((n + 127) / 128, 2048);
+    int level = 0;
+    while (true) {
+      for (int b = 0; b < 8; b++, level++) {
+        uint32_t *in = counters + 2 + (level & 1);
+        uint32_t *outCount = counters + 2 + ((level + 1) & 1);
+        VRTX_TRY(cudaMemsetAsync(outCount, 0, sizeof(uint32_t), stream));
+        CollapseArgs ca;
+        ca.left = left;
+        ca.right = right;
+        ca.internalCount = iCount;
+        ca.internalBoxes = iBoxes;
+        ca.boxes = d_boxes;
+        ca.sortedIdx = valsSorted;
+        ca.nodes = out.nodes;
+        ca.primOrder = out.primOrder;
+        ca.counters = counters;
+        ca.tasksIn = tasksA;
+        ca.numTasks = in;
+        ca.capacity = (uint32_t)n;
+        ca.tasksOut = tasksB;
+        ca.numTasksOut = outCount;
+        ca.maxLeaf = maxLeafPrims;
+        ca.dec = sahDec;
+        k_collapse<<<grid, 128, 0, stream>>>(ca);
+        uint2 *t = tasksA;
+        tasksA = tasksB;
+        tasksB = t;
+      }
+      VRTX_TRY(cudaMemcpyAsync(hostCounters,
+          counters,
+          sizeof(uint32_t) * 4,
+          cudaMemcpyDeviceToHost,
+          stream));
+      VRTX_TRY(cudaStreamSynchronize(stream));
+      const uint32_t pending = hostCounters[2 + (level & 1)];
+      if (pending == 0)
+        break;
+      if (level > 512 || pending > n) {
         err = cudaErrorUnknown; // a radix tree over n keys is shallower
         goto fail;
       }
-      CollapseArgs ca;
-      ca.left = left;
-      ca.right = right;
-      ca.internalCount = iCount;
-      ca.internalBoxes = iBoxes;
-      ca.boxes = d_boxes;
-      ca.sortedIdx = valsSorted;
-      ca.nodes = out.nodes;
-      ca.primOrder = out.primOrder;
-      ca.counters = counters;
-      ca.tasksIn = tasksA;
-      ca.numTasks = numTasks;
-      ca.tasksOut = tasksB;
-      ca.maxLeaf = maxLeafPrims;
-      ca.dec = sahDec;
-      k_collapse<<<(numTasks + 127) / 128, 128, 0, stream>>>(ca);
-      VRTX_TRY(cudaMemcpyAsync(hostCounters,
-          counters,
-          sizeof(uint32_t) * 3,
-          cudaMemcpyDeviceToHost,
-          stream));
-      VRTX_TRY(cudaMemsetAsync(counters + 2, 0, sizeof(uint32_t), stream));
-      VRTX_TRY(cudaStreamSynchronize(stream));
-      numTasks = hostCounters[2];
-      uint2 *t = tasksA;
-      tasksA = tasksB;
-      tasksB = t;
     }
   }
   VRTX_TRY(cudaMemcpyAsync(
