@@ -656,16 +656,23 @@ def build_on_device(dev, spec: SceneSpec, channels=("color", "depth", "primitive
 
     world = dev.new_world()
     insts = []
+    # instances of the same surfaces share one group (one BLAS, as ANARI
+    # instancing is meant to be used)
+    groups = {}
     for ins in spec.instances:
         members = [surfs[i] for i in ins.surfaces]
         if ins.zero:
             if members:
                 world.set("surface", arr(members))
             continue
-        grp = dev.new_group()
-        if members:
-            grp.set("surface", arr(members))
-        grp.commit()
+        key = tuple(ins.surfaces)
+        grp = groups.get(key)
+        if grp is None:
+            grp = dev.new_group()
+            if members:
+                grp.set("surface", arr(members))
+            grp.commit()
+            groups[key] = grp
         inst = dev.new_instance("transform")
         inst.set("group", grp)
         inst.set("transform", np.asarray(ins.xfm, np.float32), L.FLOAT32_MAT4)
