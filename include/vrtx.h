@@ -51,6 +51,7 @@ typedef enum VRTXDataType {
   VRTX_BOOL = 3,
   VRTX_FUNCTION_POINTER = 4, /* frameCompletionCallback */
   VRTX_MEMORY_DELETER = 5,
+  VRTX_STRING_LIST = 6, /* const char *const *, NULL-terminated */
 
   VRTX_OBJECT = 100,
   VRTX_ARRAY1D = 101,
@@ -69,6 +70,7 @@ typedef enum VRTXDataType {
   VRTX_SPATIAL_FIELD = 114,
   VRTX_VOLUME = 115,
   VRTX_WORLD = 116,
+  VRTX_DEVICE = 117, /* object type of the device itself (feature queries) */
 
   VRTX_INT32 = 200,
   VRTX_INT32_VEC2 = 201,
@@ -152,7 +154,8 @@ VRTX_API void vrtxDeviceCommitParameters(VRTXDevice d);
 /* Releases the device and every object it still owns. */
 VRTX_API void vrtxDeviceRelease(VRTXDevice d);
 
-/* Device properties ("version", "visrtx", "extension"); replaces
+/* Device properties ("version": INT32, "visrtx": BOOL, "extension":
+ * STRING_LIST, written as one const char *const * pointer); replaces
  * VisRTXDevice::deviceGetProperty (VisRTXDevice.cpp:520-552). Returns 1 when
  * the property was written. */
 VRTX_API int vrtxDeviceGetProperty(VRTXDevice d,
@@ -164,6 +167,40 @@ VRTX_API int vrtxDeviceGetProperty(VRTXDevice d,
 
 /* 1 when the build has a usable CUDA device, 0 otherwise (after init). */
 VRTX_API int vrtxDeviceIsValid(VRTXDevice d);
+
+/* ------------------------------------------------------------------------ */
+/* Feature queries                                                          */
+/* ------------------------------------------------------------------------ */
+
+/* The subtypes this library creates for an object type (VRTX_CAMERA ...
+ * VRTX_VOLUME), as a static NULL-terminated list; NULL for types without
+ * subtypes. Replaces VisRTXDevice::getObjectSubtypes
+ * (VisRTXDevice.cpp:296-299). */
+VRTX_API const char *const *vrtxGetObjectSubtypes(VRTXDevice d, int objectType);
+
+/* The reference's extension flags (visrtx.h:55-64), one int per feature. */
+typedef struct VRTXExtensions {
+  int VISRTX_ARRAY_CUDA;
+  int VISRTX_CUDA_OUTPUT_BUFFERS;
+  int VISRTX_INSTANCE_ATTRIBUTES;
+  int VISRTX_MATERIAL_MDL;
+  int VISRTX_SPATIAL_FIELD_NANOVDB;
+  int VISRTX_TRIANGLE_BACK_FACE_CULLING;
+  int VISRTX_TRIANGLE_FACE_VARYING_ATTRIBUTES;
+} VRTXExtensions;
+
+/* Fill *ext from the features of one object subtype; returns 1 when the
+ * subtype is known, else 0 (ext untouched). Replaces
+ * visrtxGetObjectExtensions (VisRTXFeatureUtility.cpp:66-80). */
+VRTX_API int vrtxGetObjectExtensions(
+    VRTXExtensions *ext, VRTXDevice d, int objectType, const char *subtype);
+
+/* Fill *ext from the device's "extension" list; returns 1 on success.
+ * object: the device itself (NULL) -- the reference reads the property of
+ * the object it is given, and only the device has one. Replaces
+ * visrtxGetInstanceExtensions (VisRTXFeatureUtility.cpp:82-99). */
+VRTX_API int vrtxGetInstanceExtensions(
+    VRTXExtensions *ext, VRTXDevice d, VRTXObject object);
 
 /* ------------------------------------------------------------------------ */
 /* Arrays                                                                   */

@@ -71,3 +71,36 @@ def test_dm_rejects_invalid_arguments(built):
     assert rc < 0
     assert dev.errors()
     dev.release()
+
+
+def test_feature_queries(built):
+    """Subtype lists, the device's extension list and the extension flags of
+    VisRTXFeatureUtility.cpp: host-only queries, answered without a GPU."""
+    from visrtx_gb300 import _lib as L
+    from visrtx_gb300 import anari
+
+    dev = anari.Device(0)
+    ext = dev.extensions()
+    assert "ANARI_KHR_SPATIAL_FIELD_NANOVDB" in ext and "ANARI_NV_ARRAY_CUDA" in ext
+    assert "ANARI_KHR_GEOMETRY_CURVE" in ext and len(ext) == len(set(ext))
+    assert dev.object_subtypes(L.GEOMETRY) == ["triangle", "quad", "sphere", "cylinder",
+                                               "cone", "curve"]
+    assert "nanovdb" in dev.object_subtypes(L.SPATIAL_FIELD)
+    assert "physicallyBased" in dev.object_subtypes(L.MATERIAL)
+    assert dev.object_subtypes(L.SURFACE) == [] and dev.object_subtypes(12345) == []
+    flags = dev.instance_extensions()
+    assert flags["VISRTX_ARRAY_CUDA"] and flags["VISRTX_CUDA_OUTPUT_BUFFERS"]
+    assert flags["VISRTX_SPATIAL_FIELD_NANOVDB"] and flags["VISRTX_TRIANGLE_BACK_FACE_CULLING"]
+    assert not flags["VISRTX_MATERIAL_MDL"] and not flags["VISRTX_INSTANCE_ATTRIBUTES"]
+    assert not flags["VISRTX_TRIANGLE_FACE_VARYING_ATTRIBUTES"]
+    tri = dev.object_extensions(L.GEOMETRY, "triangle")
+    assert tri["VISRTX_TRIANGLE_BACK_FACE_CULLING"] and not tri["VISRTX_ARRAY_CUDA"]
+    assert dev.object_extensions(L.SPATIAL_FIELD, "nanovdb")["VISRTX_SPATIAL_FIELD_NANOVDB"]
+    assert not any(dev.object_extensions(L.GEOMETRY, "sphere").values())
+    assert dev.object_extensions(L.GEOMETRY, "neural") is None
+    assert dev.object_extensions(L.DEVICE, "") == flags
+    # the reference reads the property of the object it is given: only the
+    # device carries one
+    e = L.VRTXExtensions()
+    assert dev.lib.vrtxGetInstanceExtensions(C.byref(e), dev.h, C.c_void_p(1)) == 0
+    dev.release()

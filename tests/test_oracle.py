@@ -67,7 +67,8 @@ def test_texture_golden_if_present():
         got = O.tex3d(vox, c, d["round_mode"])
         worst = max(worst, abs(got - want))
     # 3D: the per-axis 8-bit-weight emulation stays within the recorded bound
-    # (it does not reproduce the hardware exactly)
+    # (the hardware's 3D weights were not recovered exactly: the emulation is
+    # within 0.0086 of it, which is why volume parity carries a tolerance)
     assert worst <= d["tolerance"] and d["tolerance"] < 0.01
     # 1D float4 (the TF path): round-to-nearest 8-bit weights match exactly
     t1 = d["tex1"]

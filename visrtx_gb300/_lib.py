@@ -18,10 +18,12 @@ STRING = 1
 VOID_POINTER = 2
 BOOL = 3
 FUNCTION_POINTER = 4
+STRING_LIST = 6
 OBJECT = 100
 ARRAY1D, ARRAY2D, ARRAY3D = 101, 102, 103
 CAMERA, FRAME, GEOMETRY, GROUP, INSTANCE, LIGHT, MATERIAL, RENDERER = range(104, 112)
 SURFACE, SAMPLER, SPATIAL_FIELD, VOLUME, WORLD = range(112, 117)
+DEVICE = 117
 INT32, INT32_VEC2, INT8, UINT8 = 200, 201, 202, 203
 UINT32, UINT32_VEC2, UINT32_VEC3, UINT32_VEC4 = 210, 211, 212, 213
 UINT64 = 214
@@ -51,6 +53,9 @@ SIGNATURES = {
     "vrtxDeviceGetProperty": (C.c_int, [C.c_void_p, C.c_char_p, C.c_int, C.c_void_p,
                                         C.c_uint64, C.c_uint32]),
     "vrtxDeviceIsValid": (C.c_int, [C.c_void_p]),
+    "vrtxGetObjectSubtypes": (C.POINTER(C.c_char_p), [C.c_void_p, C.c_int]),
+    "vrtxGetObjectExtensions": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_char_p]),
+    "vrtxGetInstanceExtensions": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "vrtxNewArray1D": (C.c_void_p, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                     C.c_int, C.c_uint64]),
     "vrtxNewArray2D": (C.c_void_p, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
@@ -109,6 +114,17 @@ SIGNATURES = {
 
 
 DM_PLAIN = 1  # VRTX_DM_PLAIN
+
+
+class VRTXExtensions(C.Structure):
+    """The extension flags of include/vrtx.h (one int per feature)."""
+    _fields_ = [(n, C.c_int) for n in (
+        "VISRTX_ARRAY_CUDA", "VISRTX_CUDA_OUTPUT_BUFFERS", "VISRTX_INSTANCE_ATTRIBUTES",
+        "VISRTX_MATERIAL_MDL", "VISRTX_SPATIAL_FIELD_NANOVDB",
+        "VISRTX_TRIANGLE_BACK_FACE_CULLING", "VISRTX_TRIANGLE_FACE_VARYING_ATTRIBUTES")]
+
+    def as_dict(self) -> dict[str, bool]:
+        return {n: bool(getattr(self, n)) for n, _ in self._fields_}
 
 
 class VRTXDMVolume(C.Structure):

@@ -181,6 +181,42 @@ class Device:
     def stream(self) -> int:
         return self.lib.vrtxDeviceStream(self.h) or 0
 
+    # feature queries (VisRTXDevice::getObjectSubtypes, VisRTXFeatureUtility.cpp)
+    @staticmethod
+    def _strings(p) -> list[str]:
+        out = []
+        i = 0
+        while p and p[i] is not None:
+            out.append(p[i].decode())
+            i += 1
+        return out
+
+    def extensions(self) -> list[str]:
+        """The device's "extension" property."""
+        p = C.POINTER(C.c_char_p)()
+        if not self.lib.vrtxDeviceGetProperty(self.h, b"extension", L.STRING_LIST,
+                                              C.byref(p), C.sizeof(p), L.WAIT):
+            return []
+        return self._strings(p)
+
+    def object_subtypes(self, object_type: int) -> list[str]:
+        return self._strings(self.lib.vrtxGetObjectSubtypes(self.h, object_type))
+
+    def object_extensions(self, object_type: int, subtype: str) -> dict[str, bool] | None:
+        """visrtxGetObjectExtensions: the flags of one subtype, None if unknown."""
+        e = L.VRTXExtensions()
+        if not self.lib.vrtxGetObjectExtensions(C.byref(e), self.h, object_type,
+                                                subtype.encode()):
+            return None
+        return e.as_dict()
+
+    def instance_extensions(self) -> dict[str, bool] | None:
+        """visrtxGetInstanceExtensions on the device."""
+        e = L.VRTXExtensions()
+        if not self.lib.vrtxGetInstanceExtensions(C.byref(e), self.h, None):
+            return None
+        return e.as_dict()
+
     # arrays -----------------------------------------------------------------
     def new_array(self, data, elem_type: int | None = None) -> Array:
         """1D/2D/3D array. `data` is a numpy array (shared with the library

@@ -3258,6 +3258,49 @@ VRTX_API void vrtxDeviceRelease(VRTXDevice d)
   delete dev;
 }
 
+// The extensions this library implements, named as the reference's device
+// declares them (visrtx_device.json "dependencies", upper-cased with the
+// ANARI_ prefix). Left out: array regions, compressed samplers, instance and
+// face-varying attributes, MDL materials, neural geometry.
+static const char *const kDeviceExtensions[] = {"ANARI_KHR_CAMERA_DEPTH_OF_FIELD",
+    "ANARI_KHR_CAMERA_ORTHOGRAPHIC",
+    "ANARI_KHR_CAMERA_PERSPECTIVE",
+    "ANARI_KHR_DEVICE_SYNCHRONIZATION",
+    "ANARI_KHR_FRAME_ACCUMULATION",
+    "ANARI_KHR_FRAME_CHANNEL_PRIMITIVE_ID",
+    "ANARI_KHR_FRAME_CHANNEL_OBJECT_ID",
+    "ANARI_KHR_FRAME_CHANNEL_INSTANCE_ID",
+    "ANARI_KHR_FRAME_COMPLETION_CALLBACK",
+    "ANARI_KHR_GEOMETRY_CONE",
+    "ANARI_KHR_GEOMETRY_CURVE",
+    "ANARI_KHR_GEOMETRY_CYLINDER",
+    "ANARI_KHR_GEOMETRY_QUAD",
+    "ANARI_KHR_GEOMETRY_SPHERE",
+    "ANARI_KHR_GEOMETRY_TRIANGLE",
+    "ANARI_KHR_INSTANCE_TRANSFORM",
+    "ANARI_KHR_INSTANCE_TRANSFORM_ARRAY",
+    "ANARI_KHR_LIGHT_DIRECTIONAL",
+    "ANARI_KHR_LIGHT_HDRI",
+    "ANARI_KHR_LIGHT_POINT",
+    "ANARI_KHR_LIGHT_SPOT",
+    "ANARI_KHR_MATERIAL_MATTE",
+    "ANARI_KHR_MATERIAL_PHYSICALLY_BASED",
+    "ANARI_KHR_RENDERER_AMBIENT_LIGHT",
+    "ANARI_KHR_RENDERER_BACKGROUND_COLOR",
+    "ANARI_KHR_RENDERER_BACKGROUND_IMAGE",
+    "ANARI_KHR_SAMPLER_IMAGE1D",
+    "ANARI_KHR_SAMPLER_IMAGE2D",
+    "ANARI_KHR_SAMPLER_IMAGE3D",
+    "ANARI_KHR_SAMPLER_PRIMITIVE",
+    "ANARI_KHR_SAMPLER_TRANSFORM",
+    "ANARI_KHR_SPATIAL_FIELD_NANOVDB",
+    "ANARI_KHR_SPATIAL_FIELD_STRUCTURED_REGULAR",
+    "ANARI_KHR_VOLUME_TRANSFER_FUNCTION1D",
+    "ANARI_NV_ARRAY_CUDA",
+    "ANARI_NV_FRAME_BUFFERS_CUDA",
+    "ANARI_VISRTX_TRIANGLE_BACK_FACE_CULLING",
+    nullptr};
+
 VRTX_API int vrtxDeviceGetProperty(VRTXDevice d,
     const char *name,
     int type,
@@ -3284,7 +3327,128 @@ VRTX_API int vrtxDeviceGetProperty(VRTXDevice d,
     std::memcpy(mem, &v, 4);
     return 1;
   }
+  if (n == "extension" && type == VRTX_STRING_LIST && size >= sizeof(void *)) {
+    const char *const *list = kDeviceExtensions;
+    std::memcpy(mem, &list, sizeof(list));
+    return 1;
+  }
   return 0;
+}
+
+// Subtype lists per object type: what the constructors above accept (the
+// reference's generated query_object_types lists, VisRTXDevice.cpp:80-92,
+// for the subtypes this library implements).
+static const char *const kCameraSubtypes[] = {"perspective", "orthographic", nullptr};
+static const char *const kGeometrySubtypes[] = {
+    "triangle", "quad", "sphere", "cylinder", "cone", "curve", nullptr};
+static const char *const kLightSubtypes[] = {"directional", "point", "spot", "hdri", nullptr};
+static const char *const kMaterialSubtypes[] = {"matte", "physicallyBased", nullptr};
+static const char *const kRendererSubtypes[] = {
+    "default", "directLight", "raycast", "ao", "dpt", "diffuse_pathtracer", nullptr};
+static const char *const kSamplerSubtypes[] = {
+    "image1D", "image2D", "image3D", "primitive", "transform", nullptr};
+static const char *const kFieldSubtypes[] = {"structuredRegular", "nanovdb", nullptr};
+static const char *const kVolumeSubtypes[] = {"transferFunction1D", "scivis", nullptr};
+static const char *const kInstanceSubtypes[] = {"transform", nullptr};
+
+VRTX_API const char *const *vrtxGetObjectSubtypes(VRTXDevice, int objectType)
+{
+  switch (objectType) {
+  case VRTX_CAMERA:
+    return kCameraSubtypes;
+  case VRTX_GEOMETRY:
+    return kGeometrySubtypes;
+  case VRTX_LIGHT:
+    return kLightSubtypes;
+  case VRTX_MATERIAL:
+    return kMaterialSubtypes;
+  case VRTX_RENDERER:
+    return kRendererSubtypes;
+  case VRTX_SAMPLER:
+    return kSamplerSubtypes;
+  case VRTX_SPATIAL_FIELD:
+    return kFieldSubtypes;
+  case VRTX_VOLUME:
+    return kVolumeSubtypes;
+  case VRTX_INSTANCE:
+    return kInstanceSubtypes;
+  default:
+    return nullptr;
+  }
+}
+
+static bool inList(const char *const *list, const char *s)
+{
+  for (; list && *list; ++list)
+    if (std::strcmp(*list, s) == 0)
+      return true;
+  return false;
+}
+
+// Sets the flags named by a feature list, as fillExtensionStruct does
+// (VisRTXFeatureUtility.cpp:39-64). The reference's flags spell three
+// features with a VISRTX prefix that its device declares under their ANARI
+// names (NV_ARRAY_CUDA, NV_FRAME_BUFFERS_CUDA, KHR_SPATIAL_FIELD_NANOVDB):
+// both spellings set the flag. MDL is never available here.
+static void fillExtensions(VRTXExtensions *ext, const char *const *list)
+{
+  std::memset(ext, 0, sizeof(*ext));
+  auto has = [&](const char *a, const char *b) {
+    return inList(list, a) || (b && inList(list, b));
+  };
+  ext->VISRTX_ARRAY_CUDA = has("ANARI_VISRTX_ARRAY_CUDA", "ANARI_NV_ARRAY_CUDA");
+  ext->VISRTX_CUDA_OUTPUT_BUFFERS =
+      has("ANARI_VISRTX_CUDA_OUTPUT_BUFFERS", "ANARI_NV_FRAME_BUFFERS_CUDA");
+  ext->VISRTX_INSTANCE_ATTRIBUTES = has("ANARI_VISRTX_INSTANCE_ATTRIBUTES", nullptr);
+  ext->VISRTX_SPATIAL_FIELD_NANOVDB =
+      has("ANARI_VISRTX_SPATIAL_FIELD_NANOVDB", "ANARI_KHR_SPATIAL_FIELD_NANOVDB");
+  ext->VISRTX_TRIANGLE_BACK_FACE_CULLING =
+      has("ANARI_VISRTX_TRIANGLE_BACK_FACE_CULLING", nullptr);
+  ext->VISRTX_TRIANGLE_FACE_VARYING_ATTRIBUTES =
+      has("ANARI_VISRTX_TRIANGLE_FACE_VARYING_ATTRIBUTES", nullptr);
+  ext->VISRTX_MATERIAL_MDL = 0;
+}
+
+// Per-subtype features: the device's whole list for the objects that
+// declare extensions in the reference (the triangle's back-face culling, the
+// NanoVDB field, the device-pointer arrays and frame channels), else an
+// empty list.
+static const char *const kTriangleFeatures[] = {
+    "ANARI_KHR_GEOMETRY_TRIANGLE", "ANARI_VISRTX_TRIANGLE_BACK_FACE_CULLING", nullptr};
+static const char *const kNanovdbFeatures[] = {"ANARI_KHR_SPATIAL_FIELD_NANOVDB", nullptr};
+static const char *const kNoFeatures[] = {nullptr};
+
+VRTX_API int vrtxGetObjectExtensions(
+    VRTXExtensions *ext, VRTXDevice d, int objectType, const char *subtype)
+{
+  if (!ext || !subtype)
+    return 0;
+  const char *const *list = nullptr;
+  if (objectType == VRTX_DEVICE)
+    list = kDeviceExtensions;
+  else if (inList(vrtxGetObjectSubtypes(d, objectType), subtype)) {
+    if (objectType == VRTX_GEOMETRY && std::strcmp(subtype, "triangle") == 0)
+      list = kTriangleFeatures;
+    else if (objectType == VRTX_SPATIAL_FIELD && std::strcmp(subtype, "nanovdb") == 0)
+      list = kNanovdbFeatures;
+    else
+      list = kNoFeatures;
+  }
+  if (!list)
+    return 0;
+  fillExtensions(ext, list);
+  return 1;
+}
+
+VRTX_API int vrtxGetInstanceExtensions(VRTXExtensions *ext, VRTXDevice d, VRTXObject o)
+{
+  if (!ext || !d || o)
+    return 0; // only the device carries an "extension" property
+  const char *const *list = nullptr;
+  if (!vrtxDeviceGetProperty(d, "extension", VRTX_STRING_LIST, &list, sizeof(list), 1))
+    return 0;
+  fillExtensions(ext, list);
+  return 1;
 }
 
 VRTX_API int vrtxDeviceIsValid(VRTXDevice d)
