@@ -1,0 +1,71 @@
+"""Frame-level behaviour through the C ABI (frame/Frame.cu:163-310,559-588):
+the completion callback, the duration / numSamples / nextFrameReset
+properties, frameReady polling, the sample limit and invalid frames."""
+import ctypes as C
+
+import pytest
+
+from visrtx_gb300 import _lib as L
+from visrtx_gb300 import scenes as S
+from tests.parity import render_gpu
+
+pytestmark = pytest.mark.gpu
+
+COMPLETION_CB = C.CFUNCTYPE(None, C.c_void_p, C.c_void_p, C.c_void_p)
+
+
+def test_completion_callback_and_frame_properties(device):
+    dev = device
+    spec = S.soup_spec(n=2000, width=64, height=48, renderer="raycast")
+    g = render_gpu(dev, spec)
+    f = g["frame"]
+    calls = []
+    cb = COMPLETION_CB(lambda user, d, fr: calls.append((user, d, fr)))
+    fp = C.c_void_p(C.cast(cb, C.c_void_p).value)
+    ud = C.c_void_p(4321)
+    dev.lib.vrtxSetParameter(dev.h, f.handle, b"frameCompletionCallback", L.FUNCTION_POINTER,
+                             C.byref(fp))
+    dev.lib.vrtxSetParameter(dev.h, f.handle, b"frameCompletionCallbackUserData",
+                             L.VOID_POINTER, C.byref(ud))
+    f.commit()
+    assert f.get_property("nextFrameReset", L.BOOL)  # the commit is a change
+    f.render()
+    f.wait()
+    assert f.ready()
+    # fired once, after the frame's work, from the stream (cudaLaunchHostFunc)
+    assert calls == [(4321, dev.h.value, f.handle.value)]
+    dur = f.get_property("duration", L.FLOAT32)
+    assert 0.0 < dur < 10.0
+    assert f.get_property("numSamples", L.INT32) == 1
+    assert not f.get_property("nextFrameReset", L.BOOL)
+    # raycast stops at its sample limit of 1: the next render does no work
+    # and fires no callback (Frame.cu:251-253 returns before the launch)
+    f.render()
+    f.wait()
+    assert len(calls) == 1
+    assert f.get_property("numSamples", L.INT32) == 1
+    # a camera change resets accumulation: the next render runs again
+    cam = g["frame"]._keep["camera"]
+    cam.set("fovy", 0.9)
+    cam.commit()
+    assert f.get_property("nextFrameReset", L.BOOL)
+    f.render()
+    f.wait()
+    assert len(calls) == 2
+    assert not dev.errors()
+
+
+def test_invalid_frame_is_skipped_with_an_error(device):
+    """A frame without a world renders nothing and reports an ERROR
+    (Frame.cu:216-234); frameReady answers at once."""
+    dev = device
+    spec = S.soup_spec(n=200, width=16, height=16, renderer="raycast")
+    g = render_gpu(dev, spec)
+    f = g["frame"]
+    f.unset("world")
+    f.commit()
+    n0 = len(dev.errors())
+    f.render()
+    assert f.ready()
+    errs = dev.errors()[n0:]
+    assert errs and any("ANARIWorld" in e for e in errs)

@@ -389,6 +389,24 @@ def test_orthographic(device):
     compare(g, r)
 
 
+@pytest.mark.parametrize("renderer", ["default", "raycast"])
+def test_depth_of_field(device, renderer):
+    """Thin-lens perspective camera (apertureRadius, focusDistance;
+    Perspective.cpp:40-72, cameraCreateRay.h:51-56): the lens sample uses the
+    third and fourth uniforms of the pixel's first draw. The lens offset goes
+    through sinf/cosf, whose last-ulp results may differ from the host's, so
+    a few edge pixels may change hands."""
+    spec = soup(renderer, n=5000, w=64, h=48)
+    spec.camera.aperture = 0.04
+    spec.camera.focus = 1.6
+    g = render_gpu(device, spec)
+    r = render_oracle(spec)
+    compare(g, r, allow_ids=4)
+    # the aperture blurs: the frame differs from the pinhole frame
+    spec.camera.aperture = 0.0
+    assert not np.array_equal(render_gpu(device, spec)["primitiveId"], g["primitiveId"])
+
+
 def test_world_bounds(device):
     spec = soup("raycast", n=1000, w=16, h=16)
     g = render_gpu(device, spec)
