@@ -36,13 +36,20 @@ def test_completion_callback_and_frame_properties(device):
     assert calls == [(4321, dev.h.value, f.handle.value)]
     dur = f.get_property("duration", L.FLOAT32)
     assert 0.0 < dur < 10.0
-    assert f.get_property("numSamples", L.INT32) == 1
+    # numSamples is the frame id of the last frame (Frame.cu:176-180): 0 for
+    # the first frame after a reset
+    assert f.get_property("numSamples", L.INT32) == 0
     assert not f.get_property("nextFrameReset", L.BOOL)
-    # raycast stops at its sample limit of 1: the next render does no work
-    # and fires no callback (Frame.cu:251-253 returns before the launch)
+    # raycast's sample limit is 1 and the limit is checked before the frame
+    # id advances (Frame.cu:251-253): the second frame (id 1) still renders,
+    # the third does no work and fires no callback
     f.render()
     f.wait()
-    assert len(calls) == 1
+    assert len(calls) == 2
+    assert f.get_property("numSamples", L.INT32) == 1
+    f.render()
+    f.wait()
+    assert len(calls) == 2
     assert f.get_property("numSamples", L.INT32) == 1
     # a camera change resets accumulation: the next render runs again
     cam = g["frame"]._keep["camera"]
@@ -51,7 +58,8 @@ def test_completion_callback_and_frame_properties(device):
     assert f.get_property("nextFrameReset", L.BOOL)
     f.render()
     f.wait()
-    assert len(calls) == 2
+    assert len(calls) == 3
+    assert f.get_property("numSamples", L.INT32) == 0
     assert not dev.errors()
 
 
