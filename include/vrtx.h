@@ -140,7 +140,11 @@ typedef void (*VRTXFrameCompletionCallback)(
 /* Replaces makeVisRTXDevice (VisRTXLibrary.cpp:76-80,
  * include/anari/ext/visrtx/visrtx.h:49-51). CUDA is initialised lazily on
  * the first object creation, as VisRTXDevice::initDevice does
- * (VisRTXDevice.cpp:435-458). Returns NULL only when out of host memory. */
+ * (VisRTXDevice.cpp:435-458). Returns NULL only when out of host memory.
+ * Every call that takes the device runs on its GPU ("cudaDevice") and
+ * leaves the calling thread's current CUDA device as it was
+ * (CUDADeviceScope, VisRTXDevice.cpp:790-814); objects may be created and
+ * used from any thread. */
 VRTX_API VRTXDevice vrtxNewDevice(
     VRTXStatusCallback statusCallback, const void *statusCallbackUserData);
 
@@ -354,7 +358,8 @@ VRTX_API void *vrtxDeviceStream(VRTXDevice d);
 /* rgb_k + T_end * background. Marching stops once T < 1e-3.                */
 /*                                                                          */
 /* All pointers are CUDA device pointers; work is queued on `stream` (a     */
-/* cudaStream_t, NULL = legacy default stream). One launch covers every    */
+/* cudaStream_t, NULL = legacy default stream) on the calling thread's     */
+/* current device, the one that owns the pointers. One launch covers every */
 /* view: views are cut into tiles that persistent blocks pull from a queue. */
 /* ------------------------------------------------------------------------ */
 

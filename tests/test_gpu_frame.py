@@ -77,3 +77,27 @@ def test_invalid_frame_is_skipped_with_an_error(device):
     assert f.ready()
     errs = dev.errors()[n0:]
     assert errs and any("ANARIWorld" in e for e in errs)
+
+
+def test_calls_keep_the_threads_current_device(built):
+    """Each call runs on the device's own GPU and restores the calling
+    thread's current device (CUDADeviceScope, VisRTXDevice.cpp:790-814).
+    Needs two GPUs: the library renders on GPU 1 while the thread stays on
+    GPU 0."""
+    torch = pytest.importorskip("torch")
+    if torch.cuda.device_count() < 2:
+        pytest.skip("needs two GPUs")
+    from visrtx_gb300 import anari
+
+    torch.cuda.set_device(0)
+    dev = anari.Device(1)
+    try:
+        spec = S.soup_spec(n=500, width=32, height=24, renderer="raycast")
+        g = render_gpu(dev, spec)
+        assert torch.cuda.current_device() == 0
+        ptr, w, h, _ = g["frame"].map_raw("channel.depthCUDA")
+        assert ptr and (w, h) == (32, 24)
+        assert not dev.errors()
+    finally:
+        dev.release()
+    assert torch.cuda.current_device() == 0

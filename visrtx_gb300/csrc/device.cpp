@@ -3183,6 +3183,35 @@ static Object *O(VRTXObject o)
   return reinterpret_cast<Object *>(o);
 }
 
+// Every API call runs on the device's GPU and leaves the calling thread's
+// current device as it found it (CUDADeviceScope, VisRTXDevice.cpp:790-814).
+// A call that initialises the device (init() selects its GPU) is restored
+// the same way. Devices without a usable GPU make no CUDA call here.
+struct DeviceScope
+{
+  int prev = -1;
+  explicit DeviceScope(Device *dev)
+  {
+    if (!dev || (dev->initTried && !dev->initOk))
+      return;
+    if (cudaGetDevice(&prev) != cudaSuccess) {
+      cudaGetLastError();
+      prev = -1;
+      return;
+    }
+    if (dev->initOk && prev != dev->cudaDevice)
+      cudaSetDevice(dev->cudaDevice);
+  }
+  ~DeviceScope()
+  {
+    int cur = -1;
+    if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev)
+      cudaSetDevice(prev);
+  }
+  DeviceScope(const DeviceScope &) = delete;
+  DeviceScope &operator=(const DeviceScope &) = delete;
+};
+
 template <typename T>
 static VRTXObject newObj(VRTXDevice d, int type, const char *subtype)
 {
@@ -3229,6 +3258,7 @@ VRTX_API void vrtxDeviceCommitParameters(VRTXDevice) {}
 
 VRTX_API void vrtxDeviceRelease(VRTXDevice d)
 {
+  DeviceScope scope(D(d));
   if (!d)
     return;
   Device *dev = D(d);
@@ -3308,6 +3338,7 @@ VRTX_API int vrtxDeviceGetProperty(VRTXDevice d,
     uint64_t size,
     uint32_t)
 {
+  DeviceScope scope(D(d));
   if (!d || !name || !mem)
     return 0;
   std::string n(name);
@@ -3453,6 +3484,7 @@ VRTX_API int vrtxGetInstanceExtensions(VRTXExtensions *ext, VRTXDevice d, VRTXOb
 
 VRTX_API int vrtxDeviceIsValid(VRTXDevice d)
 {
+  DeviceScope scope(D(d));
   return d && D(d)->init() ? 1 : 0;
 }
 
@@ -3491,6 +3523,7 @@ VRTX_API VRTXArray vrtxNewArray1D(VRTXDevice d,
     int et,
     uint64_t n1)
 {
+  DeviceScope scope(D(d));
   return newArray(d, 1, mem, del, ud, et, n1, 1, 1);
 }
 
@@ -3502,6 +3535,7 @@ VRTX_API VRTXArray vrtxNewArray2D(VRTXDevice d,
     uint64_t n1,
     uint64_t n2)
 {
+  DeviceScope scope(D(d));
   return newArray(d, 2, mem, del, ud, et, n1, n2, 1);
 }
 
@@ -3514,11 +3548,13 @@ VRTX_API VRTXArray vrtxNewArray3D(VRTXDevice d,
     uint64_t n2,
     uint64_t n3)
 {
+  DeviceScope scope(D(d));
   return newArray(d, 3, mem, del, ud, et, n1, n2, n3);
 }
 
 VRTX_API void *vrtxMapArray(VRTXDevice d, VRTXArray a)
 {
+  DeviceScope scope(D(d));
   if (!d || !a)
     return nullptr;
   return static_cast<Array *>(O(a))->map();
@@ -3526,6 +3562,7 @@ VRTX_API void *vrtxMapArray(VRTXDevice d, VRTXArray a)
 
 VRTX_API void vrtxUnmapArray(VRTXDevice d, VRTXArray a)
 {
+  DeviceScope scope(D(d));
   if (!d || !a)
     return;
   std::lock_guard<std::recursive_mutex> lock(D(d)->mutex);
@@ -3534,22 +3571,27 @@ VRTX_API void vrtxUnmapArray(VRTXDevice d, VRTXArray a)
 
 VRTX_API VRTXObject vrtxNewCamera(VRTXDevice d, const char *st)
 {
+  DeviceScope scope(D(d));
   return newObj<Camera>(d, VRTX_CAMERA, st);
 }
 VRTX_API VRTXObject vrtxNewGeometry(VRTXDevice d, const char *st)
 {
+  DeviceScope scope(D(d));
   return newObj<Geometry>(d, VRTX_GEOMETRY, st);
 }
 VRTX_API VRTXObject vrtxNewLight(VRTXDevice d, const char *st)
 {
+  DeviceScope scope(D(d));
   return newObj<Light>(d, VRTX_LIGHT, st);
 }
 VRTX_API VRTXObject vrtxNewMaterial(VRTXDevice d, const char *st)
 {
+  DeviceScope scope(D(d));
   return newObj<Material>(d, VRTX_MATERIAL, st);
 }
 VRTX_API VRTXObject vrtxNewRenderer(VRTXDevice d, const char *st)
 {
+  DeviceScope scope(D(d));
   VRTXObject o = newObj<Renderer>(d, VRTX_RENDERER, st);
   if (o) // renderers are usable with defaults before any commit
     static_cast<Renderer *>(O(o))->commit();
@@ -3557,26 +3599,32 @@ VRTX_API VRTXObject vrtxNewRenderer(VRTXDevice d, const char *st)
 }
 VRTX_API VRTXObject vrtxNewSampler(VRTXDevice d, const char *st)
 {
+  DeviceScope scope(D(d));
   return newObj<Sampler>(d, VRTX_SAMPLER, st);
 }
 VRTX_API VRTXObject vrtxNewSpatialField(VRTXDevice d, const char *st)
 {
+  DeviceScope scope(D(d));
   return newObj<SpatialField>(d, VRTX_SPATIAL_FIELD, st);
 }
 VRTX_API VRTXObject vrtxNewVolume(VRTXDevice d, const char *st)
 {
+  DeviceScope scope(D(d));
   return newObj<Volume>(d, VRTX_VOLUME, st);
 }
 VRTX_API VRTXObject vrtxNewSurface(VRTXDevice d)
 {
+  DeviceScope scope(D(d));
   return newObj<Surface>(d, VRTX_SURFACE, "");
 }
 VRTX_API VRTXObject vrtxNewGroup(VRTXDevice d)
 {
+  DeviceScope scope(D(d));
   return newObj<Group>(d, VRTX_GROUP, "");
 }
 VRTX_API VRTXObject vrtxNewInstance(VRTXDevice d, const char *st)
 {
+  DeviceScope scope(D(d));
   VRTXObject o = newObj<Instance>(d, VRTX_INSTANCE, st ? st : "transform");
   if (o)
     static_cast<Instance *>(O(o))->commit();
@@ -3584,6 +3632,7 @@ VRTX_API VRTXObject vrtxNewInstance(VRTXDevice d, const char *st)
 }
 VRTX_API VRTXObject vrtxNewWorld(VRTXDevice d)
 {
+  DeviceScope scope(D(d));
   VRTXObject o = newObj<World>(d, VRTX_WORLD, "");
   if (o)
     static_cast<World *>(O(o))->commit();
@@ -3591,12 +3640,14 @@ VRTX_API VRTXObject vrtxNewWorld(VRTXDevice d)
 }
 VRTX_API VRTXFrame vrtxNewFrame(VRTXDevice d)
 {
+  DeviceScope scope(D(d));
   return newObj<Frame>(d, VRTX_FRAME, "");
 }
 
 VRTX_API void vrtxSetParameter(
     VRTXDevice d, VRTXObject o, const char *name, int type, const void *mem)
 {
+  DeviceScope scope(D(d));
   if (!d || !o || !name)
     return;
   VRTX_GUARD_BEGIN
@@ -3607,6 +3658,7 @@ VRTX_API void vrtxSetParameter(
 
 VRTX_API void vrtxUnsetParameter(VRTXDevice d, VRTXObject o, const char *name)
 {
+  DeviceScope scope(D(d));
   if (!d || !o || !name)
     return;
   std::lock_guard<std::recursive_mutex> lock(D(d)->mutex);
@@ -3615,6 +3667,7 @@ VRTX_API void vrtxUnsetParameter(VRTXDevice d, VRTXObject o, const char *name)
 
 VRTX_API void vrtxUnsetAllParameters(VRTXDevice d, VRTXObject o)
 {
+  DeviceScope scope(D(d));
   if (!d || !o)
     return;
   std::lock_guard<std::recursive_mutex> lock(D(d)->mutex);
@@ -3623,6 +3676,7 @@ VRTX_API void vrtxUnsetAllParameters(VRTXDevice d, VRTXObject o)
 
 VRTX_API void vrtxCommitParameters(VRTXDevice d, VRTXObject o)
 {
+  DeviceScope scope(D(d));
   if (!d || !o)
     return;
   VRTX_GUARD_BEGIN
@@ -3633,6 +3687,7 @@ VRTX_API void vrtxCommitParameters(VRTXDevice d, VRTXObject o)
 
 VRTX_API void vrtxRelease(VRTXDevice d, VRTXObject o)
 {
+  DeviceScope scope(D(d));
   if (!d || !o)
     return;
   std::lock_guard<std::recursive_mutex> lock(D(d)->mutex);
@@ -3646,6 +3701,7 @@ VRTX_API void vrtxRelease(VRTXDevice d, VRTXObject o)
 
 VRTX_API void vrtxRetain(VRTXDevice d, VRTXObject o)
 {
+  DeviceScope scope(D(d));
   if (!d || !o)
     return;
   O(o)->publicRefs++;
@@ -3660,6 +3716,7 @@ VRTX_API int vrtxGetProperty(VRTXDevice d,
     uint64_t size,
     uint32_t mask)
 {
+  DeviceScope scope(D(d));
   if (!d || !o || !name || !mem)
     return 0;
   VRTX_GUARD_BEGIN
@@ -3670,6 +3727,7 @@ VRTX_API int vrtxGetProperty(VRTXDevice d,
 
 VRTX_API void vrtxRenderFrame(VRTXDevice d, VRTXFrame f)
 {
+  DeviceScope scope(D(d));
   if (!d || !f)
     return;
   VRTX_GUARD_BEGIN
@@ -3683,6 +3741,7 @@ VRTX_API void vrtxRenderFrame(VRTXDevice d, VRTXFrame f)
 
 VRTX_API int vrtxFrameReady(VRTXDevice d, VRTXFrame f, uint32_t waitMask)
 {
+  DeviceScope scope(D(d));
   if (!d || !f)
     return 1;
   auto *fr = static_cast<Frame *>(O(f));
@@ -3702,6 +3761,7 @@ VRTX_API const void *vrtxMapFrame(VRTXDevice d,
     uint32_t *height,
     int *pixelType)
 {
+  DeviceScope scope(D(d));
   uint32_t w0, h0;
   int t0;
   if (!width)
@@ -3725,6 +3785,7 @@ VRTX_API void vrtxUnmapFrame(VRTXDevice, VRTXFrame, const char *) {}
 VRTX_API uint64_t vrtxDebugCopyAccel(
     VRTXDevice d, VRTXObject world, int kind, void *dst, uint64_t capacity)
 {
+  DeviceScope scope(D(d));
   if (!d || !world || O(world)->type != VRTX_WORLD)
     return 0;
   std::lock_guard<std::recursive_mutex> lock(D(d)->mutex);
@@ -3779,6 +3840,7 @@ VRTX_API uint64_t vrtxDebugCopyAccel(
 
 VRTX_API float vrtxWorldBuildMilliseconds(VRTXDevice d, VRTXObject world)
 {
+  DeviceScope scope(D(d));
   if (!d || !world || O(world)->type != VRTX_WORLD)
     return 0.f;
   return static_cast<World *>(O(world))->buildMs;
@@ -3786,6 +3848,7 @@ VRTX_API float vrtxWorldBuildMilliseconds(VRTXDevice d, VRTXObject world)
 
 VRTX_API float vrtxFrameKernelMilliseconds(VRTXDevice d, VRTXFrame f)
 {
+  DeviceScope scope(D(d));
   if (!d || !f)
     return 0.f;
   auto *fr = static_cast<Frame *>(O(f));
@@ -3799,6 +3862,7 @@ VRTX_API float vrtxFrameKernelMilliseconds(VRTXDevice d, VRTXFrame f)
 
 VRTX_API int vrtxFrameKernelLaunches(VRTXDevice d, VRTXFrame f)
 {
+  DeviceScope scope(D(d));
   if (!d || !f)
     return 0;
   return static_cast<Frame *>(O(f))->launches;
@@ -3812,6 +3876,7 @@ void vrtxInternalReport(VRTXDevice d, int severity, const char *msg)
 
 VRTX_API void *vrtxDeviceStream(VRTXDevice d)
 {
+  DeviceScope scope(D(d));
   if (!d || !D(d)->init())
     return nullptr;
   return D(d)->stream;

@@ -441,8 +441,10 @@ struct Device
   const void *cbPtr = nullptr;
   int cudaDevice = 0;
   std::recursive_mutex mutex;
-  bool initTried = false;
-  bool initOk = false;
+  // written once under the mutex by init(); read without it by the
+  // per-call device scope
+  std::atomic<bool> initTried{false};
+  std::atomic<bool> initOk{false};
   cudaStream_t stream = nullptr;
   int numSMs = 0;
   std::atomic<uint64_t> lastChange{0};
