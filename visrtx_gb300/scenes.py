@@ -274,7 +274,7 @@ def pinhole_basis(pos, target, fovy_deg: float, width: int, height: int, up=(0.0
 
 
 # ---------------------------------------------------------------------------
-# scene specification shared by the ANARI-side builder and test checkers
+# scene specification shared by the ANARI-side builder and the oracle
 # ---------------------------------------------------------------------------
 
 from dataclasses import dataclass, field as _field
