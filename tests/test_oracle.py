@@ -1,6 +1,7 @@
 """CPU checks of the oracle itself: known-answer vectors for Philox4x32-10
 (the SC'11 paper's algorithm), curand-style stream semantics, the TF
-discretisation, single-ray analytic hits, sRGB endpoints, and an FP64
+discretisation, single-ray analytic hits, point and spot light shading, sRGB
+endpoints, and an FP64
 central-difference check of the differentiable marcher's adjoint. GPU-dumped
 curand and texture outputs pin the RNG and filter emulation where fixtures
 exist (tests/golden/)."""
@@ -113,6 +114,35 @@ def test_single_triangle_known_answer():
     expect = round((0.8 ** 0.41666 * 1.055 - 0.055) * 255)
     # tonemap / inverse tonemap round trip of 0.8 is exact to 1 ulp
     assert np.all(np.abs(c[..., 0].astype(int) - expect) <= 1)
+
+
+def lit_triangle_accum(light):
+    """The single triangle (0.8 grey matte, facing the camera) under one
+    light, `default` renderer without AO: the accumulated (tonemapped) RGB."""
+    spec = single_triangle_spec("default")
+    spec.renderer.ambient_samples = 0
+    spec.lights = [light]
+    return O.render(spec)["accum"][..., :3]
+
+
+def test_point_and_spot_light_known_answers():
+    """Point light radiance is colour x intensity with no distance falloff
+    (sampleLight.h:72-80); a spot adds only its cone factor (:84-101).
+    With intensity pi the matte term 0.8/pi x N.L x radiance is 0.8, stored
+    tonemapped as 0.8 / 1.8."""
+    expect = 0.8 / 1.8
+    for z in (0.0, -8.0):  # 2 and 10 units from the lit point: same result
+        acc = lit_triangle_accum(S.LightSpec(type="point", position=(0.25, 0.25, z),
+                                             irradiance=math.pi))
+        assert np.allclose(acc, expect, atol=1e-4), (z, acc)
+    inside = lit_triangle_accum(S.LightSpec(type="spot", position=(0.25, 0.25, 0.0),
+                                            direction=(0.0, 0.0, 1.0), irradiance=math.pi,
+                                            opening_angle=math.pi / 2))
+    assert np.allclose(inside, expect, atol=1e-4)
+    outside = lit_triangle_accum(S.LightSpec(type="spot", position=(0.25, 0.25, 0.0),
+                                             direction=(0.0, 0.0, -1.0), irradiance=math.pi,
+                                             opening_angle=math.pi / 2))
+    assert np.allclose(outside, 0.0, atol=1e-7)
 
 
 def test_single_sphere_known_answer():
