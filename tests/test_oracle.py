@@ -1,8 +1,8 @@
 """CPU checks of the oracle itself: known-answer vectors for Philox4x32-10
 (the SC'11 paper's algorithm), curand-style stream semantics, the TF
 discretisation, single-ray analytic hits, point and spot light shading, sRGB
-endpoints, and an FP64
-central-difference check of the differentiable marcher's adjoint. GPU-dumped
+endpoints, and an FP64 central-difference check of the differentiable
+marcher's adjoint. GPU-dumped
 curand and texture outputs pin the RNG and filter emulation where fixtures
 exist (tests/golden/)."""
 import json
