@@ -2,9 +2,8 @@
 (the SC'11 paper's algorithm), curand-style stream semantics, the TF
 discretisation, single-ray analytic hits, point and spot light shading, sRGB
 endpoints, and an FP64 central-difference check of the differentiable
-marcher's adjoint. GPU-dumped
-curand and texture outputs pin the RNG and filter emulation where fixtures
-exist (tests/golden/)."""
+marcher's adjoint. GPU-dumped curand and texture outputs pin the RNG and
+filter emulation where fixtures exist (tests/golden/)."""
 import json
 import math
 import os
