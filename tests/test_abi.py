@@ -104,3 +104,23 @@ def test_feature_queries(built):
     e = L.VRTXExtensions()
     assert dev.lib.vrtxGetInstanceExtensions(C.byref(e), dev.h, C.c_void_p(1)) == 0
     dev.release()
+
+
+def test_binding_arity_matches_header():
+    """Every ctypes signature takes as many arguments as the header's
+    declaration, so a binding cannot drift from the ABI unnoticed."""
+    from visrtx_gb300 import _lib
+
+    decls = {}
+    for fn in sorted(os.listdir(os.path.join(ROOT, "include"))):
+        if fn.endswith(".h"):
+            src = open(os.path.join(ROOT, "include", fn)).read()
+            src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+            for name, params in re.findall(r"VRTX_API\s+[\w\s\*]+?\b(vrtx\w+)\s*\(([^)]*)\)\s*;",
+                                           src):
+                p = params.strip()
+                decls[name] = 0 if p in ("", "void") else p.count(",") + 1
+    assert decls and set(decls) <= set(_lib.SIGNATURES)
+    wrong = {n: (k, len(_lib.SIGNATURES[n][1])) for n, k in decls.items()
+             if len(_lib.SIGNATURES[n][1]) != k}
+    assert not wrong, wrong
