@@ -141,16 +141,20 @@ typedef void (*VRTXFrameCompletionCallback)(
  * include/anari/ext/visrtx/visrtx.h:49-51). CUDA is initialised lazily on
  * the first object creation, as VisRTXDevice::initDevice does
  * (VisRTXDevice.cpp:435-458). Returns NULL only when out of host memory.
- * Every call that takes the device runs on its GPU ("cudaDevice") and
+ * Every ANARI object call (arrays, objects, parameters, frames) runs on
+ * the device's GPU ("cudaDevice", fixed when the device initialises) and
  * leaves the calling thread's current CUDA device as it was
  * (CUDADeviceScope, VisRTXDevice.cpp:790-814); objects may be created and
- * used from any thread. */
+ * used from any thread. The vrtxDM* calls are the exception: they run on
+ * the calling thread's current device, the one that owns their pointers. */
 VRTX_API VRTXDevice vrtxNewDevice(
     VRTXStatusCallback statusCallback, const void *statusCallbackUserData);
 
-/* Device parameters ("cudaDevice", "statusCallback"); replaces
+/* Device parameters ("cudaDevice", "forceInit", "statusCallback"); replaces
  * VisRTXDevice::deviceSetParameter / deviceCommitParameters
- * (VisRTXDevice.cpp:460-471). */
+ * (VisRTXDevice.cpp:460-478). "cudaDevice" set after the device has
+ * initialised is reported as a warning and ignored; with "forceInit" the
+ * commit initialises CUDA instead of the first object creation. */
 VRTX_API void vrtxDeviceSetParameter(
     VRTXDevice d, const char *name, int type, const void *mem);
 VRTX_API void vrtxDeviceCommitParameters(VRTXDevice d);
@@ -460,8 +464,12 @@ VRTX_API void vrtxDMPlanRelease(VRTXDMPlan plan);
  * views per call (about 400 KB, held on every GPU that loads the library
  * until the process exits); larger requests are rejected with an error.
  * The first call on a device looks up that array's device address; make
- * that first call before any stream capture. All calls share the array:
- * calls that overlap on the GPU (unordered streams) race on it. */
+ * that first call before any stream capture. The address is kept for the
+ * life of the process and does not survive a cudaDeviceReset. Every call
+ * copies its descriptors from host memory it frees on return, so a call
+ * on a stream that is capturing is rejected with an error. All calls share
+ * the array: calls that overlap on the GPU (unordered streams) race on
+ * it. */
 VRTX_API int vrtxDMForwardNoAlloc(VRTXDevice d,
     const VRTXDMVolume *volumes,
     int numVolumes,

@@ -35,15 +35,18 @@ def build() -> str:
     return LIB
 
 
-REF_TREE = "/root/reference"
+# The VisRTX source tree: VISRTX_REFERENCE_TREE, or build_ref(tree=...);
+# the default is where this recipe's build machine mounts it.
+REF_TREE = os.environ.get("VISRTX_REFERENCE_TREE", "/root/reference")
 REF_OUT = os.path.join(HERE, "_ref")
 REF_LIB = os.path.join(REF_OUT, "libnvdbref.so")
 
 
-def build_ref() -> str | None:
+def build_ref(tree: str | None = None) -> str | None:
     """oracle/_ref/libnvdbref.so from ref_nvdb.cpp and the reference's vendored
-    NanoVDB headers; None when the reference tree is absent."""
-    inc = os.path.join(REF_TREE, "external", "nanovdb", "include")
+    NanoVDB headers under `tree` (default REF_TREE); None when the reference
+    tree is absent."""
+    inc = os.path.join(tree or REF_TREE, "external", "nanovdb", "include")
     if not os.path.isdir(inc):
         return None
     src = os.path.join(HERE, "ref_nvdb.cpp")
@@ -61,5 +64,7 @@ def build_ref() -> str | None:
 
 
 if __name__ == "__main__":
+    import sys
+
     print(build())
-    print(build_ref())
+    print(build_ref(sys.argv[1] if len(sys.argv) > 1 else None))

@@ -1,9 +1,7 @@
 """Generates tests/golden/curand_philox.json and tests/golden/tex_filter.json
 on a machine with a GPU: compiles cuda_fixtures.cu (sm_103a), runs it, and
-records the GPU's curand draws and hardware-filtered texture values. For the
-texture it also records how closely the oracle's filter emulation (weights
-with 8 fractional bits, truncated or rounded) reproduces the hardware, and
-picks the rounding that does.
+records the GPU's curand draws and hardware-filtered texture values, and
+prints how many of them the oracle's texture-unit emulation misses.
 
     python tests/golden/gen_cuda_fixtures.py [out_dir]
 """
@@ -44,26 +42,19 @@ def main(out_dir: str = HERE) -> None:
 
     t3 = raw["tex3"]
     vox = np.array(t3["volume"], np.float32).reshape(t3["dims"][::-1])
-    errs = {}
-    for mode in (0, 1):
-        e = [abs(O.tex3d(vox, c, mode) - v) for c, v in zip(t3["coords"], t3["values"])]
-        errs[mode] = float(max(e))
-    mode = min(errs, key=errs.get)
+    got = np.array([O.tex3d(vox, c, 1) for c in t3["coords"]], np.float32)
     t1 = raw["tex1"]
     table = np.array(t1["table"], np.float32).reshape(-1, 4)
-    e1 = {}
-    for m in (0, 1):
-        e1[m] = float(max(np.abs(O.tex1d(table, c, m) - np.array(t1["values"][4 * i:4 * i + 4])).max()
-                          for i, c in enumerate(t1["coords"])))
+    got1 = np.array([O.tex1d(table, c, 1) for c in t1["coords"]], np.float32).reshape(-1)
     with open(os.path.join(out_dir, "tex_filter.json"), "w") as f:
         json.dump({"source": "tex3D<float> / tex1D<float4>, linear, clamp, normalised, on a GB300",
                    "dims": t3["dims"], "volume": t3["volume"], "coords": t3["coords"],
-                   "values": t3["values"], "round_mode": mode,
-                   "max_error_by_round_mode": errs,
-                   "tolerance": errs[mode] * 1.01 + 1e-7,
+                   "values": t3["values"],
                    "tex1": {"table": t1["table"], "coords": t1["coords"],
-                            "values": t1["values"], "max_error_by_round_mode": e1}}, f)
-    print("tex3 max error by rounding mode:", errs, "tex1:", e1)
+                            "values": t1["values"]}}, f)
+    print("oracle texture emulation mismatches: 3D",
+          int((got != np.array(t3["values"], np.float32)).sum()), "of", len(got),
+          "1D", int((got1 != np.array(t1["values"], np.float32)).sum()), "of", len(got1))
 
 
 if __name__ == "__main__":

@@ -124,3 +124,42 @@ def test_binding_arity_matches_header():
     wrong = {n: (k, len(_lib.SIGNATURES[n][1])) for n, k in decls.items()
              if len(_lib.SIGNATURES[n][1]) != k}
     assert not wrong, wrong
+
+
+def test_cuda_device_change_after_init_is_ignored(built):
+    """The GPU is chosen once, when the device initialises; a later
+    'cudaDevice' is reported as a warning and ignored
+    (VisRTXDevice.cpp:464-470), so objects never move off the GPU that owns
+    their memory."""
+    from visrtx_gb300 import _lib as L
+    from visrtx_gb300 import anari
+
+    dev = anari.Device(0)
+    dev.lib.vrtxNewWorld(dev.h)  # initialises (or fails to, without a GPU)
+    before = len(dev.messages)
+    v = C.c_int32(1)
+    dev.lib.vrtxDeviceSetParameter(dev.h, b"cudaDevice", L.INT32, C.byref(v))
+    dev.lib.vrtxDeviceCommitParameters(dev.h)
+    new = dev.messages[before:]
+    assert any(s == L.SEVERITY_WARNING and "is ignored" in m for s, m in new), new
+    dev.release()
+
+
+def test_force_init_initialises_at_commit(built):
+    """'forceInit' makes the device initialise at commit rather than at the
+    first object creation (VisRTXDevice.cpp:473-476)."""
+    import torch
+
+    from visrtx_gb300 import _lib as L
+    from visrtx_gb300 import anari
+
+    dev = anari.Device(0)
+    assert not dev.messages
+    v = C.c_int32(1)
+    dev.lib.vrtxDeviceSetParameter(dev.h, b"forceInit", L.BOOL, C.byref(v))
+    dev.lib.vrtxDeviceCommitParameters(dev.h)
+    if torch.cuda.is_available():
+        assert dev.is_valid()
+    else:
+        assert any("no CUDA device" in m for m in dev.errors())
+    dev.release()

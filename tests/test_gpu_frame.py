@@ -101,3 +101,37 @@ def test_calls_keep_the_threads_current_device(built):
     finally:
         dev.release()
     assert torch.cuda.current_device() == 0
+
+
+@pytest.mark.parametrize("renderer", ["default", "ao"])
+def test_traversal_step_limit_sets_error_flag(device, renderer):
+    """The device-side traversal bound ends a ray's traversal and sets bit 1
+    of the frame's error flags instead of spinning; "vrtx.maxTraversalSteps"
+    lowers it so that the guard runs out on a real scene. The context stays
+    usable: with the default bound the next frame is clean and equal to a
+    frame that never hit the guard. "ao" over opaque surfaces runs the
+    wavefront kernels (closest-hit primary rays and the resumable any-hit
+    loop), "default" the per-pixel kernel."""
+    import numpy as np
+
+    if renderer == "ao":
+        spec = S.instanced_spec(subdiv=3, n_inst=8, n_spheres=3000, width=64, height=48, spp=1,
+                                ao_samples=4, renderer="ao")
+    else:
+        spec = S.soup_spec(n=4000, width=64, height=48, renderer="default")
+    g = render_gpu(device, spec)
+    f = g["frame"]
+    assert f.stats()["error_flags"] == 0
+    clean = f.map("channel.color")
+    f.set("vrtx.maxTraversalSteps", 3)
+    f.commit()
+    f.render()
+    f.wait()
+    assert f.stats()["error_flags"] & 2
+    f.unset("vrtx.maxTraversalSteps")
+    f.commit()
+    f.render()
+    f.wait()
+    assert f.stats()["error_flags"] == 0
+    assert np.array_equal(f.map("channel.color"), clean)
+    assert not device.errors()

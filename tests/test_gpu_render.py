@@ -9,7 +9,7 @@ import pytest
 
 from visrtx_gb300 import scenes as S
 from visrtx_gb300 import _lib as L
-from tests.parity import compare, render_gpu, render_oracle
+from tests.parity import compare, inverse_tonemap, render_gpu, render_oracle
 
 pytestmark = pytest.mark.gpu
 
@@ -431,24 +431,24 @@ def test_volume_parity(device, rate):
     spec = small_volume(rate=rate)
     g = render_gpu(device, spec)
     r = render_oracle(spec)
-    rep = compare(g, r, color_tol=2)
+    rep = compare(g, r, color_tol=1)
     print(rep)
 
 
 def test_volume_fp64_rms(device):
-    """Volume colour against the clean FP64 marcher: RMS <= 1e-3."""
+    """Volume colour against the clean FP64 marcher (exact trilinear, FP64
+    compositing): RMS <= 1e-3 over the FLOAT32_VEC4 colour channel, so no
+    output quantisation enters the figure."""
     spec = small_volume()
     spec.renderer.background = (0.0, 0.0, 0.0, 1.0)
-    g = render_gpu(device, spec)
+    g = render_gpu(device, spec, float_color=True)
     r = render_oracle(spec, volume_mode=1)
-    from visrtx_gb300 import anari
-
-    cg = anari.rgba8(g["color"]).astype(np.float64) / 255.0
-    cr = anari.rgba8(r["color"]).astype(np.float64) / 255.0
+    cr = inverse_tonemap(r["accum"])
+    cg = g["color"].astype(np.float64)
     rms = float(np.sqrt(np.mean((cg[..., :3] - cr[..., :3]) ** 2)))
-    print("rms vs fp64", rms)
-    # 8-bit output quantisation alone contributes ~1/255/sqrt(12)
-    assert rms <= 1e-3 + 1.0 / 255 / math.sqrt(12)
+    print("rms vs fp64", rms, "max", float(np.abs(cg[..., :3] - cr[..., :3]).max()))
+    assert cr[..., :3].std() > 0.02  # the volume is visible
+    assert rms <= 1e-3
 
 
 def dpt_volume_scene(with_surface=False, spp=8):
@@ -487,7 +487,7 @@ def test_dpt_volume_parity(device, with_surface):
     same = np.all(np.abs(cg - cr) <= 1, axis=-1)
     print("dpt volume: identical pixel fraction", same.mean(),
           "mean", cg[..., :3].mean(), cr[..., :3].mean())
-    assert same.mean() >= 0.9
+    assert same.mean() >= 0.999
     assert abs(cg[..., :3].mean() - cr[..., :3].mean()) <= 0.02 * max(cr[..., :3].mean(), 1.0)
     assert cr[..., :3].std() > 5.0  # the medium is visible
     # dpt writes the primary tmax as depth and ~0u ids (the raygen's
@@ -524,7 +524,7 @@ def test_nanovdb_volume_parity(device, gtype, renderer):
     spec = nvdb_volume(gtype, renderer=renderer)
     g = render_gpu(device, spec)
     r = render_oracle(spec)
-    rep = compare(g, r, color_tol=2)
+    rep = compare(g, r, color_tol=1)
     from visrtx_gb300 import anari
 
     c = anari.rgba8(g["color"])[..., :3]
@@ -545,7 +545,7 @@ def test_nanovdb_golden_grids(device, gtype):
     spec.volumes[0].opacity = spec.volumes[0].opacity * 4
     g = render_gpu(device, spec)
     r = render_oracle(spec)
-    rep = compare(g, r, color_tol=2)
+    rep = compare(g, r, color_tol=1)
     from visrtx_gb300 import anari
 
     assert anari.rgba8(g["color"])[..., :3].std() > 5.0
@@ -573,15 +573,14 @@ def test_nanovdb_brick_cache_matches_walk(device, gtype):
 def test_nanovdb_fp64_rms(device):
     """NanoVDB volume colour against the clean FP64 marcher: RMS <= 1e-3."""
     spec = nvdb_volume("float", sparse=False)
-    g = render_gpu(device, spec)
+    g = render_gpu(device, spec, float_color=True)
     r = render_oracle(spec, volume_mode=1)
-    from visrtx_gb300 import anari
-
-    cg = anari.rgba8(g["color"]).astype(np.float64) / 255.0
-    cr = anari.rgba8(r["color"]).astype(np.float64) / 255.0
+    cr = inverse_tonemap(r["accum"])
+    cg = g["color"].astype(np.float64)
     rms = float(np.sqrt(np.mean((cg[..., :3] - cr[..., :3]) ** 2)))
     print("nanovdb rms vs fp64", rms)
-    assert rms <= 1e-3 + 1.0 / 255 / math.sqrt(12)
+    assert cr[..., :3].std() > 0.02
+    assert rms <= 1e-3
 
 
 def test_nanovdb_dpt(device):
@@ -606,7 +605,7 @@ def test_nanovdb_dpt(device):
     cr = anari.rgba8(r["color"]).astype(np.int32)
     same = np.all(np.abs(cg - cr) <= 1, axis=-1)
     print("nanovdb dpt: identical pixel fraction", same.mean())
-    assert same.mean() >= 0.9
+    assert same.mean() >= 0.999
     assert abs(cg[..., :3].mean() - cr[..., :3].mean()) <= 0.02 * max(cr[..., :3].mean(), 1.0)
     assert cr[..., :3].std() > 5.0
 

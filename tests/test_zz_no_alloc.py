@@ -68,3 +68,33 @@ def test_no_alloc_rejects_oversized_requests():
     rc, _, _ = _run("vrtxDMForwardNoAlloc", b)
     assert rc < 0
     assert any("4096 views" in m for m in dm._device().errors())
+
+
+def test_no_alloc_rejects_a_capturing_stream():
+    """Each call copies its descriptors from host memory that it frees on
+    return, so it refuses a stream under capture (a captured copy would
+    read freed memory at every replay) and leaves the capture usable."""
+    v = _volume(5)
+    views = [dm.look_at_view(0, v.dims, (0.0, 0.0, 2.0), 50.0, 8, 8)]
+    b = dm.Batch([v], views, tile=(8, 4))
+    rc, _, _ = _run("vrtxDMForwardNoAlloc", b)  # set-up call, outside capture
+    assert rc == 0
+    lib = L.load()
+    image = torch.zeros((b.pixels, 3), device="cuda")
+    state = torch.zeros((b.pixels, 2), device="cuda")
+    x = torch.zeros(4, device="cuda")
+    vols, vws = b.descriptors()
+    g = torch.cuda.CUDAGraph()
+    s = torch.cuda.Stream()
+    with torch.cuda.stream(s):
+        with torch.cuda.graph(g, stream=s):
+            x.add_(1.0)
+            rc = lib.vrtxDMForwardNoAlloc(dm._device().h, vols, len(vols), vws, len(vws),
+                                          C.c_void_p(image.data_ptr()),
+                                          C.c_void_p(state.data_ptr()), 8, 4,
+                                          C.c_void_p(s.cuda_stream))
+    assert rc < 0
+    assert any("capturing" in m for m in dm._device().errors())
+    g.replay()
+    torch.cuda.synchronize()
+    assert float(x[0]) == 1.0  # capture records the add, the one replay runs it

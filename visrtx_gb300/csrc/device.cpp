@@ -151,6 +151,7 @@ bool Device::init()
         "no CUDA device found: libvrtx has no CPU path");
     return false;
   }
+  cudaDevice = desiredDevice;
   if (cudaDevice < 0 || cudaDevice >= n) {
     report(nullptr, VRTX_SEVERITY_FATAL_ERROR, "invalid 'cudaDevice'");
     return false;
@@ -2850,15 +2851,22 @@ void Frame::commit()
     alloc(9, n * 12);
   if (!workCounter)
     cudaMalloc(&workCounter, 16);
-  if (!errorFlag) {
+  // error flags collect over the frames rendered since the last commit
+  if (!errorFlag)
     cudaMalloc(&errorFlag, 16);
+  if (errorFlag)
     cudaMemset(errorFlag, 0, 16);
-  }
   if (!stats) {
     cudaMalloc(&stats, 16 * sizeof(unsigned long long));
     cudaMemset(stats, 0, 16 * sizeof(unsigned long long));
   }
   countTraversal = get<int32_t>("vrtx.countTraversal", VRTX_BOOL, 0) != 0;
+  // the traversal loop bound per ray; lowering it makes the device guard
+  // end traversals early and report bit 1 of "error_flags" (no GPU fault)
+  {
+    const int32_t m = get<int32_t>("vrtx.maxTraversalSteps", VRTX_INT32, 1 << 22);
+    maxTraversalSteps = m > 0 ? (uint32_t)m : 1u;
+  }
   forceMegakernel = get<int32_t>("vrtx.megakernel", VRTX_BOOL, 0) != 0;
   for (cudaEvent_t *e : {&evStart, &evEnd, &evKStart, &evKEnd})
     if (!*e)
@@ -2936,6 +2944,7 @@ void Frame::render()
   }
   FrameParams P{};
   P.world = world->gpu;
+  P.world.maxTraversalSteps = maxTraversalSteps;
   P.camera = camera->gpu;
   renderer->ensureBackground();
   P.renderer = renderer->gpu;
@@ -3212,6 +3221,24 @@ struct DeviceScope
   DeviceScope &operator=(const DeviceScope &) = delete;
 };
 
+// The GPU is chosen once, by init(); a later "cudaDevice" is reported and
+// ignored, as VisRTXDevice::deviceCommitParameters does
+// (VisRTXDevice.cpp:464-470), so every object stays on the GPU that owns its
+// memory and the device's stream.
+static void warnDeviceChange(Device *dev)
+{
+  if (dev->initTried && dev->desiredDevice != dev->cudaDevice) {
+    char msg[160];
+    std::snprintf(msg,
+        sizeof(msg),
+        "libvrtx was already initialised to use GPU %d: new device number %d is "
+        "ignored",
+        dev->cudaDevice,
+        dev->desiredDevice);
+    dev->report(nullptr, VRTX_SEVERITY_WARNING, msg);
+  }
+}
+
 template <typename T>
 static VRTXObject newObj(VRTXDevice d, int type, const char *subtype)
 {
@@ -3246,15 +3273,32 @@ VRTX_API void vrtxDeviceSetParameter(
   if (!d || !name)
     return;
   std::string n(name);
-  if (n == "cudaDevice" && type == VRTX_INT32 && mem)
-    D(d)->cudaDevice = *(const int32_t *)mem;
+  Device *dev = D(d);
+  if (n == "cudaDevice" && type == VRTX_INT32 && mem) {
+    std::lock_guard<std::recursive_mutex> lock(dev->mutex);
+    dev->desiredDevice = *(const int32_t *)mem;
+    warnDeviceChange(dev);
+  } else if (n == "forceInit" && type == VRTX_BOOL && mem)
+    dev->forceInit = *(const int32_t *)mem != 0;
   else if (n == "statusCallback" && mem)
     D(d)->cb = *(const VRTXStatusCallback *)mem;
   else if (n == "statusCallbackUserData")
     D(d)->cbPtr = mem ? *(const void *const *)mem : nullptr;
 }
 
-VRTX_API void vrtxDeviceCommitParameters(VRTXDevice) {}
+// deviceCommitParameters (VisRTXDevice.cpp:460-478): "forceInit" initialises
+// CUDA now instead of at the first object creation.
+VRTX_API void vrtxDeviceCommitParameters(VRTXDevice d)
+{
+  Device *dev = D(d);
+  if (!dev)
+    return;
+  std::lock_guard<std::recursive_mutex> lock(dev->mutex);
+  if (dev->forceInit && !dev->initTried) {
+    DeviceScope scope(dev);
+    dev->init();
+  }
+}
 
 VRTX_API void vrtxDeviceRelease(VRTXDevice d)
 {

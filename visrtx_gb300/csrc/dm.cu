@@ -931,7 +931,10 @@ constexpr size_t kNoAllocBytes = 256
 __device__ __align__(256) uint8_t g_dmNoAllocScratch[kNoAllocBytes];
 
 // Device address of g_dmNoAllocScratch per device ordinal. The symbol's name
-// in host code is only a host-side stand-in; kernels need this address.
+// in host code is only a host-side stand-in; kernels need this address. It
+// is looked up once per device and kept for the life of the process, so it
+// does not survive a cudaDeviceReset (or a primary-context re-creation) of
+// that device.
 std::mutex g_noAllocMutex;
 uint8_t *g_noAllocAddr[64] = {};
 
@@ -971,6 +974,18 @@ extern "C" VRTX_API int vrtxDMForwardNoAlloc(VRTXDevice d,
     void *stream)
 {
   cudaStream_t s = (cudaStream_t)stream;
+  // The descriptors are copied from host memory that this call frees when
+  // it returns; a captured copy would read freed memory at every replay.
+  cudaStreamCaptureStatus capture = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(s, &capture) != cudaSuccess) {
+    cudaGetLastError();
+    return fail(d, "vrtxDMForwardNoAlloc: cannot query the stream's capture state", -12);
+  }
+  if (capture != cudaStreamCaptureStatusNone)
+    return fail(d,
+        "vrtxDMForwardNoAlloc: the stream is capturing; this entry point copies its "
+        "descriptors from host memory on every call",
+        -12);
   if (!image || !state)
     return fail(d, "vrtxDMForwardNoAlloc: image and state are required", -1);
   if (numVolumes > kNoAllocMaxVolumes || numViews > kNoAllocMaxViews)

@@ -430,6 +430,10 @@ struct WorldGPU
   const SamplerGPU *samplers; // the materials' samplers
   uint32_t hasNanovdb; // some volume samples a NanoVDB field
   int hdri; // index into lights of the world's HDRI light, -1: none
+  // Traversal loop bound per ray (node steps). A well-formed BVH ends far
+  // below it; a ray that reaches it stops, counts as a miss and sets bit 1
+  // of the frame's error flag. Frames set it from "vrtx.maxTraversalSteps".
+  uint32_t maxTraversalSteps = 1u << 22;
 };
 
 // Per-thread work counters. Rays and volume samples are counted by every
@@ -452,7 +456,8 @@ struct FrameParams
   RendererGPU renderer;
   FramebufferGPU fb;
   uint32_t *workCounter; // persistent scheduling counter (zeroed per launch)
-  uint32_t *errorFlag; // bit 0: traversal stack overflow
+  uint32_t *errorFlag; // bit 0: traversal stack overflow, bit 1: a ray
+                       // reached world.maxTraversalSteps
   unsigned long long *stats; // [0] rays, [1] nodes, [2] tri tests,
                              // [3] sphere tests, [4] BLAS entries,
                              // [5] volume samples, [6] volume fetches;

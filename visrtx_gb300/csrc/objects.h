@@ -403,6 +403,7 @@ struct Frame : Object
   uint32_t *errorFlag = nullptr;
   unsigned long long *stats = nullptr; // see FrameParams::stats
   bool countTraversal = false; // "vrtx.countTraversal": counting build
+  uint32_t maxTraversalSteps = 1u << 22; // "vrtx.maxTraversalSteps"
   bool forceMegakernel = false; // "vrtx.megakernel": per-pixel kernel only
   void *scratch = nullptr; // wavefront queues (stream-ordered allocation)
   size_t scratchBytes = 0;
@@ -439,7 +440,11 @@ struct Device
 {
   VRTXStatusCallback cb = nullptr;
   const void *cbPtr = nullptr;
+  // the GPU requested through "cudaDevice", and the one init() chose; a
+  // request after init is reported and ignored (VisRTXDevice.cpp:464-470)
+  int desiredDevice = 0;
   int cudaDevice = 0;
+  bool forceInit = false;
   std::recursive_mutex mutex;
   // written once under the mutex by init(); read without it by the
   // per-call device scope

@@ -644,8 +644,9 @@ __device__ __forceinline__ bool traverse(const WorldGPU &w,
 
   // A well-formed BVH ends the loop long before this bound; a corrupt one
   // (cyclic child links) must not spin forever: give up and flag it.
+  const uint32_t maxSteps = w.maxTraversalSteps;
   for (uint32_t guard = 0;; guard++) {
-    if (guard > (1u << 22)) {
+    if (guard > maxSteps) {
       if (errorFlag)
         atomicOr(errorFlag, 2u);
       break;
@@ -947,7 +948,7 @@ __device__ __forceinline__ int occlusionStep(const WorldGPU &w,
     uint32_t *errorFlag,
     TravStats &st)
 {
-  if (s.guard++ > (1u << 22)) {
+  if (s.guard++ > w.maxTraversalSteps) {
     if (errorFlag)
       atomicOr(errorFlag, 2u);
     return OCC_MISS;

@@ -482,9 +482,11 @@ def attr_type(a: np.ndarray) -> int:
 
 
 def build_on_device(dev, spec: SceneSpec, channels=("color", "depth", "primitiveId",
-                                                      "objectId", "instanceId")):
+                                                      "objectId", "instanceId"),
+                    float_color: bool = False):
     """Creates the spec's ANARI objects on an anari.Device; returns
-    (frame, world, keep) where keep holds every object handle."""
+    (frame, world, keep) where keep holds every object handle. The colour
+    channel is UFIXED8_RGBA_SRGB, or FLOAT32_VEC4 with `float_color`."""
     from . import _lib as L
     from .anari import DataType
 
@@ -729,7 +731,7 @@ def build_on_device(dev, spec: SceneSpec, channels=("color", "depth", "primitive
 
     fr = dev.new_frame()
     fr.set("size", (spec.width, spec.height), L.UINT32_VEC2)
-    fr.set("channel.color", DataType(L.UFIXED8_RGBA_SRGB))
+    fr.set("channel.color", DataType(L.FLOAT32_VEC4 if float_color else L.UFIXED8_RGBA_SRGB))
     for ch in channels:
         if ch == "depth":
             fr.set("channel.depth", DataType(L.FLOAT32))
