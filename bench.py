@@ -1,10 +1,18 @@
 """Benchmark of the hot path on one GB300 (or N, one process per GPU).
 
-Workload (one "step" = one frame): 64 instances of a 1.31M-triangle
+Headline workload (one "step" = one frame): 64 instances of a 1.31M-triangle
 displaced icosphere (subdivision 8) + 1M spheres, 1920x1080, 64 samples per
 pixel, 16 AO rays per hit, renderer "ao", FP32 -- the instanced-geometry +
 AO configuration. Metric: Mrays/s (primary + AO rays traced, counted on the
 device).
+
+At N=1 the same JSON line also carries, under "workloads", the other
+configurations' metrics measured in the same run (bench_workloads.py): the
+100k-triangle soup with the "default" renderer (Mrays/s), the 512^3 volume
+(Msamples/s), the differentiable marcher on 128 views of a 256^3 FP16
+volume and the batched uneven 64-volume set (forward + backward views/s
+against the FP32 one-view-per-launch forms), each with its roofline,
+end-to-end figure and CPU-oracle baseline. --headline-only skips them.
 
 Arms:
   ours (default)     libvrtx through its C ABI; `value` from the device
@@ -15,7 +23,8 @@ Arms:
   --impl reference   the reference's algorithm on the host cores: the CPU
                      oracle (a restatement of VisRTX's integrator; VisRTX
                      itself needs OptiX + the ANARI-SDK and cannot be built
-                     here), each step a bounded band of rows at 1 spp.
+                     here), each step the band of rows REF_ROWS at 1 spp --
+                     the same sample as the `cpu_baseline` leg of ours.
 
 Multi-GPU (torchrun): every rank renders its own frame of the same workload
 (weak scaling, no collective on the data path); rank 0 prints the line.
@@ -39,6 +48,10 @@ sys.path.insert(0, ROOT)
 
 METRIC = "Mrays/s"
 WORKLOAD = "instanced64_icosphere_s8_1Mspheres_1920x1080_64spp_ao16"
+# the CPU sample of the headline workload: these rows of the 1920x1080
+# frame at 1 spp (16 AO rays per hit), for the reference arm and the
+# cpu_baseline leg alike
+REF_ROWS = (476, 604)
 
 
 def _args():
@@ -52,8 +65,10 @@ def _args():
     p.add_argument("--cpu-seconds", type=float, default=12.0)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--workload", default="instanced",
-                   choices=["instanced", "volume", "nanovdb", "dm", "batched"],
-                   help="instanced (default line) | volume | nanovdb | dm | batched")
+                   choices=["instanced", "soup", "volume", "nanovdb", "dm", "batched"],
+                   help="instanced (default line) | soup | volume | nanovdb | dm | batched")
+    p.add_argument("--headline-only", action="store_true",
+                   help="skip the other workloads in the N=1 line")
     p.add_argument("--nvdb-type", default="fp16", choices=["float", "fp4", "fp8", "fp16", "fpn"])
     p.add_argument("--dm-views", type=int, default=128)
     return p.parse_args()
@@ -156,9 +171,21 @@ def algorithmic_bytes(st: dict) -> float:
             + st["sphere_tests"] * 16.0 + st["blas_entries"] * 48.0)
 
 
+def cpu_sample(sc, spec, cores):
+    """Renders REF_ROWS of the 1-spp oracle scene; returns (rays, seconds)."""
+    t0 = time.perf_counter()
+    o = sc.render(rows=REF_ROWS, threads=cores)
+    return o["rays"], time.perf_counter() - t0
+
+
+def ref_sample_text(steps: int) -> str:
+    return (f"rows {REF_ROWS[0]}-{REF_ROWS[1]} of 1920x1080 at 1 spp (AO 16) per step, "
+            f"oracle BVH prebuilt; the workload's 64 spp scale linearly")
+
+
 def run_reference(args, ws, rank):
     """The CPU restatement of the reference integrator, all host threads,
-    each step a band of rows at 1 spp (AO 16) of the same workload."""
+    each step the rows REF_ROWS at 1 spp (AO 16) of the same workload."""
     if rank != 0:
         return
     from oracle import oracle as O
@@ -167,30 +194,17 @@ def run_reference(args, ws, rank):
     spec = S.instanced_spec(spp=1)
     sc = O.OracleScene(spec)
     cores = os.cpu_count() or 1
-    mid = spec.height // 2
-    rows = 8
-    # size the band so a step takes about cpu-seconds / (steps + warmup)
-    t0 = time.perf_counter()
-    probe = sc.render(rows=(mid - rows // 2, mid + rows // 2), threads=cores)
-    dt = time.perf_counter() - t0
-    per_row = dt / rows
-    target = max(1.0, args.cpu_seconds / max(1, args.steps))
-    band = int(min(spec.height, max(8, target / max(per_row, 1e-6))))
-    r0 = max(0, mid - band // 2)
-    r1 = min(spec.height, r0 + band)
     for _ in range(max(0, args.warmup)):
-        sc.render(rows=(r0, min(r1, r0 + 8)), threads=cores)
+        sc.render(rows=(REF_ROWS[0], REF_ROWS[0] + 8), threads=cores)
     rays = 0
     secs = 0.0
     for _ in range(args.steps):
-        t0 = time.perf_counter()
-        o = sc.render(rows=(r0, r1), threads=cores)
-        secs += time.perf_counter() - t0
-        rays += o["rays"]
+        r, dt = cpu_sample(sc, spec, cores)
+        rays += r
+        secs += dt
     sc.release()
     value = rays / secs / 1e6
-    sample = (f"rows {r0}-{r1} of 1920x1080 at 1 spp (AO 16), per step; the workload's "
-              f"64 spp scale linearly; oracle BVH prebuilt")
+    sample = ref_sample_text(args.steps)
     line = {
         "impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": METRIC,
         "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
@@ -222,9 +236,7 @@ def main():
     if args.workload != "instanced":
         import bench_workloads as BW
 
-        {"volume": BW.run_volume, "nanovdb": BW.run_nanovdb, "dm": BW.run_dm,
-         "batched": BW.run_batched}[args.workload](
-            args, ws, rank, local)
+        BW.run(args.workload, args, ws, rank, local)
         return
     if args.impl == "reference":
         run_reference(args, ws, rank)
@@ -350,7 +362,28 @@ def main():
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
-        cpu = cpu_baseline(spec, args.cpu_seconds)
+        cpu = cpu_baseline()
+    for o in keep + [frame]:
+        o.release()
+    del flush
+    torch.cuda.empty_cache()
+
+    # the other configurations, measured in the same run (N=1 only)
+    workloads = None
+    if ws == 1 and not args.headline_only:
+        import bench_workloads as BW
+
+        n = min(args.steps, 10)
+        w = max(3, min(args.warmup, 5))
+        workloads = {}
+        for name, fn in (("soup100k_512x384_default", lambda: BW.measure_soup(local, n, w)),
+                         ("volume512_raycast", lambda: BW.measure_volume(local, n, w)),
+                         ("dm256_fp16_128views", lambda: BW.measure_dm(local, n, w)),
+                         ("batched64_bf16_uneven", lambda: BW.measure_batched(local, 2, 3))):
+            t0 = time.perf_counter()
+            workloads[name] = fn()
+            workloads[name]["wall_s"] = round(time.perf_counter() - t0, 1)
+            torch.cuda.empty_cache()
 
     if rank == 0:
         line = {
@@ -368,35 +401,28 @@ def main():
             "roofline": roofline,
             "cpu_baseline": cpu,
         }
+        if workloads:
+            line["workloads"] = workloads
         print(json.dumps(line), flush=True)
     dev.release()
     if ws > 1:
         torch.distributed.destroy_process_group()
 
 
-def cpu_baseline(spec, seconds: float):
-    """The oracle's multithreaded C++ tracer on a bounded band of rows at
-    1 spp (AO 16), all host threads."""
+def cpu_baseline():
+    """The oracle's multithreaded C++ tracer on the rows REF_ROWS at 1 spp
+    (AO 16), all host threads: the same sample as the reference arm."""
     from oracle import oracle as O
     from visrtx_gb300 import scenes as S
 
     s1 = S.instanced_spec(spp=1)
     sc = O.OracleScene(s1)
     cores = os.cpu_count() or 1
-    mid = s1.height // 2
-    t0 = time.perf_counter()
-    sc.render(rows=(mid - 4, mid + 4), threads=cores)
-    per_row = (time.perf_counter() - t0) / 8
-    band = int(min(s1.height, max(8, seconds / max(per_row, 1e-6))))
-    r0 = max(0, mid - band // 2)
-    r1 = min(s1.height, r0 + band)
-    t0 = time.perf_counter()
-    o = sc.render(rows=(r0, r1), threads=cores)
-    dt = time.perf_counter() - t0
+    sc.render(rows=(REF_ROWS[0], REF_ROWS[0] + 8), threads=cores)
+    rays, dt = cpu_sample(sc, s1, cores)
     sc.release()
-    return {"value": round(o["rays"] / dt / 1e6, 4), "unit": METRIC, "cores": cores,
-            "kind": "port",
-            "sample": f"rows {r0}-{r1} of 1920x1080 at 1 spp, AO 16 ({o['rays']} rays, {dt:.1f} s)"}
+    return {"value": round(rays / dt / 1e6, 4), "unit": METRIC, "cores": cores,
+            "kind": "port", "sample": ref_sample_text(1) + f" ({rays} rays, {dt:.1f} s)"}
 
 
 if __name__ == "__main__":

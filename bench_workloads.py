@@ -1,6 +1,10 @@
-"""Opt-in benchmark workloads beside bench.py's default line (run as
-`python bench.py --workload volume|dm|batched`); each prints one JSON line.
+"""The benchmark workloads beside bench.py's headline (instanced geometry +
+AO). bench.py puts each one's measurement into its JSON line under
+"workloads"; `python bench.py --workload <name>` prints one of them alone.
 
+  soup     100k-triangle FP32 soup, one instance, 512x384 pinhole camera,
+           1 spp, one directional light, matte, renderer "default"; Mrays/s
+           (primary + shadow rays) and primary Mrays/s.
   volume   structured-regular 512^3 FP32 volume (64 Gaussian blobs), 256-entry
            TF from 8-knot ramps, 16^3 macrocells, 0.5-voxel steps, 1920x1080
            orbit camera, 1 spp, raycast renderer; Msamples/s (march
@@ -8,20 +12,26 @@
   nanovdb  the same 512^3 field as a sparse NanoVDB grid (voxels >= 0.02 set;
            --nvdb-type float|fp4|fp8|fp16|fpn, default fp16) through the
            "nanovdb" spatial field, same TF, camera, steps and renderer;
-           Msamples/s.
+           Msamples/s (opt-in only).
   dm       differentiable marcher: 256^3 FP16 density (32 blobs), 128 views
            of 512x512 on a Fibonacci sphere of radius 2, L2 loss against a
            target rendered from a second volume; forward + backward views/s,
            batched (one graph-captured launch pair, autotuned tiles) against
-           the plain FP32 one-view-per-launch form.
+           the FP32 one-view-per-launch form, both with staged gradient
+           accumulation and with one atomic per gradient term.
   batched  64 volumes with edges U[64,384] (BF16, own TFs), 4-32 views each
            at {256,512,1024}^2; forward + backward views/s, one
            graph-captured launch pair against FP32 one launch per view.
+
+Every figure is device time (CUDA events on the launching stream) with L2
+flushed between steps; `e2e` is the same metric through the public API
+with host inputs copied in and the result read back inside the timed
+region; `cpu_baseline` is the CPU oracle (a restatement of the reference's
+algorithm) on the host's cores over a bounded sample of the workload.
 """
 from __future__ import annotations
 
 import json
-import math
 import os
 import statistics
 import time
@@ -29,7 +39,7 @@ import time
 import numpy as np
 import torch
 
-from bench import ClockSampler, measured_peaks
+from bench import ClockSampler, algorithmic_bytes, measured_peaks
 from visrtx_gb300 import anari, dm, scenes as S
 
 L2_FLUSH_BYTES = 256 * 1024 * 1024
@@ -40,76 +50,238 @@ def _flush(buf):
     torch.cuda.synchronize()
 
 
-def run_volume(args, ws, rank, local):
-    torch.cuda.set_device(local)
-    import __graft_entry__ as g
+def _cores() -> int:
+    return os.cpu_count() or 1
 
-    g.build()
+
+def _frames(frame, steps, warmup, flush, before=None):
+    """Renders warmup + steps frames; returns per-frame (duration s, stats,
+    kernel launches) of the timed ones."""
+    out = []
+    for i in range(warmup + steps):
+        if before:
+            before()
+        _flush(flush)
+        frame.render()
+        frame.wait()
+        if i >= warmup:
+            out.append((frame.get_property("duration", 240), frame.stats(),
+                        frame.kernel_launches()))
+    return out
+
+
+def _roofline(bytes_, seconds, peaks, bound="hbm", traffic=None, **extra):
+    ach = bytes_ / seconds / 1e9
+    r = {"bound": bound, "achieved": round(ach, 1), "peak": peaks["hbm_gbs"], "unit": "GB/s",
+         "frac": round(ach / peaks["hbm_gbs"], 4), "traffic": traffic,
+         "peak_source": peaks["source"]}
+    r.update(extra)
+    return r
+
+
+# ---------------------------------------------------------------------------
+# config 1: the plain 100k-triangle soup, renderer "default"
+# ---------------------------------------------------------------------------
+
+def measure_soup(local=0, steps=20, warmup=5, with_cpu=True):
+    dev = anari.Device(local)
+    spec = S.soup_spec(renderer="default")
+    chans = ("color", "depth", "primitiveId")
+    frame, world, keep = S.build_on_device(dev, spec, channels=chans)
+    ren = frame._keep["renderer"]
+    ren.set("sampleLimit", 0)
+    ren.commit()
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+    res = _frames(frame, steps, warmup, flush)
+    assert not dev.errors(), dev.errors()
+    secs = sum(r[0] for r in res)
+    rays = sum(r[1]["rays"] for r in res)
+    prim = spec.width * spec.height * steps
+    assert all(r[1]["error_flags"] == 0 for r in res)
+    build_ms = float(dev.lib.vrtxWorldBuildMilliseconds(dev.h, world.handle))
+    # counting pass (untimed): nodes and primitive tests of one frame
+    frame.set("vrtx.countTraversal", True)
+    frame.commit()
+    frame.render()
+    frame.wait()
+    cst = frame.stats()
+    kms = frame.kernel_ms()
+    frame.set("vrtx.countTraversal", False)
+    frame.commit()
+    peaks = measured_peaks()
+    fbytes = algorithmic_bytes(cst)
+    # end to end through the C ABI: scene from host arrays, BVH build,
+    # render, the three channels read back
+    e2e, h2d, d2h = [], 0, 0
+    for i in range(4):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        fr2, w2, k2 = S.build_on_device(dev, spec, channels=chans)
+        r2 = fr2._keep["renderer"]
+        r2.set("sampleLimit", 0)
+        r2.commit()
+        fr2.render()
+        outs = [fr2.map("channel." + c) for c in chans]
+        t1 = time.perf_counter()
+        st2 = fr2.stats()
+        if i:  # the first one warms the allocator
+            e2e.append(st2["rays"] / (t1 - t0) / 1e6)
+        h2d = int(spec.surfaces[0].vertices.nbytes)
+        d2h = sum(int(o.nbytes) for o in outs)
+        for o in k2 + [fr2]:
+            o.release()
+    line = {
+        "metric": "Mrays/s", "value": round(rays / secs / 1e6, 2), "unit": "Mrays/s",
+        "steps": steps, "warmup": warmup, "ms_per_step": round(1000 * secs / steps, 4),
+        "dtype": "f32",
+        "config": {"workload": "soup100k_512x384_default_1spp", "renderer": "default",
+                   "l2": "flushed between frames (256 MiB)", "bvh_build_ms": round(build_ms, 2)},
+        "primary_mrays_per_s": round(prim / secs / 1e6, 2),
+        "rays_per_frame": rays / steps,
+        "gpu_launches": sum(r[2] for r in res),
+        "roofline": _roofline(fbytes, kms / 1e3, peaks, kernel="k_render<default>",
+                              algorithmic_bytes_per_launch=fbytes,
+                              launch_ms=round(kms, 4),
+                              nodes_per_ray=round(cst["nodes"] / max(cst["rays"], 1), 2)),
+        "e2e": {"value": round(statistics.median(e2e), 2), "unit": "Mrays/s",
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "includes": "array upload, BVH build, frame, colour/depth/primitiveId read-back"},
+    }
+    for o in keep + [frame]:
+        o.release()
+    dev.release()
+    if with_cpu:
+        line["cpu_baseline"] = cpu_soup()
+    return line
+
+
+def cpu_soup():
+    """The oracle's tracer on the full soup frame, all host threads."""
+    from oracle import oracle as O
+
+    spec = S.soup_spec(renderer="default")
+    sc = O.OracleScene(spec)
+    cores = _cores()
+    sc.render(threads=cores)
+    t0 = time.perf_counter()
+    reps = 0
+    rays = 0
+    while reps < 3 or time.perf_counter() - t0 < 2.0:
+        o = sc.render(threads=cores)
+        rays += o["rays"]
+        reps += 1
+    dt = time.perf_counter() - t0
+    sc.release()
+    return {"value": round(rays / dt / 1e6, 3), "unit": "Mrays/s", "cores": cores,
+            "kind": "port", "sample": f"the full 512x384 frame x {reps} ({dt:.1f} s)"}
+
+
+# ---------------------------------------------------------------------------
+# config 3: the 512^3 structured-regular volume
+# ---------------------------------------------------------------------------
+
+VOLUME_WORKLOAD = "volume512_blobs64_tf256_step0.5_1920x1080_1spp_raycast"
+
+
+def measure_volume(local=0, steps=20, warmup=5, with_cpu=True, cpu_seconds=6.0):
     dev = anari.Device(local)
     field = S.gaussian_blobs((512, 512, 512), 64, 0, device="cuda")
     spec = S.volume_spec(field=field, renderer="raycast", sampling_rate=1.0)
     frame, world, keep = S.build_on_device(dev, spec, channels=("color", "depth"))
     cam = frame._keep["camera"]
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
-
-    def one():
-        cam.commit()  # raycast renders one sample per reset (sampleLimit 1)
-        _flush(flush)
-        frame.render()
-        frame.wait()
-        return frame.get_property("duration", 240), frame.stats(), frame.kernel_ms()
-
-    for _ in range(args.warmup):
-        one()
     clocks = ClockSampler(local)
     clocks.start()
-    durs, kms, samples, fetches, rays = [], [], 0, 0, 0
-    for _ in range(args.steps):
-        d, st, km = one()
-        durs.append(d)
-        kms.append(km)
-        samples += st["volume_samples"]
-        fetches += st["volume_fetches"]
-        rays += st["rays"]
+    res = _frames(frame, steps, warmup, flush, before=cam.commit)
     clk = clocks.stop()
-    secs = sum(durs)
+    kms = frame.kernel_ms()
+    assert not dev.errors(), dev.errors()
+    secs = sum(r[0] for r in res)
+    samples = sum(r[1]["volume_samples"] for r in res)
+    fetches = sum(r[1]["volume_fetches"] for r in res)
+    rays = sum(r[1]["rays"] for r in res)
     peaks = measured_peaks()
-    # compulsory bytes per frame: the field once (upper bound: every brick
-    # touched), majorants, TF, framebuffer writes
     n = 512
     compulsory = n ** 3 * 4 + (n // 16) ** 3 * 4 + 256 * 16 + 1920 * 1080 * 8
-    kmean = statistics.mean(kms) / 1e3
+    # end to end: the field from pinned host memory through a new array,
+    # commit (texture upload, grids), render, colour read-back
+    host = field.cpu().pin_memory()
+    spec_h = S.volume_spec(field=host.numpy(), renderer="raycast", sampling_rate=1.0)
+    e2e = []
+    for i in range(3):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        fr2, w2, k2 = S.build_on_device(dev, spec_h, channels=("color",))
+        fr2.render()
+        col = fr2.map("channel.color")
+        t1 = time.perf_counter()
+        st2 = fr2.stats()
+        if i:
+            e2e.append(st2["volume_samples"] / (t1 - t0) / 1e6)
+        for o in k2 + [fr2]:
+            o.release()
     line = {
-        "metric": "Msamples/s", "value": round(samples / secs / 1e6, 2), "unit": "Msamples/s",
-        "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": round(1000 * secs / args.steps, 3), "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": "volume512_blobs64_tf256_step0.5_1920x1080_1spp_raycast",
-                   "l2": "flushed between frames (256 MiB)"},
+        "metric": "Msamples/s", "value": round(samples / secs / 1e6, 1), "unit": "Msamples/s",
+        "steps": steps, "warmup": warmup, "ms_per_step": round(1000 * secs / steps, 4),
+        "dtype": "f32",
+        "config": {"workload": VOLUME_WORKLOAD, "l2": "flushed between frames (256 MiB)"},
         "mrays_per_s": round(rays / secs / 1e6, 2),
-        "samples_per_frame": samples / args.steps,
+        "samples_per_frame": samples / steps,
         "fetched_fraction": round(fetches / max(samples, 1), 4),
-        "roofline": {"bound": "hbm", "achieved": round(compulsory / kmean / 1e9, 1),
-                     "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                     "frac": round(compulsory / kmean / 1e9 / peaks["hbm_gbs"], 4),
-                     "traffic": None, "algorithmic_bytes_per_launch": compulsory},
+        "gpu_launches": sum(r[2] for r in res),
+        "roofline": _roofline(compulsory, kms / 1e3, peaks, kernel="k_render<raycast, volumes>",
+                              algorithmic_bytes_per_launch=compulsory, launch_ms=round(kms, 4),
+                              note="compulsory bytes (the field once, grids, TF, framebuffer)"
+                                   "; the march is texture- and issue-bound"),
+        "e2e": {"value": round(statistics.median(e2e), 1), "unit": "Msamples/s",
+                "h2d_bytes_per_step": int(host.numel() * 4), "d2h_bytes_per_step": int(col.nbytes),
+                "includes": "field upload (pinned host), texture + grid build, frame, read-back"},
         "clocks": clk,
     }
-    print(json.dumps(line), flush=True)
+    for o in keep + [frame]:
+        o.release()
     dev.release()
+    del field, host
+    torch.cuda.empty_cache()
+    if with_cpu:
+        line["cpu_baseline"] = cpu_volume(spec_h, cpu_seconds)
+    return line
 
 
-def run_nanovdb(args, ws, rank, local):
-    torch.cuda.set_device(local)
-    import __graft_entry__ as g
+def cpu_volume(spec, seconds):
+    """The oracle's parity-mode marcher (FP32, the texture unit's filter
+    restated) on a band of rows through the middle of the frame."""
+    from oracle import oracle as O
 
+    sc = O.OracleScene(spec)
+    cores = _cores()
+    mid = spec.height // 2
+    t0 = time.perf_counter()
+    sc.render(rows=(mid - 2, mid + 2), threads=cores)
+    per_row = (time.perf_counter() - t0) / 4
+    band = int(min(spec.height, max(4, seconds / max(per_row, 1e-6))))
+    r0 = max(0, mid - band // 2)
+    r1 = min(spec.height, r0 + band)
+    t0 = time.perf_counter()
+    o = sc.render(rows=(r0, r1), threads=cores)
+    dt = time.perf_counter() - t0
+    sc.release()
+    return {"value": round(o["volume_samples"] / dt / 1e6, 3), "unit": "Msamples/s",
+            "cores": cores, "kind": "port",
+            "sample": f"rows {r0}-{r1} of 1920x1080 ({o['volume_samples']} samples, {dt:.1f} s)"}
+
+
+# ---------------------------------------------------------------------------
+# NanoVDB (opt-in)
+# ---------------------------------------------------------------------------
+
+def measure_nanovdb(local=0, steps=5, warmup=3, nvdb_type="fp16"):
     from visrtx_gb300 import nanovdb as NV
 
-    g.build()
     dev = anari.Device(local)
     field = S.gaussian_blobs((512, 512, 512), 64, 0, device="cuda").cpu().numpy()
     t0 = time.time()
-    grid = NV.build_grid(field, field >= 0.02, grid_type=args.nvdb_type)
+    grid = NV.build_grid(field, field >= 0.02, grid_type=nvdb_type)
     build_s = time.time() - t0
     info = NV.grid_info(grid)
     del field
@@ -117,51 +289,40 @@ def run_nanovdb(args, ws, rank, local):
     frame, world, keep = S.build_on_device(dev, spec, channels=("color", "depth"))
     cam = frame._keep["camera"]
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
-
-    def one():
-        cam.commit()
-        _flush(flush)
-        frame.render()
-        frame.wait()
-        return frame.get_property("duration", 240), frame.stats(), frame.kernel_ms()
-
-    for _ in range(args.warmup):
-        one()
     clocks = ClockSampler(local)
     clocks.start()
-    durs, kms, samples, rays = [], [], 0, 0
-    for _ in range(args.steps):
-        d, st, km = one()
-        durs.append(d)
-        kms.append(km)
-        samples += st["volume_samples"]
-        rays += st["rays"]
+    res = _frames(frame, steps, warmup, flush, before=cam.commit)
     clk = clocks.stop()
-    secs = sum(durs)
+    kms = frame.kernel_ms()
+    secs = sum(r[0] for r in res)
+    samples = sum(r[1]["volume_samples"] for r in res)
+    rays = sum(r[1]["rays"] for r in res)
     peaks = measured_peaks()
-    compulsory = int(grid.size) + 256 * 16 + 1920 * 1080 * 8  # the grid once, TF, framebuffer
-    kmean = statistics.mean(kms) / 1e3
+    compulsory = int(grid.size) + 256 * 16 + 1920 * 1080 * 8
     line = {
         "metric": "Msamples/s", "value": round(samples / secs / 1e6, 2), "unit": "Msamples/s",
-        "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": round(1000 * secs / args.steps, 3), "higher_is_better": True,
+        "n_gpus": 1, "steps": steps, "warmup": warmup,
+        "ms_per_step": round(1000 * secs / steps, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": f"nanovdb512_{args.nvdb_type}_blobs64_tf256_step0.5_1920x1080"
+        "config": {"workload": f"nanovdb512_{nvdb_type}_blobs64_tf256_step0.5_1920x1080"
                                "_1spp_raycast",
                    "grid_bytes": int(grid.size), "active_voxels": info["voxels"],
                    "leaves": info["leaves"], "grid_build_s": round(build_s, 1),
                    "l2": "flushed between frames (256 MiB)"},
         "mrays_per_s": round(rays / secs / 1e6, 2),
-        "samples_per_frame": samples / args.steps,
-        "roofline": {"bound": "hbm", "achieved": round(compulsory / kmean / 1e9, 1),
-                     "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                     "frac": round(compulsory / kmean / 1e9 / peaks["hbm_gbs"], 4),
-                     "traffic": None, "algorithmic_bytes_per_launch": compulsory},
+        "samples_per_frame": samples / steps,
+        "roofline": _roofline(compulsory, kms / 1e3, peaks, algorithmic_bytes_per_launch=compulsory),
         "clocks": clk,
     }
-    print(json.dumps(line), flush=True)
+    for o in keep + [frame]:
+        o.release()
     dev.release()
+    return line
 
+
+# ---------------------------------------------------------------------------
+# configs 4 and 5: the differentiable marcher
+# ---------------------------------------------------------------------------
 
 def _dm_problem(n=256, views=128, res=512, dtype=torch.float16, seed=0):
     d = S.gaussian_blobs((n, n, n), 32, seed, device="cuda")
@@ -170,12 +331,11 @@ def _dm_problem(n=256, views=128, res=512, dtype=torch.float16, seed=0):
     scale = torch.tensor([1.0], device="cuda")
     vol = dm.VolumeInput(d.to(dtype).contiguous(), tf, scale,
                          step=0.5, unit=1.0, value_range=(0.0, 1.0))
-    vol32 = dm.VolumeInput(d, tf, scale, step=0.5, unit=1.0, value_range=(0.0, 1.0), plain=True)
     tgt = dm.VolumeInput(S.gaussian_blobs((n, n, n), 32, seed + 1, device="cuda"), tf, scale,
                          step=0.5, unit=1.0, value_range=(0.0, 1.0))
     dirs = S.fibonacci_sphere(views)
     vws = [dm.look_at_view(0, vol.dims, 2.0 * dirs[i], 45.0, res, res) for i in range(views)]
-    return vol, vol32, tgt, vws
+    return vol, d, tgt, vws
 
 
 def _time_steps(fn, steps, warmup, flush):
@@ -219,23 +379,31 @@ def _batched_step(vols, views, tile, target):
     graph = torch.cuda.CUDAGraph()
     with torch.cuda.graph(graph):
         body()
-    return p, graph, target
+    return p, graph
 
 
 def _per_view_fp32_step(vols32, views, target):
+    """The FP32 one-view-per-launch form: a forward and a backward launch
+    per view, gradients into one set of buffers per volume."""
     targets, off = [], 0
     for w in views:
         targets.append(target[off:off + w.width * w.height])
         off += w.width * w.height
+    grads = [(torch.zeros(v.density.shape, device="cuda"), torch.zeros(v.tf.shape, device="cuda"),
+              torch.zeros(1, device="cuda")) for v in vols32]
+    batches = [dm.Batch([vols32[w.volume]], [dm.View(0, w.width, w.height, w.eye, w.d00, w.du,
+                                                      w.dv, w.background)], (16, 8))
+               for w in views]
 
     def body():
+        for gd, gt, gs in grads:
+            gd.zero_()
+            gt.zero_()
+            gs.zero_()
         for i, w in enumerate(views):
-            v = vols32[w.volume]
-            b = dm.Batch([v], [dm.View(0, w.width, w.height, w.eye, w.d00, w.du, w.dv,
-                                       w.background)], (16, 8))
-            img, st = dm.forward(b)
-            dm.backward(b, st, 2.0 * (img - targets[i]))
-    return body
+            img, st = dm.forward(batches[i])
+            dm.backward(batches[i], st, 2.0 * (img - targets[i]), grads=[grads[w.volume]])
+    return body, grads
 
 
 def _targets(target_vols, views):
@@ -245,66 +413,133 @@ def _targets(target_vols, views):
     return img
 
 
-def _dm_line(name, workload, vols, vols32, targets, views, args, local):
-    torch.cuda.set_device(local)
+def _dm_measure(workload, vols, dens32, targets, views, steps, warmup, fp32_steps,
+                with_cpu=True):
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
     target = _targets(targets, views)
-    cache = os.path.join(os.path.expanduser("~"), ".cache", "vrtx", "dm_tune.json")
-    tile = dm.autotune(vols, views, reps=1, cache=cache)
-    p, graph, _ = _batched_step(vols, views, tile, target)
-    clocks = ClockSampler(local)
+    # the tile search times a forward + backward of up to 96 of the views
+    tile = dm.autotune(vols, views[:96], reps=1)
+    p, graph = _batched_step(vols, views, tile, target)
+    clocks = ClockSampler(torch.cuda.current_device())
     clocks.start()
-    tb = _time_steps(graph.replay, args.steps, args.warmup, flush)
+    tb = _time_steps(graph.replay, steps, warmup, flush)
     clk = clocks.stop()
-    # the plain FP32 one-view-per-launch form on the same views (the FP32
-    # fields the low-precision copies were made from, direct atomics)
-    body32 = _per_view_fp32_step(vols32, views, target)
-    t32 = _time_steps(body32, max(1, args.steps // 2), 1, flush)
-    # image error of the batched low-precision form against FP32
-    b32 = dm.Batch(vols32, views, tile)
-    img32, _ = dm.forward(b32)
-    rms = float(torch.sqrt(torch.mean((p.image - img32) ** 2)))
     nviews = len(views)
     vps = nviews / statistics.median(tb)
-    vps32 = nviews / statistics.median(t32)
+    # the FP32 one-view-per-launch forms on the same views, from the FP32
+    # fields the low-precision copies were made from: staged gradient
+    # accumulation (the library's default) and one atomic per term
+    out = {}
+    for name, plain in (("staged", False), ("plain", True)):
+        v32 = [dm.VolumeInput(d, v.tf, v.scale, v.step, v.unit, v.value_range, plain=plain)
+               for d, v in zip(dens32, vols)]
+        body, _ = _per_view_fp32_step(v32, views, target)
+        t32 = _time_steps(body, fp32_steps, 1, flush)
+        out[name] = nviews / statistics.median(t32)
+    # image and gradient error of the batched low-precision form against
+    # the FP32 form (same views, same loss)
+    v32 = [dm.VolumeInput(d, v.tf, v.scale, v.step, v.unit, v.value_range)
+           for d, v in zip(dens32, vols)]
+    b32 = dm.Batch(v32, views, tile)
+    img32, st32 = dm.forward(b32)
+    g32 = dm.backward(b32, st32, 2.0 * (img32 - target))
+    graph.replay()
+    torch.cuda.synchronize()
+    rms = float(torch.sqrt(torch.mean((p.image - img32) ** 2)))
+    gnum = sum(float(torch.sum((a[0] - b[0]) ** 2)) for a, b in zip(p.grads, g32))
+    gden = sum(float(torch.sum(b[0] ** 2)) for b in g32)
+    grel = (gnum / max(gden, 1e-30)) ** 0.5
     dens_bytes = sum(v.density.numel() * v.density.element_size() for v in vols)
+    peaks = measured_peaks()
+    # compulsory bytes per step: the density read by the forward and again
+    # by the backward, the FP32 density gradient written, the image written
+    # and read back
+    comp = 2 * dens_bytes + sum(v.density.numel() * 4 for v in vols) + p.image.numel() * 4 * 2
     line = {
         "metric": "views/s (fwd+bwd)", "value": round(vps, 2), "unit": "views/s",
-        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": round(1000 * statistics.median(tb), 3), "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None,
+        "steps": steps, "warmup": warmup, "ms_per_step": round(1000 * statistics.median(tb), 3),
         "dtype": {torch.float16: "f16", torch.bfloat16: "bf16"}.get(vols[0].density.dtype, "f32"),
-        "data": "synthetic", "config": {"workload": workload, "tile": list(tile),
-                                        "pixels": int(p.batch.pixels),
-                                        "l2": "flushed between steps (256 MiB)"},
-        "fp32_one_view_per_launch_views_per_s": round(vps32, 2),
-        "speedup_vs_fp32_per_view": round(vps / vps32, 2),
-        "rms_vs_fp32": rms,
-        "density_bytes": dens_bytes,
+        "config": {"workload": workload, "tile": list(tile), "pixels": int(p.batch.pixels),
+                   "views": nviews, "l2": "flushed between steps (256 MiB)"},
+        "fp32_per_view_staged_views_per_s": round(out["staged"], 2),
+        "fp32_per_view_plain_views_per_s": round(out["plain"], 2),
+        "speedup_vs_fp32_per_view_staged": round(vps / out["staged"], 2),
+        "speedup_vs_fp32_per_view_plain": round(vps / out["plain"], 2),
+        "image_rms_vs_fp32": rms,
+        "density_grad_rel_err_vs_fp32": grel,
+        "gpu_launches": 2 * steps,
+        "roofline": _roofline(comp, statistics.median(tb), peaks, kernel="k_dmForward+k_dmBackward",
+                              algorithmic_bytes_per_launch=comp,
+                              note="compulsory bytes per step; the march is issue-bound"),
         "clocks": clk,
-        "gpu_launches": 2 * 1,
     }
-    print(json.dumps(line), flush=True)
     p.release()
+    return line, target
 
 
-def run_dm(args, ws, rank, local):
+def measure_dm(local=0, steps=10, warmup=3, views=128, with_cpu=True):
     torch.cuda.set_device(local)
-    import __graft_entry__ as g
+    vol, d32, tgt, vws = _dm_problem(views=views)
+    line, target = _dm_measure(f"dm256_fp16_{len(vws)}views_512x512", [vol], [d32], [tgt], vws,
+                               steps, warmup, max(1, min(steps, 3)))
+    # end to end through the autograd API: FP16 density and TF copied from
+    # pinned host memory, forward + loss + backward, the loss and the
+    # density gradient read back
+    hd = vol.density.cpu().pin_memory()
+    ht = vol.tf.cpu().pin_memory()
+    tile = tuple(line["config"]["tile"])
+    e2e = []
+    for i in range(3):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        d = hd.to("cuda", non_blocking=True).requires_grad_()
+        tf = ht.to("cuda", non_blocking=True).requires_grad_()
+        v = dm.VolumeInput(d, tf, vol.scale, 0.5, 1.0, (0.0, 1.0))
+        img = dm.render(dm.Batch([v], vws, tile))
+        loss = torch.sum((img - target) ** 2)
+        loss.backward()
+        lv = float(loss.item())
+        gcpu = d.grad.cpu()
+        t1 = time.perf_counter()
+        if i:
+            e2e.append(len(vws) / (t1 - t0))
+    line["e2e"] = {"value": round(statistics.median(e2e), 2), "unit": "views/s",
+                   "h2d_bytes_per_step": int(hd.numel() * 2 + ht.numel() * 4),
+                   "d2h_bytes_per_step": int(gcpu.numel() * gcpu.element_size() + 4),
+                   "includes": "density + TF upload, forward, loss, backward through the "
+                               "autograd Function, loss and density-gradient read-back",
+                   "loss": lv}
+    if with_cpu:
+        line["cpu_baseline"] = cpu_dm(vol, vws[0])
+    return line
 
-    g.build()
-    vol, vol32, tgt, views = _dm_problem(views=args.dm_views)
-    _dm_line("dm", f"dm256_fp16_{len(views)}views_512x512", [vol], [vol32], [tgt], views, args,
-             local)
+
+def cpu_dm(vol, view, rows=32):
+    """The FP64 oracle forward + adjoint on a band of rows of one 512x512
+    view, all host threads; views/s scaled from the band's pixels."""
+    from oracle import oracle as O
+
+    d = vol.density.float().cpu().numpy()
+    tf = vol.tf.cpu().numpy()
+    r0 = view.height // 2 - rows // 2
+    d00 = tuple(np.asarray(view.d00) + r0 * np.asarray(view.dv))
+    vw = {"width": view.width, "height": rows, "eye": view.eye, "d00": d00, "du": view.du,
+          "dv": view.dv, "background": view.background}
+    g = np.ones((rows, view.width, 3))
+    cores = _cores()
+    t0 = time.perf_counter()
+    O.dm(d, tf, vw, 1.0, 0.5, 1.0, (0.0, 1.0), grad_image=g, threads=cores)
+    dt = time.perf_counter() - t0
+    frac = rows / view.height
+    return {"value": round(frac / dt, 4), "unit": "views/s", "cores": cores, "kind": "port",
+            "sample": f"FP64 forward + adjoint, rows {r0}-{r0 + rows} of one 512x512 view "
+                      f"({dt:.1f} s), scaled to the view"}
 
 
-def run_batched(args, ws, rank, local):
+def measure_batched(local=0, steps=3, warmup=3, with_cpu=True):
     torch.cuda.set_device(local)
-    import __graft_entry__ as g
-
-    g.build()
     rng = S.Rng(5, stream=17)
-    vols, vols32, tgts, views = [], [], [], []
+    vols, dens32, tgts, views = [], [], [], []
     res_choices = [256, 512, 1024]
     for i in range(64):
         dims = tuple(int(x) for x in rng.uniform(3, 64, 385).astype(int))
@@ -314,7 +549,7 @@ def run_batched(args, ws, rank, local):
         scale = torch.tensor([1.0], device="cuda")
         vols.append(dm.VolumeInput(d.to(torch.bfloat16).contiguous(), tf, scale, 0.5, 1.0,
                                    (0.0, 1.0)))
-        vols32.append(dm.VolumeInput(d, tf, scale, 0.5, 1.0, (0.0, 1.0), plain=True))
+        dens32.append(d)
         t = S.gaussian_blobs(dims, 16, 5000 + i, device="cuda", sigma_scale=max(dims) / 512)
         tgts.append(dm.VolumeInput(t, tf, scale, 0.5, 1.0, (0.0, 1.0)))
         nv = int(rng.uniform(1, 4, 33)[0])
@@ -323,5 +558,38 @@ def run_batched(args, ws, rank, local):
             w = res_choices[int(rng.uniform(1, 0, 3)[0])]
             h = res_choices[int(rng.uniform(1, 0, 3)[0])]
             views.append(dm.look_at_view(i, vols[-1].dims, 2.0 * dirs[k], 45.0, w, h))
-    _dm_line("batched", f"batched64_bf16_{len(views)}views_uneven", vols, vols32, tgts, views,
-             args, local)
+    line, _ = _dm_measure(f"batched64_bf16_{len(views)}views_uneven", vols, dens32, tgts, views,
+                          steps, warmup, 1)
+    del vols, dens32, tgts
+    torch.cuda.empty_cache()
+    return line
+
+
+# ---------------------------------------------------------------------------
+# `python bench.py --workload <name>`: one workload's line alone
+# ---------------------------------------------------------------------------
+
+def _print(line, ws):
+    full = {"n_gpus": ws, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "data": "synthetic"}
+    full.update(line)
+    print(json.dumps(full), flush=True)
+
+
+def run(name, args, ws, rank, local):
+    torch.cuda.set_device(local)
+    import __graft_entry__ as g
+
+    g.build()
+    if rank != 0:
+        return
+    if name == "soup":
+        _print(measure_soup(local, args.steps, args.warmup), ws)
+    elif name == "volume":
+        _print(measure_volume(local, args.steps, args.warmup), ws)
+    elif name == "nanovdb":
+        _print(measure_nanovdb(local, args.steps, args.warmup, args.nvdb_type), ws)
+    elif name == "dm":
+        _print(measure_dm(local, args.steps, args.warmup, args.dm_views), ws)
+    elif name == "batched":
+        _print(measure_batched(local, args.steps, args.warmup), ws)

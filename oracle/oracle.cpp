@@ -394,10 +394,14 @@ float tex3dLinear(const float *v, const int d[3], float cx, float cy, float cz, 
   return sum.toFloatTiesAway();
 }
 
+// nearest filtering: the coordinate truncated to 21 fractional bits, then
+// floor(u * n) clamped (as the texture unit; see texSample)
 float tex3dPoint(const float *v, const int d[3], float cx, float cy, float cz)
 {
   auto idx = [](float c, int n) {
-    return std::min(std::max((int)std::floor(c * (float)n), 0), n - 1);
+    const double u = std::isfinite(c) ? std::floor((double)c * 2097152.0) / 2097152.0 : 0.0;
+    const double x = std::min(std::max(std::floor(u * n), 0.0), (double)(n - 1));
+    return (int)x;
   };
   return v[((size_t)idx(cz, d[2]) * d[1] + idx(cy, d[1])) * d[0] + idx(cx, d[0])];
 }
@@ -1366,6 +1370,7 @@ struct Ctx
   int volMode;
   int texRound;
   uint64_t rays = 0;
+  uint64_t samples = 0; // volume march positions
   // per volume: the reference's delta-tracking majorants (dpt only)
   const std::vector<std::vector<float>> *dptMaj = nullptr;
 };
@@ -1663,6 +1668,7 @@ float rayMarchVolume(Ctx &C, const OrcVolume &v, const VolHit &h, Stream &rs, V3
   if (C.volMode == 0) {
     float T = 1.f;
     while (opacity < 0.99f && upper - lower >= 0.f) {
+      C.samples++;
       const V3 p = h.lo + h.ld * lower;
       const float s = sampleFieldParity(v, p, C.texRound);
       if (!std::isnan(s)) {
@@ -1688,6 +1694,7 @@ float rayMarchVolume(Ctx &C, const OrcVolume &v, const VolHit &h, Stream &rs, V3
   double col[3] = {0, 0, 0};
   const double sx = v.spacing[0], sy = v.spacing[1], sz = v.spacing[2];
   for (long k = 0; op < 0.99 && (double)upper - lo >= 0.0; k++) {
+    C.samples++;
     const double px = (double)h.lo.x + (double)h.ld.x * lo;
     const double py = (double)h.lo.y + (double)h.ld.y * lo;
     const double pz = (double)h.lo.z + (double)h.ld.z * lo;
@@ -2167,73 +2174,118 @@ V4 readAttribute(const SceneCtx &S, const SHit &sh, int id)
 }
 
 // Texture lookup with normalised coordinates, float4 texels: address modes
-// clamp / wrap / mirror, point or linear filtering (8-bit weights,
-// round-to-nearest, as the emulation of the TF path)
-int wrapIndex(int i, int n, int mode)
+// clamp (0) / repeat (1) / mirror (2), point or linear filtering, as the
+// texture unit computes them (recovered from GPU-captured sweeps of every
+// mode in 1D, 2D and 3D and reproduced bit for bit):
+//  * the coordinate is truncated to 21 fractional bits;
+//  * point: clamp takes floor(u * n) clamped; repeat the same of u's
+//    fraction; mirror folds u into [0, 1] over a period of 2 first;
+//  * linear: x = u * n - 0.5 and the fraction rounded half up to 8 bits, as
+//    hwAxis; clamp clamps x to [0, n - 1]; repeat takes u's fraction
+//    first and wraps the texel indices; mirror mirrors the texel indices
+//    (period 2n) of the unfolded x;
+//  * the corner weights are integers summing to 256 (hwCornerWeights) and
+//    the value is their exact weighted sum rounded once to float.
+int wrapIndex(long long i, int n, int mode)
 {
   if (mode == 1) {
-    i %= n;
-    return i < 0 ? i + n : i;
+    long long m = i % n;
+    return (int)(m < 0 ? m + n : m);
   }
   if (mode == 2) {
-    const int p = 2 * n;
-    int m = i % p;
+    const long long p = 2LL * n;
+    long long m = i % p;
     if (m < 0)
       m += p;
-    return m < n ? m : p - 1 - m;
+    return (int)(m < n ? m : p - 1 - m);
   }
-  return std::min(std::max(i, 0), n - 1);
+  return (int)std::min(std::max(i, 0LL), (long long)n - 1);
 }
 
-float wrapCoord(float c, int mode)
+// texel pair (or the single texel, i0 == i1, w == 0) of one axis
+void hwTap(float coord, int n, int mode, int linear, int &i0, int &i1, int &w)
 {
-  if (mode == 1)
-    return c - std::floor(c);
-  if (mode == 2) {
-    const float f = std::floor(c);
-    const float r = c - f;
-    return ((long long)f % 2 != 0) ? 1.f - r : r;
+  double u = std::isfinite(coord) ? std::floor((double)coord * 2097152.0) / 2097152.0 : 0.0;
+  if (!linear) {
+    double x;
+    if (mode == 1)
+      x = (u - std::floor(u)) * n;
+    else if (mode == 2) {
+      const double t = u - 2.0 * std::floor(u * 0.5);
+      x = (t > 1.0 ? 2.0 - t : t) * n;
+    } else
+      x = u * n;
+    i0 = i1 = wrapIndex((long long)std::floor(std::min(std::max(x, -1.0), (double)n + 1.0)), n,
+        mode == 1 ? 1 : 0);
+    w = 0;
+    return;
   }
-  return c;
+  if (mode == 1)
+    u -= std::floor(u);
+  double x = u * (double)n - 0.5;
+  if (mode == 0)
+    x = std::min(std::max(x, 0.0), (double)(n - 1));
+  else
+    x = std::min(std::max(x, -4.0 * n), 4.0 * n);
+  const double fl = std::floor(x);
+  long long i = (long long)fl;
+  w = (int)std::floor((x - fl) * 256.0 + 0.5);
+  if (w >= 256) {
+    w = 0;
+    i++;
+  }
+  i0 = wrapIndex(i, n, mode);
+  i1 = wrapIndex(i + 1, n, mode);
+}
+
+// Integer corner weights (sum 256) of a linear fetch from the per-axis
+// 8-bit weights w[]: corner q = x + 2y + 4z. 3D splits z, then x within
+// each z slice, then y within each x column; 2D is one slice of budget 256;
+// the y split rounds half down in the x0 column and half up in the x1
+// column, the x split half up.
+void hwCornerWeights(int ndim, const int w[3], int out[8])
+{
+  for (int q = 0; q < 8; q++)
+    out[q] = 0;
+  if (ndim == 1) {
+    out[0] = 256 - w[0];
+    out[1] = w[0];
+    return;
+  }
+  for (int z = 0; z < (ndim == 3 ? 2 : 1); z++) {
+    const int B = ndim == 3 ? (z ? w[2] : 256 - w[2]) : 256;
+    const int x1 = (w[0] * B + 128) >> 8;
+    for (int x = 0; x < 2; x++) {
+      const int C = x ? x1 : B - x1;
+      const int y1 = (w[1] * C + (x ? 128 : 127)) >> 8;
+      out[x + 4 * z] = C - y1;
+      out[x + 2 + 4 * z] = y1;
+    }
+  }
 }
 
 V4 texSample(const OrcSampler &sm, int ndim, const float tc[3])
 {
-  int i0[3] = {0, 0, 0}, i1[3] = {0, 0, 0};
-  float w[3] = {0.f, 0.f, 0.f};
-  for (int k = 0; k < ndim; k++) {
-    const int n = sm.dims[k];
-    const float c = wrapCoord(tc[k], sm.wrap[k]);
-    if (sm.filter == 0) {
-      i0[k] = i1[k] = wrapIndex((int)std::floor(c * (float)n), n, sm.wrap[k]);
-    } else {
-      const float x = c * (float)n - 0.5f;
-      const float fl = std::floor(x);
-      w[k] = quantW(x - fl, 1);
-      i0[k] = wrapIndex((int)fl, n, sm.wrap[k]);
-      i1[k] = wrapIndex((int)fl + 1, n, sm.wrap[k]);
-    }
-  }
+  int i0[3] = {0, 0, 0}, i1[3] = {0, 0, 0}, w[3] = {0, 0, 0};
+  for (int k = 0; k < ndim; k++)
+    hwTap(tc[k], sm.dims[k], sm.wrap[k], sm.filter != 0, i0[k], i1[k], w[k]);
   auto at = [&](int x, int y, int z, int c) {
     return sm.image[4 * (((size_t)z * sm.dims[1] + y) * sm.dims[0] + x) + c];
   };
+  if (sm.filter == 0)
+    return {at(i0[0], i0[1], i0[2], 0), at(i0[0], i0[1], i0[2], 1), at(i0[0], i0[1], i0[2], 2),
+        at(i0[0], i0[1], i0[2], 3)};
+  int cw[8];
+  hwCornerWeights(ndim, w, cw);
   float out[4];
   for (int c = 0; c < 4; c++) {
-    const float c00 = (1.f - w[0]) * at(i0[0], i0[1], i0[2], c) + w[0] * at(i1[0], i0[1], i0[2], c);
-    if (ndim == 1) {
-      out[c] = c00;
-      continue;
-    }
-    const float c10 = (1.f - w[0]) * at(i0[0], i1[1], i0[2], c) + w[0] * at(i1[0], i1[1], i0[2], c);
-    const float c0 = (1.f - w[1]) * c00 + w[1] * c10;
-    if (ndim == 2) {
-      out[c] = c0;
-      continue;
-    }
-    const float c01 = (1.f - w[0]) * at(i0[0], i0[1], i1[2], c) + w[0] * at(i1[0], i0[1], i1[2], c);
-    const float c11 = (1.f - w[0]) * at(i0[0], i1[1], i1[2], c) + w[0] * at(i1[0], i1[1], i1[2], c);
-    const float c1 = (1.f - w[1]) * c01 + w[1] * c11;
-    out[c] = (1.f - w[2]) * c0 + w[2] * c1;
+    ExactSum sum;
+    for (int q = 0; q < 8; q++)
+      if (cw[q])
+        sum.add((double)cw[q] * (1.0 / 256.0)
+            * (double)at((q & 1) ? i1[0] : i0[0], (q & 2) ? i1[1] : i0[1],
+                (q & 4) ? i1[2] : i0[2], c));
+    out[c] = sum.toFloatTiesAway();
   }
   return {out[0], out[1], out[2], out[3]};
 }
@@ -2334,28 +2386,26 @@ struct LightSample
   float dist, pdf;
 };
 
-// the HDRI texture: float4 texels (rgb, 1), linear filtering with 8-bit
-// weights, normalised coordinates, x repeat, y clamp (HDRI.cu:121-122)
+// the HDRI texture: float4 texels (rgb, 1), linear filtering, normalised
+// coordinates, x repeat, y clamp (HDRI.cu:121-122), as the texture unit
+// filters (texSample)
 V3 hdriTexel(const OrcLight &L, float u, float v)
 {
   const int W = L.hdriW, H = L.hdriH;
-  const float cu = u - std::floor(u); // repeat
-  const float xs = cu * (float)W - 0.5f, ys = v * (float)H - 0.5f;
-  const float fx = std::floor(xs), fy = std::floor(ys);
-  const float a = quantW(xs - fx, 1), b = quantW(ys - fy, 1);
-  auto wrapX = [&](int i) {
-    i %= W;
-    return i < 0 ? i + W : i;
-  };
-  auto clampY = [&](int j) { return std::min(std::max(j, 0), H - 1); };
-  const int x0 = wrapX((int)fx), x1 = wrapX((int)fx + 1);
-  const int y0 = clampY((int)fy), y1 = clampY((int)fy + 1);
+  int x0, x1, y0, y1, w[3] = {0, 0, 0};
+  hwTap(u, W, 1, 1, x0, x1, w[0]);
+  hwTap(v, H, 0, 1, y0, y1, w[1]);
+  int cw[8];
+  hwCornerWeights(2, w, cw);
   float out[3];
   for (int c = 0; c < 3; c++) {
     auto at = [&](int x, int y) { return L.hdri[3 * ((size_t)y * W + x) + c]; };
-    const float r0 = (1.f - a) * at(x0, y0) + a * at(x1, y0);
-    const float r1 = (1.f - a) * at(x0, y1) + a * at(x1, y1);
-    out[c] = (1.f - b) * r0 + b * r1;
+    ExactSum sum;
+    const float t[4] = {at(x0, y0), at(x1, y0), at(x0, y1), at(x1, y1)};
+    for (int q = 0; q < 4; q++)
+      if (cw[q])
+        sum.add((double)cw[q] * (1.0 / 256.0) * (double)t[q]);
+    out[c] = sum.toFloatTiesAway();
   }
   return v3(out[0], out[1], out[2]);
 }
@@ -2397,22 +2447,25 @@ uint8_t bgTexel(const OrcRenderer &R, size_t i, int c)
 }
 
 // normalised-float reads of the RGBA8 image: linear, clamped, normalised
-// coordinates, 8-bit weights
+// coordinates. The texture unit filters 8-bit normalised texels as
+// integers: the weighted sum F of the bytes (weights summing to 256) is
+// scaled to a 16-bit normalised value R = round-half-up(F * 257 / 256) and
+// read as R / 65535.
 V4 bgImageAt(const OrcRenderer &R, float u, float v)
 {
   const int W = R.bgW, H = R.bgH;
-  const float xs = u * (float)W - 0.5f, ys = v * (float)H - 0.5f;
-  const float fx = std::floor(xs), fy = std::floor(ys);
-  const float a = quantW(xs - fx, 1), b = quantW(ys - fy, 1);
-  auto cx = [&](int i) { return std::min(std::max(i, 0), W - 1); };
-  auto cy = [&](int j) { return std::min(std::max(j, 0), H - 1); };
-  const int x0 = cx((int)fx), x1 = cx((int)fx + 1), y0 = cy((int)fy), y1 = cy((int)fy + 1);
+  int x0, x1, y0, y1, w[3] = {0, 0, 0};
+  hwTap(u, W, 0, 1, x0, x1, w[0]);
+  hwTap(v, H, 0, 1, y0, y1, w[1]);
+  int cw[8];
+  hwCornerWeights(2, w, cw);
   float out[4];
   for (int c = 0; c < 4; c++) {
-    auto at = [&](int x, int y) { return bgTexel(R, (size_t)y * W + x, c) / 255.f; };
-    const float r0 = (1.f - a) * at(x0, y0) + a * at(x1, y0);
-    const float r1 = (1.f - a) * at(x0, y1) + a * at(x1, y1);
-    out[c] = (1.f - b) * r0 + b * r1;
+    auto at = [&](int x, int y) { return (int64_t)bgTexel(R, (size_t)y * W + x, c); };
+    const int64_t F = cw[0] * at(x0, y0) + cw[1] * at(x1, y0) + cw[2] * at(x0, y1)
+        + cw[3] * at(x1, y1);
+    const int64_t r16 = (F * 257 + 128) >> 8;
+    out[c] = (float)((double)r16 / 65535.0);
   }
   return {out[0], out[1], out[2], out[3]};
 }
@@ -2956,6 +3009,37 @@ float orc_tex3d(const float *vox, const int dims[3], const float coord[3], int r
   return tex3dLinear(vox, dims, coord[0], coord[1], coord[2], round);
 }
 
+void orc_tex_float4(const float *texels, int ndim, const int dims[3], int filter,
+    const int wrap[3], const float coord[3], float out[4])
+{
+  OrcSampler sm{};
+  sm.image = texels;
+  for (int k = 0; k < 3; k++) {
+    sm.dims[k] = k < ndim ? dims[k] : 1;
+    sm.wrap[k] = k < ndim ? wrap[k] : 0;
+  }
+  sm.filter = filter;
+  const V4 r = texSample(sm, ndim, coord);
+  out[0] = r.x;
+  out[1] = r.y;
+  out[2] = r.z;
+  out[3] = r.w;
+}
+
+void orc_tex_rgba8(const uint8_t *texels, int w, int h, const float coord[2], float out[4])
+{
+  OrcRenderer R{};
+  R.bgImage = texels;
+  R.bgType = 260;
+  R.bgW = w;
+  R.bgH = h;
+  const V4 r = bgImageAt(R, coord[0], coord[1]);
+  out[0] = r.x;
+  out[1] = r.y;
+  out[2] = r.z;
+  out[3] = r.w;
+}
+
 int orc_nvdb_sample(const uint8_t *grid, const float *xyz, int n, int fused, float *out)
 {
   Nvdb g;
@@ -3180,9 +3264,9 @@ int orc_render_prepared(void *prepared, const OrcCamera *camera, const OrcRender
   const int rb = std::max(0, F.rowBegin), re = std::min(LH, F.rowEnd);
   const int tilesX = (LW + 15) / 16, tilesY = (re - rb + 15) / 16;
   std::atomic<int> next{0};
-  std::atomic<uint64_t> rays{0};
+  std::atomic<uint64_t> rays{0}, samples{0};
   auto worker = [&]() {
-    Ctx C{&S, renderer, volumeMode, texRound, 0, &dptMaj};
+    Ctx C{&S, renderer, volumeMode, texRound, 0, 0, &dptMaj};
     while (true) {
       const int t = next.fetch_add(1);
       if (t >= tilesX * tilesY)
@@ -3249,6 +3333,7 @@ int orc_render_prepared(void *prepared, const OrcCamera *camera, const OrcRender
         }
     }
     rays += C.rays;
+    samples += C.samples;
   };
   int nt = threads > 0 ? threads : (int)std::thread::hardware_concurrency();
   nt = std::max(1, nt);
@@ -3258,6 +3343,7 @@ int orc_render_prepared(void *prepared, const OrcCamera *camera, const OrcRender
   for (auto &t : pool)
     t.join();
   F.raysTraced = rays.load();
+  F.volumeSamples = samples.load();
   return 0;
 }
 

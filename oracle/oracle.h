@@ -46,13 +46,22 @@ void orc_philox_stream(uint64_t seed,
 
 /* --- texture filter emulation (parity mode) ------------------------------ */
 
-/* Linear-filtered, clamped, normalised-coordinate fetch from a 1D table of
- * `comps`-component floats, with weights quantised to 8 fractional bits
- * (CUDA Programming Guide, "Linear Filtering"). round: 0 = truncate,
- * 1 = round to nearest. */
-void orc_tex1d(const float *table, int n, int comps, float coord, int round,
+/* Linear-filtered, clamped, normalised-coordinate fetches from a 1D table
+ * of `comps`-component floats and from a 3D float field. mode 1: the
+ * texture unit's arithmetic (coordinates truncated to 21 fractional bits,
+ * 8-bit weights split into integer corner weights, one rounding of the
+ * exact sum; bit-exact against GPU captures); mode 0: FP32 lerps with
+ * weights rounded to 8 bits (the textbook form). */
+void orc_tex1d(const float *table, int n, int comps, float coord, int mode,
     float *out);
-float orc_tex3d(const float *vox, const int dims[3], const float coord[3], int round);
+float orc_tex3d(const float *vox, const int dims[3], const float coord[3], int mode);
+/* Float4 texture fetch of `ndim` dimensions (dims[ndim]), filter 0 point /
+ * 1 linear, wrap[k] 0 clamp / 1 repeat / 2 mirror, as the image samplers
+ * and the HDRI map are read; and the RGBA8 normalised-float linear clamped
+ * fetch of the background image. */
+void orc_tex_float4(const float *texels, int ndim, const int dims[3], int filter,
+    const int wrap[3], const float coord[3], float out[4]);
+void orc_tex_rgba8(const uint8_t *texels, int w, int h, const float coord[2], float out[4]);
 
 /* --- NanoVDB fields ------------------------------------------------------ */
 
@@ -226,6 +235,8 @@ typedef struct OrcFrame {
   uint64_t raysTraced;
   int checkerboardID; /* -1: off; 0..3: which pixel of each 2x2 block */
   float *albedo, *normal; /* vec3 accumulations (in/out) or NULL */
+  /* statistics: volume march positions (the reference's samples) */
+  uint64_t volumeSamples;
 } OrcFrame;
 
 /* Renders rows [rowBegin, rowEnd). volumeMode 0: parity (texture

@@ -160,7 +160,8 @@ class OrcFrame(C.Structure):
                 ("accum", C.c_void_p), ("color", C.c_void_p), ("depth", C.c_void_p),
                 ("primId", C.c_void_p), ("objId", C.c_void_p), ("instId", C.c_void_p),
                 ("raysTraced", C.c_uint64), ("checkerboardID", C.c_int),
-                ("albedo", C.c_void_p), ("normal", C.c_void_p)]
+                ("albedo", C.c_void_p), ("normal", C.c_void_p),
+                ("volumeSamples", C.c_uint64)]
 
 
 class OrcDMVolume(C.Structure):
@@ -486,6 +487,7 @@ def _render_prepared(lib, handle, spec, frame_id, rows, volume_mode, tex_round, 
                                  C.c_int(volume_mode), C.c_int(tex_round), C.c_int(threads))
     assert rc == 0
     out["rays"] = int(fr.raysTraced)
+    out["volume_samples"] = int(fr.volumeSamples)
     return out
 
 
@@ -522,6 +524,33 @@ def tex3d(vox: np.ndarray, coord, round_mode: int = 1) -> float:
     dims = np.array([v.shape[2], v.shape[1], v.shape[0]], np.int32)
     c = np.asarray(coord, np.float32)
     return float(lib.orc_tex3d(_ptr(v), _ptr(dims), _ptr(c), C.c_int(round_mode)))
+
+
+def tex_float4(texels: np.ndarray, dims, filter_: int, wrap, coord) -> np.ndarray:
+    """Float4 texture fetch (texels (..., 4) with x fastest; dims per axis;
+    filter 0 point / 1 linear; wrap per axis 0 clamp / 1 repeat / 2 mirror)
+    as the texture unit computes it."""
+    lib = load()
+    t = np.ascontiguousarray(texels, np.float32)
+    nd = len(dims)
+    d = np.array(list(dims) + [1] * (3 - nd), np.int32)
+    w = np.array(list(wrap) + [0] * (3 - nd), np.int32)
+    c = np.array(list(coord) + [0.0] * (3 - nd), np.float32)
+    out = np.zeros(4, np.float32)
+    lib.orc_tex_float4(_ptr(t), C.c_int(nd), _ptr(d), C.c_int(filter_), _ptr(w), _ptr(c),
+                       _ptr(out))
+    return out
+
+
+def tex_rgba8(texels: np.ndarray, width: int, height: int, coord) -> np.ndarray:
+    """Linear, clamped, normalised-float fetch of an RGBA8 image (the
+    background image's texture)."""
+    lib = load()
+    t = np.ascontiguousarray(texels, np.uint8)
+    c = np.asarray(coord, np.float32)
+    out = np.zeros(4, np.float32)
+    lib.orc_tex_rgba8(_ptr(t), C.c_int(width), C.c_int(height), _ptr(c), _ptr(out))
+    return out
 
 
 def bvh8_count(nodes: bytes, tris: bytes, rays: np.ndarray):

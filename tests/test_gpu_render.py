@@ -335,11 +335,11 @@ SAMPLER_CASES = {
         "image2D", image=rng.integers(0, 256, (8, 12, 4)).astype(np.uint8),
         wrap=("repeat", "repeat", "clampToEdge"),
         in_transform=np.diag([3.0, 2.5, 1.0, 1.0]).astype(np.float32),
-        in_offset=(-0.7, 0.3, 0.0, 0.0)), 2),
+        in_offset=(-0.7, 0.3, 0.0, 0.0)), 1),
     "image1D-linear-clamp-f3": (1, lambda rng, np_: S.SamplerSpec(
         "image1D", image=rng.random((32, 3)).astype(np.float32),
         in_transform=np.diag([1.4, 1.0, 1.0, 1.0]).astype(np.float32),
-        in_offset=(-0.2, 0.0, 0.0, 0.0)), 2),
+        in_offset=(-0.2, 0.0, 0.0, 0.0)), 1),
     "image3D-nearest-mirror-f1": (3, lambda rng, np_: S.SamplerSpec(
         "image3D", image=rng.random((6, 7, 5)).astype(np.float32), filter="nearest",
         wrap=("mirrorRepeat",) * 3, in_transform=np.diag([2.5, 2.5, 2.5, 1.0]).astype(np.float32),
@@ -652,7 +652,7 @@ def test_volume_in_front_of_surface(device):
     spec.renderer.ambient_samples = 0
     g = render_gpu(device, spec)
     r = render_oracle(spec)
-    compare(g, r, color_tol=2, allow_ids=3)
+    compare(g, r, color_tol=1, allow_ids=3)
 
 
 def test_ao_wavefront_matches_megakernel(device):
@@ -730,7 +730,7 @@ def test_lights_and_materials(device, material, lights):
     spec = lit_scene(material, lights)
     g = render_gpu(device, spec)
     r = render_oracle(spec)
-    rep = compare(g, r, allow_ids=3, color_tol=3)
+    rep = compare(g, r, allow_ids=3, color_tol=1)
     from visrtx_gb300 import anari
 
     c = anari.rgba8(g["color"])[..., :3]
@@ -754,10 +754,10 @@ def test_hdri_background(device, renderer):
     if renderer == "dpt":
         cg = anari.rgba8(g["color"]).astype(np.int32)
         cr = anari.rgba8(r["color"]).astype(np.int32)
-        same = np.all(np.abs(cg - cr) <= 2, axis=-1)
-        assert same.mean() >= 0.9, same.mean()
+        same = np.all(np.abs(cg - cr) <= 1, axis=-1)
+        assert same.mean() >= 0.999, same.mean()
     else:
-        compare(g, r, allow_ids=3, color_tol=2)
+        compare(g, r, allow_ids=3, color_tol=1)
     miss = g["depth"] >= 1e29
     bg = anari.rgba8(g["color"])[..., :3][miss].astype(np.float64)
     assert miss.any() and bg.std() > 2.0, "the environment varies across the background"
@@ -787,7 +787,7 @@ def test_background_image(device, case):
     spec.renderer.ambient_samples = 2 if renderer == "ao" else 0
     g = render_gpu(device, spec)
     r = render_oracle(spec)
-    rep = compare(g, r, allow_ids=3, color_tol=3)
+    rep = compare(g, r, allow_ids=3, color_tol=1)
     from visrtx_gb300 import anari
 
     miss = g["depth"] >= 1e29
@@ -818,7 +818,7 @@ def test_pbr_parameters_from_attributes_and_samplers(device, renderer):
                                    in_offset=(0.3, 0.0, 0.0, 0.0))
     g = render_gpu(device, spec)
     r = render_oracle(spec)
-    rep = compare(g, r, allow_ids=3, color_tol=3)
+    rep = compare(g, r, allow_ids=3, color_tol=1)
     from visrtx_gb300 import anari
 
     hit = g["depth"] < 1e29
