@@ -335,6 +335,15 @@ VRTX_API void vrtxUnmapFrame(VRTXDevice d, VRTXFrame f, const char *channel);
 VRTX_API uint64_t vrtxDebugCopyAccel(
     VRTXDevice d, VRTXObject world, int kind, void *dst, uint64_t capacity);
 
+/* Sorts n (key, value) pairs held in host memory with the BVH builder's
+ * Morton sort (a stable LSD radix sort by the low `bits` bits of the keys,
+ * bits in 1..64), through device copies on the device's stream. Replaces
+ * nothing in the reference: its sort is inside optixAccelBuild
+ * (optix_visrtx.cpp:288-372). Returns 0, or a negative code after
+ * reporting the error. */
+VRTX_API int vrtxDebugRadixSort(
+    VRTXDevice d, uint64_t *keys, uint32_t *vals, uint32_t n, int bits);
+
 /* Milliseconds spent in the last BVH / macrocell-grid build of a world
  * (host wall clock around the device build, synchronised). */
 VRTX_API float vrtxWorldBuildMilliseconds(VRTXDevice d, VRTXObject world);

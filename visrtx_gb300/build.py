@@ -20,9 +20,14 @@ LIBDIR = os.path.join(HERE, "lib")
 LIB = os.path.join(LIBDIR, "libvrtx.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_SOURCES = ["bvh.cu", "scene.cu", "render.cu", "render_counting.cu", "render_volume.cu", "render_ao.cu",
+CU_SOURCES = ["bvh.cu", "radix_sort.cu", "scene.cu", "render.cu", "render_counting.cu", "render_volume.cu", "render_ao.cu",
               "dm.cu"]
 CPP_SOURCES = ["device.cpp"]
+# Translation units whose arithmetic decides ids, depth and colour: compiled
+# without implicit multiply-add contraction, so every operation rounds as
+# written (the CPU oracle is built the same way, -ffp-contract=off); fused
+# multiply-adds there are explicit fmaf calls.
+NO_FMAD = {"render.cu", "render_counting.cu", "render_volume.cu", "render_ao.cu", "scene.cu"}
 
 
 def _nvcc() -> str:
@@ -81,6 +86,8 @@ def _build(verbose: bool, ptxas_info: bool, dflags: list) -> str:
         if _stale(o, [s] + headers):
             cmd = [nvcc, *ARCH, "-lineinfo", "-O3", "-std=c++17", "--expt-relaxed-constexpr",
                    "--extended-lambda", "-Xcompiler", "-fPIC", *dflags, "-c", s, "-o", o]
+            if src in NO_FMAD:
+                cmd.insert(1, "-fmad=false")
             if ptxas_info:
                 cmd.insert(1, "-Xptxas=-v")
             jobs.append(cmd)

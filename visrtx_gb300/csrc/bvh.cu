@@ -21,9 +21,10 @@
 //    order, quantises child boxes outward, and appends one task per internal
 //    child. Node and primitive ranges are claimed with atomics, so a node's
 //    internal children are contiguous and its leaf primitives are contiguous.
-#include <cub/device/device_radix_sort.cuh>
+#include <utility>
 
 #include "bvh.h"
+#include "radix_sort.h"
 
 namespace vrtx {
 namespace {
@@ -61,17 +62,31 @@ __global__ void k_boundsPartial(
   }
 }
 
+// the partial boxes of k_boundsPartial's blocks reduced by one block of
+// 256 threads (one partial per thread, then a shared-memory tree)
 __global__ void k_boundsFinal(box3 *partialCent, box3 *partialAll, int nb)
 {
-  if (threadIdx.x != 0 || blockIdx.x != 0)
-    return;
+  __shared__ box3 sc[256];
+  __shared__ box3 sa[256];
   box3 c = emptyBox(), a = emptyBox();
-  for (int i = 0; i < nb; i++) {
+  for (int i = threadIdx.x; i < nb; i += blockDim.x) {
     extend(c, partialCent[i]);
     extend(a, partialAll[i]);
   }
-  partialCent[0] = c;
-  partialAll[0] = a;
+  sc[threadIdx.x] = c;
+  sa[threadIdx.x] = a;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) {
+      extend(sc[threadIdx.x], sc[threadIdx.x + s]);
+      extend(sa[threadIdx.x], sa[threadIdx.x + s]);
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    partialCent[0] = sc[0];
+    partialAll[0] = sa[0];
+  }
 }
 
 // --- Morton codes -----------------------------------------------------------
@@ -614,7 +629,6 @@ cudaError_t buildBVH8(const box3 *d_boxes,
   uint64_t *keys = nullptr, *keysSorted = nullptr;
   uint32_t *vals = nullptr, *valsSorted = nullptr;
   void *tmp = nullptr;
-  size_t tmpBytes = 0;
   uint32_t *left = nullptr, *right = nullptr, *parI = nullptr, *parL = nullptr;
   box3 *iBoxes = nullptr;
   uint32_t *iCount = nullptr, *flags = nullptr, *counters = nullptr;
@@ -627,34 +641,24 @@ cudaError_t buildBVH8(const box3 *d_boxes,
   VRTX_TRY(dalloc(&pCent, nbPartial, stream));
   VRTX_TRY(dalloc(&pAll, nbPartial, stream));
   k_boundsPartial<<<nbPartial, 256, 0, stream>>>(d_boxes, n, pCent, pAll);
-  k_boundsFinal<<<1, 32, 0, stream>>>(pCent, pAll, nbPartial);
+  k_boundsFinal<<<1, 256, 0, stream>>>(pCent, pAll, nbPartial);
 
   VRTX_TRY(dalloc(&keys, n, stream));
   VRTX_TRY(dalloc(&keysSorted, n, stream));
   VRTX_TRY(dalloc(&vals, n, stream));
   VRTX_TRY(dalloc(&valsSorted, n, stream));
   k_morton<<<(n + T - 1) / T, T, 0, stream>>>(d_boxes, n, pCent, keys, vals);
-  VRTX_TRY(cub::DeviceRadixSort::SortPairs(nullptr,
-      tmpBytes,
-      keys,
-      keysSorted,
-      vals,
-      valsSorted,
-      (int)n,
-      0,
-      63,
-      stream));
-  VRTX_TRY(cudaMallocAsync(&tmp, tmpBytes, stream));
-  VRTX_TRY(cub::DeviceRadixSort::SortPairs(tmp,
-      tmpBytes,
-      keys,
-      keysSorted,
-      vals,
-      valsSorted,
-      (int)n,
-      0,
-      63,
-      stream));
+  VRTX_TRY(cudaMallocAsync(&tmp, radixSortScratchBytes(n), stream));
+  {
+    uint64_t *kSorted = nullptr;
+    uint32_t *vSorted = nullptr;
+    VRTX_TRY(radixSortPairs64(
+        keys, vals, keysSorted, valsSorted, n, 63, tmp, stream, &kSorted, &vSorted));
+    if (kSorted != keysSorted) {
+      std::swap(keys, keysSorted);
+      std::swap(vals, valsSorted);
+    }
+  }
 
   VRTX_TRY(dalloc(&left, n, stream));
   VRTX_TRY(dalloc(&right, n, stream));

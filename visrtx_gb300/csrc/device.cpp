@@ -14,6 +14,7 @@
 #include <set>
 
 #include "objects.h"
+#include "radix_sort.h"
 
 namespace vrtx {
 
@@ -3825,6 +3826,58 @@ VRTX_API const void *vrtxMapFrame(VRTXDevice d,
 }
 
 VRTX_API void vrtxUnmapFrame(VRTXDevice, VRTXFrame, const char *) {}
+
+VRTX_API int vrtxDebugRadixSort(
+    VRTXDevice d, uint64_t *keys, uint32_t *vals, uint32_t n, int bits)
+{
+  DeviceScope scope(D(d));
+  Device *dev = D(d);
+  if (!dev || !dev->init())
+    return -1;
+  if ((n && (!keys || !vals)) || bits < 1 || bits > 64) {
+    dev->report(nullptr, VRTX_SEVERITY_ERROR, "vrtxDebugRadixSort: invalid arguments");
+    return -2;
+  }
+  if (n == 0)
+    return 0;
+  cudaStream_t s = dev->stream;
+  uint64_t *k[2] = {nullptr, nullptr};
+  uint32_t *v[2] = {nullptr, nullptr};
+  void *scratch = nullptr;
+  cudaError_t e = cudaMallocAsync((void **)&k[0], sizeof(uint64_t) * n, s);
+  if (e == cudaSuccess)
+    e = cudaMallocAsync((void **)&k[1], sizeof(uint64_t) * n, s);
+  if (e == cudaSuccess)
+    e = cudaMallocAsync((void **)&v[0], sizeof(uint32_t) * n, s);
+  if (e == cudaSuccess)
+    e = cudaMallocAsync((void **)&v[1], sizeof(uint32_t) * n, s);
+  if (e == cudaSuccess)
+    e = cudaMallocAsync(&scratch, radixSortScratchBytes(n), s);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(k[0], keys, sizeof(uint64_t) * n, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(v[0], vals, sizeof(uint32_t) * n, cudaMemcpyHostToDevice, s);
+  uint64_t *ko = nullptr;
+  uint32_t *vo = nullptr;
+  if (e == cudaSuccess)
+    e = radixSortPairs64(k[0], v[0], k[1], v[1], n, bits, scratch, s, &ko, &vo);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(keys, ko, sizeof(uint64_t) * n, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(vals, vo, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost, s);
+  for (void *p : {(void *)k[0], (void *)k[1], (void *)v[0], (void *)v[1], scratch})
+    if (p)
+      cudaFreeAsync(p, s);
+  const cudaError_t se = cudaStreamSynchronize(s);
+  if (e == cudaSuccess)
+    e = se;
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    dev->report(nullptr, VRTX_SEVERITY_ERROR, cudaGetErrorString(e));
+    return -3;
+  }
+  return 0;
+}
 
 VRTX_API uint64_t vrtxDebugCopyAccel(
     VRTXDevice d, VRTXObject world, int kind, void *dst, uint64_t capacity)
