@@ -380,7 +380,7 @@ typedef struct VRTXDMVolume {
   const void *density;   /* dims[0] fastest; fp32, fp16 or bf16 */
   int densityType;       /* VRTX_FLOAT32, VRTX_FLOAT16 or VRTX_BFLOAT16 */
   int dims[3];
-  const float *tf;       /* tfSize x RGBA, fp32 */
+  const void *tf;        /* tfSize x RGBA, of type tfType */
   int tfSize;            /* 2..256 */
   float opacityScale;    /* multiplies TF alpha */
   float step;            /* sample spacing, voxels */
@@ -392,6 +392,8 @@ typedef struct VRTXDMVolume {
   const float *opacityScaleDevice; /* when not NULL, read instead of
                                       opacityScale (device scalar) */
   int flags;             /* VRTX_DM_* bits, 0 by default */
+  int tfType;            /* VRTX_FLOAT32 (or 0), VRTX_FLOAT16 or VRTX_BFLOAT16;
+                            entries are read in fp32, gradTf stays fp32 */
 } VRTXDMVolume;
 
 /* Backward pass: one atomic add per gradient term per sample instead of

@@ -13,16 +13,23 @@ from visrtx_gb300 import dm, scenes as S
 pytestmark = pytest.mark.gpu
 
 
-def make_volume(n=(24, 20, 28), seed=0, dtype=torch.float32, blobs=5):
+def make_volume(n=(24, 20, 28), seed=0, dtype=torch.float32, blobs=5, tf_dtype=torch.float32):
+    """A volume in the given storage types; .src_density / .src_tf keep the
+    FP32 originals the low-precision copies were rounded from, which is
+    what the FP64 oracle is given, so every stated error includes the
+    storage rounding."""
     nx, ny, nz = n
     d = S.gaussian_blobs((nx, ny, nz), n_blobs=blobs, seed=seed, sigma_scale=0.12)
     color, op = S.tf_knots(seed, max_opacity=0.6)
     tf = S.tf_table(color, op, 256)
     dt = torch.tensor(d, device="cuda").to(dtype).contiguous()
-    tft = torch.tensor(tf, device="cuda").contiguous()
+    tft = torch.tensor(tf, device="cuda").to(tf_dtype).contiguous()
     scale = torch.tensor([1.5], device="cuda", dtype=torch.float32)
     # value range wider than the data: no sample sits on a TF-clamp kink
-    return dm.VolumeInput(dt, tft, scale, step=0.5, unit=1.0, value_range=(-0.5, 1.5))
+    v = dm.VolumeInput(dt, tft, scale, step=0.5, unit=1.0, value_range=(-0.5, 1.5))
+    v.src_density = d
+    v.src_tf = tf
+    return v
 
 
 def views_for(v: dm.VolumeInput, k=2, res=(40, 32), vol=0, seed=0):
@@ -39,8 +46,8 @@ def oracle_view(w: dm.View):
 def ref_forward(v, views, grad=None):
     from oracle import oracle as O
 
-    dens = v.density.float().cpu().numpy().astype(np.float64)
-    tf = v.tf.cpu().numpy().astype(np.float64)
+    dens = np.asarray(v.src_density, np.float64)
+    tf = np.asarray(v.src_tf, np.float64)
     imgs, gD, gT, gS = [], np.zeros_like(dens), np.zeros_like(tf), 0.0
     off = 0
     for w in views:
@@ -64,25 +71,41 @@ def rel(a, b):
     return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30))
 
 
-@pytest.mark.parametrize("dtype", [torch.float32, torch.float16, torch.bfloat16])
-def test_forward_rms_vs_fp64(dtype):
-    v = make_volume(dtype=dtype)
+STORAGE = [(torch.float32, torch.float32), (torch.float16, torch.float32),
+           (torch.bfloat16, torch.float32), (torch.float16, torch.float16),
+           (torch.bfloat16, torch.bfloat16)]
+
+
+@pytest.mark.parametrize("dtype,tf_dtype", STORAGE)
+def test_forward_rms_vs_fp64(dtype, tf_dtype):
+    """Image RMS <= 1e-3 against the FP64 oracle run on the FP32 originals
+    (density and TF storage rounding included; measured 7e-8 FP32, 8.5e-6
+    FP16 density, 9e-5 BF16 density, 6.4e-5 FP16 density and TF, 4.7e-4
+    BF16 density and TF)."""
+    v = make_volume(dtype=dtype, tf_dtype=tf_dtype)
     views = views_for(v)
     b = dm.Batch([v], views)
     img, state = dm.forward(b)
     ref, *_ = ref_forward(v, views)
     rms = float(np.sqrt(np.mean((img.cpu().numpy() - ref) ** 2)))
-    print(dtype, "rms", rms)
+    print(dtype, tf_dtype, "image rms vs fp64 on the fp32 originals", rms)
     assert rms <= 1e-3
     assert 0.05 < float(img.mean()) < 1.0  # the views see the volume
 
 
-@pytest.mark.parametrize("dtype,plain", [(torch.float32, False), (torch.float16, False),
-                                         (torch.float32, True)])
-def test_adjoint_vs_fp64(dtype, plain):
+@pytest.mark.parametrize("dtype,plain,tf_dtype", [
+    (torch.float32, False, torch.float32), (torch.float16, False, torch.float32),
+    (torch.float32, True, torch.float32), (torch.bfloat16, False, torch.float32),
+    (torch.float16, False, torch.float16), (torch.bfloat16, False, torch.bfloat16)])
+def test_adjoint_vs_fp64(dtype, plain, tf_dtype):
     """Both gradient accumulation forms (run-length per thread, and one
-    atomic per term) against the FP64 oracle adjoint."""
-    v = make_volume(dtype=dtype, seed=1)
+    atomic per term) against the FP64 oracle adjoint run on the FP32
+    originals. With an FP32 TF every gradient is within 1e-2 relative (FP16
+    density measured 4e-4, BF16 7e-3). A 16-bit TF moves the density
+    gradient further: it follows the TF's slope, the difference of adjacent
+    entries, which 16-bit storage rounds coarsely (measured FP16 1.1e-2,
+    BF16 0.11); those bounds are stated per storage type."""
+    v = make_volume(dtype=dtype, seed=1, tf_dtype=tf_dtype)
     v.plain = plain
     views = views_for(v, k=2, seed=1)
     b = dm.Batch([v], views)
@@ -94,8 +117,10 @@ def test_adjoint_vs_fp64(dtype, plain):
     gd = grads[0][0].cpu().numpy()
     gt = grads[0][1].cpu().numpy()
     gs = float(grads[0][2].item())
-    print("density", rel(gd, gD), "tf", rel(gt, gT), "scale", abs(gs - gS) / abs(gS))
-    assert rel(gd, gD) <= 1e-2
+    print(dtype, tf_dtype, "plain" if plain else "staged", "density", rel(gd, gD), "tf",
+          rel(gt, gT), "scale", abs(gs - gS) / abs(gS))
+    dens_bound = {torch.float32: 1e-2, torch.float16: 2e-2, torch.bfloat16: 0.15}[tf_dtype]
+    assert rel(gd, gD) <= dens_bound
     assert rel(gt, gT) <= 1e-2
     assert abs(gs - gS) <= 1e-2 * abs(gS)
 

@@ -676,6 +676,76 @@ def test_ao_wavefront_matches_megakernel(device):
     assert g1["frame"].kernel_launches() > fr.kernel_launches()
 
 
+def _frames_equal_forced_megakernel(device, spec, frames=1, channels=False):
+    """Renders spec twice, the second time with "vrtx.megakernel" (the
+    per-pixel integrator kernel); returns both frames' channel maps after
+    asserting they are equal bit for bit."""
+    from visrtx_gb300 import scenes as S2
+
+    chans = ("color", "depth", "primitiveId", "objectId", "instanceId")
+    if channels:
+        chans += ("albedo", "normal")
+    outs = []
+    for mega in (False, True):
+        fr, w, keep = S2.build_on_device(device, spec, channels=chans)
+        if mega:
+            fr.set("vrtx.megakernel", True)
+            fr.commit()
+        for _ in range(frames):
+            fr.render()
+        fr.wait()
+        outs.append(({ch: fr.map("channel." + ch) for ch in chans}, fr.kernel_launches()))
+    for ch in chans:
+        assert np.array_equal(outs[0][0][ch], outs[1][0][ch]), ch
+    return outs
+
+
+@pytest.mark.parametrize("case", ["soup-1spp", "lights-ao3-spp3", "hdri-hidden-checkerboard"])
+def test_default_wavefront_matches_megakernel(device, case):
+    """The wavefront "default" renderer (primary kernel queuing AO and
+    shadow rays, the any-hit queue kernel, resolve) draws every random
+    number where the per-pixel kernel does and sums the lights in the same
+    order: identical frames, bit for bit, over directional, point, spot and
+    HDRI lights, AO samples, several samples per pixel and checkerboarding."""
+    if case == "soup-1spp":
+        spec = S.soup_spec(n=20_000, width=128, height=96, renderer="default")
+        frames = 1
+    else:
+        spec = soup("default", n=4000, w=96, h=72)
+        spec.lights = [S.LightSpec(direction=(0.3, -0.4, 1.0), irradiance=1.5),
+                       S.LightSpec("point", position=(0.5, 1.2, -0.6), irradiance=1.5),
+                       S.LightSpec("spot", position=(0.4, 0.6, -1.2), direction=(0.1, -0.1, 1.0),
+                                   opening_angle=0.45, falloff_angle=0.1, irradiance=2.0)]
+        spec.renderer.ambient_samples = 3
+        spec.renderer.ambient_radiance = 0.4
+        spec.renderer.pixel_samples = 3
+        frames = 2
+        if case.startswith("hdri"):
+            spec.lights.append(S.LightSpec("hdri", radiance=hdri_image(seed=5), visible=False))
+            spec.renderer.checkerboard = True
+            spec.renderer.pixel_samples = 1
+            frames = 5
+    outs = _frames_equal_forced_megakernel(device, spec, frames=frames)
+    assert outs[0][1] > outs[1][1]  # the wavefront ran (more launches)
+    hit = outs[0][0]["depth"] < 1e29
+    assert hit.any()
+    assert not device.errors()
+
+
+@pytest.mark.parametrize("case", ["soup", "instanced", "checkerboard"])
+def test_raycast_wavefront_matches_megakernel(device, case):
+    """The one-kernel "raycast" (opaque surfaces, no volumes) equals the
+    per-pixel kernel bit for bit."""
+    if case == "instanced":
+        spec = small_instanced("raycast")
+    else:
+        spec = soup("raycast", n=8000, w=100, h=70)
+        spec.renderer.checkerboard = case == "checkerboard"
+    outs = _frames_equal_forced_megakernel(device, spec, frames=4 if case == "checkerboard" else 1)
+    assert (outs[0][0]["depth"] < 1e29).any()
+    assert not device.errors()
+
+
 # --- lights and the physically based material -------------------------------
 
 def hdri_image(w=32, h=16, seed=3):

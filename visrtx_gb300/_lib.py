@@ -135,7 +135,7 @@ class VRTXDMVolume(C.Structure):
         ("step", C.c_float), ("unitDistance", C.c_float), ("valueLo", C.c_float),
         ("valueHi", C.c_float), ("gradDensity", C.c_void_p), ("gradTf", C.c_void_p),
         ("gradOpacityScale", C.c_void_p), ("opacityScaleDevice", C.c_void_p),
-        ("flags", C.c_int),
+        ("flags", C.c_int), ("tfType", C.c_int),
     ]
 
 

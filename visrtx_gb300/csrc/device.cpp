@@ -2309,7 +2309,7 @@ bool World::rebuild()
     hSamplers.push_back(sm->gpuData());
     return k;
   };
-  bool allOpaque = true;
+  bool allOpaque = true, allMatte = true;
   for (Material *m : mats) {
     MaterialGPU mg = m->gpu;
     for (int k = 0; k < MP_COUNT; k++) {
@@ -2322,6 +2322,8 @@ bool World::rebuild()
     hMats.push_back(mg);
     if (m->gpu.alphaMode != ALPHA_OPAQUE)
       allOpaque = false;
+    if (m->gpu.type == MATERIAL_PBR)
+      allMatte = false;
   }
   std::vector<SurfaceGPU> hSurfs;
   for (Surface *sf : surfaces)
@@ -2553,6 +2555,7 @@ bool World::rebuild()
   gpu.volumes = uploadVec(this, vols, s);
   gpu.numVolumes = (uint32_t)vols.size();
   gpu.allOpaque = allOpaque ? 1u : 0u;
+  gpu.allMatte = allMatte ? 1u : 0u;
   gpu.hasNanovdb = 0u;
   for (const VolumeGPU &v : vols)
     if (v.fieldKind == FIELD_NANOVDB)
@@ -2959,17 +2962,31 @@ void Frame::render()
   P.stats = stats;
   cudaMemsetAsync(workCounter, 0, 4, s);
   cudaMemsetAsync(stats, 0, 16 * sizeof(unsigned long long), s);
-  // The "ao" renderer over opaque surfaces (no volumes) runs as a
-  // wavefront (primary / any-hit / resolve kernels per sample); everything
-  // else runs the per-pixel integrator kernel.
-  // (a background image is read at each sample's jittered screen position,
-  // which the wavefront's resolve does not keep: such frames run per pixel)
-  const bool wavefront = P.renderer.type == RENDERER_AO && P.world.allOpaque
-      && P.world.numVolumes == 0 && !forceMegakernel && !P.renderer.backgroundTex;
+  // Wavefront forms (per sample a primary / any-hit / resolve kernel, or
+  // one kernel for raycast) where the frame's path has no volume and no
+  // translucent surface: "ao", "default" over matte surfaces, "raycast".
+  // Everything else runs the per-pixel integrator kernel. ("ao" and
+  // "default" read a background image at each sample's jittered screen
+  // position, which their resolve does not keep: such frames run per
+  // pixel.)
+  const bool plainSurfaces =
+      P.world.allOpaque && P.world.numVolumes == 0 && !forceMegakernel;
+  const bool aoWave = P.renderer.type == RENDERER_AO && plainSurfaces
+      && !P.renderer.backgroundTex;
+  const bool dlWave = P.renderer.type == RENDERER_DIRECT_LIGHT && plainSurfaces
+      && P.world.allMatte && !P.renderer.backgroundTex;
+  const bool rcWave = P.renderer.type == RENDERER_RAYCAST && plainSurfaces;
+  const bool wavefront = aoWave || dlWave;
   cudaError_t err = cudaSuccess;
   cudaEventRecord(evKStart, s);
-  if (wavefront) {
-    const size_t need = aoWavefrontBytes(fb.w, fb.h, P.renderer.aoSamples);
+  if (rcWave) {
+    tracePairs = 0;
+    err = launchRaycastWavefront(P, countTraversal, s);
+    launches++;
+  } else if (wavefront) {
+    const size_t need = aoWave
+        ? aoWavefrontBytes(fb.w, fb.h, P.renderer.aoSamples)
+        : dlWavefrontBytes(fb.w, fb.h, P.renderer.aoSamples, P.world.numLights);
     if (need > scratchBytes) {
       if (scratch)
         cudaFreeAsync(scratch, s);
@@ -2989,8 +3006,10 @@ void Frame::render()
     const bool timed = (int)traceEvents.size() >= 2 * n;
     tracePairs = timed ? n : 0;
     if (err == cudaSuccess)
-      err = launchAOWavefront(P, d->numSMs, countTraversal, scratch, s,
-          timed ? traceEvents.data() : nullptr);
+      err = aoWave ? launchAOWavefront(P, d->numSMs, countTraversal, scratch, s,
+                         timed ? traceEvents.data() : nullptr)
+                   : launchDLWavefront(P, d->numSMs, countTraversal, scratch, s,
+                         timed ? traceEvents.data() : nullptr);
     launches += 3 * std::max(P.renderer.numIterations, 1);
   } else {
     tracePairs = 0;

@@ -38,7 +38,8 @@ struct DMVol
   const void *density;
   int type;
   int dims[3];
-  const float4 *tf;
+  const void *tf; // tfSize x RGBA, fp32 (float4) or fp16 / bf16 (4 x 16 bit)
+  int tfType; // 0 fp32, 1 fp16, 2 bf16
   int tfSize;
   float scale, step, ratio, lo, hi;
   float *gD;
@@ -128,6 +129,23 @@ __device__ __forceinline__ float trilinear(const DMVol &v, const Tri &t)
   return c0 + t.fz * (c1 - c0);
 }
 
+// One TF entry in fp32 whatever the storage type (uniform per volume).
+__device__ __forceinline__ float4 tfEntry(const DMVol &v, int i)
+{
+  if (v.tfType == 0)
+    return __ldg(reinterpret_cast<const float4 *>(v.tf) + i);
+  const uint2 raw = __ldg(reinterpret_cast<const uint2 *>(v.tf) + i);
+  float2 lo, hi;
+  if (v.tfType == 1) {
+    lo = __half22float2(*reinterpret_cast<const __half2 *>(&raw.x));
+    hi = __half22float2(*reinterpret_cast<const __half2 *>(&raw.y));
+  } else {
+    lo = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162 *>(&raw.x));
+    hi = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162 *>(&raw.y));
+  }
+  return make_float4(lo.x, lo.y, hi.x, hi.y);
+}
+
 struct Classified
 {
   float4 c; // rgb + raw TF alpha
@@ -146,7 +164,7 @@ __device__ __forceinline__ Classified classify(const DMVol &v, float s)
   const float x = u * float(v.tfSize - 1);
   r.i0 = min((int)floorf(x), v.tfSize - 2);
   r.f = x - float(r.i0);
-  const float4 a = __ldg(v.tf + r.i0), b = __ldg(v.tf + r.i0 + 1);
+  const float4 a = tfEntry(v, r.i0), b = tfEntry(v, r.i0 + 1);
   r.c = make_float4(a.x + r.f * (b.x - a.x),
       a.y + r.f * (b.y - a.y),
       a.z + r.f * (b.z - a.z),
@@ -533,7 +551,7 @@ __global__ void __launch_bounds__(256, VRTX_DM_BWD_MIN_BLOCKS) k_dmBackward(cons
             }
           }
           if (v.gD && cl.dxds != 0.f) {
-            const float4 ea = __ldg(v.tf + cl.i0), eb = __ldg(v.tf + cl.i0 + 1);
+            const float4 ea = tfEntry(v, cl.i0), eb = tfEntry(v, cl.i0 + 1);
             const float dval = dc.x * (eb.x - ea.x) + dc.y * (eb.y - ea.y)
                 + dc.z * (eb.z - ea.z) + dA * (eb.w - ea.w);
             const float ds = dval * cl.dxds;
@@ -628,6 +646,19 @@ int layout(const VRTXDMVolume *volumes,
       *err = "density must be FLOAT32, FLOAT16 or BFLOAT16";
       return -4;
     }
+    const int tfType = v.tfType == 0 || v.tfType == VRTX_FLOAT32 ? 0
+        : v.tfType == VRTX_FLOAT16                              ? 1
+        : v.tfType == VRTX_BFLOAT16                             ? 2
+                                                                : -1;
+    if (tfType < 0) {
+      *err = "tf must be FLOAT32, FLOAT16 or BFLOAT16";
+      return -4;
+    }
+    const size_t elemAlign = tfType == 0 ? 16 : 8;
+    if ((reinterpret_cast<uintptr_t>(v.tf) % elemAlign) != 0) {
+      *err = "tf must be aligned to one entry (16 bytes fp32, 8 bytes fp16 / bf16)";
+      return -4;
+    }
     if (i == 0)
       L.type = v.densityType;
     else if (v.densityType != L.type) {
@@ -640,7 +671,8 @@ int layout(const VRTXDMVolume *volumes,
     o.type = v.densityType;
     for (int k = 0; k < 3; k++)
       o.dims[k] = v.dims[k];
-    o.tf = reinterpret_cast<const float4 *>(v.tf);
+    o.tf = v.tf;
+    o.tfType = tfType;
     o.tfSize = v.tfSize;
     o.scale = v.opacityScale;
     o.step = v.step;

@@ -426,6 +426,7 @@ struct WorldGPU
   const VolumeGPU *volumes;
   uint32_t numVolumes;
   uint32_t allOpaque; // every material is opaque: any-hit = first hit
+  uint32_t allMatte; // no physicallyBased material: no bounce rays
   uint32_t hasSegments; // some BLAS holds cylinders, cones or curves
   const SamplerGPU *samplers; // the materials' samplers
   uint32_t hasNanovdb; // some volume samples a NanoVDB field

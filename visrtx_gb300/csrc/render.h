@@ -39,6 +39,20 @@ cudaError_t launchAOWavefront(const FrameParams &P,
     cudaStream_t s,
     cudaEvent_t *traceEvents);
 
+// Wavefront "default" renderer (opaque matte materials, no volumes, no
+// background image): per sample a primary kernel that queues the AO rays
+// and one shadow ray per light, the AO any-hit kernel over that queue, and
+// a resolve kernel. scratch: dlWavefrontBytes() bytes.
+size_t dlWavefrontBytes(uint32_t w, uint32_t h, int aoSamples, uint32_t numLights);
+cudaError_t launchDLWavefront(const FrameParams &P,
+    int numSMs,
+    bool stats,
+    void *scratch,
+    cudaStream_t s,
+    cudaEvent_t *traceEvents);
+// "raycast" over opaque surfaces without volumes: one kernel per frame
+cudaError_t launchRaycastWavefront(const FrameParams &P, bool stats, cudaStream_t s);
+
 // scene preparation (scene.cu)
 cudaError_t launchTriangleBoxes(const GeometryGPU *geoms,
     const uint2 *refs, // (surface, prim) per BLAS primitive

@@ -1,5 +1,7 @@
-// The wavefront "ao" kernels (primary, any-hit queue, resolve) and their
-// launcher; shared device code in render_impl.cuh.
+// The wavefront kernels and their launchers: "ao" (primary, any-hit queue,
+// resolve), "default" (primary, the same any-hit queue with shadow rays,
+// resolve) and "raycast" (one kernel); shared device code in
+// render_impl.cuh.
 #include "render_impl.cuh"
 
 namespace vrtx {
@@ -256,6 +258,75 @@ __global__ void __launch_bounds__(128, VRTX_TRACE_MIN_BLOCKS) k_aoTrace(const Fr
   }
 }
 
+// One sample of a wavefront pixel into the frame, as renderPixel and
+// accumResults do it (gpu_util.h:393-443): tonemapped accumulation, the
+// albedo and normal channels, depth-tested ids, and on the last sample the
+// output colour with the first-frame 2x2 splat.
+__device__ __forceinline__ void accumulateSample(const FrameParams &P,
+    uint32_t idx,
+    int x,
+    int y,
+    int sampleIdx,
+    int numSamples,
+    f3 outputColor,
+    float outputOpacity,
+    f3 normal,
+    float depth,
+    uint32_t prim,
+    uint32_t obj,
+    uint32_t inst)
+{
+  const FramebufferGPU &fb = P.fb;
+  float4 acc = fb.accum[idx];
+  const float4 tm = tonemap(make_float4(
+      outputColor.x, outputColor.y, outputColor.z, outputOpacity));
+  acc.x += tm.x;
+  acc.y += tm.y;
+  acc.z += tm.z;
+  acc.w += tm.w;
+  fb.accum[idx] = acc;
+  if (fb.albedo)
+    fb.albedo[idx] += outputColor;
+  if (fb.normal)
+    fb.normal[idx] += normal;
+  if (!fb.depth || depth < fb.depth[idx]) {
+    if (fb.depth)
+      fb.depth[idx] = depth;
+    if (fb.primID)
+      fb.primID[idx] = prim;
+    if (fb.objID)
+      fb.objID[idx] = obj;
+    if (fb.instID)
+      fb.instID[idx] = inst;
+  }
+  if (sampleIdx == numSamples - 1) {
+    writeOutputColor(fb, acc, idx, sampleIdx);
+    if (fb.checkerboardID == 0 && fb.frameID + sampleIdx == 0) {
+      if (x + 1 < (int)fb.w)
+        writeOutputColor(fb, acc, idx + 1, sampleIdx);
+      if (y + 1 < (int)fb.h)
+        writeOutputColor(fb, acc, idx + fb.w, sampleIdx);
+      if (x + 1 < (int)fb.w && y + 1 < (int)fb.h)
+        writeOutputColor(fb, acc, idx + fb.w + 1, sampleIdx);
+    }
+  }
+}
+
+// the colour of a miss: the background along the ray, at screen position
+// (sx, sy) for a background image
+__device__ __forceinline__ void missColor(
+    const FrameParams &P, f3 dir, float sx, float sy, f3 &outputColor, float &outputOpacity)
+{
+  f3 color = mk3(0.f, 0.f, 0.f);
+  float opacity = 0.f;
+  color *= opacity;
+  const float4 bg = backgroundOf(P, dir, sx, sy);
+  color += mk3(bg.x, bg.y, bg.z) * (1.f - opacity);
+  opacity += bg.w * (1.f - opacity);
+  outputColor = mk3(0.f, 0.f, 0.f) + color * (1.f - 0.f);
+  outputOpacity = 0.f + opacity * (1.f - 0.f);
+}
+
 __global__ void __launch_bounds__(128) k_aoResolve(const FrameParams P,
     int sampleIdx,
     int numSamples,
@@ -290,48 +361,308 @@ __global__ void __launch_bounds__(128) k_aoResolve(const FrameParams P,
     outputColor = mk3(0.f, 0.f, 0.f) + color * (1.f - 0.f);
     outputOpacity = 0.f + opacity * (1.f - 0.f);
   } else {
-    f3 color = mk3(0.f, 0.f, 0.f);
-    float opacity = 0.f;
-    color *= opacity;
     // a miss keeps the ray direction (frames with a background image do
     // not take this path)
-    const float4 bg = backgroundOf(P, px.normal, 0.f, 0.f);
-    color += mk3(bg.x, bg.y, bg.z) * (1.f - opacity);
-    opacity += bg.w * (1.f - opacity);
+    missColor(P, px.normal, 0.f, 0.f, outputColor, outputOpacity);
+  }
+  accumulateSample(P, idx, x, y, sampleIdx, numSamples, outputColor, outputOpacity, px.normal,
+      px.depth, px.prim, px.obj, px.inst);
+}
+
+// ---------------------------------------------------------------------------
+// Wavefront form of the "default" (directLight) renderer over opaque matte
+// surfaces without volumes, and of "raycast" over opaque surfaces without
+// volumes.
+//
+// The reference's directLight raygen shades each hit inline
+// (DirectLight_ptx.cu:73-224,294-418): computeAO's occlusion rays, then per
+// light a sample and a shadow any-hit ray (attenuation 1 - opacity along it),
+// the contributions summed in light order and scaled by the AO factor; matte
+// surfaces give no bounce ray. Inline, lanes whose camera ray missed idle
+// while their neighbours trace shadow rays. Here each sample is three
+// kernels:
+//   k_dlPrimary  camera ray, closest hit, the AO directions and the light
+//                samples in the reference's draw order; appends the AO rays
+//                and one shadow ray per light (its shaded contribution kept
+//                beside it) to the queue that k_aoTrace consumes;
+//   k_aoTrace    the any-hit pass, unchanged (a shadow ray has weight 1, so
+//                its result is the surface opacity along it);
+//   k_dlResolve  AO factor, the lights' contributions times (1 - opacity)
+//                in light order, then the compositing and accumulation of
+//                the per-pixel kernel.
+// "raycast" traces no secondary rays: one kernel shades and accumulates in
+// place.
+// ---------------------------------------------------------------------------
+
+struct DLPixel
+{
+  float depth;
+  uint32_t prim, obj, inst;
+  f3 normal; // outputNormal (Ns of the hit, or the ray direction)
+  f3 ambient; // the shaded colour's ambient term
+  float opacity; // the material's opacity; < 0 marks a miss
+  float weights; // sum of the AO weights
+  uint32_t rayBase; // AO rays, then one shadow ray per light
+};
+
+template <bool STATS>
+__global__ void __launch_bounds__(128, VRTX_PRIMARY_MIN_BLOCKS) k_dlPrimary(const FrameParams P,
+    int sampleIdx,
+    uint32_t *consumed,
+    DLPixel *pixels,
+    AORay *rays,
+    float4 *payload,
+    uint32_t *rayCount)
+{
+  const uint32_t lx = blockIdx.x * 8 + (threadIdx.x & 7);
+  const uint32_t ly = blockIdx.y * 16 + (threadIdx.x >> 3);
+  const FramebufferGPU &fb = P.fb;
+  const RendererGPU &rp = P.renderer;
+  const int x = computePixelX((int)lx, fb.checkerboardID);
+  const int y = computePixelY((int)ly, fb.checkerboardID);
+  const bool valid = lx < P.launchW && ly < P.launchH && x < (int)fb.w && y < (int)fb.h;
+  TravStats st{0u, 0u, 0u, 0u, 0u, 0u, 0u};
+  RandState rs;
+  DLPixel px;
+  px.opacity = -1.f;
+  px.weights = 0.f;
+  px.rayBase = 0u;
+  px.ambient = mk3(0.f, 0.f, 0.f);
+  SurfaceHit sh;
+  Ray ray;
+  bool found = false;
+  uint32_t idx = 0, used = 0;
+  if (valid) {
+    idx = (uint32_t)x + (uint32_t)y * fb.w;
+    used = sampleIdx ? consumed[idx] : 0u;
+    curand_init((unsigned long long)(y * (int)fb.w + x),
+        0ull,
+        (unsigned long long)fb.frameID * 512ull + used,
+        &rs);
+    float sx, sy;
+    ray = makePrimaryRay(P, rs, x, y, false, sx, sy);
+    Hit h;
+    float unused;
+    found = traverse<0, STATS, true>(P.world,
+        ray.org,
+        ray.dir,
+        ray.tmin,
+        ray.tmax,
+        rp.cullTriangleBF != 0,
+        true,
+        h,
+        unused,
+        P.errorFlag,
+        st);
+    if (found) {
+      populateSurfaceHit(P.world, ray, h, sh);
+      px.depth = sh.t;
+      px.prim = geometryPrimId(P.world, sh);
+      px.obj = P.world.surfaces[sh.surface].id;
+      px.inst = sh.instUserId;
+      px.normal = sh.Ns;
+    } else {
+      px.depth = fminf(1e30f, ray.tmax);
+      px.prim = 0u;
+      px.obj = ~0u;
+      px.inst = ~0u;
+      px.normal = ray.dir;
+    }
+  }
+  const uint32_t nAO = (uint32_t)max(rp.aoSamples, 0);
+  const uint32_t nL = P.world.numLights;
+  const uint32_t base = warpAppendAll(rayCount, valid && found ? nAO + nL : 0u);
+  if (valid) {
+    uint32_t draws = 4;
+    if (found) {
+      px.rayBase = base;
+      // computeAO first (shadeSurface, DirectLight_ptx.cu:84-90)
+      const f3 aoOrg = sh.hitpoint + (sh.epsilon * sh.Ng);
+      for (uint32_t i = 0; i < nAO; i++) {
+        const f3 dir = randomDir(rs, sh.Ns);
+        const float weight = fmaxf(0.f, dot(dir, sh.Ns));
+        px.weights += weight;
+        AORay r;
+        r.orgTmax = make_float4(
+            aoOrg.x, aoOrg.y, aoOrg.z, weight != 0.f ? rp.occlusionDistance : -1.f);
+        r.dirWeight = make_float4(dir.x, dir.y, dir.z, weight);
+        rays[base + i] = r;
+      }
+      draws += 4 * nAO;
+      const MatteState ms = matteInit(P.world, sh);
+      px.opacity = ms.opacity;
+      if (rp.ambientIntensity > 0.f)
+        px.ambient = rp.ambientColor * rp.ambientIntensity * ms.baseColor;
+      const f3 shadePoint = sh.hitpoint + (sh.epsilon * sh.Ns);
+      for (uint32_t l = 0; l < nL; l++) {
+        const LightGPU &L = P.world.lights[l];
+        if (L.type != LIGHT_DIRECTIONAL && L.type != LIGHT_POINT && L.type != LIGHT_SPOT)
+          draws += 2; // sampleHDRILight's two uniforms
+        const LightSample ls = sampleLight(L, sh.hitpoint, rs);
+        AORay r;
+        float4 pl = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (ls.pdf == 0.f) {
+          r.orgTmax = make_float4(0.f, 0.f, 0.f, -1.f); // no shadow ray
+          r.dirWeight = make_float4(0.f, 0.f, 0.f, 0.f);
+        } else {
+          const f3 thisLight = shadeMaterial(ms, sh.Ns, ls, -ray.dir);
+          r.orgTmax = make_float4(shadePoint.x, shadePoint.y, shadePoint.z, ls.dist);
+          r.dirWeight = make_float4(ls.dir.x, ls.dir.y, ls.dir.z, 1.f);
+          pl = make_float4(thisLight.x, thisLight.y, thisLight.z, anyNan(thisLight) ? 0.f : 1.f);
+        }
+        rays[base + nAO + l] = r;
+        payload[base + nAO + l] = pl;
+      }
+    }
+    consumed[idx] = used + draws;
+    pixels[idx] = px;
+  }
+  const unsigned long long r = warpSum(valid ? st.rays : 0u);
+  if ((threadIdx.x & 31) == 0)
+    atomicAdd(P.stats + 0, r);
+  if (STATS) {
+    const unsigned long long n = warpSum(st.nodes), t = warpSum(st.tris),
+                             sp = warpSum(st.spheres), in = warpSum(st.instances);
+    if ((threadIdx.x & 31) == 0) {
+      atomicAdd(P.stats + 1, n);
+      atomicAdd(P.stats + 2, t);
+      atomicAdd(P.stats + 3, sp);
+      atomicAdd(P.stats + 4, in);
+    }
+  }
+}
+
+__global__ void __launch_bounds__(128) k_dlResolve(const FrameParams P,
+    int sampleIdx,
+    int numSamples,
+    const DLPixel *pixels,
+    const float *weighted,
+    const float4 *payload)
+{
+  const uint32_t lx = blockIdx.x * 8 + (threadIdx.x & 7);
+  const uint32_t ly = blockIdx.y * 16 + (threadIdx.x >> 3);
+  const FramebufferGPU &fb = P.fb;
+  const int x = computePixelX((int)lx, fb.checkerboardID);
+  const int y = computePixelY((int)ly, fb.checkerboardID);
+  if (lx >= P.launchW || ly >= P.launchH || x >= (int)fb.w || y >= (int)fb.h)
+    return;
+  const RendererGPU &rp = P.renderer;
+  const uint32_t idx = (uint32_t)x + (uint32_t)y * fb.w;
+  const DLPixel px = pixels[idx];
+  f3 outputColor;
+  float outputOpacity;
+  if (px.opacity >= 0.f) {
+    const int nAO = max(rp.aoSamples, 0);
+    float aoFactor = 1.f;
+    if (nAO > 0) {
+      float hits = 0.f;
+      for (int i = 0; i < nAO; i++)
+        hits += weighted[px.rayBase + i];
+      aoFactor = px.weights > 0.f ? 1.f - hits / px.weights : 0.f;
+    }
+    f3 contrib = px.ambient;
+    for (uint32_t l = 0; l < P.world.numLights; l++) {
+      const uint32_t j = px.rayBase + (uint32_t)nAO + l;
+      const float4 pl = payload[j];
+      if (pl.w == 0.f)
+        continue;
+      // surface_o * volume_o, with no volume on the path
+      const float attenuation = (1.f - weighted[j]) * 1.f;
+      contrib += mk3(pl.x, pl.y, pl.z) * attenuation;
+    }
+    contrib *= aoFactor;
+    // the compositing of the per-pixel kernel (DirectLight_ptx.cu:362-373)
+    const f3 srgb = contrib;
+    f3 color;
+    float opacity;
+    if (anyNan(srgb)) {
+      color = mk3(0.f, 0.f, 0.f);
+      opacity = 0.f;
+    } else {
+      color = srgb;
+      opacity = px.opacity;
+    }
+    color += srgb * (1.f - opacity);
+    opacity += px.opacity * (1.f - opacity);
+    color *= opacity;
     outputColor = mk3(0.f, 0.f, 0.f) + color * (1.f - 0.f);
     outputOpacity = 0.f + opacity * (1.f - 0.f);
+  } else {
+    missColor(P, px.normal, 0.f, 0.f, outputColor, outputOpacity);
   }
-  float4 acc = fb.accum[idx];
-  const float4 tm = tonemap(make_float4(
-      outputColor.x, outputColor.y, outputColor.z, outputOpacity));
-  acc.x += tm.x;
-  acc.y += tm.y;
-  acc.z += tm.z;
-  acc.w += tm.w;
-  fb.accum[idx] = acc;
-  if (fb.albedo)
-    fb.albedo[idx] += outputColor;
-  if (fb.normal)
-    fb.normal[idx] += px.normal;
-  if (!fb.depth || px.depth < fb.depth[idx]) {
-    if (fb.depth)
-      fb.depth[idx] = px.depth;
-    if (fb.primID)
-      fb.primID[idx] = px.prim;
-    if (fb.objID)
-      fb.objID[idx] = px.obj;
-    if (fb.instID)
-      fb.instID[idx] = px.inst;
+  accumulateSample(P, idx, x, y, sampleIdx, numSamples, outputColor, outputOpacity, px.normal,
+      px.depth, px.prim, px.obj, px.inst);
+}
+
+// "raycast" over opaque surfaces: pixel-corner camera ray, closest hit,
+// |dir . Ns| * ambientColor * baseColor (Raycast_ptx.cu:60-179), shaded and
+// accumulated in place.
+template <bool STATS>
+__global__ void __launch_bounds__(128, VRTX_PRIMARY_MIN_BLOCKS) k_raycastWave(const FrameParams P)
+{
+  const uint32_t lx = blockIdx.x * 8 + (threadIdx.x & 7);
+  const uint32_t ly = blockIdx.y * 16 + (threadIdx.x >> 3);
+  const FramebufferGPU &fb = P.fb;
+  const RendererGPU &rp = P.renderer;
+  const int x = computePixelX((int)lx, fb.checkerboardID);
+  const int y = computePixelY((int)ly, fb.checkerboardID);
+  const bool valid = lx < P.launchW && ly < P.launchH && x < (int)fb.w && y < (int)fb.h;
+  TravStats st{0u, 0u, 0u, 0u, 0u, 0u, 0u};
+  if (valid) {
+    RandState rs;
+    curand_init((unsigned long long)(y * (int)fb.w + x),
+        0ull,
+        (unsigned long long)fb.frameID * 512ull,
+        &rs);
+    float sx, sy;
+    const Ray ray = makePrimaryRay(P, rs, x, y, true, sx, sy);
+    Hit h;
+    float unused;
+    const bool found = traverse<0, STATS, true>(P.world,
+        ray.org,
+        ray.dir,
+        ray.tmin,
+        ray.tmax,
+        rp.cullTriangleBF != 0,
+        true,
+        h,
+        unused,
+        P.errorFlag,
+        st);
+    const uint32_t idx = (uint32_t)x + (uint32_t)y * fb.w;
+    f3 outputColor;
+    float outputOpacity;
+    if (found) {
+      SurfaceHit sh;
+      populateSurfaceHit(P.world, ray, h, sh);
+      const MatteState ms = matteInit(P.world, sh);
+      const f3 lighting = fabsf(dot(ray.dir, sh.Ns)) * rp.ambientColor;
+      f3 color = mk3(0.f, 0.f, 0.f);
+      float opacity = 0.f;
+      color += (ms.baseColor * lighting) * (1.f - opacity);
+      opacity += ms.opacity * (1.f - opacity);
+      color *= opacity;
+      outputColor = mk3(0.f, 0.f, 0.f) + color * (1.f - 0.f);
+      outputOpacity = 0.f + opacity * (1.f - 0.f);
+      accumulateSample(P, idx, x, y, 0, 1, outputColor, outputOpacity, sh.Ng, sh.t,
+          geometryPrimId(P.world, sh), P.world.surfaces[sh.surface].id, sh.instUserId);
+    } else {
+      missColor(P, ray.dir, sx, sy, outputColor, outputOpacity);
+      accumulateSample(P, idx, x, y, 0, 1, outputColor, outputOpacity, ray.dir,
+          fminf(1e30f, ray.tmax), 0u, ~0u, ~0u);
+    }
   }
-  if (sampleIdx == numSamples - 1) {
-    writeOutputColor(fb, acc, idx, sampleIdx);
-    if (fb.checkerboardID == 0 && fb.frameID + sampleIdx == 0) {
-      if (x + 1 < (int)fb.w)
-        writeOutputColor(fb, acc, idx + 1, sampleIdx);
-      if (y + 1 < (int)fb.h)
-        writeOutputColor(fb, acc, idx + fb.w, sampleIdx);
-      if (x + 1 < (int)fb.w && y + 1 < (int)fb.h)
-        writeOutputColor(fb, acc, idx + fb.w + 1, sampleIdx);
+  const unsigned long long r = warpSum(valid ? st.rays : 0u);
+  if ((threadIdx.x & 31) == 0)
+    atomicAdd(P.stats + 0, r);
+  if (STATS) {
+    const unsigned long long n = warpSum(st.nodes), t = warpSum(st.tris),
+                             sp = warpSum(st.spheres), in = warpSum(st.instances);
+    if ((threadIdx.x & 31) == 0) {
+      atomicAdd(P.stats + 1, n);
+      atomicAdd(P.stats + 2, t);
+      atomicAdd(P.stats + 3, sp);
+      atomicAdd(P.stats + 4, in);
     }
   }
 }
@@ -375,6 +706,89 @@ static void aoSamples(const FrameParams &P,
       cudaEventRecord(traceEvents[2 * i + 1], s);
     k_aoResolve<<<grid, 128, 0, s>>>(P, i, n, pixels, weighted);
   }
+}
+
+size_t dlWavefrontBytes(uint32_t w, uint32_t h, int aoSamples, uint32_t numLights)
+{
+  const size_t px = (size_t)w * h;
+  const size_t rays = px * ((size_t)max(aoSamples, 0) + numLights);
+  return px * (sizeof(DLPixel) + sizeof(uint32_t)) + rays * (sizeof(AORay) + 4 + 16) + 1536;
+}
+
+template <bool STATS, bool SEG>
+static void dlSamples(const FrameParams &P,
+    dim3 grid,
+    int numSMs,
+    uint32_t *consumed,
+    DLPixel *pixels,
+    AORay *rays,
+    float4 *payload,
+    uint32_t *rayCount,
+    float *weighted,
+    cudaStream_t s,
+    cudaEvent_t *traceEvents)
+{
+  int occ = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_aoTrace<STATS, SEG>, 128, 0);
+  const int traceGrid = numSMs * (occ > 0 ? occ : 1);
+  const int n = max(P.renderer.numIterations, 1);
+  for (int i = 0; i < n; i++) {
+    cudaMemsetAsync(rayCount, 0, 8, s); // queue length, fetch counter
+    k_dlPrimary<STATS><<<grid, 128, 0, s>>>(P, i, consumed, pixels, rays, payload, rayCount);
+    if (traceEvents)
+      cudaEventRecord(traceEvents[2 * i], s);
+    k_aoTrace<STATS, SEG><<<traceGrid, 128, 0, s>>>(P, rays, rayCount, rayCount + 1, weighted);
+    if (traceEvents)
+      cudaEventRecord(traceEvents[2 * i + 1], s);
+    k_dlResolve<<<grid, 128, 0, s>>>(P, i, n, pixels, weighted, payload);
+  }
+}
+
+cudaError_t launchDLWavefront(const FrameParams &P,
+    int numSMs,
+    bool stats,
+    void *scratch,
+    cudaStream_t s,
+    cudaEvent_t *traceEvents)
+{
+  const size_t px = (size_t)P.fb.w * P.fb.h;
+  const size_t nr = px * ((size_t)max(P.renderer.aoSamples, 0) + P.world.numLights);
+  uint8_t *p = (uint8_t *)scratch;
+  uint32_t *rayCount = (uint32_t *)p;
+  p += 256;
+  uint32_t *consumed = (uint32_t *)p;
+  p += ((px * 4 + 255) / 256) * 256;
+  DLPixel *pixels = (DLPixel *)p;
+  p += ((px * sizeof(DLPixel) + 255) / 256) * 256;
+  AORay *rays = (AORay *)p;
+  p += ((nr * sizeof(AORay) + 255) / 256) * 256;
+  float4 *payload = (float4 *)p;
+  p += ((nr * sizeof(float4) + 255) / 256) * 256;
+  float *weighted = (float *)p;
+  const dim3 grid((P.launchW + 7) / 8, (P.launchH + 15) / 16);
+  const bool seg = P.world.hasSegments != 0;
+  if (stats) {
+    if (seg)
+      dlSamples<true, true>(P, grid, numSMs, consumed, pixels, rays, payload, rayCount, weighted, s, traceEvents);
+    else
+      dlSamples<true, false>(P, grid, numSMs, consumed, pixels, rays, payload, rayCount, weighted, s, traceEvents);
+  } else {
+    if (seg)
+      dlSamples<false, true>(P, grid, numSMs, consumed, pixels, rays, payload, rayCount, weighted, s, traceEvents);
+    else
+      dlSamples<false, false>(P, grid, numSMs, consumed, pixels, rays, payload, rayCount, weighted, s, traceEvents);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launchRaycastWavefront(const FrameParams &P, bool stats, cudaStream_t s)
+{
+  const dim3 grid((P.launchW + 7) / 8, (P.launchH + 15) / 16);
+  if (stats)
+    k_raycastWave<true><<<grid, 128, 0, s>>>(P);
+  else
+    k_raycastWave<false><<<grid, 128, 0, s>>>(P);
+  return cudaGetLastError();
 }
 
 cudaError_t launchAOWavefront(const FrameParams &P,

@@ -91,7 +91,7 @@ def look_at_view(volume: int, dims, eye_unit, fovy_deg: float, width: int, heigh
 @dataclass
 class VolumeInput:
     density: torch.Tensor  # (nz, ny, nx) fp32 / fp16 / bf16, CUDA
-    tf: torch.Tensor  # (N, 4) fp32, CUDA
+    tf: torch.Tensor  # (N, 4) fp32 / fp16 / bf16, CUDA
     scale: torch.Tensor  # () or (1,) fp32, CUDA (opacity scale)
     step: float = 0.5
     unit: float = 1.0
@@ -133,6 +133,7 @@ class Batch:
             o.densityType = _DT[v.density.dtype]
             o.dims = (C.c_int * 3)(*v.dims)
             o.tf = v.tf.data_ptr()
+            o.tfType = _DT[v.tf.dtype]
             o.tfSize = v.tf.shape[0]
             o.opacityScale = 1.0
             o.opacityScaleDevice = v.scale.data_ptr()
