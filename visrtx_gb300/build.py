@@ -22,7 +22,7 @@ LIB = os.path.join(LIBDIR, "libvrtx.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_SOURCES = ["bvh.cu", "radix_sort.cu", "scene.cu", "render.cu", "render_counting.cu", "render_volume.cu", "render_ao.cu",
               "dm.cu"]
-CPP_SOURCES = ["device.cpp"]
+CPP_SOURCES = ["device.cpp", "anari_shim.cpp"]
 # Translation units whose arithmetic decides ids, depth and colour: compiled
 # without implicit multiply-add contraction, so every operation rounds as
 # written (the CPU oracle is built the same way, -ffp-contract=off); fused
@@ -77,6 +77,7 @@ def _build(verbose: bool, ptxas_info: bool, dflags: list) -> str:
     os.makedirs(os.path.dirname(LIB), exist_ok=True)
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
     headers.append(os.path.join(ROOT, "include", "vrtx.h"))
+    headers.append(os.path.join(ROOT, "include", "anari_visrtx.h"))
     jobs = []
     objs = []
     for src in CU_SOURCES:

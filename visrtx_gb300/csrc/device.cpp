@@ -13,6 +13,8 @@
 #include <cstdio>
 #include <set>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "objects.h"
 #include "radix_sort.h"
 
@@ -122,19 +124,53 @@ const char *typeName(int t)
 }
 
 // ---------------------------------------------------------------------------
+// NVTX ranges under the reference's names (utility/instrument.cpp:39-54,
+// call sites Frame.cu:201-306), so a profile timeline reads the same.
+// Without a profiler attached the calls do nothing measurable.
+// ---------------------------------------------------------------------------
+
+struct NvtxRange
+{
+  explicit NvtxRange(const char *name)
+  {
+    nvtxRangePushA(name);
+  }
+  ~NvtxRange()
+  {
+    nvtxRangePop();
+  }
+  NvtxRange(const NvtxRange &) = delete;
+  NvtxRange &operator=(const NvtxRange &) = delete;
+};
+
+// ---------------------------------------------------------------------------
 // Device
 // ---------------------------------------------------------------------------
 
 void Device::report(const Object *src, int severity, const char *msg)
 {
-  if (cb)
-    cb(cbPtr,
-        reinterpret_cast<VRTXDevice>(this),
-        reinterpret_cast<VRTXObject>(const_cast<Object *>(src)),
-        src ? src->type : 0,
-        severity,
-        0,
-        msg);
+  if (!cb)
+    return;
+  int type = src ? src->type : 0;
+  if (reportMap) {
+    type = reportMap(0, type);
+    severity = reportMap(1, severity);
+  }
+  cb(cbPtr,
+      reinterpret_cast<VRTXDevice>(this),
+      reinterpret_cast<VRTXObject>(const_cast<Object *>(src)),
+      type,
+      severity,
+      0,
+      msg);
+}
+
+// the ANARI entry points (anari_shim.cpp) make their devices report ANARI
+// codes
+void setReportCodes(VRTXDevice d, int (*map)(int kind, int value))
+{
+  if (d)
+    reinterpret_cast<Device *>(d)->reportMap = map;
 }
 
 // Lazy CUDA init (VisRTXDevice::initDevice, VisRTXDevice.cpp:435-458).
@@ -2899,6 +2935,7 @@ bool Frame::ready()
 
 void Frame::render()
 {
+  NvtxRange frameRange("Frame::renderFrame()");
   Device *d = Object::dev;
   wait();
   launches = 0;
@@ -2918,6 +2955,8 @@ void Frame::render()
   }
   cudaStream_t s = d->stream;
   if (world->builtStamp == 0 || world->deepStamp() > world->builtStamp) {
+    NvtxRange updateRange("update scene");
+    NvtxRange bvhRange("rebuild BVHs");
     if (!world->rebuild())
       return;
     d->markChanged();
@@ -2932,7 +2971,9 @@ void Frame::render()
       && fb.frameID >= renderer->sampleLimit)
     return;
   cudaEventRecord(evStart, s);
+  NvtxRange renderRange("render all frames");
   // newFrame (Frame.cu:590-660)
+  nvtxRangePushA("Frame::newFrame()");
   if (nextFrameReset) {
     fb.frameID = 0;
     fb.checkerboardID = renderer->checkerboard ? 0 : -1;
@@ -2946,6 +2987,7 @@ void Frame::render()
       fb.frameID += renderer->spp;
     fb.checkerboardID = renderer->checkerboard ? ((fb.checkerboardID + 1) & 0x3) : -1;
   }
+  nvtxRangePop(); // Frame::newFrame()
   FrameParams P{};
   P.world = world->gpu;
   P.world.maxTraversalSteps = maxTraversalSteps;
@@ -2978,6 +3020,9 @@ void Frame::render()
   const bool rcWave = P.renderer.type == RENDERER_RAYCAST && plainSurfaces;
   const bool wavefront = aoWave || dlWave;
   cudaError_t err = cudaSuccess;
+  // the one range not named as the reference's ("optixLaunch()"): the
+  // integrator kernels replace the OptiX launch
+  NvtxRange launchRange("render kernels");
   cudaEventRecord(evKStart, s);
   if (rcWave) {
     tracePairs = 0;
@@ -3103,6 +3148,7 @@ const void *Frame::map(
     ret = src;
   else {
     host->resize(bytes);
+    NvtxRange copyRange("copy to host");
     cudaMemcpy(host->data(), src, bytes, cudaMemcpyDeviceToHost);
     ret = host->data();
   }

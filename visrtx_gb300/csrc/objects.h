@@ -445,6 +445,9 @@ struct Device
   int desiredDevice = 0;
   int cudaDevice = 0;
   bool forceInit = false;
+  // devices made through the ANARI entry points report ANARI codes:
+  // reportMap(0, objectType) and reportMap(1, severity)
+  int (*reportMap)(int kind, int value) = nullptr;
   std::recursive_mutex mutex;
   // written once under the mutex by init(); read without it by the
   // per-call device scope
