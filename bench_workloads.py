@@ -354,11 +354,13 @@ def _time_steps(fn, steps, warmup, flush):
     return ts
 
 
-def _batched_step(vols, views, tile, target):
-    """One forward + L2 loss gradient + backward through a plan, captured
-    in a CUDA graph."""
+def _batched_step(vols, views, tile, target, shape=(0, 1)):
+    """One forward + L2 loss gradient + backward through a plan (launch
+    shape: blocks per SM, tiles per queue fetch), captured in a CUDA
+    graph."""
     b = dm.Batch(vols, views, tile)
     p = dm.Plan(b)
+    p.set_launch(*shape)
     grad = torch.empty_like(p.image)
 
     def body():
@@ -419,9 +421,12 @@ def _dm_measure(workload, vols, dens32, targets, views, steps, warmup, fp32_step
                 with_cpu=True):
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
     target = _targets(targets, views)
-    # the tile search times a forward + backward of up to 96 of the views
-    tile = dm.autotune(vols, views[:96], reps=1)
-    p, graph = _batched_step(vols, views, tile, target)
+    # the launch search (tile shape, then blocks per SM x tiles per queue
+    # fetch) times a forward + backward of up to 96 of the views
+    launch = dm.autotune_launch(vols, views[:96], reps=1)
+    tile = launch.tile
+    p, graph = _batched_step(vols, views, tile, target,
+                             (launch.blocks_per_sm, launch.tiles_per_fetch))
     clocks = ClockSampler(torch.cuda.current_device())
     clocks.start()
     tb = _time_steps(graph.replay, steps, warmup, flush)
@@ -461,7 +466,9 @@ def _dm_measure(workload, vols, dens32, targets, views, steps, warmup, fp32_step
         "metric": "views/s (fwd+bwd)", "value": round(vps, 2), "unit": "views/s",
         "steps": steps, "warmup": warmup, "ms_per_step": round(1000 * statistics.median(tb), 3),
         "dtype": {torch.float16: "f16", torch.bfloat16: "bf16"}.get(vols[0].density.dtype, "f32"),
-        "config": {"workload": workload, "tile": list(tile), "pixels": int(p.batch.pixels),
+        "config": {"workload": workload, "tile": list(tile),
+                   "blocks_per_sm": launch.blocks_per_sm,
+                   "tiles_per_fetch": launch.tiles_per_fetch, "pixels": int(p.batch.pixels),
                    "views": nviews, "l2": "flushed between steps (256 MiB)"},
         "fp32_per_view_staged_views_per_s": round(out["staged"], 2),
         "fp32_per_view_plain_views_per_s": round(out["plain"], 2),

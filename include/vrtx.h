@@ -461,6 +461,13 @@ VRTX_API int vrtxDMPlanBackward(VRTXDMPlan plan,
     const float *state,
     const float *gradImage,
     void *stream);
+/* The plan's launch shape: resident blocks per SM of both kernels (0: as
+ * many as fit, the default) and work items each block takes from the queue
+ * per atomic fetch (1..64 consecutive tiles, default 1). Results do not
+ * depend on it beyond float summation order of the gradient reductions.
+ * No reference counterpart (the differentiable marcher is this library's
+ * own). Returns 0, or a negative code after reporting the error. */
+VRTX_API int vrtxDMPlanSetLaunch(VRTXDMPlan plan, int blocksPerSM, int tilesPerFetch);
 VRTX_API void vrtxDMPlanRelease(VRTXDMPlan plan);
 
 /* The forward pass of vrtxDMForward for callers that cannot allocate

@@ -213,3 +213,68 @@ def test_autotune_returns_candidate(tmp_path):
     best = dm.autotune([v], views, candidates=[(16, 8), (32, 4)], reps=1, cache=cache)
     assert best in [(16, 8), (32, 4)]
     assert dm.autotune([v], views, candidates=[(16, 8), (32, 4)], cache=cache) == best
+
+
+def test_autotune_launch_and_plan_launch_shapes():
+    """The tuned launch is one of the candidates, and every launch shape
+    (blocks per SM, tiles per queue fetch) gives the same image bit for bit
+    and the same gradients up to reduction order."""
+    v = make_volume(seed=6, dtype=torch.float16)
+    views = views_for(v, k=3, seed=6)
+    best = dm.autotune_launch([v], views, tiles=[(16, 8), (32, 4)], blocks_per_sm=(0, 1),
+                              tiles_per_fetch=(1, 4), reps=1)
+    assert best.tile in [(16, 8), (32, 4)] and best.blocks_per_sm in (0, 1)
+    assert best.tiles_per_fetch in (1, 4)
+    b = dm.Batch([v], views, tile=(16, 8))
+    g = torch.randn((b.pixels, 3), device="cuda", generator=torch.Generator("cuda").manual_seed(1))
+    ref = None
+    for shape in [(0, 1), (1, 1), (0, 3), (2, 64)]:
+        p = dm.Plan(b)
+        p.set_launch(*shape)
+        img = p.forward().clone()
+        p.backward(g)
+        torch.cuda.synchronize()
+        out = (img, [t.clone() for t in p.grads[0]])
+        p.release()
+        if ref is None:
+            ref = out
+            continue
+        assert torch.equal(out[0], ref[0]), shape
+        for a, r in zip(out[1], ref[1]):
+            torch.testing.assert_close(a, r, rtol=1e-4, atol=1e-6)
+    p = dm.Plan(b)
+    with pytest.raises(RuntimeError):
+        p.set_launch(0, 65)
+    p.release()
+
+
+def test_batched_uneven_against_fp64_oracle():
+    """One launch over 3 volumes of different shapes (BF16 density) and 7
+    views of different resolutions, against the FP64 oracle run per view on
+    the FP32 originals: image RMS <= 1e-3, gradients <= 1e-2 relative."""
+    vols = [make_volume(n, seed=10 + i, dtype=torch.bfloat16)
+            for i, n in enumerate([(20, 24, 16), (33, 17, 25), (12, 30, 22)])]
+    views = []
+    res = [(32, 24), (16, 40), (48, 32), (24, 24), (40, 16), (32, 32), (8, 64)]
+    for i, r in enumerate(res):
+        vi = i % 3
+        views += views_for(vols[vi], k=1, res=r, vol=vi, seed=i)
+    batch = dm.Batch(vols, views, tile=(16, 8))
+    img, state = dm.forward(batch)
+    rng = np.random.default_rng(3)
+    g = rng.standard_normal((batch.pixels, 3)).astype(np.float32)
+    grads = dm.backward(batch, state, torch.tensor(g, device="cuda"))
+    imgs = img.cpu().numpy()
+    for vi in range(3):
+        idx = [i for i, w in enumerate(views) if w.volume == vi]
+        vws = [dm.View(0, views[i].width, views[i].height, views[i].eye, views[i].d00,
+                       views[i].du, views[i].dv, views[i].background) for i in idx]
+        sl = np.concatenate([np.arange(batch.offsets[i], batch.offsets[i] + views[i].width
+                                       * views[i].height) for i in idx])
+        ref, gD, gT, gS = ref_forward(vols[vi], vws, grad=g[sl].astype(np.float64))
+        rms = float(np.sqrt(np.mean((imgs[sl] - ref) ** 2)))
+        print("volume", vi, "rms", rms, "density", rel(grads[vi][0].cpu().numpy(), gD),
+              "tf", rel(grads[vi][1].cpu().numpy(), gT))
+        assert rms <= 1e-3
+        assert rel(grads[vi][0].cpu().numpy(), gD) <= 1e-2
+        assert rel(grads[vi][1].cpu().numpy(), gT) <= 1e-2

@@ -210,16 +210,24 @@ __global__ void __launch_bounds__(256) k_dmForward(const DMVol *vols,
     unsigned *counter,
     int tileW,
     int tileH,
+    unsigned fetch,
     float *image,
     float *state)
 {
+  // work items come from the queue `fetch` consecutive tiles at a time
   __shared__ unsigned item;
+  unsigned next = 0, left = 0;
   while (true) {
-    __syncthreads();
-    if (threadIdx.x == 0)
-      item = atomicAdd(counter, 1u);
-    __syncthreads();
-    const unsigned it = item;
+    if (left == 0) {
+      __syncthreads();
+      if (threadIdx.x == 0)
+        item = atomicAdd(counter, fetch);
+      __syncthreads();
+      next = item;
+      left = fetch;
+    }
+    const unsigned it = next++;
+    left--;
     if (it >= numItems)
       break;
     const DMViewG vw = views[findView(views, numViews, it)];
@@ -436,6 +444,7 @@ __global__ void __launch_bounds__(256, VRTX_DM_BWD_MIN_BLOCKS) k_dmBackward(cons
     unsigned *counter,
     int tileW,
     int tileH,
+    unsigned fetch,
     int tfMax,
     const float *state,
     const float *gradImage)
@@ -451,12 +460,19 @@ __global__ void __launch_bounds__(256, VRTX_DM_BWD_MIN_BLOCKS) k_dmBackward(cons
   // committed when the volume changes and at exit.
   int curVol = -1;
   float gScale = 0.f;
+  // work items come from the queue `fetch` consecutive tiles at a time
+  unsigned next = 0, left = 0;
   while (true) {
     __syncthreads();
-    if (threadIdx.x == 0)
-      item = atomicAdd(counter, 1u);
-    __syncthreads();
-    const unsigned it = item;
+    if (left == 0) {
+      if (threadIdx.x == 0)
+        item = atomicAdd(counter, fetch);
+      __syncthreads();
+      next = item;
+      left = fetch;
+    }
+    const unsigned it = next++;
+    left--;
     const int nextVol =
         it < numItems ? views[findView(views, numViews, it)].vol : -1;
     if (nextVol != curVol) {
@@ -613,6 +629,10 @@ struct Layout
   int maxTf = 0;
   int numViews = 0;
   int tileW = 0, tileH = 0;
+  // launch shape: resident blocks per SM (0: as many as fit) and work items
+  // per queue fetch
+  int blocksPerSM = 0;
+  unsigned fetch = 1;
 };
 
 int layout(const VRTXDMVolume *volumes,
@@ -720,13 +740,16 @@ int layout(const VRTXDMVolume *volumes,
   return 0;
 }
 
-int gridFor(const void *kernel, int threads, size_t smem)
+int gridFor(const void *kernel, int threads, size_t smem, int blocksPerSM)
 {
   int dev = 0, sms = 0, per = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, threads, smem);
-  return sms * (per > 0 ? per : 1);
+  per = per > 0 ? per : 1;
+  if (blocksPerSM > 0 && blocksPerSM < per)
+    per = blocksPerSM;
+  return sms * per;
 }
 
 // The forward kernel over a descriptor block already on the device.
@@ -740,16 +763,16 @@ cudaError_t launchForward(const Layout &L, uint8_t *block, float *image, float *
   const int threads = L.tileW * L.tileH;
   switch (L.type) {
   case VRTX_FLOAT16:
-    k_dmForward<__half><<<gridFor((const void *)k_dmForward<__half>, threads, 0), threads, 0, s>>>(
-        vols, views, L.numViews, L.numItems, counter, L.tileW, L.tileH, image, state);
+    k_dmForward<__half><<<gridFor((const void *)k_dmForward<__half>, threads, 0, L.blocksPerSM), threads, 0, s>>>(
+        vols, views, L.numViews, L.numItems, counter, L.tileW, L.tileH, L.fetch, image, state);
     break;
   case VRTX_BFLOAT16:
-    k_dmForward<__nv_bfloat16><<<gridFor((const void *)k_dmForward<__nv_bfloat16>, threads, 0), threads, 0, s>>>(
-        vols, views, L.numViews, L.numItems, counter, L.tileW, L.tileH, image, state);
+    k_dmForward<__nv_bfloat16><<<gridFor((const void *)k_dmForward<__nv_bfloat16>, threads, 0, L.blocksPerSM), threads, 0, s>>>(
+        vols, views, L.numViews, L.numItems, counter, L.tileW, L.tileH, L.fetch, image, state);
     break;
   default:
-    k_dmForward<float><<<gridFor((const void *)k_dmForward<float>, threads, 0), threads, 0, s>>>(
-        vols, views, L.numViews, L.numItems, counter, L.tileW, L.tileH, image, state);
+    k_dmForward<float><<<gridFor((const void *)k_dmForward<float>, threads, 0, L.blocksPerSM), threads, 0, s>>>(
+        vols, views, L.numViews, L.numItems, counter, L.tileW, L.tileH, L.fetch, image, state);
     break;
   }
   return cudaGetLastError();
@@ -767,16 +790,16 @@ cudaError_t launchBackward(const Layout &L, uint8_t *block, const float *state,
   const size_t smem = sizeof(float4) * (size_t)(threads / 32) * L.maxTf;
   switch (L.type) {
   case VRTX_FLOAT16:
-    k_dmBackward<__half><<<gridFor((const void *)k_dmBackward<__half>, threads, smem), threads, smem, s>>>(
-        vols, views, L.numViews, L.numItems, counter, L.tileW, L.tileH, L.maxTf, state, gradImage);
+    k_dmBackward<__half><<<gridFor((const void *)k_dmBackward<__half>, threads, smem, L.blocksPerSM), threads, smem, s>>>(
+        vols, views, L.numViews, L.numItems, counter, L.tileW, L.tileH, L.fetch, L.maxTf, state, gradImage);
     break;
   case VRTX_BFLOAT16:
-    k_dmBackward<__nv_bfloat16><<<gridFor((const void *)k_dmBackward<__nv_bfloat16>, threads, smem), threads, smem, s>>>(
-        vols, views, L.numViews, L.numItems, counter, L.tileW, L.tileH, L.maxTf, state, gradImage);
+    k_dmBackward<__nv_bfloat16><<<gridFor((const void *)k_dmBackward<__nv_bfloat16>, threads, smem, L.blocksPerSM), threads, smem, s>>>(
+        vols, views, L.numViews, L.numItems, counter, L.tileW, L.tileH, L.fetch, L.maxTf, state, gradImage);
     break;
   default:
-    k_dmBackward<float><<<gridFor((const void *)k_dmBackward<float>, threads, smem), threads, smem, s>>>(
-        vols, views, L.numViews, L.numItems, counter, L.tileW, L.tileH, L.maxTf, state, gradImage);
+    k_dmBackward<float><<<gridFor((const void *)k_dmBackward<float>, threads, smem, L.blocksPerSM), threads, smem, s>>>(
+        vols, views, L.numViews, L.numItems, counter, L.tileW, L.tileH, L.fetch, L.maxTf, state, gradImage);
     break;
   }
   return cudaGetLastError();
@@ -925,6 +948,19 @@ VRTX_API int vrtxDMPlanBackward(
   const cudaError_t e =
       launchBackward(plan->L, plan->block, state, gradImage, (cudaStream_t)stream);
   return e == cudaSuccess ? 0 : fail(plan->dev, cudaGetErrorString(e), -8);
+}
+
+VRTX_API int vrtxDMPlanSetLaunch(VRTXDMPlan plan, int blocksPerSM, int tilesPerFetch)
+{
+  if (!plan)
+    return -1;
+  if (blocksPerSM < 0 || blocksPerSM > 64 || tilesPerFetch < 1 || tilesPerFetch > 64)
+    return fail(plan->dev,
+        "vrtxDMPlanSetLaunch: blocksPerSM must be 0..64, tilesPerFetch 1..64",
+        -2);
+  plan->L.blocksPerSM = blocksPerSM;
+  plan->L.fetch = (unsigned)tilesPerFetch;
+  return 0;
 }
 
 VRTX_API void vrtxDMPlanRelease(VRTXDMPlan plan)

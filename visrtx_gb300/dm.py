@@ -11,7 +11,8 @@ computes the rendering.
 
 Many views of many volumes render in one launch; Plan keeps the launch
 descriptors on the device so forward + backward can be captured in a CUDA
-graph; autotune() picks the tile shape.
+graph; autotune() picks the tile shape, autotune_launch() the tile shape,
+resident blocks per SM and tiles per queue fetch.
 """
 from __future__ import annotations
 
@@ -254,10 +255,80 @@ class Plan:
                "vrtxDMPlanBackward")
         return self.grads
 
+    def set_launch(self, blocks_per_sm: int = 0, tiles_per_fetch: int = 1):
+        """Launch shape of both kernels: resident blocks per SM (0: as many
+        as fit) and tiles taken from the work queue per fetch."""
+        _check(L.load().vrtxDMPlanSetLaunch(C.c_void_p(self.h), int(blocks_per_sm),
+                                            int(tiles_per_fetch)), "vrtxDMPlanSetLaunch")
+        self.launch = (int(blocks_per_sm), int(tiles_per_fetch))
+
     def release(self):
         if self.h:
             L.load().vrtxDMPlanRelease(C.c_void_p(self.h))
             self.h = None
+
+
+BLOCKS_PER_SM = (0, 1, 2)
+TILES_PER_FETCH = (1, 2, 8)
+
+
+@dataclass
+class Launch:
+    """A tuned launch: tile shape, resident blocks per SM (0: as many as
+    fit) and tiles per queue fetch."""
+    tile: tuple
+    blocks_per_sm: int = 0
+    tiles_per_fetch: int = 1
+
+
+def _time_plan(volumes, views, tile, shape, reps):
+    p = Plan(Batch(volumes, views, tile))
+    p.set_launch(*shape)
+    g = torch.ones_like(p.image)
+    p.forward()
+    p.backward(g)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        p.forward()
+        p.backward(g)
+    torch.cuda.synchronize()
+    p.release()
+    return (time.perf_counter() - t0) / reps
+
+
+def autotune_launch(volumes: list[VolumeInput], views: list[View], tiles=TILES,
+                    blocks_per_sm=BLOCKS_PER_SM, tiles_per_fetch=TILES_PER_FETCH, reps: int = 2,
+                    cache: str | None = None) -> Launch:
+    """Times forward + backward of this workload over the tile shapes, then,
+    for the fastest tile, over resident blocks per SM x tiles per queue
+    fetch; returns the fastest Launch. Cached in a JSON file keyed by the
+    workload's shape when `cache` is given."""
+    key = "launch:" + json.dumps({"dtype": str(volumes[0].density.dtype),
+                                  "dims": sorted({v.dims for v in volumes}),
+                                  "res": sorted({(w.width, w.height) for w in views}),
+                                  "views": len(views), "volumes": len(volumes)}, default=list)
+    table = {}
+    if cache and os.path.exists(cache):
+        with open(cache) as f:
+            table = json.load(f)
+        if key in table:
+            e = table[key]
+            return Launch(tuple(e["tile"]), e["blocks_per_sm"], e["tiles_per_fetch"])
+    times = {tile: _time_plan(volumes, views, tile, (0, 1), reps) for tile in tiles}
+    tile = min(times, key=times.get)
+    shapes = {(b, f): _time_plan(volumes, views, tile, (b, f), reps)
+              for b in blocks_per_sm for f in tiles_per_fetch}
+    b, f = min(shapes, key=shapes.get)
+    best = Launch(tuple(tile), b, f)
+    if cache:
+        table[key] = {"tile": list(tile), "blocks_per_sm": b, "tiles_per_fetch": f,
+                      "ms_tiles": {f"{a}x{c}": 1e3 * t for (a, c), t in times.items()},
+                      "ms_shapes": {f"{a}/{c}": 1e3 * t for (a, c), t in shapes.items()}}
+        os.makedirs(os.path.dirname(os.path.abspath(cache)), exist_ok=True)
+        with open(cache, "w") as fh:
+            json.dump(table, fh, indent=1)
+    return best
 
 
 def autotune(volumes: list[VolumeInput], views: list[View], candidates=TILES, reps: int = 3,
