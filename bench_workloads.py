@@ -422,8 +422,11 @@ def _dm_measure(workload, vols, dens32, targets, views, steps, warmup, fp32_step
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
     target = _targets(targets, views)
     # the launch search (tile shape, then blocks per SM x tiles per queue
-    # fetch) times a forward + backward of up to 96 of the views
-    launch = dm.autotune_launch(vols, views[:96], reps=1)
+    # fetch) times a forward + backward of about 96 views spread over the
+    # whole set (every k-th view), two repetitions each
+    sub = views[::max(1, len(views) // 96)]
+    launch = dm.autotune_launch(vols, [dm.View(w.volume, w.width, w.height, w.eye, w.d00, w.du,
+                                               w.dv, w.background) for w in sub], reps=2)
     tile = launch.tile
     p, graph = _batched_step(vols, views, tile, target,
                              (launch.blocks_per_sm, launch.tiles_per_fetch))
