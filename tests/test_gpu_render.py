@@ -435,6 +435,39 @@ def test_volume_parity(device, rate):
     print(rep)
 
 
+@pytest.mark.parametrize("renderer", ["raycast", "default"])
+def test_volume_dda_march_matches_plain_march(device, renderer):
+    """A volume whose TF is transparent over its low values has empty
+    macrocells: its march runs the DDA over the skipping grid (empty cells
+    crossed without fetches). The frames equal those of the plain
+    fixed-step march ("vrtx.emptySpaceSkipping" false) bit for bit, with the
+    same sample count and fewer fetches, and match the oracle."""
+    spec = small_volume(n=64, renderer=renderer)
+    op = np.array(spec.volumes[0].opacity, np.float32)
+    op[: len(op) // 2] = 0.0
+    spec.volumes[0].opacity = op
+    if renderer == "default":
+        spec.renderer.ambient_samples = 0
+    frames = []
+    for skipping in (True, False):
+        fr, w, keep = S.build_on_device(device, spec)
+        vols = [o for o in keep if getattr(o, "subtype", "") == "transferFunction1D"]
+        assert len(vols) == 1
+        vols[0].set("vrtx.emptySpaceSkipping", skipping)
+        vols[0].commit()
+        fr.render()
+        fr.wait()
+        frames.append(({ch: fr.map("channel." + ch)
+                        for ch in ("color", "depth", "primitiveId", "objectId", "instanceId")},
+                       fr.stats()))
+    for ch in frames[0][0]:
+        assert np.array_equal(frames[0][0][ch], frames[1][0][ch]), ch
+    (_, st_dda), (_, st_plain) = frames
+    assert st_dda["volume_samples"] == st_plain["volume_samples"]
+    assert st_dda["volume_fetches"] < 0.9 * st_plain["volume_fetches"], (st_dda, st_plain)
+    compare(dict(frames[0][0]), render_oracle(spec), color_tol=1)
+
+
 def test_volume_fp64_rms(device):
     """Volume colour against the clean FP64 marcher (exact trilinear, FP64
     compositing): RMS <= 1e-3 over the FLOAT32_VEC4 colour channel, so no

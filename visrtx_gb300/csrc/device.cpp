@@ -1950,6 +1950,9 @@ void Volume::commit()
         "volume subtype '%s' is not supported",
         subtype.c_str());
   id = get<uint32_t>("id", VRTX_UINT32, ~0u);
+  // "vrtx.emptySpaceSkipping" false: march every sample with a fetch (the
+  // plain fixed-step loop); results are the same either way
+  emptySpaceSkipping = get<int32_t>("vrtx.emptySpaceSkipping", VRTX_BOOL, 1) != 0;
   field = static_cast<SpatialField *>(getObject("value", VRTX_SPATIAL_FIELD));
   color = static_cast<Array *>(getObject("color", VRTX_ARRAY1D));
   opacity = static_cast<Array *>(getObject("opacity", VRTX_ARRAY1D));
@@ -2536,7 +2539,8 @@ bool World::rebuild()
         vg.id = v->id;
         vg.instId = inst->userID(t);
         vg.worldToObject = r.worldToObject;
-        vg.majorants = v->hasEmptyCells ? v->majorants : nullptr;
+        vg.majorants =
+            v->hasEmptyCells && v->emptySpaceSkipping ? v->majorants : nullptr;
         vg.dptMajorants = v->dptMajorants;
         for (int k = 0; k < 3; k++) {
           vg.mcDims[k] = f->mcDims[k];

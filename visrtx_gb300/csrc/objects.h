@@ -281,6 +281,7 @@ struct Volume : Object
   float *majorants = nullptr;
   float *dptMajorants = nullptr; // delta-tracking majorants (reference rule)
   bool hasEmptyCells = false; // some skipping-grid cell has majorant 0
+  bool emptySpaceSkipping = true; // "vrtx.emptySpaceSkipping"
   uint64_t builtStamp = 0;
   ~Volume() override;
   void commit() override;

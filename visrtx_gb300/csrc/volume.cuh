@@ -1,11 +1,13 @@
 // Scivis volume integration (device code): the fixed-step emission-absorption
 // marcher of the reference (devices/rtx/gpu/volumeIntegration.h:64-165,
 // 318-350) with two additions that leave its results unchanged:
-//  * samples whose macrocell majorant is 0 (no voxel the trilinear filter can
-//    reach in that cell maps to a non-zero TF alpha) are not fetched: their
-//    contribution is exactly zero (1 - pow(1 - 0, x) == 0), and the march
-//    position still advances by the same repeated float additions, so every
-//    later sample sits where the reference puts it;
+//  * in a volume with empty macrocells the march is driven by a 3D DDA over
+//    the conservative macrocell grid, and samples in a cell whose majorant
+//    is 0 (no voxel the trilinear filter can reach there maps to a non-zero
+//    TF alpha) are not fetched: their contribution is exactly zero
+//    (1 - pow(1 - 0, x) == 0), and the march position still advances by the
+//    same repeated float additions, so every later sample sits where the
+//    reference puts it;
 //  * the volume "TLAS" is a flat list scanned for the nearest entry, in
 //    place of the OptiX volume BVH (the lists here are short).
 #pragma once
@@ -131,6 +133,108 @@ __device__ __forceinline__ float cellMajorant(const VolumeGPU &v, f3 p)
       + ((size_t)cz * v.mcDims[1] + cy) * v.mcDims[0] + cx);
 }
 
+// One sample of the march: classify, composite front to back
+// (volumeIntegration.h:46-103).
+__device__ __forceinline__ void compositeSample(const VolumeGPU &v,
+    float s,
+    float exponent,
+    f3 *color,
+    float &opacity,
+    float &transmittance)
+{
+  if (isnan(s))
+    return;
+  const float4 co = classifySample(v, s);
+  const float stepT = powf(1.f - co.w, exponent);
+  const float a = transmittance * (1.f - stepT);
+  if (color)
+    *color += a * mk3(co.x, co.y, co.z);
+  opacity += a;
+  transmittance *= stepT;
+}
+
+// The fixed-step march of a volume with empty macrocells, driven by a 3D
+// DDA over the conservative skipping grid (16^3-voxel cells from the field
+// origin): each cell gives the ray distance at which the ray leaves it; in
+// a cell whose majorant is 0 the samples are only counted and the position
+// advances by the same float additions, in a non-empty cell every sample is
+// fetched and composited. The samples, their positions and the
+// accumulation order are the plain march's, so the result is the same bit
+// for bit. A sample within rounding of a cell face can be taken for either
+// cell; the majorants cover one voxel of apron around each cell, so either
+// cell's majorant bounds it.
+template <typename Field>
+__device__ __forceinline__ void marchCellsDDA(const VolumeGPU &v,
+    Field &field,
+    const VolumeHitG &h,
+    float lower,
+    float upper,
+    float stepSize,
+    float exponent,
+    f3 *color,
+    float &opacity,
+    TravStats &st)
+{
+  float transmittance = 1.f;
+  // voxel coordinates along the ray: q(t) = qo + qd * t
+  const f3 inv = mk3(1.f / v.spacing.x, 1.f / v.spacing.y, 1.f / v.spacing.z);
+  const f3 qo = (h.localOrg - v.origin) * inv;
+  const f3 qd = h.localDir * inv;
+  const f3 q0 = qo + qd * lower;
+  int cell[3], stepDir[3];
+  float tNext[3], tDelta[3];
+  const float o[3] = {qo.x, qo.y, qo.z}, d[3] = {qd.x, qd.y, qd.z}, q[3] = {q0.x, q0.y, q0.z};
+#pragma unroll
+  for (int a = 0; a < 3; a++) {
+    cell[a] = min(max((int)floorf(q[a] * (1.f / 16.f)), 0), v.mcDims[a] - 1);
+    if (d[a] > 0.f) {
+      stepDir[a] = 1;
+      tNext[a] = (16.f * float(cell[a] + 1) - o[a]) / d[a];
+      tDelta[a] = 16.f / d[a];
+    } else if (d[a] < 0.f) {
+      stepDir[a] = -1;
+      tNext[a] = (16.f * float(cell[a]) - o[a]) / d[a];
+      tDelta[a] = -16.f / d[a];
+    } else {
+      stepDir[a] = 0;
+      tNext[a] = __int_as_float(0x7f800000);
+      tDelta[a] = 0.f;
+    }
+  }
+  bool inGrid = true;
+  int guard = 0;
+  while (guard < (1 << 24) && opacity < 0.99f && upper - lower >= 0.f) {
+    const int a = tNext[0] <= tNext[1] ? (tNext[0] <= tNext[2] ? 0 : 2)
+                                       : (tNext[1] <= tNext[2] ? 1 : 2);
+    // past the grid (rounding at its far face): march the rest as non-empty
+    const float tExit = inGrid ? tNext[a] : __int_as_float(0x7f800000);
+    const float maj = inGrid
+        ? __ldg(v.majorants + ((size_t)cell[2] * v.mcDims[1] + cell[1]) * v.mcDims[0] + cell[0])
+        : 1.f;
+    if (maj == 0.f) {
+      for (; guard < (1 << 24) && lower <= tExit && upper - lower >= 0.f; guard++) {
+        st.samples++;
+        lower += stepSize;
+      }
+    } else {
+      for (; guard < (1 << 24) && lower <= tExit && opacity < 0.99f && upper - lower >= 0.f;
+           guard++) {
+        st.samples++;
+        st.fetches++;
+        const float s = field(v, h.localOrg + h.localDir * lower);
+        compositeSample(v, s, exponent, color, opacity, transmittance);
+        lower += stepSize;
+      }
+    }
+    if (!inGrid)
+      break;
+    cell[a] += stepDir[a];
+    tNext[a] += tDelta[a];
+    inGrid = cell[a] >= 0 && cell[a] < v.mcDims[a];
+    guard++;
+  }
+}
+
 // rayMarchVolume + _rayMarchVolume (volumeIntegration.h:64-126): returns the
 // entry depth; accumulates into color (when non-null) and opacity.
 template <typename Field>
@@ -153,6 +257,10 @@ __device__ __forceinline__ float rayMarchVolumeF(const VolumeGPU &v,
   float transmittance = 1.f;
   if (!(stepSize > 0.f))
     return depth;
+  if (v.majorants) {
+    marchCellsDDA(v, field, h, lower, upper, stepSize, exponent, color, opacity, st);
+    return depth;
+  }
   // Software-pipelined: the field fetch for the next position is issued
   // before the current sample is classified, so the two dependent texture
   // reads of consecutive samples overlap. Positions, the order of the
