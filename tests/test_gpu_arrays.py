@@ -155,3 +155,19 @@ def test_cuda_array_used_in_place(device):
     dev.lib.vrtxUnmapArray(dev.h, a.handle)
     assert centre_depth(f) == pytest.approx(1.5, abs=1e-4)
     assert not dev.errors()
+
+
+def test_object_array_from_gpu_memory_is_rejected(device):
+    """Arrays of object handles must live in host memory (Array.cpp:78-81):
+    one made from a CUDA pointer is refused with an error and a null
+    handle, and its memory is left alone."""
+    import torch
+
+    buf = torch.zeros(4, dtype=torch.int64, device="cuda")
+    dev = device
+    h = dev.lib.vrtxNewArray1D(dev.h, C.c_void_p(buf.data_ptr()), None, None, L.SURFACE, 4)
+    assert not h
+    assert any("object arrays from GPU memory" in m for m in dev.errors())
+    dev.messages.clear()
+    torch.cuda.synchronize()
+    assert int(buf.sum()) == 0

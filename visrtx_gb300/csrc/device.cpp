@@ -382,11 +382,16 @@ Array::Array(Device *d,
     owned.resize(bytes());
   else if (d->initOk) {
     // NV_ARRAY_CUDA: application device pointers are used in place
+    // getPointerAddressSpace (Array.cpp:38-65): device memory of this GPU
+    // and managed memory are used in place; another GPU's memory is foreign
     cudaPointerAttributes attr{};
-    if (cudaPointerGetAttributes(&attr, appMem) == cudaSuccess
-        && (attr.type == cudaMemoryTypeDevice
-            || attr.type == cudaMemoryTypeManaged))
-      appIsDevice = true;
+    if (cudaPointerGetAttributes(&attr, appMem) == cudaSuccess) {
+      if (attr.type == cudaMemoryTypeManaged
+          || (attr.type == cudaMemoryTypeDevice && attr.device == d->cudaDevice))
+        appIsDevice = true;
+      else if (attr.type == cudaMemoryTypeDevice)
+        appIsForeign = true;
+    }
     cudaGetLastError();
   }
   dataStamp = newStamp();
@@ -405,7 +410,7 @@ Array::~Array()
 
 const void *Array::hostData() const
 {
-  if (appIsDevice)
+  if (appIsDevice || appIsForeign)
     return nullptr;
   return appMem ? appMem : owned.data();
 }
@@ -433,15 +438,19 @@ const void *Array::deviceData()
     }
     devBytes = b;
   }
-  cudaMemcpyAsync(
-      dptr, hostData(), b, cudaMemcpyHostToDevice, Object::dev->stream);
+  // a foreign array comes from the other GPU through unified addressing
+  cudaMemcpyAsync(dptr,
+      appIsForeign ? appMem : hostData(),
+      b,
+      appIsForeign ? cudaMemcpyDefault : cudaMemcpyHostToDevice,
+      Object::dev->stream);
   devStamp = dataStamp;
   return dptr;
 }
 
 void *Array::map()
 {
-  if (appIsDevice)
+  if (appIsDevice || appIsForeign)
     return const_cast<void *>(appMem);
   return const_cast<void *>(hostData());
 }
@@ -455,7 +464,7 @@ void Array::unmap()
 
 void Array::privatize()
 {
-  if (!appMem || deleter || appIsDevice)
+  if (!appMem || deleter || appIsDevice || appIsForeign)
     return;
   owned.assign((const uint8_t *)appMem, (const uint8_t *)appMem + bytes());
   appMem = nullptr;
@@ -466,7 +475,7 @@ void Array::refreshHandles()
   for (auto *h : handles)
     releaseObj(h);
   handles.clear();
-  if (!isObjectType(elemType) || appIsDevice)
+  if (!isObjectType(elemType) || appIsDevice || appIsForeign)
     return;
   const Object *const *p = reinterpret_cast<const Object *const *>(hostData());
   if (!p)
@@ -3624,6 +3633,16 @@ static VRTXArray newArray(VRTXDevice d,
     return nullptr;
   }
   auto *a = new Array(dev, dims, mem, del, ud, et, n1, n2, n3);
+  if (isObjectType(et) && (a->appIsDevice || a->appIsForeign)) {
+    // Array.cpp:78-81
+    a->appMem = nullptr; // not the library's to release or delete
+    a->deleter = nullptr;
+    delete a;
+    dev->report(nullptr,
+        VRTX_SEVERITY_ERROR,
+        "illegal operation: cannot create object arrays from GPU memory");
+    return nullptr;
+  }
   dev->live.push_back(a);
   dev->markChanged();
   return reinterpret_cast<VRTXArray>(a);

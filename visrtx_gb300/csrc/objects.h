@@ -95,7 +95,11 @@ struct Array : Object
   VRTXMemoryDeleter deleter = nullptr;
   const void *deleterPtr = nullptr;
   std::vector<uint8_t> owned; // managed arrays / privatised copies
-  bool appIsDevice = false;
+  bool appIsDevice = false; // application memory on this device's GPU
+  // application memory on another GPU (the reference's FOREIGN address
+  // space, Array.cpp:50-53): copied to this GPU at upload, never read in
+  // place
+  bool appIsForeign = false;
   void *dptr = nullptr;
   size_t devBytes = 0;
   uint64_t dataStamp = 0;
