@@ -71,6 +71,10 @@ def _args():
                    help="skip the other workloads in the N=1 line")
     p.add_argument("--nvdb-type", default="fp16", choices=["float", "fp4", "fp8", "fp16", "fpn"])
     p.add_argument("--dm-views", type=int, default=128)
+    p.add_argument("--size", default="1920x1080",
+                   help="frame size of the default line's scene (a smaller frame for profiling)")
+    p.add_argument("--lib", default=None,
+                   help="libvrtx.so to load (a tuning variant from python -m visrtx_gb300.build --lib)")
     return p.parse_args()
 
 
@@ -257,8 +261,9 @@ def main():
     from visrtx_gb300 import anari
     from visrtx_gb300 import scenes as S
 
-    spec = S.instanced_spec(spp=args.spp)
-    dev = anari.Device(local)
+    width, height = (int(v) for v in args.size.split("x"))
+    spec = S.instanced_spec(spp=args.spp, width=width, height=height)
+    dev = anari.Device(local, lib_path=args.lib)
     assert dev.is_valid(), dev.errors()
     frame, world, keep = build_scene(dev, spec)
 
@@ -391,8 +396,9 @@ def main():
             "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": round(1000 * secs_max / args.steps, 3), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "renderer": "ao", "spp": args.spp, "ao_samples": 16,
-                       "width": 1920, "height": 1080, "l2": "flushed between frames (256 MiB)",
+            "config": {"workload": WORKLOAD.replace("1920x1080", args.size), "renderer": "ao",
+                       "spp": args.spp, "ao_samples": 16, "width": width, "height": height,
+                       "l2": "flushed between frames (256 MiB)",
                        "bvh_build_ms": round(build_ms, 2)},
             "rays_per_frame": rays / args.steps,
             "gpu_launches": launches,

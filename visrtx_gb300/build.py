@@ -113,4 +113,16 @@ def _build(verbose: bool, ptxas_info: bool, dflags: list) -> str:
 
 
 if __name__ == "__main__":
-    build(verbose=True, ptxas_info="--ptxas" in sys.argv)
+    import argparse
+
+    ap = argparse.ArgumentParser(description="build libvrtx.so (sm_103a)")
+    ap.add_argument("--ptxas", action="store_true", help="print ptxas register / spill info")
+    ap.add_argument("--define", action="append", default=[],
+                    help="NAME=VALUE for a tuning macro (e.g. VRTX_AO_LEAF_TURN=0); needs --lib")
+    ap.add_argument("--lib", default=None, help="output path of a tuning variant")
+    a = ap.parse_args()
+    if a.define and not a.lib:
+        ap.error("--define builds a variant: give its --lib path")
+    obj = os.path.join(os.path.dirname(os.path.abspath(a.lib)), "_obj") if a.lib else None
+    build(verbose=True, ptxas_info=a.ptxas, defines=tuple(a.define),
+          lib_path=os.path.abspath(a.lib) if a.lib else None, obj_dir=obj)

@@ -196,6 +196,15 @@ __global__ void __launch_bounds__(128, VRTX_TRACE_MIN_BLOCKS) k_aoTrace(const Fr
   while (true) {
     const uint32_t want = __ballot_sync(0xffffffffu, !live && !exhausted);
     const uint32_t busy = __ballot_sync(0xffffffffu, live);
+#if VRTX_AO_LEAF_TURN > 0
+    // leaf tests run once this share (percent) of the live lanes hold a
+    // leaf group, or all of them do; until then those lanes keep to nodes
+    const uint32_t pend = __ballot_sync(0xffffffffu, live && s.tri.y != 0u);
+    const bool leafTurn =
+        pend == busy || __popc(pend) * 100u >= __popc(busy) * (uint32_t)VRTX_AO_LEAF_TURN;
+#else
+    const bool leafTurn = true;
+#endif
     if (want && (__popc(want) >= VRTX_AO_REFILL || busy == 0u)) {
       const uint32_t leader = __ffs(want) - 1;
       uint32_t base = 0;
@@ -229,7 +238,8 @@ __global__ void __launch_bounds__(128, VRTX_TRACE_MIN_BLOCKS) k_aoTrace(const Fr
           stack,
           reinterpret_cast<const float4 *>(rays + idx),
           P.errorFlag,
-          st);
+          st,
+          leafTurn);
       if (r != OCC_CONTINUE) {
         weighted[idx] = r == OCC_HIT ? __ldg(&rays[idx].dirWeight.w) : 0.f;
         live = false;

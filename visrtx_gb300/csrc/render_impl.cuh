@@ -36,6 +36,12 @@
 #define VRTX_AO_REFILL 4
 #endif
 
+// leaf postponement in the AO any-hit kernel: a warp tests leaf groups once
+// this percentage of its live lanes hold one (0: every step, no postponing)
+#ifndef VRTX_AO_LEAF_TURN
+#define VRTX_AO_LEAF_TURN 50
+#endif
+
 // traversal stack entries of the AO any-hit kernel kept in shared memory
 #ifndef VRTX_AO_SHARED_STACK
 #define VRTX_AO_SHARED_STACK 16
@@ -53,9 +59,10 @@
 #define VRTX_NANOVDB_MIN_BLOCKS 4
 #endif
 
-// the same for the wavefront AO's primary (closest-hit) kernel
+// the same for the wavefront primary (closest-hit) kernels of "ao",
+// "default" and "raycast" (5: <= 102 registers; a few spills, more warps)
 #ifndef VRTX_PRIMARY_MIN_BLOCKS
-#define VRTX_PRIMARY_MIN_BLOCKS 1
+#define VRTX_PRIMARY_MIN_BLOCKS 5
 #endif
 
 #ifndef VRTX_TRACE_MIN_BLOCKS
