@@ -254,8 +254,9 @@ def main():
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     import __graft_entry__ as g
 
-    if rank == 0 or not os.path.exists(os.path.join(ROOT, "visrtx_gb300", "lib", "libvrtx.so")):
-        g.build()
+    if args.lib is None and (
+            rank == 0 or not os.path.exists(os.path.join(ROOT, "visrtx_gb300", "lib", "libvrtx.so"))):
+        g.build()  # a --lib variant is built beforehand (python -m visrtx_gb300.build --lib)
     if ws > 1:
         torch.distributed.barrier()
     from visrtx_gb300 import anari
@@ -338,6 +339,7 @@ def main():
                 "algorithmic_bytes_per_launch": trace_launch_bytes,
                 "launch_ms": round(trace_launch_ms, 4),
                 "share_of_frame_kernel_time": round(statistics.mean(tms) / k_ms, 4),
+                "nodes_per_ray": round(tst["nodes"] / max(tst["rays"], 1), 2),
                 "per_launch": {k: tst[k] / args.spp for k in ("rays", "nodes", "tri_tests",
                                                               "sphere_tests", "blas_entries")},
                 "frame": {"achieved": round(frame_bytes / (k_ms / 1e3) / 1e9, 1),

@@ -149,16 +149,20 @@ class VRTXDMView(C.Structure):
 
 
 _lib = None
+_lib_path = None
 _lock = threading.Lock()
 
 
 def load(path: str | None = None) -> C.CDLL:
     """Loads libvrtx.so (built by visrtx_gb300.build) and declares its ABI."""
-    global _lib
+    global _lib, _lib_path
     with _lock:
+        p = os.path.realpath(path or LIB_PATH)
         if _lib is not None:
+            if path is not None and p != _lib_path:
+                raise RuntimeError(f"libvrtx is already loaded from {_lib_path}; "
+                                   f"one process loads one library (asked for {p})")
             return _lib
-        p = path or LIB_PATH
         if not os.path.exists(p):
             raise RuntimeError(
                 f"libvrtx.so not found at {p}; build it with "
@@ -170,4 +174,5 @@ def load(path: str | None = None) -> C.CDLL:
             fn.restype = res
             fn.argtypes = args
         _lib = lib
+        _lib_path = p
         return lib

@@ -171,8 +171,11 @@ __global__ void __launch_bounds__(128, VRTX_PRIMARY_MIN_BLOCKS) k_aoPrimary(cons
 // holds one ray; a lane whose ray has ended takes the next one from the
 // queue (one atomic per warp, once at least VRTX_AO_REFILL lanes wait, or
 // when the warp has no live ray), so a warp keeps most lanes busy instead
-// of waiting for its slowest ray. Each ray's result depends on that ray
-// alone: the queue order in which lanes take rays does not change it.
+// of waiting for its slowest ray. Between refill checks each lane takes up
+// to VRTX_AO_STEPS traversal steps; the warp votes each time whether this
+// is a leaf turn (leaf postponement, occlusionStep). Each ray's result
+// depends on that ray alone: neither the queue order in which lanes take
+// rays nor the order of its tests changes it.
 template <bool STATS, bool SEG>
 __global__ void __launch_bounds__(128, VRTX_TRACE_MIN_BLOCKS) k_aoTrace(const FrameParams P,
     const AORay *rays,
@@ -232,14 +235,15 @@ __global__ void __launch_bounds__(128, VRTX_TRACE_MIN_BLOCKS) k_aoTrace(const Fr
     }
     if (__all_sync(0xffffffffu, exhausted))
       break;
-    if (live) {
+#pragma unroll 1
+    for (int k = 0; k < VRTX_AO_STEPS && live; k++) {
       const int r = occlusionStep<STATS, VRTX_TRAVERSAL_STACK, decltype(stack), SEG>(P.world,
           s,
           stack,
           reinterpret_cast<const float4 *>(rays + idx),
           P.errorFlag,
           st,
-          leafTurn);
+          leafTurn && k == 0);
       if (r != OCC_CONTINUE) {
         weighted[idx] = r == OCC_HIT ? __ldg(&rays[idx].dirWeight.w) : 0.f;
         live = false;

@@ -42,6 +42,12 @@
 #define VRTX_AO_LEAF_TURN 50
 #endif
 
+// traversal steps per lane between the AO any-hit kernel's queue refills
+// (3: fewer refill votes per node test; more leave lanes idle at a ray's end)
+#ifndef VRTX_AO_STEPS
+#define VRTX_AO_STEPS 3
+#endif
+
 // traversal stack entries of the AO any-hit kernel kept in shared memory
 #ifndef VRTX_AO_SHARED_STACK
 #define VRTX_AO_SHARED_STACK 16
