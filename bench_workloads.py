@@ -354,10 +354,12 @@ def _time_steps(fn, steps, warmup, flush):
     return ts
 
 
-def _batched_step(vols, views, tile, target, shape=(0, 1)):
-    """One forward + L2 loss gradient + backward through a plan (launch
-    shape: blocks per SM, tiles per queue fetch), captured in a CUDA
-    graph."""
+def _batched_step(vols, views, tile, target, shape=(0, 1), fused=True):
+    """One training step of the L2 loss through a plan (launch shape:
+    blocks per SM, tiles per queue fetch), captured in a CUDA graph: with
+    `fused` the one-launch step (forward, loss gradient and backward in one
+    persistent kernel), else a forward launch, the loss gradient in torch
+    and a backward launch."""
     b = dm.Batch(vols, views, tile)
     p = dm.Plan(b)
     p.set_launch(*shape)
@@ -368,6 +370,9 @@ def _batched_step(vols, views, tile, target, shape=(0, 1)):
             gd.zero_()
             gt.zero_()
             gs.zero_()
+        if fused:
+            p.step_l2(target)
+            return
         img = p.forward()
         torch.sub(img, target, out=grad)
         grad.mul_(2.0)
@@ -410,6 +415,31 @@ def _per_view_fp32_step(vols32, views, target):
     return body, grads
 
 
+def _per_view_fp32_fused_step(vols32, views, target):
+    """The FP32 one-launch-per-view form of the fused step: one plan per
+    view, one Plan.step_l2 launch each."""
+    plans, off = [], 0
+    for w in views:
+        b = dm.Batch([vols32[w.volume]], [dm.View(0, w.width, w.height, w.eye, w.d00, w.du, w.dv,
+                                                   w.background)], (16, 8))
+        p = dm.Plan(b)
+        plans.append((p, target[off:off + w.width * w.height].contiguous()))
+        off += w.width * w.height
+
+    def body():
+        for p, t in plans:
+            for gd, gt, gs in p.grads:
+                gd.zero_()
+                gt.zero_()
+                gs.zero_()
+            p.step_l2(t, image=False)
+
+    def release():
+        for p, _ in plans:
+            p.release()
+    return body, release
+
+
 def _targets(target_vols, views):
     """Target images of the L2 loss: every view rendered (FP32) from the
     second seeded volume of its slot."""
@@ -426,19 +456,28 @@ def _dm_measure(workload, vols, dens32, targets, views, steps, warmup, fp32_step
     # whole set (every k-th view), two repetitions each
     sub = views[::max(1, len(views) // 96)]
     launch = dm.autotune_launch(vols, [dm.View(w.volume, w.width, w.height, w.eye, w.d00, w.du,
-                                               w.dv, w.background) for w in sub], reps=2)
+                                               w.dv, w.background) for w in sub], reps=2,
+                                fused=True)
     tile = launch.tile
-    p, graph = _batched_step(vols, views, tile, target,
-                             (launch.blocks_per_sm, launch.tiles_per_fetch))
+    shape = (launch.blocks_per_sm, launch.tiles_per_fetch)
+    p, graph = _batched_step(vols, views, tile, target, shape)
     clocks = ClockSampler(torch.cuda.current_device())
     clocks.start()
     tb = _time_steps(graph.replay, steps, warmup, flush)
     clk = clocks.stop()
     nviews = len(views)
     vps = nviews / statistics.median(tb)
+    # the same batched step as two launches (forward, torch loss gradient,
+    # backward) in one graph, same tile and launch shape
+    p2, graph2 = _batched_step(vols, views, tile, target, shape, fused=False)
+    t2 = _time_steps(graph2.replay, max(1, min(steps, 5)), 1, flush)
+    p2.release()
+    del graph2
     # the FP32 one-view-per-launch forms on the same views, from the FP32
-    # fields the low-precision copies were made from: staged gradient
-    # accumulation (the library's default) and one atomic per term
+    # fields the low-precision copies were made from: forward + torch loss
+    # gradient + backward per view with staged gradient accumulation (the
+    # library's default) and with one atomic per term, and the fused step
+    # as one launch per view
     out = {}
     for name, plain in (("staged", False), ("plain", True)):
         v32 = [dm.VolumeInput(d, v.tf, v.scale, v.step, v.unit, v.value_range, plain=plain)
@@ -446,6 +485,12 @@ def _dm_measure(workload, vols, dens32, targets, views, steps, warmup, fp32_step
         body, _ = _per_view_fp32_step(v32, views, target)
         t32 = _time_steps(body, fp32_steps, 1, flush)
         out[name] = nviews / statistics.median(t32)
+    v32 = [dm.VolumeInput(d, v.tf, v.scale, v.step, v.unit, v.value_range)
+           for d, v in zip(dens32, vols)]
+    body, release = _per_view_fp32_fused_step(v32, views, target)
+    t32 = _time_steps(body, fp32_steps, 1, flush)
+    out["fused"] = nviews / statistics.median(t32)
+    release()
     # image and gradient error of the batched low-precision form against
     # the FP32 form (same views, same loss)
     v32 = [dm.VolumeInput(d, v.tf, v.scale, v.step, v.unit, v.value_range)
@@ -463,7 +508,7 @@ def _dm_measure(workload, vols, dens32, targets, views, steps, warmup, fp32_step
     peaks = measured_peaks()
     # compulsory bytes per step: the density read by the forward and again
     # by the backward, the FP32 density gradient written, the image written
-    # and read back
+    # and the target read
     comp = 2 * dens_bytes + sum(v.density.numel() * 4 for v in vols) + p.image.numel() * 4 * 2
     line = {
         "metric": "views/s (fwd+bwd)", "value": round(vps, 2), "unit": "views/s",
@@ -473,14 +518,18 @@ def _dm_measure(workload, vols, dens32, targets, views, steps, warmup, fp32_step
                    "blocks_per_sm": launch.blocks_per_sm,
                    "tiles_per_fetch": launch.tiles_per_fetch, "pixels": int(p.batch.pixels),
                    "views": nviews, "l2": "flushed between steps (256 MiB)"},
+        "step": "one launch: forward, L2 loss gradient and backward fused (Plan.step_l2)",
+        "batched_two_launch_views_per_s": round(nviews / statistics.median(t2), 2),
         "fp32_per_view_staged_views_per_s": round(out["staged"], 2),
         "fp32_per_view_plain_views_per_s": round(out["plain"], 2),
+        "fp32_per_view_fused_views_per_s": round(out["fused"], 2),
         "speedup_vs_fp32_per_view_staged": round(vps / out["staged"], 2),
         "speedup_vs_fp32_per_view_plain": round(vps / out["plain"], 2),
+        "speedup_vs_fp32_per_view_fused": round(vps / out["fused"], 2),
         "image_rms_vs_fp32": rms,
         "density_grad_rel_err_vs_fp32": grel,
-        "gpu_launches": 2 * steps,
-        "roofline": _roofline(comp, statistics.median(tb), peaks, kernel="k_dmForward+k_dmBackward",
+        "gpu_launches": steps,
+        "roofline": _roofline(comp, statistics.median(tb), peaks, kernel="k_dmBackward<T, fused>",
                               algorithmic_bytes_per_launch=comp,
                               note="compulsory bytes per step; the march is issue-bound"),
         "clocks": clk,
@@ -527,8 +576,8 @@ def measure_dm(local=0, steps=10, warmup=3, views=128, with_cpu=True):
 
 
 def cpu_dm(vol, view, rows=32):
-    """The FP64 oracle forward + adjoint on a band of rows of one 512x512
-    view, all host threads; views/s scaled from the band's pixels."""
+    """The FP64 oracle forward + adjoint on a band of rows of one view,
+    all host threads; views/s scaled from the band's pixels."""
     from oracle import oracle as O
 
     d = vol.density.float().cpu().numpy()
@@ -544,8 +593,8 @@ def cpu_dm(vol, view, rows=32):
     dt = time.perf_counter() - t0
     frac = rows / view.height
     return {"value": round(frac / dt, 4), "unit": "views/s", "cores": cores, "kind": "port",
-            "sample": f"FP64 forward + adjoint, rows {r0}-{r0 + rows} of one 512x512 view "
-                      f"({dt:.1f} s), scaled to the view"}
+            "sample": f"FP64 forward + adjoint, rows {r0}-{r0 + rows} of one "
+                      f"{view.width}x{view.height} view ({dt:.1f} s), scaled to the view"}
 
 
 def measure_batched(local=0, steps=3, warmup=3, with_cpu=True):
@@ -570,9 +619,46 @@ def measure_batched(local=0, steps=3, warmup=3, with_cpu=True):
             w = res_choices[int(rng.uniform(1, 0, 3)[0])]
             h = res_choices[int(rng.uniform(1, 0, 3)[0])]
             views.append(dm.look_at_view(i, vols[-1].dims, 2.0 * dirs[k], 45.0, w, h))
-    line, _ = _dm_measure(f"batched64_bf16_{len(views)}views_uneven", vols, dens32, tgts, views,
-                          steps, warmup, 1)
-    del vols, dens32, tgts
+    line, target = _dm_measure(f"batched64_bf16_{len(views)}views_uneven", vols, dens32, tgts,
+                               views, steps, warmup, 1)
+    del dens32, tgts
+    torch.cuda.empty_cache()
+    # end to end through the autograd API: the 64 BF16 densities and TFs
+    # copied from pinned host memory, forward + loss + backward over all
+    # views in one batch, the loss and every density gradient read back
+    hds = [v.density.cpu().pin_memory() for v in vols]
+    hts = [v.tf.cpu().pin_memory() for v in vols]
+    tile = tuple(line["config"]["tile"])
+    e2e = []
+    for i in range(2):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ins, ts = [], []
+        for hd, ht, v in zip(hds, hts, vols):
+            d = hd.to("cuda", non_blocking=True).requires_grad_()
+            tf = ht.to("cuda", non_blocking=True).requires_grad_()
+            ins.append(dm.VolumeInput(d, tf, v.scale, 0.5, 1.0, (0.0, 1.0)))
+            ts += [d, tf]
+        img = dm.render(dm.Batch(ins, views, tile))
+        loss = torch.sum((img - target) ** 2)
+        loss.backward()
+        lv = float(loss.item())
+        grads = [t.grad.cpu() for t in ts[0::2]]
+        t1 = time.perf_counter()
+        if i:
+            e2e.append(len(views) / (t1 - t0))
+        del ins, ts, img, loss
+    line["e2e"] = {"value": round(statistics.median(e2e), 2), "unit": "views/s",
+                   "h2d_bytes_per_step": int(sum(h.numel() * 2 for h in hds)
+                                             + sum(h.numel() * 4 for h in hts)),
+                   "d2h_bytes_per_step": int(sum(g.numel() * g.element_size() for g in grads) + 4),
+                   "includes": "64 densities + TFs uploaded, forward, loss, backward through the "
+                               "autograd Function, loss and density-gradient read-back",
+                   "loss": lv}
+    if with_cpu:
+        v0 = next(w for w in views if w.volume == 0)
+        line["cpu_baseline"] = cpu_dm(vols[0], v0, rows=min(32, v0.height))
+    del vols, grads, hds, hts
     torch.cuda.empty_cache()
     return line
 

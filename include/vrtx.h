@@ -461,6 +461,23 @@ VRTX_API int vrtxDMPlanBackward(VRTXDMPlan plan,
     const float *state,
     const float *gradImage,
     void *stream);
+/* One training step of an L2 image loss in a single persistent launch:
+ * every pixel of every view is marched forward, its loss gradient
+ * 2 * lossScale * (pixel - target) is formed in registers, and the same
+ * thread runs the adjoint at once, adding into the plan's gradient buffers
+ * (as vrtxDMPlanBackward would with that gradImage). target: 3 floats per
+ * pixel, the plan's image layout. image (may be NULL) receives the pixels;
+ * loss (a device float, may be NULL) has lossScale * sum((pixel -
+ * target)^2) added to it. No per-pixel state is written and no loss kernel
+ * runs between the passes. No reference counterpart (VisRTX has no
+ * gradient path). Returns 0, or a negative code after reporting the
+ * error. */
+VRTX_API int vrtxDMPlanStepL2(VRTXDMPlan plan,
+    const float *target,
+    float lossScale,
+    float *image,
+    float *loss,
+    void *stream);
 /* The plan's launch shape: resident blocks per SM of both kernels (0: as
  * many as fit, the default) and work items each block takes from the queue
  * per atomic fetch (1..64 consecutive tiles, default 1). Results do not

@@ -108,6 +108,8 @@ SIGNATURES = {
                                       C.c_int, C.c_int, C.c_void_p]),
     "vrtxDMPlanForward": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "vrtxDMPlanBackward": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "vrtxDMPlanStepL2": (C.c_int, [C.c_void_p, C.c_void_p, C.c_float, C.c_void_p, C.c_void_p,
+                                   C.c_void_p]),
     "vrtxDMPlanSetLaunch": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     "vrtxDMPlanRelease": (None, [C.c_void_p]),
     "vrtxDMForwardNoAlloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_int,

@@ -26,8 +26,11 @@ CPP_SOURCES = ["device.cpp", "anari_shim.cpp"]
 # Translation units whose arithmetic decides ids, depth and colour: compiled
 # without implicit multiply-add contraction, so every operation rounds as
 # written (the CPU oracle is built the same way, -ffp-contract=off); fused
-# multiply-adds there are explicit fmaf calls.
-NO_FMAD = {"render.cu", "render_counting.cu", "render_volume.cu", "render_ao.cu", "scene.cu"}
+# multiply-adds there are explicit fmaf calls. The differentiable marcher
+# (dm.cu) is built the same way so that its forward kernel, its adjoint's
+# recomputation and the fused training step round every sample alike.
+NO_FMAD = {"render.cu", "render_counting.cu", "render_volume.cu", "render_ao.cu", "scene.cu",
+           "dm.cu"}
 
 
 def _nvcc() -> str:

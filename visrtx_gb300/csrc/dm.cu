@@ -41,7 +41,8 @@ struct DMVol
   const void *tf; // tfSize x RGBA, fp32 (float4) or fp16 / bf16 (4 x 16 bit)
   int tfType; // 0 fp32, 1 fp16, 2 bf16
   int tfSize;
-  float scale, step, ratio, lo, hi;
+  float scale, step, ratio, lo, hi, invRange;
+  int sx, sy, sz; // index strides to the +1 neighbour (0 on a 1-voxel axis)
   float *gD;
   float *gTF;
   float *gS;
@@ -75,39 +76,41 @@ __device__ __forceinline__ float ld<__nv_bfloat16>(const __nv_bfloat16 *p, size_
   return __bfloat162float(__ldg(p + i));
 }
 
+// a * s + b per component, one rounding each (the file is compiled
+// without implicit contraction, so every kernel rounds alike)
+__device__ __forceinline__ f3 fma3(float s, f3 a, f3 b)
+{
+  return mk3(fmaf(s, a.x, b.x), fmaf(s, a.y, b.y), fmaf(s, a.z, b.z));
+}
+
+// A trilinear cell: the index of its lowest corner and the fractions.
 struct Tri
 {
   size_t base;
-  int sx, sy, sz; // index strides to the +1 neighbour (0 on a 1-voxel axis)
   float fx, fy, fz;
 };
 
-__device__ __forceinline__ void axis(float p, int n, int &i0, int &step, float &f)
+__device__ __forceinline__ void axis(float p, int n, int &i0, float &f)
 {
   if (n < 2) {
     i0 = 0;
-    step = 0;
     f = 0.f;
     return;
   }
   const float c = fminf(fmaxf(p, 0.f), float(n - 1));
   i0 = min((int)floorf(c), n - 2);
-  step = 1;
   f = c - float(i0);
 }
 
 __device__ __forceinline__ Tri triSetup(const DMVol &v, f3 p)
 {
-  int ix, iy, iz, sx, sy, sz;
+  int ix, iy, iz;
   Tri t;
-  axis(p.x, v.dims[0], ix, sx, t.fx);
-  axis(p.y, v.dims[1], iy, sy, t.fy);
-  axis(p.z, v.dims[2], iz, sz, t.fz);
+  axis(p.x, v.dims[0], ix, t.fx);
+  axis(p.y, v.dims[1], iy, t.fy);
+  axis(p.z, v.dims[2], iz, t.fz);
   const size_t X = v.dims[0], XY = (size_t)v.dims[0] * v.dims[1];
   t.base = (size_t)iz * XY + (size_t)iy * X + ix;
-  t.sx = sx;
-  t.sy = sy * v.dims[0];
-  t.sz = (int)(sz * XY);
   return t;
 }
 
@@ -116,17 +119,17 @@ __device__ __forceinline__ float trilinear(const DMVol &v, const Tri &t)
 {
   const T *D = reinterpret_cast<const T *>(v.density);
   const size_t b = t.base;
-  const float c000 = ld(D, b), c100 = ld(D, b + t.sx);
-  const float c010 = ld(D, b + t.sy), c110 = ld(D, b + t.sy + t.sx);
-  const float c001 = ld(D, b + t.sz), c101 = ld(D, b + t.sz + t.sx);
-  const float c011 = ld(D, b + t.sz + t.sy), c111 = ld(D, b + t.sz + t.sy + t.sx);
-  const float c00 = c000 + t.fx * (c100 - c000);
-  const float c10 = c010 + t.fx * (c110 - c010);
-  const float c01 = c001 + t.fx * (c101 - c001);
-  const float c11 = c011 + t.fx * (c111 - c011);
-  const float c0 = c00 + t.fy * (c10 - c00);
-  const float c1 = c01 + t.fy * (c11 - c01);
-  return c0 + t.fz * (c1 - c0);
+  const float c000 = ld(D, b), c100 = ld(D, b + v.sx);
+  const float c010 = ld(D, b + v.sy), c110 = ld(D, b + v.sy + v.sx);
+  const float c001 = ld(D, b + v.sz), c101 = ld(D, b + v.sz + v.sx);
+  const float c011 = ld(D, b + v.sz + v.sy), c111 = ld(D, b + v.sz + v.sy + v.sx);
+  const float c00 = fmaf(t.fx, c100 - c000, c000);
+  const float c10 = fmaf(t.fx, c110 - c010, c010);
+  const float c01 = fmaf(t.fx, c101 - c001, c001);
+  const float c11 = fmaf(t.fx, c111 - c011, c011);
+  const float c0 = fmaf(t.fy, c10 - c00, c00);
+  const float c1 = fmaf(t.fy, c11 - c01, c01);
+  return fmaf(t.fz, c1 - c0, c0);
 }
 
 // One TF entry in fp32 whatever the storage type (uniform per volume).
@@ -149,6 +152,7 @@ __device__ __forceinline__ float4 tfEntry(const DMVol &v, int i)
 struct Classified
 {
   float4 c; // rgb + raw TF alpha
+  float4 ea, eb; // the two TF entries interpolated
   int i0;
   float f;
   float dxds; // d(x)/d(s), 0 where the value range clamps
@@ -157,18 +161,18 @@ struct Classified
 __device__ __forceinline__ Classified classify(const DMVol &v, float s)
 {
   Classified r;
-  const float range = v.hi - v.lo;
-  float u = (s - v.lo) / range;
-  r.dxds = (u > 0.f && u < 1.f) ? float(v.tfSize - 1) / range : 0.f;
+  float u = (s - v.lo) * v.invRange;
+  r.dxds = (u > 0.f && u < 1.f) ? float(v.tfSize - 1) * v.invRange : 0.f;
   u = fminf(fmaxf(u, 0.f), 1.f);
   const float x = u * float(v.tfSize - 1);
   r.i0 = min((int)floorf(x), v.tfSize - 2);
   r.f = x - float(r.i0);
-  const float4 a = tfEntry(v, r.i0), b = tfEntry(v, r.i0 + 1);
-  r.c = make_float4(a.x + r.f * (b.x - a.x),
-      a.y + r.f * (b.y - a.y),
-      a.z + r.f * (b.z - a.z),
-      a.w + r.f * (b.w - a.w));
+  r.ea = tfEntry(v, r.i0);
+  r.eb = tfEntry(v, r.i0 + 1);
+  r.c = make_float4(fmaf(r.f, r.eb.x - r.ea.x, r.ea.x),
+      fmaf(r.f, r.eb.y - r.ea.y, r.ea.y),
+      fmaf(r.f, r.eb.z - r.ea.z, r.ea.z),
+      fmaf(r.f, r.eb.w - r.ea.w, r.ea.w));
   return r;
 }
 
@@ -199,7 +203,49 @@ __device__ __forceinline__ int findView(const DMViewG *views, int n, unsigned it
 
 __device__ __forceinline__ f3 viewRay(const DMViewG &vw, int px, int py)
 {
-  return normalize(vw.d00 + (float(px) + 0.5f) * vw.du + (float(py) + 0.5f) * vw.dv);
+  return normalize(fma3(float(py) + 0.5f, vw.dv, fma3(float(px) + 0.5f, vw.du, vw.d00)));
+}
+
+// One ray's forward march: premultiplied colour (background not added),
+// final log-transmittance and sample count.
+template <typename T>
+__device__ __forceinline__ void forwardRay(
+    const DMVol &v, f3 eye, f3 d, f3 &C, float &logT, int &k)
+{
+  C = mk3(0.f, 0.f, 0.f);
+  logT = 0.f;
+  k = 0;
+  float comp = 0.f, t0, t1;
+  if (!rayBox(eye, d, v.dims, t0, t1))
+    return;
+  while (k < kMaxSamples) {
+    const float t = fmaf(float(k) + 0.5f, v.step, t0);
+    if (t > t1)
+      break;
+    const f3 p = fma3(t, d, eye);
+    const float s = trilinear<T>(v, triSetup(v, p));
+    const Classified cl = classify(v, s);
+    const float alpha = fminf(cl.c.w * v.scale, kAlphaMax);
+    const float sigma = v.ratio * log1pf(-alpha);
+    const float T0 = __expf(logT);
+    const float a = -expm1f(sigma);
+    C = fma3(T0 * a, mk3(cl.c.x, cl.c.y, cl.c.z), C);
+    // Kahan: logT += sigma
+    const float y = sigma - comp;
+    const float nt = logT + y;
+    comp = (nt - logT) - y;
+    logT = nt;
+    k++;
+    if (logT < kLogTStop)
+      break;
+  }
+}
+
+// The pixel value: marched colour plus the background seen through T_end.
+__device__ __forceinline__ f3 pixelValue(f3 C, float logT, f3 bg)
+{
+  const float Tend = __expf(logT);
+  return fma3(Tend, bg, C);
 }
 
 template <typename T>
@@ -239,39 +285,15 @@ __global__ void __launch_bounds__(256) k_dmForward(const DMVol *vols,
     DMVol v = vols[vw.vol];
     if (v.scalePtr)
       v.scale = __ldg(v.scalePtr);
-    const f3 d = viewRay(vw, px, py);
-    float t0, t1;
-    f3 C = mk3(0.f, 0.f, 0.f);
-    float logT = 0.f, comp = 0.f;
-    int k = 0;
-    if (rayBox(vw.eye, d, v.dims, t0, t1)) {
-      while (k < kMaxSamples) {
-        const float t = t0 + (float(k) + 0.5f) * v.step;
-        if (t > t1)
-          break;
-        const f3 p = vw.eye + t * d;
-        const float s = trilinear<T>(v, triSetup(v, p));
-        const Classified cl = classify(v, s);
-        const float alpha = fminf(cl.c.w * v.scale, kAlphaMax);
-        const float sigma = v.ratio * log1pf(-alpha);
-        const float T0 = __expf(logT);
-        const float a = -expm1f(sigma);
-        C += (T0 * a) * mk3(cl.c.x, cl.c.y, cl.c.z);
-        // Kahan: logT += sigma
-        const float y = sigma - comp;
-        const float nt = logT + y;
-        comp = (nt - logT) - y;
-        logT = nt;
-        k++;
-        if (logT < kLogTStop)
-          break;
-      }
-    }
-    const float Tend = __expf(logT);
+    f3 C;
+    float logT;
+    int k;
+    forwardRay<T>(v, vw.eye, viewRay(vw, px, py), C, logT, k);
+    const f3 img = pixelValue(C, logT, vw.bg);
     const size_t pix = (size_t)vw.pixOff + (size_t)py * vw.w + px;
-    image[3 * pix + 0] = C.x + Tend * vw.bg.x;
-    image[3 * pix + 1] = C.y + Tend * vw.bg.y;
-    image[3 * pix + 2] = C.z + Tend * vw.bg.z;
+    image[3 * pix + 0] = img.x;
+    image[3 * pix + 1] = img.y;
+    image[3 * pix + 2] = img.z;
     state[2 * pix + 0] = logT;
     state[2 * pix + 1] = __int_as_float(k);
   }
@@ -324,15 +346,16 @@ __device__ __forceinline__ void redPair(float *p, float a, float b, int dx, bool
 // (y, z) rows go out as one 16-byte vector reduction each when the pair
 // sits inside an aligned float4 (`vec`: the gradient array is 16-byte
 // aligned), else as scalar atomics.
-__device__ __forceinline__ void flushCell(float *G, const Tri &c, float acc[8], bool vec)
+__device__ __forceinline__ void flushCell(
+    const DMVol &v, size_t base, float acc[8], bool vec)
 {
-  if (c.base == ~size_t(0))
+  if (base == ~size_t(0))
     return;
-  float *g = G + c.base;
-  redPair(g, acc[0], acc[1], c.sx, vec);
-  redPair(g + c.sy, acc[2], acc[3], c.sx, vec);
-  redPair(g + c.sz, acc[4], acc[5], c.sx, vec);
-  redPair(g + c.sz + c.sy, acc[6], acc[7], c.sx, vec);
+  float *g = v.gD + base;
+  redPair(g, acc[0], acc[1], v.sx, vec);
+  redPair(g + v.sy, acc[2], acc[3], v.sx, vec);
+  redPair(g + v.sz, acc[4], acc[5], v.sx, vec);
+  redPair(g + v.sz + v.sy, acc[6], acc[7], v.sx, vec);
 #pragma unroll
   for (int q = 0; q < 8; q++)
     acc[q] = 0.f;
@@ -386,6 +409,64 @@ __device__ __forceinline__ void flushTF(float4 *wTF, int seg, float acc[8])
     acc[q] = 0.f;
 }
 
+// 1: a run that moves to a neighbouring TF segment keeps the entry the two
+// segments share staged (measured 28.0 ms against 31.0 ms for committing
+// both entries at every change, backward of 32 views of 512^2 at 256^3;
+// shared-memory float atomics instead of match.any groups measured 36.6 ms
+// staged and 62.1 ms per term).
+#ifndef VRTX_DM_TF_SLIDE
+#define VRTX_DM_TF_SLIDE 1
+#endif
+
+// Moves a lane's TF staging (the terms of entries seg and seg + 1) to the
+// segment `to`. When `to` is a neighbour the shared entry stays staged and
+// only the other entry is committed, so a ray crossing segments one by one
+// commits one entry per crossing instead of two.
+__device__ __forceinline__ void slideTF(float4 *wTF, int &seg, float acc[8], int to)
+{
+#if VRTX_DM_TF_SLIDE
+  const unsigned mask = __activemask();
+  int e0 = -1, e1 = -2;
+  float4 v0 = make_float4(0.f, 0.f, 0.f, 0.f), v1 = v0;
+  if (seg >= 0) {
+    if (to == seg + 1) {
+      e0 = seg;
+      v0 = make_float4(acc[0], acc[1], acc[2], acc[3]);
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        acc[q] = acc[q + 4];
+        acc[q + 4] = 0.f;
+      }
+    } else if (to == seg - 1) {
+      e0 = seg + 1;
+      v0 = make_float4(acc[4], acc[5], acc[6], acc[7]);
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        acc[q + 4] = acc[q];
+        acc[q] = 0.f;
+      }
+    } else {
+      e0 = seg;
+      v0 = make_float4(acc[0], acc[1], acc[2], acc[3]);
+      e1 = seg + 1;
+      v1 = make_float4(acc[4], acc[5], acc[6], acc[7]);
+#pragma unroll
+      for (int q = 0; q < 8; q++)
+        acc[q] = 0.f;
+    }
+  }
+  addEntry(wTF, e0, v0, mask);
+  __syncwarp(mask);
+  if (__any_sync(mask, e1 >= 0)) {
+    addEntry(wTF, e1, v1, mask);
+    __syncwarp(mask);
+  }
+#else
+  flushTF(wTF, seg, acc);
+#endif
+  seg = to;
+}
+
 // Commits a block's TF gradient (the sum of its warps' shared-memory
 // copies; one vector reduction per entry when gTF is 16-byte aligned) and
 // its opacity-scale gradient (block reduction, one atomic). All threads of
@@ -436,7 +517,165 @@ __device__ __forceinline__ void commitBlockGrads(
 #define VRTX_DM_BWD_MIN_BLOCKS 3
 #endif
 
+// Per-thread gradient staging of the backward march: the trilinear cell and
+// the TF segment the ray is in, with the terms accumulated there since it
+// entered them.
+struct Stage
+{
+  size_t cell; // lowest-corner index of the staged trilinear cell
+  float dacc[8];
+  int tfSeg;
+  float tacc[8];
+};
+
+__device__ __forceinline__ void stageReset(Stage &st)
+{
+  st.cell = ~size_t(0);
+  st.tfSeg = -1;
+#pragma unroll
+  for (int q = 0; q < 8; q++) {
+    st.dacc[q] = 0.f;
+    st.tacc[q] = 0.f;
+  }
+}
+
+// Commits what a work item left staged. Every lane of the warp calls it.
+__device__ __forceinline__ void stageFlush(
+    const DMVol &v, bool plain, bool vecD, float4 *wTF, Stage &st)
+{
+  if (plain)
+    return;
+  if (v.gTF)
+    flushTF(wTF, st.tfSeg, st.tacc);
+  if (v.gD)
+    flushCell(v, st.cell, st.dacc, vecD);
+}
+
+// One ray's adjoint: walks its K samples in reverse from the end state
+// (log T_end) with the pixel's loss gradient g, adding the density and TF
+// terms to the staging (or straight to memory when `plain`) and the
+// opacity-scale term to gScale.
 template <typename T>
+__device__ __forceinline__ void backwardRay(const DMVol &v,
+    f3 eye,
+    f3 d,
+    f3 bg,
+    int K,
+    float logT,
+    f3 g,
+    bool plain,
+    bool vecD,
+    float4 *wTF,
+    Stage &st,
+    float &gScale)
+{
+  float t0 = 0.f, t1 = 0.f;
+  if (K <= 0 || !rayBox(eye, d, v.dims, t0, t1))
+    return;
+  float Tnext = __expf(logT);
+  f3 S = Tnext * bg;
+  float comp = 0.f;
+  for (int k = K - 1; k >= 0; k--) {
+    const float t = fmaf(float(k) + 0.5f, v.step, t0);
+    const f3 p = fma3(t, d, eye);
+    const Tri tr = triSetup(v, p);
+    const float s = trilinear<T>(v, tr);
+    const Classified cl = classify(v, s);
+    const float araw = cl.c.w * v.scale;
+    const float alpha = fminf(araw, kAlphaMax);
+    const float sigma = v.ratio * log1pf(-alpha);
+    // Kahan: logT -= sigma
+    const float y = -sigma - comp;
+    const float nt = logT + y;
+    comp = (nt - logT) - y;
+    logT = nt;
+    const float Tk = __expf(logT);
+    const float a = -expm1f(sigma);
+    const float w = Tk * a;
+    const f3 c = mk3(cl.c.x, cl.c.y, cl.c.z);
+    const f3 dc = w * g;
+    const f3 r = fma3(-Tnext, c, S);
+    const float dSigma = fmaf(g.z, r.z, fmaf(g.y, r.y, g.x * r.x));
+    S = fma3(w, c, S);
+    Tnext = Tk;
+    // d sigma / d alpha = -ratio / (1 - alpha), with 1 - alpha >= 1e-3
+    const float dAlpha =
+        araw < kAlphaMax ? dSigma * __fdividef(-v.ratio, 1.f - alpha) : 0.f;
+    const float dA = dAlpha * v.scale;
+    gScale = fmaf(dAlpha, cl.c.w, gScale);
+    const float f0 = 1.f - cl.f, f1 = cl.f;
+    if (v.gTF) {
+      if (plain) {
+        float *e0 = reinterpret_cast<float *>(wTF + cl.i0);
+        atomicAdd(e0 + 0, f0 * dc.x);
+        atomicAdd(e0 + 1, f0 * dc.y);
+        atomicAdd(e0 + 2, f0 * dc.z);
+        atomicAdd(e0 + 3, f0 * dA);
+        atomicAdd(e0 + 4, f1 * dc.x);
+        atomicAdd(e0 + 5, f1 * dc.y);
+        atomicAdd(e0 + 6, f1 * dc.z);
+        atomicAdd(e0 + 7, f1 * dA);
+      } else {
+        if (cl.i0 != st.tfSeg)
+          slideTF(wTF, st.tfSeg, st.tacc, cl.i0);
+        st.tacc[0] = fmaf(f0, dc.x, st.tacc[0]);
+        st.tacc[1] = fmaf(f0, dc.y, st.tacc[1]);
+        st.tacc[2] = fmaf(f0, dc.z, st.tacc[2]);
+        st.tacc[3] = fmaf(f0, dA, st.tacc[3]);
+        st.tacc[4] = fmaf(f1, dc.x, st.tacc[4]);
+        st.tacc[5] = fmaf(f1, dc.y, st.tacc[5]);
+        st.tacc[6] = fmaf(f1, dc.z, st.tacc[6]);
+        st.tacc[7] = fmaf(f1, dA, st.tacc[7]);
+      }
+    }
+    if (v.gD && cl.dxds != 0.f) {
+      const float dval = fmaf(dA, cl.eb.w - cl.ea.w,
+          fmaf(dc.z, cl.eb.z - cl.ea.z, fmaf(dc.y, cl.eb.y - cl.ea.y, dc.x * (cl.eb.x - cl.ea.x))));
+      const float ds = dval * cl.dxds;
+      if (ds != 0.f) {
+        const float gx0 = 1.f - tr.fx, gy0 = 1.f - tr.fy, gz0 = 1.f - tr.fz;
+        const float wt[8] = {gx0 * gy0 * gz0,
+            tr.fx * gy0 * gz0,
+            gx0 * tr.fy * gz0,
+            tr.fx * tr.fy * gz0,
+            gx0 * gy0 * tr.fz,
+            tr.fx * gy0 * tr.fz,
+            gx0 * tr.fy * tr.fz,
+            tr.fx * tr.fy * tr.fz};
+        if (plain) {
+          float *G = v.gD + tr.base;
+          atomicAdd(G, ds * wt[0]);
+          atomicAdd(G + v.sx, ds * wt[1]);
+          atomicAdd(G + v.sy, ds * wt[2]);
+          atomicAdd(G + v.sy + v.sx, ds * wt[3]);
+          atomicAdd(G + v.sz, ds * wt[4]);
+          atomicAdd(G + v.sz + v.sx, ds * wt[5]);
+          atomicAdd(G + v.sz + v.sy, ds * wt[6]);
+          atomicAdd(G + v.sz + v.sy + v.sx, ds * wt[7]);
+        } else {
+          // consecutive samples mostly stay in one trilinear cell:
+          // accumulate there and commit when the ray leaves it
+          if (tr.base != st.cell) {
+            flushCell(v, st.cell, st.dacc, vecD);
+            st.cell = tr.base;
+          }
+#pragma unroll
+          for (int q = 0; q < 8; q++)
+            st.dacc[q] = fmaf(ds, wt[q], st.dacc[q]);
+        }
+      }
+    }
+  }
+}
+
+// The backward pass (FUSED false): each pixel's end state and loss gradient
+// come from memory (the forward's state, the caller's gradImage).
+// The training step (FUSED true): each pixel is marched forward first, its
+// L2 loss gradient lossGrad * (pixel - target) formed in registers, and the
+// same thread then runs the adjoint, so one launch does forward, loss and
+// backward; `image` (optional) receives the pixels and `loss` (optional)
+// has lossScale * sum((pixel - target)^2) added to it.
+template <typename T, bool FUSED>
 __global__ void __launch_bounds__(256, VRTX_DM_BWD_MIN_BLOCKS) k_dmBackward(const DMVol *vols,
     const DMViewG *views,
     int numViews,
@@ -447,7 +686,12 @@ __global__ void __launch_bounds__(256, VRTX_DM_BWD_MIN_BLOCKS) k_dmBackward(cons
     unsigned fetch,
     int tfMax,
     const float *state,
-    const float *gradImage)
+    const float *gradImage,
+    const float *target,
+    float lossGrad,
+    float lossScale,
+    float *image,
+    float *loss)
 {
   // TF gradient of one volume: one copy of tfStride float4 entries per warp
   extern __shared__ float4 sTF[];
@@ -460,6 +704,7 @@ __global__ void __launch_bounds__(256, VRTX_DM_BWD_MIN_BLOCKS) k_dmBackward(cons
   // committed when the volume changes and at exit.
   int curVol = -1;
   float gScale = 0.f;
+  float lossAcc = 0.f;
   // work items come from the queue `fetch` consecutive tiles at a time
   unsigned next = 0, left = 0;
   while (true) {
@@ -496,123 +741,42 @@ __global__ void __launch_bounds__(256, VRTX_DM_BWD_MIN_BLOCKS) k_dmBackward(cons
     const int py = (int)(tile / vw.tilesX) * tileH + (int)threadIdx.x / tileW;
     const bool plain = (v.flags & VRTX_DM_PLAIN) != 0;
     const bool vecD = (reinterpret_cast<uintptr_t>(v.gD) & 15u) == 0;
-    // run-length gradient caches (one trilinear cell, one TF segment)
-    Tri cell;
-    cell.base = ~size_t(0);
-    float dacc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-    int tfSeg = -1;
-    float tacc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    Stage st;
+    stageReset(st);
     if (px < vw.w && py < vw.h) {
       const size_t pix = (size_t)vw.pixOff + (size_t)py * vw.w + px;
-      const int K = __float_as_int(state[2 * pix + 1]);
-      float logT = state[2 * pix + 0];
-      const f3 g = mk3(gradImage[3 * pix], gradImage[3 * pix + 1], gradImage[3 * pix + 2]);
       const f3 d = viewRay(vw, px, py);
-      float t0 = 0.f, t1 = 0.f;
-      if (K > 0 && rayBox(vw.eye, d, v.dims, t0, t1)) {
-        float Tnext = __expf(logT);
-        f3 S = Tnext * vw.bg;
-        float comp = 0.f;
-        for (int k = K - 1; k >= 0; k--) {
-          const float t = t0 + (float(k) + 0.5f) * v.step;
-          const f3 p = vw.eye + t * d;
-          const Tri tr = triSetup(v, p);
-          const float s = trilinear<T>(v, tr);
-          const Classified cl = classify(v, s);
-          const float araw = cl.c.w * v.scale;
-          const float alpha = fminf(araw, kAlphaMax);
-          const float sigma = v.ratio * log1pf(-alpha);
-          // Kahan: logT -= sigma
-          const float y = -sigma - comp;
-          const float nt = logT + y;
-          comp = (nt - logT) - y;
-          logT = nt;
-          const float Tk = __expf(logT);
-          const float a = -expm1f(sigma);
-          const float w = Tk * a;
-          const f3 c = mk3(cl.c.x, cl.c.y, cl.c.z);
-          const f3 dc = w * g;
-          const float dSigma = dot(g, S - Tnext * c);
-          S += w * c;
-          Tnext = Tk;
-          const float dAlpha =
-              araw < kAlphaMax ? dSigma * (-v.ratio / (1.f - alpha)) : 0.f;
-          const float dA = dAlpha * v.scale;
-          gScale += dAlpha * cl.c.w;
-          const float f0 = 1.f - cl.f, f1 = cl.f;
-          if (v.gTF) {
-            if (plain) {
-              float *e0 = reinterpret_cast<float *>(wTF + cl.i0);
-              atomicAdd(e0 + 0, f0 * dc.x);
-              atomicAdd(e0 + 1, f0 * dc.y);
-              atomicAdd(e0 + 2, f0 * dc.z);
-              atomicAdd(e0 + 3, f0 * dA);
-              atomicAdd(e0 + 4, f1 * dc.x);
-              atomicAdd(e0 + 5, f1 * dc.y);
-              atomicAdd(e0 + 6, f1 * dc.z);
-              atomicAdd(e0 + 7, f1 * dA);
-            } else {
-              if (cl.i0 != tfSeg) {
-                flushTF(wTF, tfSeg, tacc);
-                tfSeg = cl.i0;
-              }
-              tacc[0] += f0 * dc.x;
-              tacc[1] += f0 * dc.y;
-              tacc[2] += f0 * dc.z;
-              tacc[3] += f0 * dA;
-              tacc[4] += f1 * dc.x;
-              tacc[5] += f1 * dc.y;
-              tacc[6] += f1 * dc.z;
-              tacc[7] += f1 * dA;
-            }
-          }
-          if (v.gD && cl.dxds != 0.f) {
-            const float4 ea = tfEntry(v, cl.i0), eb = tfEntry(v, cl.i0 + 1);
-            const float dval = dc.x * (eb.x - ea.x) + dc.y * (eb.y - ea.y)
-                + dc.z * (eb.z - ea.z) + dA * (eb.w - ea.w);
-            const float ds = dval * cl.dxds;
-            if (ds != 0.f) {
-              const float gx0 = 1.f - tr.fx, gy0 = 1.f - tr.fy, gz0 = 1.f - tr.fz;
-              const float wt[8] = {gx0 * gy0 * gz0,
-                  tr.fx * gy0 * gz0,
-                  gx0 * tr.fy * gz0,
-                  tr.fx * tr.fy * gz0,
-                  gx0 * gy0 * tr.fz,
-                  tr.fx * gy0 * tr.fz,
-                  gx0 * tr.fy * tr.fz,
-                  tr.fx * tr.fy * tr.fz};
-              if (plain) {
-                float *G = v.gD + tr.base;
-                atomicAdd(G, ds * wt[0]);
-                atomicAdd(G + tr.sx, ds * wt[1]);
-                atomicAdd(G + tr.sy, ds * wt[2]);
-                atomicAdd(G + tr.sy + tr.sx, ds * wt[3]);
-                atomicAdd(G + tr.sz, ds * wt[4]);
-                atomicAdd(G + tr.sz + tr.sx, ds * wt[5]);
-                atomicAdd(G + tr.sz + tr.sy, ds * wt[6]);
-                atomicAdd(G + tr.sz + tr.sy + tr.sx, ds * wt[7]);
-              } else {
-                // consecutive samples mostly stay in one trilinear cell:
-                // accumulate there and commit when the ray leaves it
-                if (tr.base != cell.base) {
-                  flushCell(v.gD, cell, dacc, vecD);
-                  cell = tr;
-                }
-#pragma unroll
-                for (int q = 0; q < 8; q++)
-                  dacc[q] += ds * wt[q];
-              }
-            }
-          }
+      int K;
+      float logT;
+      f3 g;
+      if (FUSED) {
+        f3 C;
+        forwardRay<T>(v, vw.eye, d, C, logT, K);
+        const f3 img = pixelValue(C, logT, vw.bg);
+        if (image) {
+          image[3 * pix + 0] = img.x;
+          image[3 * pix + 1] = img.y;
+          image[3 * pix + 2] = img.z;
         }
+        const f3 diff = mk3(img.x - __ldg(target + 3 * pix),
+            img.y - __ldg(target + 3 * pix + 1),
+            img.z - __ldg(target + 3 * pix + 2));
+        lossAcc += diff.x * diff.x + diff.y * diff.y + diff.z * diff.z;
+        g = lossGrad * diff;
+      } else {
+        K = __float_as_int(state[2 * pix + 1]);
+        logT = state[2 * pix + 0];
+        g = mk3(gradImage[3 * pix], gradImage[3 * pix + 1], gradImage[3 * pix + 2]);
       }
+      backwardRay<T>(v, vw.eye, d, vw.bg, K, logT, g, plain, vecD, wTF, st, gScale);
     }
-    if (!plain) {
-      if (v.gTF)
-        flushTF(wTF, tfSeg, tacc);
-      if (v.gD)
-        flushCell(v.gD, cell, dacc, vecD);
-    }
+    stageFlush(v, plain, vecD, wTF, st);
+  }
+  if (FUSED && loss) {
+    for (int o = 16; o > 0; o >>= 1)
+      lossAcc += __shfl_xor_sync(0xffffffffu, lossAcc, o);
+    if ((threadIdx.x & 31) == 0 && lossAcc != 0.f)
+      atomicAdd(loss, lossScale * lossAcc);
   }
 }
 
@@ -699,6 +863,10 @@ int layout(const VRTXDMVolume *volumes,
     o.ratio = v.step / v.unitDistance;
     o.lo = v.valueLo;
     o.hi = v.valueHi;
+    o.invRange = 1.f / (v.valueHi - v.valueLo);
+    o.sx = v.dims[0] > 1 ? 1 : 0;
+    o.sy = v.dims[1] > 1 ? v.dims[0] : 0;
+    o.sz = v.dims[2] > 1 ? v.dims[0] * v.dims[1] : 0;
     o.gD = v.gradDensity;
     o.gTF = v.gradTf;
     o.gS = v.gradOpacityScale;
@@ -778,8 +946,18 @@ cudaError_t launchForward(const Layout &L, uint8_t *block, float *image, float *
   return cudaGetLastError();
 }
 
-cudaError_t launchBackward(const Layout &L, uint8_t *block, const float *state,
-    const float *gradImage, cudaStream_t s)
+// The adjoint over a descriptor block already on the device: the backward
+// pass (state, gradImage) or, with `target`, the fused training step.
+struct AdjointArgs
+{
+  const float *state = nullptr, *gradImage = nullptr;
+  const float *target = nullptr;
+  float lossGrad = 0.f, lossScale = 0.f;
+  float *image = nullptr, *loss = nullptr;
+};
+
+template <typename T, bool FUSED>
+void launchAdjointT(const Layout &L, uint8_t *block, const AdjointArgs &a, cudaStream_t s)
 {
   unsigned *counter = reinterpret_cast<unsigned *>(block);
   const DMVol *vols = reinterpret_cast<const DMVol *>(block + L.offVols);
@@ -788,21 +966,49 @@ cudaError_t launchBackward(const Layout &L, uint8_t *block, const float *state,
   const int threads = L.tileW * L.tileH;
   // one float4 TF-gradient copy per warp
   const size_t smem = sizeof(float4) * (size_t)(threads / 32) * L.maxTf;
+  const void *k = (const void *)k_dmBackward<T, FUSED>;
+  k_dmBackward<T, FUSED><<<gridFor(k, threads, smem, L.blocksPerSM), threads, smem, s>>>(vols,
+      views,
+      L.numViews,
+      L.numItems,
+      counter,
+      L.tileW,
+      L.tileH,
+      L.fetch,
+      L.maxTf,
+      a.state,
+      a.gradImage,
+      a.target,
+      a.lossGrad,
+      a.lossScale,
+      a.image,
+      a.loss);
+}
+
+template <bool FUSED>
+cudaError_t launchAdjoint(const Layout &L, uint8_t *block, const AdjointArgs &a, cudaStream_t s)
+{
   switch (L.type) {
   case VRTX_FLOAT16:
-    k_dmBackward<__half><<<gridFor((const void *)k_dmBackward<__half>, threads, smem, L.blocksPerSM), threads, smem, s>>>(
-        vols, views, L.numViews, L.numItems, counter, L.tileW, L.tileH, L.fetch, L.maxTf, state, gradImage);
+    launchAdjointT<__half, FUSED>(L, block, a, s);
     break;
   case VRTX_BFLOAT16:
-    k_dmBackward<__nv_bfloat16><<<gridFor((const void *)k_dmBackward<__nv_bfloat16>, threads, smem, L.blocksPerSM), threads, smem, s>>>(
-        vols, views, L.numViews, L.numItems, counter, L.tileW, L.tileH, L.fetch, L.maxTf, state, gradImage);
+    launchAdjointT<__nv_bfloat16, FUSED>(L, block, a, s);
     break;
   default:
-    k_dmBackward<float><<<gridFor((const void *)k_dmBackward<float>, threads, smem, L.blocksPerSM), threads, smem, s>>>(
-        vols, views, L.numViews, L.numItems, counter, L.tileW, L.tileH, L.fetch, L.maxTf, state, gradImage);
+    launchAdjointT<float, FUSED>(L, block, a, s);
     break;
   }
   return cudaGetLastError();
+}
+
+cudaError_t launchBackward(const Layout &L, uint8_t *block, const float *state,
+    const float *gradImage, cudaStream_t s)
+{
+  AdjointArgs a;
+  a.state = state;
+  a.gradImage = gradImage;
+  return launchAdjoint<false>(L, block, a, s);
 }
 
 // Stream-ordered device copy of a layout (freed by the caller).
@@ -947,6 +1153,28 @@ VRTX_API int vrtxDMPlanBackward(
     return -1;
   const cudaError_t e =
       launchBackward(plan->L, plan->block, state, gradImage, (cudaStream_t)stream);
+  return e == cudaSuccess ? 0 : fail(plan->dev, cudaGetErrorString(e), -8);
+}
+
+VRTX_API int vrtxDMPlanStepL2(VRTXDMPlan plan,
+    const float *target,
+    float lossScale,
+    float *image,
+    float *loss,
+    void *stream)
+{
+  if (!plan || !target)
+    return plan ? fail(plan->dev, "vrtxDMPlanStepL2: target is required", -1) : -1;
+  if (!(lossScale == lossScale) || lossScale == INFINITY || lossScale == -INFINITY)
+    return fail(plan->dev, "vrtxDMPlanStepL2: lossScale must be finite", -2);
+  AdjointArgs a;
+  a.target = target;
+  a.lossScale = lossScale;
+  a.lossGrad = 2.f * lossScale;
+  a.image = image;
+  a.loss = loss;
+  launchAdjoint<true>(plan->L, plan->block, a, (cudaStream_t)stream);
+  const cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? 0 : fail(plan->dev, cudaGetErrorString(e), -8);
 }
 

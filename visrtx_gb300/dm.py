@@ -11,8 +11,10 @@ computes the rendering.
 
 Many views of many volumes render in one launch; Plan keeps the launch
 descriptors on the device so forward + backward can be captured in a CUDA
-graph; autotune() picks the tile shape, autotune_launch() the tile shape,
-resident blocks per SM and tiles per queue fetch.
+graph, and Plan.step_l2 runs forward, L2 loss gradient and backward of a
+training step in one persistent launch; autotune() picks the tile shape,
+autotune_launch() the tile shape, resident blocks per SM and tiles per
+queue fetch.
 """
 from __future__ import annotations
 
@@ -255,6 +257,23 @@ class Plan:
                "vrtxDMPlanBackward")
         return self.grads
 
+    def step_l2(self, target: torch.Tensor, loss_scale: float = 1.0, image: bool = True,
+                loss: torch.Tensor | None = None):
+        """One fused training step of the L2 loss loss_scale * sum((image -
+        target)^2): forward, loss gradient and backward in one launch,
+        gradients added into self.grads. Writes self.image when `image`;
+        adds the loss into `loss` (a one-element fp32 CUDA tensor) when
+        given."""
+        if target.dtype != torch.float32 or not target.is_contiguous() \
+                or target.numel() != self.image.numel():
+            raise ValueError("target must be a contiguous fp32 tensor shaped like the image")
+        _check(L.load().vrtxDMPlanStepL2(
+            C.c_void_p(self.h), C.c_void_p(target.data_ptr()), float(loss_scale),
+            C.c_void_p(self.image.data_ptr()) if image else None,
+            C.c_void_p(loss.data_ptr()) if loss is not None else None, _stream()),
+            "vrtxDMPlanStepL2")
+        return self.grads
+
     def set_launch(self, blocks_per_sm: int = 0, tiles_per_fetch: int = 1):
         """Launch shape of both kernels: resident blocks per SM (0: as many
         as fit) and tiles taken from the work queue per fetch."""
@@ -281,17 +300,23 @@ class Launch:
     tiles_per_fetch: int = 1
 
 
-def _time_plan(volumes, views, tile, shape, reps):
+def _time_plan(volumes, views, tile, shape, reps, fused=False):
     p = Plan(Batch(volumes, views, tile))
     p.set_launch(*shape)
     g = torch.ones_like(p.image)
-    p.forward()
-    p.backward(g)
+
+    def step():
+        if fused:
+            p.step_l2(g, image=False)
+        else:
+            p.forward()
+            p.backward(g)
+
+    step()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(reps):
-        p.forward()
-        p.backward(g)
+        step()
     torch.cuda.synchronize()
     p.release()
     return (time.perf_counter() - t0) / reps
@@ -299,12 +324,13 @@ def _time_plan(volumes, views, tile, shape, reps):
 
 def autotune_launch(volumes: list[VolumeInput], views: list[View], tiles=TILES,
                     blocks_per_sm=BLOCKS_PER_SM, tiles_per_fetch=TILES_PER_FETCH, reps: int = 2,
-                    cache: str | None = None) -> Launch:
-    """Times forward + backward of this workload over the tile shapes, then,
-    for the fastest tile, over resident blocks per SM x tiles per queue
-    fetch; returns the fastest Launch. Cached in a JSON file keyed by the
+                    cache: str | None = None, fused: bool = False) -> Launch:
+    """Times forward + backward of this workload (with `fused`, the one-launch
+    L2 training step, Plan.step_l2) over the tile shapes, then, for the
+    fastest tile, over resident blocks per SM x tiles per queue fetch;
+    returns the fastest Launch. Cached in a JSON file keyed by the
     workload's shape when `cache` is given."""
-    key = "launch:" + json.dumps({"dtype": str(volumes[0].density.dtype),
+    key = "launch:" + json.dumps({"fused": fused, "dtype": str(volumes[0].density.dtype),
                                   "dims": sorted({v.dims for v in volumes}),
                                   "res": sorted({(w.width, w.height) for w in views}),
                                   "views": len(views), "volumes": len(volumes)}, default=list)
@@ -315,9 +341,9 @@ def autotune_launch(volumes: list[VolumeInput], views: list[View], tiles=TILES,
         if key in table:
             e = table[key]
             return Launch(tuple(e["tile"]), e["blocks_per_sm"], e["tiles_per_fetch"])
-    times = {tile: _time_plan(volumes, views, tile, (0, 1), reps) for tile in tiles}
+    times = {tile: _time_plan(volumes, views, tile, (0, 1), reps, fused) for tile in tiles}
     tile = min(times, key=times.get)
-    shapes = {(b, f): _time_plan(volumes, views, tile, (b, f), reps)
+    shapes = {(b, f): _time_plan(volumes, views, tile, (b, f), reps, fused)
               for b in blocks_per_sm for f in tiles_per_fetch}
     b, f = min(shapes, key=shapes.get)
     best = Launch(tuple(tile), b, f)
