@@ -344,6 +344,20 @@ def test_step_l2_matches_forward_loss_backward():
         assert abs(float(loss) - ref_loss) <= 1e-5 * abs(ref_loss)
     with pytest.raises(ValueError):
         p.step_l2(target[:-1])
+    # through the C ABI: a missing target or a non-finite loss scale is
+    # refused with an error code, and nothing is launched
+    import ctypes as C
+    from visrtx_gb300 import _lib as L
+
+    g0 = p.grads[0][0].clone()
+    lib = L.load()
+    assert lib.vrtxDMPlanStepL2(C.c_void_p(p.h), None, 1.0, None, None, None) == -1
+    assert lib.vrtxDMPlanStepL2(C.c_void_p(p.h), C.c_void_p(target.data_ptr()), float("nan"),
+                                None, None, None) == -2
+    assert lib.vrtxDMPlanStepL2(None, C.c_void_p(target.data_ptr()), 1.0, None, None,
+                                None) == -1
+    torch.cuda.synchronize()
+    assert torch.equal(p.grads[0][0], g0)
     p.release()
 
 
