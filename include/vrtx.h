@@ -335,6 +335,26 @@ VRTX_API void vrtxUnmapFrame(VRTXDevice d, VRTXFrame f, const char *channel);
 VRTX_API uint64_t vrtxDebugCopyAccel(
     VRTXDevice d, VRTXObject world, int kind, void *dst, uint64_t capacity);
 
+/* The 256-entry RGBA table a transferFunction1D volume's colour / opacity
+ * arrays discretise to at commit, computed on the host (no device, no GPU):
+ * the colour array (numColor >= 2 entries of colorComponents = 3 or 4
+ * floats) and the opacity array (numOpacity >= 2 floats) spread uniformly
+ * over [valueLo, valueHi]; either may be NULL, the uniform colour (4 floats)
+ * / opacity then stand in, as the volume's "color" / "opacity" values do.
+ * Writes 256 x 4 floats to out. Replaces
+ * TransferFunction1D::discritizeTFData (TransferFunction1D.cpp:101-150) as a
+ * separate entry for checking. Returns 0, or -1 for invalid arguments. */
+VRTX_API int vrtxDebugDiscretizeTF(const float *color,
+    int numColor,
+    int colorComponents,
+    const float *opacity,
+    int numOpacity,
+    float valueLo,
+    float valueHi,
+    const float *uniformColor,
+    float uniformOpacity,
+    float *out);
+
 /* Sorts n (key, value) pairs held in host memory with the BVH builder's
  * Morton sort (a stable LSD radix sort by the low `bits` bits of the keys,
  * bits in 1..64), through device copies on the device's stream. Replaces

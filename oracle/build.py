@@ -3,11 +3,16 @@ and, where the reference tree is present, oracle/_ref/libnvdbref.so.
 
 The reference's renderer cannot be compiled here (its device path needs
 OptiX headers fetched at configure time and the ANARI-SDK, neither present);
-see oracle.h for the parity status. The NanoVDB library it vendors
-(external/nanovdb, header-only) does compile with g++ alone: ref_nvdb.cpp
-drives its grid builder, sampler and validator, compiled from the headers
-where they lie under the reference tree, with the output only in
-oracle/_ref/. The GPU machine has no reference tree and never builds it.
+see oracle.h for the parity status. Two parts of it do compile with g++
+alone, from the headers where they lie under the reference tree, with the
+output only in oracle/_ref/:
+  * the NanoVDB library it vendors (external/nanovdb, header-only):
+    ref_nvdb.cpp drives its grid builder, sampler and validator
+    (libnvdbref.so);
+  * its transfer-function helpers (devices/rtx/utility/colorMapHelpers.h
+    with gpu/gpu_math.h and the vendored glm): ref_tf.cpp repeats
+    TransferFunction1D::discritizeTFData's calls (libtfref.so).
+The GPU machine has no reference tree and never builds them.
 """
 from __future__ import annotations
 
@@ -40,27 +45,41 @@ def build() -> str:
 REF_TREE = os.environ.get("VISRTX_REFERENCE_TREE", "/root/reference")
 REF_OUT = os.path.join(HERE, "_ref")
 REF_LIB = os.path.join(REF_OUT, "libnvdbref.so")
+REF_TF_LIB = os.path.join(REF_OUT, "libtfref.so")
 
 
-def build_ref(tree: str | None = None) -> str | None:
-    """oracle/_ref/libnvdbref.so from ref_nvdb.cpp and the reference's vendored
-    NanoVDB headers under `tree` (default REF_TREE); None when the reference
-    tree is absent."""
-    inc = os.path.join(tree or REF_TREE, "external", "nanovdb", "include")
-    if not os.path.isdir(inc):
-        return None
-    src = os.path.join(HERE, "ref_nvdb.cpp")
+def _compile_ref(src: str, out: str, incs: list[str]) -> str:
     os.makedirs(REF_OUT, exist_ok=True)
-    if os.path.exists(REF_LIB) and os.path.getmtime(REF_LIB) >= os.path.getmtime(src):
-        return REF_LIB
-    tmp = REF_LIB + ".tmp"
-    cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off",
-           "-I", inc, "-o", tmp, src, "-lpthread"]
+    if os.path.exists(out) and os.path.getmtime(out) >= os.path.getmtime(src):
+        return out
+    tmp = out + ".tmp"
+    cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off"]
+    for i in incs:
+        cmd += ["-I", i]
+    cmd += ["-o", tmp, src, "-lpthread"]
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
         raise RuntimeError("oracle/_ref build failed:\n" + res.stdout + res.stderr)
-    os.replace(tmp, REF_LIB)
-    return REF_LIB
+    os.replace(tmp, out)
+    return out
+
+
+def build_ref(tree: str | None = None) -> str | None:
+    """oracle/_ref/libnvdbref.so (ref_nvdb.cpp over the reference's vendored
+    NanoVDB headers) and oracle/_ref/libtfref.so (ref_tf.cpp over its
+    transfer-function helpers) from the reference tree `tree` (default
+    REF_TREE); returns the NanoVDB harness's path, or None when the
+    reference tree is absent."""
+    root = tree or REF_TREE
+    inc = os.path.join(root, "external", "nanovdb", "include")
+    if not os.path.isdir(inc):
+        return None
+    lib = _compile_ref(os.path.join(HERE, "ref_nvdb.cpp"), REF_LIB, [inc])
+    rtx = os.path.join(root, "devices", "rtx")
+    glm = os.path.join(root, "external", "glm", "include")
+    if os.path.isfile(os.path.join(rtx, "utility", "colorMapHelpers.h")) and os.path.isdir(glm):
+        _compile_ref(os.path.join(HERE, "ref_tf.cpp"), REF_TF_LIB, [rtx, glm])
+    return lib
 
 
 if __name__ == "__main__":

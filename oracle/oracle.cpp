@@ -3060,7 +3060,7 @@ void orc_dpt_majorants(const OrcVolume *volume, int round, float *out)
 // TransferFunction1D::discritizeTFData (TransferFunction1D.cpp:101-150) with
 // generateLinearPositions / getInterpolatedValue (colorMapHelpers.h:43-73)
 void orc_discretize_tf(const float *color, int nc, int cc, const float *opacity, int no,
-    float lo, float hi, float uniformOpacity, float *out)
+    float lo, float hi, const float *uniformColor, float uniformOpacity, float *out)
 {
   auto positions = [&](int n) {
     std::vector<float> p(n);
@@ -3099,7 +3099,12 @@ void orc_discretize_tf(const float *color, int nc, int cc, const float *opacity,
     op = positions(no);
   for (int i = 0; i < 256; i++) {
     const float p = (float)i / 255.f;
+    // the volume's uniform colour (TransferFunction1D.cpp:50-54) where no
+    // colour array is set
     float c[4] = {1.f, 1.f, 1.f, 1.f};
+    if (uniformColor)
+      for (int k = 0; k < 4; k++)
+        c[k] = uniformColor[k];
     if (!cp.empty()) {
       float v[4] = {0, 0, 0, 1};
       interp(color, cc, cp, p, v);

@@ -264,7 +264,9 @@ int orc_render(const OrcScene *scene,
     int threads);
 
 /* TF discretisation of the reference (TransferFunction1D.cpp:101-150):
- * color (nc x 3 or 4 floats), opacity (no floats) -> 256 x RGBA. */
+ * color (nc x 3 or 4 floats), opacity (no floats) -> 256 x RGBA; where an
+ * array is absent the uniform colour (4 floats, NULL: white) / opacity
+ * stand in. */
 void orc_discretize_tf(const float *color,
     int nc,
     int colorComps,
@@ -272,6 +274,7 @@ void orc_discretize_tf(const float *color,
     int no,
     float valueLo,
     float valueHi,
+    const float *uniformColor4,
     float uniformOpacity,
     float *out256x4);
 

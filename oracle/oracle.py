@@ -191,15 +191,21 @@ def _rows(m4):
     return (C.c_float * 12)(*[float(m[r, c]) for r in range(3) for c in range(4)])
 
 
-def discretize_tf(color, opacity, value_range=(0.0, 1.0), uniform_opacity=1.0) -> np.ndarray:
+def discretize_tf(color, opacity, value_range=(0.0, 1.0), uniform_opacity=1.0,
+                  uniform_color=(1.0, 1.0, 1.0, 1.0)) -> np.ndarray:
+    """The reference's 256-entry TF table; uniform_color (3 or 4 floats, w 1
+    when 3) and uniform_opacity stand in for an absent array."""
     lib = load()
     out = np.zeros((256, 4), np.float32)
     c = None if color is None else np.ascontiguousarray(color, np.float32)
     o = None if opacity is None else np.ascontiguousarray(opacity, np.float32)
+    uc = np.ones(4, np.float32)
+    uc[:len(uniform_color)] = uniform_color
     lib.orc_discretize_tf(_ptr(c), C.c_int(0 if c is None else len(c)),
                           C.c_int(0 if c is None else c.shape[1]), _ptr(o),
                           C.c_int(0 if o is None else len(o)), C.c_float(value_range[0]),
-                          C.c_float(value_range[1]), C.c_float(uniform_opacity), _ptr(out))
+                          C.c_float(value_range[1]), _ptr(uc), C.c_float(uniform_opacity),
+                          _ptr(out))
     return out
 
 
@@ -376,7 +382,8 @@ def _pack_volume(v, o, keep, world_id):
     o.spacing = (C.c_float * 3)(*map(float, v.spacing))
     o.filterLinear = int(v.filter != "nearest")
     if v.color is not None or v.opacity is not None:
-        tf = discretize_tf(v.color, v.opacity, v.value_range, v.uniform_opacity)
+        tf = discretize_tf(v.color, v.opacity, v.value_range, v.uniform_opacity,
+                           v.uniform_color)
         keep.append(tf)
         o.tf = _ptr(tf)
     o.valueRange = (C.c_float * 2)(*map(float, v.value_range))

@@ -1,0 +1,63 @@
+// Test infrastructure: a harness around the reference's own transfer-function
+// helpers (devices/rtx/utility/colorMapHelpers.h: generateLinearPositions,
+// getInterpolatedValue, with gpu/gpu_math.h's box1 / position / contains and
+// the vendored glm), compiled from those headers where they lie into
+// oracle/_ref/libtfref.so by oracle/build.py, only where the reference tree
+// is present, and used only by tests/golden/make_tf_golden.py.
+//
+// tfref_discretize repeats the call sequence of
+// TransferFunction1D::discritizeTFData (TransferFunction1D.cpp:101-150): the
+// colour and opacity knots placed uniformly over the value range, each of
+// the tfDim entries sampled at p = i / (tfDim - 1), the entry (rgb, a * o)
+// with a = 1 for vec3 colours, and the uniform colour / opacity where an
+// array is absent. That file itself needs the ANARI-SDK and cannot be built
+// here; the arithmetic it calls is the helpers', compiled unchanged.
+#include "utility/colorMapHelpers.h"
+
+#include <vector>
+
+extern "C" void tfref_discretize(const float *color,
+    int numColor,
+    int colorComps,
+    const float *opacity,
+    int numOpacity,
+    float lo,
+    float hi,
+    const float *uniformColor,
+    float uniformOpacity,
+    int tfDim,
+    float *out)
+{
+  using namespace visrtx;
+  const box1 range(lo, hi);
+  std::vector<float> cPos, oPos;
+  Span<float> cPositions, oPositions;
+  if (color) {
+    cPos = generateLinearPositions((size_t)numColor, range);
+    cPositions = make_Span(cPos.data(), cPos.size());
+  }
+  if (opacity) {
+    oPos = generateLinearPositions((size_t)numOpacity, range);
+    oPositions = make_Span(oPos.data(), oPos.size());
+  }
+  for (int i = 0; i < tfDim; i++) {
+    const float p = float(i) / (tfDim - 1);
+    vec4 c(uniformColor[0], uniformColor[1], uniformColor[2], uniformColor[3]);
+    if (color) {
+      if (colorComps == 3)
+        c = vec4(getInterpolatedValue(
+                     reinterpret_cast<const vec3 *>(color), cPositions, range, p),
+            1.f);
+      else
+        c = getInterpolatedValue(
+            reinterpret_cast<const vec4 *>(color), cPositions, range, p);
+    }
+    const float o = opacity
+        ? getInterpolatedValue(opacity, oPositions, range, p)
+        : uniformOpacity;
+    out[4 * i + 0] = c.x;
+    out[4 * i + 1] = c.y;
+    out[4 * i + 2] = c.z;
+    out[4 * i + 3] = c.w * o;
+  }
+}

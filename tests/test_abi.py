@@ -163,3 +163,32 @@ def test_force_init_initialises_at_commit(built):
     else:
         assert any("no CUDA device" in m for m in dev.errors())
     dev.release()
+
+
+def test_library_tf_discretization_matches_reference(built):
+    """The library's TF discretisation (the host code a transferFunction1D
+    volume commits with, through vrtxDebugDiscretizeTF, no GPU involved)
+    equals bit for bit the tables the reference's own helpers computed
+    (tests/golden/tf_golden.npz); invalid arguments return -1."""
+    import numpy as np
+
+    from tests.test_oracle import tf_golden_cases
+    from visrtx_gb300 import _lib as L
+
+    lib = L.load()
+    for i, (c, o, vr, uc, uo, ref) in enumerate(tf_golden_cases()):
+        out = np.zeros((256, 4), np.float32)
+        uc = np.ascontiguousarray(uc, np.float32)
+        rc = lib.vrtxDebugDiscretizeTF(
+            c.ctypes.data if c is not None else None, 0 if c is None else len(c),
+            0 if c is None else c.shape[1], o.ctypes.data if o is not None else None,
+            0 if o is None else len(o), vr[0], vr[1], uc.ctypes.data, uo, out.ctypes.data)
+        assert rc == 0
+        assert np.array_equal(out, ref), (i, float(np.abs(out - ref).max()))
+    one = np.ones((1, 3), np.float32)
+    out = np.zeros((256, 4), np.float32)
+    uc = np.ones(4, np.float32)
+    assert lib.vrtxDebugDiscretizeTF(one.ctypes.data, 1, 3, None, 0, 0.0, 1.0, uc.ctypes.data,
+                                     1.0, out.ctypes.data) == -1
+    assert lib.vrtxDebugDiscretizeTF(None, 0, 0, None, 0, 0.0, 1.0, uc.ctypes.data, 1.0,
+                                     None) == -1

@@ -435,6 +435,21 @@ def test_volume_parity(device, rate):
     print(rep)
 
 
+def test_volume_uniform_colour_with_opacity_array(device):
+    """A transferFunction1D volume with an opacity array and no colour array
+    takes its uniform colour for every TF entry (TransferFunction1D.cpp:
+    50-54,101-150): GPU against the oracle at the colour bar."""
+    spec = small_volume()
+    spec.volumes[0].color = None
+    spec.volumes[0].uniform_color = (0.9, 0.4, 0.1)
+    g = render_gpu(device, spec)
+    r = render_oracle(spec)
+    rep = compare(g, r, color_tol=1)
+    print(rep)
+    c = g["color"]
+    assert c.std() > 0  # the volume is visible
+
+
 @pytest.mark.parametrize("renderer", ["raycast", "default"])
 def test_volume_dda_march_matches_plain_march(device, renderer):
     """A volume whose TF is transparent over its low values has empty

@@ -1,6 +1,7 @@
 """CPU checks of the oracle itself: known-answer vectors for Philox4x32-10
 (the SC'11 paper's algorithm), curand-style stream semantics, the TF
-discretisation, single-ray analytic hits, point and spot light shading, sRGB
+discretisation (pinned to the reference's own TF helpers), single-ray
+analytic hits, point and spot light shading, sRGB
 endpoints, and an FP64 central-difference check of the differentiable
 marcher's adjoint. GPU-dumped curand and texture outputs pin the RNG and
 filter emulation where fixtures exist (tests/golden/)."""
@@ -142,6 +143,34 @@ def test_tf_value_range_outside_knots():
                          (-2.0, 6.0), uniform_opacity=0.5)
     assert tf[0, 0] == 1.0 and tf[-1, 1] == 1.0
     assert np.allclose(tf[:, 3], 0.5)
+
+
+def tf_golden_cases():
+    """The cases of tests/golden/tf_golden.npz: knots, value range, uniform
+    colour and opacity, and the table the reference's own TF helpers
+    computed for them (tests/golden/make_tf_golden.py)."""
+    z = np.load(os.path.join(GOLDEN, "tf_golden.npz"))
+    out = []
+    for i in range(int(z["count"][0])):
+        out.append((z[f"c{i}_color"] if f"c{i}_color" in z else None,
+                    z[f"c{i}_opacity"] if f"c{i}_opacity" in z else None,
+                    tuple(float(x) for x in z[f"c{i}_range"]),
+                    z[f"c{i}_uniform_color"], float(z[f"c{i}_uniform_opacity"][0]),
+                    z[f"c{i}_table"]))
+    return out
+
+
+def test_tf_golden_reference_helpers():
+    """The oracle's TF discretisation equals, bit for bit, the tables the
+    reference's own helpers (colorMapHelpers.h, called as
+    TransferFunction1D.cpp:101-150 does) computed for 40 knot sets: vec3 and
+    vec4 colours, 2-17 knots, absent colour or opacity arrays (the uniform
+    values), offset, negative, narrow and wide value ranges."""
+    cases = tf_golden_cases()
+    assert len(cases) == 40
+    for i, (c, o, vr, uc, uo, ref) in enumerate(cases):
+        got = O.discretize_tf(c, o, vr, uo, uc)
+        assert np.array_equal(got, ref), (i, float(np.abs(got - ref).max()))
 
 
 def single_triangle_spec(renderer="raycast"):

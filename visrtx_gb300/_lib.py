@@ -95,6 +95,9 @@ SIGNATURES = {
     "vrtxDebugCopyAccel": (C.c_uint64, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p,
                                         C.c_uint64]),
     "vrtxWorldBuildMilliseconds": (C.c_float, [C.c_void_p, C.c_void_p]),
+    "vrtxDebugDiscretizeTF": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_int,
+                                        C.c_float, C.c_float, C.c_void_p, C.c_float,
+                                        C.c_void_p]),
     "vrtxDebugRadixSort": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_int]),
     "vrtxFrameKernelMilliseconds": (C.c_float, [C.c_void_p, C.c_void_p]),
     "vrtxFrameKernelLaunches": (C.c_int, [C.c_void_p, C.c_void_p]),

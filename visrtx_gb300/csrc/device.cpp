@@ -2053,48 +2053,76 @@ static void interpolated(const float *values,
     out[c] = values[k * nc + c];
 }
 
-// discritizeTFData (TransferFunction1D.cpp:101-150): 256 entries,
-// entry = (rgb, c.w * o)
+// discritizeTFData (TransferFunction1D.cpp:101-150): n entries sampled at
+// i / (n - 1), entry = (rgb, c.w * o); the colour array (nc = 3 or 4
+// components) or the opacity array may be absent (NULL), and the uniform
+// colour / opacity stand in for it.
+static void discretizeTF(const float *cvals,
+    int numColor,
+    int nc,
+    const float *ovals,
+    int numOpacity,
+    float lo,
+    float hi,
+    const float uniformColor[4],
+    float uniformOpacity,
+    int n,
+    float *out)
+{
+  std::vector<float> cpos, opos;
+  if (cvals)
+    cpos = linearPositions((size_t)numColor, lo, hi);
+  if (ovals)
+    opos = linearPositions((size_t)numOpacity, lo, hi);
+  for (int i = 0; i < n; i++) {
+    const float p = float(i) / float(n - 1);
+    float c[4] = {uniformColor[0], uniformColor[1], uniformColor[2], uniformColor[3]};
+    if (cvals) {
+      float v[4] = {0.f, 0.f, 0.f, 1.f};
+      interpolated(cvals, nc, cpos, lo, hi, p, v);
+      c[0] = v[0];
+      c[1] = v[1];
+      c[2] = v[2];
+      c[3] = nc == 4 ? v[3] : 1.f;
+    }
+    float o = uniformOpacity;
+    if (ovals)
+      interpolated(ovals, 1, opos, lo, hi, p, &o);
+    out[4 * i + 0] = c[0];
+    out[4 * i + 1] = c[1];
+    out[4 * i + 2] = c[2];
+    out[4 * i + 3] = c[3] * o;
+  }
+}
+
 void Volume::discretize()
 {
   const int N = 256;
   tf.assign(N * 4, 0.f);
-  const float lo = valueRange[0], hi = valueRange[1];
-  std::vector<float> cpos, opos;
   const float *cvals = nullptr;
   int cnc = 0;
   if (color && color->count() >= 2
       && (color->elemType == VRTX_FLOAT32_VEC3
           || color->elemType == VRTX_FLOAT32_VEC4)) {
-    cpos = linearPositions(color->count(), lo, hi);
     cvals = reinterpret_cast<const float *>(color->hostData());
     cnc = color->elemType == VRTX_FLOAT32_VEC3 ? 3 : 4;
   } else if (color)
     report(VRTX_SEVERITY_WARNING, "unusable tf1D color array type set");
   const float *ovals = nullptr;
-  if (opacity && opacity->count() >= 2 && opacity->elemType == VRTX_FLOAT32) {
-    opos = linearPositions(opacity->count(), lo, hi);
+  if (opacity && opacity->count() >= 2 && opacity->elemType == VRTX_FLOAT32)
     ovals = reinterpret_cast<const float *>(opacity->hostData());
-  }
-  for (int i = 0; i < N; i++) {
-    const float p = float(i) / float(N - 1);
-    float c[4] = {uniformColor.x, uniformColor.y, uniformColor.z, uniformColorW};
-    if (cvals) {
-      float v[4] = {0.f, 0.f, 0.f, 1.f};
-      interpolated(cvals, cnc, cpos, lo, hi, p, v);
-      c[0] = v[0];
-      c[1] = v[1];
-      c[2] = v[2];
-      c[3] = cnc == 4 ? v[3] : 1.f;
-    }
-    float o = uniformOpacity;
-    if (ovals)
-      interpolated(ovals, 1, opos, lo, hi, p, &o);
-    tf[4 * i + 0] = c[0];
-    tf[4 * i + 1] = c[1];
-    tf[4 * i + 2] = c[2];
-    tf[4 * i + 3] = c[3] * o;
-  }
+  const float uc[4] = {uniformColor.x, uniformColor.y, uniformColor.z, uniformColorW};
+  discretizeTF(cvals,
+      cvals ? (int)color->count() : 0,
+      cnc,
+      ovals,
+      ovals ? (int)opacity->count() : 0,
+      valueRange[0],
+      valueRange[1],
+      uc,
+      uniformOpacity,
+      N,
+      tf.data());
 }
 
 bool Volume::ensureBuilt()
@@ -3914,6 +3942,34 @@ VRTX_API const void *vrtxMapFrame(VRTXDevice d,
 }
 
 VRTX_API void vrtxUnmapFrame(VRTXDevice, VRTXFrame, const char *) {}
+
+VRTX_API int vrtxDebugDiscretizeTF(const float *color,
+    int numColor,
+    int colorComponents,
+    const float *opacity,
+    int numOpacity,
+    float valueLo,
+    float valueHi,
+    const float *uniformColor,
+    float uniformOpacity,
+    float *out)
+{
+  if (!out || !uniformColor || (color && (numColor < 2 || (colorComponents != 3 && colorComponents != 4)))
+      || (opacity && numOpacity < 2))
+    return -1;
+  discretizeTF(color,
+      numColor,
+      colorComponents,
+      opacity,
+      numOpacity,
+      valueLo,
+      valueHi,
+      uniformColor,
+      uniformOpacity,
+      256,
+      out);
+  return 0;
+}
 
 VRTX_API int vrtxDebugRadixSort(
     VRTXDevice d, uint64_t *keys, uint32_t *vals, uint32_t n, int bits)
