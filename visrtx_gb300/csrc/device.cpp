@@ -398,12 +398,20 @@ Array::Array(Device *d,
   refreshHandles();
 }
 
+void Array::settleHostReads()
+{
+  if (hostReadQueued && Object::dev->initOk)
+    cudaStreamSynchronize(Object::dev->stream);
+  hostReadQueued = false;
+}
+
 Array::~Array()
 {
+  settleHostReads();
   for (auto *h : handles)
     releaseObj(h);
   if (dptr && devBytes)
-    cudaFree(dptr);
+    cudaFreeAsync(dptr, Object::dev->stream);
   if (deleter && appMem)
     deleter(deleterPtr, appMem);
 }
@@ -426,12 +434,15 @@ const void *Array::deviceData()
     return nullptr;
   if (devStamp >= dataStamp && dptr)
     return dptr;
+  // stream-ordered from the device's pool (kept between frames): a scene
+  // rebuilt every frame reuses its buffers without cudaMalloc / cudaFree
+  // round trips, and a release does not synchronise the device
   if (devBytes < b) {
     if (dptr)
-      cudaFree(dptr);
+      cudaFreeAsync(dptr, Object::dev->stream);
     dptr = nullptr;
     devBytes = 0;
-    if (cudaMalloc(&dptr, b) != cudaSuccess) {
+    if (cudaMallocAsync(&dptr, b, Object::dev->stream) != cudaSuccess) {
       report(VRTX_SEVERITY_ERROR, "device allocation of %zu bytes failed", b);
       cudaGetLastError();
       return nullptr;
@@ -444,6 +455,8 @@ const void *Array::deviceData()
       b,
       appIsForeign ? cudaMemcpyDefault : cudaMemcpyHostToDevice,
       Object::dev->stream);
+  if (!appIsForeign && appMem)
+    hostReadQueued = true;
   devStamp = dataStamp;
   return dptr;
 }
@@ -466,6 +479,7 @@ void Array::privatize()
 {
   if (!appMem || deleter || appIsDevice || appIsForeign)
     return;
+  settleHostReads();
   owned.assign((const uint8_t *)appMem, (const uint8_t *)appMem + bytes());
   appMem = nullptr;
 }
@@ -1874,16 +1888,25 @@ bool SpatialField::ensureBuilt()
     cuArray = nullptr;
     return false;
   }
+  // host-resident voxels go straight into the texture array (no linear
+  // device copy); device and other-GPU arrays are copied from device memory
   cudaMemcpy3DParms cp{};
-  const void *src = data->deviceData();
+  const void *host = data->hostData();
+  const void *src = host ? host : data->deviceData();
+  if (!src) {
+    report(VRTX_SEVERITY_ERROR, "field data is not readable");
+    return false;
+  }
   cp.srcPtr = make_cudaPitchedPtr(const_cast<void *>(src),
       dims[0] * sizeOfType(et),
       dims[0],
       dims[1]);
   cp.dstArray = cuArray;
   cp.extent = make_cudaExtent(dims[0], dims[1], dims[2]);
-  cp.kind = cudaMemcpyDeviceToDevice;
+  cp.kind = host ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
   cudaMemcpy3DAsync(&cp, s);
+  if (host && data->appMem)
+    data->hostReadQueued = true;
   cudaResourceDesc rd{};
   rd.resType = cudaResourceTypeArray;
   rd.res.array.array = cuArray;

@@ -104,6 +104,11 @@ struct Array : Object
   size_t devBytes = 0;
   uint64_t dataStamp = 0;
   uint64_t devStamp = 0;
+  // an asynchronous copy reading the application's host memory has been
+  // queued on the device stream since the last synchronisation: the stream
+  // is synchronised before that memory is given back (privatisation,
+  // destruction)
+  bool hostReadQueued = false;
   std::vector<Object *> handles; // object arrays: retained elements
 
   Array(Device *d,
@@ -125,6 +130,8 @@ struct Array : Object
     return count() * sizeOfType(elemType);
   }
   const void *hostData() const;
+  // waits for queued copies that read the application's host memory
+  void settleHostReads();
   // device copy (uploads on first use after a data change)
   const void *deviceData();
   void *map();
