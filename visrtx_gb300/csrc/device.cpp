@@ -1009,7 +1009,15 @@ bool Sampler::ensureBuilt()
   const size_t n = (size_t)image->n[0] * image->n[1] * image->n[2];
   std::vector<float> staging(4 * n);
   std::vector<uint8_t> host(image->bytes());
-  cudaMemcpy(host.data(), image->deviceData(), host.size(), cudaMemcpyDefault);
+  if (const void *h = image->hostData())
+    std::memcpy(host.data(), h, host.size());
+  else {
+    // device-resident or other-GPU images: the upload is stream-ordered on
+    // the device stream, which the synchronous read-back must follow
+    const void *d = image->deviceData();
+    cudaStreamSynchronize(Object::dev->stream);
+    cudaMemcpy(host.data(), d, host.size(), cudaMemcpyDefault);
+  }
   auto srgbToLinear = [](float c) {
     return c <= 0.04045f ? c / 12.92f : std::pow((c + 0.055f) / 1.055f, 2.4f);
   };
@@ -1200,9 +1208,11 @@ bool Light::ensureBuilt()
   std::vector<float> rgb((size_t)W * H * 3);
   if (const void *h = radiance->hostData())
     std::memcpy(rgb.data(), h, rgb.size() * sizeof(float));
-  else
-    cudaMemcpy(rgb.data(), radiance->deviceData(), rgb.size() * sizeof(float),
-        cudaMemcpyDeviceToHost);
+  else {
+    const void *d = radiance->deviceData();
+    cudaStreamSynchronize(Object::dev->stream);
+    cudaMemcpy(rgb.data(), d, rgb.size() * sizeof(float), cudaMemcpyDeviceToHost);
+  }
   std::vector<float> lum((size_t)W * H), rowSums(H), cdf((size_t)H + (size_t)W * H);
   for (int y = 0; y < H; y++) {
     const float sinTheta = std::sin(float(M_PI) * (float(y) + 0.5f) / float(H));
@@ -1696,9 +1706,10 @@ bool SpatialField::buildNanovdb()
   std::vector<uint8_t> host(size);
   if (const void *h = data->hostData())
     std::memcpy(host.data(), h, size);
-  else if (const void *d = data->deviceData())
+  else if (const void *d = data->deviceData()) {
+    cudaStreamSynchronize(s);
     cudaMemcpy(host.data(), d, size, cudaMemcpyDeviceToHost);
-  else
+  } else
     return false;
   std::string why;
   std::vector<int32_t> origins;
@@ -2747,8 +2758,11 @@ bool Renderer::ensureBackground()
   std::vector<uint8_t> raw(bgImage->bytes());
   if (const void *h = bgImage->hostData())
     std::memcpy(raw.data(), h, raw.size());
-  else
-    cudaMemcpy(raw.data(), bgImage->deviceData(), raw.size(), cudaMemcpyDeviceToHost);
+  else {
+    const void *d = bgImage->deviceData();
+    cudaStreamSynchronize(Object::dev->stream);
+    cudaMemcpy(raw.data(), d, raw.size(), cudaMemcpyDeviceToHost);
+  }
   std::vector<uint8_t> rgba(W * H * 4);
   for (size_t i = 0; i < W * H; i++) {
     for (int c = 0; c < 4; c++) {
@@ -2861,22 +2875,26 @@ Frame::~Frame()
         cudaEventDestroy(e);
     for (cudaEvent_t e : traceEvents)
       cudaEventDestroy(e);
+    cudaStream_t s = Object::dev->stream;
     if (workCounter)
-      cudaFree(workCounter);
+      cudaFreeAsync(workCounter, s);
     if (errorFlag)
-      cudaFree(errorFlag);
+      cudaFreeAsync(errorFlag, s);
     if (stats)
-      cudaFree(stats);
+      cudaFreeAsync(stats, s);
     if (scratch)
       cudaFree(scratch);
   }
 }
 
+// Frame buffers and counters come from the device's stream-ordered pool:
+// a frame created, resized or released every step reuses pool memory
+// instead of cudaMalloc / cudaFree round trips that synchronise the device.
 void Frame::freeBuffers()
 {
   for (void *&b : buffers) {
     if (b)
-      cudaFree(b);
+      cudaFreeAsync(b, Object::dev->stream);
     b = nullptr;
   }
   fb = FramebufferGPU{};
@@ -2923,10 +2941,11 @@ void Frame::commit()
   const bool cDepth = depthType == VRTX_FLOAT32 || cPrim || cObj || cInst;
   if (cDepth)
     depthType = VRTX_FLOAT32;
+  cudaStream_t s = Object::dev->stream;
   auto alloc = [&](int slot, size_t bytes) -> void * {
     if (!bytes)
       return nullptr;
-    if (cudaMalloc(&buffers[slot], bytes) != cudaSuccess) {
+    if (cudaMallocAsync(&buffers[slot], bytes, s) != cudaSuccess) {
       cudaGetLastError();
       report(VRTX_SEVERITY_ERROR, "frame buffer allocation failed");
       buffers[slot] = nullptr;
@@ -2953,16 +2972,24 @@ void Frame::commit()
     alloc(8, n * 12);
   if (wantNormal)
     alloc(9, n * 12);
-  if (!workCounter)
-    cudaMalloc(&workCounter, 16);
+  if (!workCounter && cudaMallocAsync(&workCounter, 16, s) != cudaSuccess) {
+    cudaGetLastError();
+    workCounter = nullptr;
+  }
   // error flags collect over the frames rendered since the last commit
-  if (!errorFlag)
-    cudaMalloc(&errorFlag, 16);
+  if (!errorFlag && cudaMallocAsync(&errorFlag, 16, s) != cudaSuccess) {
+    cudaGetLastError();
+    errorFlag = nullptr;
+  }
   if (errorFlag)
-    cudaMemset(errorFlag, 0, 16);
+    cudaMemsetAsync(errorFlag, 0, 16, s);
   if (!stats) {
-    cudaMalloc(&stats, 16 * sizeof(unsigned long long));
-    cudaMemset(stats, 0, 16 * sizeof(unsigned long long));
+    if (cudaMallocAsync(&stats, 16 * sizeof(unsigned long long), s) == cudaSuccess)
+      cudaMemsetAsync(stats, 0, 16 * sizeof(unsigned long long), s);
+    else {
+      cudaGetLastError();
+      stats = nullptr;
+    }
   }
   countTraversal = get<int32_t>("vrtx.countTraversal", VRTX_BOOL, 0) != 0;
   // the traversal loop bound per ray; lowering it makes the device guard
@@ -3208,6 +3235,10 @@ const void *Frame::map(
     *pixelType = VRTX_UNKNOWN;
     return nullptr;
   }
+  // the buffers are stream-ordered allocations of the device stream: the
+  // mapped pointer (or the host copy) is only handed out once the stream has
+  // reached them, so any stream or the host may read it
+  cudaStreamSynchronize(Object::dev->stream);
   if (cuda)
     ret = src;
   else {
