@@ -154,7 +154,11 @@ VRTX_API VRTXDevice vrtxNewDevice(
  * VisRTXDevice::deviceSetParameter / deviceCommitParameters
  * (VisRTXDevice.cpp:460-478). "cudaDevice" set after the device has
  * initialised is reported as a warning and ignored; with "forceInit" the
- * commit initialises CUDA instead of the first object creation. */
+ * commit initialises CUDA instead of the first object creation. This
+ * library also takes "vrtx.failFrameAllocations" (INT32 N, no reference
+ * counterpart): the next N frame allocations fail on the host, without a
+ * CUDA call, to test error handling; such a frame reports the failure, is
+ * skipped by render, and allocates again at its next commit. */
 VRTX_API void vrtxDeviceSetParameter(
     VRTXDevice d, const char *name, int type, const void *mem);
 VRTX_API void vrtxDeviceCommitParameters(VRTXDevice d);

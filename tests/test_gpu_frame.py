@@ -135,3 +135,40 @@ def test_traversal_step_limit_sets_error_flag(device, renderer):
     assert f.stats()["error_flags"] == 0
     assert np.array_equal(f.map("channel.color"), clean)
     assert not device.errors()
+
+
+def test_frame_allocation_failure_is_reported_and_recovers(device):
+    """Host-side fault injection: the device is told to fail the next frame
+    allocation ("vrtx.failFrameAllocations"; no CUDA call is made for it).
+    The commit reports the failure and frees what it had allocated, render
+    skips the frame with an error (no kernel touches a missing buffer), map
+    returns nothing; the next commit allocates again and the frame equals
+    one that never failed. Nothing faults the GPU."""
+    import numpy as np
+
+    dev = device
+    spec = S.soup_spec(n=2000, width=64, height=48, renderer="raycast")
+    ref = render_gpu(dev, spec)
+    assert not dev.errors()
+    # the first 1, 3 or 9 allocations of the frame's commit fail: the
+    # accumulation buffer alone, the first channels too, or every buffer and
+    # counter (6 buffers, then 3 counters)
+    for fail_at in (1, 3, 9):
+        k = C.c_int32(fail_at)
+        dev.lib.vrtxDeviceSetParameter(dev.h, b"vrtx.failFrameAllocations", L.INT32, C.byref(k))
+        frame, world, keep = S.build_on_device(dev, spec)
+        # the frame commit used up the injected failures
+        assert any("frame buffer allocation failed" in m for m in dev.errors())
+        frame.render()
+        frame.wait()
+        assert any("invalid frame buffers" in m for m in dev.errors())
+        assert frame.map("channel.color") is None
+        dev.messages.clear()
+        frame.commit()
+        frame.render()
+        frame.wait()
+        assert not dev.errors(), dev.errors()
+        for ch in ("color", "depth", "primitiveId", "objectId", "instanceId"):
+            assert np.array_equal(frame.map("channel." + ch), ref[ch]), (fail_at, ch)
+        for o in keep + [frame]:
+            o.release()

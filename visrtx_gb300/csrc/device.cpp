@@ -2887,6 +2887,25 @@ Frame::~Frame()
   }
 }
 
+// A frame allocation from the device's pool, or a failure the device was
+// told to inject ("vrtx.failFrameAllocations": host-side fault injection for
+// tests of the error path; no CUDA call is made for an injected failure).
+cudaError_t Frame::frameAlloc(void **p, size_t bytes, cudaStream_t s)
+{
+  std::atomic<int> &inject = Object::dev->failFrameAllocs;
+  for (int k = inject.load(); k > 0;)
+    if (inject.compare_exchange_weak(k, k - 1)) {
+      *p = nullptr;
+      return cudaErrorMemoryAllocation;
+    }
+  const cudaError_t e = cudaMallocAsync(p, bytes, s);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    *p = nullptr;
+  }
+  return e;
+}
+
 // Frame buffers and counters come from the device's stream-ordered pool:
 // a frame created, resized or released every step reuses pool memory
 // instead of cudaMalloc / cudaFree round trips that synchronise the device.
@@ -2942,13 +2961,15 @@ void Frame::commit()
   if (cDepth)
     depthType = VRTX_FLOAT32;
   cudaStream_t s = Object::dev->stream;
+  // one failed allocation leaves the frame without buffers: render then
+  // skips it with an error instead of writing to a missing buffer
+  bool failed = false;
   auto alloc = [&](int slot, size_t bytes) -> void * {
     if (!bytes)
       return nullptr;
-    if (cudaMallocAsync(&buffers[slot], bytes, s) != cudaSuccess) {
-      cudaGetLastError();
-      report(VRTX_SEVERITY_ERROR, "frame buffer allocation failed");
+    if (frameAlloc(&buffers[slot], bytes, s) != cudaSuccess) {
       buffers[slot] = nullptr;
+      failed = true;
     }
     return buffers[slot];
   };
@@ -2972,24 +2993,28 @@ void Frame::commit()
     alloc(8, n * 12);
   if (wantNormal)
     alloc(9, n * 12);
-  if (!workCounter && cudaMallocAsync(&workCounter, 16, s) != cudaSuccess) {
-    cudaGetLastError();
+  if (!workCounter && frameAlloc((void **)&workCounter, 16, s) != cudaSuccess) {
     workCounter = nullptr;
+    failed = true;
   }
   // error flags collect over the frames rendered since the last commit
-  if (!errorFlag && cudaMallocAsync(&errorFlag, 16, s) != cudaSuccess) {
-    cudaGetLastError();
+  if (!errorFlag && frameAlloc((void **)&errorFlag, 16, s) != cudaSuccess) {
     errorFlag = nullptr;
+    failed = true;
   }
   if (errorFlag)
     cudaMemsetAsync(errorFlag, 0, 16, s);
   if (!stats) {
-    if (cudaMallocAsync(&stats, 16 * sizeof(unsigned long long), s) == cudaSuccess)
+    if (frameAlloc((void **)&stats, 16 * sizeof(unsigned long long), s) == cudaSuccess)
       cudaMemsetAsync(stats, 0, 16 * sizeof(unsigned long long), s);
     else {
-      cudaGetLastError();
       stats = nullptr;
+      failed = true;
     }
+  }
+  if (failed) {
+    report(VRTX_SEVERITY_ERROR, "frame buffer allocation failed");
+    freeBuffers();
   }
   countTraversal = get<int32_t>("vrtx.countTraversal", VRTX_BOOL, 0) != 0;
   // the traversal loop bound per ray; lowering it makes the device guard
@@ -3034,7 +3059,7 @@ void Frame::render()
     report(VRTX_SEVERITY_ERROR, "skipping render: no CUDA device");
     return;
   }
-  if (!isValid() || !fb.accum) {
+  if (!isValid() || !fb.accum || !workCounter || !errorFlag || !stats) {
     const char *why = !renderer ? "missing ANARIRenderer"
         : !camera                ? "missing ANARICamera"
         : !world                 ? "missing ANARIWorld"
@@ -3441,6 +3466,8 @@ VRTX_API void vrtxDeviceSetParameter(
     warnDeviceChange(dev);
   } else if (n == "forceInit" && type == VRTX_BOOL && mem)
     dev->forceInit = *(const int32_t *)mem != 0;
+  else if (n == "vrtx.failFrameAllocations" && type == VRTX_INT32 && mem)
+    dev->failFrameAllocs = std::max(0, *(const int32_t *)mem);
   else if (n == "statusCallback" && mem)
     D(d)->cb = *(const VRTXStatusCallback *)mem;
   else if (n == "statusCallbackUserData")

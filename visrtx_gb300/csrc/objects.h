@@ -434,6 +434,7 @@ struct Frame : Object
   void commit() override;
   bool isValid() const override;
   void freeBuffers();
+  cudaError_t frameAlloc(void **p, size_t bytes, cudaStream_t s);
   void render();
   void wait();
   bool ready();
@@ -467,6 +468,9 @@ struct Device
   std::atomic<bool> initOk{false};
   cudaStream_t stream = nullptr;
   int numSMs = 0;
+  // host-side fault injection: the next N frame allocations fail without a
+  // CUDA call ("vrtx.failFrameAllocations")
+  std::atomic<int> failFrameAllocs{0};
   std::atomic<uint64_t> lastChange{0};
   std::vector<Object *> live; // every object ever created and not destroyed
 
