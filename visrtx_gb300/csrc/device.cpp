@@ -2883,7 +2883,7 @@ Frame::~Frame()
     if (stats)
       cudaFreeAsync(stats, s);
     if (scratch)
-      cudaFree(scratch);
+      cudaFreeAsync(scratch, s);
   }
 }
 

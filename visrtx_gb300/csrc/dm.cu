@@ -19,6 +19,7 @@
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
+#include <cmath>
 #include <cstring>
 #include <mutex>
 #include <vector>
@@ -1165,7 +1166,7 @@ VRTX_API int vrtxDMPlanStepL2(VRTXDMPlan plan,
 {
   if (!plan || !target)
     return plan ? fail(plan->dev, "vrtxDMPlanStepL2: target is required", -1) : -1;
-  if (!(lossScale == lossScale) || lossScale == INFINITY || lossScale == -INFINITY)
+  if (!std::isfinite(lossScale))
     return fail(plan->dev, "vrtxDMPlanStepL2: lossScale must be finite", -2);
   AdjointArgs a;
   a.target = target;
@@ -1173,8 +1174,7 @@ VRTX_API int vrtxDMPlanStepL2(VRTXDMPlan plan,
   a.lossGrad = 2.f * lossScale;
   a.image = image;
   a.loss = loss;
-  launchAdjoint<true>(plan->L, plan->block, a, (cudaStream_t)stream);
-  const cudaError_t e = cudaGetLastError();
+  const cudaError_t e = launchAdjoint<true>(plan->L, plan->block, a, (cudaStream_t)stream);
   return e == cudaSuccess ? 0 : fail(plan->dev, cudaGetErrorString(e), -8);
 }
 
