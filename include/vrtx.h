@@ -359,6 +359,20 @@ VRTX_API int vrtxDebugDiscretizeTF(const float *color,
     float uniformOpacity,
     float *out);
 
+/* The frame's colour write (the end of every render kernel: the
+ * accumulation divided by frameID + 1 samples, inverse-tonemapped and
+ * packed as sRGB rgba8 for format 0 or linear rgba8 for format 1) applied
+ * on the device's GPU to n accumulated RGBA colours (4 floats each, host
+ * memory), packed into out (n uint32, host memory). Replaces
+ * writeOutputColor (gpu/gpu_util.h:370-389) as a separate entry for
+ * checking. Returns 0, or a negative code after reporting the error. */
+VRTX_API int vrtxDebugWriteColors(VRTXDevice d,
+    const float *accum,
+    uint32_t n,
+    int frameID,
+    int format,
+    uint32_t *out);
+
 /* Sorts n (key, value) pairs held in host memory with the BVH builder's
  * Morton sort (a stable LSD radix sort by the low `bits` bits of the keys,
  * bits in 1..64), through device copies on the device's stream. Replaces

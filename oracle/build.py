@@ -11,7 +11,10 @@ output only in oracle/_ref/:
     (libnvdbref.so);
   * its transfer-function helpers (devices/rtx/utility/colorMapHelpers.h
     with gpu/gpu_math.h and the vendored glm): ref_tf.cpp repeats
-    TransferFunction1D::discritizeTFData's calls (libtfref.so).
+    TransferFunction1D::discritizeTFData's calls (libtfref.so);
+  * the vendored glm's colour packing (glm::convertLinearToSRGB,
+    glm::packUnorm4x8): ref_glm.cpp repeats writeOutputColor's calls
+    (libglmref.so).
 The GPU machine has no reference tree and never builds them.
 """
 from __future__ import annotations
@@ -46,6 +49,7 @@ REF_TREE = os.environ.get("VISRTX_REFERENCE_TREE", "/root/reference")
 REF_OUT = os.path.join(HERE, "_ref")
 REF_LIB = os.path.join(REF_OUT, "libnvdbref.so")
 REF_TF_LIB = os.path.join(REF_OUT, "libtfref.so")
+REF_GLM_LIB = os.path.join(REF_OUT, "libglmref.so")
 
 
 def _compile_ref(src: str, out: str, incs: list[str]) -> str:
@@ -66,8 +70,9 @@ def _compile_ref(src: str, out: str, incs: list[str]) -> str:
 
 def build_ref(tree: str | None = None) -> str | None:
     """oracle/_ref/libnvdbref.so (ref_nvdb.cpp over the reference's vendored
-    NanoVDB headers) and oracle/_ref/libtfref.so (ref_tf.cpp over its
-    transfer-function helpers) from the reference tree `tree` (default
+    NanoVDB headers), oracle/_ref/libtfref.so (ref_tf.cpp over its
+    transfer-function helpers) and oracle/_ref/libglmref.so (ref_glm.cpp
+    over its vendored glm) from the reference tree `tree` (default
     REF_TREE); returns the NanoVDB harness's path, or None when the
     reference tree is absent."""
     root = tree or REF_TREE
@@ -79,6 +84,7 @@ def build_ref(tree: str | None = None) -> str | None:
     glm = os.path.join(root, "external", "glm", "include")
     if os.path.isfile(os.path.join(rtx, "utility", "colorMapHelpers.h")) and os.path.isdir(glm):
         _compile_ref(os.path.join(HERE, "ref_tf.cpp"), REF_TF_LIB, [rtx, glm])
+        _compile_ref(os.path.join(HERE, "ref_glm.cpp"), REF_GLM_LIB, [glm])
     return lib
 
 

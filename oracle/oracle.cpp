@@ -3050,6 +3050,18 @@ int orc_nvdb_sample(const uint8_t *grid, const float *xyz, int n, int fused, flo
   return 0;
 }
 
+// writeOutputColor (gpu/gpu_util.h:370-389) on n accumulated colours, as
+// the frame writes them (format 0 sRGB rgba8, 1 linear rgba8)
+void orc_write_colors(const float *accum, int n, int frameID, int format, uint32_t *out)
+{
+  OrcFrame F{};
+  F.frameID = frameID;
+  F.colorFormat = format;
+  F.color = out;
+  for (int i = 0; i < n; i++)
+    writeColor(F, accum + 4 * i, (size_t)i, 0);
+}
+
 void orc_dpt_majorants(const OrcVolume *volume, int round, float *out)
 {
   std::vector<float> m;

@@ -263,6 +263,11 @@ int orc_render(const OrcScene *scene,
     int texRound,
     int threads);
 
+/* The frame's colour write (gpu_util.h:370-389) of n accumulated RGBA
+ * colours after frameID + 1 samples: format 0 sRGB rgba8, 1 linear
+ * rgba8, packed into out (n uint32). */
+void orc_write_colors(const float *accum, int n, int frameID, int format, uint32_t *out);
+
 /* TF discretisation of the reference (TransferFunction1D.cpp:101-150):
  * color (nc x 3 or 4 floats), opacity (no floats) -> 256 x RGBA; where an
  * array is absent the uniform colour (4 floats, NULL: white) / opacity

@@ -191,6 +191,16 @@ def _rows(m4):
     return (C.c_float * 12)(*[float(m[r, c]) for r in range(3) for c in range(4)])
 
 
+def write_colors(accum, frame_id: int = 0, fmt: int = 0) -> np.ndarray:
+    """The frame's packed colour (sRGB rgba8 for fmt 0, linear rgba8 for 1)
+    of accumulated RGBA values after frame_id + 1 samples."""
+    lib = load()
+    a = np.ascontiguousarray(accum, np.float32).reshape(-1, 4)
+    out = np.zeros(len(a), np.uint32)
+    lib.orc_write_colors(_ptr(a), C.c_int(len(a)), C.c_int(frame_id), C.c_int(fmt), _ptr(out))
+    return out
+
+
 def discretize_tf(color, opacity, value_range=(0.0, 1.0), uniform_opacity=1.0,
                   uniform_color=(1.0, 1.0, 1.0, 1.0)) -> np.ndarray:
     """The reference's 256-entry TF table; uniform_color (3 or 4 floats, w 1

@@ -172,3 +172,30 @@ def test_frame_allocation_failure_is_reported_and_recovers(device):
             assert np.array_equal(frame.map("channel." + ch), ref[ch]), (fail_at, ch)
         for o in keep + [frame]:
             o.release()
+
+
+def test_device_colour_write_against_reference_glm(device):
+    """The colour write every render kernel ends with, run on the GPU
+    (vrtxDebugWriteColors), against writeOutputColor's glm calls computed on
+    the host from the glm the reference vendors (tests/golden/
+    color_golden.npz): bit-exact in both formats on all 3269 colours after 1
+    and 7 samples, including sRGB, whose powf runs on the device here and on
+    the host in the fixtures."""
+    import os
+
+    import numpy as np
+
+    z = np.load(os.path.join(os.path.dirname(__file__), "golden", "color_golden.npz"))
+    for frames in (1, 7):
+        acc = np.ascontiguousarray(z[f"accum_{frames}"], np.float32)
+        for fmt in (0, 1):
+            out = np.zeros(len(acc), np.uint32)
+            rc = device.lib.vrtxDebugWriteColors(device.h, acc.ctypes.data, len(acc), frames - 1,
+                                                 fmt, out.ctypes.data)
+            assert rc == 0, device.errors()
+            ref = z[f"packed_{frames}_{fmt}"]
+            diff = np.abs(out.view(np.uint8).astype(np.int32).reshape(-1, 4)
+                          - ref.view(np.uint8).astype(np.int32).reshape(-1, 4))
+            exact = float(np.mean(out == ref))
+            print("frames", frames, "format", fmt, "exact", exact, "max step", int(diff.max()))
+            assert exact == 1.0, (frames, fmt, int(diff.max()))

@@ -173,6 +173,21 @@ def test_tf_golden_reference_helpers():
         assert np.array_equal(got, ref), (i, float(np.abs(got - ref).max()))
 
 
+def test_output_colour_write_matches_reference_glm():
+    """The oracle's frame colour write (inverse tonemap, sRGB or linear rgba8
+    packing) equals, bit for bit, writeOutputColor's calls into the glm the
+    reference vendors (glm::convertLinearToSRGB, glm::packUnorm4x8; fixtures
+    by tests/golden/make_color_golden.py) on 3269 accumulated colours after
+    1 and 7 samples: out-of-range, negative, the sRGB curve's linear segment
+    and its edge, and values next to every 8-bit rounding boundary."""
+    z = np.load(os.path.join(GOLDEN, "color_golden.npz"))
+    for frames in (1, 7):
+        for fmt in (0, 1):
+            got = O.write_colors(z[f"accum_{frames}"], frames - 1, fmt)
+            ref = z[f"packed_{frames}_{fmt}"]
+            assert np.array_equal(got, ref), (frames, fmt, int((got != ref).sum()))
+
+
 def single_triangle_spec(renderer="raycast"):
     v = np.array([[0, 0, 2], [1, 0, 2], [0, 1, 2]], np.float32)
     surf = S.SurfaceSpec("triangle", v, id=11)

@@ -4052,6 +4052,55 @@ VRTX_API int vrtxDebugDiscretizeTF(const float *color,
   return 0;
 }
 
+VRTX_API int vrtxDebugWriteColors(VRTXDevice d,
+    const float *accum,
+    uint32_t n,
+    int frameID,
+    int format,
+    uint32_t *out)
+{
+  DeviceScope scope(D(d));
+  Device *dev = D(d);
+  if (!dev || !dev->init())
+    return -1;
+  if ((n && (!accum || !out)) || frameID < 0 || (format != 0 && format != 1)) {
+    dev->report(nullptr, VRTX_SEVERITY_ERROR, "vrtxDebugWriteColors: invalid arguments");
+    return -2;
+  }
+  if (n == 0)
+    return 0;
+  cudaStream_t s = dev->stream;
+  float4 *dAcc = nullptr;
+  uint32_t *dOut = nullptr;
+  cudaError_t e = cudaMallocAsync((void **)&dAcc, sizeof(float4) * n, s);
+  if (e == cudaSuccess)
+    e = cudaMallocAsync((void **)&dOut, sizeof(uint32_t) * n, s);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(dAcc, accum, sizeof(float4) * n, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) {
+    FramebufferGPU fb{};
+    fb.frameID = frameID;
+    fb.format = format == 0 ? FORMAT_SRGB : FORMAT_UINT;
+    fb.outColorU = dOut;
+    e = launchWriteColors(fb, dAcc, n, s);
+  }
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(out, dOut, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost, s);
+  if (dAcc)
+    cudaFreeAsync(dAcc, s);
+  if (dOut)
+    cudaFreeAsync(dOut, s);
+  const cudaError_t es = cudaStreamSynchronize(s);
+  if (e == cudaSuccess)
+    e = es;
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    dev->report(nullptr, VRTX_SEVERITY_ERROR, cudaGetErrorString(e));
+    return -3;
+  }
+  return 0;
+}
+
 VRTX_API int vrtxDebugRadixSort(
     VRTXDevice d, uint64_t *keys, uint32_t *vals, uint32_t n, int bits)
 {

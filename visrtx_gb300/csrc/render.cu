@@ -83,6 +83,24 @@ cudaError_t launchScale3(const f3 *in, f3 *out, size_t n, float scale, cudaStrea
   return cudaGetLastError();
 }
 
+// The frame's colour write (writeOutputColor, the function every render
+// kernel ends with) applied to n given accumulations, for checking the
+// output encoding on its own
+__global__ void k_writeColors(FramebufferGPU fb, const float4 *accum, uint32_t n)
+{
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n)
+    writeOutputColor(fb, accum[i], i, 0);
+}
+
+cudaError_t launchWriteColors(const FramebufferGPU &fb, const float4 *accum, uint32_t n,
+    cudaStream_t s)
+{
+  if (n)
+    k_writeColors<<<(n + 255) / 256, 256, 0, s>>>(fb, accum, n);
+  return cudaGetLastError();
+}
+
 cudaError_t launchClearFrame(const FramebufferGPU &fb, cudaStream_t s)
 {
   k_clearFrame<<<1216, 256, 0, s>>>(fb);

@@ -24,6 +24,10 @@ void dispatchVolumeOnly(const FrameParams &P,
 cudaError_t launchRender(
     const FrameParams &P, int gridBlocks, bool stats, cudaStream_t s);
 cudaError_t launchClearFrame(const FramebufferGPU &fb, cudaStream_t s);
+// fb.outColorU[i] (or fb.outColorF[i]) = the frame's colour write of
+// accum[i] after fb.frameID + 1 samples, for i < n
+cudaError_t launchWriteColors(const FramebufferGPU &fb, const float4 *accum, uint32_t n,
+    cudaStream_t s);
 // out[i] = in[i] * scale for n vec3 elements (albedo / normal map)
 cudaError_t launchScale3(const f3 *in, f3 *out, size_t n, float scale, cudaStream_t s);
 
