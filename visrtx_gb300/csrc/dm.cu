@@ -8,14 +8,17 @@
 // log-transmittance form so that
 //   * the forward sums sigma_k = (step/unit) * log(1 - alpha_k) with Kahan
 //     compensation (long rays keep T accurate), and
-//   * the adjoint walks the same samples in reverse from the stored end
-//     state (log T_end, sample count), recovering log T_k = log T_{k+1} -
-//     sigma_k without storing any per-sample state, and building the suffix
-//     radiance S_k = S_{k+1} + T_k a_k c_k from S_K = T_end * background, so
-//     dL/dsigma_k = g . (S_{k+1} - T_{k+1} c_k) needs no division.
+//   * the adjoint walks the same samples in reverse from the end state
+//     (log T_end, sample count: stored by the forward kernel, or still in
+//     registers in the fused L2 training step), recovering log T_k =
+//     log T_{k+1} - sigma_k without storing any per-sample state, and
+//     building the suffix radiance S_k = S_{k+1} + T_k a_k c_k from
+//     S_K = T_end * background, so dL/dsigma_k = g . (S_{k+1} - T_{k+1} c_k)
+//     needs no division.
 // Density is read as fp32, fp16 or bf16 and interpolated in fp32; TF
-// gradients are accumulated per tile in shared memory; density gradients go
-// to fp32 global memory with atomics.
+// gradients are staged per thread and per warp in shared memory; density
+// gradients are staged per thread and go to fp32 global memory as vector
+// reductions.
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
@@ -410,11 +413,11 @@ __device__ __forceinline__ void flushTF(float4 *wTF, int seg, float acc[8])
     acc[q] = 0.f;
 }
 
-// 1: a run that moves to a neighbouring TF segment keeps the entry the two
-// segments share staged (measured 28.0 ms against 31.0 ms for committing
-// both entries at every change, backward of 32 views of 512^2 at 256^3;
-// shared-memory float atomics instead of match.any groups measured 36.6 ms
-// staged and 62.1 ms per term).
+// With VRTX_DM_TF_SLIDE 1 (the default) a run that moves to a neighbouring
+// TF segment keeps the entry the two segments share staged (measured
+// 28.0 ms against 31.0 ms for committing both entries at every change,
+// backward of 32 views of 512^2 at 256^3; shared-memory float atomics
+// instead of match.any groups measured 36.6 ms staged and 62.1 ms per term).
 #ifndef VRTX_DM_TF_SLIDE
 #define VRTX_DM_TF_SLIDE 1
 #endif
