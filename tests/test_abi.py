@@ -70,6 +70,10 @@ def test_dm_rejects_invalid_arguments(built):
                                C.c_void_p(8), 16, 8, None)
     assert rc < 0
     assert dev.errors()
+    # plan entry points without a plan refuse before touching a device
+    assert dev.lib.vrtxDMPlanStepL2(None, C.c_void_p(8), 1.0, None, None, None) == -1
+    assert dev.lib.vrtxDMPlanForward(None, C.c_void_p(8), C.c_void_p(8), None) == -1
+    assert dev.lib.vrtxDMPlanSetLaunch(None, 0, 1) == -1
     dev.release()
 
 
