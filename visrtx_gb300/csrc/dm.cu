@@ -774,6 +774,10 @@ __global__ void __launch_bounds__(256, VRTX_DM_BWD_MIN_BLOCKS) k_dmBackward(cons
       }
       backwardRay<T>(v, vw.eye, d, vw.bg, K, logT, g, plain, vecD, wTF, st, gScale);
     }
+    // every lane of the warp reaches this point each item; reconverge so
+    // that no lane still inside its sample loop (committing TF entries of
+    // the warp's shared copy) runs beside this final commit
+    __syncwarp();
     stageFlush(v, plain, vecD, wTF, st);
   }
   if (FUSED && loss) {
