@@ -1226,6 +1226,23 @@ inline float mixf(float a, float b, float t)
 }
 
 // makePrimaryRay + cameraCreateRay (gpu/cameraCreateRay.h:38-81)
+// uniformSampleDisk (gpu/gpu_math.h:292-297): the thin-lens aperture sample
+void uniformSampleDisk(float radius, float s0, float s1, float &x, float &y)
+{
+  const float r = std::sqrt(s0) * radius;
+  const float phi = 2.f * (float)M_PI * s1;
+  x = r * std::cos(phi);
+  y = r * std::sin(phi);
+}
+
+// sphericalCoordsFromDirection (gpu/gpu_math.h:254-261): the HDRI lookup
+void sphericalCoordsFromDirection(V3 d, float &theta, float &phi)
+{
+  theta = std::acos(std::min(std::max(d.z, -1.f), 1.f));
+  const float p = std::atan2(d.y, d.x);
+  phi = p < 0.f ? p + 2.f * (float)M_PI : p;
+}
+
 Ray primaryRay(const CamPre &c, Stream &rs, int px, int py, float invW, float invH,
     bool centerPixel, float *screen = nullptr)
 {
@@ -1246,9 +1263,9 @@ Ray primaryRay(const CamPre &c, Stream &rs, int px, int py, float invW, float in
     ray.org = c.pos;
     V3 d = c.d00 + sx * c.du + sy * c.dv;
     if (c.aperture > 0.f) {
-      const float rr = std::sqrt(r[2]) * c.aperture;
-      const float phi = 2.f * (float)M_PI * r[3];
-      const V3 lp = (rr * std::cos(phi)) * c.du + ((rr * std::sin(phi)) * c.aspect) * c.dv;
+      float lx, ly;
+      uniformSampleDisk(c.aperture, r[2], r[3], lx, ly);
+      const V3 lp = lx * c.du + (ly * c.aspect) * c.dv;
       ray.org = ray.org + lp;
       d = d - lp;
     }
@@ -2418,9 +2435,8 @@ V3 hdriRadiance(const SceneCtx &S, int li, V3 dir)
   const V3 d = v3(std::fma(R[2], dir.z, std::fma(R[1], dir.y, R[0] * dir.x)),
       std::fma(R[5], dir.z, std::fma(R[4], dir.y, R[3] * dir.x)),
       std::fma(R[8], dir.z, std::fma(R[7], dir.y, R[6] * dir.x)));
-  const float theta = std::acos(std::min(std::max(d.z, -1.f), 1.f));
-  const float pp = std::atan2(d.y, d.x);
-  const float phi = pp < 0.f ? pp + 2.f * (float)M_PI : pp;
+  float theta, phi;
+  sphericalCoordsFromDirection(d, theta, phi);
   return hdriTexel(L, phi * (1.f / (2.f * (float)M_PI)), theta * (1.f / (float)M_PI));
 }
 
@@ -3048,6 +3064,21 @@ int orc_nvdb_sample(const uint8_t *grid, const float *xyz, int n, int fused, flo
   for (int i = 0; i < n; i++)
     out[i] = nvdbSample(g, v3(xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]), fused);
   return 0;
+}
+
+// the two helpers above on n inputs (radius, s0, s1 -> x, y; dir -> theta,
+// phi), for checking against the reference's gpu_math.h
+void orc_uniform_sample_disk(const float *in3, int n, float *out2)
+{
+  for (int i = 0; i < n; i++)
+    uniformSampleDisk(in3[3 * i], in3[3 * i + 1], in3[3 * i + 2], out2[2 * i], out2[2 * i + 1]);
+}
+
+void orc_spherical_from_dir(const float *dir3, int n, float *out2)
+{
+  for (int i = 0; i < n; i++)
+    sphericalCoordsFromDirection(
+        v3(dir3[3 * i], dir3[3 * i + 1], dir3[3 * i + 2]), out2[2 * i], out2[2 * i + 1]);
 }
 
 // writeOutputColor (gpu/gpu_util.h:370-389) on n accumulated colours, as

@@ -263,6 +263,13 @@ int orc_render(const OrcScene *scene,
     int texRound,
     int threads);
 
+/* uniformSampleDisk (gpu_math.h:292-297) on n (radius, s0, s1) triples
+ * -> n (x, y); sphericalCoordsFromDirection (gpu_math.h:254-261) on n
+ * directions -> n (theta, phi): the oracle's own thin-lens and HDRI
+ * helpers. */
+void orc_uniform_sample_disk(const float *in3, int n, float *out2);
+void orc_spherical_from_dir(const float *dir3, int n, float *out2);
+
 /* The frame's colour write (gpu_util.h:370-389) of n accumulated RGBA
  * colours after frameID + 1 samples: format 0 sRGB rgba8, 1 linear
  * rgba8, packed into out (n uint32). */

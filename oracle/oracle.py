@@ -191,6 +191,24 @@ def _rows(m4):
     return (C.c_float * 12)(*[float(m[r, c]) for r in range(3) for c in range(4)])
 
 
+def uniform_sample_disk(radius_s0_s1) -> np.ndarray:
+    """(n, 3) of (radius, s0, s1) -> (n, 2) disk samples (the thin lens)."""
+    lib = load()
+    a = np.ascontiguousarray(radius_s0_s1, np.float32).reshape(-1, 3)
+    out = np.zeros((len(a), 2), np.float32)
+    lib.orc_uniform_sample_disk(_ptr(a), C.c_int(len(a)), _ptr(out))
+    return out
+
+
+def spherical_from_dir(dirs) -> np.ndarray:
+    """(n, 3) directions -> (n, 2) (theta, phi) (the HDRI lookup)."""
+    lib = load()
+    a = np.ascontiguousarray(dirs, np.float32).reshape(-1, 3)
+    out = np.zeros((len(a), 2), np.float32)
+    lib.orc_spherical_from_dir(_ptr(a), C.c_int(len(a)), _ptr(out))
+    return out
+
+
 def write_colors(accum, frame_id: int = 0, fmt: int = 0) -> np.ndarray:
     """The frame's packed colour (sRGB rgba8 for fmt 0, linear rgba8 for 1)
     of accumulated RGBA values after frame_id + 1 samples."""

@@ -3,7 +3,9 @@
 // getInterpolatedValue, with gpu/gpu_math.h's box1 / position / contains and
 // the vendored glm), compiled from those headers where they lie into
 // oracle/_ref/libtfref.so by oracle/build.py, only where the reference tree
-// is present, and used only by tests/golden/make_tf_golden.py.
+// is present, and used only by tests/golden/make_tf_golden.py and
+// tests/golden/make_math_golden.py (the latter for the two gpu_math.h
+// helpers at the end of this file).
 //
 // tfref_discretize repeats the call sequence of
 // TransferFunction1D::discritizeTFData (TransferFunction1D.cpp:101-150): the
@@ -59,5 +61,28 @@ extern "C" void tfref_discretize(const float *color,
     out[4 * i + 1] = c.y;
     out[4 * i + 2] = c.z;
     out[4 * i + 3] = c.w * o;
+  }
+}
+
+// The reference's own gpu/gpu_math.h helpers on the thin-lens and HDRI
+// paths (uniformSampleDisk :292-297, sphericalCoordsFromDirection
+// :254-261), compiled unchanged, on n inputs.
+extern "C" void mathref_uniform_sample_disk(const float *in3, int n, float *out2)
+{
+  for (int i = 0; i < n; i++) {
+    const visrtx::vec2 r = visrtx::uniformSampleDisk(
+        in3[3 * i], visrtx::vec2(in3[3 * i + 1], in3[3 * i + 2]));
+    out2[2 * i] = r.x;
+    out2[2 * i + 1] = r.y;
+  }
+}
+
+extern "C" void mathref_spherical_from_dir(const float *dir3, int n, float *out2)
+{
+  for (int i = 0; i < n; i++) {
+    const visrtx::vec2 r = visrtx::sphericalCoordsFromDirection(
+        visrtx::vec3(dir3[3 * i], dir3[3 * i + 1], dir3[3 * i + 2]));
+    out2[2 * i] = r.x;
+    out2[2 * i + 1] = r.y;
   }
 }

@@ -1,0 +1,58 @@
+"""Generates tests/golden/math_golden.npz: the reference's own gpu_math.h
+helpers on the thin-lens and HDRI paths, compiled unchanged on the host
+(oracle/ref_tf.cpp): uniformSampleDisk (gpu/gpu_math.h:292-297, the
+aperture sample of cameraCreateRay.h:52) on seeded (radius, s0, s1) and
+sphericalCoordsFromDirection (gpu/gpu_math.h:254-261, the HDRI lookup of
+gpu_util.h:283) on seeded unit directions plus the poles, the axes and
+directions on the phi = 0 seam from both sides.
+
+Run in a tree that holds the reference (it builds oracle/_ref/libtfref.so
+from the reference's headers):  python tests/golden/make_math_golden.py
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+
+
+def inputs(seed=7):
+    rng = np.random.default_rng(seed)
+    disk = np.stack([rng.uniform(0.0, 2.0, 2000), rng.uniform(0.0, 1.0, 2000),
+                     rng.uniform(0.0, 1.0, 2000)], axis=1)
+    disk = np.concatenate([disk, [[1.0, 0.0, 0.0], [1.0, 1.0, 0.5], [0.5, 0.25, 1.0]]])
+    d = rng.normal(size=(2000, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    edge = np.array([[0, 0, 1], [0, 0, -1], [1, 0, 0], [-1, 0, 0], [0, 1, 0], [0, -1, 0],
+                     [1, 1e-7, 0], [1, -1e-7, 0], [-1, 1e-7, 0], [-1, -1e-7, 0],
+                     [0.6, 0.0, 0.8], [0.6, -0.0, -0.8]], np.float64)
+    return disk.astype(np.float32), np.concatenate([d, edge]).astype(np.float32)
+
+
+def main():
+    from oracle import build as B
+
+    if B.build_ref() is None or not os.path.exists(B.REF_TF_LIB):
+        raise SystemExit("the reference tree is needed to generate the fixtures")
+    lib = C.CDLL(B.REF_TF_LIB)
+    for f in (lib.mathref_uniform_sample_disk, lib.mathref_spherical_from_dir):
+        f.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
+        f.restype = None
+    disk, dirs = inputs()
+    d_out = np.zeros((len(disk), 2), np.float32)
+    s_out = np.zeros((len(dirs), 2), np.float32)
+    lib.mathref_uniform_sample_disk(disk.ctypes.data, len(disk), d_out.ctypes.data)
+    lib.mathref_spherical_from_dir(dirs.ctypes.data, len(dirs), s_out.ctypes.data)
+    np.savez_compressed(os.path.join(HERE, "math_golden.npz"), disk_in=disk, disk_out=d_out,
+                        dir_in=dirs, dir_out=s_out)
+    print("wrote", os.path.join(HERE, "math_golden.npz"), len(disk), "disk samples,",
+          len(dirs), "directions")
+
+
+if __name__ == "__main__":
+    main()
