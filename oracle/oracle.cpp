@@ -1235,6 +1235,18 @@ void uniformSampleDisk(float radius, float s0, float s1, float &x, float &y)
   y = r * std::sin(phi);
 }
 
+// uniformSampleCone (gpu/gpu_math.h:299-312): the physically based
+// material's next-ray sample (2 * M_PI * s0 is a double product there, as
+// here)
+V3 uniformSampleCone(float cosThetaMax, float s0, float s1, float s2)
+{
+  const float phi = (float)(2.0 * M_PI * (double)s0);
+  const float cosTheta = (1.f - s1) + s1 * cosThetaMax;
+  const float sinTheta = std::sqrt(1.f - cosTheta * cosTheta);
+  const float d = std::pow(s2, 1.f / 3.f);
+  return v3(d * sinTheta * std::cos(phi), d * sinTheta * std::sin(phi), d * cosTheta);
+}
+
 // sphericalCoordsFromDirection (gpu/gpu_math.h:254-261): the HDRI lookup
 void sphericalCoordsFromDirection(V3 d, float &theta, float &phi)
 {
@@ -2627,11 +2639,7 @@ bool nextRay(const Matte &m, V3 Ns, V3 rayDir, Stream &rs, V3 &dir, V3 &weight)
   const V3 refl = rayDir - 2.f * dot(rayDir, Ns) * Ns;
   const float cosThetaMax = 1.f - m.roughness * m.roughness;
   const float s0 = uniform(rs), s1 = uniform(rs), s2 = uniform(rs);
-  const float phi = (float)(2.0 * M_PI * (double)s0);
-  const float cosTheta = (1.f - s1) + s1 * cosThetaMax;
-  const float sinTheta = std::sqrt(1.f - cosTheta * cosTheta);
-  const float d = std::pow(s2, 1.f / 3.f);
-  const V3 cone = v3(d * sinTheta * std::cos(phi), d * sinTheta * std::sin(phi), d * cosTheta);
+  const V3 cone = uniformSampleCone(cosThetaMax, s0, s1, s2);
   dir = onbMul(normalize(refl), cone);
   weight = m.base * m.metallic;
   return true;
@@ -3072,6 +3080,16 @@ void orc_uniform_sample_disk(const float *in3, int n, float *out2)
 {
   for (int i = 0; i < n; i++)
     uniformSampleDisk(in3[3 * i], in3[3 * i + 1], in3[3 * i + 2], out2[2 * i], out2[2 * i + 1]);
+}
+
+void orc_uniform_sample_cone(const float *in4, int n, float *out3)
+{
+  for (int i = 0; i < n; i++) {
+    const V3 r = uniformSampleCone(in4[4 * i], in4[4 * i + 1], in4[4 * i + 2], in4[4 * i + 3]);
+    out3[3 * i] = r.x;
+    out3[3 * i + 1] = r.y;
+    out3[3 * i + 2] = r.z;
+  }
 }
 
 void orc_spherical_from_dir(const float *dir3, int n, float *out2)

@@ -200,6 +200,15 @@ def uniform_sample_disk(radius_s0_s1) -> np.ndarray:
     return out
 
 
+def uniform_sample_cone(cos_s0_s1_s2) -> np.ndarray:
+    """(n, 4) of (cosThetaMax, s0, s1, s2) -> (n, 3) cone samples."""
+    lib = load()
+    a = np.ascontiguousarray(cos_s0_s1_s2, np.float32).reshape(-1, 4)
+    out = np.zeros((len(a), 3), np.float32)
+    lib.orc_uniform_sample_cone(_ptr(a), C.c_int(len(a)), _ptr(out))
+    return out
+
+
 def spherical_from_dir(dirs) -> np.ndarray:
     """(n, 3) directions -> (n, 2) (theta, phi) (the HDRI lookup)."""
     lib = load()

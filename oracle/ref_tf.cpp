@@ -64,9 +64,10 @@ extern "C" void tfref_discretize(const float *color,
   }
 }
 
-// The reference's own gpu/gpu_math.h helpers on the thin-lens and HDRI
-// paths (uniformSampleDisk :292-297, sphericalCoordsFromDirection
-// :254-261), compiled unchanged, on n inputs.
+// The reference's own gpu/gpu_math.h helpers on the thin-lens, HDRI and
+// physically based next-ray paths (uniformSampleDisk :292-297,
+// sphericalCoordsFromDirection :254-261, uniformSampleCone below),
+// compiled unchanged, on n inputs.
 extern "C" void mathref_uniform_sample_disk(const float *in3, int n, float *out2)
 {
   for (int i = 0; i < n; i++) {
@@ -84,5 +85,17 @@ extern "C" void mathref_spherical_from_dir(const float *dir3, int n, float *out2
         visrtx::vec3(dir3[3 * i], dir3[3 * i + 1], dir3[3 * i + 2]));
     out2[2 * i] = r.x;
     out2[2 * i + 1] = r.y;
+  }
+}
+
+// uniformSampleCone (gpu/gpu_math.h:299-312), compiled unchanged
+extern "C" void mathref_uniform_sample_cone(const float *in4, int n, float *out3)
+{
+  for (int i = 0; i < n; i++) {
+    const visrtx::vec3 r = visrtx::uniformSampleCone(
+        in4[4 * i], visrtx::vec3(in4[4 * i + 1], in4[4 * i + 2], in4[4 * i + 3]));
+    out3[3 * i] = r.x;
+    out3[3 * i + 1] = r.y;
+    out3[3 * i + 2] = r.z;
   }
 }

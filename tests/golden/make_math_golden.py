@@ -4,7 +4,9 @@ helpers on the thin-lens and HDRI paths, compiled unchanged on the host
 aperture sample of cameraCreateRay.h:52) on seeded (radius, s0, s1) and
 sphericalCoordsFromDirection (gpu/gpu_math.h:254-261, the HDRI lookup of
 gpu_util.h:283) on seeded unit directions plus the poles, the axes and
-directions on the phi = 0 seam from both sides.
+directions on the phi = 0 seam from both sides, and uniformSampleCone
+(gpu/gpu_math.h:299-312, the physically based material's next ray,
+PhysicallyBasedShader_ptx.cu:75) on seeded (cosThetaMax, s0, s1, s2).
 
 Run in a tree that holds the reference (it builds oracle/_ref/libtfref.so
 from the reference's headers):  python tests/golden/make_math_golden.py
@@ -31,7 +33,11 @@ def inputs(seed=7):
     edge = np.array([[0, 0, 1], [0, 0, -1], [1, 0, 0], [-1, 0, 0], [0, 1, 0], [0, -1, 0],
                      [1, 1e-7, 0], [1, -1e-7, 0], [-1, 1e-7, 0], [-1, -1e-7, 0],
                      [0.6, 0.0, 0.8], [0.6, -0.0, -0.8]], np.float64)
-    return disk.astype(np.float32), np.concatenate([d, edge]).astype(np.float32)
+    cone = np.stack([rng.uniform(-1.0, 1.0, 2000), rng.uniform(0.0, 1.0, 2000),
+                     rng.uniform(0.0, 1.0, 2000), rng.uniform(0.0, 1.0, 2000)], axis=1)
+    cone = np.concatenate([cone, [[1.0, 0.0, 0.0, 0.0], [0.0, 0.5, 1.0, 1.0]]])
+    return (disk.astype(np.float32), np.concatenate([d, edge]).astype(np.float32),
+            cone.astype(np.float32))
 
 
 def main():
@@ -40,18 +46,21 @@ def main():
     if B.build_ref() is None or not os.path.exists(B.REF_TF_LIB):
         raise SystemExit("the reference tree is needed to generate the fixtures")
     lib = C.CDLL(B.REF_TF_LIB)
-    for f in (lib.mathref_uniform_sample_disk, lib.mathref_spherical_from_dir):
+    for f in (lib.mathref_uniform_sample_disk, lib.mathref_spherical_from_dir,
+              lib.mathref_uniform_sample_cone):
         f.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
         f.restype = None
-    disk, dirs = inputs()
+    disk, dirs, cone = inputs()
     d_out = np.zeros((len(disk), 2), np.float32)
     s_out = np.zeros((len(dirs), 2), np.float32)
     lib.mathref_uniform_sample_disk(disk.ctypes.data, len(disk), d_out.ctypes.data)
     lib.mathref_spherical_from_dir(dirs.ctypes.data, len(dirs), s_out.ctypes.data)
+    c_out = np.zeros((len(cone), 3), np.float32)
+    lib.mathref_uniform_sample_cone(cone.ctypes.data, len(cone), c_out.ctypes.data)
     np.savez_compressed(os.path.join(HERE, "math_golden.npz"), disk_in=disk, disk_out=d_out,
-                        dir_in=dirs, dir_out=s_out)
+                        dir_in=dirs, dir_out=s_out, cone_in=cone, cone_out=c_out)
     print("wrote", os.path.join(HERE, "math_golden.npz"), len(disk), "disk samples,",
-          len(dirs), "directions")
+          len(dirs), "directions,", len(cone), "cone samples")
 
 
 if __name__ == "__main__":

@@ -190,14 +190,16 @@ def test_output_colour_write_matches_reference_glm():
 
 def test_thin_lens_and_hdri_helpers_match_reference_gpu_math():
     """The oracle's aperture sample (uniformSampleDisk, used by the thin-lens
-    camera) and HDRI direction-to-angles map (sphericalCoordsFromDirection)
-    equal, bit for bit, the reference's own gpu/gpu_math.h functions
+    camera), HDRI direction-to-angles map (sphericalCoordsFromDirection)
+    and next-ray cone sample (uniformSampleCone) equal, bit for bit, the reference's own gpu/gpu_math.h functions
     compiled on the host (fixtures by tests/golden/make_math_golden.py):
-    2003 seeded disk samples and 2012 directions including the poles, the
-    axes and both sides of the phi = 0 seam."""
+    2003 seeded disk samples, 2012 directions including the poles, the
+    axes and both sides of the phi = 0 seam, and 2002 cone samples."""
     z = np.load(os.path.join(GOLDEN, "math_golden.npz"))
     assert np.array_equal(O.uniform_sample_disk(z["disk_in"]), z["disk_out"])
     assert np.array_equal(O.spherical_from_dir(z["dir_in"]), z["dir_out"])
+    # the physically based material's next-ray cone sample
+    assert np.array_equal(O.uniform_sample_cone(z["cone_in"]), z["cone_out"])
 
 
 def single_triangle_spec(renderer="raycast"):
