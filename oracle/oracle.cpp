@@ -3092,6 +3092,16 @@ void orc_uniform_sample_cone(const float *in4, int n, float *out3)
   }
 }
 
+// projectOnGrid (gpu/uniformGrid.h:43-50) of n points onto a dims grid
+// over the box (lo xyz, hi xyz), axis by axis as the majorant grid builds
+// use it
+void orc_project_on_grid(const float *p3, int n, const int *dims3, const float *box6, int *out3)
+{
+  for (int i = 0; i < n; i++)
+    for (int a = 0; a < 3; a++)
+      out3[3 * i + a] = projectAxis(p3[3 * i + a], box6[a], box6[3 + a], dims3[a]);
+}
+
 void orc_spherical_from_dir(const float *dir3, int n, float *out2)
 {
   for (int i = 0; i < n; i++)

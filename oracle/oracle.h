@@ -272,6 +272,9 @@ void orc_spherical_from_dir(const float *dir3, int n, float *out2);
 /* uniformSampleCone (gpu_math.h:299-312) on n (cosThetaMax, s0, s1, s2)
  * -> n directions: the physically based material's next-ray sample. */
 void orc_uniform_sample_cone(const float *in4, int n, float *out3);
+/* projectOnGrid (uniformGrid.h:43-50) of n points onto a dims3 grid over
+ * box6 (lo xyz, hi xyz) -> n integer cells. */
+void orc_project_on_grid(const float *p3, int n, const int *dims3, const float *box6, int *out3);
 
 /* The frame's colour write (gpu_util.h:370-389) of n accumulated RGBA
  * colours after frameID + 1 samples: format 0 sRGB rgba8, 1 linear

@@ -209,6 +209,17 @@ def uniform_sample_cone(cos_s0_s1_s2) -> np.ndarray:
     return out
 
 
+def project_on_grid(points, dims, box) -> np.ndarray:
+    """(n, 3) points -> (n, 3) cells of a dims grid over box (lo, hi)."""
+    lib = load()
+    p = np.ascontiguousarray(points, np.float32).reshape(-1, 3)
+    d = np.ascontiguousarray(dims, np.int32)
+    b = np.ascontiguousarray(box, np.float32).reshape(6)
+    out = np.zeros((len(p), 3), np.int32)
+    lib.orc_project_on_grid(_ptr(p), C.c_int(len(p)), _ptr(d), _ptr(b), _ptr(out))
+    return out
+
+
 def spherical_from_dir(dirs) -> np.ndarray:
     """(n, 3) directions -> (n, 2) (theta, phi) (the HDRI lookup)."""
     lib = load()

@@ -14,6 +14,7 @@
 // with a = 1 for vec3 colours, and the uniform colour / opacity where an
 // array is absent. That file itself needs the ANARI-SDK and cannot be built
 // here; the arithmetic it calls is the helpers', compiled unchanged.
+#include "gpu/uniformGrid.h"
 #include "utility/colorMapHelpers.h"
 
 #include <vector>
@@ -97,5 +98,23 @@ extern "C" void mathref_uniform_sample_cone(const float *in4, int n, float *out3
     out3[3 * i] = r.x;
     out3[3 * i + 1] = r.y;
     out3[3 * i + 2] = r.z;
+  }
+}
+
+// projectOnGrid (gpu/uniformGrid.h:43-50), compiled unchanged, for points
+// inside the box (outside it the host's float-to-int conversion is not
+// defined)
+extern "C" void mathref_project_on_grid(
+    const float *p3, int n, const int *dims3, const float *box6, int *out3)
+{
+  const visrtx::ivec3 dims(dims3[0], dims3[1], dims3[2]);
+  const visrtx::box3 b(visrtx::vec3(box6[0], box6[1], box6[2]),
+      visrtx::vec3(box6[3], box6[4], box6[5]));
+  for (int i = 0; i < n; i++) {
+    const visrtx::ivec3 c = visrtx::projectOnGrid(
+        visrtx::vec3(p3[3 * i], p3[3 * i + 1], p3[3 * i + 2]), dims, b);
+    out3[3 * i] = c.x;
+    out3[3 * i + 1] = c.y;
+    out3[3 * i + 2] = c.z;
   }
 }

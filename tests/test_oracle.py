@@ -194,12 +194,18 @@ def test_thin_lens_and_hdri_helpers_match_reference_gpu_math():
     and next-ray cone sample (uniformSampleCone) equal, bit for bit, the reference's own gpu/gpu_math.h functions
     compiled on the host (fixtures by tests/golden/make_math_golden.py):
     2003 seeded disk samples, 2012 directions including the poles, the
-    axes and both sides of the phi = 0 seam, and 2002 cone samples."""
+    axes and both sides of the phi = 0 seam, and 2002 cone samples; and
+    its macrocell projection (projectOnGrid) of 2120 points inside 40
+    seeded boxes, faces included."""
     z = np.load(os.path.join(GOLDEN, "math_golden.npz"))
     assert np.array_equal(O.uniform_sample_disk(z["disk_in"]), z["disk_out"])
     assert np.array_equal(O.spherical_from_dir(z["dir_in"]), z["dir_out"])
     # the physically based material's next-ray cone sample
     assert np.array_equal(O.uniform_sample_cone(z["cone_in"]), z["cone_out"])
+    # the macrocell projection of the delta-tracking grid
+    for k in range(int(z["grids"][0])):
+        got = O.project_on_grid(z[f"grid{k}_points"], z[f"grid{k}_dims"], z[f"grid{k}_box"])
+        assert np.array_equal(got, z[f"grid{k}_cells"]), k
 
 
 def single_triangle_spec(renderer="raycast"):
