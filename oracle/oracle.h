@@ -19,6 +19,14 @@
  * library the reference vendors (external/nanovdb): its builder made the
  * golden grids and its sampler the golden values, which the reader here
  * reproduces bit for bit (oracle/ref_nvdb.cpp, tests/golden/nvdb_golden.npz).
+ * The reference's own host-compilable code on the path pins more of it:
+ * its TF discretisation helpers (utility/colorMapHelpers.h), its
+ * gpu/gpu_math.h helpers for the thin-lens aperture, the HDRI direction map
+ * and the physically based cone sample, its macrocell projection
+ * (gpu/uniformGrid.h) and its frame colour write's glm calls, compiled in
+ * place (oracle/ref_tf.cpp, oracle/ref_glm.cpp), made the fixtures
+ * tests/golden/tf_golden.npz, math_golden.npz and color_golden.npz, which
+ * the functions here reproduce bit for bit.
  */
 #ifndef VRTX_ORACLE_H
 #define VRTX_ORACLE_H
