@@ -309,3 +309,31 @@ def test_multithreaded_object_creation(shim):
     bad = [m for s, m in msgs if s <= A["ANARI_SEVERITY_ERROR"]]
     assert not bad, bad[:5]
     shim.anariRelease(dev, dev)
+
+
+@pytest.mark.gpu
+def test_device_force_init(shim):
+    """The reference's other API test (tests/api/TestDeviceInit.cpp:37-44)
+    through the ANARI names: makeVisRTXDevice, "forceInit" set on the
+    device and committed initialises CUDA at once with no fatal or error
+    status, and the device reports its "visrtx" property; then it is
+    released."""
+    msgs = []
+
+    def status(user, device, source, source_type, severity, code, message):
+        msgs.append((severity, message))
+
+    cb = STATUS_CB(status)
+    dev = shim.makeVisRTXDevice(cb, None)
+    assert dev
+    on = C.c_int32(1)
+    shim.lib.anariSetParameter(C.c_void_p(dev), C.c_void_p(dev), b"forceInit",
+                               A["ANARI_BOOL"], C.byref(on))
+    shim.lib.anariCommitParameters(C.c_void_p(dev), C.c_void_p(dev))
+    bad = [m for s, m in msgs if s <= A["ANARI_SEVERITY_ERROR"]]
+    assert not bad, bad
+    flag = C.c_int32(0)
+    assert shim.lib.anariGetProperty(C.c_void_p(dev), C.c_void_p(dev), b"visrtx",
+                                     A["ANARI_BOOL"], C.byref(flag), 4, 1) == 1
+    assert flag.value == 1
+    shim.anariRelease(dev, dev)
