@@ -14,12 +14,21 @@ output only in oracle/_ref/:
     TransferFunction1D::discritizeTFData's calls (libtfref.so);
   * the vendored glm's colour packing (glm::convertLinearToSRGB,
     glm::packUnorm4x8): ref_glm.cpp repeats writeOutputColor's calls
-    (libglmref.so).
+    (libglmref.so);
+  * its macrocell walk (devices/rtx/gpu/dda.h, dda3): ref_dda.cpp runs it
+    (libddaref.so). dda.h includes the OptiX-bound gpu_objects.h, so it is
+    compiled through oracle/_ref/dda_inc/gpu/, links to the reference's
+    headers beside a link to oracle/ref_shim/gpu_objects.h, and with
+    floating-point contraction on, as nvcc builds the reference's device
+    code (-fmad=true): -ffp-contract=fast, with -mfma on x86-64, where the
+    fused multiply-add is not in the base instruction set.
 The GPU machine has no reference tree and never builds them.
 """
 from __future__ import annotations
 
 import os
+import platform
+import shutil
 import subprocess
 
 HERE = os.path.dirname(os.path.abspath(__file__))
@@ -50,14 +59,20 @@ REF_OUT = os.path.join(HERE, "_ref")
 REF_LIB = os.path.join(REF_OUT, "libnvdbref.so")
 REF_TF_LIB = os.path.join(REF_OUT, "libtfref.so")
 REF_GLM_LIB = os.path.join(REF_OUT, "libglmref.so")
+REF_DDA_LIB = os.path.join(REF_OUT, "libddaref.so")
+DDA_HEADERS = ("dda.h", "gpu_debug.h", "gpu_math.h", "gpu_decl.h", "uniformGrid.h")
 
 
-def _compile_ref(src: str, out: str, incs: list[str]) -> str:
+def _compile_ref(src: str, out: str, incs: list[str], contract: str = "off",
+                 deps: tuple[str, ...] = ()) -> str:
     os.makedirs(REF_OUT, exist_ok=True)
-    if os.path.exists(out) and os.path.getmtime(out) >= os.path.getmtime(src):
+    if os.path.exists(out) and all(os.path.getmtime(out) >= os.path.getmtime(f)
+                                   for f in (src, *deps)):
         return out
     tmp = out + ".tmp"
-    cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off"]
+    cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", f"-ffp-contract={contract}"]
+    if contract == "fast" and platform.machine().lower() in ("x86_64", "amd64"):
+        cmd.append("-mfma")
     for i in incs:
         cmd += ["-I", i]
     cmd += ["-o", tmp, src, "-lpthread"]
@@ -71,8 +86,9 @@ def _compile_ref(src: str, out: str, incs: list[str]) -> str:
 def build_ref(tree: str | None = None) -> str | None:
     """oracle/_ref/libnvdbref.so (ref_nvdb.cpp over the reference's vendored
     NanoVDB headers), oracle/_ref/libtfref.so (ref_tf.cpp over its
-    transfer-function helpers) and oracle/_ref/libglmref.so (ref_glm.cpp
-    over its vendored glm) from the reference tree `tree` (default
+    transfer-function helpers), oracle/_ref/libglmref.so (ref_glm.cpp
+    over its vendored glm) and oracle/_ref/libddaref.so (ref_dda.cpp over
+    its dda.h) from the reference tree `tree` (default
     REF_TREE); returns the NanoVDB harness's path, or None when the
     reference tree is absent."""
     root = tree or REF_TREE
@@ -85,7 +101,34 @@ def build_ref(tree: str | None = None) -> str | None:
     if os.path.isfile(os.path.join(rtx, "utility", "colorMapHelpers.h")) and os.path.isdir(glm):
         _compile_ref(os.path.join(HERE, "ref_tf.cpp"), REF_TF_LIB, [rtx, glm])
         _compile_ref(os.path.join(HERE, "ref_glm.cpp"), REF_GLM_LIB, [glm])
+        if all(os.path.isfile(os.path.join(rtx, "gpu", h)) for h in DDA_HEADERS):
+            # the links point into the reference tree: made for the compile
+            # only, so that no dangling link is left in oracle/_ref
+            inc = _dda_include_dir(os.path.join(rtx, "gpu"))
+            try:
+                _compile_ref(os.path.join(HERE, "ref_dda.cpp"), REF_DDA_LIB, [inc, glm],
+                             contract="fast",
+                             deps=(os.path.join(HERE, "ref_shim", "gpu_objects.h"),))
+            finally:
+                shutil.rmtree(inc, ignore_errors=True)
     return lib
+
+
+def _dda_include_dir(gpu_dir: str) -> str:
+    """oracle/_ref/dda_inc: gpu/ holds links to the reference's dda.h and the
+    headers it includes, and to oracle/ref_shim/gpu_objects.h, so that
+    dda.h's own-directory includes find the stand-in for gpu_objects.h."""
+    inc = os.path.join(REF_OUT, "dda_inc")
+    d = os.path.join(inc, "gpu")
+    os.makedirs(d, exist_ok=True)
+    links = {h: os.path.join(gpu_dir, h) for h in DDA_HEADERS}
+    links["gpu_objects.h"] = os.path.join(HERE, "ref_shim", "gpu_objects.h")
+    for name, target in links.items():
+        p = os.path.join(d, name)
+        if os.path.lexists(p):
+            os.remove(p)
+        os.symlink(target, p)
+    return inc
 
 
 if __name__ == "__main__":

@@ -3102,6 +3102,37 @@ void orc_project_on_grid(const float *p3, int n, const int *dims3, const float *
       out3[3 * i + a] = projectAxis(p3[3 * i + a], box6[a], box6[3 + a], dims3[a]);
 }
 
+// dda3 (gpu/dda.h:43-122), the walk the delta-tracking march takes, for n
+// rays (org xyz, dir xyz, tlo, thi) over a dims3 grid spanning box6: per
+// visited cell its linear index and [t0, t1], at most maxCells per ray
+int orc_dda_walk(const float *rays8,
+    int n,
+    const int *dims3,
+    const float *box6,
+    int maxCells,
+    int *counts,
+    long long *cells,
+    float *t01)
+{
+  const V3 blo = v3(box6[0], box6[1], box6[2]), bhi = v3(box6[3], box6[4], box6[5]);
+  int total = 0;
+  for (int i = 0; i < n; i++) {
+    const float *r = rays8 + 8 * i;
+    int k = 0;
+    dda3(v3(r[0], r[1], r[2]), v3(r[3], r[4], r[5]), r[6], r[7], dims3, blo, bhi,
+        [&](size_t cell, float t0, float t1) {
+          const size_t j = (size_t)i * maxCells + k;
+          cells[j] = (long long)cell;
+          t01[2 * j] = t0;
+          t01[2 * j + 1] = t1;
+          return ++k < maxCells;
+        });
+    counts[i] = k;
+    total += k;
+  }
+  return total;
+}
+
 void orc_spherical_from_dir(const float *dir3, int n, float *out2)
 {
   for (int i = 0; i < n; i++)

@@ -23,10 +23,12 @@
  * its TF discretisation helpers (utility/colorMapHelpers.h), its
  * gpu/gpu_math.h helpers for the thin-lens aperture, the HDRI direction map
  * and the physically based cone sample, its macrocell projection
- * (gpu/uniformGrid.h) and its frame colour write's glm calls, compiled in
- * place (oracle/ref_tf.cpp, oracle/ref_glm.cpp), made the fixtures
- * tests/golden/tf_golden.npz, math_golden.npz and color_golden.npz, which
- * the functions here reproduce bit for bit.
+ * (gpu/uniformGrid.h), its macrocell walk (gpu/dda.h, compiled with
+ * contraction on, as nvcc builds it) and its frame colour write's glm
+ * calls, compiled in place (oracle/ref_tf.cpp, oracle/ref_dda.cpp,
+ * oracle/ref_glm.cpp), made the fixtures tests/golden/tf_golden.npz,
+ * math_golden.npz, dda_golden.npz and color_golden.npz, which the
+ * functions here reproduce bit for bit.
  */
 #ifndef VRTX_ORACLE_H
 #define VRTX_ORACLE_H
@@ -283,6 +285,18 @@ void orc_uniform_sample_cone(const float *in4, int n, float *out3);
 /* projectOnGrid (uniformGrid.h:43-50) of n points onto a dims3 grid over
  * box6 (lo xyz, hi xyz) -> n integer cells. */
 void orc_project_on_grid(const float *p3, int n, const int *dims3, const float *box6, int *out3);
+/* dda3 (dda.h:43-122) for n rays (org xyz, dir xyz, tlo, thi) over a dims3
+ * grid spanning box6: counts[i] cells per ray (at most maxCells), their
+ * linear indices in cells[i * maxCells ...] and intervals in
+ * t01[2 * (i * maxCells + k) ...]; returns the total. */
+int orc_dda_walk(const float *rays8,
+    int n,
+    const int *dims3,
+    const float *box6,
+    int maxCells,
+    int *counts,
+    long long *cells,
+    float *t01);
 
 /* The frame's colour write (gpu_util.h:370-389) of n accumulated RGBA
  * colours after frameID + 1 samples: format 0 sRGB rgba8, 1 linear

@@ -220,6 +220,21 @@ def project_on_grid(points, dims, box) -> np.ndarray:
     return out
 
 
+def dda_walk(rays, dims, box, max_cells):
+    """(n, 8) rays (org, dir, tlo, thi) -> (counts (n,), cells (n, max_cells),
+    t01 (n, max_cells, 2)): the macrocell walk of the delta-tracking march."""
+    lib = load()
+    r = np.ascontiguousarray(rays, np.float32).reshape(-1, 8)
+    d = np.ascontiguousarray(dims, np.int32)
+    b = np.ascontiguousarray(box, np.float32).reshape(6)
+    counts = np.zeros(len(r), np.int32)
+    cells = np.full((len(r), max_cells), -1, np.int64)
+    t01 = np.zeros((len(r), max_cells, 2), np.float32)
+    lib.orc_dda_walk(_ptr(r), C.c_int(len(r)), _ptr(d), _ptr(b), C.c_int(max_cells),
+                     _ptr(counts), _ptr(cells), _ptr(t01))
+    return counts, cells, t01
+
+
 def spherical_from_dir(dirs) -> np.ndarray:
     """(n, 3) directions -> (n, 2) (theta, phi) (the HDRI lookup)."""
     lib = load()

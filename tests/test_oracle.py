@@ -1,6 +1,7 @@
 """CPU checks of the oracle itself: known-answer vectors for Philox4x32-10
 (the SC'11 paper's algorithm), curand-style stream semantics, the TF
-discretisation (pinned to the reference's own TF helpers), single-ray
+discretisation, gpu_math.h helpers, macrocell projection and walk, and
+frame colour write (pinned to the reference's own code), single-ray
 analytic hits, point and spot light shading, sRGB
 endpoints, and an FP64 central-difference check of the differentiable
 marcher's adjoint. GPU-dumped curand and texture outputs pin the RNG and
@@ -206,6 +207,33 @@ def test_thin_lens_and_hdri_helpers_match_reference_gpu_math():
     for k in range(int(z["grids"][0])):
         got = O.project_on_grid(z[f"grid{k}_points"], z[f"grid{k}_dims"], z[f"grid{k}_box"])
         assert np.array_equal(got, z[f"grid{k}_cells"]), k
+
+
+def test_macrocell_walk_matches_reference_dda():
+    """The oracle's macrocell walk (dda3, which the delta-tracking march
+    runs over the majorant grid) visits the same cells with the same
+    [t0, t1] intervals, bit for bit, as the reference's own gpu/dda.h
+    compiled on the host with contraction on, as nvcc builds it (fixtures
+    by tests/golden/make_dda_golden.py): 1796 rays, 17378 cells, over six
+    grids: random and axis-aligned directions (a zero component walks that
+    axis down at t = 0), ties between axes from exact faces and corners of
+    a power-of-two grid, a one-cell grid, [tlo, thi] inside the box and
+    negative tlo, origins just outside the box, and walks cut short after
+    three cells. Compiled without contraction, the reference's walk gives
+    other intervals on 7200 of these cells and other cells on the tie grid,
+    so the fixtures pin the fused first-boundary step."""
+    z = np.load(os.path.join(GOLDEN, "dda_golden.npz"))
+    rays = cells = 0
+    for i in range(int(z["num_cases"])):
+        mc = int(z[f"c{i}_max_cells"])
+        counts, walk, t01 = O.dda_walk(z[f"c{i}_rays"], z[f"c{i}_dims"], z[f"c{i}_box"], mc)
+        assert np.array_equal(counts, z[f"c{i}_counts"]), i
+        keep = np.arange(mc)[None, :] < counts[:, None]
+        assert np.array_equal(walk[keep], z[f"c{i}_cells"]), i
+        assert np.array_equal(t01[keep].view(np.uint32), z[f"c{i}_t01"].view(np.uint32)), i
+        rays += len(counts)
+        cells += int(counts.sum())
+    assert (rays, cells) == (1796, 17378)
 
 
 def single_triangle_spec(renderer="raycast"):
