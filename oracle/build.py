@@ -16,12 +16,18 @@ output only in oracle/_ref/:
     glm::packUnorm4x8): ref_glm.cpp repeats writeOutputColor's calls
     (libglmref.so);
   * its macrocell walk (devices/rtx/gpu/dda.h, dda3): ref_dda.cpp runs it
-    (libddaref.so). dda.h includes the OptiX-bound gpu_objects.h, so it is
-    compiled through oracle/_ref/dda_inc/gpu/, links to the reference's
-    headers beside a link to oracle/ref_shim/gpu_objects.h, and with
-    floating-point contraction on, as nvcc builds the reference's device
-    code (-fmad=true): -ffp-contract=fast, with -mfma on x86-64, where the
-    fused multiply-add is not in the base instruction set.
+    (libddaref.so), with floating-point contraction on, as nvcc builds the
+    reference's device code (-fmad=true): -ffp-contract=fast, with -mfma
+    on x86-64, where the fused multiply-add is not in the base instruction
+    set;
+  * its primary-ray generation (devices/rtx/gpu/cameraCreateRay.h):
+    ref_camera.cpp runs it without contraction (libcamref.so, each
+    operation rounded once, as the oracle and the library's kernels round
+    it) and with it (libcamref_fused.so, to size the gap).
+  Both headers include the OptiX-bound gpu_objects.h, so these two are
+  compiled through oracle/_ref/gpu_inc/gpu/, links to the reference's
+  headers beside a link to oracle/ref_shim/gpu_objects.h, made for the
+  compile and removed after it.
 The GPU machine has no reference tree and never builds them.
 """
 from __future__ import annotations
@@ -60,7 +66,10 @@ REF_LIB = os.path.join(REF_OUT, "libnvdbref.so")
 REF_TF_LIB = os.path.join(REF_OUT, "libtfref.so")
 REF_GLM_LIB = os.path.join(REF_OUT, "libglmref.so")
 REF_DDA_LIB = os.path.join(REF_OUT, "libddaref.so")
-DDA_HEADERS = ("dda.h", "gpu_debug.h", "gpu_math.h", "gpu_decl.h", "uniformGrid.h")
+REF_CAM_LIB = os.path.join(REF_OUT, "libcamref.so")
+REF_CAM_FUSED_LIB = os.path.join(REF_OUT, "libcamref_fused.so")
+GPU_HEADERS = ("dda.h", "gpu_debug.h", "gpu_math.h", "gpu_decl.h", "uniformGrid.h",
+               "cameraCreateRay.h")
 
 
 def _compile_ref(src: str, out: str, incs: list[str], contract: str = "off",
@@ -87,8 +96,9 @@ def build_ref(tree: str | None = None) -> str | None:
     """oracle/_ref/libnvdbref.so (ref_nvdb.cpp over the reference's vendored
     NanoVDB headers), oracle/_ref/libtfref.so (ref_tf.cpp over its
     transfer-function helpers), oracle/_ref/libglmref.so (ref_glm.cpp
-    over its vendored glm) and oracle/_ref/libddaref.so (ref_dda.cpp over
-    its dda.h) from the reference tree `tree` (default
+    over its vendored glm), oracle/_ref/libddaref.so (ref_dda.cpp over
+    its dda.h) and oracle/_ref/libcamref{,_fused}.so (ref_camera.cpp over
+    its cameraCreateRay.h) from the reference tree `tree` (default
     REF_TREE); returns the NanoVDB harness's path, or None when the
     reference tree is absent."""
     root = tree or REF_TREE
@@ -101,27 +111,31 @@ def build_ref(tree: str | None = None) -> str | None:
     if os.path.isfile(os.path.join(rtx, "utility", "colorMapHelpers.h")) and os.path.isdir(glm):
         _compile_ref(os.path.join(HERE, "ref_tf.cpp"), REF_TF_LIB, [rtx, glm])
         _compile_ref(os.path.join(HERE, "ref_glm.cpp"), REF_GLM_LIB, [glm])
-        if all(os.path.isfile(os.path.join(rtx, "gpu", h)) for h in DDA_HEADERS):
+        if all(os.path.isfile(os.path.join(rtx, "gpu", h)) for h in GPU_HEADERS):
             # the links point into the reference tree: made for the compile
             # only, so that no dangling link is left in oracle/_ref
-            inc = _dda_include_dir(os.path.join(rtx, "gpu"))
+            inc = _gpu_include_dir(os.path.join(rtx, "gpu"))
+            shim = (os.path.join(HERE, "ref_shim", "gpu_objects.h"),)
+            cam = os.path.join(HERE, "ref_camera.cpp")
             try:
                 _compile_ref(os.path.join(HERE, "ref_dda.cpp"), REF_DDA_LIB, [inc, glm],
-                             contract="fast",
-                             deps=(os.path.join(HERE, "ref_shim", "gpu_objects.h"),))
+                             contract="fast", deps=shim)
+                _compile_ref(cam, REF_CAM_LIB, [inc, glm], contract="off", deps=shim)
+                _compile_ref(cam, REF_CAM_FUSED_LIB, [inc, glm], contract="fast", deps=shim)
             finally:
                 shutil.rmtree(inc, ignore_errors=True)
     return lib
 
 
-def _dda_include_dir(gpu_dir: str) -> str:
-    """oracle/_ref/dda_inc: gpu/ holds links to the reference's dda.h and the
-    headers it includes, and to oracle/ref_shim/gpu_objects.h, so that
-    dda.h's own-directory includes find the stand-in for gpu_objects.h."""
-    inc = os.path.join(REF_OUT, "dda_inc")
+def _gpu_include_dir(gpu_dir: str) -> str:
+    """oracle/_ref/gpu_inc: gpu/ holds links to the reference's dda.h and
+    cameraCreateRay.h, the headers they include, and
+    oracle/ref_shim/gpu_objects.h, so that their own-directory includes
+    find the stand-in for gpu_objects.h."""
+    inc = os.path.join(REF_OUT, "gpu_inc")
     d = os.path.join(inc, "gpu")
     os.makedirs(d, exist_ok=True)
-    links = {h: os.path.join(gpu_dir, h) for h in DDA_HEADERS}
+    links = {h: os.path.join(gpu_dir, h) for h in GPU_HEADERS}
     links["gpu_objects.h"] = os.path.join(HERE, "ref_shim", "gpu_objects.h")
     for name, target in links.items():
         p = os.path.join(d, name)

@@ -1255,11 +1255,11 @@ void sphericalCoordsFromDirection(V3 d, float &theta, float &phi)
   phi = p < 0.f ? p + 2.f * (float)M_PI : p;
 }
 
-Ray primaryRay(const CamPre &c, Stream &rs, int px, int py, float invW, float invH,
-    bool centerPixel, float *screen = nullptr)
+// The ray of pixel (px, py) from one uniform4 draw r: r[0..1] the
+// sub-pixel offset, r[2..3] the aperture sample.
+Ray primaryRayFrom(const CamPre &c, const float r[4], int px, int py, float invW, float invH,
+    bool centerPixel, float *screen)
 {
-  float r[4];
-  uniform4(rs, r);
   const float sx0 = (centerPixel ? (float)px : (float)px + r[0]) * invW;
   const float sy0 = (centerPixel ? (float)py : (float)py + r[1]) * invH;
   if (screen) {
@@ -1287,6 +1287,14 @@ Ray primaryRay(const CamPre &c, Stream &rs, int px, int py, float invW, float in
     ray.org = c.p00 + sx * c.pdu + sy * c.pdv;
   }
   return ray;
+}
+
+Ray primaryRay(const CamPre &c, Stream &rs, int px, int py, float invW, float invH,
+    bool centerPixel, float *screen = nullptr)
+{
+  float r[4];
+  uniform4(rs, r);
+  return primaryRayFrom(c, r, px, py, invW, invH, centerPixel, screen);
 }
 
 struct SHit
@@ -3100,6 +3108,46 @@ void orc_project_on_grid(const float *p3, int n, const int *dims3, const float *
   for (int i = 0; i < n; i++)
     for (int a = 0; a < 3; a++)
       out3[3 * i + a] = projectAxis(p3[3 * i + a], box6[a], box6[3 + a], dims3[a]);
+}
+
+// makePrimaryRay + cameraCreateRay (gpu/cameraCreateRay.h:38-81) for n
+// samples (pixel x, pixel y, r0..r3) of a camera record (30 floats: region,
+// pos, dir, dir_00, dir_du, dir_dv, scaledAperture, aspect, pos_00, pos_du,
+// pos_dv; type 0 perspective, 1 orthographic) -> n x (org, dir, screen)
+void orc_primary_rays(const float *cam,
+    int type,
+    const float *samples,
+    int n,
+    float invW,
+    float invH,
+    int centerPixel,
+    float *out)
+{
+  CamPre c{};
+  c.type = type;
+  for (int i = 0; i < 4; i++)
+    c.region[i] = cam[i];
+  c.pos = ld3(cam + 4, 0);
+  c.dir = ld3(cam + 7, 0);
+  c.d00 = ld3(cam + 10, 0);
+  c.du = ld3(cam + 13, 0);
+  c.dv = ld3(cam + 16, 0);
+  c.aperture = cam[19];
+  c.aspect = cam[20];
+  c.p00 = ld3(cam + 21, 0);
+  c.pdu = ld3(cam + 24, 0);
+  c.pdv = ld3(cam + 27, 0);
+  for (int i = 0; i < n; i++) {
+    const float *s = samples + 6 * i;
+    float *o = out + 8 * i;
+    const Ray r = primaryRayFrom(c, s + 2, (int)s[0], (int)s[1], invW, invH, centerPixel != 0, o + 6);
+    o[0] = r.org.x;
+    o[1] = r.org.y;
+    o[2] = r.org.z;
+    o[3] = r.dir.x;
+    o[4] = r.dir.y;
+    o[5] = r.dir.z;
+  }
 }
 
 // dda3 (gpu/dda.h:43-122), the walk the delta-tracking march takes, for n

@@ -24,11 +24,14 @@
  * gpu/gpu_math.h helpers for the thin-lens aperture, the HDRI direction map
  * and the physically based cone sample, its macrocell projection
  * (gpu/uniformGrid.h), its macrocell walk (gpu/dda.h, compiled with
- * contraction on, as nvcc builds it) and its frame colour write's glm
- * calls, compiled in place (oracle/ref_tf.cpp, oracle/ref_dda.cpp,
- * oracle/ref_glm.cpp), made the fixtures tests/golden/tf_golden.npz,
- * math_golden.npz, dda_golden.npz and color_golden.npz, which the
- * functions here reproduce bit for bit.
+ * contraction on, as nvcc builds it), its primary-ray generation
+ * (gpu/cameraCreateRay.h, compiled without contraction, as the oracle and
+ * the library's kernels round it) and its frame colour write's glm calls,
+ * compiled in place (oracle/ref_tf.cpp, oracle/ref_dda.cpp,
+ * oracle/ref_camera.cpp, oracle/ref_glm.cpp), made the fixtures
+ * tests/golden/tf_golden.npz, math_golden.npz, dda_golden.npz,
+ * camera_golden.npz and color_golden.npz, which the functions here
+ * reproduce bit for bit.
  */
 #ifndef VRTX_ORACLE_H
 #define VRTX_ORACLE_H
@@ -285,6 +288,20 @@ void orc_uniform_sample_cone(const float *in4, int n, float *out3);
 /* projectOnGrid (uniformGrid.h:43-50) of n points onto a dims3 grid over
  * box6 (lo xyz, hi xyz) -> n integer cells. */
 void orc_project_on_grid(const float *p3, int n, const int *dims3, const float *box6, int *out3);
+/* makePrimaryRay + cameraCreateRay (cameraCreateRay.h:38-81) for n
+ * samples (pixel x, pixel y, r0..r3: the uniform4 draw) of a camera record
+ * (30 floats: region 4, pos 3, dir 3, dir_00 3, dir_du 3, dir_dv 3,
+ * scaledAperture, aspect, pos_00 3, pos_du 3, pos_dv 3; type 0
+ * perspective, 1 orthographic) over a frame of 1 / invW x 1 / invH pixels
+ * -> out n x (org xyz, dir xyz, screen xy). */
+void orc_primary_rays(const float *cam,
+    int type,
+    const float *samples,
+    int n,
+    float invW,
+    float invH,
+    int centerPixel,
+    float *out);
 /* dda3 (dda.h:43-122) for n rays (org xyz, dir xyz, tlo, thi) over a dims3
  * grid spanning box6: counts[i] cells per ray (at most maxCells), their
  * linear indices in cells[i * maxCells ...] and intervals in

@@ -220,6 +220,20 @@ def project_on_grid(points, dims, box) -> np.ndarray:
     return out
 
 
+def primary_rays(cam, cam_type, samples, inv_w, inv_h, center_pixel=False):
+    """Camera record (30 floats: region, pos, dir, dir_00, dir_du, dir_dv,
+    scaledAperture, aspect, pos_00, pos_du, pos_dv), type 0 perspective /
+    1 orthographic, (n, 6) samples (pixel x, pixel y, r0..r3) -> (n, 8)
+    (org, dir, screen): the primary ray of each sample."""
+    lib = load()
+    c = np.ascontiguousarray(cam, np.float32).reshape(30)
+    s = np.ascontiguousarray(samples, np.float32).reshape(-1, 6)
+    out = np.zeros((len(s), 8), np.float32)
+    lib.orc_primary_rays(_ptr(c), C.c_int(cam_type), _ptr(s), C.c_int(len(s)),
+                         C.c_float(inv_w), C.c_float(inv_h), C.c_int(int(center_pixel)), _ptr(out))
+    return out
+
+
 def dda_walk(rays, dims, box, max_cells):
     """(n, 8) rays (org, dir, tlo, thi) -> (counts (n,), cells (n, max_cells),
     t01 (n, max_cells, 2)): the macrocell walk of the delta-tracking march."""

@@ -5,7 +5,7 @@
 // tests/golden/make_dda_golden.py.
 //
 // dda.h includes gpu_objects.h, which needs OptiX. oracle/build.py therefore
-// compiles this file through oracle/_ref/dda_inc/gpu/, a directory of links
+// compiles this file through oracle/_ref/gpu_inc/gpu/, a directory of links
 // to the reference's dda.h, gpu_debug.h, gpu_math.h, gpu_decl.h and
 // uniformGrid.h beside a link to oracle/ref_shim/gpu_objects.h (the launch
 // queries gpu_debug.h calls); every other line is the reference's.

@@ -1,13 +1,25 @@
 // Test infrastructure: a host stand-in for the reference's
 // devices/rtx/gpu/gpu_objects.h, which needs OptiX, curand and the ANARI-SDK
-// (none present here). It is put ahead of the reference's own header only
-// when oracle/build.py compiles oracle/ref_dda.cpp, which needs from it no
-// more than gpu_debug.h does: the launch-index queries of debug() /
-// crosshair(), here a launch of one pixel. The vector, box and ray types
-// come from the reference's own gpu/gpu_math.h.
+// (none present here). oracle/build.py puts it ahead of the reference's own
+// header only when it compiles the harnesses oracle/ref_dda.cpp and
+// oracle/ref_camera.cpp. It declares what those reference headers use from
+// gpu_objects.h and nothing else:
+//  * the launch-index queries of gpu_debug.h's debug() / crosshair(), here a
+//    launch of one pixel;
+//  * the camera record cameraCreateRay reads (the same member names; the
+//    perspective and orthographic parts side by side rather than in a
+//    union, since the harness fills them by name);
+//  * the frame record and screen sample makePrimaryRay reads, with
+//    curand_uniform4 returning the four numbers the harness put in the
+//    sample's generator state, so that a harness call chooses the
+//    sub-pixel offset and aperture sample.
+// The vector, box and ray types come from the reference's own
+// gpu/gpu_math.h.
 #pragma once
 
 #include "gpu/gpu_math.h"
+
+#include <glm/ext/vector_uint2.hpp>
 
 namespace visrtx_host_shim {
 struct LaunchIndex
@@ -25,3 +37,80 @@ inline visrtx_host_shim::LaunchIndex optixGetLaunchDimensions()
 {
   return {1u, 1u, 1u};
 }
+
+// CUDA's float4 and a generator whose next uniform4 draw is preset
+struct float4
+{
+  float x, y, z, w;
+};
+
+namespace visrtx_host_shim {
+struct PresetUniform4
+{
+  ::float4 next;
+};
+} // namespace visrtx_host_shim
+
+inline ::float4 curand_uniform4(visrtx_host_shim::PresetUniform4 *s)
+{
+  return s->next;
+}
+
+namespace visrtx {
+
+using RandState = visrtx_host_shim::PresetUniform4;
+
+enum class CameraType
+{
+  PERSPECTIVE,
+  ORTHOGRAPHIC,
+  UNKNOWN
+};
+
+struct PerspectiveCameraGPUData
+{
+  vec3 dir_du;
+  vec3 dir_dv;
+  vec3 dir_00;
+  float scaledAperture;
+  float aspect;
+};
+
+struct OrthographicCameraGPUData
+{
+  vec3 pos_du;
+  vec3 pos_dv;
+  vec3 pos_00;
+};
+
+struct CameraGPUData
+{
+  CameraType type{CameraType::UNKNOWN};
+  vec4 region;
+  vec3 pos;
+  vec3 dir;
+  vec3 up;
+  PerspectiveCameraGPUData perspective;
+  OrthographicCameraGPUData orthographic;
+};
+
+struct FramebufferGPUData
+{
+  glm::vec2 invSize;
+};
+
+struct FrameGPUData
+{
+  FramebufferGPUData fb;
+  CameraGPUData *camera;
+};
+
+struct ScreenSample
+{
+  glm::uvec2 pixel;
+  glm::vec2 screen;
+  mutable RandState rs;
+  const FrameGPUData *frameData;
+};
+
+} // namespace visrtx

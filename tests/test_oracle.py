@@ -209,6 +209,37 @@ def test_thin_lens_and_hdri_helpers_match_reference_gpu_math():
         assert np.array_equal(got, z[f"grid{k}_cells"]), k
 
 
+def test_primary_rays_match_reference_camera():
+    """The oracle's primary ray (makePrimaryRay + cameraCreateRay: the pixel
+    and sub-pixel offset to a screen position, the image region, the
+    perspective direction with the thin-lens aperture sample, the
+    orthographic origin, glm's normalize) equals, bit for bit, the
+    reference's own gpu/cameraCreateRay.h compiled on the host without
+    contraction (fixtures by tests/golden/make_camera_golden.py): 3960 rays
+    from pinhole, thin-lens and orthographic cameras over full and partial
+    image regions, three frame sizes, the pixel-centre flag on and off,
+    edge pixels and uniform draws of 2^-24 and 1. The same code built with
+    contraction, the kind of rounding an nvcc build applies, gives other
+    bits on 2393 of those rays, all within 5e-7 of the vector's largest
+    component: the gap the parity tolerances cover."""
+    z = np.load(os.path.join(GOLDEN, "camera_golden.npz"))
+    n = fused_differ = 0
+    for i in range(int(z["num_cases"])):
+        typ, w, h, center = (int(v) for v in z[f"c{i}_meta"])
+        got = O.primary_rays(z[f"c{i}_cam"], typ, z[f"c{i}_samples"],
+                             np.float32(1) / np.float32(w), np.float32(1) / np.float32(h), center)
+        assert np.array_equal(got.view(np.uint32), z[f"c{i}_rays"].view(np.uint32)), i
+        fused = z[f"c{i}_rays_fused"]
+        fused_differ += int((got.view(np.uint32) != fused.view(np.uint32)).any(1).sum())
+        for a, b in ((0, 3), (3, 6)):
+            scale = np.abs(got[:, a:b]).max(1)
+            gap = np.abs(got[:, a:b] - fused[:, a:b]).max(1)
+            assert (gap <= 5e-7 * scale).all(), i
+        assert np.array_equal(got[:, 6:], fused[:, 6:]), i
+        n += len(got)
+    assert (n, fused_differ) == (3960, 2393)
+
+
 def test_macrocell_walk_matches_reference_dda():
     """The oracle's macrocell walk (dda3, which the delta-tracking march
     runs over the majorant grid) visits the same cells with the same
