@@ -339,6 +339,29 @@ VRTX_API void vrtxUnmapFrame(VRTXDevice d, VRTXFrame f, const char *channel);
 VRTX_API uint64_t vrtxDebugCopyAccel(
     VRTXDevice d, VRTXObject world, int kind, void *dst, uint64_t capacity);
 
+/* Image texels as the device stages them at commit, computed on the host
+ * (no device, no GPU), for checking. background = 0: an image sampler's
+ * image, n texels of elementType (FLOAT32..FLOAT32_VEC4, UFIXED8,
+ * UFIXED16, UFIXED8_VEC4, UFIXED8_RGBA_SRGB); float types go to outFloat
+ * as n x 4 floats (missing channels 0, alpha 1) and return 1; every other
+ * type goes to outBytes as n x 4 bytes that the texture reads as
+ * normalised float (8-bit values as they are, sRGB bytes -- alpha too --
+ * linearised and truncated to 8 bits, 16-bit values truncated from
+ * (c / 65535) * 255; missing channels 0, alpha 255) and returns 0.
+ * background = 1: the renderer's background image (FLOAT32_VEC3/4,
+ * UFIXED8_VEC4, UFIXED8_RGBA_SRGB) to outBytes as n x 4 bytes (floats
+ * truncated from c * 255, clamped to [0, 255]), returning 0. Replaces
+ * Image1D/2D/3D::finalize's and Renderer::finalize's staging
+ * (scene/surface/material/sampler/Image2D.cpp:70-78, Renderer.cpp:173-179,
+ * utility/CudaImageTexture.cpp:43-111) as a separate entry for checking.
+ * Returns -1 for an unsupported type or a missing buffer. */
+VRTX_API int vrtxDebugStageImage(int elementType,
+    int background,
+    const void *texels,
+    uint64_t n,
+    float *outFloat,
+    uint8_t *outBytes);
+
 /* The 256-entry RGBA table a transferFunction1D volume's colour / opacity
  * arrays discretise to at commit, computed on the host (no device, no GPU):
  * the colour array (numColor >= 2 entries of colorComponents = 3 or 4

@@ -24,10 +24,17 @@ output only in oracle/_ref/:
     ref_camera.cpp runs it without contraction (libcamref.so, each
     operation rounded once, as the oracle and the library's kernels round
     it) and with it (libcamref_fused.so, to size the gap).
-  Both headers include the OptiX-bound gpu_objects.h, so these two are
-  compiled through oracle/_ref/gpu_inc/gpu/, links to the reference's
-  headers beside a link to oracle/ref_shim/gpu_objects.h, made for the
-  compile and removed after it.
+  * its image staging (devices/rtx/utility/CudaImageTexture.cpp,
+    convertComponentUint8 / Float and transformToStagingBuffer*):
+    ref_image.cpp includes that .cpp (its staging functions are
+    file-local) and runs them (libimgref.so, linked to the CUDA runtime
+    for the .cpp's array and texture calls, which it never makes).
+  Those headers include the OptiX-bound gpu_objects.h, and the .cpp its
+  helium-bound CudaImageTexture.h, so these are compiled through
+  oracle/_ref/gpu_inc/{gpu,utility}/, links to the reference's files beside
+  links to the stand-ins oracle/ref_shim/gpu_objects.h and
+  CudaImageTexture.h, made for the compile and removed after it;
+  oracle/ref_shim/anari/anari.h names the ANARI data types.
 The GPU machine has no reference tree and never builds them.
 """
 from __future__ import annotations
@@ -68,12 +75,15 @@ REF_GLM_LIB = os.path.join(REF_OUT, "libglmref.so")
 REF_DDA_LIB = os.path.join(REF_OUT, "libddaref.so")
 REF_CAM_LIB = os.path.join(REF_OUT, "libcamref.so")
 REF_CAM_FUSED_LIB = os.path.join(REF_OUT, "libcamref_fused.so")
+REF_IMG_LIB = os.path.join(REF_OUT, "libimgref.so")
 GPU_HEADERS = ("dda.h", "gpu_debug.h", "gpu_math.h", "gpu_decl.h", "uniformGrid.h",
                "cameraCreateRay.h")
+UTILITY_FILES = ("CudaImageTexture.cpp", "AnariTypeHelpers.h")
+CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 
 
 def _compile_ref(src: str, out: str, incs: list[str], contract: str = "off",
-                 deps: tuple[str, ...] = ()) -> str:
+                 deps: tuple[str, ...] = (), libs: tuple[str, ...] = ()) -> str:
     os.makedirs(REF_OUT, exist_ok=True)
     if os.path.exists(out) and all(os.path.getmtime(out) >= os.path.getmtime(f)
                                    for f in (src, *deps)):
@@ -84,7 +94,7 @@ def _compile_ref(src: str, out: str, incs: list[str], contract: str = "off",
         cmd.append("-mfma")
     for i in incs:
         cmd += ["-I", i]
-    cmd += ["-o", tmp, src, "-lpthread"]
+    cmd += ["-o", tmp, src, *libs, "-lpthread"]
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
         raise RuntimeError("oracle/_ref build failed:\n" + res.stdout + res.stderr)
@@ -97,8 +107,9 @@ def build_ref(tree: str | None = None) -> str | None:
     NanoVDB headers), oracle/_ref/libtfref.so (ref_tf.cpp over its
     transfer-function helpers), oracle/_ref/libglmref.so (ref_glm.cpp
     over its vendored glm), oracle/_ref/libddaref.so (ref_dda.cpp over
-    its dda.h) and oracle/_ref/libcamref{,_fused}.so (ref_camera.cpp over
-    its cameraCreateRay.h) from the reference tree `tree` (default
+    its dda.h), oracle/_ref/libcamref{,_fused}.so (ref_camera.cpp over
+    its cameraCreateRay.h) and oracle/_ref/libimgref.so (ref_image.cpp over
+    its CudaImageTexture.cpp) from the reference tree `tree` (default
     REF_TREE); returns the NanoVDB harness's path, or None when the
     reference tree is absent."""
     root = tree or REF_TREE
@@ -111,34 +122,49 @@ def build_ref(tree: str | None = None) -> str | None:
     if os.path.isfile(os.path.join(rtx, "utility", "colorMapHelpers.h")) and os.path.isdir(glm):
         _compile_ref(os.path.join(HERE, "ref_tf.cpp"), REF_TF_LIB, [rtx, glm])
         _compile_ref(os.path.join(HERE, "ref_glm.cpp"), REF_GLM_LIB, [glm])
-        if all(os.path.isfile(os.path.join(rtx, "gpu", h)) for h in GPU_HEADERS):
+        if all(os.path.isfile(os.path.join(rtx, "gpu", h)) for h in GPU_HEADERS) and all(
+                os.path.isfile(os.path.join(rtx, "utility", f)) for f in UTILITY_FILES):
             # the links point into the reference tree: made for the compile
             # only, so that no dangling link is left in oracle/_ref
-            inc = _gpu_include_dir(os.path.join(rtx, "gpu"))
-            shim = (os.path.join(HERE, "ref_shim", "gpu_objects.h"),)
+            inc = _gpu_include_dir(rtx)
+            shims = os.path.join(HERE, "ref_shim")
+            shim = (os.path.join(shims, "gpu_objects.h"),)
             cam = os.path.join(HERE, "ref_camera.cpp")
+            cuda_lib = os.path.join(CUDA_HOME, "lib64")
             try:
                 _compile_ref(os.path.join(HERE, "ref_dda.cpp"), REF_DDA_LIB, [inc, glm],
                              contract="fast", deps=shim)
                 _compile_ref(cam, REF_CAM_LIB, [inc, glm], contract="off", deps=shim)
                 _compile_ref(cam, REF_CAM_FUSED_LIB, [inc, glm], contract="fast", deps=shim)
+                if os.path.isdir(os.path.join(CUDA_HOME, "include")):
+                    _compile_ref(os.path.join(HERE, "ref_image.cpp"), REF_IMG_LIB,
+                                 [inc, shims, glm, os.path.join(CUDA_HOME, "include")],
+                                 deps=(os.path.join(shims, "CudaImageTexture.h"),
+                                       os.path.join(shims, "anari", "anari.h")),
+                                 libs=(f"-L{cuda_lib}", f"-Wl,-rpath,{cuda_lib}", "-lcudart"))
             finally:
                 shutil.rmtree(inc, ignore_errors=True)
     return lib
 
 
-def _gpu_include_dir(gpu_dir: str) -> str:
+def _gpu_include_dir(rtx: str) -> str:
     """oracle/_ref/gpu_inc: gpu/ holds links to the reference's dda.h and
     cameraCreateRay.h, the headers they include, and
-    oracle/ref_shim/gpu_objects.h, so that their own-directory includes
-    find the stand-in for gpu_objects.h."""
+    oracle/ref_shim/gpu_objects.h; utility/ links to its
+    CudaImageTexture.cpp and AnariTypeHelpers.h and to
+    oracle/ref_shim/CudaImageTexture.h: their own-directory includes find
+    the stand-ins."""
     inc = os.path.join(REF_OUT, "gpu_inc")
-    d = os.path.join(inc, "gpu")
-    os.makedirs(d, exist_ok=True)
-    links = {h: os.path.join(gpu_dir, h) for h in GPU_HEADERS}
-    links["gpu_objects.h"] = os.path.join(HERE, "ref_shim", "gpu_objects.h")
+    shims = os.path.join(HERE, "ref_shim")
+    links = {os.path.join("gpu", h): os.path.join(rtx, "gpu", h) for h in GPU_HEADERS}
+    links[os.path.join("gpu", "gpu_objects.h")] = os.path.join(shims, "gpu_objects.h")
+    for f in UTILITY_FILES:
+        links[os.path.join("utility", f)] = os.path.join(rtx, "utility", f)
+    links[os.path.join("utility", "CudaImageTexture.h")] = os.path.join(
+        shims, "CudaImageTexture.h")
     for name, target in links.items():
-        p = os.path.join(d, name)
+        p = os.path.join(inc, name)
+        os.makedirs(os.path.dirname(p), exist_ok=True)
         if os.path.lexists(p):
             os.remove(p)
         os.symlink(target, p)

@@ -2301,11 +2301,72 @@ void hwCornerWeights(int ndim, const int w[3], int out[8])
   }
 }
 
+// glm::convertSRGBToLinear of one component (gamma 2.4), as the
+// reference's image staging calls it
+float srgbToLinearGlm(float x)
+{
+  return x <= 0.04045f ? x * 0.07739938080495356f
+                       : std::pow((x + 0.055f) * 0.94786729857819905f, 2.4f);
+}
+
+// convertComponentUint8 (utility/CudaImageTexture.cpp:43-57) of component c
+// of one texel of element type et: 8-bit values as they are, sRGB bytes
+// linearised and truncated to 8 bits, 16-bit values truncated from
+// (c / 65535) * 255
+uint8_t stageByte(int et, const uint8_t *texel, int c)
+{
+  if (et == 223) {
+    uint16_t v;
+    std::memcpy(&v, texel + 2 * c, 2);
+    return (uint8_t)((v / 65535.f) * 255.f);
+  }
+  if (et == 261)
+    return (uint8_t)(srgbToLinearGlm(texel[c] / 255.f) * 255.f);
+  return texel[c];
+}
+
+// the texture unit's normalised-float read of 8-bit texels: point reads
+// b / 255; linear filters the bytes as integers, the weighted sum F (weights
+// summing to 256) scaled to a 16-bit normalised value
+// round-half-up(F * 257 / 256) and read as that / 65535
+float unorm8Point(int b)
+{
+  return (float)((double)b / 255.0);
+}
+
+float unorm8Linear(int64_t F)
+{
+  const int64_t r16 = (F * 257 + 128) >> 8;
+  return (float)((double)r16 / 65535.0);
+}
+
 V4 texSample(const OrcSampler &sm, int ndim, const float tc[3])
 {
   int i0[3] = {0, 0, 0}, i1[3] = {0, 0, 0}, w[3] = {0, 0, 0};
   for (int k = 0; k < ndim; k++)
     hwTap(tc[k], sm.dims[k], sm.wrap[k], sm.filter != 0, i0[k], i1[k], w[k]);
+  if (sm.image8) {
+    auto at8 = [&](int x, int y, int z, int c) {
+      return (int)sm.image8[4 * (((size_t)z * sm.dims[1] + y) * sm.dims[0] + x) + c];
+    };
+    float out[4];
+    if (sm.filter == 0) {
+      for (int c = 0; c < 4; c++)
+        out[c] = unorm8Point(at8(i0[0], i0[1], i0[2], c));
+    } else {
+      int cw[8];
+      hwCornerWeights(ndim, w, cw);
+      for (int c = 0; c < 4; c++) {
+        int64_t F = 0;
+        for (int q = 0; q < 8; q++)
+          if (cw[q])
+            F += (int64_t)cw[q]
+                * at8((q & 1) ? i1[0] : i0[0], (q & 2) ? i1[1] : i0[1], (q & 4) ? i1[2] : i0[2], c);
+        out[c] = unorm8Linear(F);
+      }
+    }
+    return {out[0], out[1], out[2], out[3]};
+  }
   auto at = [&](int x, int y, int z, int c) {
     return sm.image[4 * (((size_t)z * sm.dims[1] + y) * sm.dims[0] + x) + c];
   };
@@ -2342,7 +2403,7 @@ V4 evaluateSampler(const SceneCtx &S, const SHit &sh, const OrcSampler &sm)
   V4 r{0.f, 0.f, 0.f, 1.f};
   const V4 tc = affine4(sm.inT, readAttribute(S, sh, sm.attribute), sm.inO);
   const float t3[3] = {tc.x, tc.y, tc.z};
-  if (sm.type >= 1 && sm.type <= 3 && sm.image)
+  if (sm.type >= 1 && sm.type <= 3 && (sm.image || sm.image8))
     r = texSample(sm, sm.type, t3);
   else if (sm.type == 5)
     r = attrValue(sm.prim, sh.prim + sm.primOffset, r);
@@ -2462,7 +2523,8 @@ V3 hdriRadiance(const SceneCtx &S, int li, V3 dir)
 
 // the background image as the device stages it (acquireCUDAArrayUint8,
 // utility/CudaImageTexture.cpp:43-93): RGBA8, float components truncated
-// from c * 255 (clamped), sRGB bytes linearised, alpha 255 for three channels
+// from c * 255 (clamped), sRGB bytes (alpha too) linearised, alpha 255 for
+// three channels
 uint8_t bgTexel(const OrcRenderer &R, size_t i, int c)
 {
   const int nc = R.bgType == 242 ? 3 : 4;
@@ -2472,14 +2534,7 @@ uint8_t bgTexel(const OrcRenderer &R, size_t i, int c)
     const float s = ((const float *)R.bgImage)[i * nc + c] * 255.f;
     return (uint8_t)(s >= 255.f ? 255.f : (s > 0.f ? s : 0.f));
   }
-  const uint8_t b = ((const uint8_t *)R.bgImage)[i * 4 + c];
-  if (R.bgType == 261 && c < 3) {
-    const float x = b / 255.f;
-    const float lin = x <= 0.04045f ? x * 0.07739938080495356f
-                                    : std::pow((x + 0.055f) * 0.94786729857819905f, 2.4f);
-    return (uint8_t)(lin * 255.f);
-  }
-  return b;
+  return stageByte(R.bgType, (const uint8_t *)R.bgImage + i * 4, c);
 }
 
 // normalised-float reads of the RGBA8 image: linear, clamped, normalised
@@ -2500,8 +2555,7 @@ V4 bgImageAt(const OrcRenderer &R, float u, float v)
     auto at = [&](int x, int y) { return (int64_t)bgTexel(R, (size_t)y * W + x, c); };
     const int64_t F = cw[0] * at(x0, y0) + cw[1] * at(x1, y0) + cw[2] * at(x0, y1)
         + cw[3] * at(x1, y1);
-    const int64_t r16 = (F * 257 + 128) >> 8;
-    out[c] = (float)((double)r16 / 65535.0);
+    out[c] = unorm8Linear(F);
   }
   return {out[0], out[1], out[2], out[3]};
 }
@@ -3108,6 +3162,53 @@ void orc_project_on_grid(const float *p3, int n, const int *dims3, const float *
   for (int i = 0; i < n; i++)
     for (int a = 0; a < 3; a++)
       out3[3 * i + a] = projectAxis(p3[3 * i + a], box6[a], box6[3 + a], dims3[a]);
+}
+
+// Image1D/2D/3D::finalize's staging (sampler/Image2D.cpp:70-78 with
+// transformToStagingBuffer{Float,Uint8}, utility/CudaImageTexture.cpp:76-111)
+int orc_stage_image(int et, const void *texels, uint64_t n, float *outFloat, uint8_t *outBytes)
+{
+  int ch = 0;
+  if (et >= 240 && et <= 243)
+    ch = et - 239;
+  else if (et == 221 || et == 223)
+    ch = 1;
+  else if (et == 260 || et == 261)
+    ch = 4;
+  if (!ch || (n && !texels))
+    return -1;
+  const uint8_t *src = (const uint8_t *)texels;
+  if (et >= 240 && et <= 243) {
+    if (!outFloat)
+      return -1;
+    for (uint64_t i = 0; i < n; i++) {
+      float v[4] = {0.f, 0.f, 0.f, 1.f};
+      std::memcpy(v, src + i * ch * 4, ch * 4);
+      std::memcpy(outFloat + 4 * i, v, 16);
+    }
+    return 1;
+  }
+  if (!outBytes)
+    return -1;
+  const int bytes = et == 223 ? 2 : 1;
+  for (uint64_t i = 0; i < n; i++)
+    for (int c = 0; c < 4; c++)
+      outBytes[4 * i + c] = c < ch ? stageByte(et, src + i * ch * bytes, c) : (c == 3 ? 255 : 0);
+  return 0;
+}
+
+// Renderer::finalize's background staging (bgTexel) of n texels
+int orc_stage_background(int et, const void *texels, uint64_t n, uint8_t *out)
+{
+  if (et != 242 && et != 243 && et != 260 && et != 261)
+    return -1;
+  OrcRenderer R{};
+  R.bgImage = texels;
+  R.bgType = et;
+  for (uint64_t i = 0; i < n; i++)
+    for (int c = 0; c < 4; c++)
+      out[4 * i + c] = bgTexel(R, i, c);
+  return 0;
 }
 
 // makePrimaryRay + cameraCreateRay (gpu/cameraCreateRay.h:38-81) for n

@@ -26,12 +26,13 @@
  * (gpu/uniformGrid.h), its macrocell walk (gpu/dda.h, compiled with
  * contraction on, as nvcc builds it), its primary-ray generation
  * (gpu/cameraCreateRay.h, compiled without contraction, as the oracle and
- * the library's kernels round it) and its frame colour write's glm calls,
+ * the library's kernels round it), its image staging
+ * (utility/CudaImageTexture.cpp) and its frame colour write's glm calls,
  * compiled in place (oracle/ref_tf.cpp, oracle/ref_dda.cpp,
- * oracle/ref_camera.cpp, oracle/ref_glm.cpp), made the fixtures
- * tests/golden/tf_golden.npz, math_golden.npz, dda_golden.npz,
- * camera_golden.npz and color_golden.npz, which the functions here
- * reproduce bit for bit.
+ * oracle/ref_camera.cpp, oracle/ref_image.cpp, oracle/ref_glm.cpp), made
+ * the fixtures tests/golden/tf_golden.npz, math_golden.npz,
+ * dda_golden.npz, camera_golden.npz, image_golden.npz and
+ * color_golden.npz, which the functions here reproduce bit for bit.
  */
 #ifndef VRTX_ORACLE_H
 #define VRTX_ORACLE_H
@@ -101,14 +102,16 @@ typedef struct OrcAttr {
 
 /* A material sampler: type 1 image1D, 2 image2D, 3 image3D, 4 transform,
  * 5 primitive; input attribute slot; column-major in / out maps; the image
- * as float4 texels (x fastest) with its dims, filter (0 nearest, 1 linear)
- * and wrap modes (0 clampToEdge, 1 repeat, 2 mirrorRepeat); or the
- * primitive array and offset. */
+ * as staged (orc_stage_image): float4 texels (image) or RGBA8 texels read
+ * as normalised float (image8), x fastest, with its dims, filter
+ * (0 nearest, 1 linear) and wrap modes (0 clampToEdge, 1 repeat,
+ * 2 mirrorRepeat); or the primitive array and offset. */
 typedef struct OrcSampler {
   int type;
   int attribute;
   float inT[16], inO[4], outT[16], outO[4];
   const float *image;
+  const uint8_t *image8;
   int dims[3];
   int filter;
   int wrap[3];
@@ -288,6 +291,18 @@ void orc_uniform_sample_cone(const float *in4, int n, float *out3);
 /* projectOnGrid (uniformGrid.h:43-50) of n points onto a dims3 grid over
  * box6 (lo xyz, hi xyz) -> n integer cells. */
 void orc_project_on_grid(const float *p3, int n, const int *dims3, const float *box6, int *out3);
+/* An image sampler's staging (Image2D.cpp:70-78, CudaImageTexture.cpp:43-111)
+ * of n texels of element type et (this library's codes: 240..243 float32
+ * x1..x4, 221 ufixed8, 223 ufixed16, 260 ufixed8 x4, 261 sRGB ufixed8 x4):
+ * float types to outFloat (n x 4, missing channels 0, alpha 1), returning
+ * 1; the others to outBytes (n x 4 RGBA8, missing channels 0, alpha 255),
+ * returning 0; -1 for another type. */
+int orc_stage_image(int et, const void *texels, uint64_t n, float *outFloat, uint8_t *outBytes);
+/* The renderer's background image staging (Renderer.cpp:173-179,
+ * CudaImageTexture.cpp:43-93) of n texels of et (242 / 243 float32 x3 / x4,
+ * 260 ufixed8 x4, 261 sRGB ufixed8 x4) to out (n x 4 RGBA8); -1 for another
+ * type. */
+int orc_stage_background(int et, const void *texels, uint64_t n, uint8_t *out);
 /* makePrimaryRay + cameraCreateRay (cameraCreateRay.h:38-81) for n
  * samples (pixel x, pixel y, r0..r3: the uniform4 draw) of a camera record
  * (30 floats: region 4, pos 3, dir 3, dir_00 3, dir_du 3, dir_dv 3,

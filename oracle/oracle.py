@@ -36,7 +36,8 @@ class OrcAttr(C.Structure):
 class OrcSampler(C.Structure):
     _fields_ = [("type", C.c_int), ("attribute", C.c_int), ("inT", C.c_float * 16),
                 ("inO", C.c_float * 4), ("outT", C.c_float * 16), ("outO", C.c_float * 4),
-                ("image", C.c_void_p), ("dims", C.c_int * 3), ("filter", C.c_int),
+                ("image", C.c_void_p), ("image8", C.c_void_p), ("dims", C.c_int * 3),
+                ("filter", C.c_int),
                 ("wrap", C.c_int * 3), ("prim", OrcAttr), ("primOffset", C.c_uint32)]
 
 
@@ -69,11 +70,35 @@ def _column_major(m):
     return (C.c_float * 16)(*np.ascontiguousarray(m.T).ravel().tolist())
 
 
+def stage_image(et, texels):
+    """An image sampler's texels as staged (orc_stage_image): (n, 4) float32
+    for float element types, else (n, 4) uint8 read as normalised float."""
+    lib = load()
+    t = np.ascontiguousarray(texels)
+    n = t.shape[0]
+    f4 = np.zeros((n, 4), np.float32)
+    u8 = np.zeros((n, 4), np.uint8)
+    r = lib.orc_stage_image(C.c_int(et), _ptr(t), C.c_uint64(n), _ptr(f4), _ptr(u8))
+    if r < 0:
+        raise ValueError(f"image element type {et} is not supported")
+    return f4 if r == 1 else u8
+
+
+def stage_background(et, texels):
+    """The renderer's background image staged as RGBA8 (orc_stage_background)."""
+    lib = load()
+    t = np.ascontiguousarray(texels)
+    n = t.shape[0]
+    out = np.zeros((n, 4), np.uint8)
+    if lib.orc_stage_background(C.c_int(et), _ptr(t), C.c_uint64(n), _ptr(out)) < 0:
+        raise ValueError(f"background element type {et} is not supported")
+    return out
+
+
 def _pack_sampler(o, sp, keep):
-    """Fills an OrcSampler from a SamplerSpec. Image texels are staged as
-    float4 the way the device stages them: missing channels 0 (alpha 1),
-    8- and 16-bit values divided by 255 / 65535 in float32."""
-    from visrtx_gb300.scenes import attr_type
+    """Fills an OrcSampler from a SamplerSpec, its image staged as the
+    device stages it (stage_image)."""
+    from visrtx_gb300.scenes import sampler_image_type
 
     o.type = _SAMPLER_TYPES[sp.type]
     o.attribute = _SAMPLER_SLOTS[sp.attribute]
@@ -83,19 +108,14 @@ def _pack_sampler(o, sp, keep):
     o.outO = (C.c_float * 4)(*map(float, sp.out_offset))
     nd = sp.image_dims
     if nd:
-        tex, c = sp.texels()
+        tex, _ = sp.texels()
         img = np.asarray(sp.image)
-        n = tex.shape[0]
-        t4 = np.zeros((n, 4), np.float32)
-        t4[:, 3] = 1.0
-        src = tex.reshape(n, c)
-        if src.dtype == np.float32:
-            t4[:, :c] = src
+        staged = stage_image(sampler_image_type(sp), tex)
+        keep.append(staged)
+        if staged.dtype == np.float32:
+            o.image = _ptr(staged)
         else:
-            scale = np.float32(65535.0 if src.dtype == np.uint16 else 255.0)
-            t4[:, :c] = src.astype(np.float32) / scale
-        keep.append(t4)
-        o.image = _ptr(t4)
+            o.image8 = _ptr(staged)
         shape = img.shape[:nd][::-1]
         o.dims = (C.c_int * 3)(*(list(shape) + [1] * (3 - nd)))
         o.filter = 0 if sp.filter == "nearest" else 1

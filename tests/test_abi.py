@@ -169,6 +169,36 @@ def test_force_init_initialises_at_commit(built):
     dev.release()
 
 
+def test_library_image_staging_matches_reference(built):
+    """The library's image staging (the host code an image sampler and the
+    renderer's background image commit with, through vrtxDebugStageImage,
+    no GPU involved) equals bit for bit the reference's own
+    utility/CudaImageTexture.cpp staging (tests/golden/image_golden.npz),
+    including its choice of float or 8-bit texels; unsupported types and
+    missing buffers return -1."""
+    import numpy as np
+
+    from tests.test_oracle import image_golden_cases
+    from visrtx_gb300 import _lib as L
+
+    lib = L.load()
+    for name, et, bg, texels, want in image_golden_cases():
+        t = np.ascontiguousarray(texels)
+        f4 = np.zeros((len(t), 4), np.float32)
+        u8 = np.zeros((len(t), 4), np.uint8)
+        rc = lib.vrtxDebugStageImage(et, bg, t.ctypes.data, len(t), f4.ctypes.data,
+                                     u8.ctypes.data)
+        assert rc == (1 if want.dtype == np.float32 else 0), name
+        got = f4 if rc == 1 else u8
+        assert np.array_equal(got.view(np.uint8), want.view(np.uint8)), name
+    one = np.zeros(4, np.float32)
+    assert lib.vrtxDebugStageImage(L.FLOAT64, 0, one.ctypes.data, 1, one.ctypes.data,
+                                   None) == -1
+    assert lib.vrtxDebugStageImage(L.UFIXED8, 0, one.ctypes.data, 1, one.ctypes.data,
+                                   None) == -1
+    assert lib.vrtxDebugStageImage(L.UFIXED16, 1, one.ctypes.data, 1, None, None) == -1
+
+
 def test_library_tf_discretization_matches_reference(built):
     """The library's TF discretisation (the host code a transferFunction1D
     volume commits with, through vrtxDebugDiscretizeTF, no GPU involved)

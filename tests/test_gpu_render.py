@@ -336,6 +336,17 @@ SAMPLER_CASES = {
         wrap=("repeat", "repeat", "clampToEdge"),
         in_transform=np.diag([3.0, 2.5, 1.0, 1.0]).astype(np.float32),
         in_offset=(-0.7, 0.3, 0.0, 0.0)), 1),
+    # sRGB bytes (alpha too) linearised and truncated to 8 bits at staging
+    "image2D-linear-clamp-srgb": (2, lambda rng, np_: S.SamplerSpec(
+        "image2D", image=rng.integers(0, 256, (8, 12, 4)).astype(np.uint8), image_srgb=True,
+        in_transform=np.diag([1.3, 1.1, 1.0, 1.0]).astype(np.float32),
+        in_offset=(-0.1, -0.05, 0.0, 0.0)), 1),
+    # 16-bit values truncated to 8 bits at staging
+    "image1D-nearest-repeat-u16": (1, lambda rng, np_: S.SamplerSpec(
+        "image1D", image=rng.integers(0, 65536, 40).astype(np.uint16), filter="nearest",
+        wrap=("repeat", "clampToEdge", "clampToEdge"),
+        in_transform=np.diag([2.2, 1.0, 1.0, 1.0]).astype(np.float32),
+        in_offset=(-0.3, 0.0, 0.0, 0.0)), 1),
     "image1D-linear-clamp-f3": (1, lambda rng, np_: S.SamplerSpec(
         "image1D", image=rng.random((32, 3)).astype(np.float32),
         in_transform=np.diag([1.4, 1.0, 1.0, 1.0]).astype(np.float32),

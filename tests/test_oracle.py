@@ -209,6 +209,46 @@ def test_thin_lens_and_hdri_helpers_match_reference_gpu_math():
         assert np.array_equal(got, z[f"grid{k}_cells"]), k
 
 
+def image_golden_cases():
+    """The cases of tests/golden/image_golden.npz (make_image_golden.py):
+    (name, element type, background, texels, expected n x 4 texels). The
+    reference's staging holds nc components per texel; a fetch of its
+    nc-channel array returns 0 for the missing colour channels and 1 (255)
+    for a missing alpha, which is the n x 4 layout here."""
+    z = np.load(os.path.join(GOLDEN, "image_golden.npz"))
+    out = []
+    for name in z["names"]:
+        et, bg, nc, uses_float = (int(v) for v in z[f"{name}_meta"])
+        staged = z[f"{name}_staged"]
+        want = np.zeros((len(staged), 4), staged.dtype)
+        want[:, :staged.shape[1]] = staged
+        if staged.shape[1] < 4:
+            want[:, 3] = 1.0 if uses_float else 255
+        out.append((str(name), et, bg, z[f"{name}_texels"], want))
+    return out
+
+
+def test_image_staging_matches_reference():
+    """The oracle stages sampler and background images as the reference's
+    own utility/CudaImageTexture.cpp does (compiled on the host; fixtures by
+    tests/golden/make_image_golden.py), bit for bit: sampler images of a
+    float type as float texels, every other type as 8-bit texels read as
+    normalised float -- 8-bit values as they are, sRGB bytes (alpha too)
+    linearised and truncated, 16-bit values truncated to 8 bits, over every
+    input value -- and background images always as 8-bit."""
+    cases = image_golden_cases()
+    assert len(cases) == 12
+    for name, et, bg, texels, want in cases:
+        got = O.stage_background(et, texels) if bg else O.stage_image(et, texels)
+        assert got.dtype == want.dtype, name
+        assert np.array_equal(got.view(np.uint8), want.view(np.uint8)), name
+    # the truncations the fixtures hold: dark sRGB bytes stage to 0, and
+    # the alpha byte is linearised with the colour
+    srgb = dict((c[0], c) for c in cases)["sampler_srgb8x4"]
+    assert (srgb[4][:13, 0] == 0).all() and srgb[4][13, 0] == 1 and srgb[4][128, 0] == 55
+    assert srgb[3][192, 3] == 128 and srgb[4][192, 3] == 55
+
+
 def test_primary_rays_match_reference_camera():
     """The oracle's primary ray (makePrimaryRay + cameraCreateRay: the pixel
     and sub-pixel offset to a screen position, the image region, the

@@ -100,6 +100,8 @@ SIGNATURES = {
                                         C.c_void_p]),
     "vrtxDebugWriteColors": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_int, C.c_int,
                                        C.c_void_p]),
+    "vrtxDebugStageImage": (C.c_int, [C.c_int, C.c_int, C.c_void_p, C.c_uint64, C.c_void_p,
+                                      C.c_void_p]),
     "vrtxDebugRadixSort": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_int]),
     "vrtxFrameKernelMilliseconds": (C.c_float, [C.c_void_p, C.c_void_p]),
     "vrtxFrameKernelLaunches": (C.c_int, [C.c_void_p, C.c_void_p]),

@@ -986,10 +986,68 @@ static cudaTextureAddressMode addressMode(const std::string &w)
   return cudaAddressModeClamp;
 }
 
-// Image samplers: the image as a float4 cudaArray (missing channels 0, alpha
-// 1; 8-bit values normalised, sRGB ones linearised as the reference's float
-// staging does), with a normalised-coordinate texture of the sampler's
-// filter and wrap modes.
+// glm::convertSRGBToLinear of one component, as the reference's image
+// staging calls it (glm's sRGB curve with gamma 2.4)
+static float srgbToLinear(float x)
+{
+  return x <= 0.04045f ? x * 0.07739938080495356f
+                       : std::pow((x + 0.055f) * 0.94786729857819905f, 2.4f);
+}
+
+// One component of the reference's 8-bit staging (convertComponentUint8,
+// utility/CudaImageTexture.cpp:43-57): 8-bit values as they are, sRGB-encoded
+// bytes linearised and truncated back to 8 bits, 16-bit values truncated
+// from (c / 65535) * 255.
+static uint8_t stageComponentUint8(int et, const uint8_t *texel, uint32_t c)
+{
+  if (et == VRTX_UFIXED16) {
+    uint16_t v;
+    std::memcpy(&v, texel + 2 * c, 2);
+    return (uint8_t)((v / 65535.f) * 255.f);
+  }
+  if (et == VRTX_UFIXED8_RGBA_SRGB)
+    return (uint8_t)(srgbToLinear(texel[c] / 255.f) * 255.f);
+  return texel[c];
+}
+
+// An image sampler's texels as the reference stages them
+// (Image1D/2D/3D::finalize, scene/surface/material/sampler/Image2D.cpp:70-78,
+// with transformToStagingBuffer{Float,Uint8},
+// utility/CudaImageTexture.cpp:76-111): float element types as float texels,
+// every other as 8-bit texels that the texture reads as normalised float,
+// all four components of an sRGB texel (alpha too) linearised. The n texels
+// of src (element type et, ch channels) go to f4 (n x 4 floats, missing
+// channels 0, alpha 1) or to u8 (n x 4 bytes, missing channels 0, alpha 255),
+// which is what a fetch of the reference's ch-channel array returns; true
+// for float staging.
+static bool stageSamplerImage(
+    int et, uint32_t ch, const uint8_t *src, size_t n, std::vector<float> &f4, std::vector<uint8_t> &u8)
+{
+  if (et >= VRTX_FLOAT32 && et <= VRTX_FLOAT32_VEC4) {
+    f4.assign(4 * n, 0.f);
+    for (size_t i = 0; i < n; i++) {
+      std::memcpy(&f4[4 * i], src + i * ch * 4, ch * 4);
+      if (ch < 4)
+        f4[4 * i + 3] = 1.f;
+    }
+    return true;
+  }
+  const size_t bytes = et == VRTX_UFIXED16 ? 2 : 1;
+  u8.assign(4 * n, 0);
+  for (size_t i = 0; i < n; i++) {
+    const uint8_t *t = src + i * ch * bytes;
+    for (uint32_t c = 0; c < ch; c++)
+      u8[4 * i + c] = stageComponentUint8(et, t, c);
+    if (ch < 4)
+      u8[4 * i + 3] = 255;
+  }
+  return false;
+}
+
+// Image samplers: the image staged as the reference stages it
+// (stageSamplerImage) into a float4 or an RGBA8 cudaArray, with a
+// normalised-coordinate texture of the sampler's filter and wrap modes,
+// RGBA8 read as normalised float.
 bool Sampler::ensureBuilt()
 {
   const uint32_t t = type();
@@ -1007,7 +1065,6 @@ bool Sampler::ensureBuilt()
     return false;
   }
   const size_t n = (size_t)image->n[0] * image->n[1] * image->n[2];
-  std::vector<float> staging(4 * n);
   std::vector<uint8_t> host(image->bytes());
   if (const void *h = image->hostData())
     std::memcpy(host.data(), h, host.size());
@@ -1018,27 +1075,12 @@ bool Sampler::ensureBuilt()
     cudaStreamSynchronize(Object::dev->stream);
     cudaMemcpy(host.data(), d, host.size(), cudaMemcpyDefault);
   }
-  auto srgbToLinear = [](float c) {
-    return c <= 0.04045f ? c / 12.92f : std::pow((c + 0.055f) / 1.055f, 2.4f);
-  };
-  for (size_t i = 0; i < n; i++) {
-    float v[4] = {0.f, 0.f, 0.f, 1.f};
-    const int et = image->elemType;
-    if (et >= VRTX_FLOAT32 && et <= VRTX_FLOAT32_VEC4)
-      std::memcpy(v, host.data() + i * ch * 4, ch * 4);
-    else if (et == VRTX_UFIXED16)
-      v[0] = ((const uint16_t *)host.data())[i] / 65535.f;
-    else {
-      const uint8_t *p = host.data() + i * ch;
-      for (uint32_t c = 0; c < ch; c++)
-        v[c] = p[c] / 255.f;
-      if (et == VRTX_UFIXED8_RGBA_SRGB)
-        for (int c = 0; c < 3; c++)
-          v[c] = srgbToLinear(v[c]);
-    }
-    std::memcpy(&staging[4 * i], v, 16);
-  }
-  cudaChannelFormatDesc desc = cudaCreateChannelDesc(32, 32, 32, 32, cudaChannelFormatKindFloat);
+  std::vector<float> f4;
+  std::vector<uint8_t> u8;
+  const bool isFloat = stageSamplerImage(image->elemType, ch, host.data(), n, f4, u8);
+  const int bits = isFloat ? 32 : 8;
+  cudaChannelFormatDesc desc = cudaCreateChannelDesc(bits, bits, bits, bits,
+      isFloat ? cudaChannelFormatKindFloat : cudaChannelFormatKindUnsigned);
   const cudaExtent ext = make_cudaExtent(image->n[0],
       t >= SAMPLER_IMAGE2D ? image->n[1] : 0,
       t == SAMPLER_IMAGE3D ? image->n[2] : 0);
@@ -1049,7 +1091,9 @@ bool Sampler::ensureBuilt()
     return false;
   }
   cudaMemcpy3DParms cp{};
-  cp.srcPtr = make_cudaPitchedPtr(staging.data(), image->n[0] * 16, image->n[0],
+  cp.srcPtr = make_cudaPitchedPtr(isFloat ? (void *)f4.data() : (void *)u8.data(),
+      image->n[0] * (isFloat ? 16 : 4),
+      image->n[0],
       t >= SAMPLER_IMAGE2D ? image->n[1] : 1);
   cp.dstArray = cuArray;
   cp.extent = make_cudaExtent(image->n[0],
@@ -1064,7 +1108,7 @@ bool Sampler::ensureBuilt()
   for (int k = 0; k < 3; k++)
     td.addressMode[k] = addressMode(wrap[k]);
   td.filterMode = filter == "nearest" ? cudaFilterModePoint : cudaFilterModeLinear;
-  td.readMode = cudaReadModeElementType;
+  td.readMode = isFloat ? cudaReadModeElementType : cudaReadModeNormalizedFloat;
   td.normalizedCoords = 1;
   cudaCreateTextureObject(&tex, &rd, &td, nullptr);
   builtStamp = want;
@@ -2717,12 +2761,45 @@ uint64_t Renderer::deepStamp() const
   return std::max(commitStamp, bgImage ? bgImage->deepStamp() : 0);
 }
 
+// The background image's n texels (element type et, nc = 3 or 4 channels)
+// staged as RGBA8 (Array2D::acquireCUDAArrayUint8 with
+// transformToStagingBufferUint8, utility/CudaImageTexture.cpp:43-93): float
+// components truncated from c * 255 (clamped to [0, 255] here, where the
+// reference's conversion is undefined), sRGB-encoded bytes (alpha too)
+// linearised, other bytes as they are; alpha 255 for three channels.
+static void stageBackgroundImage(int et, int nc, const uint8_t *raw, size_t n, uint8_t *rgba)
+{
+  for (size_t i = 0; i < n; i++) {
+    for (int c = 0; c < 4; c++) {
+      uint8_t v = 255;
+      if (c < nc) {
+        if (et == VRTX_FLOAT32_VEC3 || et == VRTX_FLOAT32_VEC4) {
+          float f;
+          std::memcpy(&f, raw + 4 * (i * nc + c), 4);
+          const float s = f * 255.f;
+          v = (uint8_t)(s >= 255.f ? 255.f : (s > 0.f ? s : 0.f));
+        } else {
+          v = stageComponentUint8(et, raw + i * 4, c);
+        }
+      }
+      rgba[i * 4 + c] = v;
+    }
+  }
+}
+
+static int backgroundChannels(int et)
+{
+  return et == VRTX_FLOAT32_VEC3 ? 3
+      : (et == VRTX_FLOAT32_VEC4 || et == VRTX_UFIXED8_VEC4 || et == VRTX_UFIXED8_RGBA_SRGB) ? 4
+                                                                                            : 0;
+}
+
 // Renderer::finalize with Array2D::acquireCUDAArrayUint8
 // (utility/CudaImageTexture.cpp:43-93,139-190): the image staged as RGBA8
 // (float components truncated from c * 255, clamped to [0, 255] here;
-// sRGB-encoded bytes linearised first; three channels get alpha 255), a
-// normalised-float, linear, clamped texture read at the sample's screen
-// position
+// sRGB-encoded bytes, alpha too, linearised first; three channels get alpha
+// 255), a normalised-float, linear, clamped texture read at the sample's
+// screen position
 bool Renderer::ensureBackground()
 {
   if (!bgImage) {
@@ -2744,9 +2821,7 @@ bool Renderer::ensureBackground()
   gpu.backgroundTex = 0;
   bgArray = nullptr;
   const int et = bgImage->elemType;
-  const int nc = et == VRTX_FLOAT32_VEC3 ? 3
-      : (et == VRTX_FLOAT32_VEC4 || et == VRTX_UFIXED8_VEC4 || et == VRTX_UFIXED8_RGBA_SRGB) ? 4
-                                                                                            : 0;
+  const int nc = backgroundChannels(et);
   if (!nc) {
     report(VRTX_SEVERITY_WARNING,
         "background image: element type %d is not supported (FLOAT32_VEC3/4, "
@@ -2764,28 +2839,7 @@ bool Renderer::ensureBackground()
     cudaMemcpy(raw.data(), d, raw.size(), cudaMemcpyDeviceToHost);
   }
   std::vector<uint8_t> rgba(W * H * 4);
-  for (size_t i = 0; i < W * H; i++) {
-    for (int c = 0; c < 4; c++) {
-      uint8_t v = 255;
-      if (c < nc) {
-        if (et == VRTX_FLOAT32_VEC3 || et == VRTX_FLOAT32_VEC4) {
-          float f;
-          std::memcpy(&f, raw.data() + 4 * (i * nc + c), 4);
-          const float s = f * 255.f;
-          v = (uint8_t)(s >= 255.f ? 255.f : (s > 0.f ? s : 0.f));
-        } else if (et == VRTX_UFIXED8_RGBA_SRGB && c < 3) {
-          // glm::convertSRGBToLinear
-          const float x = raw[i * 4 + c] / 255.f;
-          const float lin = x <= 0.04045f ? x * 0.07739938080495356f
-                                          : std::pow((x + 0.055f) * 0.94786729857819905f, 2.4f);
-          v = (uint8_t)(lin * 255.f);
-        } else {
-          v = raw[i * 4 + c];
-        }
-      }
-      rgba[i * 4 + c] = v;
-    }
-  }
+  stageBackgroundImage(et, nc, raw.data(), W * H, rgba.data());
   cudaChannelFormatDesc desc = cudaCreateChannelDesc<uchar4>();
   if (cudaMallocArray(&bgArray, &desc, W, H) != cudaSuccess) {
     cudaGetLastError();
@@ -4050,6 +4104,35 @@ VRTX_API int vrtxDebugDiscretizeTF(const float *color,
       256,
       out);
   return 0;
+}
+
+VRTX_API int vrtxDebugStageImage(int elementType,
+    int background,
+    const void *texels,
+    uint64_t n,
+    float *outFloat,
+    uint8_t *outBytes)
+{
+  if (background) {
+    const int nc = backgroundChannels(elementType);
+    if (!nc || (n && (!texels || !outBytes)))
+      return -1;
+    stageBackgroundImage(elementType, nc, (const uint8_t *)texels, n, outBytes);
+    return 0;
+  }
+  const uint32_t ch = attrChannels(elementType);
+  if (!ch || (n && !texels))
+    return -1;
+  std::vector<float> f4;
+  std::vector<uint8_t> u8;
+  const bool isFloat = stageSamplerImage(elementType, ch, (const uint8_t *)texels, n, f4, u8);
+  if (isFloat ? !outFloat : !outBytes)
+    return -1;
+  if (isFloat)
+    std::memcpy(outFloat, f4.data(), f4.size() * sizeof(float));
+  else
+    std::memcpy(outBytes, u8.data(), u8.size());
+  return isFloat ? 1 : 0;
 }
 
 VRTX_API int vrtxDebugWriteColors(VRTXDevice d,

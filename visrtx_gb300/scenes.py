@@ -285,11 +285,13 @@ class SamplerSpec:
     """A material sampler (sampler/Image1D.cpp, Image2D.cpp, Image3D.cpp,
     TransformSampler.cpp, PrimitiveSampler.cpp): "image1D" / "image2D" /
     "image3D" over `image` ((n[, c]) / (ny, nx[, c]) / (nz, ny, nx[, c]);
-    float32 x1-4, uint8 x1 / x4, uint16 x1), "transform", or "primitive" over
-    `array` (an attribute-typed array read at primID + offset). Transforms
-    are 4x4 in row-major (math) layout."""
+    float32 x1-4, uint8 x1 / x4, uint16 x1; uint8 x4 sRGB-encoded when
+    image_srgb), "transform", or "primitive" over `array` (an
+    attribute-typed array read at primID + offset). Transforms are 4x4 in
+    row-major (math) layout."""
     type: str
     image: np.ndarray | None = None
+    image_srgb: bool = False
     array: np.ndarray | None = None
     offset: int = 0
     attribute: str = "attribute0"
@@ -467,6 +469,18 @@ def background_image_type(img: np.ndarray, srgb: bool = False) -> int:
     raise ValueError("background images are (H, W, 3|4) float32 or (H, W, 4) uint8")
 
 
+def sampler_image_type(sp: SamplerSpec) -> int:
+    """Element type code of an image sampler's image (SamplerSpec.image)."""
+    from . import _lib as L
+
+    tex, c = sp.texels()
+    if sp.image_srgb:
+        if tex.dtype != np.uint8 or c != 4:
+            raise ValueError("sRGB sampler images are uint8 x 4")
+        return L.UFIXED8_RGBA_SRGB
+    return attr_type(tex)
+
+
 def attr_type(a: np.ndarray) -> int:
     """Element type code of an attribute array (see SurfaceSpec.attrs)."""
     from . import _lib as L
@@ -508,7 +522,7 @@ def build_on_device(dev, spec: SceneSpec, channels=("color", "depth", "primitive
         if nd:
             tex, _ = sp.texels()
             img = np.ascontiguousarray(sp.image)
-            et = attr_type(tex)
+            et = sampler_image_type(sp)
             a = (dev.new_array(tex, et) if nd == 1 else
                  dev.new_array2d(img, et) if nd == 2 else dev.new_array3d(img, et))
             keep.append(a)
