@@ -98,7 +98,7 @@ def stage_background(et, texels):
 def _pack_sampler(o, sp, keep):
     """Fills an OrcSampler from a SamplerSpec, its image staged as the
     device stages it (stage_image)."""
-    from visrtx_gb300.scenes import sampler_image_type
+    from visrtx_gb300.scenes import attr_type, sampler_image_type
 
     o.type = _SAMPLER_TYPES[sp.type]
     o.attribute = _SAMPLER_SLOTS[sp.attribute]
