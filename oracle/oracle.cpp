@@ -1448,18 +1448,30 @@ struct VolHit
 void volBounds(const OrcVolume &v, V3 &lo, V3 &hi);
 void gridDims(const OrcVolume &v, int d[3]);
 
+// intersectBox (gpu/gpu_math.h:278-290): the ray's interval in the box,
+// false where it misses (tin < tout fails, NaN included)
+bool intersectBox(V3 blo, V3 bhi, V3 org, V3 dir, float &t0, float &t1)
+{
+  const V3 inv = v3(1.f / dir.x, 1.f / dir.y, 1.f / dir.z);
+  const V3 mins = (blo - org) * inv, maxs = (bhi - org) * inv;
+  const V3 nr = v3(std::min(mins.x, maxs.x), std::min(mins.y, maxs.y), std::min(mins.z, maxs.z));
+  const V3 fr = v3(std::max(mins.x, maxs.x), std::max(mins.y, maxs.y), std::max(mins.z, maxs.z));
+  const float tin = cmax(nr), tout = std::min(fr.x, std::min(fr.y, fr.z));
+  if (!(tin < tout))
+    return false;
+  t0 = tin;
+  t1 = tout;
+  return true;
+}
+
 bool volumeSlab(const OrcVolume &v, const X34 &w2o, V3 o, V3 d, float tmin, float tmax,
     VolHit &h)
 {
   const V3 lo = xPoint(w2o, o), ld = xVec(w2o, d);
-  const V3 inv = v3(1.f / ld.x, 1.f / ld.y, 1.f / ld.z);
   V3 blo, bhi;
   volBounds(v, blo, bhi);
-  const V3 mins = (blo - lo) * inv, maxs = (bhi - lo) * inv;
-  const V3 nr = v3(std::min(mins.x, maxs.x), std::min(mins.y, maxs.y), std::min(mins.z, maxs.z));
-  const V3 fr = v3(std::max(mins.x, maxs.x), std::max(mins.y, maxs.y), std::max(mins.z, maxs.z));
-  float t0 = cmax(nr), t1 = std::min(fr.x, std::min(fr.y, fr.z));
-  if (!(t0 < t1))
+  float t0, t1;
+  if (!intersectBox(blo, bhi, lo, ld, t0, t1))
     return false;
   t0 = std::max(tmin, std::min(t0, tmax));
   t1 = std::max(tmin, std::min(t1, tmax));
@@ -3162,6 +3174,20 @@ void orc_project_on_grid(const float *p3, int n, const int *dims3, const float *
   for (int i = 0; i < n; i++)
     for (int a = 0; a < 3; a++)
       out3[3 * i + a] = projectAxis(p3[3 * i + a], box6[a], box6[3 + a], dims3[a]);
+}
+
+// intersectBox (gpu/gpu_math.h:278-290) for n rays (org xyz, dir xyz)
+// against box6: hit[i] 1 / 0 and, on a hit, [t0, t1]
+void orc_intersect_box(const float *rays6, int n, const float *box6, int *hit, float *t01)
+{
+  const V3 blo = v3(box6[0], box6[1], box6[2]), bhi = v3(box6[3], box6[4], box6[5]);
+  for (int i = 0; i < n; i++) {
+    const float *r = rays6 + 6 * i;
+    float t0 = 0.f, t1 = 0.f;
+    hit[i] = intersectBox(blo, bhi, v3(r[0], r[1], r[2]), v3(r[3], r[4], r[5]), t0, t1) ? 1 : 0;
+    t01[2 * i] = hit[i] ? t0 : 0.f;
+    t01[2 * i + 1] = hit[i] ? t1 : 0.f;
+  }
 }
 
 // Image1D/2D/3D::finalize's staging (sampler/Image2D.cpp:70-78 with

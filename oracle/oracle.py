@@ -254,6 +254,17 @@ def primary_rays(cam, cam_type, samples, inv_w, inv_h, center_pixel=False):
     return out
 
 
+def intersect_box(rays, box):
+    """(n, 6) rays (org, dir) against a box (lo, hi) -> (hit (n,), t01 (n, 2))."""
+    lib = load()
+    r = np.ascontiguousarray(rays, np.float32).reshape(-1, 6)
+    b = np.ascontiguousarray(box, np.float32).reshape(6)
+    hit = np.zeros(len(r), np.int32)
+    t01 = np.zeros((len(r), 2), np.float32)
+    lib.orc_intersect_box(_ptr(r), C.c_int(len(r)), _ptr(b), _ptr(hit), _ptr(t01))
+    return hit, t01
+
+
 def dda_walk(rays, dims, box, max_cells):
     """(n, 8) rays (org, dir, tlo, thi) -> (counts (n,), cells (n, max_cells),
     t01 (n, max_cells, 2)): the macrocell walk of the delta-tracking march."""

@@ -4,8 +4,8 @@
 // the vendored glm), compiled from those headers where they lie into
 // oracle/_ref/libtfref.so by oracle/build.py, only where the reference tree
 // is present, and used only by tests/golden/make_tf_golden.py and
-// tests/golden/make_math_golden.py (the latter for the two gpu_math.h
-// helpers at the end of this file).
+// tests/golden/make_math_golden.py (the latter for the gpu_math.h and
+// uniformGrid.h helpers after it).
 //
 // tfref_discretize repeats the call sequence of
 // TransferFunction1D::discritizeTFData (TransferFunction1D.cpp:101-150): the
@@ -116,5 +116,26 @@ extern "C" void mathref_project_on_grid(
     out3[3 * i] = c.x;
     out3[3 * i + 1] = c.y;
     out3[3 * i + 2] = c.z;
+  }
+}
+
+// intersectBox (gpu/gpu_math.h:278-290), compiled unchanged, for n rays
+// (org xyz, dir xyz) against box6: hit 1 / 0 and the interval on a hit
+extern "C" void mathref_intersect_box(
+    const float *rays6, int n, const float *box6, int *hit, float *t01)
+{
+  const visrtx::box3 b(visrtx::vec3(box6[0], box6[1], box6[2]),
+      visrtx::vec3(box6[3], box6[4], box6[5]));
+  for (int i = 0; i < n; i++) {
+    const float *r = rays6 + 6 * i;
+    visrtx::box1 io(0.f, 0.f);
+    hit[i] = visrtx::intersectBox(b,
+                 visrtx::vec3(r[0], r[1], r[2]),
+                 visrtx::vec3(r[3], r[4], r[5]),
+                 io)
+        ? 1
+        : 0;
+    t01[2 * i] = hit[i] ? io.lower : 0.f;
+    t01[2 * i + 1] = hit[i] ? io.upper : 0.f;
   }
 }

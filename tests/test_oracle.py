@@ -280,6 +280,26 @@ def test_primary_rays_match_reference_camera():
     assert (n, fused_differ) == (3960, 2393)
 
 
+def test_volume_entry_interval_matches_reference_intersect_box():
+    """The oracle's ray/box interval (the volume entry of the scivis and dpt
+    marches) equals, bit for bit, the reference's own gpu/gpu_math.h
+    intersectBox compiled on the host (fixtures by
+    tests/golden/make_box_golden.py): 2000 rays over five boxes, with
+    axis-aligned directions (+0 and -0 components, 1 / d = +-inf), origins
+    on the box's planes (NaN slabs), on faces, edges and corners, and a
+    flat box, which no ray enters."""
+    z = np.load(os.path.join(GOLDEN, "box_golden.npz"))
+    n = hits = 0
+    for i in range(len(z["boxes"])):
+        hit, t01 = O.intersect_box(z[f"b{i}_rays"], z["boxes"][i])
+        assert np.array_equal(hit, z[f"b{i}_hit"]), i
+        assert np.array_equal(t01.view(np.uint32), z[f"b{i}_t01"].view(np.uint32)), i
+        n += len(hit)
+        hits += int(hit.sum())
+    assert (n, hits) == (2000, 246)
+    assert int(z["b3_hit"].sum()) == 0
+
+
 def test_macrocell_walk_matches_reference_dda():
     """The oracle's macrocell walk (dda3, which the delta-tracking march
     runs over the majorant grid) visits the same cells with the same
