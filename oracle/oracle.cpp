@@ -1448,19 +1448,34 @@ struct VolHit
 void volBounds(const OrcVolume &v, V3 &lo, V3 &hi);
 void gridDims(const OrcVolume &v, int d[3]);
 
-// intersectBox (gpu/gpu_math.h:278-290): the ray's interval in the box,
-// false where it misses (tin < tout fails, NaN included)
-bool intersectBox(V3 blo, V3 bhi, V3 org, V3 dir, float &t0, float &t1)
+// glm::min / glm::max on floats (glm/detail/func_common.inl): the first
+// operand where either is NaN
+inline float glmMin(float a, float b)
+{
+  return (b < a) ? b : a;
+}
+inline float glmMax(float a, float b)
+{
+  return (a < b) ? b : a;
+}
+
+// intersectVolume (scene/Intersectors_ptx.cu:248-274): the local ray's slab
+// interval in the volume's bounds -- glm::min / glm::max per axis, then
+// glm::compMax / glm::compMin (left folds), so that a ray parallel to a
+// bounding plane with its origin on it (a NaN slab) enters or misses as the
+// reference's does -- clamped to [tmin, tmax] (gpu_math.h clamp)
+bool volumeInterval(V3 blo, V3 bhi, V3 org, V3 dir, float tmin, float tmax, float &t0, float &t1)
 {
   const V3 inv = v3(1.f / dir.x, 1.f / dir.y, 1.f / dir.z);
   const V3 mins = (blo - org) * inv, maxs = (bhi - org) * inv;
-  const V3 nr = v3(std::min(mins.x, maxs.x), std::min(mins.y, maxs.y), std::min(mins.z, maxs.z));
-  const V3 fr = v3(std::max(mins.x, maxs.x), std::max(mins.y, maxs.y), std::max(mins.z, maxs.z));
-  const float tin = cmax(nr), tout = std::min(fr.x, std::min(fr.y, fr.z));
+  const V3 nr = v3(glmMin(mins.x, maxs.x), glmMin(mins.y, maxs.y), glmMin(mins.z, maxs.z));
+  const V3 fr = v3(glmMax(mins.x, maxs.x), glmMax(mins.y, maxs.y), glmMax(mins.z, maxs.z));
+  const float tin = glmMax(glmMax(nr.x, nr.y), nr.z);
+  const float tout = glmMin(glmMin(fr.x, fr.y), fr.z);
   if (!(tin < tout))
     return false;
-  t0 = tin;
-  t1 = tout;
+  t0 = glmMax(tmin, glmMin(tin, tmax));
+  t1 = glmMax(tmin, glmMin(tout, tmax));
   return true;
 }
 
@@ -1471,10 +1486,8 @@ bool volumeSlab(const OrcVolume &v, const X34 &w2o, V3 o, V3 d, float tmin, floa
   V3 blo, bhi;
   volBounds(v, blo, bhi);
   float t0, t1;
-  if (!intersectBox(blo, bhi, lo, ld, t0, t1))
+  if (!volumeInterval(blo, bhi, lo, ld, tmin, tmax, t0, t1))
     return false;
-  t0 = std::max(tmin, std::min(t0, tmax));
-  t1 = std::max(tmin, std::min(t1, tmax));
   h.lo = lo;
   h.ld = ld;
   h.t0 = t0;
@@ -3176,15 +3189,18 @@ void orc_project_on_grid(const float *p3, int n, const int *dims3, const float *
       out3[3 * i + a] = projectAxis(p3[3 * i + a], box6[a], box6[3 + a], dims3[a]);
 }
 
-// intersectBox (gpu/gpu_math.h:278-290) for n rays (org xyz, dir xyz)
-// against box6: hit[i] 1 / 0 and, on a hit, [t0, t1]
-void orc_intersect_box(const float *rays6, int n, const float *box6, int *hit, float *t01)
+// intersectVolume's interval (scene/Intersectors_ptx.cu:248-274) for n
+// local rays (org xyz, dir xyz, tmin, tmax) against box6: hit[i] 1 / 0 and,
+// on a hit, the clamped [t0, t1]
+void orc_volume_interval(const float *rays8, int n, const float *box6, int *hit, float *t01)
 {
   const V3 blo = v3(box6[0], box6[1], box6[2]), bhi = v3(box6[3], box6[4], box6[5]);
   for (int i = 0; i < n; i++) {
-    const float *r = rays6 + 6 * i;
+    const float *r = rays8 + 8 * i;
     float t0 = 0.f, t1 = 0.f;
-    hit[i] = intersectBox(blo, bhi, v3(r[0], r[1], r[2]), v3(r[3], r[4], r[5]), t0, t1) ? 1 : 0;
+    hit[i] = volumeInterval(blo, bhi, v3(r[0], r[1], r[2]), v3(r[3], r[4], r[5]), r[6], r[7], t0, t1)
+        ? 1
+        : 0;
     t01[2 * i] = hit[i] ? t0 : 0.f;
     t01[2 * i + 1] = hit[i] ? t1 : 0.f;
   }

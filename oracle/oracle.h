@@ -303,10 +303,11 @@ int orc_stage_image(int et, const void *texels, uint64_t n, float *outFloat, uin
  * 260 ufixed8 x4, 261 sRGB ufixed8 x4) to out (n x 4 RGBA8); -1 for another
  * type. */
 int orc_stage_background(int et, const void *texels, uint64_t n, uint8_t *out);
-/* intersectBox (gpu_math.h:278-290), the volume's entry interval, for n
- * rays (org xyz, dir xyz) against box6 (lo xyz, hi xyz): hit[i] 1 or 0,
- * t01[2i..2i+1] the interval on a hit (0, 0 otherwise). */
-void orc_intersect_box(const float *rays6, int n, const float *box6, int *hit, float *t01);
+/* intersectVolume's slab interval (Intersectors_ptx.cu:248-274), the
+ * volume's entry, for n local rays (org xyz, dir xyz, tmin, tmax) against
+ * box6 (lo xyz, hi xyz): hit[i] 1 or 0, t01[2i..2i+1] the clamped interval
+ * on a hit (0, 0 otherwise). */
+void orc_volume_interval(const float *rays8, int n, const float *box6, int *hit, float *t01);
 /* makePrimaryRay + cameraCreateRay (cameraCreateRay.h:38-81) for n
  * samples (pixel x, pixel y, r0..r3: the uniform4 draw) of a camera record
  * (30 floats: region 4, pos 3, dir 3, dir_00 3, dir_du 3, dir_dv 3,

@@ -254,14 +254,15 @@ def primary_rays(cam, cam_type, samples, inv_w, inv_h, center_pixel=False):
     return out
 
 
-def intersect_box(rays, box):
-    """(n, 6) rays (org, dir) against a box (lo, hi) -> (hit (n,), t01 (n, 2))."""
+def volume_interval(rays, box):
+    """(n, 8) local rays (org, dir, tmin, tmax) against a volume's bounds
+    (lo, hi) -> (hit (n,), t01 (n, 2)): the volume's entry interval."""
     lib = load()
-    r = np.ascontiguousarray(rays, np.float32).reshape(-1, 6)
+    r = np.ascontiguousarray(rays, np.float32).reshape(-1, 8)
     b = np.ascontiguousarray(box, np.float32).reshape(6)
     hit = np.zeros(len(r), np.int32)
     t01 = np.zeros((len(r), 2), np.float32)
-    lib.orc_intersect_box(_ptr(r), C.c_int(len(r)), _ptr(b), _ptr(hit), _ptr(t01))
+    lib.orc_volume_interval(_ptr(r), C.c_int(len(r)), _ptr(b), _ptr(hit), _ptr(t01))
     return hit, t01
 
 

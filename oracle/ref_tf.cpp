@@ -14,8 +14,11 @@
 // with a = 1 for vec3 colours, and the uniform colour / opacity where an
 // array is absent. That file itself needs the ANARI-SDK and cannot be built
 // here; the arithmetic it calls is the helpers', compiled unchanged.
+#define GLM_ENABLE_EXPERIMENTAL
 #include "gpu/uniformGrid.h"
 #include "utility/colorMapHelpers.h"
+
+#include <glm/gtx/component_wise.hpp>
 
 #include <vector>
 
@@ -119,23 +122,32 @@ extern "C" void mathref_project_on_grid(
   }
 }
 
-// intersectBox (gpu/gpu_math.h:278-290), compiled unchanged, for n rays
-// (org xyz, dir xyz) against box6: hit 1 / 0 and the interval on a hit
-extern "C" void mathref_intersect_box(
-    const float *rays6, int n, const float *box6, int *hit, float *t01)
+// intersectVolume's slab interval (scene/Intersectors_ptx.cu:248-274): its
+// calls repeated over the vendored glm (glm::min / glm::max of the slab
+// vectors, glm::compMax / glm::compMin) and gpu_math.h's range clamp, for n
+// local rays (org xyz, dir xyz, tmin, tmax) against box6. That file is an
+// OptiX program and cannot be built here; the arithmetic it calls is glm's
+// and gpu_math.h's, compiled unchanged.
+extern "C" void mathref_volume_interval(
+    const float *rays8, int n, const float *box6, int *hit, float *t01)
 {
-  const visrtx::box3 b(visrtx::vec3(box6[0], box6[1], box6[2]),
-      visrtx::vec3(box6[3], box6[4], box6[5]));
+  using namespace visrtx;
+  const box3 bounds(vec3(box6[0], box6[1], box6[2]), vec3(box6[3], box6[4], box6[5]));
   for (int i = 0; i < n; i++) {
-    const float *r = rays6 + 6 * i;
-    visrtx::box1 io(0.f, 0.f);
-    hit[i] = visrtx::intersectBox(b,
-                 visrtx::vec3(r[0], r[1], r[2]),
-                 visrtx::vec3(r[3], r[4], r[5]),
-                 io)
-        ? 1
-        : 0;
-    t01[2 * i] = hit[i] ? io.lower : 0.f;
-    t01[2 * i + 1] = hit[i] ? io.upper : 0.f;
+    const float *r = rays8 + 8 * i;
+    const vec3 org(r[0], r[1], r[2]), dir(r[3], r[4], r[5]);
+    const vec3 mins = (bounds.lower - org) * (1.f / dir);
+    const vec3 maxs = (bounds.upper - org) * (1.f / dir);
+    const vec3 nears = glm::min(mins, maxs);
+    const vec3 fars = glm::max(mins, maxs);
+    box1 t(glm::compMax(nears), glm::compMin(fars));
+    hit[i] = t.lower < t.upper ? 1 : 0;
+    if (hit[i]) {
+      const box1 rayt{r[6], r[7]};
+      t.lower = visrtx::clamp(t.lower, rayt);
+      t.upper = visrtx::clamp(t.upper, rayt);
+    }
+    t01[2 * i] = hit[i] ? t.lower : 0.f;
+    t01[2 * i + 1] = hit[i] ? t.upper : 0.f;
   }
 }

@@ -280,24 +280,27 @@ def test_primary_rays_match_reference_camera():
     assert (n, fused_differ) == (3960, 2393)
 
 
-def test_volume_entry_interval_matches_reference_intersect_box():
-    """The oracle's ray/box interval (the volume entry of the scivis and dpt
-    marches) equals, bit for bit, the reference's own gpu/gpu_math.h
-    intersectBox compiled on the host (fixtures by
-    tests/golden/make_box_golden.py): 2000 rays over five boxes, with
-    axis-aligned directions (+0 and -0 components, 1 / d = +-inf), origins
-    on the box's planes (NaN slabs), on faces, edges and corners, and a
-    flat box, which no ray enters."""
-    z = np.load(os.path.join(GOLDEN, "box_golden.npz"))
+def test_volume_entry_interval_matches_reference_intersect_volume():
+    """The oracle's volume entry interval equals, bit for bit, the
+    reference's intersectVolume (scene/Intersectors_ptx.cu:248-274), its glm
+    and gpu_math.h calls compiled on the host (fixtures by
+    tests/golden/make_volume_interval_golden.py): 2400 local rays over five
+    boxes, with axis-aligned directions (+0 and -0 components,
+    1 / d = +-inf), origins on each of the six bounding planes with the
+    direction parallel to it (NaN slabs, where glm's min / max keep the
+    first operand), origins on faces, edges and corners, ray intervals that
+    start inside the box or end before it, and a flat box. With fminf /
+    fmaxf in place of glm's min / max, 128 of those rays would enter or miss
+    differently."""
+    z = np.load(os.path.join(GOLDEN, "volume_interval_golden.npz"))
     n = hits = 0
     for i in range(len(z["boxes"])):
-        hit, t01 = O.intersect_box(z[f"b{i}_rays"], z["boxes"][i])
+        hit, t01 = O.volume_interval(z[f"b{i}_rays"], z["boxes"][i])
         assert np.array_equal(hit, z[f"b{i}_hit"]), i
         assert np.array_equal(t01.view(np.uint32), z[f"b{i}_t01"].view(np.uint32)), i
         n += len(hit)
         hits += int(hit.sum())
-    assert (n, hits) == (2000, 246)
-    assert int(z["b3_hit"].sum()) == 0
+    assert (n, hits) == (2400, 421)
 
 
 def test_macrocell_walk_matches_reference_dda():

@@ -28,8 +28,22 @@ struct VolumeHitG
   float tlo, thi;
 };
 
-// Slab test in the volume's object space (Intersectors_ptx.cu:248-274),
-// clamped to the ray interval [tmin, tmax].
+// glm::min / glm::max on floats: the first operand where either is NaN
+// (where fminf / fmaxf would return the other)
+__device__ __forceinline__ float glmMin(float a, float b)
+{
+  return (b < a) ? b : a;
+}
+__device__ __forceinline__ float glmMax(float a, float b)
+{
+  return (a < b) ? b : a;
+}
+
+// Slab test in the volume's object space (Intersectors_ptx.cu:248-274):
+// glm::min / glm::max per axis and glm::compMax / glm::compMin as left
+// folds, so that a ray parallel to a bounding plane with its origin on it
+// (a NaN slab) enters or misses as the reference's does; clamped to the ray
+// interval [tmin, tmax] (gpu_math.h clamp).
 __device__ __forceinline__ bool volumeSlab(const VolumeGPU &v,
     f3 worldOrg,
     f3 worldDir,
@@ -42,14 +56,14 @@ __device__ __forceinline__ bool volumeSlab(const VolumeGPU &v,
   const f3 inv = mk3(1.f / ld.x, 1.f / ld.y, 1.f / ld.z);
   const f3 mins = (v.bounds.lo - lo) * inv;
   const f3 maxs = (v.bounds.hi - lo) * inv;
-  const f3 nears = fmin3(mins, maxs);
-  const f3 fars = fmax3(mins, maxs);
-  float t0 = compMax(nears);
-  float t1 = compMin(fars);
+  const f3 nears = mk3(glmMin(mins.x, maxs.x), glmMin(mins.y, maxs.y), glmMin(mins.z, maxs.z));
+  const f3 fars = mk3(glmMax(mins.x, maxs.x), glmMax(mins.y, maxs.y), glmMax(mins.z, maxs.z));
+  float t0 = glmMax(glmMax(nears.x, nears.y), nears.z);
+  float t1 = glmMin(glmMin(fars.x, fars.y), fars.z);
   if (!(t0 < t1))
     return false;
-  t0 = fmaxf(tmin, fminf(t0, tmax));
-  t1 = fmaxf(tmin, fminf(t1, tmax));
+  t0 = glmMax(tmin, glmMin(t0, tmax));
+  t1 = glmMax(tmin, glmMin(t1, tmax));
   h.localOrg = lo;
   h.localDir = ld;
   h.tlo = t0;
