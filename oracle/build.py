@@ -11,7 +11,9 @@ output only in oracle/_ref/:
     (libnvdbref.so);
   * its transfer-function helpers (devices/rtx/utility/colorMapHelpers.h
     with gpu/gpu_math.h and the vendored glm): ref_tf.cpp repeats
-    TransferFunction1D::discritizeTFData's calls (libtfref.so);
+    TransferFunction1D::discritizeTFData's calls, runs gpu_math.h's and
+    uniformGrid.h's sampling and grid helpers, and repeats
+    intersectVolume's glm calls (libtfref.so);
   * the vendored glm's colour packing (glm::convertLinearToSRGB,
     glm::packUnorm4x8): ref_glm.cpp repeats writeOutputColor's calls
     (libglmref.so);

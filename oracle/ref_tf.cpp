@@ -3,9 +3,10 @@
 // getInterpolatedValue, with gpu/gpu_math.h's box1 / position / contains and
 // the vendored glm), compiled from those headers where they lie into
 // oracle/_ref/libtfref.so by oracle/build.py, only where the reference tree
-// is present, and used only by tests/golden/make_tf_golden.py and
-// tests/golden/make_math_golden.py (the latter for the gpu_math.h and
-// uniformGrid.h helpers after it).
+// is present, and used only by tests/golden/make_tf_golden.py,
+// tests/golden/make_math_golden.py (the gpu_math.h and uniformGrid.h
+// helpers after it) and tests/golden/make_volume_interval_golden.py
+// (intersectVolume's glm calls, at the end).
 //
 // tfref_discretize repeats the call sequence of
 // TransferFunction1D::discritizeTFData (TransferFunction1D.cpp:101-150): the
