@@ -26,6 +26,9 @@ output only in oracle/_ref/:
     ref_camera.cpp runs it without contraction (libcamref.so, each
     operation rounded once, as the oracle and the library's kernels round
     it) and with it (libcamref_fused.so, to size the gap).
+  * its structured-field sampler (devices/rtx/gpu/sampleSpatialField.h):
+    ref_field.cpp records the texture coordinate it fetches at
+    (libfieldref.so);
   * its image staging (devices/rtx/utility/CudaImageTexture.cpp,
     convertComponentUint8 / Float and transformToStagingBuffer*):
     ref_image.cpp includes that .cpp (its staging functions are
@@ -78,8 +81,9 @@ REF_DDA_LIB = os.path.join(REF_OUT, "libddaref.so")
 REF_CAM_LIB = os.path.join(REF_OUT, "libcamref.so")
 REF_CAM_FUSED_LIB = os.path.join(REF_OUT, "libcamref_fused.so")
 REF_IMG_LIB = os.path.join(REF_OUT, "libimgref.so")
+REF_FIELD_LIB = os.path.join(REF_OUT, "libfieldref.so")
 GPU_HEADERS = ("dda.h", "gpu_debug.h", "gpu_math.h", "gpu_decl.h", "uniformGrid.h",
-               "cameraCreateRay.h")
+               "cameraCreateRay.h", "sampleSpatialField.h")
 UTILITY_FILES = ("CudaImageTexture.cpp", "AnariTypeHelpers.h")
 CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 
@@ -110,8 +114,9 @@ def build_ref(tree: str | None = None) -> str | None:
     transfer-function helpers), oracle/_ref/libglmref.so (ref_glm.cpp
     over its vendored glm), oracle/_ref/libddaref.so (ref_dda.cpp over
     its dda.h), oracle/_ref/libcamref{,_fused}.so (ref_camera.cpp over
-    its cameraCreateRay.h) and oracle/_ref/libimgref.so (ref_image.cpp over
-    its CudaImageTexture.cpp) from the reference tree `tree` (default
+    its cameraCreateRay.h), oracle/_ref/libfieldref.so (ref_field.cpp over
+    its sampleSpatialField.h) and oracle/_ref/libimgref.so (ref_image.cpp
+    over its CudaImageTexture.cpp) from the reference tree `tree` (default
     REF_TREE); returns the NanoVDB harness's path, or None when the
     reference tree is absent."""
     root = tree or REF_TREE
@@ -139,6 +144,10 @@ def build_ref(tree: str | None = None) -> str | None:
                 _compile_ref(cam, REF_CAM_LIB, [inc, glm], contract="off", deps=shim)
                 _compile_ref(cam, REF_CAM_FUSED_LIB, [inc, glm], contract="fast", deps=shim)
                 if os.path.isdir(os.path.join(CUDA_HOME, "include")):
+                    nvdb = os.path.join(root, "external", "nanovdb", "include")
+                    _compile_ref(os.path.join(HERE, "ref_field.cpp"), REF_FIELD_LIB,
+                                 [inc, nvdb, glm, os.path.join(CUDA_HOME, "include")],
+                                 deps=shim)
                     _compile_ref(os.path.join(HERE, "ref_image.cpp"), REF_IMG_LIB,
                                  [inc, shims, glm, os.path.join(CUDA_HOME, "include")],
                                  deps=(os.path.join(shims, "CudaImageTexture.h"),

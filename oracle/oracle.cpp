@@ -1673,16 +1673,25 @@ double nvdbSampleExact(const Nvdb &n, double px, double py, double pz)
   return r;
 }
 
+// SpatialFieldSampler<cudaTextureObject_t> (gpu/sampleSpatialField.h:54-78)
+// with StructuredRegularField::gpuData's invSpacing
+// (StructuredRegularField.cpp:188-189): the normalised texture coordinate of
+// world point p
+V3 fieldCoord(const float *origin, const float *spacing, const int *dims, V3 p)
+{
+  const V3 sp = ld3(spacing, 0);
+  const V3 inv = v3(1.f / (sp.x * (float)dims[0]), 1.f / (sp.y * (float)dims[1]),
+      1.f / (sp.z * (float)dims[2]));
+  return ((p - ld3(origin, 0)) + 0.5f * sp) * inv;
+}
+
 float sampleFieldParity(const OrcVolume &v, V3 p, int round)
 {
   if (v.nvdb) {
     Nvdb n;
     return nvdbOpen(v.nvdb, n) ? nvdbSample(n, p, 1) : 0.f;
   }
-  const V3 sp = ld3(v.spacing, 0);
-  const V3 inv = v3(1.f / (sp.x * (float)v.dims[0]), 1.f / (sp.y * (float)v.dims[1]),
-      1.f / (sp.z * (float)v.dims[2]));
-  const V3 c = ((p - ld3(v.origin, 0)) + 0.5f * sp) * inv;
+  const V3 c = fieldCoord(v.origin, v.spacing, v.dims, p);
   return v.filterLinear ? tex3dLinear(v.field, v.dims, c.x, c.y, c.z, round)
                         : tex3dPoint(v.field, v.dims, c.x, c.y, c.z);
 }
@@ -3187,6 +3196,18 @@ void orc_project_on_grid(const float *p3, int n, const int *dims3, const float *
   for (int i = 0; i < n; i++)
     for (int a = 0; a < 3; a++)
       out3[3 * i + a] = projectAxis(p3[3 * i + a], box6[a], box6[3 + a], dims3[a]);
+}
+
+// the structured field's texture coordinates (fieldCoord) of n points
+void orc_field_coords(const float *origin3, const float *spacing3, const int *dims3,
+    const float *p3, int n, float *out3)
+{
+  for (int i = 0; i < n; i++) {
+    const V3 c = fieldCoord(origin3, spacing3, dims3, ld3(p3, i));
+    out3[3 * i] = c.x;
+    out3[3 * i + 1] = c.y;
+    out3[3 * i + 2] = c.z;
+  }
 }
 
 // intersectVolume's interval (scene/Intersectors_ptx.cu:248-274) for n

@@ -26,13 +26,12 @@
  * (gpu/uniformGrid.h), its macrocell walk (gpu/dda.h, compiled with
  * contraction on, as nvcc builds it), its primary-ray generation
  * (gpu/cameraCreateRay.h, compiled without contraction, as the oracle and
- * the library's kernels round it), its image staging
- * (utility/CudaImageTexture.cpp) and its frame colour write's glm calls,
- * compiled in place (oracle/ref_tf.cpp, oracle/ref_dda.cpp,
- * oracle/ref_camera.cpp, oracle/ref_image.cpp, oracle/ref_glm.cpp), made
- * the fixtures tests/golden/tf_golden.npz, math_golden.npz,
- * dda_golden.npz, camera_golden.npz, image_golden.npz and
- * color_golden.npz, which the functions here reproduce bit for bit.
+ * the library's kernels round it), its structured-field sampler
+ * (gpu/sampleSpatialField.h), its image staging
+ * (utility/CudaImageTexture.cpp), and the glm calls of its frame colour
+ * write and volume entry, compiled in place (oracle/ref_*.cpp), made the
+ * fixtures tests/golden/*_golden.npz, which the functions here reproduce
+ * bit for bit.
  */
 #ifndef VRTX_ORACLE_H
 #define VRTX_ORACLE_H
@@ -303,6 +302,12 @@ int orc_stage_image(int et, const void *texels, uint64_t n, float *outFloat, uin
  * 260 ufixed8 x4, 261 sRGB ufixed8 x4) to out (n x 4 RGBA8); -1 for another
  * type. */
 int orc_stage_background(int et, const void *texels, uint64_t n, uint8_t *out);
+/* The structured-regular field's texture coordinates
+ * (sampleSpatialField.h:54-78, invSpacing as StructuredRegularField.cpp:
+ * 188-189) of n world points p3 for a field of origin3, spacing3 over dims3
+ * voxels -> out3 (n x 3). */
+void orc_field_coords(const float *origin3, const float *spacing3, const int *dims3,
+    const float *p3, int n, float *out3);
 /* intersectVolume's slab interval (Intersectors_ptx.cu:248-274), the
  * volume's entry, for n local rays (org xyz, dir xyz, tmin, tmax) against
  * box6 (lo xyz, hi xyz): hit[i] 1 or 0, t01[2i..2i+1] the clamped interval

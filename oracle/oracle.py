@@ -254,6 +254,19 @@ def primary_rays(cam, cam_type, samples, inv_w, inv_h, center_pixel=False):
     return out
 
 
+def field_coords(origin, spacing, dims, points):
+    """(n, 3) world points -> (n, 3) texture coordinates of a
+    structured-regular field (origin, spacing, dims)."""
+    lib = load()
+    o = np.ascontiguousarray(origin, np.float32).reshape(3)
+    s = np.ascontiguousarray(spacing, np.float32).reshape(3)
+    d = np.ascontiguousarray(dims, np.int32).reshape(3)
+    p = np.ascontiguousarray(points, np.float32).reshape(-1, 3)
+    out = np.zeros((len(p), 3), np.float32)
+    lib.orc_field_coords(_ptr(o), _ptr(s), _ptr(d), _ptr(p), C.c_int(len(p)), _ptr(out))
+    return out
+
+
 def volume_interval(rays, box):
     """(n, 8) local rays (org, dir, tmin, tmax) against a volume's bounds
     (lo, hi) -> (hit (n,), t01 (n, 2)): the volume's entry interval."""

@@ -280,6 +280,26 @@ def test_primary_rays_match_reference_camera():
     assert (n, fused_differ) == (3960, 2393)
 
 
+def test_structured_field_coordinates_match_reference_sampler():
+    """The oracle reads a structured-regular field's texture at the
+    coordinate the reference's own SpatialFieldSampler computes
+    (gpu/sampleSpatialField.h:54-78, compiled on the host with a tex3D that
+    records its coordinate; fixtures by tests/golden/make_field_golden.py),
+    bit for bit: 2424 points on voxel centres, voxel boundaries, the bounds
+    and outside them, over six fields (unit and non-unit spacing, off-grid
+    and negative origins, one voxel, elongated grids, the 512^3 bench
+    layout). The texture unit's filtering at that coordinate is pinned by
+    the GPU sweeps above."""
+    z = np.load(os.path.join(GOLDEN, "field_golden.npz"))
+    n = 0
+    for i in range(int(z["num_fields"])):
+        got = O.field_coords(z[f"f{i}_origin"], z[f"f{i}_spacing"], z[f"f{i}_dims"],
+                             z[f"f{i}_points"])
+        assert np.array_equal(got.view(np.uint32), z[f"f{i}_coords"].view(np.uint32)), i
+        n += len(got)
+    assert n == 2424
+
+
 def test_volume_entry_interval_matches_reference_intersect_volume():
     """The oracle's volume entry interval equals, bit for bit, the
     reference's intersectVolume (scene/Intersectors_ptx.cu:248-274), its glm
