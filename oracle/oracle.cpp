@@ -3146,6 +3146,23 @@ void orc_tex_float4(const float *texels, int ndim, const int dims[3], int filter
   out[3] = r.w;
 }
 
+void orc_tex_unorm8(const uint8_t *texels, int ndim, const int dims[3], int filter,
+    const int wrap[3], const float coord[3], float out[4])
+{
+  OrcSampler sm{};
+  sm.image8 = texels;
+  for (int k = 0; k < 3; k++) {
+    sm.dims[k] = k < ndim ? dims[k] : 1;
+    sm.wrap[k] = k < ndim ? wrap[k] : 0;
+  }
+  sm.filter = filter;
+  const V4 r = texSample(sm, ndim, coord);
+  out[0] = r.x;
+  out[1] = r.y;
+  out[2] = r.z;
+  out[3] = r.w;
+}
+
 void orc_tex_rgba8(const uint8_t *texels, int w, int h, const float coord[2], float out[4])
 {
   OrcRenderer R{};

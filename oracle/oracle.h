@@ -75,6 +75,11 @@ float orc_tex3d(const float *vox, const int dims[3], const float coord[3], int m
 void orc_tex_float4(const float *texels, int ndim, const int dims[3], int filter,
     const int wrap[3], const float coord[3], float out[4]);
 void orc_tex_rgba8(const uint8_t *texels, int w, int h, const float coord[2], float out[4]);
+/* The same fetch as orc_tex_float4 from RGBA8 texels read as normalised
+ * float (8-bit image samplers): point b / 255, linear the texture unit's
+ * integer filter scaled to 16 bits. */
+void orc_tex_unorm8(const uint8_t *texels, int ndim, const int dims[3], int filter,
+    const int wrap[3], const float coord[3], float out[4]);
 
 /* --- NanoVDB fields ------------------------------------------------------ */
 

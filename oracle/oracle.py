@@ -671,6 +671,21 @@ def tex_float4(texels: np.ndarray, dims, filter_: int, wrap, coord) -> np.ndarra
     return out
 
 
+def tex_unorm8(texels: np.ndarray, dims, filter_: int, wrap, coord) -> np.ndarray:
+    """tex_float4's fetch from RGBA8 texels (..., 4) read as normalised float,
+    as an 8-bit image sampler's texture is read."""
+    lib = load()
+    t = np.ascontiguousarray(texels, np.uint8)
+    nd = len(dims)
+    d = np.array(list(dims) + [1] * (3 - nd), np.int32)
+    w = np.array(list(wrap) + [0] * (3 - nd), np.int32)
+    c = np.array(list(coord) + [0.0] * (3 - nd), np.float32)
+    out = np.zeros(4, np.float32)
+    lib.orc_tex_unorm8(_ptr(t), C.c_int(nd), _ptr(d), C.c_int(filter_), _ptr(w), _ptr(c),
+                       _ptr(out))
+    return out
+
+
 def tex_rgba8(texels: np.ndarray, width: int, height: int, coord) -> np.ndarray:
     """Linear, clamped, normalised-float fetch of an RGBA8 image (the
     background image's texture)."""

@@ -101,8 +101,9 @@ def test_texture_sweep_golden():
     on texel boundaries), 1D/2D/3D float4 tables with clamp, repeat and
     mirror addressing, the HDRI map's repeat-x / clamp-y, and the RGBA8
     background image read as normalised float. Normalised-integer field
-    formats are checked in nearest mode (their linear filter runs at 16-bit
-    precision, which the oracle does not restate)."""
+    formats are checked in nearest mode here; the 8-bit ones' linear filter
+    is checked by test_texture_sweep_unorm8_sampler_path, and the 16-bit and
+    signed ones' linear filter is not restated."""
     checked = 0
     for rec in _sweep_records():
         dim, nx, ny, nz, ch, fmt, flt, a0, a1, a2, k, tag = (int(v) for v in rec["hdr"][:12])
@@ -128,6 +129,35 @@ def test_texture_sweep_golden():
         assert np.array_equal(got, want), (rec["hdr"][:12], int((got != want).any(1).sum()))
         checked += 1
     assert checked >= 50
+
+
+def test_texture_sweep_unorm8_sampler_path():
+    """The oracle's fetch of 8-bit texels read as normalised float (the path
+    every non-float image sampler now takes, as the reference stages it)
+    gives the GB300 texture unit's values bit for bit on every 8-bit record
+    of the GPU sweep: a 3D single-channel field with linear and nearest
+    filtering (the integer filter scaled to 16 bits, corner weights split
+    z, x, y as for float texels) and the RGBA8 2D image."""
+    checked = 0
+    for rec in _sweep_records():
+        dim, nx, ny, nz, ch, fmt, flt, a0, a1, a2, k, tag = (int(v) for v in rec["hdr"][:12])
+        if fmt != 1:
+            continue
+        tex = rec["tex"]
+        if ch == 1:
+            t4 = np.zeros((tex.size, 4), np.uint8)
+            t4[:, 0] = tex.ravel()
+            t4[:, 3] = 255
+        else:
+            t4 = tex.reshape(-1, 4)
+        dims = [nx, ny, nz][:dim]
+        wrap = [_ADDR[a] for a in (a0, a1, a2)][:dim]
+        want = rec["vals"]
+        got = np.array([O.tex_unorm8(t4, dims, flt, wrap, c)[:want.shape[1]]
+                        for c in rec["coords"]], np.float32)
+        assert np.array_equal(got, want), rec["hdr"][:12]
+        checked += 1
+    assert checked == 3
 
 
 def test_tf_two_knot_ramp():
