@@ -3163,6 +3163,34 @@ void orc_tex_unorm8(const uint8_t *texels, int ndim, const int dims[3], int filt
   out[3] = r.w;
 }
 
+// The texture unit's linear (or point) read of a single-channel 16-bit
+// normalised texture (UFIXED16 scale 65535, FIXED16 scale 32767): the
+// integer texels weighted as hwCornerWeights splits them (sum 256), the sum
+// F rounded half up to F / 256 and read as that / scale. (The 8-bit rule,
+// unorm8Linear, is this rule on the bytes widened to 16 bits as b * 257.)
+float orc_tex_norm16(const int32_t *texels, int ndim, const int dims[3], int filter,
+    const int wrap[3], const float coord[3], int scale)
+{
+  int d[3], i0[3] = {0, 0, 0}, i1[3] = {0, 0, 0}, w[3] = {0, 0, 0};
+  for (int k = 0; k < 3; k++)
+    d[k] = k < ndim ? dims[k] : 1;
+  for (int k = 0; k < ndim; k++)
+    hwTap(coord[k], d[k], wrap[k], filter != 0, i0[k], i1[k], w[k]);
+  auto at = [&](int x, int y, int z) {
+    return (int64_t)texels[((size_t)z * d[1] + y) * d[0] + x];
+  };
+  if (filter == 0)
+    return (float)((double)at(i0[0], i0[1], i0[2]) / scale);
+  int cw[8];
+  hwCornerWeights(ndim, w, cw);
+  int64_t F = 0;
+  for (int q = 0; q < 8; q++)
+    if (cw[q])
+      F += cw[q] * at((q & 1) ? i1[0] : i0[0], (q & 2) ? i1[1] : i0[1], (q & 4) ? i1[2] : i0[2]);
+  const int64_t r = (F + 128) >> 8; // floor(F / 256 + 1/2), negative F too
+  return (float)((double)r / scale);
+}
+
 void orc_tex_rgba8(const uint8_t *texels, int w, int h, const float coord[2], float out[4])
 {
   OrcRenderer R{};

@@ -80,6 +80,11 @@ void orc_tex_rgba8(const uint8_t *texels, int w, int h, const float coord[2], fl
  * integer filter scaled to 16 bits. */
 void orc_tex_unorm8(const uint8_t *texels, int ndim, const int dims[3], int filter,
     const int wrap[3], const float coord[3], float out[4]);
+/* The read of a single-channel 16-bit normalised texture (texels as
+ * integers; scale 65535 for UFIXED16, 32767 for FIXED16): linear filtering
+ * rounds the integer weighted sum once, F / 256 half up. */
+float orc_tex_norm16(const int32_t *texels, int ndim, const int dims[3], int filter,
+    const int wrap[3], const float coord[3], int scale);
 
 /* --- NanoVDB fields ------------------------------------------------------ */
 

@@ -686,6 +686,20 @@ def tex_unorm8(texels: np.ndarray, dims, filter_: int, wrap, coord) -> np.ndarra
     return out
 
 
+def tex_norm16(texels: np.ndarray, dims, filter_: int, wrap, coord, scale: int) -> float:
+    """Read of a single-channel 16-bit normalised texture (integer texels, x
+    fastest; scale 65535 unsigned / 32767 signed)."""
+    lib = load()
+    t = np.ascontiguousarray(texels, np.int32)
+    nd = len(dims)
+    d = np.array(list(dims) + [1] * (3 - nd), np.int32)
+    w = np.array(list(wrap) + [0] * (3 - nd), np.int32)
+    c = np.array(list(coord) + [0.0] * (3 - nd), np.float32)
+    lib.orc_tex_norm16.restype = C.c_float
+    return float(lib.orc_tex_norm16(_ptr(t), C.c_int(nd), _ptr(d), C.c_int(filter_), _ptr(w),
+                                    _ptr(c), C.c_int(scale)))
+
+
 def tex_rgba8(texels: np.ndarray, width: int, height: int, coord) -> np.ndarray:
     """Linear, clamped, normalised-float fetch of an RGBA8 image (the
     background image's texture)."""
