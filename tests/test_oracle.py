@@ -303,6 +303,21 @@ def test_image_staging_matches_reference():
     assert srgb[3][192, 3] == 128 and srgb[4][192, 3] == 55
 
 
+def test_reference_harness_build_leaves_no_links():
+    """The harnesses that compile the reference's own code (oracle/build.py
+    build_ref) link its headers only for the compile: oracle/_ref keeps the
+    built libraries and no link into the reference tree, which does not
+    exist where the built files are copied."""
+    from oracle import build as B
+
+    if B.build_ref() is None:
+        pytest.skip("no reference tree here")
+    for dirpath, dirnames, filenames in os.walk(B.REF_OUT):
+        for name in dirnames + filenames:
+            assert not os.path.islink(os.path.join(dirpath, name)), name
+    assert not os.path.exists(os.path.join(B.REF_OUT, "gpu_inc"))
+
+
 def test_primary_rays_match_reference_camera():
     """The oracle's primary ray (makePrimaryRay + cameraCreateRay: the pixel
     and sub-pixel offset to a screen position, the image region, the
